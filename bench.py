@@ -1,0 +1,336 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 path on the pressure-Poisson workload.
+
+Workload (one "step"): the SIMPLE pressure solve of freeCappuccino on a
+128^3 hex mesh of the unit cube (2,097,152 cells) whose interior vertices are
+perturbed by U(-0.15h, 0.15h) (seed 42): the implicit Laplacian of
+laplacian.f90 with Gamma = 1, Dirichlet on the x=0 patch and Neumann
+elsewhere, a N(0,1) right-hand side with its mean removed (seed 43), solved
+by the reference's ICCG (DIC-preconditioned CG, linear_solvers.f90:364) from
+a zero start to the reference's relative L1 criterion 1e-10.
+
+value  : p-solves/s with matrix, RHS and solution resident in HBM (the whole
+         solve, incl. the DIC setup, is one persistent kernel).
+e2e    : the same through the C ABI call fc_csrsolve (the csrsolve drop-in)
+         with HOST buffers: a, rhs and fi copied in and fi copied out per step.
+mixed  : the FP32-inner / FP64-refinement solve to the same FP64 criterion.
+
+`--impl reference` times the reference algorithm on the host cores (the C++
+restatement of linear_solvers.f90, single thread like the serial reference).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "freecappuccino-dev_gb300")
+METRIC = "SIMPLE iters/s & p-solve time to 1e-8 resid, mixed vs FP64 GPU; HBM GB/s"
+PERTURB, MESH_SEED, RHS_SEED = 0.15, 42, 43
+TOL_REL, ITR_MAX = 1e-10, 20000
+
+
+def load_fc():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("fcgpu", os.path.join(PKG, "fcgpu.py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["fcgpu"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def rhs(n):
+    b = np.random.default_rng(RHS_SEED).standard_normal(n)
+    return b - b.mean()
+
+
+def iccg_bytes_per_iteration(n, nnz):
+    """Algorithmic HBM bytes of one FP64 ICCG iteration, each array counted
+    once per pass (int32 indices, perfect reuse of gathered vectors):
+      SpMV z = A p          12*nnz + 4*(n+1) + 8n (p) + 8n (z)
+      DIC forward+backward  12*(nnz-n) + 2*4*(n+1) + 4n (diag) + 8n*4 (r, d, z write, z read)
+                            + 8n*3 (backward: d, z read, z write)
+      p = z + beta p        8n*3
+      x += a p, r -= a z    8n*6
+    """
+    spmv = 12 * nnz + 4 * (n + 1) + 16 * n
+    sweeps = 12 * (nnz - n) + 8 * (n + 1) + 4 * n + 32 * n + 24 * n
+    vec = 24 * n + 48 * n
+    return spmv + sweeps + vec
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.samples = []
+        self.stop = threading.Event()
+        self.t = threading.Thread(target=self.run, daemon=True)
+
+    def run(self):
+        while not self.stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([v.strip() for v in out.split(",")])
+            except Exception:
+                pass
+            self.stop.wait(0.2)
+
+    def __enter__(self):
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if len(s) > 5 + k and
+                          s[5 + k].strip().lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per ICCG launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "iccg_fp64_poisson.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch_128:"):
+            try:
+                return float(line.split(":")[1])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(ia, ja, a, diag, b, iters_per_solve, sample_iters):
+    """The oracle's ICCG (fast build, one core) on the same matrix, bounded
+    sample of sample_iters iterations; p-solves/s scaled to a full solve."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    n = len(diag)
+    t0 = time.perf_counter()
+    x, r0, info, st = oracle_lib.solve("iccg", ia, ja, a, diag, np.zeros(n), b, sample_iters, 0.0, 1e-30, fast=True)
+    dt = time.perf_counter() - t0
+    done = max(1, int(info[0]))
+    per_iter = dt / done
+    solve_s = per_iter * iters_per_solve
+    return {"value": 1.0 / solve_s, "unit": "p-solves/s", "cores": 1, "kind": "port",
+            "sample": f"{done} ICCG iterations (incl. DIC setup and residual) of the same 128^3 system "
+                      f"in {dt:.1f} s, scaled to the {iters_per_solve} iterations of a full solve"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    fc = load_fc()
+    n = args.n
+    m = fc.Mesh.box(n, n, n, 1.0, 1.0, 1.0, perturb=PERTURB, seed=MESH_SEED)
+    oc = oracle_lib.Case(m.arrays(), fast=True)
+    b = rhs(m.numCells)
+    oc.set("su", b)
+    oc.laplacian(np.ones(m.numCells), np.zeros(m.numTotal), 0b1)
+    ia, ja, a, dg = oc.get_int("ia"), oc.get_int("ja"), oc.get("a"), oc.get_int("diag")
+    # iterations of a full solve, from a short FP64 run's convergence rate is
+    # not known in advance: estimate from the problem size of previous runs
+    iters = args.ref_iters
+    per = []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        x, r0, info, st = oracle_lib.solve("iccg", ia, ja, a, dg, np.zeros(m.numCells), b, args.ref_sample, 0.0,
+                                           1e-30, fast=True)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            per.append(dt / max(1, int(info[0])))
+    per_iter = float(np.mean(per))
+    value = 1.0 / (per_iter * iters)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "p-solves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_iter * iters * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{n}^3 perturbed-hex pressure Poisson, ICCG (DIC) FP64 to 1e-10 rel. L1",
+                       "cells": m.numCells, "nnz": len(ja), "iterations_per_solve": iters},
+            "cpu_baseline": {"value": value, "unit": "p-solves/s", "cores": 1, "kind": "port",
+                             "sample": f"each step: {args.ref_sample} ICCG iterations of the {n}^3 system "
+                                       f"(C++ restatement of linear_solvers.f90, -O3, one thread), scaled to "
+                                       f"{iters} iterations per solve"},
+            "e2e": {"value": value, "unit": "p-solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank, world, dist):
+    fc = load_fc()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    n = args.n
+    mesh = fc.Mesh.box(n, n, n, 1.0, 1.0, 1.0, perturb=PERTURB, seed=MESH_SEED)
+    ctx = fc.Context(dev)
+    ctx.set_mesh(mesh)
+    nC = mesh.numCells
+    b = rhs(nC)
+    ctx.field_set("su", b)
+    ctx.laplacian(np.ones(nC), np.zeros(mesh.numTotal), 0b1)
+    nnz = 2 * mesh.numInnerFaces + nC
+
+    def step():
+        ctx.field_fill("pp", 0.0)
+        r0, info, st = ctx.solve_field("iccg", "pp", "su", ITR_MAX, 0.0, TOL_REL)
+        if st != 0:
+            raise RuntimeError(f"ICCG status {st}")
+        return info
+
+    for _ in range(args.warmup):
+        info = step()
+    iters = info.itr_used
+    if dist:
+        dist.barrier()
+    ctx.sync()
+    launches0 = ctx.kernel_launches()
+    solve_ms = []
+    with ClockSampler(dev) as clk:
+        ctx.event(0)
+        for _ in range(args.steps):
+            info = step()
+            solve_ms.append(info.ms)
+        ctx.event(1)
+        elapsed = ctx.elapsed_ms()
+    launches = ctx.kernel_launches() - launches0
+    if dist:
+        import torch
+        t = torch.tensor([elapsed], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t[0])
+    ms_per_step = elapsed / args.steps
+    value = world * args.steps / (elapsed / 1e3)
+
+    # end to end through the csrsolve drop-in with host buffers
+    ia, ja, dg, _, _ = ctx.csr_pattern()
+    a_host = ctx.field_get("a")
+    pin = None
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pin = lambda arr: torch.from_numpy(arr).pin_memory().numpy()  # noqa: E731
+    except Exception:
+        pin = None
+    a_h = pin(a_host) if pin else a_host
+    b_h = pin(b.copy()) if pin else b.copy()
+    x_h = pin(np.zeros(nC)) if pin else np.zeros(nC)
+    for _ in range(max(1, args.warmup)):
+        x_h[:] = 0.0
+        ctx.csrsolve_sized("iccg", nC, nnz, ia, ja, a_h, dg, x_h, b_h, ITR_MAX, 0.0, TOL_REL, "p")
+    ctx.sync()
+    ctx.event(0)
+    for _ in range(args.steps):
+        x_h[:] = 0.0
+        ctx.csrsolve_sized("iccg", nC, nnz, ia, ja, a_h, dg, x_h, b_h, ITR_MAX, 0.0, TOL_REL, "p")
+    ctx.event(1)
+    e2e_ms = ctx.elapsed_ms() / args.steps
+    h2d = a_h.nbytes + b_h.nbytes + x_h.nbytes
+    d2h = x_h.nbytes
+
+    # mixed precision (FP32 inner, FP64 refinement) to the same criterion
+    ctx.set_precision(fc.FC_PREC_MIXED, 1e-4, 0)
+    for _ in range(max(1, args.warmup)):
+        minfo = step()
+    ctx.sync()
+    ctx.event(0)
+    for _ in range(args.steps):
+        minfo = step()
+    ctx.event(1)
+    mixed_ms = ctx.elapsed_ms() / args.steps
+    ctx.set_precision(fc.FC_PREC_FP64)
+    x_mixed = ctx.field_get("pp")[:nC].copy()
+    step()
+    x_fp64 = ctx.field_get("pp")[:nC].copy()
+    mixed_err = float(np.abs(x_mixed - x_fp64).max() / np.abs(x_fp64).max())
+
+    peak, peak_kind = measured_peak()
+    bytes_launch = iccg_bytes_per_iteration(nC, nnz) * iters
+    avg_launch_ms = float(np.mean(solve_ms))
+    achieved = bytes_launch / (avg_launch_ms * 1e-3) / 1e9
+    traffic = profiled_traffic()
+    if rank != 0:
+        ctx.close()
+        return
+    line = {"metric": METRIC, "value": value, "unit": "p-solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{n}^3 perturbed-hex pressure Poisson, ICCG (DIC) FP64 to 1e-10 rel. L1",
+                       "cells": nC, "nnz": nnz, "iterations_per_solve": iters,
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (matrix + vectors ~0.3 GB)"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_iccg<double> (whole solve, one persistent launch)",
+                         "peak_source": peak_kind},
+            "e2e": {"value": 1e3 / e2e_ms, "unit": "p-solves/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+            "mixed": {"value": 1e3 / mixed_ms, "unit": "p-solves/s", "ms_per_step": mixed_ms,
+                      "speedup_vs_fp64": ms_per_step / mixed_ms, "inner_iterations": minfo.itr_used,
+                      "outer_iterations": minfo.outer_iterations, "max_rel_diff_vs_fp64": mixed_err}}
+    ctx.close()
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(ia, ja, a_host, dg, b, iters, args.ref_sample)
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=128, help="cells per side of the cube")
+    ap.add_argument("--ref-sample", type=int, default=40, help="ICCG iterations per CPU sample")
+    ap.add_argument("--ref-iters", type=int, default=0, help="iterations of a full solve for the reference arm")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        if not args.ref_iters:
+            args.ref_iters = {128: 560}.get(args.n, int(4.4 * args.n))
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world, dist)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

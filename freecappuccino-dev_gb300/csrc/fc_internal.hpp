@@ -1,0 +1,157 @@
+// Internal declarations of the GB300 library: device buffers, the context,
+// the CSR system (pattern analysis + solver workspace) and the mesh on device.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "fc_gpu.h"
+
+// Single-precision literals of the reference, promoted to double
+// (parameters.f90:6 small = 1e-20, linear_solvers.f90:447 s0 = 1.e20).
+constexpr double FC_SMALL = static_cast<double>(1e-20f);
+constexpr double FC_S0 = static_cast<double>(1.e20f);
+
+#define FC_CUDA_TRY(ctx, expr)                                                  \
+  do {                                                                          \
+    cudaError_t _e = (expr);                                                    \
+    if (_e != cudaSuccess) return fc_fail((ctx), FC_ERR_CUDA, #expr, _e);       \
+  } while (0)
+
+template <class T>
+struct DVec {
+  T* p = nullptr;
+  size_t n = 0;
+  DVec() = default;
+  DVec(const DVec&) = delete;
+  DVec& operator=(const DVec&) = delete;
+  ~DVec() { release(); }
+  cudaError_t alloc(size_t count) {
+    if (count == n && p) return cudaSuccess;
+    release();
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count; else p = nullptr;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+// Cross-block control block of the persistent solver kernels: a bounded
+// generation barrier, per-block partial sums and a sticky status word.
+struct GridCtl {
+  unsigned* bar;     // [0] arrival count, [1] generation
+  double* part;      // nblocks * FC_NPART partial sums
+  int* status;       // 0 or a negative FC_* code (first error sticks)
+  double* out;       // scalar results written by block 0 (FC_OUT_*)
+};
+#define FC_NPART 4
+enum { FC_OUT_RES0 = 0, FC_OUT_RESL, FC_OUT_FACTOR, FC_OUT_RESOR, FC_OUT_ITR, FC_OUT_EARLY, FC_OUT_BAD, FC_OUT_N = 16 };
+
+struct LevelSchedule {
+  int nlev = 0;
+  int max_width = 0;
+  std::vector<int> h_ptr, h_rows;
+  DVec<int> ptr, rows;
+};
+
+// A square CSR system on the device plus everything the solvers need.
+struct CsrSystem {
+  int n = 0, nnz = 0;
+  DVec<int> ia, ja, diag, tslot;     // 0-based; tslot = transpose slot (DILU search)
+  bool tslot_oob = false;            // some DILU search ran past its row (non-symmetric pattern)
+  DVec<double> a;
+  DVec<float> a32;
+  LevelSchedule lf, lb;              // forward (lower) and backward (upper) level sets
+  // workspace
+  DVec<double> x, b, r, r0, p, u, z, v, d, w;
+  DVec<float> fr, fr0, fp, fu, fz, fv, fd, fx;
+  DVec<double> part, out;
+  DVec<unsigned> bar;
+  DVec<int> status;
+  double* h_out = nullptr;           // pinned FC_OUT_N doubles
+  int* h_status = nullptr;
+  // identity of an externally supplied pattern (fc_csrsolve cache)
+  const void* key_ia = nullptr; const void* key_ja = nullptr; const void* key_diag = nullptr;
+  std::vector<int> h_ia, h_ja, h_diag;  // 0-based host copies
+  DVec<int> tptr, tsrc, trow;        // transpose (column-major) view, built on demand
+  ~CsrSystem();
+};
+
+// Mesh topology and geometry resident on the device (SoA, 0-based).
+struct MeshDev {
+  int numNodes = 0, numCells = 0, numInnerFaces = 0, numBoundaryFaces = 0, numFaces = 0, numTotal = 0;
+  int numBoundaries = 0, nwal = 0, nsym = 0;
+  std::vector<int> h_bctype, h_nfaces, h_startFace;  // per patch; startFace 0-based face offset
+  DVec<double> x, y, z;
+  DVec<int> nnodes, nodes;                 // nodes: numFaces*FC_NOMAX, 0-based node ids
+  DVec<int> owner, neighbour;              // 0-based cells
+  DVec<int> bface_patch;                   // patch index of every boundary face
+  DVec<int> bface_wall;                    // running wall-face counter (iWall-1) or -1
+  DVec<int> cf_ptr, cf_face;               // cell -> faces (ascending face index)
+  DVec<double> arx, ary, arz, xf, yf, zf;  // numFaces
+  DVec<double> xc, yc, zc, vol;            // numCells
+  DVec<double> facint, Df;                 // numInnerFaces
+  DVec<int> ijk, jik;                      // face -> CSR slot (0-based)
+  std::vector<int> h_owner, h_neighbour;
+};
+
+struct FieldStore;
+
+struct fc_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string last_error;
+  int verbosity = 0;   // 1: print the reference's solver report lines
+  int precision = 0;   // FC_PREC_*
+  int inner_itmax = 0; double inner_tol = 0.0;
+  MeshDev mesh;
+  bool has_mesh = false;
+  CsrSystem* sys_ext = nullptr;    // pattern cache of fc_csrsolve
+  CsrSystem* sys_mesh = nullptr;   // global matrix of the mesh (sparse_matrix module)
+  std::vector<CsrSystem*> sys_user;
+  FieldStore* fields = nullptr;
+  long long kernel_launches = 0;
+};
+
+int fc_fail(fc_ctx* ctx, int code, const char* what, cudaError_t e = cudaSuccess);
+int fc_fail_msg(fc_ctx* ctx, int code, const std::string& msg);
+
+// pattern analysis (host) + upload
+int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, const int* ja1, const int* diag1);
+int sys_upload_values(fc_ctx* ctx, CsrSystem* s, const double* a, bool a_on_device);
+int sys_alloc_work(fc_ctx* ctx, CsrSystem* s);
+
+struct SolveResult {
+  int status = 0;
+  int itr_used = 0;
+  double res0 = 0, resl = 0, factor = 0, resor = 0;
+  int early = 0;
+  double ms = 0;
+  int outer = 0;
+};
+
+// solve on a system; a (nnz values, NULL = s->a), x and b are device
+// vectors (x in/out).  solver: gauss-seidel|dpcg|iccg|bicgstab|pmgmres
+int sys_solve(fc_ctx* ctx, CsrSystem* s, const char* solver, const double* a, double* x, const double* b,
+              int itr_max, double tol_abs, double tol_rel, SolveResult* res);
+int sys_precond(fc_ctx* ctx, CsrSystem* s, int dilu, const double* q, double* z_out, double* d_out, int apply);
+
+bool is_device_ptr(const void* p);
+
+// cross-file helpers (C++ linkage)
+int solve_global(fc_ctx* ctx, const char* solver, double* x, const double* b, double* res0, int itr_max,
+                 double tol_abs, double tol_rel, const char* chvar, fc_solve_info* info);
+void launch_soa_to_aos(cudaStream_t st, const double* s, double* a, int n);
+int fc_fields_alloc(fc_ctx* ctx);
+int gmres_solve(fc_ctx* ctx, CsrSystem* s, const double* a, double* x, const double* b, int itr_max, int mr,
+                double tol_abs, double tol_rel, SolveResult* res);

@@ -1,0 +1,328 @@
+// Mesh on the device: topology upload, geometry (read_mesh_native's geometry
+// part, src/mesh/geometry.f90:416-665) computed by face- and cell-parallel
+// kernels, and the CSR pattern with its face -> slot maps (create_CSR_matrix,
+// src/sparseMatrix/sparse_matrix.f90:86-296).
+//
+// Deterministic by construction: every cell accumulates its faces in
+// ascending face index (the order of the reference's face loops) through a
+// cell -> face list, so no atomics are used and the sums are those of the
+// reference.  The geometry uses non-contracted FP64 arithmetic and matches
+// the reference bit for bit.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fc_internal.hpp"
+#include "fc_mesh.hpp"
+
+namespace {
+
+#define DM __dmul_rn
+#define DA __dadd_rn
+#define DS __dsub_rn
+#define DD __ddiv_rn
+
+// face area vector (triangle fan from node 1) and area-weighted centroid,
+// geometry.f90:430-466 and :517-519
+__global__ void k_face_geom(int nF, const int* __restrict__ nnodes, const int* __restrict__ nodes,
+                            const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z,
+                            double* arx, double* ary, double* arz, double* xf, double* yf, double* zf) {
+  const double third = 1.0 / 3.0;
+  for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nF; f += gridDim.x * blockDim.x) {
+    const int* nd = nodes + (size_t)f * FC_NOMAX;
+    const int nn = nnodes[f];
+    const double x1 = x[nd[0]], y1 = y[nd[0]], z1 = z[nd[0]];
+    double ax = 0, ay = 0, az = 0, sx = 0, sy = 0, sz = 0, areasum = 0;
+    for (int i = 0; i < nn - 2; ++i) {
+      const double x2 = x[nd[i + 1]], y2 = y[nd[i + 1]], z2 = z[nd[i + 1]];
+      const double x3 = x[nd[i + 2]], y3 = y[nd[i + 2]], z3 = z[nd[i + 2]];
+      const double px = DS(x2, x1), py = DS(y2, y1), pz = DS(z2, z1);
+      const double qx = DS(x3, x1), qy = DS(y3, y1), qz = DS(z3, z1);
+      const double nx = DM(0.5, DS(DM(py, qz), DM(pz, qy)));
+      const double ny = DM(0.5, DS(DM(pz, qx), DM(px, qz)));
+      const double nz = DM(0.5, DS(DM(px, qy), DM(py, qx)));
+      ax = DA(ax, nx); ay = DA(ay, ny); az = DA(az, nz);
+      const double cx = DM(third, DA(DA(x3, x2), x1));
+      const double cy = DM(third, DA(DA(y3, y2), y1));
+      const double cz = DM(third, DA(DA(z3, z2), z1));
+      const double are = __dsqrt_rn(DA(DA(DM(nx, nx), DM(ny, ny)), DM(nz, nz)));
+      sx = DA(sx, DM(are, cx)); sy = DA(sy, DM(are, cy)); sz = DA(sz, DM(are, cz));
+      areasum = DA(areasum, are);
+    }
+    arx[f] = ax; ary[f] = ay; arz[f] = az;
+    xf[f] = DD(sx, areasum); yf[f] = DD(sy, areasum); zf[f] = DD(sz, areasum);
+  }
+}
+
+// cell volume and centroid (Wang 1999 divergence formulae), geometry.f90:486-559:
+// the cell's faces in ascending index, each face's triangles in order
+__global__ void k_cell_geom(int nC, int nI, const int* __restrict__ cf_ptr, const int* __restrict__ cf_face,
+                            const int* __restrict__ owner, const int* __restrict__ nnodes,
+                            const int* __restrict__ nodes, const double* __restrict__ x,
+                            const double* __restrict__ y, const double* __restrict__ z, double* xc, double* yc,
+                            double* zc, double* vol) {
+  const double third = 1.0 / 3.0;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nC; c += gridDim.x * blockDim.x) {
+    double v = 0, X = 0, Y = 0, Z = 0, den = 0;
+    for (int q = cf_ptr[c]; q < cf_ptr[c + 1]; ++q) {
+      const int f = cf_face[q];
+      const bool own = owner[f] == c;
+      const int* nd = nodes + (size_t)f * FC_NOMAX;
+      const int nn = nnodes[f];
+      const double x1 = x[nd[0]], y1 = y[nd[0]], z1 = z[nd[0]];
+      for (int i = 0; i < nn - 2; ++i) {
+        const double x2 = x[nd[i + 1]], y2 = y[nd[i + 1]], z2 = z[nd[i + 1]];
+        const double x3 = x[nd[i + 2]], y3 = y[nd[i + 2]], z3 = z[nd[i + 2]];
+        const double px = DS(x2, x1), py = DS(y2, y1), pz = DS(z2, z1);
+        const double qx = DS(x3, x1), qy = DS(y3, y1), qz = DS(z3, z1);
+        const double nx = DM(0.5, DS(DM(py, qz), DM(pz, qy)));
+        const double ny = DM(0.5, DS(DM(pz, qx), DM(px, qz)));
+        const double nz = DM(0.5, DS(DM(px, qy), DM(py, qx)));
+        const double cx = DM(third, DA(DA(x3, x2), x1));
+        const double cy = DM(third, DA(DA(y3, y2), y1));
+        const double cz = DM(third, DA(DA(z3, z2), z1));
+        double riSi = DA(DA(DM(cx, nx), DM(cy, ny)), DM(cz, nz));
+        if (!own) riSi = -riSi;
+        v = DA(v, DM(third, riSi));
+        X = DA(X, DM(DM(0.75, riSi), cx));
+        Y = DA(Y, DM(DM(0.75, riSi), cy));
+        Z = DA(Z, DM(DM(0.75, riSi), cz));
+        den = DA(den, riSi);
+      }
+    }
+    vol[c] = v;
+    xc[c] = DD(X, den); yc[c] = DD(Y, den); zc[c] = DD(Z, den);
+  }
+  (void)nI;
+}
+
+// facint (variant 2, geometry.f90:581-603) and Df (:650-665)
+__global__ void k_inner_geom(int nI, const int* __restrict__ owner, const int* __restrict__ neighbour,
+                             const double* __restrict__ arx, const double* __restrict__ ary,
+                             const double* __restrict__ arz, const double* __restrict__ xf,
+                             const double* __restrict__ yf, const double* __restrict__ zf,
+                             const double* __restrict__ xc, const double* __restrict__ yc,
+                             const double* __restrict__ zc, double* facint, double* Df) {
+  for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nI; f += gridDim.x * blockDim.x) {
+    const int p = owner[f], n = neighbour[f];
+    double xpn = DS(xf[f], xc[p]), ypn = DS(yf[f], yc[p]), zpn = DS(zf[f], zc[p]);
+    const double djp = __dsqrt_rn(DA(DA(DM(xpn, xpn), DM(ypn, ypn)), DM(zpn, zpn)));
+    xpn = DS(xf[f], xc[n]); ypn = DS(yf[f], yc[n]); zpn = DS(zf[f], zc[n]);
+    const double djn = __dsqrt_rn(DA(DA(DM(xpn, xpn), DM(ypn, ypn)), DM(zpn, zpn)));
+    facint[f] = DD(djp, DA(djp, djn));
+    xpn = DS(xc[n], xc[p]); ypn = DS(yc[n], yc[p]); zpn = DS(zc[n], zc[p]);
+    const double ax = arx[f], ay = ary[f], az = arz[f];
+    const double are = DA(DA(DM(ax, ax), DM(ay, ay)), DM(az, az));
+    Df[f] = DD(are, DA(DA(DM(ax, xpn), DM(ay, ypn)), DM(az, zpn)));
+  }
+}
+
+}  // namespace
+
+static void free_mesh_dev(MeshDev& m) {
+  DVec<double>* dv[] = {&m.x, &m.y, &m.z, &m.arx, &m.ary, &m.arz, &m.xf, &m.yf, &m.zf,
+                        &m.xc, &m.yc, &m.zc, &m.vol, &m.facint, &m.Df};
+  for (auto* v : dv) v->release();
+  DVec<int>* iv[] = {&m.nnodes, &m.nodes, &m.owner, &m.neighbour, &m.bface_patch, &m.bface_wall,
+                     &m.cf_ptr, &m.cf_face, &m.ijk, &m.jik};
+  for (auto* v : iv) v->release();
+  m.h_owner.clear(); m.h_neighbour.clear();
+}
+
+void fc_release_mesh(fc_ctx* ctx) {
+  if (!ctx) return;
+  free_mesh_dev(ctx->mesh);
+  ctx->has_mesh = false;
+}
+
+template <class T>
+static int up(fc_ctx* ctx, DVec<T>& d, const T* h, size_t n) {
+  FC_CUDA_TRY(ctx, d.alloc(n));
+  if (n) FC_CUDA_TRY(ctx, cudaMemcpy(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice));
+  return FC_OK;
+}
+
+#define UP(dst, src, cnt) do { int _s = up(ctx, dst, src, cnt); if (_s) return _s; } while (0)
+
+// Build everything the path needs from the host mesh.  Host work is the
+// one-time topology bookkeeping (cell -> face lists, CSR pattern, slot
+// maps); the geometry is computed on the device.
+extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
+  if (!ctx || !hm) return FC_ERR_BAD_INPUT;
+  std::string why;
+  if (hm->validate(&why) != FC_OK) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_set_mesh: " + why);
+  cudaSetDevice(ctx->device);
+  fc_release_mesh(ctx);
+  delete ctx->sys_mesh;
+  ctx->sys_mesh = nullptr;
+  MeshDev& m = ctx->mesh;
+  const int nN = hm->numNodes, nC = hm->numCells, nI = hm->numInnerFaces, nB = hm->numBoundaryFaces;
+  const int nF = nI + nB;
+  m.numNodes = nN; m.numCells = nC; m.numInnerFaces = nI; m.numBoundaryFaces = nB; m.numFaces = nF;
+  m.numTotal = nC + nB;
+  m.numBoundaries = (int)hm->bctype.size();
+  m.h_bctype = hm->bctype; m.h_nfaces = hm->nfaces; m.h_startFace = hm->startFace;
+  // 0-based topology
+  std::vector<int> owner(nF), neighbour(nI), nodes((size_t)nF * FC_NOMAX, 0);
+  for (int f = 0; f < nF; ++f) {
+    owner[f] = hm->owner[f] - 1;
+    for (int k = 0; k < hm->nnodes[f]; ++k) nodes[(size_t)f * FC_NOMAX + k] = hm->nodes[(size_t)f * FC_NOMAX + k] - 1;
+  }
+  for (int f = 0; f < nI; ++f) neighbour[f] = hm->neighbour[f] - 1;
+  // cell -> faces, ascending face index
+  std::vector<int> cf_ptr(nC + 1, 0), cf_face;
+  for (int f = 0; f < nF; ++f) {
+    cf_ptr[owner[f] + 1]++;
+    if (f < nI) cf_ptr[neighbour[f] + 1]++;
+  }
+  for (int c = 0; c < nC; ++c) cf_ptr[c + 1] += cf_ptr[c];
+  cf_face.resize(cf_ptr[nC]);
+  {
+    std::vector<int> pos(cf_ptr.begin(), cf_ptr.end() - 1);
+    for (int f = 0; f < nF; ++f) {  // f ascending -> lists come out sorted
+      cf_face[pos[owner[f]]++] = f;
+      if (f < nI) cf_face[pos[neighbour[f]]++] = f;
+    }
+  }
+  // boundary face -> patch, wall counter
+  std::vector<int> bpatch(nB, -1), bwall(nB, -1);
+  int iwall = 0;
+  m.nwal = m.nsym = 0;
+  for (int b = 0; b < m.numBoundaries; ++b) {
+    for (int i = 0; i < hm->nfaces[b]; ++i) {
+      int f = hm->startFace[b] + i - nI;
+      bpatch[f] = b;
+      if (hm->bctype[b] == FC_BC_WALL) bwall[f] = iwall++;
+    }
+    if (hm->bctype[b] == FC_BC_WALL) m.nwal += hm->nfaces[b];
+    if (hm->bctype[b] == FC_BC_SYMMETRY) m.nsym += hm->nfaces[b];
+  }
+  // CSR pattern: row i = sorted {i} U {cells sharing an inner face}; the
+  // reference sorts (row, col) pairs lexicographically, which gives exactly
+  // these rows (sparse_matrix.f90:110-202)
+  const int nnz = 2 * nI + nC;
+  std::vector<int> ia(nC + 1, 0), ja(nnz), diag(nC), ijk(nI), jik(nI);
+  for (int c = 0; c < nC; ++c) ia[c + 1] = 1 + (cf_ptr[c + 1] - cf_ptr[c]);
+  // boundary faces do not make matrix entries
+  for (int f = nI; f < nF; ++f) ia[owner[f] + 1]--;
+  for (int c = 0; c < nC; ++c) ia[c + 1] += ia[c];
+  if (ia[nC] != nnz) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_set_mesh: inconsistent face lists");
+  {
+    std::vector<int> cols;
+    for (int c = 0; c < nC; ++c) {
+      cols.clear();
+      cols.push_back(c);
+      for (int q = cf_ptr[c]; q < cf_ptr[c + 1]; ++q) {
+        int f = cf_face[q];
+        if (f >= nI) continue;
+        cols.push_back(owner[f] == c ? neighbour[f] : owner[f]);
+      }
+      std::sort(cols.begin(), cols.end());
+      for (size_t k = 0; k < cols.size(); ++k) {
+        ja[ia[c] + k] = cols[k];
+        if (cols[k] == c) diag[c] = ia[c] + (int)k;
+      }
+    }
+    // csr_to_k (utils.f90:96-147): first slot of row icell holding jcell
+    auto csr_to_k = [&](int icell, int jcell) {
+      for (int l = ia[icell]; l < ia[icell + 1]; ++l)
+        if (ja[l] == jcell) return l;
+      return -1;
+    };
+    for (int f = 0; f < nI; ++f) {
+      ijk[f] = csr_to_k(owner[f], neighbour[f]);
+      jik[f] = csr_to_k(neighbour[f], owner[f]);
+    }
+  }
+  m.h_owner = owner;
+  m.h_neighbour = neighbour;
+  UP(m.x, hm->x.data(), nN); UP(m.y, hm->y.data(), nN); UP(m.z, hm->z.data(), nN);
+  UP(m.nnodes, hm->nnodes.data(), nF);
+  UP(m.nodes, nodes.data(), nodes.size());
+  UP(m.owner, owner.data(), nF);
+  UP(m.neighbour, neighbour.data(), nI);
+  UP(m.cf_ptr, cf_ptr.data(), cf_ptr.size());
+  UP(m.cf_face, cf_face.data(), cf_face.size());
+  UP(m.bface_patch, bpatch.data(), nB);
+  UP(m.bface_wall, bwall.data(), nB);
+  UP(m.ijk, ijk.data(), nI);
+  UP(m.jik, jik.data(), nI);
+  DVec<double>* fv[] = {&m.arx, &m.ary, &m.arz, &m.xf, &m.yf, &m.zf};
+  for (auto* v : fv) FC_CUDA_TRY(ctx, v->alloc(nF));
+  DVec<double>* cv[] = {&m.xc, &m.yc, &m.zc, &m.vol};
+  for (auto* v : cv) FC_CUDA_TRY(ctx, v->alloc(nC));
+  FC_CUDA_TRY(ctx, m.facint.alloc(nI));
+  FC_CUDA_TRY(ctx, m.Df.alloc(nI));
+  const int TB = 256;
+  auto grid = [&](int n) { return std::max(1, std::min(65535, (n + TB - 1) / TB)); };
+  k_face_geom<<<grid(nF), TB, 0, ctx->stream>>>(nF, m.nnodes.p, m.nodes.p, m.x.p, m.y.p, m.z.p, m.arx.p, m.ary.p,
+                                                 m.arz.p, m.xf.p, m.yf.p, m.zf.p);
+  k_cell_geom<<<grid(nC), TB, 0, ctx->stream>>>(nC, nI, m.cf_ptr.p, m.cf_face.p, m.owner.p, m.nnodes.p, m.nodes.p,
+                                                 m.x.p, m.y.p, m.z.p, m.xc.p, m.yc.p, m.zc.p, m.vol.p);
+  if (nI > 0)
+    k_inner_geom<<<grid(nI), TB, 0, ctx->stream>>>(nI, m.owner.p, m.neighbour.p, m.arx.p, m.ary.p, m.arz.p, m.xf.p,
+                                                    m.yf.p, m.zf.p, m.xc.p, m.yc.p, m.zc.p, m.facint.p, m.Df.p);
+  ctx->kernel_launches += 3;
+  FC_CUDA_TRY(ctx, cudaGetLastError());
+  FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  // the global matrix system of the mesh (module globals ia, ja, a, diag)
+  CsrSystem* s = new CsrSystem();
+  std::vector<int> ia1(ia), ja1(ja), dg1(diag);
+  for (auto& v : ia1) ++v;
+  for (auto& v : ja1) ++v;
+  for (auto& v : dg1) ++v;
+  int st = sys_set_pattern(ctx, s, nC, nnz, ia1.data(), ja1.data(), dg1.data());
+  if (st) { delete s; return st; }
+  FC_CUDA_TRY(ctx, cudaMemset(s->a.p, 0, (size_t)nnz * sizeof(double)));
+  ctx->sys_mesh = s;
+  ctx->has_mesh = true;
+  return fc_fields_alloc(ctx);
+}
+
+// geometry arrays back to the host (FC_GEO_* selects; length by kind)
+extern "C" int fc_get_geometry(fc_ctx* ctx, const char* name, double* out) {
+  if (!ctx || !name || !out) return FC_ERR_BAD_INPUT;
+  if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
+  MeshDev& m = ctx->mesh;
+  std::string n(name);
+  DVec<double>* v = nullptr;
+  if (n == "arx") v = &m.arx; else if (n == "ary") v = &m.ary; else if (n == "arz") v = &m.arz;
+  else if (n == "xf") v = &m.xf; else if (n == "yf") v = &m.yf; else if (n == "zf") v = &m.zf;
+  else if (n == "xc") v = &m.xc; else if (n == "yc") v = &m.yc; else if (n == "zc") v = &m.zc;
+  else if (n == "vol") v = &m.vol; else if (n == "facint") v = &m.facint; else if (n == "Df") v = &m.Df;
+  else return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "unknown geometry array '" + n + "'");
+  FC_CUDA_TRY(ctx, cudaMemcpy(out, v->p, v->bytes(), cudaMemcpyDeviceToHost));
+  return FC_OK;
+}
+
+// CSR pattern and face -> slot maps of the mesh, 1-based as the reference
+// stores them (ia(n+1), ja(nnz), diag(n), icell_jcell_csr_index(nI),
+// jcell_icell_csr_index(nI)); any pointer may be NULL
+extern "C" int fc_get_csr_pattern(fc_ctx* ctx, int* n_out, int* nnz_out, int* ia, int* ja, int* diag, int* ijk,
+                                  int* jik) {
+  if (!ctx) return FC_ERR_BAD_INPUT;
+  if (!ctx->has_mesh || !ctx->sys_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
+  CsrSystem* s = ctx->sys_mesh;
+  if (n_out) *n_out = s->n;
+  if (nnz_out) *nnz_out = s->nnz;
+  if (ia) for (int i = 0; i <= s->n; ++i) ia[i] = s->h_ia[i] + 1;
+  if (ja) for (int k = 0; k < s->nnz; ++k) ja[k] = s->h_ja[k] + 1;
+  if (diag) for (int i = 0; i < s->n; ++i) diag[i] = s->h_diag[i] + 1;
+  const int nI = ctx->mesh.numInnerFaces;
+  if (ijk || jik) {
+    std::vector<int> t(nI);
+    if (ijk) {
+      FC_CUDA_TRY(ctx, cudaMemcpy(t.data(), ctx->mesh.ijk.p, nI * sizeof(int), cudaMemcpyDeviceToHost));
+      for (int f = 0; f < nI; ++f) ijk[f] = t[f] + 1;
+    }
+    if (jik) {
+      FC_CUDA_TRY(ctx, cudaMemcpy(t.data(), ctx->mesh.jik.p, nI * sizeof(int), cudaMemcpyDeviceToHost));
+      for (int f = 0; f < nI; ++f) jik[f] = t[f] + 1;
+    }
+  }
+  return FC_OK;
+}

@@ -1,0 +1,409 @@
+"""Python view of libfcgpu.so (the C ABI declared in include/fc_gpu.h).
+
+A thin ctypes layer used by the tests and bench.py; every call goes straight
+to the CUDA library.  There is no CPU fallback: if the library is missing or
+no GPU is present, the calls fail with an error.
+
+Array arguments may be numpy arrays (host memory, copied by the library) or
+objects exposing data_ptr() (device memory used in place, e.g. torch CUDA
+tensors), or raw integer device addresses.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfcgpu.so")
+
+FC_OK = 0
+FC_WARN_MAXITER = 1
+FC_ERR_BAD_INPUT = -1
+FC_ERR_CUDA = -2
+FC_ERR_NAN = -3
+FC_ERR_BREAKDOWN = -4
+FC_ERR_TIMEOUT = -5
+FC_ERR_STATE = -6
+FC_ERR_UNSUPPORTED = -7
+FC_ERR_ZERO_PIVOT = -8
+
+BC = {"wall": 1, "inlet": 2, "outlet": 3, "symmetry": 4, "pressure": 5, "empty": 6, "periodic": 7}
+FC_PREC_FP64 = 0
+FC_PREC_MIXED = 1
+GRAD = {"gauss": 0, "lstsq": 1, "lstsq_dm": 2}
+NOMAX = 6
+
+
+class FcError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"fc error {code}: {msg}")
+        self.code = code
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("itr_used", C.c_int), ("outer_iterations", C.c_int),
+                ("early_exit", C.c_int), ("res0_l1", C.c_double), ("resor", C.c_double),
+                ("resl", C.c_double), ("factor", C.c_double), ("ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib():
+    """Load libfcgpu.so (building it first if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("fc_build", os.path.join(HERE, "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    L = C.CDLL(LIB_PATH)
+    vp, ip, i, d, cp = C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_char_p
+    sig = {
+        "fc_mesh_box": (i, [i, i, i, d, d, d, d, C.c_ulonglong, i, vp, C.POINTER(vp)]),
+        "fc_mesh_from_arrays": (i, [i, i, i, i, vp, vp, vp, vp, vp, vp, vp, i, vp, vp, vp, C.POINTER(vp)]),
+        "fc_mesh_read_native": (i, [cp, C.POINTER(vp)]),
+        "fc_mesh_write_native": (i, [vp, cp]),
+        "fc_mesh_info": (i, [vp, vp]),
+        "fc_mesh_export": (i, [vp] + [vp] * 10),
+        "fc_mesh_free": (None, [vp]),
+        "fc_init": (i, [i, C.POINTER(vp)]),
+        "fc_finalize": (None, [vp]),
+        "fc_last_error": (cp, [vp]),
+        "fc_set_verbosity": (i, [vp, i]),
+        "fc_set_precision": (i, [vp, i, d, i]),
+        "fc_kernel_launches": (C.c_longlong, [vp]),
+        "fc_stream_sync": (i, [vp]),
+        "fc_stream": (vp, [vp]),
+        "fc_event_record": (i, [vp, i]),
+        "fc_event_elapsed_ms": (i, [vp, C.POINTER(C.c_float)]),
+        "fc_csrsolve": (i, [vp, cp, i, i, vp, vp, vp, vp, vp, vp, vp, i, d, d, cp, i, C.POINTER(SolveInfo)]),
+        "fc_csr_pattern_forget": (i, [vp]),
+        "fc_precond_setup": (i, [vp, cp, i, i, vp, vp, vp, vp, vp]),
+        "fc_precond_apply": (i, [vp, cp, i, i, vp, vp, vp, vp, vp, vp]),
+        "fc_spmv": (i, [vp, i, i, vp, vp, vp, vp, vp, vp, i]),
+        "fc_ilu0": (i, [vp, i, i, vp, vp, vp, vp, vp]),
+        "fc_set_mesh": (i, [vp, vp]),
+        "fc_get_geometry": (i, [vp, cp, vp]),
+        "fc_get_csr_pattern": (i, [vp, vp, vp, vp, vp, vp, vp, vp]),
+        "fc_field_set": (i, [vp, cp, vp, C.c_longlong]),
+        "fc_field_get": (i, [vp, cp, vp, C.c_longlong]),
+        "fc_field_fill": (i, [vp, cp, d]),
+        "fc_field_ptr": (vp, [vp, cp]),
+        "fc_grad": (i, [vp, i, vp, vp]),
+        "fc_laplacian": (i, [vp, vp, vp, C.c_ulonglong]),
+        "fc_solve_field": (i, [vp, cp, cp, cp, vp, i, d, d, cp, C.POINTER(SolveInfo)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def declared_symbols(header=None):
+    """Names of the functions declared in include/fc_gpu.h."""
+    import re
+    header = header or os.path.join(os.path.dirname(HERE), "include", "fc_gpu.h")
+    txt = open(header).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(fc_[a-z0-9_]+)\s*\(", txt)))
+
+
+def _ptr(x):
+    if x is None:
+        return None
+    if isinstance(x, np.ndarray):
+        assert x.flags.c_contiguous
+        return x.ctypes.data_as(C.c_void_p)
+    if hasattr(x, "data_ptr"):
+        return C.c_void_p(x.data_ptr())
+    if isinstance(x, int):
+        return C.c_void_p(x)
+    raise TypeError(type(x))
+
+
+def _f64(x):
+    if hasattr(x, "data_ptr") or isinstance(x, int):
+        return x
+    return np.ascontiguousarray(x, dtype=np.float64)
+
+
+def _i32(x):
+    if hasattr(x, "data_ptr") or isinstance(x, int):
+        return x
+    return np.ascontiguousarray(x, dtype=np.int32)
+
+
+class Mesh:
+    """Host mesh in the reference's native layout (1-based indices)."""
+
+    def __init__(self, handle):
+        self.h = handle
+        info = np.zeros(6, np.int32)
+        lib().fc_mesh_info(self.h, _ptr(info))
+        (self.numNodes, self.numCells, self.numInnerFaces, self.numBoundaryFaces, self.numFaces,
+         self.numBoundaries) = [int(v) for v in info]
+        self.numTotal = self.numCells + self.numBoundaryFaces
+
+    @classmethod
+    def box(cls, nx, ny, nz, lx=1.0, ly=1.0, lz=1.0, perturb=0.0, seed=42, tets=False, sides=None):
+        sides = np.array([BC[s] if isinstance(s, str) else s for s in (sides or ["wall"] * 6)], np.int32)
+        h = C.c_void_p()
+        st = lib().fc_mesh_box(nx, ny, nz, lx, ly, lz, perturb, seed, int(tets), _ptr(sides), C.byref(h))
+        if st != 0:
+            raise FcError(st, "fc_mesh_box")
+        return cls(h)
+
+    @classmethod
+    def from_arrays(cls, a):
+        h = C.c_void_p()
+        arrs = [_f64(a["x"]), _f64(a["y"]), _f64(a["z"]), _i32(a["nnodes"]), _i32(a["nodes"]), _i32(a["owner"]),
+                _i32(a["neighbour"]), _i32(a["bctype"]), _i32(a["nfaces"]), _i32(a["startFace"])]
+        st = lib().fc_mesh_from_arrays(a["numNodes"], a["numCells"], a["numInnerFaces"], a["numBoundaryFaces"],
+                                       *[_ptr(v) for v in arrs[:7]], len(a["bctype"]),
+                                       *[_ptr(v) for v in arrs[7:]], C.byref(h))
+        if st != 0:
+            raise FcError(st, "fc_mesh_from_arrays")
+        return cls(h)
+
+    @classmethod
+    def read_native(cls, d):
+        h = C.c_void_p()
+        st = lib().fc_mesh_read_native(d.encode(), C.byref(h))
+        if st != 0:
+            raise FcError(st, "fc_mesh_read_native")
+        return cls(h)
+
+    def write_native(self, d):
+        os.makedirs(d, exist_ok=True)
+        st = lib().fc_mesh_write_native(self.h, d.encode())
+        if st != 0:
+            raise FcError(st, "fc_mesh_write_native")
+
+    def arrays(self):
+        nN, nF, nI, nB = self.numNodes, self.numFaces, self.numInnerFaces, self.numBoundaries
+        out = dict(x=np.zeros(nN), y=np.zeros(nN), z=np.zeros(nN), nnodes=np.zeros(nF, np.int32),
+                   nodes=np.zeros(nF * NOMAX, np.int32), owner=np.zeros(nF, np.int32),
+                   neighbour=np.zeros(max(nI, 1), np.int32), bctype=np.zeros(nB, np.int32),
+                   nfaces=np.zeros(nB, np.int32), startFace=np.zeros(nB, np.int32))
+        lib().fc_mesh_export(self.h, *[_ptr(out[k]) for k in ("x", "y", "z", "nnodes", "nodes", "owner",
+                                                              "neighbour", "bctype", "nfaces", "startFace")])
+        out["neighbour"] = out["neighbour"][:nI]
+        out.update(numNodes=nN, numCells=self.numCells, numInnerFaces=nI, numBoundaryFaces=self.numBoundaryFaces)
+        return out
+
+    def __del__(self):
+        try:
+            lib().fc_mesh_free(self.h)
+        except Exception:
+            pass
+
+
+class Context:
+    """One GPU context (fc_ctx): a stream, the mesh, its matrix and fields."""
+
+    def __init__(self, device=0):
+        self.L = lib()
+        h = C.c_void_p()
+        st = self.L.fc_init(device, C.byref(h))
+        if st != 0:
+            raise FcError(st, "fc_init (is a GPU present?)")
+        self.h = h
+        self.mesh = None
+
+    def close(self):
+        if self.h:
+            self.L.fc_finalize(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st, what):
+        if st < 0:
+            raise FcError(st, f"{what}: {self.L.fc_last_error(self.h).decode()}")
+        return st
+
+    def error(self):
+        return self.L.fc_last_error(self.h).decode()
+
+    def set_verbosity(self, level):
+        self.L.fc_set_verbosity(self.h, level)
+
+    def set_precision(self, mode, inner_tol=0.0, inner_itmax=0):
+        self._check(self.L.fc_set_precision(self.h, mode, inner_tol, inner_itmax), "fc_set_precision")
+
+    def kernel_launches(self):
+        return int(self.L.fc_kernel_launches(self.h))
+
+    def sync(self):
+        self._check(self.L.fc_stream_sync(self.h), "sync")
+
+    def stream(self):
+        return self.L.fc_stream(self.h)
+
+    def event(self, which):
+        self._check(self.L.fc_event_record(self.h, which), "event")
+
+    def elapsed_ms(self):
+        ms = C.c_float()
+        self._check(self.L.fc_event_elapsed_ms(self.h, C.byref(ms)), "elapsed")
+        return float(ms.value)
+
+    # --------------------------------------------------------------- solvers
+    def csrsolve(self, solver, ia, ja, a, diag, fi, rhs, itr_max, tol_abs, tol_rel, chvar="x", verbose=0,
+                 raise_on_error=True):
+        """Returns (x, res0, info, status); fi is not modified when it is a numpy array."""
+        ia, ja, diag = _i32(ia), _i32(ja), _i32(diag)
+        a, rhs = _f64(a), _f64(rhs)
+        x = _f64(fi).copy() if isinstance(fi, np.ndarray) or not hasattr(fi, "data_ptr") else fi
+        n = len(ia) - 1 if isinstance(ia, np.ndarray) else None
+        nnz = len(ja) if isinstance(ja, np.ndarray) else None
+        self._keep = (ia, ja, diag)  # pattern cache is keyed by these addresses
+        r0 = np.zeros(1)
+        info = SolveInfo()
+        st = self.L.fc_csrsolve(self.h, solver.encode(), n, nnz, _ptr(ia), _ptr(ja), _ptr(a), _ptr(diag), _ptr(x),
+                                _ptr(rhs), _ptr(r0), int(itr_max), float(tol_abs), float(tol_rel), chvar.encode(),
+                                int(verbose), C.byref(info))
+        if raise_on_error:
+            self._check(st, "fc_csrsolve")
+        return x, float(r0[0]), info, st
+
+    def csrsolve_sized(self, solver, n, nnz, ia, ja, a, diag, x, rhs, itr_max, tol_abs, tol_rel, chvar="x"):
+        """Same call with explicit sizes (device arrays); x is updated in place."""
+        r0 = np.zeros(1)
+        info = SolveInfo()
+        st = self.L.fc_csrsolve(self.h, solver.encode(), n, nnz, _ptr(ia), _ptr(ja), _ptr(a), _ptr(diag), _ptr(x),
+                                _ptr(rhs), _ptr(r0), int(itr_max), float(tol_abs), float(tol_rel), chvar.encode(),
+                                0, C.byref(info))
+        self._check(st, "fc_csrsolve")
+        return float(r0[0]), info, st
+
+    def pattern_forget(self):
+        self.L.fc_csr_pattern_forget(self.h)
+
+    def precond_setup(self, kind, ia, ja, a, diag):
+        ia, ja, diag, a = _i32(ia), _i32(ja), _i32(diag), _f64(a)
+        self._keep = (ia, ja, diag)
+        d = np.zeros(len(ia) - 1)
+        self._check(self.L.fc_precond_setup(self.h, kind.encode(), len(ia) - 1, len(ja), _ptr(ia), _ptr(ja), _ptr(a),
+                                            _ptr(diag), _ptr(d)), "fc_precond_setup")
+        return d
+
+    def precond_apply(self, kind, ia, ja, a, diag, q):
+        ia, ja, diag, a, q = _i32(ia), _i32(ja), _i32(diag), _f64(a), _f64(q)
+        self._keep = (ia, ja, diag)
+        z = np.zeros(len(ia) - 1)
+        self._check(self.L.fc_precond_apply(self.h, kind.encode(), len(ia) - 1, len(ja), _ptr(ia), _ptr(ja), _ptr(a),
+                                            _ptr(diag), _ptr(q), _ptr(z)), "fc_precond_apply")
+        return z
+
+    def spmv(self, ia, ja, a, diag, x, transpose=False):
+        ia, ja, diag, a, x = _i32(ia), _i32(ja), _i32(diag), _f64(a), _f64(x)
+        self._keep = (ia, ja, diag)
+        y = np.zeros(len(ia) - 1)
+        self._check(self.L.fc_spmv(self.h, len(ia) - 1, len(ja), _ptr(ia), _ptr(ja), _ptr(a), _ptr(diag), _ptr(x),
+                                   _ptr(y), int(transpose)), "fc_spmv")
+        return y
+
+    def ilu0(self, ia, ja, a, diag):
+        ia, ja, diag, a = _i32(ia), _i32(ja), _i32(diag), _f64(a)
+        self._keep = (ia, ja, diag)
+        l = np.zeros(len(ja))
+        self._check(self.L.fc_ilu0(self.h, len(ia) - 1, len(ja), _ptr(ia), _ptr(ja), _ptr(a), _ptr(diag), _ptr(l)),
+                    "fc_ilu0")
+        return l
+
+    # ------------------------------------------------------- mesh and fields
+    def set_mesh(self, mesh):
+        self._check(self.L.fc_set_mesh(self.h, mesh.h), "fc_set_mesh")
+        self.mesh = mesh
+
+    def geometry(self, name):
+        m = self.mesh
+        n = {"arx": m.numFaces, "ary": m.numFaces, "arz": m.numFaces, "xf": m.numFaces, "yf": m.numFaces,
+             "zf": m.numFaces, "xc": m.numCells, "yc": m.numCells, "zc": m.numCells, "vol": m.numCells,
+             "facint": m.numInnerFaces, "Df": m.numInnerFaces}[name]
+        out = np.zeros(n)
+        self._check(self.L.fc_get_geometry(self.h, name.encode(), _ptr(out)), "fc_get_geometry")
+        return out
+
+    def csr_pattern(self):
+        m = self.mesh
+        nnz = 2 * m.numInnerFaces + m.numCells
+        ia = np.zeros(m.numCells + 1, np.int32)
+        ja = np.zeros(nnz, np.int32)
+        dg = np.zeros(m.numCells, np.int32)
+        ijk = np.zeros(max(1, m.numInnerFaces), np.int32)
+        jik = np.zeros(max(1, m.numInnerFaces), np.int32)
+        self._check(self.L.fc_get_csr_pattern(self.h, None, None, _ptr(ia), _ptr(ja), _ptr(dg), _ptr(ijk), _ptr(jik)),
+                    "fc_get_csr_pattern")
+        return ia, ja, dg, ijk[:m.numInnerFaces], jik[:m.numInnerFaces]
+
+    def field_len(self, name):
+        m = self.mesh
+        if name in ("u", "v", "w", "p", "pp", "vis", "den", "t"):
+            return m.numTotal
+        if name == "flmass":
+            return m.numFaces
+        if name in ("su", "sv", "sw", "spu", "spv", "sp", "apu", "apv", "apw"):
+            return m.numCells
+        if name in ("dUdxi", "dVdxi", "dWdxi", "dPdxi", "dTdxi"):
+            return 3 * m.numTotal
+        if name == "a":
+            return 2 * m.numInnerFaces + m.numCells
+        if name == "visw":
+            return self._nwal()
+        raise KeyError(name)
+
+    def _nwal(self):
+        a = self.mesh.arrays()
+        n = int(sum(nf for t, nf in zip(a["bctype"], a["nfaces"]) if t == BC["wall"]))
+        return max(n, 1)
+
+    def field_set(self, name, values):
+        v = _f64(values)
+        n = self.field_len(name)
+        if isinstance(v, np.ndarray):
+            assert v.size == n, (name, v.size, n)
+        self._check(self.L.fc_field_set(self.h, name.encode(), _ptr(v), n), f"fc_field_set({name})")
+
+    def field_get(self, name):
+        n = self.field_len(name)
+        out = np.zeros(n)
+        self._check(self.L.fc_field_get(self.h, name.encode(), _ptr(out), n), f"fc_field_get({name})")
+        return out
+
+    def field_fill(self, name, value):
+        self._check(self.L.fc_field_fill(self.h, name.encode(), float(value)), f"fc_field_fill({name})")
+
+    def field_ptr(self, name):
+        return self.L.fc_field_ptr(self.h, name.encode())
+
+    def grad(self, scheme, phi):
+        out = np.zeros(3 * self.mesh.numTotal)
+        s = GRAD[scheme] if isinstance(scheme, str) else scheme
+        self._check(self.L.fc_grad(self.h, s, _ptr(_f64(phi)), _ptr(out)), "fc_grad")
+        return out
+
+    def laplacian(self, mu, phi, mask=(1 << 64) - 1):
+        self._check(self.L.fc_laplacian(self.h, _ptr(_f64(mu)), _ptr(_f64(phi)), mask), "fc_laplacian")
+
+    def solve_field(self, solver, x_field, rhs_field, itr_max, tol_abs, tol_rel, chvar="x"):
+        r0 = np.zeros(1)
+        info = SolveInfo()
+        st = self.L.fc_solve_field(self.h, solver.encode(), x_field.encode(), rhs_field.encode(), _ptr(r0),
+                                   int(itr_max), float(tol_abs), float(tol_rel), chvar.encode(), C.byref(info))
+        self._check(st, "fc_solve_field")
+        return float(r0[0]), info, st

@@ -1,0 +1,206 @@
+/*
+ * fc_gpu.h -- C ABI of the GB300 (sm_103a) implementation of freeCappuccino's
+ * per-iteration hot path: face-based flux assembly into CSR, cell gradients and
+ * the built-in sparse Krylov solvers.
+ *
+ * Conventions shared by every entry point
+ *  - Every call returns an int status: 0 = OK, >0 = warning, <0 = error
+ *    (FC_* codes below).  No call aborts the process; the text of the last
+ *    error of a context is returned by fc_last_error().
+ *  - Index arrays handed over from the Fortran side are 1-based exactly as the
+ *    reference stores them (ia, ja, diag, owner, neighbour, face nodes).
+ *  - Fields follow the reference layout: numTotal = numCells+numBoundaryFaces
+ *    values, cell values first, then one value per boundary face
+ *    (geometry.f90:282).  Gradients are (3,numTotal) column-major, i.e. xyz
+ *    interleaved per cell (variables.f90:10).
+ *  - Host pointers are copied; pointers to device memory are used in place.
+ *  - One fc_ctx per host thread; calls on one context are stream ordered and
+ *    not thread safe.
+ */
+#ifndef FC_GPU_H
+#define FC_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define FC_OK                0
+#define FC_WARN_MAXITER      1   /* solver stopped at itr_max (the reference continues silently) */
+#define FC_ERR_BAD_INPUT    -1   /* invalid argument / inconsistent sizes / bad index */
+#define FC_ERR_CUDA         -2   /* CUDA runtime error */
+#define FC_ERR_NAN          -3   /* NaN or Inf met in a residual norm */
+#define FC_ERR_BREAKDOWN    -4   /* Krylov breakdown (zero denominator) */
+#define FC_ERR_TIMEOUT      -5   /* a bounded device spin-wait ran out */
+#define FC_ERR_STATE        -6   /* call made in the wrong state (e.g. no mesh set) */
+#define FC_ERR_UNSUPPORTED  -7   /* option not implemented */
+#define FC_ERR_ZERO_PIVOT   -8   /* zero pivot in ILU(0) (ilu_cr stops the program) */
+#define FC_ERR_NOMEM        -9   /* device allocation failed */
+
+/* ---- boundary condition types (bctype strings of the native mesh) ------- */
+#define FC_BC_WALL       1   /* 'wall'     */
+#define FC_BC_INLET      2   /* 'inlet'    */
+#define FC_BC_OUTLET     3   /* 'outlet'   */
+#define FC_BC_SYMMETRY   4   /* 'symmetry' */
+#define FC_BC_PRESSURE   5   /* 'pressure' */
+#define FC_BC_EMPTY      6   /* 'empty'    */
+#define FC_BC_PERIODIC   7   /* 'periodic' (not supported on this path yet) */
+
+/* ======================================================================== */
+/* Host-side mesh (native polyMesh format of read_mesh_native,              */
+/* geometry.f90:118-410).  These calls need no GPU.                          */
+/* ======================================================================== */
+typedef struct fc_mesh fc_mesh;
+
+#define FC_NOMAX 6   /* max nodes per face, geometry.f90:40 */
+
+/* Structured nx*ny*nz hex box on [0,lx]x[0,ly]x[0,lz].  Interior vertices are
+ * moved by U(-perturb*h, +perturb*h) per axis (seeded).  tets!=0 splits every
+ * hex into 6 tetrahedra.  side_bctype[6] gives the FC_BC_* type of the
+ * patches xmin,xmax,ymin,ymax,zmin,zmax (NULL: all walls).  Inner faces are
+ * ordered by (owner,neighbour), owner<neighbour, area vector owner->neighbour;
+ * boundary faces are grouped by patch in the order above. */
+int fc_mesh_box(int nx, int ny, int nz, double lx, double ly, double lz,
+                double perturb, unsigned long long seed, int tets,
+                const int* side_bctype, fc_mesh** out);
+
+/* Build from arrays in the reference's native layout (1-based owner,
+ * neighbour and face nodes; nodes has FC_NOMAX entries per face; startFace is
+ * the 0-based face offset of each patch as in the 'boundary' file). */
+int fc_mesh_from_arrays(int numNodes, int numCells, int numInnerFaces, int numBoundaryFaces,
+                        const double* x, const double* y, const double* z,
+                        const int* nnodes, const int* nodes,
+                        const int* owner, const int* neighbour,
+                        int numBoundaries, const int* bctype, const int* nfaces,
+                        const int* startFace, fc_mesh** out);
+
+/* Read / write the native files points, faces, owner, neighbour, boundary,
+ * size of a polyMesh directory (read_mesh_native, geometry.f90:165-410). */
+int fc_mesh_read_native(const char* dir, fc_mesh** out);
+int fc_mesh_write_native(const fc_mesh* m, const char* dir);
+
+/* info[6] = numNodes, numCells, numInnerFaces, numBoundaryFaces, numFaces, numBoundaries */
+int fc_mesh_info(const fc_mesh* m, int* info);
+/* Copy the mesh out (any pointer may be NULL). */
+int fc_mesh_export(const fc_mesh* m, double* x, double* y, double* z,
+                   int* nnodes, int* nodes, int* owner, int* neighbour,
+                   int* bctype, int* nfaces, int* startFace);
+void fc_mesh_free(fc_mesh* m);
+
+/* ======================================================================== */
+/* Context                                                                  */
+/* ======================================================================== */
+typedef struct fc_ctx fc_ctx;
+
+#define FC_PREC_FP64   0   /* everything in FP64, as the reference */
+#define FC_PREC_MIXED  1   /* FP32 matrix/preconditioner/Krylov vectors inside FP64 iterative refinement */
+
+int fc_init(int device, fc_ctx** out);
+void fc_finalize(fc_ctx* ctx);
+const char* fc_last_error(const fc_ctx* ctx);
+/* level 1: print the reference's solver report line after every solve */
+int fc_set_verbosity(fc_ctx* ctx, int level);
+/* FC_PREC_MIXED: inner FP32 solves to the relative tolerance inner_tol
+ * (<=0: 1e-4), at most inner_itmax iterations each (<=0: itr_max); the
+ * refinement loop stops on the reference's criterion in FP64. */
+int fc_set_precision(fc_ctx* ctx, int mode, double inner_tol, int inner_itmax);
+long long fc_kernel_launches(const fc_ctx* ctx);  /* kernels launched so far by this context */
+int fc_stream_sync(fc_ctx* ctx);
+void* fc_stream(fc_ctx* ctx);                     /* the cudaStream_t every call is ordered on */
+int fc_event_record(fc_ctx* ctx, int which);      /* which: 0 start, 1 stop (on the context stream) */
+int fc_event_elapsed_ms(fc_ctx* ctx, float* ms);
+
+/* ======================================================================== */
+/* Linear solvers                                                           */
+/* ======================================================================== */
+typedef struct {
+  int status;            /* FC_* of this solve */
+  int itr_used;          /* Krylov iterations (inner iterations in FC_PREC_MIXED) */
+  int outer_iterations;  /* refinement steps (FC_PREC_MIXED) */
+  int early_exit;        /* 1: initial residual below tol_abs, nothing done */
+  double res0_l1;        /* initial residual, L1 norm */
+  double resor;          /* res0_l1 / factor: the normalised residual the reference reports */
+  double resl;           /* final residual, L1 norm (|g(k+1)| for pmgmres) */
+  double factor;         /* sum|a_ii x_i| + small after the first iteration */
+  double ms;             /* device time of the solve */
+} fc_solve_info;
+
+/* Drop-in for csrsolve (src/linearSolvers/linear_solvers.f90:40-91) with the
+ * matrix passed explicitly, as the individual solvers take it
+ * (linear_solvers.f90:96,206,364,548,789).  solver: "iccg" (DIC-PCG),
+ * "bicgstab" (DILU-BiCGStab), "dpcg" (Jacobi-PCG), "gauss-seidel",
+ * "pmgmres" (GMRES(4)+ILU(0)).  ia(n+1), ja(nnz), diag(n) are 1-based; fi
+ * (in/out), rhs, a may be host or device memory.  *res0 receives the
+ * normalised initial residual (left unchanged on the early exit, as in the
+ * reference).  The pattern analysis is cached per (ia, ja, diag) address and
+ * size; call fc_csr_pattern_forget() after changing a pattern in place.
+ * Returns FC_OK, FC_WARN_MAXITER, or an error. */
+int fc_csrsolve(fc_ctx* ctx, const char* solver, int n, int nnz, const int* ia, const int* ja,
+                const double* a, const int* diag, double* fi, const double* rhs, double* res0,
+                int itr_max, double tol_abs, double tol_rel, const char* chvar, int verbose,
+                fc_solve_info* info);
+int fc_csr_pattern_forget(fc_ctx* ctx);
+
+/* Diagonal factors of the DIC (iccg, linear_solvers.f90:439-445) or DILU
+ * (bicgstab, :613-624) preconditioner, d_i stored inverted as there. */
+int fc_precond_setup(fc_ctx* ctx, const char* kind, int n, int nnz, const int* ia, const int* ja,
+                     const double* a, const int* diag, double* d_out);
+/* z = M^-1 q with the same preconditioner (forward sweep, z/(d+small),
+ * backward sweep: linear_solvers.f90:458-475). */
+int fc_precond_apply(fc_ctx* ctx, const char* kind, int n, int nnz, const int* ia, const int* ja,
+                     const double* a, const int* diag, const double* q, double* z_out);
+/* y = A x (ax_cr, linear_solvers.f90:1173) or y = A^T x (atx_cr, :1079). */
+int fc_spmv(fc_ctx* ctx, int n, int nnz, const int* ia, const int* ja, const double* a, const int* diag,
+            const double* x, double* y, int transpose);
+/* ILU(0) factors of ilu_cr (linear_solvers.f90:1267-1385) in the CSR slots. */
+int fc_ilu0(fc_ctx* ctx, int n, int nnz, const int* ia, const int* ja, const double* a, const int* diag,
+            double* l_out);
+
+/* ======================================================================== */
+/* Mesh, fields and finite-volume operators on the device                   */
+/* ======================================================================== */
+/* Upload the mesh and build everything derived from it once: cell -> face
+ * lists, the geometry of read_mesh_native (geometry.f90:416-665, computed on
+ * the device), the CSR pattern and face -> CSR slot maps of create_CSR_matrix
+ * (sparse_matrix.f90:86-296), and zeroed fields.  Replaces read_mesh +
+ * create_CSR_matrix + create_fields (main.f90:105-107). */
+int fc_set_mesh(fc_ctx* ctx, const fc_mesh* m);
+/* Geometry arrays by the reference's names: "arx","ary","arz","xf","yf","zf"
+ * (numFaces), "xc","yc","zc","vol" (numCells), "facint","Df" (numInnerFaces). */
+int fc_get_geometry(fc_ctx* ctx, const char* name, double* out);
+/* CSR pattern (ia, ja, diag) and icell_jcell_csr_index / jcell_icell_csr_index,
+ * 1-based; any output may be NULL. */
+int fc_get_csr_pattern(fc_ctx* ctx, int* n, int* nnz, int* ia, int* ja, int* diag, int* ijk, int* jik);
+
+/* Fields by the reference's variable names: "u","v","w","p","pp","vis","den","t"
+ * (numTotal), "flmass" (numFaces), "visw" (number of wall faces), "su","sv",
+ * "sw","spu","spv","sp","apu","apv","apw" (numCells), "dUdxi","dVdxi",
+ * "dWdxi","dPdxi","dTdxi" (3*numTotal, (3,numTotal) layout) and "a" (nnz, the
+ * global matrix).  count must equal the field length. */
+int fc_field_set(fc_ctx* ctx, const char* name, const double* values, long long count);
+int fc_field_get(fc_ctx* ctx, const char* name, double* out, long long count);
+int fc_field_fill(fc_ctx* ctx, const char* name, double value);
+double* fc_field_ptr(fc_ctx* ctx, const char* name);  /* device address, NULL if unknown */
+
+#define FC_GRAD_GAUSS   0   /* grad_gauss    gradients.f90:1607 */
+#define FC_GRAD_LSQ     1   /* grad_lsq      gradients.f90:782  */
+#define FC_GRAD_LSQ_DM  2   /* grad_lsq_dm   gradients.f90:1334 */
+/* grad(phi, dPhidxi) (gradients.f90:106-163, no limiter): phi numTotal values,
+ * dphi (3,numTotal); host or device memory. */
+int fc_grad(fc_ctx* ctx, int scheme, const double* phi, double* dphi);
+/* laplacian(mu, phi) (laplacian.f90:1-105): fills the global matrix "a" and
+ * accumulates the Dirichlet terms into "su" (not cleared, as there).  Bit b
+ * of dirichlet_mask enables the boundary term on patch b; ~0ULL reproduces
+ * the reference, which applies it on every patch. */
+int fc_laplacian(fc_ctx* ctx, const double* mu, const double* phi, unsigned long long dirichlet_mask);
+/* csrsolve(solver, fi, rhs, res0, ...) on the global matrix with the fields
+ * x_field (in/out) and rhs_field, exactly the reference's call convention. */
+int fc_solve_field(fc_ctx* ctx, const char* solver, const char* x_field, const char* rhs_field, double* res0,
+                   int itr_max, double tol_abs, double tol_rel, const char* chvar, fc_solve_info* info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FC_GPU_H */

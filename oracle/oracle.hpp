@@ -1,0 +1,130 @@
+// ORACLE -- test infrastructure only.  A CPU restatement (FP64, no FMA
+// contraction: built with -ffp-contract=off) of the reference Fortran routines
+// of freeCappuccino's per-iteration path, statement order preserved, so that
+// the GPU library can be checked against it.  Nothing in the product links or
+// calls this code; only tests/, the smoke check and the CPU-baseline leg of
+// bench.py do.
+//
+// Parity status: the reference is Fortran and no Fortran compiler exists in
+// the build container, so the reference itself cannot be run; this
+// restatement is pinned by the reference's own known-answer programs
+// (test/test_linear_solvers_spsolve.f90 5x5 systems,
+// test/testFieldOperations linear-field gradient on its 20x20x1 polyMesh)
+// and by the properties its code guarantees (see tests/).
+//
+// Arrays inside the oracle are 1-based: every vector has a dummy element 0 so
+// that loops read exactly like the Fortran.  (3,n) arrays are stored as
+// g[3*i + k-1], k = 1..3.
+#pragma once
+#include <string>
+#include <vector>
+
+namespace orc {
+
+// Single-precision literals of the reference promoted to double
+// (parameters.f90:6 small=1e-20, linear_solvers.f90:238,447 s0=1.e20).
+static const double kSmall = (double)1e-20f;
+static const double kS0 = (double)1.e20f;
+static const double kTiny30 = (double)1e-30f;   // interpolation.f90:556 (+1e-30)
+
+enum { BC_WALL = 1, BC_INLET = 2, BC_OUTLET = 3, BC_SYMMETRY = 4, BC_PRESSURE = 5, BC_EMPTY = 6, BC_PERIODIC = 7 };
+
+struct Case {
+  // sizes (geometry.f90:17-24)
+  int numNodes = 0, numCells = 0, numInnerFaces = 0, numBoundaryFaces = 0, numFaces = 0, numTotal = 0;
+  int numBoundaries = 0;
+  std::vector<int> bctype, nfaces, startFace, iBndValueStart;  // 1-based per boundary
+  int nwal = 0, nsym = 0;
+  // mesh (1-based)
+  std::vector<double> x, y, z;
+  std::vector<int> nnodes, node;  // node[(iface)*6 + k] k=1..6 -> stored at node[iface*6 + k-1]
+  std::vector<int> owner, neighbour;
+  // geometry
+  std::vector<double> arx, ary, arz, xf, yf, zf, xc, yc, zc, vol, facint, Df;
+  std::vector<double> dns, srds, dnw, srdw;
+  // CSR (sparse_matrix.f90:10-18), 1-based values
+  int nnz = 0;
+  std::vector<int> ia, ja, diag, ijk, jik;
+  // matrix / sources (sparse_matrix.f90:21-25)
+  std::vector<double> a, su, sv, sw, spu, spv, sp, apu, apv, apw;
+  // fields (variables.f90)
+  std::vector<double> u, v, w, p, pp, flmass, vis, den, visw;
+  std::vector<double> dUdxi, dVdxi, dWdxi, dPdxi;  // 3*(numTotal+1)
+  std::vector<double> Dmat;                        // 9*(numCells+1)  (gradients.f90:12)
+  // solver work vectors (linear_solvers.f90:33)
+  std::vector<double> res, reso, pk, zk, d, uk, vk;
+  // parameters of the SIMPLE path
+  int gradScheme = 0;  // 0 gauss, 1 lstsq, 2 lstsq_dm
+  int pscheme = 0;     // 0 linear, 1 central, 2 weighted
+  double densit = 1.0, viscos = 0.01;
+  double urfU[3] = {0.8, 0.8, 0.8}, gdsU = 1.0, urfP = 0.3;
+  int cSchemeU = 1;    // interpolation scheme id (see face_value)
+  int maxiterU = 5, maxiterP = 20, npcor = 1, pRefCell = 1;
+  double tolAbsU = 1e-15, tolRelU = 0.01, tolAbsP = 1e-15, tolRelP = 0.025;
+  std::string lSolverU = "bicgstab", lSolverP = "iccg";
+  double resor[13] = {0};
+  double cumulativeContErr = 0.0;
+  double flomas = 0.0;
+  int verbose = 0;
+};
+
+inline double& G(std::vector<double>& g, int k, int i) { return g[3 * (size_t)i + (k - 1)]; }
+
+// mesh + geometry + CSR
+void setup_case(Case& c, int numNodes, int numCells, int numInnerFaces, int numBoundaryFaces,
+                const double* x, const double* y, const double* z, const int* nnodes, const int* nodes,
+                const int* owner, const int* neighbour, int numBoundaries, const int* bctype,
+                const int* nfaces, const int* startFace);
+void geometry(Case& c);
+void create_csr(Case& c);
+
+// linear solvers (linear_solvers.f90); arrays 1-based raw pointers
+struct SolveInfo { int itr_used = 0; double res0 = 0, resl = 0, factor = 0, resor = 0; int early = 0; };
+void gauss_seidel(int n, int nnz, const int* ia, const int* ja, const double* a, const int* diag, double* fi,
+                  const double* rhs, double& resor, int itr_max, double tol_abs, double tol_rel, double* res,
+                  SolveInfo& si);
+void dpcg(int n, int nnz, const int* ia, const int* ja, const double* a, const int* diag, double* fi,
+          const double* rhs, double& resor, int itr_max, double tol_abs, double tol_rel, double* res, double* pk,
+          double* zk, SolveInfo& si);
+void iccg(int n, int nnz, const int* ia, const int* ja, const double* a, const int* diag, double* fi,
+          const double* rhs, double& resor, int itr_max, double tol_abs, double tol_rel, double* res, double* pk,
+          double* zk, double* d, SolveInfo& si);
+void bicgstab(int n, int nnz, const int* ia, const int* ja, const double* a, const int* diag, double* fi,
+              const double* rhs, double& resor, int itr_max, double tol_abs, double tol_rel, double* res,
+              double* reso, double* pk, double* uk, double* zk, double* vk, double* d, SolveInfo& si);
+int pmgmres_ilu(int n, int nz_num, const int* ia, const int* ja, const double* a, int* ua, double* x,
+                const double* rhs, double& resor, int itr_max, int mr, double tol_abs, double tol_rel, SolveInfo& si);
+void dic_setup(int n, const int* ia, const int* ja, const double* a, const int* diag, double* d);
+void dilu_setup(int n, const int* ia, const int* ja, const double* a, const int* diag, double* d);
+void diag_precond_apply(int n, const int* ia, const int* ja, const double* a, const int* diag, const double* d,
+                        const double* r, double* z);
+void ax_cr(int n, const int* ia, const int* ja, const double* a, const double* x, double* w);
+void atx_cr(int n, const int* ia, const int* ja, const double* a, const double* x, double* w);
+int ilu_cr(int n, const int* ia, const int* ja, const double* a, int* ua, double* l);
+void lus_cr(int n, const int* ia, const int* ja, const double* l, const int* ua, const double* r, double* z);
+int csrsolve(Case& c, const std::string& solver, std::vector<double>& fi, const std::vector<double>& rhs,
+             double& res0, int itr_max, double tol_abs, double tol_rel, SolveInfo& si);
+
+// gradients (gradients.f90)
+void grad_gauss(Case& c, const std::vector<double>& u, std::vector<double>& dudxi);
+void create_matrix_lsq(Case& c);
+void grad_lsq(Case& c, const std::vector<double>& phi, std::vector<double>& dphidxi);
+void create_matrix_lsq_dm(Case& c);
+void grad_lsq_dm(Case& c, const std::vector<double>& phi, std::vector<double>& dphidxi);
+void grad(Case& c, const std::vector<double>& phi, std::vector<double>& dphidxi);
+
+// operators
+void laplacian(Case& c, const std::vector<double>& mu, const std::vector<double>& phi, unsigned long long dirichlet_mask);
+
+// SIMPLE path
+void gradp_and_sources(Case& c, std::vector<double>& p);
+void bpres(Case& c, std::vector<double>& p, int istage);
+void updateVelocityAtBoundary(Case& c);
+void init_flmass(Case& c);
+int calcuvw(Case& c);
+int calcp_simple(Case& c);
+void continuityErrors(Case& c);
+double face_value(Case& c, int ijp, int ijn, double xf, double yf, double zf, double lambda,
+                  const std::vector<double>& u, std::vector<double>& dUdxi, int scheme);
+
+}  // namespace orc

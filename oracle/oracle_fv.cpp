@@ -1,0 +1,757 @@
+// ORACLE (test infrastructure only) -- finite-volume operators of the SIMPLE
+// path: gradients (src/finiteVolume/fvExplicit/gradients.f90), face
+// interpolation (src/finiteVolume/interpolation/interpolation.f90), implicit
+// Laplacian (src/finiteVolume/fvImplicit/laplacian.f90), pressure gradient
+// and sources (Pressure/nablap.f90, Pressure/bpres.f90), momentum assembly
+// (Velocity/velocity.f90) and SIMPLE pressure correction
+// (Pressure/calcp_simple.f90, fluxes/faceflux_mass.f90,
+// Pressure/continuityErrors.f90), mass-flux initialisation
+// (cappuccino/init.f90:167-176).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "oracle.hpp"
+
+namespace orc {
+
+// ---------------------------------------------------------------- gradients
+// grad_gauss + gradbc, gradients.f90:1607-1715
+void grad_gauss(Case& c, const std::vector<double>& u, std::vector<double>& dudxi) {
+  std::fill(dudxi.begin(), dudxi.end(), 0.0);
+  for (int i = 1; i <= c.numInnerFaces; ++i) {
+    int ijp = c.owner[i], ijn = c.neighbour[i];
+    double fie = u[ijp] + (u[ijn] - u[ijp]) * c.facint[i];
+    double dfxe = fie * c.arx[i], dfye = fie * c.ary[i], dfze = fie * c.arz[i];
+    G(dudxi, 1, ijp) = G(dudxi, 1, ijp) + dfxe;
+    G(dudxi, 2, ijp) = G(dudxi, 2, ijp) + dfye;
+    G(dudxi, 3, ijp) = G(dudxi, 3, ijp) + dfze;
+    G(dudxi, 1, ijn) = G(dudxi, 1, ijn) - dfxe;
+    G(dudxi, 2, ijn) = G(dudxi, 2, ijn) - dfye;
+    G(dudxi, 3, ijn) = G(dudxi, 3, ijn) - dfze;
+  }
+  for (int i = 1; i <= c.numBoundaryFaces; ++i) {
+    int iface = c.numInnerFaces + i;
+    int ijp = c.owner[iface], ijb = c.numCells + i;
+    G(dudxi, 1, ijp) = G(dudxi, 1, ijp) + u[ijb] * c.arx[iface];
+    G(dudxi, 2, ijp) = G(dudxi, 2, ijp) + u[ijb] * c.ary[iface];
+    G(dudxi, 3, ijp) = G(dudxi, 3, ijp) + u[ijb] * c.arz[iface];
+  }
+  for (int ijp = 1; ijp <= c.numCells; ++ijp) {
+    double volr = 1.0 / c.vol[ijp];
+    for (int k = 1; k <= 3; ++k) G(dudxi, k, ijp) = G(dudxi, k, ijp) * volr;
+  }
+}
+
+// shared cofactor step of create_matrix_lsq (:742-777) and _dm (:1292-1326)
+static void lsq_invert(Case& c) {
+  for (int inp = 1; inp <= c.numCells; ++inp) {
+    double* D = &c.Dmat[9 * (size_t)inp];
+    double d11 = D[0], d12 = D[1], d13 = D[2], d22 = D[3], d23 = D[4], d33 = D[5];
+    double d21 = d12, d31 = d13, d32 = d23;
+    double tmp = 1.0 / (d11 * d22 * d33 - d11 * d23 * d32 - d12 * d21 * d33 + d12 * d23 * d31 + d13 * d21 * d32 -
+                        d13 * d22 * d31 + kSmall);
+    D[0] = (d22 * d33 - d23 * d32) * tmp;
+    D[1] = (d21 * d33 - d23 * d31) * tmp;
+    D[2] = (d21 * d32 - d22 * d31) * tmp;
+    D[3] = (d11 * d33 - d13 * d31) * tmp;
+    D[4] = (d12 * d33 - d13 * d32) * tmp;
+    D[5] = (d11 * d32 - d12 * d31) * tmp;
+    D[6] = (d12 * d23 - d13 * d22) * tmp;
+    D[7] = (d11 * d23 - d13 * d21) * tmp;
+    D[8] = (d11 * d22 - d12 * d21) * tmp;
+  }
+}
+
+// create_matrix_lsq, gradients.f90:660-779
+void create_matrix_lsq(Case& c) {
+  c.Dmat.assign(9 * (size_t)(c.numCells + 1), 0.0);
+  auto D = [&](int k, int i) -> double& { return c.Dmat[9 * (size_t)i + (k - 1)]; };
+  for (int i = 1; i <= c.numInnerFaces; ++i) {
+    int ijp = c.owner[i], ijn = c.neighbour[i];
+    double Dx = c.xc[ijn] - c.xc[ijp], Dy = c.yc[ijn] - c.yc[ijp], Dz = c.zc[ijn] - c.zc[ijp];
+    D(1, ijp) = D(1, ijp) + Dx * Dx; D(1, ijn) = D(1, ijn) + Dx * Dx;
+    D(4, ijp) = D(4, ijp) + Dy * Dy; D(4, ijn) = D(4, ijn) + Dy * Dy;
+    D(6, ijp) = D(6, ijp) + Dz * Dz; D(6, ijn) = D(6, ijn) + Dz * Dz;
+    D(2, ijp) = D(2, ijp) + Dx * Dy; D(2, ijn) = D(2, ijn) + Dx * Dy;
+    D(3, ijp) = D(3, ijp) + Dx * Dz; D(3, ijn) = D(3, ijn) + Dx * Dz;
+    D(5, ijp) = D(5, ijp) + Dy * Dz; D(5, ijn) = D(5, ijn) + Dy * Dz;
+  }
+  for (int i = 1; i <= c.numBoundaryFaces; ++i) {
+    int iface = c.numInnerFaces + i, ijp = c.owner[iface];
+    double Dx = c.xf[iface] - c.xc[ijp], Dy = c.yf[iface] - c.yc[ijp], Dz = c.zf[iface] - c.zc[ijp];
+    D(1, ijp) = D(1, ijp) + Dx * Dx;
+    D(4, ijp) = D(4, ijp) + Dy * Dy;
+    D(6, ijp) = D(6, ijp) + Dz * Dz;
+    D(2, ijp) = D(2, ijp) + Dx * Dy;
+    D(3, ijp) = D(3, ijp) + Dx * Dz;
+    D(5, ijp) = D(5, ijp) + Dy * Dz;
+  }
+  // D(1..6) hold d11 d12 d13 d22 d23 d33 before inversion
+  lsq_invert(c);
+}
+
+// create_matrix_lsq_dm, gradients.f90:1157-1328
+void create_matrix_lsq_dm(Case& c) {
+  c.Dmat.assign(9 * (size_t)(c.numCells + 1), 0.0);
+  auto D = [&](int k, int i) -> double& { return c.Dmat[9 * (size_t)i + (k - 1)]; };
+  for (int i = 1; i <= c.numInnerFaces; ++i) {
+    int ijp = c.owner[i], ijn = c.neighbour[i];
+    double ddx = c.xc[ijn] - c.xc[ijp], ddy = c.yc[ijn] - c.yc[ijp], ddz = c.zc[ijn] - c.zc[ijp];
+    double w = 1.0 / (ddx * ddx + ddy * ddy + ddz * ddz);
+    double Dx = c.xc[ijn] - c.xc[ijp], Dy = c.yc[ijn] - c.yc[ijp], Dz = c.zc[ijn] - c.zc[ijp];
+    D(1, ijp) = D(1, ijp) + w * Dx * Dx; D(1, ijn) = D(1, ijn) + w * Dx * Dx;
+    D(4, ijp) = D(4, ijp) + w * Dy * Dy; D(4, ijn) = D(4, ijn) + w * Dy * Dy;
+    D(6, ijp) = D(6, ijp) + w * Dz * Dz; D(6, ijn) = D(6, ijn) + w * Dz * Dz;
+    D(2, ijp) = D(2, ijp) + w * Dx * Dy; D(2, ijn) = D(2, ijn) + w * Dx * Dy;
+    D(3, ijp) = D(3, ijp) + w * Dx * Dz; D(3, ijn) = D(3, ijn) + w * Dx * Dz;
+    D(5, ijp) = D(5, ijp) + w * Dy * Dz; D(5, ijn) = D(5, ijn) + w * Dy * Dz;
+  }
+  for (int i = 1; i <= c.numBoundaryFaces; ++i) {
+    int iface = c.numInnerFaces + i, ijp = c.owner[iface];
+    double ddx = c.xf[iface] - c.xc[ijp], ddy = c.yf[iface] - c.yc[ijp], ddz = c.zf[iface] - c.zc[ijp];
+    double w = 1.0 / (ddx * ddx + ddy * ddy + ddz * ddz);
+    double Dx = c.xf[iface] - c.xc[ijp], Dy = c.yf[iface] - c.yc[ijp], Dz = c.zf[iface] - c.zc[ijp];
+    D(1, ijp) = D(1, ijp) + w * Dx * Dx;
+    D(4, ijp) = D(4, ijp) + w * Dy * Dy;
+    D(6, ijp) = D(6, ijp) + w * Dz * Dz;
+    D(2, ijp) = D(2, ijp) + w * Dx * Dy;
+    D(3, ijp) = D(3, ijp) + w * Dx * Dz;
+    D(5, ijp) = D(5, ijp) + w * Dy * Dz;
+  }
+  lsq_invert(c);
+}
+
+// cofactor apply of grad_lsq (:883-889) / grad_lsq_dm (:1476-1482),
+// including the reference's y-row (b1*D4 - b2*D5 - b3*D6)
+static void lsq_apply(Case& c, std::vector<double>& g) {
+  for (int inp = 1; inp <= c.numCells; ++inp) {
+    const double* D = &c.Dmat[9 * (size_t)inp];
+    double b1 = G(g, 1, inp), b2 = G(g, 2, inp), b3 = G(g, 3, inp);
+    G(g, 1, inp) = b1 * D[0] - b2 * D[1] + b3 * D[2];
+    G(g, 2, inp) = b1 * D[3] - b2 * D[4] - b3 * D[5];
+    G(g, 3, inp) = b1 * D[6] - b2 * D[7] + b3 * D[8];
+  }
+}
+
+// grad_lsq, gradients.f90:782-893
+void grad_lsq(Case& c, const std::vector<double>& phi, std::vector<double>& g) {
+  std::fill(g.begin(), g.end(), 0.0);
+  for (int i = 1; i <= c.numInnerFaces; ++i) {
+    int ijp = c.owner[i], ijn = c.neighbour[i];
+    double delta = phi[ijn] - phi[ijp];
+    double Dx = (c.xc[ijn] - c.xc[ijp]) * delta, Dy = (c.yc[ijn] - c.yc[ijp]) * delta,
+           Dz = (c.zc[ijn] - c.zc[ijp]) * delta;
+    G(g, 1, ijp) = G(g, 1, ijp) + Dx; G(g, 2, ijp) = G(g, 2, ijp) + Dy; G(g, 3, ijp) = G(g, 3, ijp) + Dz;
+    G(g, 1, ijn) = G(g, 1, ijn) + Dx; G(g, 2, ijn) = G(g, 2, ijn) + Dy; G(g, 3, ijn) = G(g, 3, ijn) + Dz;
+  }
+  for (int i = 1; i <= c.numBoundaryFaces; ++i) {
+    int iface = c.numInnerFaces + i, ijp = c.owner[iface], ijn = c.numCells + i;
+    double delta = phi[ijn] - phi[ijp];
+    double Dx = (c.xf[iface] - c.xc[ijp]) * delta, Dy = (c.yf[iface] - c.yc[ijp]) * delta,
+           Dz = (c.zf[iface] - c.zc[ijp]) * delta;
+    G(g, 1, ijp) = G(g, 1, ijp) + Dx; G(g, 2, ijp) = G(g, 2, ijp) + Dy; G(g, 3, ijp) = G(g, 3, ijp) + Dz;
+  }
+  lsq_apply(c, g);
+}
+
+// grad_lsq_dm, gradients.f90:1334-1486 (boundary weight reads xf(i)...
+// at the boundary-face counter i, as the reference does at :1459)
+void grad_lsq_dm(Case& c, const std::vector<double>& phi, std::vector<double>& g) {
+  std::fill(g.begin(), g.end(), 0.0);
+  for (int i = 1; i <= c.numInnerFaces; ++i) {
+    int ijp = c.owner[i], ijn = c.neighbour[i];
+    double ddx = c.xc[ijn] - c.xc[ijp], ddy = c.yc[ijn] - c.yc[ijp], ddz = c.zc[ijn] - c.zc[ijp];
+    double w = (phi[ijn] - phi[ijp]) / (ddx * ddx + ddy * ddy + ddz * ddz);
+    double Dx = w * (c.xc[ijn] - c.xc[ijp]), Dy = w * (c.yc[ijn] - c.yc[ijp]), Dz = w * (c.zc[ijn] - c.zc[ijp]);
+    G(g, 1, ijp) = G(g, 1, ijp) + Dx; G(g, 2, ijp) = G(g, 2, ijp) + Dy; G(g, 3, ijp) = G(g, 3, ijp) + Dz;
+    G(g, 1, ijn) = G(g, 1, ijn) + Dx; G(g, 2, ijn) = G(g, 2, ijn) + Dy; G(g, 3, ijn) = G(g, 3, ijn) + Dz;
+  }
+  for (int i = 1; i <= c.numBoundaryFaces; ++i) {
+    int iface = c.numInnerFaces + i, ijp = c.owner[iface], ijn = c.numCells + i;
+    double ddx = c.xf[i] - c.xc[ijp], ddy = c.yf[i] - c.yc[ijp], ddz = c.zf[i] - c.zc[ijp];
+    double w = (phi[ijn] - phi[ijp]) / (ddx * ddx + ddy * ddy + ddz * ddz);
+    double Dx = w * (c.xf[iface] - c.xc[ijp]), Dy = w * (c.yf[iface] - c.yc[ijp]), Dz = w * (c.zf[iface] - c.zc[ijp]);
+    G(g, 1, ijp) = G(g, 1, ijp) + Dx; G(g, 2, ijp) = G(g, 2, ijp) + Dy; G(g, 3, ijp) = G(g, 3, ijp) + Dz;
+  }
+  lsq_apply(c, g);
+}
+
+// grad_scalar_field without limiter, gradients.f90:106-163
+void grad(Case& c, const std::vector<double>& phi, std::vector<double>& g) {
+  if (c.gradScheme == 1) grad_lsq(c, phi, g);
+  else if (c.gradScheme == 2) grad_lsq_dm(c, phi, g);
+  else grad_gauss(c, phi, g);
+}
+
+// ------------------------------------------------------------ interpolation
+// Scheme ids shared with the GPU library (fc_gpu.h FC_SCHEME_*).
+enum {
+  S_CDS = 0, S_CENTRAL = 1, S_LINEARUPWIND = 2, S_KAPPA = 3,
+  S_MUSCL = 10, S_UMIST, S_KOREN, S_SMART, S_AVLSMART, S_CHARM, S_VANLEER, S_OSPRE, S_MINMOD,
+  S_BLU, S_BLU02, S_BCENTRAL, S_FROMM, S_CUI, S_QUICK, S_SPL13
+};
+
+// face_value_flux_limiter, interpolation.f90:489-650
+static double face_value_flux_limiter(Case& c, int ijp, int ijn, double lambda, const std::vector<double>& u,
+                                      std::vector<double>& dUdxi, int scheme) {
+  double fxp = 1.0 - lambda;
+  double psi = 1.0;
+  double xpn = c.xc[ijn] - c.xc[ijp], ypn = c.yc[ijn] - c.yc[ijp], zpn = c.zc[ijn] - c.zc[ijp];
+  double r = (2 * G(dUdxi, 1, ijp) * xpn + 2 * G(dUdxi, 2, ijp) * ypn + 2 * G(dUdxi, 3, ijp) * zpn) /
+                 (u[ijn] - u[ijp] + kTiny30) - 1.0;
+  const double two3s = (double)(2.0f / 3.0f), one3s = (double)(1.0f / 3.0f);  // 2./3. and 1./3. (single)
+  const double two3d = 2.0 / 3.0, one3d = 1.0 / 3.0;                          // 2./3._dp, 1./3.0_dp
+  switch (scheme) {
+    case S_MUSCL: psi = std::max(0.0, std::min(std::min(2 * r, 0.5 * r + 0.5), 2.0)); break;
+    case S_UMIST: psi = std::max(0.0, std::min(std::min(std::min(2 * r, 0.75 * r + 0.25), 0.25 * r + 0.75), 2.0)); break;
+    case S_KOREN: psi = std::max(0.0, std::min(std::min(2 * r, two3d * r + one3d), 2.0)); break;
+    case S_SMART: psi = std::max(0.0, std::min(std::min(2 * r, 0.75 * r + 0.25), 4.0)); break;
+    case S_AVLSMART: psi = std::max(0.0, std::min(std::min(1.5 * r, 0.75 * r + 0.25), 2.5)); break;
+    case S_CHARM: psi = std::max(0.0, (r + std::fabs(r)) * (3 * r + 1.0) / (2 * ((r + 1.0) * (r + 1.0)))); break;
+    case S_VANLEER: psi = std::max(0.0, std::min((r + std::fabs(r)) / (r + 1.0), 2.0)); break;
+    case S_OSPRE: psi = std::max(0.0, 3 * r * (r + 1.0) / (2 * (r * r + r + 1.0))); break;
+    case S_MINMOD: psi = std::max(0.0, std::min(r, 1.0)); break;
+    case S_BLU: psi = std::max(0.0, std::min(2 * r, 1.0)); break;
+    case S_BLU02: psi = std::max(0.0, std::min(10 * r, 1.0)); break;
+    case S_BCENTRAL: psi = std::max(0.0, std::min(r, 4.0)); break;
+    case S_FROMM: psi = 0.5 * r + 0.5; break;
+    case S_CUI: psi = two3s * r + one3s; break;
+    case S_QUICK: psi = 0.75 * r + 0.25; break;
+    case S_SPL13:
+      psi = std::max(0.0, std::min(std::min(std::min(2 * r, one3s * r + two3s), two3s * r + one3s), 2.0));
+      break;
+    default: psi = 1.0; break;
+  }
+  return u[ijp] + fxp * psi * (u[ijn] - u[ijp]);
+}
+
+// face_value, interpolation.f90:28-113
+double face_value(Case& c, int ijp, int ijn, double xf, double yf, double zf, double lambda,
+                  const std::vector<double>& u, std::vector<double>& dUdxi, int scheme) {
+  switch (scheme) {
+    case S_CDS:  // face_value_cds :116-157
+      return u[ijp] + (u[ijn] - u[ijp]) * lambda;
+    case S_CENTRAL: {  // face_value_central :218-264
+      double gradfidr = G(dUdxi, 1, ijp) * (xf - c.xc[ijp]) + G(dUdxi, 2, ijp) * (yf - c.yc[ijp]) +
+                        G(dUdxi, 3, ijp) * (zf - c.zc[ijp]) + G(dUdxi, 1, ijn) * (xf - c.xc[ijn]) +
+                        G(dUdxi, 2, ijn) * (yf - c.yc[ijn]) + G(dUdxi, 3, ijn) * (zf - c.zc[ijn]);
+      return 0.5 * (u[ijp] + u[ijn] + gradfidr);
+    }
+    case S_LINEARUPWIND: {  // face_value_2nd_upwind :318-356
+      double gradfidr = G(dUdxi, 1, ijp) * (xf - c.xc[ijp]) + G(dUdxi, 2, ijp) * (yf - c.yc[ijp]) +
+                        G(dUdxi, 3, ijp) * (zf - c.zc[ijp]);
+      return u[ijp] + gradfidr;
+    }
+    case S_KAPPA: {  // face_value_kappa :359-416, theta = 2./3. (single)
+      const double theta = (double)(2.0f / 3.0f);
+      double g2 = G(dUdxi, 1, ijp) * (xf - c.xc[ijp]) + G(dUdxi, 2, ijp) * (yf - c.yc[ijp]) +
+                  G(dUdxi, 3, ijp) * (zf - c.zc[ijp]);
+      double gc = G(dUdxi, 1, ijp) * (xf - c.xc[ijp]) + G(dUdxi, 2, ijp) * (yf - c.yc[ijp]) +
+                  G(dUdxi, 3, ijp) * (zf - c.zc[ijp]) + G(dUdxi, 1, ijn) * (xf - c.xc[ijn]) +
+                  G(dUdxi, 2, ijn) * (yf - c.yc[ijn]) + G(dUdxi, 3, ijn) * (zf - c.zc[ijn]);
+      double vf2 = (u[ijp] + g2);
+      double vfc = 0.5 * (u[ijp] + u[ijn] + gc);
+      return theta * vfc + (1.0 - theta) * vf2;
+    }
+    default:
+      return face_value_flux_limiter(c, ijp, ijn, lambda, u, dUdxi, scheme);
+  }
+}
+
+// ----------------------------------------------------------------- laplacian
+// laplacian + faceFluxLaplacian, laplacian.f90:1-151.  The reference applies
+// the boundary term on every patch (its bctype filter is commented out at
+// :73); dirichlet_mask selects patches (bit ib-1), all bits = reference.
+void laplacian(Case& c, const std::vector<double>& mu, const std::vector<double>& phi,
+               unsigned long long dirichlet_mask) {
+  std::fill(c.a.begin(), c.a.end(), 0.0);
+  for (int i = 1; i <= c.numInnerFaces; ++i) {
+    int ijp = c.owner[i], ijn = c.neighbour[i];
+    double fxn = c.facint[i], fxp = 1.0 - c.facint[i];
+    double xpn = c.xc[ijn] - c.xc[ijp], ypn = c.yc[ijn] - c.yc[ijp], zpn = c.zc[ijn] - c.zc[ijp];
+    double smdpn = (c.arx[i] * c.arx[i] + c.ary[i] * c.ary[i] + c.arz[i] * c.arz[i]) /
+                   (c.arx[i] * xpn + c.ary[i] * ypn + c.arz[i] * zpn);
+    double cap = (fxp * mu[ijp] + fxn * mu[ijn]) * smdpn;
+    double can = cap;
+    c.a[c.ijk[i]] = can;
+    c.a[c.jik[i]] = cap;
+    c.a[c.diag[ijp]] = c.a[c.diag[ijp]] - can;
+    c.a[c.diag[ijn]] = c.a[c.diag[ijn]] - cap;
+  }
+  for (int ib = 1; ib <= c.numBoundaries; ++ib) {
+    if (ib <= 64 && !((dirichlet_mask >> (ib - 1)) & 1ULL)) continue;
+    for (int i = 1; i <= c.nfaces[ib]; ++i) {
+      int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
+      double are = std::sqrt(c.arx[iface] * c.arx[iface] + c.ary[iface] * c.ary[iface] + c.arz[iface] * c.arz[iface]);
+      double nxf = c.arx[iface] / are, nyf = c.ary[iface] / are, nzf = c.arz[iface] / are;
+      double dfn = (c.xf[iface] - c.xc[ijp]) * nxf + (c.yf[iface] - c.yc[ijp]) * nyf + (c.zf[iface] - c.zc[ijp]) * nzf;
+      double dcoef = mu[ijp] * are / dfn;
+      c.a[c.diag[ijp]] = c.a[c.diag[ijp]] - dcoef;
+      c.su[ijp] = c.su[ijp] - dcoef * phi[ijb];
+    }
+  }
+}
+
+// ------------------------------------------------------ pressure gradient
+// bpres, bpres.f90:55-180
+void bpres(Case& c, std::vector<double>& p, int istage) {
+  if (istage == 1) {
+    for (int ib = 1; ib <= c.numBoundaries; ++ib) {
+      if (c.bctype[ib] == BC_PRESSURE) continue;
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
+        p[ijb] = p[ijp];
+      }
+    }
+  } else {
+    for (int ib = 1; ib <= c.numBoundaries; ++ib) {
+      if (c.bctype[ib] != BC_WALL) continue;
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
+        double xpb = c.xf[iface] - c.xc[ijp], ypb = c.yf[iface] - c.yc[ijp], zpb = c.zf[iface] - c.zc[ijp];
+        p[ijb] = p[ijp] + G(c.dPdxi, 1, ijp) * xpb + G(c.dPdxi, 2, ijp) * ypb + G(c.dPdxi, 3, ijp) * zpb;
+      }
+    }
+  }
+}
+
+// gradp_and_sources, nablap.f90:19-208
+void gradp_and_sources(Case& c, std::vector<double>& p) {
+  const int nC = c.numCells;
+  auto inner_sum = [&](int mode) {
+    for (int i = 1; i <= c.numInnerFaces; ++i) {
+      int ijp = c.owner[i], ijn = c.neighbour[i];
+      double pf;
+      if (mode == 0) pf = p[ijp] + (p[ijn] - p[ijp]) * c.facint[i];
+      else if (mode == 1) pf = face_value(c, ijp, ijn, c.xf[i], c.yf[i], c.zf[i], c.facint[i], p, c.dPdxi, S_CENTRAL);
+      else pf = (p[ijp] * c.apu[ijp] + p[ijn] * c.apu[ijn]) / (c.apu[ijp] + c.apu[ijn] + kSmall);
+      double dfxe = pf * c.arx[i], dfye = pf * c.ary[i], dfze = pf * c.arz[i];
+      c.su[ijp] = c.su[ijp] - dfxe; c.sv[ijp] = c.sv[ijp] - dfye; c.sw[ijp] = c.sw[ijp] - dfze;
+      c.su[ijn] = c.su[ijn] + dfxe; c.sv[ijn] = c.sv[ijn] + dfye; c.sw[ijn] = c.sw[ijn] + dfze;
+    }
+  };
+  std::fill(c.su.begin(), c.su.end(), 0.0);
+  std::fill(c.sv.begin(), c.sv.end(), 0.0);
+  std::fill(c.sw.begin(), c.sw.end(), 0.0);
+  inner_sum(c.pscheme == 2 ? 2 : 0);
+  for (int istage = 1; istage <= 2; ++istage) {
+    bpres(c, p, istage);
+    if (istage == 2 && c.pscheme == 1) {
+      std::fill(c.su.begin(), c.su.end(), 0.0);
+      std::fill(c.sv.begin(), c.sv.end(), 0.0);
+      std::fill(c.sw.begin(), c.sw.end(), 0.0);
+      inner_sum(1);
+    }
+    for (int i = 1; i <= nC; ++i) {
+      G(c.dPdxi, 1, i) = -c.su[i];
+      G(c.dPdxi, 2, i) = -c.sv[i];
+      G(c.dPdxi, 3, i) = -c.sw[i];
+    }
+    for (int i = 1; i <= c.numBoundaryFaces; ++i) {
+      int iface = c.numInnerFaces + i, ijp = c.owner[iface], ijb = nC + i;
+      G(c.dPdxi, 1, ijp) = G(c.dPdxi, 1, ijp) + p[ijb] * c.arx[iface];
+      G(c.dPdxi, 2, ijp) = G(c.dPdxi, 2, ijp) + p[ijb] * c.ary[iface];
+      G(c.dPdxi, 3, ijp) = G(c.dPdxi, 3, ijp) + p[ijb] * c.arz[iface];
+    }
+    for (int ijp = 1; ijp <= nC; ++ijp) {
+      double volr = 1.0 / c.vol[ijp];
+      for (int k = 1; k <= 3; ++k) G(c.dPdxi, k, ijp) = G(c.dPdxi, k, ijp) * volr;
+    }
+  }
+  for (int i = 1; i <= c.numBoundaryFaces; ++i) {
+    int iface = c.numInnerFaces + i, ijp = c.owner[iface], ijb = nC + i;
+    c.su[ijp] = c.su[ijp] - p[ijb] * c.arx[iface];
+    c.sv[ijp] = c.sv[ijp] - p[ijb] * c.ary[iface];
+    c.sw[ijp] = c.sw[ijp] - p[ijb] * c.arz[iface];
+  }
+}
+
+// updateVelocityAtBoundary, velocity.f90:1184-1279
+void updateVelocityAtBoundary(Case& c) {
+  for (int ib = 1; ib <= c.numBoundaries; ++ib) {
+    if (c.bctype[ib] == BC_EMPTY || c.bctype[ib] == BC_PERIODIC) {
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
+        c.u[ijb] = c.u[ijp]; c.v[ijb] = c.v[ijp]; c.w[ijb] = c.w[ijp];
+      }
+    } else if (c.bctype[ib] == BC_SYMMETRY) {
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
+        double Unmag = c.u[ijp] * c.arx[iface] + c.v[ijp] * c.ary[iface] + c.w[ijp] * c.arz[iface];
+        c.u[ijb] = c.u[ijp] - Unmag * c.arx[iface];
+        c.v[ijb] = c.v[ijp] - Unmag * c.ary[iface];
+        c.w[ijb] = c.w[ijp] - Unmag * c.arz[iface];
+      }
+    }
+  }
+}
+
+// inner-face mass flux initialisation, init.f90:167-176
+void init_flmass(Case& c) {
+  for (int i = 1; i <= c.numInnerFaces; ++i) {
+    int ijp = c.owner[i], ijn = c.neighbour[i];
+    double fxn = c.facint[i], fxp = 1.0 - c.facint[i];
+    double ui = c.u[ijp] * fxp + c.u[ijn] * fxn;
+    double vi = c.v[ijp] * fxp + c.v[ijn] * fxn;
+    double wi = c.w[ijp] * fxp + c.w[ijn] * fxn;
+    c.flmass[i] = c.den[ijp] * (c.arx[i] * ui + c.ary[i] * vi + c.arz[i] * wi);
+  }
+}
+
+// --------------------------------------------------------------- momentum
+// sngrad (variant 1), gradients.f90:1720-1779
+static inline void sngrad(Case& c, int i, int ijp, int ijn, double arx, double ary, double arz, double lambda,
+                          const std::vector<double>& Phi, std::vector<double>& dPhidxi, double& dfixi, double& dfiyi,
+                          double& dfizi, double& dfixii, double& dfiyii, double& dfizii) {
+  double fxn = lambda, fxp = 1.0 - lambda;
+  double xpn = c.xc[ijn] - c.xc[ijp], ypn = c.yc[ijn] - c.yc[ijp], zpn = c.zc[ijn] - c.zc[ijp];
+  double vole = xpn * arx + ypn * ary + zpn * arz;
+  dfixi = G(dPhidxi, 1, ijp) * fxp + G(dPhidxi, 1, ijn) * fxn;
+  dfiyi = G(dPhidxi, 2, ijp) * fxp + G(dPhidxi, 2, ijn) * fxn;
+  dfizi = G(dPhidxi, 3, ijp) * fxp + G(dPhidxi, 3, ijn) * fxn;
+  dfixii = dfixi + arx / vole * (Phi[ijn] - Phi[ijp] - dfixi * xpn - dfiyi * ypn - dfizi * zpn);
+  dfiyii = dfiyi + ary / vole * (Phi[ijn] - Phi[ijp] - dfixi * xpn - dfiyi * ypn - dfizi * zpn);
+  dfizii = dfizi + arz / vole * (Phi[ijn] - Phi[ijp] - dfixi * xpn - dfiyi * ypn - dfizi * zpn);
+  dfixi = dfixi * (arx - c.Df[i] * xpn);
+  dfiyi = dfiyi * (ary - c.Df[i] * ypn);
+  dfizi = dfizi * (arz - c.Df[i] * zpn);
+}
+
+// facefluxuvw, velocity.f90:754-878
+static void facefluxuvw(Case& c, int i, int ijp, int ijn, double xf, double yf, double zf, double arx, double ary,
+                        double arz, double flomass, double lambda, double gam, double& cap, double& can, double& sup,
+                        double& svp, double& swp) {
+  double fxn = lambda, fxp = 1.0 - lambda;
+  double game = c.vis[ijp] + (c.vis[ijn] - c.vis[ijp]) * lambda;
+  double de = game * c.Df[i];
+  double ce = std::min(flomass, 0.0), cp = std::max(flomass, 0.0);
+  can = -de + ce;
+  cap = -de - cp;
+  double duxi, duyi, duzi, duxii, duyii, duzii, dvxi, dvyi, dvzi, dvxii, dvyii, dvzii, dwxi, dwyi, dwzi, dwxii,
+      dwyii, dwzii;
+  sngrad(c, i, ijp, ijn, arx, ary, arz, lambda, c.u, c.dUdxi, duxi, duyi, duzi, duxii, duyii, duzii);
+  sngrad(c, i, ijp, ijn, arx, ary, arz, lambda, c.v, c.dVdxi, dvxi, dvyi, dvzi, dvxii, dvyii, dvzii);
+  sngrad(c, i, ijp, ijn, arx, ary, arz, lambda, c.w, c.dWdxi, dwxi, dwyi, dwzi, dwxii, dwyii, dwzii);
+  double fdue = game * (duxii * arx + dvxii * ary + dwxii * arz);
+  double fdve = game * (duyii * arx + dvyii * ary + dwyii * arz);
+  double fdwe = game * (duzii * arx + dvzii * ary + dwzii * arz);
+  double fdui = game * (duxi + duyi + duzi);
+  double fdvi = game * (dvxi + dvyi + dvzi);
+  double fdwi = game * (dwxi + dwyi + dwzi);
+  fdue = fdue + fdui;
+  fdve = fdve + fdvi;
+  fdwe = fdwe + fdwi;
+  double fuuds = cp * c.u[ijp] + ce * c.u[ijn];
+  double fvuds = cp * c.v[ijp] + ce * c.v[ijn];
+  double fwuds = cp * c.w[ijp] + ce * c.w[ijn];
+  double ue, ve, we;
+  if (flomass >= 0.0) {
+    ue = face_value(c, ijp, ijn, xf, yf, zf, fxp, c.u, c.dUdxi, c.cSchemeU);
+    ve = face_value(c, ijp, ijn, xf, yf, zf, fxp, c.v, c.dVdxi, c.cSchemeU);
+    we = face_value(c, ijp, ijn, xf, yf, zf, fxp, c.w, c.dWdxi, c.cSchemeU);
+  } else {
+    ue = face_value(c, ijn, ijp, xf, yf, zf, fxn, c.u, c.dUdxi, c.cSchemeU);
+    ve = face_value(c, ijn, ijp, xf, yf, zf, fxn, c.v, c.dVdxi, c.cSchemeU);
+    we = face_value(c, ijn, ijp, xf, yf, zf, fxn, c.w, c.dWdxi, c.cSchemeU);
+  }
+  double fuhigh = flomass * ue, fvhigh = flomass * ve, fwhigh = flomass * we;
+  sup = -gam * (fuhigh - fuuds) + fdue;
+  svp = -gam * (fvhigh - fvuds) + fdve;
+  swp = -gam * (fwhigh - fwuds) + fdwe;
+}
+
+// facefluxuvw_bnd, velocity.f90:882-1034
+static void facefluxuvw_bnd(Case& c, int ijp, int ijb, double xf, double yf, double zf, double arx, double ary,
+                            double arz, double flomass, double& cap, double& can, double& sup, double& svp,
+                            double& swp) {
+  double xpn = xf - c.xc[ijp], ypn = yf - c.yc[ijp], zpn = zf - c.zc[ijp];
+  double vole = xpn * arx + ypn * ary + zpn * arz;
+  double Dfi = (arx * arx + ary * ary + arz * arz) / vole;
+  double game = c.vis[ijb];
+  double de = game * Dfi;
+  can = -de + std::min(flomass, 0.0);
+  cap = -de - std::max(flomass, 0.0);
+  auto comp = [&](const std::vector<double>& f, std::vector<double>& g, double& dxi, double& dyi, double& dzi,
+                  double& dxii, double& dyii, double& dzii) {
+    dxi = G(g, 1, ijp); dyi = G(g, 2, ijp); dzi = G(g, 3, ijp);
+    dxii = dxi + arx / vole * (f[ijb] - f[ijp] - dxi * xpn - dyi * ypn - dzi * zpn);
+    dyii = dyi + ary / vole * (f[ijb] - f[ijp] - dxi * xpn - dyi * ypn - dzi * zpn);
+    dzii = dzi + arz / vole * (f[ijb] - f[ijp] - dxi * xpn - dyi * ypn - dzi * zpn);
+    dxi = dxi * (arx - Dfi * xpn);
+    dyi = dyi * (ary - Dfi * ypn);
+    dzi = dzi * (arz - Dfi * zpn);
+  };
+  double duxi, duyi, duzi, duxii, duyii, duzii, dvxi, dvyi, dvzi, dvxii, dvyii, dvzii, dwxi, dwyi, dwzi, dwxii,
+      dwyii, dwzii;
+  comp(c.u, c.dUdxi, duxi, duyi, duzi, duxii, duyii, duzii);
+  comp(c.v, c.dVdxi, dvxi, dvyi, dvzi, dvxii, dvyii, dvzii);
+  comp(c.w, c.dWdxi, dwxi, dwyi, dwzi, dwxii, dwyii, dwzii);
+  double fdue = game * (duxii * arx + dvxii * ary + dwxii * arz);
+  double fdve = game * (duyii * arx + dvyii * ary + dwyii * arz);
+  double fdwe = game * (duzii * arx + dvzii * ary + dwzii * arz);
+  double fdui = game * (duxi + duyi + duzi);
+  double fdvi = game * (dvxi + dvyi + dvzi);
+  double fdwi = game * (dwxi + dwyi + dwzi);
+  sup = fdue + fdui;
+  svp = fdve + fdvi;
+  swp = fdwe + fdwi;
+}
+
+// calcuvw, velocity.f90:50-750 for steady SIMPLE without buoyancy, MHD,
+// transient or periodic terms.  Returns the worst csrsolve status.
+int calcuvw(Case& c) {
+  const int nC = c.numCells;
+  std::fill(c.spu.begin(), c.spu.end(), 0.0);
+  std::fill(c.spv.begin(), c.spv.end(), 0.0);
+  std::fill(c.sp.begin(), c.sp.end(), 0.0);
+  updateVelocityAtBoundary(c);
+  grad(c, c.u, c.dUdxi);
+  grad(c, c.v, c.dVdxi);
+  grad(c, c.w, c.dWdxi);
+  gradp_and_sources(c, c.p);
+  // inner faces :286-314
+  for (int i = 1; i <= c.numInnerFaces; ++i) {
+    int ijp = c.owner[i], ijn = c.neighbour[i];
+    double cap, can, sup, svp, swp;
+    facefluxuvw(c, i, ijp, ijn, c.xf[i], c.yf[i], c.zf[i], c.arx[i], c.ary[i], c.arz[i], c.flmass[i], c.facint[i],
+                c.gdsU, cap, can, sup, svp, swp);
+    c.a[c.ijk[i]] = can;
+    c.a[c.jik[i]] = cap;
+    c.su[ijp] = c.su[ijp] + sup; c.sv[ijp] = c.sv[ijp] + svp; c.sw[ijp] = c.sw[ijp] + swp;
+    c.su[ijn] = c.su[ijn] - sup; c.sv[ijn] = c.sv[ijn] - svp; c.sw[ijn] = c.sw[ijn] - swp;
+  }
+  // boundaries :326-562
+  int iWall = 0;
+  const int inp_stale = nC + 1;  // loop variable 'inp' after the cell loop at :183 (used at :379)
+  for (int ib = 1; ib <= c.numBoundaries; ++ib) {
+    int t = c.bctype[ib];
+    if (t == BC_INLET || t == BC_OUTLET || t == BC_PRESSURE) {
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
+        double cp, cb, sup, svp, swp;
+        facefluxuvw_bnd(c, ijp, ijb, c.xf[iface], c.yf[iface], c.zf[iface], c.arx[iface], c.ary[iface], c.arz[iface],
+                        c.flmass[iface], cp, cb, sup, svp, swp);
+        c.spu[ijp] = c.spu[ijp] - cb; c.spv[ijp] = c.spv[ijp] - cb; c.sp[ijp] = c.sp[ijp] - cb;
+        c.su[ijp] = c.su[ijp] - cb * c.u[ijb] + sup;
+        c.sv[ijp] = c.sv[ijp] - cb * c.v[ijb] + svp;
+        c.sw[ijp] = c.sw[ijp] - cb * c.w[ijb] + swp;
+      }
+    } else if (t == BC_SYMMETRY) {
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int iface = c.startFace[ib] + i, ijp = c.owner[iface];
+        double are = std::sqrt(c.arx[iface] * c.arx[iface] + c.ary[iface] * c.ary[iface] + c.arz[iface] * c.arz[iface]);
+        double arer = 1.0 / are;
+        double nxf = c.arx[iface] * arer, nyf = c.ary[iface] * arer, nzf = c.arz[iface] * arer;
+        double dpb = (c.xf[iface] - c.xc[ijp]) * nxf + (c.yf[iface] - c.yc[ijp]) * nyf + (c.zf[iface] - c.zc[ijp]) * nzf;
+        double cf = 2 * c.vis[inp_stale] * are / dpb;
+        c.su[ijp] = c.su[ijp] - cf * nxf * (nyf * c.v[ijp] + nzf * c.w[ijp]);
+        c.sv[ijp] = c.sv[ijp] - cf * nyf * (nxf * c.u[ijp] + nzf * c.w[ijp]);
+        c.sw[ijp] = c.sw[ijp] - cf * nzf * (nxf * c.u[ijp] + nyf * c.v[ijp]);
+        c.spu[ijp] = c.spu[ijp] + cf * (nxf * nxf);
+        c.spv[ijp] = c.spv[ijp] + cf * (nyf * nyf);
+        c.sp[ijp] = c.sp[ijp] + cf * (nzf * nzf);
+      }
+    } else if (t == BC_WALL) {
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
+        ++iWall;
+        double viss = std::max(c.viscos, c.visw[iWall]);
+        double are = std::sqrt(c.arx[iface] * c.arx[iface] + c.ary[iface] * c.ary[iface] + c.arz[iface] * c.arz[iface]);
+        double arer = 1.0 / are;
+        double nxf = c.arx[iface] * arer, nyf = c.ary[iface] * arer, nzf = c.arz[iface] * arer;
+        double dpb = (c.xf[iface] - c.xc[ijp]) * nxf + (c.yf[iface] - c.yc[ijp]) * nyf + (c.zf[iface] - c.zc[ijp]) * nzf;
+        double vsol = viss * are / dpb;
+        double upb = c.u[ijp] - c.u[ijb], vpb = c.v[ijp] - c.v[ijb], wpb = c.w[ijp] - c.w[ijb];
+        c.spu[ijp] = c.spu[ijp] + vsol * (1. - nxf * nxf);
+        c.spv[ijp] = c.spv[ijp] + vsol * (1. - nyf * nyf);
+        c.sp[ijp] = c.sp[ijp] + vsol * (1. - nzf * nzf);
+        c.su[ijp] = c.su[ijp] + vsol * (c.u[ijb] * (1. - nxf * nxf) + vpb * nyf * nxf + wpb * nzf * nxf);
+        c.sv[ijp] = c.sv[ijp] + vsol * (upb * nxf * nyf + c.v[ijb] * (1. - nyf * nyf) + wpb * nzf * nyf);
+        c.sw[ijp] = c.sw[ijp] + vsol * (upb * nxf * nzf + vpb * nyf * nzf + c.w[ijb] * (1. - nzf * nzf));
+      }
+    }
+  }
+  int worst = 0;
+  SolveInfo si;
+  // U :611-638  (the diagonal slot still holds the previous matrix's value)
+  {
+    double urfr = 1.0 / c.urfU[0], urfm = 1.0 - c.urfU[0];
+    for (int inp = 1; inp <= nC; ++inp) {
+      double s = 0.0;
+      for (int k = c.ia[inp]; k <= c.ia[inp + 1] - 1; ++k) s += c.a[k];
+      double off = s - c.a[c.diag[inp]];
+      c.a[c.diag[inp]] = c.spu[inp] - off;
+      c.apu[inp] = 1. / (c.a[c.diag[inp]] + kSmall);
+      c.a[c.diag[inp]] = c.a[c.diag[inp]] * urfr;
+      c.su[inp] = c.su[inp] + urfm * c.a[c.diag[inp]] * c.u[inp];
+    }
+    int st = csrsolve(c, c.lSolverU, c.u, c.su, c.resor[1], c.maxiterU, c.tolAbsU, c.tolRelU, si);
+    worst = std::min(worst, st);
+  }
+  // V :667-693 and W :722-748
+  for (int comp = 2; comp <= 3; ++comp) {
+    for (int inp = 1; inp <= nC; ++inp) { c.a[c.diag[inp]] = 0.0; c.su[inp] = 0.0; }
+    double urfr = 1.0 / c.urfU[comp - 1], urfm = 1.0 - c.urfU[comp - 1];
+    std::vector<double>& spc = (comp == 2) ? c.spv : c.sp;
+    std::vector<double>& apc = (comp == 2) ? c.apv : c.apw;
+    std::vector<double>& src = (comp == 2) ? c.sv : c.sw;
+    std::vector<double>& fld = (comp == 2) ? c.v : c.w;
+    for (int inp = 1; inp <= nC; ++inp) {
+      double s = 0.0;
+      for (int k = c.ia[inp]; k <= c.ia[inp + 1] - 1; ++k) s += c.a[k];
+      double off = s - c.a[c.diag[inp]];
+      c.a[c.diag[inp]] = spc[inp] - off;
+      apc[inp] = 1. / (c.a[c.diag[inp]] + kSmall);
+      c.a[c.diag[inp]] = c.a[c.diag[inp]] * urfr;
+      c.su[inp] = src[inp] + urfm * c.a[c.diag[inp]] * fld[inp];
+    }
+    int st = csrsolve(c, c.lSolverU, fld, c.su, c.resor[comp], c.maxiterU, c.tolAbsU, c.tolRelU, si);
+    worst = std::min(worst, st);
+  }
+  return worst;
+}
+
+// ------------------------------------------------------- pressure (SIMPLE)
+// facefluxmass2, faceflux_mass.f90:175-249 (dPdxi weights as written)
+static void facefluxmass2(Case& c, int i, int ijp, int ijn, double arx, double ary, double arz, double lambda,
+                          double& cap, double& can, double& fluxmass) {
+  double fxn = lambda, fxp = 1.0 - lambda;
+  double xpn = c.xc[ijn] - c.xc[ijp], ypn = c.yc[ijn] - c.yc[ijp], zpn = c.zc[ijn] - c.zc[ijp];
+  double dene = c.den[ijp] * fxp + c.den[ijn] * fxn;
+  double Kj = c.vol[ijp] * c.apu[ijp] * fxp + c.vol[ijn] * c.apu[ijn] * fxn;
+  cap = -dene * Kj * c.Df[i];
+  can = cap;
+  double ui = c.u[ijp] + (c.u[ijn] - c.u[ijp]) * lambda;
+  double vi = c.v[ijp] + (c.v[ijn] - c.v[ijp]) * lambda;
+  double wi = c.w[ijp] + (c.w[ijn] - c.w[ijp]) * lambda;
+  double dpxi = (G(c.dPdxi, 1, ijn) * fxp + G(c.dPdxi, 1, ijp) * fxn) * xpn;
+  double dpyi = (G(c.dPdxi, 2, ijn) * fxp + G(c.dPdxi, 2, ijp) * fxn) * ypn;
+  double dpzi = (G(c.dPdxi, 3, ijn) * fxp + G(c.dPdxi, 3, ijp) * fxn) * zpn;
+  fluxmass = dene * (ui * arx + vi * ary + wi * arz) + cap * (c.p[ijn] - c.p[ijp] - dpxi - dpyi - dpzi);
+}
+
+// fluxmc2, faceflux_mass.f90:650-696
+static void fluxmc2(Case& c, int ijp, int ijn, double sx, double sy, double sz, double& fmc) {
+  double xpn = c.xc[ijn] - c.xc[ijp], ypn = c.yc[ijn] - c.yc[ijp], zpn = c.zc[ijn] - c.zc[ijp];
+  double s2 = sx * sx + sy * sy + sz * sz;
+  double dn = xpn * sx + ypn * sy + zpn * sz;
+  double rapr = -0.5 * (c.apu[ijp] * c.den[ijp] + c.apu[ijn] * c.den[ijn]);
+  double dpx = 0.5 * (G(c.dPdxi, 1, ijn) + G(c.dPdxi, 1, ijp));
+  double dpy = 0.5 * (G(c.dPdxi, 2, ijn) + G(c.dPdxi, 2, ijp));
+  double dpz = 0.5 * (G(c.dPdxi, 3, ijn) + G(c.dPdxi, 3, ijp));
+  fmc = rapr * ((dn * sx - xpn * s2) * dpx + (dn * sy - ypn * s2) * dpy + (dn * sz - zpn * s2) * dpz);
+}
+
+// adjustMassFlow, faceflux_mass.f90:833-916
+static void adjustMassFlow(Case& c) {
+  double flowo = 0.0;
+  for (int ib = 1; ib <= c.numBoundaries; ++ib) {
+    if (c.bctype[ib] != BC_OUTLET) continue;
+    for (int i = 1; i <= c.nfaces[ib]; ++i) {
+      int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
+      c.u[ijb] = c.u[ijp]; c.v[ijb] = c.v[ijp]; c.w[ijb] = c.w[ijp];
+      c.flmass[iface] = c.den[ijp] * (c.u[ijb] * c.arx[iface] + c.v[ijb] * c.ary[iface] + c.w[ijb] * c.arz[iface]);
+      flowo = flowo + c.flmass[iface];
+    }
+  }
+  double fac = c.flomas / (flowo + kSmall);
+  for (int ib = 1; ib <= c.numBoundaries; ++ib) {
+    if (c.bctype[ib] != BC_OUTLET) continue;
+    for (int i = 1; i <= c.nfaces[ib]; ++i) {
+      int iface = c.startFace[ib] + i, ijb = c.iBndValueStart[ib] + i;
+      c.flmass[iface] = c.flmass[iface] * fac;
+      c.u[ijb] = c.u[ijb] * fac; c.v[ijb] = c.v[ijb] * fac; c.w[ijb] = c.w[ijb] * fac;
+    }
+  }
+}
+
+// continuityErrors, continuityErrors.f90:1-77 (flmass indexed by the owner
+// cell as written at :26-27)
+void continuityErrors(Case& c) {
+  const int nC = c.numCells;
+  std::fill(c.su.begin(), c.su.end(), 0.0);
+  for (int i = 1; i <= c.numInnerFaces; ++i) {
+    int ijp = c.owner[i], ijn = c.neighbour[i];
+    c.su[ijp] = c.su[ijp] - c.flmass[ijp];
+    c.su[ijn] = c.su[ijn] + c.flmass[ijp];
+  }
+  for (int ib = 1; ib <= c.numBoundaries; ++ib) {
+    if (c.bctype[ib] != BC_INLET && c.bctype[ib] != BC_OUTLET) continue;
+    for (int i = 1; i <= c.nfaces[ib]; ++i) {
+      int iface = c.startFace[ib] + i, ijp = c.owner[iface];
+      c.su[ijp] = c.su[ijp] - c.flmass[iface];
+    }
+  }
+  double wavg = 0.0, sumvol = 0.0;
+  for (int inp = 1; inp <= nC; ++inp) {
+    wavg = wavg + (c.vol[inp] * std::fabs(c.su[inp] * c.apu[inp]));
+    sumvol = sumvol + c.vol[inp];
+  }
+  wavg = wavg / sumvol;
+  double glob = 0.0;
+  for (int inp = 1; inp <= nC; ++inp) glob += c.su[inp];
+  c.cumulativeContErr = c.cumulativeContErr + glob;
+  std::fill(c.su.begin(), c.su.end(), 0.0);
+  c.resor[4] = wavg;
+}
+
+// calcp_simple, calcp_simple.f90:1-470 for incompressible SIMPLE without
+// periodic or pressure boundaries.
+int calcp_simple(Case& c) {
+  const int nC = c.numCells;
+  std::fill(c.a.begin(), c.a.end(), 0.0);
+  std::fill(c.su.begin(), c.su.end(), 0.0);
+  for (int i = 1; i <= c.numInnerFaces; ++i) {
+    int ijp = c.owner[i], ijn = c.neighbour[i];
+    double cap, can;
+    facefluxmass2(c, i, ijp, ijn, c.arx[i], c.ary[i], c.arz[i], c.facint[i], cap, can, c.flmass[i]);
+    c.a[c.ijk[i]] = cap;
+    c.a[c.jik[i]] = cap;
+    c.a[c.diag[ijp]] = c.a[c.diag[ijp]] - cap;
+    c.a[c.diag[ijn]] = c.a[c.diag[ijn]] - cap;
+    c.su[ijp] = c.su[ijp] - c.flmass[i];
+    c.su[ijn] = c.su[ijn] + c.flmass[i];
+  }
+  adjustMassFlow(c);
+  for (int ib = 1; ib <= c.numBoundaries; ++ib) {
+    if (c.bctype[ib] != BC_INLET && c.bctype[ib] != BC_OUTLET) continue;
+    for (int i = 1; i <= c.nfaces[ib]; ++i) {
+      int iface = c.startFace[ib] + i, ijp = c.owner[iface];
+      c.su[ijp] = c.su[ijp] - c.flmass[iface];
+    }
+  }
+  int worst = 0;
+  for (int ipcorr = 1; ipcorr <= c.npcor; ++ipcorr) {
+    SolveInfo si;
+    int st = csrsolve(c, c.lSolverP, c.pp, c.su, c.resor[4], c.maxiterP, c.tolAbsP, c.tolRelP, si);
+    worst = std::min(worst, st);
+    for (int iface = 1; iface <= c.numInnerFaces; ++iface) {
+      int ijp = c.owner[iface], ijn = c.neighbour[iface];
+      c.flmass[iface] = c.flmass[iface] + c.a[c.ijk[iface]] * (c.pp[ijn] - c.pp[ijp]);
+    }
+    double ppref = c.pp[c.pRefCell];
+    gradp_and_sources(c, c.pp);
+    for (int i = 1; i <= nC; ++i) c.u[i] = c.u[i] + c.su[i] * c.apu[i];
+    for (int i = 1; i <= nC; ++i) c.v[i] = c.v[i] + c.sv[i] * c.apv[i];
+    for (int i = 1; i <= nC; ++i) c.w[i] = c.w[i] + c.sw[i] * c.apw[i];
+    for (int i = 1; i <= nC; ++i) c.p[i] = c.p[i] + c.urfP * (c.pp[i] - ppref);
+    updateVelocityAtBoundary(c);
+    if (ipcorr != c.npcor) {
+      std::fill(c.su.begin(), c.su.end(), 0.0);
+      for (int i = 1; i <= c.numInnerFaces; ++i) {
+        int ijp = c.owner[i], ijn = c.neighbour[i];
+        double fmcor;
+        fluxmc2(c, ijp, ijn, c.arx[i], c.ary[i], c.arz[i], fmcor);
+        c.flmass[i] = c.flmass[i] + fmcor;
+        c.su[ijp] = c.su[ijp] - fmcor;
+        c.su[ijn] = c.su[ijn] + fmcor;
+      }
+    }
+  }
+  continuityErrors(c);
+  return worst;
+}
+
+}  // namespace orc

@@ -1,0 +1,75 @@
+"""C-ABI library: it builds, loads and exports every declared entry point;
+host-side mesh logic (no GPU needed)."""
+import ctypes as C
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+
+def test_library_exports_every_declared_symbol(fc):
+    L = fc.lib()
+    names = fc.declared_symbols()
+    assert "fc_csrsolve" in names and "fc_set_mesh" in names
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_no_gpu_calls_fail_cleanly_without_device(fc):
+    # fc_init must either succeed (GPU present) or return an error code
+    h = C.c_void_p()
+    st = fc.lib().fc_init(0, C.byref(h))
+    if st == 0:
+        fc.lib().fc_finalize(h)
+    else:
+        assert st < 0
+
+
+@pytest.mark.parametrize("n,tets", [((3, 2, 2), False), ((2, 2, 2), True), ((5, 4, 3), False)])
+def test_box_mesh_counts_and_orientation(fc, n, tets):
+    nx, ny, nz = n
+    m = fc.Mesh.box(nx, ny, nz, 1.0, 1.0, 1.0, perturb=0.1, seed=7, tets=tets)
+    a = m.arrays()
+    ncell = nx * ny * nz * (6 if tets else 1)
+    assert m.numCells == ncell
+    if not tets:
+        assert m.numInnerFaces == (nx - 1) * ny * nz + nx * (ny - 1) * nz + nx * ny * (nz - 1)
+        assert m.numBoundaryFaces == 2 * (nx * ny + ny * nz + nx * nz)
+    else:
+        assert 4 * ncell == 2 * m.numInnerFaces + m.numBoundaryFaces
+        assert m.numBoundaryFaces == 4 * (nx * ny + ny * nz + nx * nz)
+    own, nb = a["owner"], a["neighbour"]
+    assert np.all(own[:m.numInnerFaces] < nb)
+    key = own[:m.numInnerFaces].astype(np.int64) * (ncell + 1) + nb
+    assert np.all(np.diff(key) > 0), "inner faces sorted by (owner, neighbour)"
+    assert list(a["startFace"]) == list(np.cumsum([m.numInnerFaces] + list(a["nfaces"][:-1])))
+
+
+def test_native_format_roundtrip(fc):
+    m = fc.Mesh.box(3, 3, 2, 2.0, 1.0, 1.0, perturb=0.15, seed=3, sides=["wall", "outlet", "wall", "wall",
+                                                                           "symmetry", "symmetry"])
+    with tempfile.TemporaryDirectory() as d:
+        m.write_native(d)
+        assert sorted(os.listdir(d)) == ["boundary", "faces", "neighbour", "owner", "points", "size"]
+        m2 = fc.Mesh.read_native(d)
+    a, b = m.arrays(), m2.arrays()
+    for k in ("x", "y", "z", "nnodes", "nodes", "owner", "neighbour", "bctype", "nfaces", "startFace"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+
+
+def test_perturbation_is_seeded(fc):
+    a = fc.Mesh.box(4, 4, 4, perturb=0.15, seed=42).arrays()
+    b = fc.Mesh.box(4, 4, 4, perturb=0.15, seed=42).arrays()
+    c = fc.Mesh.box(4, 4, 4, perturb=0.15, seed=43).arrays()
+    np.testing.assert_array_equal(a["x"], b["x"])
+    assert np.abs(a["x"] - c["x"]).max() > 0
+
+
+def test_mesh_rejects_bad_input(fc):
+    m = fc.Mesh.box(2, 2, 2).arrays()
+    bad = dict(m)
+    bad["owner"] = m["owner"].copy()
+    bad["owner"][0] = 999
+    with pytest.raises(fc.FcError):
+        fc.Mesh.from_arrays(bad)

@@ -1,0 +1,147 @@
+"""GPU solvers vs the oracle (the CPU restatement of linear_solvers.f90).
+
+Tolerances: the DIC/DILU factors, the preconditioner application, the ILU(0)
+factors and A^T x follow the reference's recurrences operation by operation
+without FMA contraction, so they are compared bit for bit.  Solver results
+differ only through the order of the FP64 dot/norm reductions and FMA in
+A*x: iterates agree to 1e-9 relative after tens of iterations and the
+converged fields to 1e-8 relative (the required bar).
+"""
+import json
+
+import numpy as np
+import pytest
+
+from conftest import golden_path
+from gpu_cases import laplacian_system, mesh_case, nonsymmetric_values
+
+pytestmark = pytest.mark.gpu
+KAT = json.load(open(golden_path("spsolve_5x5.json")))
+
+
+@pytest.mark.parametrize("system,solver", [("nonsymmetric", "bicgstab"), ("spd", "iccg"), ("spd", "dpcg"),
+                                           ("spd", "gauss-seidel"), ("nonsymmetric", "pmgmres")])
+def test_reference_5x5_systems(ctx, oracle, system, solver):
+    s = KAT[system]
+    itr = KAT["itr_max_gauss_seidel"] if solver == "gauss-seidel" else KAT["itr_max"]
+    args = (s["ia"], s["ja"], s["a"], s["diag"], np.zeros(5), s["b"], itr, KAT["tol_abs"], KAT["tol_rel"])
+    xo, r0o, info_o, _ = oracle.solve(solver, *args)
+    x, r0, info, st = ctx.csrsolve(solver, *args)
+    assert st >= 0
+    np.testing.assert_allclose(x, xo, rtol=1e-9, atol=1e-12)
+    assert info.itr_used == int(info_o[0])
+    if solver != "pmgmres":  # gmres as written misses the printed answer (see the oracle test)
+        np.testing.assert_allclose(x, s["x_expected"], atol=0.006)
+        assert r0 == pytest.approx(r0o, rel=1e-12)
+
+
+@pytest.mark.parametrize("mesh", ["hex", "tet"])
+@pytest.mark.parametrize("kind", ["dic", "dilu"])
+def test_preconditioner_bit_exact(ctx, oracle, mesh, kind):
+    m, a, oc = mesh_case(mesh, 9, 7, 6, tets=(mesh == "tet"))
+    if kind == "dic":
+        ia, ja, av, dg, b = laplacian_system(oc, mask=0b1)
+    else:
+        ia, ja, av, dg = nonsymmetric_values(oc)
+        b = np.random.default_rng(9).standard_normal(len(dg))
+    d_gpu = ctx.precond_setup(kind, ia, ja, av, dg)
+    d_ref = oracle.dic_setup(ia, ja, av, dg, dilu=(kind == "dilu"))
+    assert np.array_equal(d_gpu, d_ref)
+    z_gpu = ctx.precond_apply(kind, ia, ja, av, dg, b)
+    z_ref = oracle.precond_apply(ia, ja, av, dg, d_ref, b)
+    assert np.array_equal(z_gpu, z_ref)
+
+
+def test_spmv_and_transpose(ctx, oracle):
+    m, a, oc = mesh_case("hex", 9, 7, 6)
+    ia, ja, av, dg = nonsymmetric_values(oc)
+    x = np.random.default_rng(1).standard_normal(len(dg))
+    y = ctx.spmv(ia, ja, av, dg, x)
+    np.testing.assert_allclose(y, oracle.spmv(ia, ja, av, x), rtol=1e-14, atol=1e-14)
+    yt = ctx.spmv(ia, ja, av, dg, x, transpose=True)
+    assert np.array_equal(yt, oracle.spmv(ia, ja, av, x, transpose=True))
+
+
+def test_ilu0_factors_bit_exact(ctx, oracle):
+    m, a, oc = mesh_case("hex", 9, 7, 6)
+    ia, ja, av, dg = nonsymmetric_values(oc)
+    l_gpu = ctx.ilu0(ia, ja, av, dg)
+    l_ref = np.zeros(len(ja))
+    L = oracle.lib()
+    assert L.orc_ilu0(len(dg), oracle._i32(ia), oracle._i32(ja), oracle._f64(av), oracle._i32(dg), l_ref,
+                      np.zeros(len(dg), np.int32)) == 0
+    assert np.array_equal(l_gpu, l_ref)
+
+
+@pytest.mark.parametrize("solver,itr", [("iccg", 30), ("dpcg", 30), ("gauss-seidel", 25), ("bicgstab", 15),
+                                        ("pmgmres", 6)])
+def test_solver_iterates_match_oracle(ctx, oracle, solver, itr):
+    m, a, oc = mesh_case("hex", 9, 7, 6)
+    if solver in ("iccg", "dpcg", "gauss-seidel"):
+        ia, ja, av, dg, b = laplacian_system(oc, mask=0b1)
+    else:
+        ia, ja, av, dg = nonsymmetric_values(oc)
+        b = np.random.default_rng(3).standard_normal(len(dg))
+    x0 = np.random.default_rng(4).standard_normal(len(dg)) * 0.1
+    args = (ia, ja, av, dg, x0, b, itr, 1e-30, 1e-30)
+    xo, r0o, info_o, _ = oracle.solve(solver, *args)
+    x, r0, info, st = ctx.csrsolve(solver, *args)
+    assert st >= 0
+    assert info.itr_used == int(info_o[0])
+    np.testing.assert_allclose(x, xo, rtol=1e-9, atol=1e-9 * np.abs(xo).max())
+    assert r0 == pytest.approx(r0o, rel=1e-12)
+
+
+@pytest.mark.parametrize("mesh", ["hex", "tet"])
+def test_converged_iccg_and_bicgstab_fields(ctx, oracle, mesh):
+    m, a, oc = mesh_case(mesh + "c", 12, 10, 9, tets=(mesh == "tet"))
+    ia, ja, av, dg, b = laplacian_system(oc, mask=0b1)
+    for solver in ("iccg", "bicgstab"):
+        xo, _, info_o, _ = oracle.solve(solver, ia, ja, av, dg, np.zeros(len(dg)), b, 4000, 0.0, 1e-10)
+        x, _, info, st = ctx.csrsolve(solver, ia, ja, av, dg, np.zeros(len(dg)), b, 4000, 0.0, 1e-10)
+        assert st == 0
+        assert abs(info.itr_used - int(info_o[0])) <= 1
+        assert np.abs(x - xo).max() <= 1e-8 * np.abs(xo).max()
+
+
+def test_mixed_precision_reaches_fp64_tolerance(ctx, oracle):
+    m, a, oc = mesh_case("hexm", 14, 12, 10)
+    ia, ja, av, dg, b = laplacian_system(oc, mask=0b1)
+    xo, _, _, _ = oracle.solve("iccg", ia, ja, av, dg, np.zeros(len(dg)), b, 5000, 0.0, 1e-10)
+    ctx.set_precision(1, 1e-4, 0)
+    try:
+        x, _, info, st = ctx.csrsolve("iccg", ia, ja, av, dg, np.zeros(len(dg)), b, 5000, 0.0, 1e-10)
+    finally:
+        ctx.set_precision(0)
+    assert st == 0 and info.outer_iterations >= 2
+    # reached the reference's stopping criterion in FP64
+    r = b - oracle.spmv(ia, ja, av, x)
+    assert np.abs(r).sum() / info.res0_l1 < 1e-10
+    assert np.abs(x - xo).max() <= 1e-7 * np.abs(xo).max()
+
+
+def test_failure_detection_nan_rhs(ctx, fc):
+    m, a, oc = mesh_case("hex", 9, 7, 6)
+    ia, ja, av, dg, b = laplacian_system(oc, mask=0b1)
+    b = b.copy()
+    b[5] = np.nan
+    x, r0, info, st = ctx.csrsolve("iccg", ia, ja, av, dg, np.zeros(len(dg)), b, 50, 0.0, 1e-8,
+                                   raise_on_error=False)
+    assert st == fc.FC_ERR_NAN
+    # the context stays usable afterwards
+    ia, ja, av, dg, b = laplacian_system(oc, mask=0b1)
+    x, r0, info, st = ctx.csrsolve("iccg", ia, ja, av, dg, np.zeros(len(dg)), b, 50, 0.0, 1e-8)
+    assert st >= 0
+
+
+def test_failure_detection_bad_pattern_and_zero_pivot(ctx, fc):
+    ia = np.array([1, 2, 3], np.int32)
+    ja = np.array([1, 3], np.int32)  # column out of range
+    with pytest.raises(fc.FcError) as e:
+        ctx.csrsolve("iccg", ia, ja, [1.0, 1.0], np.array([1, 2], np.int32), np.zeros(2), np.ones(2), 5, 0, 1e-6)
+    assert e.value.code == fc.FC_ERR_BAD_INPUT
+    ia = np.array([1, 3, 5], np.int32)
+    ja = np.array([1, 2, 1, 2], np.int32)
+    with pytest.raises(fc.FcError) as e:
+        ctx.ilu0(ia, ja, [0.0, 1.0, 1.0, 1.0], np.array([1, 4], np.int32))
+    assert e.value.code == fc.FC_ERR_ZERO_PIVOT

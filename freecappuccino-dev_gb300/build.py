@@ -20,6 +20,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I" + INCLUDE, "-I" + CSRC, "-I" + HOST]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + INCLUDE, "-I" + HOST, "-I" + CSRC]
+# Translation units whose FP64 expressions are written in the reference's
+# evaluation order and must not be contracted into FMAs.
+PER_FILE = {"fc_simple.cu": ["--fmad=false"]}
 
 
 def _nvcc():
@@ -55,7 +58,7 @@ def build(verbose=False, jobs=None):
         o = os.path.join(BUILD, os.path.basename(s) + ".o")
         objs.append(o)
         if _stale(o, [s] + headers):
-            cmds.append([nvcc] + ARCH + NVCC_FLAGS + ["-c", s, "-o", o])
+            cmds.append([nvcc] + ARCH + NVCC_FLAGS + PER_FILE.get(os.path.basename(s), []) + ["-c", s, "-o", o])
     for s in cpp:
         o = os.path.join(BUILD, os.path.basename(s) + ".o")
         objs.append(o)

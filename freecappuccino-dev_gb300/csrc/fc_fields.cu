@@ -27,6 +27,7 @@ int fc_fields_alloc(fc_ctx* ctx) {
   const size_t nT = m.numTotal, nC = m.numCells, nF = m.numFaces, nI = m.numInnerFaces;
   const size_t nW = m.nwal > 0 ? m.nwal : 1;
   F.list.clear();
+  F.dmat_scheme = 0;  // least-squares cofactors belong to the previous mesh
   auto add = [&](const char* name, DVec<double>* v, size_t n, int kind) {
     FieldSlot s;
     s.name = name; s.vec = v; s.n = n; s.kind = kind;

@@ -104,6 +104,7 @@ struct MeshDev {
 };
 
 struct FieldStore;
+struct SimpleState;
 
 struct fc_ctx {
   int device = 0;
@@ -116,10 +117,12 @@ struct fc_ctx {
   int inner_itmax = 0; double inner_tol = 0.0;
   MeshDev mesh;
   bool has_mesh = false;
+  int mesh_gen = 0;    // incremented by every fc_set_mesh
   CsrSystem* sys_ext = nullptr;    // pattern cache of fc_csrsolve
   CsrSystem* sys_mesh = nullptr;   // global matrix of the mesh (sparse_matrix module)
   std::vector<CsrSystem*> sys_user;
   FieldStore* fields = nullptr;
+  SimpleState* simple = nullptr;
   long long kernel_launches = 0;
 };
 

@@ -280,6 +280,7 @@ extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
   FC_CUDA_TRY(ctx, cudaMemset(s->a.p, 0, (size_t)nnz * sizeof(double)));
   ctx->sys_mesh = s;
   ctx->has_mesh = true;
+  ctx->mesh_gen++;
   return fc_fields_alloc(ctx);
 }
 

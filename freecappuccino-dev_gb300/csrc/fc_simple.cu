@@ -1,0 +1,813 @@
+// The SIMPLE path on the device: pressure gradient and sources
+// (Pressure/nablap.f90, bpres.f90), momentum assembly (Velocity/velocity.f90
+// calcuvw, facefluxuvw, facefluxuvw_bnd, updateVelocityAtBoundary), the SIMPLE
+// pressure correction (Pressure/calcp_simple.f90 with fluxes/faceflux_mass.f90
+// facefluxmass2, fluxmc2, adjustMassFlow and continuityErrors.f90) and the
+// mass-flux initialisation of init.f90.
+//
+// This translation unit is compiled with --fmad=false: the expressions below
+// are written in the reference's evaluation order and evaluate exactly as the
+// reference does in FP64.  Face loops that scatter into cells are split into
+// a face-parallel kernel (matrix slots through the face -> CSR maps, per-face
+// source terms to scratch) and a cell-parallel gather over the cell's faces
+// in ascending face index, which reproduces the reference's summation order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "fc_fields.hpp"
+#include "fc_fv.cuh"
+#include "fc_internal.hpp"
+
+using namespace fcfv;
+
+namespace {
+
+constexpr double SMALL = FC_SMALL;
+
+struct Fld {  // SoA gradient access
+  const double* g;
+  int nT;
+  __device__ double x(int i) const { return g[i]; }
+  __device__ double y(int i) const { return g[nT + i]; }
+  __device__ double z(int i) const { return g[2 * (size_t)nT + i]; }
+};
+
+// ------------------------------------------------------------ interpolation
+// face_value_flux_limiter, interpolation.f90:489-650
+__device__ double fv_flux_limiter(const MeshView& M, int ijp, int ijn, double lambda, const double* u, Fld g,
+                                  int scheme) {
+  const double fxp = 1.0 - lambda;
+  double psi = 1.0;
+  const double xpn = M.xc[ijn] - M.xc[ijp], ypn = M.yc[ijn] - M.yc[ijp], zpn = M.zc[ijn] - M.zc[ijp];
+  const double r = (2 * g.x(ijp) * xpn + 2 * g.y(ijp) * ypn + 2 * g.z(ijp) * zpn) /
+                       (u[ijn] - u[ijp] + (double)1e-30f) - 1.0;
+  const double two3s = (double)(2.0f / 3.0f), one3s = (double)(1.0f / 3.0f);
+  const double two3d = 2.0 / 3.0, one3d = 1.0 / 3.0;
+  switch (scheme) {
+    case FC_SCHEME_MUSCL: psi = fmax(0.0, fmin(fmin(2 * r, 0.5 * r + 0.5), 2.0)); break;
+    case FC_SCHEME_UMIST: psi = fmax(0.0, fmin(fmin(fmin(2 * r, 0.75 * r + 0.25), 0.25 * r + 0.75), 2.0)); break;
+    case FC_SCHEME_KOREN: psi = fmax(0.0, fmin(fmin(2 * r, two3d * r + one3d), 2.0)); break;
+    case FC_SCHEME_SMART: psi = fmax(0.0, fmin(fmin(2 * r, 0.75 * r + 0.25), 4.0)); break;
+    case FC_SCHEME_AVLSMART: psi = fmax(0.0, fmin(fmin(1.5 * r, 0.75 * r + 0.25), 2.5)); break;
+    case FC_SCHEME_CHARM: psi = fmax(0.0, (r + fabs(r)) * (3 * r + 1.0) / (2 * ((r + 1.0) * (r + 1.0)))); break;
+    case FC_SCHEME_VANLEER: psi = fmax(0.0, fmin((r + fabs(r)) / (r + 1.0), 2.0)); break;
+    case FC_SCHEME_OSPRE: psi = fmax(0.0, 3 * r * (r + 1.0) / (2 * (r * r + r + 1.0))); break;
+    case FC_SCHEME_MINMOD: psi = fmax(0.0, fmin(r, 1.0)); break;
+    case FC_SCHEME_BOUNDED_LINEAR_UPWIND: psi = fmax(0.0, fmin(2 * r, 1.0)); break;
+    case FC_SCHEME_BOUNDED_LINEAR_UPWIND02: psi = fmax(0.0, fmin(10 * r, 1.0)); break;
+    case FC_SCHEME_BOUNDED_CENTRAL: psi = fmax(0.0, fmin(r, 4.0)); break;
+    case FC_SCHEME_FROMM: psi = 0.5 * r + 0.5; break;
+    case FC_SCHEME_CUI: psi = two3s * r + one3s; break;
+    case FC_SCHEME_QUICK: psi = 0.75 * r + 0.25; break;
+    case FC_SCHEME_SPL13: psi = fmax(0.0, fmin(fmin(fmin(2 * r, one3s * r + two3s), two3s * r + one3s), 2.0)); break;
+    default: psi = 1.0;
+  }
+  return u[ijp] + fxp * psi * (u[ijn] - u[ijp]);
+}
+
+// face_value, interpolation.f90:28-113
+__device__ double face_value(const MeshView& M, int ijp, int ijn, double xf, double yf, double zf, double lambda,
+                             const double* u, Fld g, int scheme) {
+  switch (scheme) {
+    case FC_SCHEME_CDS:
+      return u[ijp] + (u[ijn] - u[ijp]) * lambda;
+    case FC_SCHEME_CENTRAL: {
+      const double gr = g.x(ijp) * (xf - M.xc[ijp]) + g.y(ijp) * (yf - M.yc[ijp]) + g.z(ijp) * (zf - M.zc[ijp]) +
+                        g.x(ijn) * (xf - M.xc[ijn]) + g.y(ijn) * (yf - M.yc[ijn]) + g.z(ijn) * (zf - M.zc[ijn]);
+      return 0.5 * (u[ijp] + u[ijn] + gr);
+    }
+    case FC_SCHEME_LINEAR_UPWIND: {
+      const double gr = g.x(ijp) * (xf - M.xc[ijp]) + g.y(ijp) * (yf - M.yc[ijp]) + g.z(ijp) * (zf - M.zc[ijp]);
+      return u[ijp] + gr;
+    }
+    case FC_SCHEME_KAPPA: {
+      const double theta = (double)(2.0f / 3.0f);
+      const double g2 = g.x(ijp) * (xf - M.xc[ijp]) + g.y(ijp) * (yf - M.yc[ijp]) + g.z(ijp) * (zf - M.zc[ijp]);
+      const double gc = g.x(ijp) * (xf - M.xc[ijp]) + g.y(ijp) * (yf - M.yc[ijp]) + g.z(ijp) * (zf - M.zc[ijp]) +
+                        g.x(ijn) * (xf - M.xc[ijn]) + g.y(ijn) * (yf - M.yc[ijn]) + g.z(ijn) * (zf - M.zc[ijn]);
+      const double vf2 = (u[ijp] + g2);
+      const double vfc = 0.5 * (u[ijp] + u[ijn] + gc);
+      return theta * vfc + (1.0 - theta) * vf2;
+    }
+    default:
+      return fv_flux_limiter(M, ijp, ijn, lambda, u, g, scheme);
+  }
+}
+
+struct Dev {  // per-call device pointers of the fields
+  double *u, *v, *w, *p, *pp, *vis, *den, *flmass, *visw;
+  double *su, *sv, *sw, *spu, *spv, *sp, *apu, *apv, *apw;
+  double *gu, *gv, *gw, *gp;
+  double* a;
+  double* fscr;
+  const int* ptype;  // FC_BC_* per patch
+};
+
+// ------------------------------------------------------- boundary updates
+// updateVelocityAtBoundary, velocity.f90:1184-1279 (the symmetry projection
+// uses the area vector as written there)
+__global__ void k_update_vel_bnd(MeshView M, Dev D) {
+  for (int bi = blockIdx.x * blockDim.x + threadIdx.x; bi < M.nB; bi += gridDim.x * blockDim.x) {
+    const int t = D.ptype[M.bpatch[bi]];
+    const int f = M.nI + bi, p = M.owner[f], b = M.nC + bi;
+    if (t == FC_BC_EMPTY || t == FC_BC_PERIODIC) {
+      D.u[b] = D.u[p]; D.v[b] = D.v[p]; D.w[b] = D.w[p];
+    } else if (t == FC_BC_SYMMETRY) {
+      const double Unmag = D.u[p] * M.arx[f] + D.v[p] * M.ary[f] + D.w[p] * M.arz[f];
+      D.u[b] = D.u[p] - Unmag * M.arx[f];
+      D.v[b] = D.v[p] - Unmag * M.ary[f];
+      D.w[b] = D.w[p] - Unmag * M.arz[f];
+    }
+  }
+}
+
+// bpres, bpres.f90:55-180
+__global__ void k_bpres(MeshView M, const int* __restrict__ ptype, double* __restrict__ p, Fld g, int stage) {
+  for (int bi = blockIdx.x * blockDim.x + threadIdx.x; bi < M.nB; bi += gridDim.x * blockDim.x) {
+    const int t = ptype[M.bpatch[bi]];
+    const int f = M.nI + bi, c = M.owner[f];
+    if (stage == 1) {
+      if (t != FC_BC_PRESSURE) p[M.nC + bi] = p[c];
+    } else if (t == FC_BC_WALL) {
+      const double xpb = M.xf[f] - M.xc[c], ypb = M.yf[f] - M.yc[c], zpb = M.zf[f] - M.zc[c];
+      p[M.nC + bi] = p[c] + g.x(c) * xpb + g.y(c) * ypb + g.z(c) * zpb;
+    }
+  }
+}
+
+// -sum_f p_f S_f over inner faces (nablap.f90:52-108), cell gather
+__global__ void k_gp_inner(MeshView M, const double* __restrict__ p, Fld gp, const double* __restrict__ apu, int mode,
+                           double* __restrict__ su, double* __restrict__ sv, double* __restrict__ sw) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int q = M.cf_ptr[c]; q < M.cf_ptr[c + 1]; ++q) {
+      const int f = M.cf_face[q];
+      if (f >= M.nI) break;
+      const int ijp = M.owner[f], ijn = M.neighbour[f];
+      double pf;
+      if (mode == 0) pf = p[ijp] + (p[ijn] - p[ijp]) * M.facint[f];
+      else if (mode == 1) pf = face_value(M, ijp, ijn, M.xf[f], M.yf[f], M.zf[f], M.facint[f], p, gp, FC_SCHEME_CENTRAL);
+      else pf = (p[ijp] * apu[ijp] + p[ijn] * apu[ijn]) / (apu[ijp] + apu[ijn] + SMALL);
+      const double dfxe = pf * M.arx[f], dfye = pf * M.ary[f], dfze = pf * M.arz[f];
+      if (ijp == c) { sx = sx - dfxe; sy = sy - dfye; sz = sz - dfze; }
+      else { sx = sx + dfxe; sy = sy + dfye; sz = sz + dfze; }
+    }
+    su[c] = sx; sv[c] = sy; sw[c] = sz;
+  }
+}
+
+// dPdxi from the accumulated sources plus boundary faces, /vol (nablap.f90:145-172)
+__global__ void k_gp_grad(MeshView M, const double* __restrict__ p, const double* __restrict__ su,
+                          const double* __restrict__ sv, const double* __restrict__ sw, double* __restrict__ g) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
+    double gx = -su[c], gy = -sv[c], gz = -sw[c];
+    for (int q = M.cf_ptr[c]; q < M.cf_ptr[c + 1]; ++q) {
+      const int f = M.cf_face[q];
+      if (f < M.nI) continue;
+      const double pb = p[M.nC + (f - M.nI)];
+      gx = gx + pb * M.arx[f]; gy = gy + pb * M.ary[f]; gz = gz + pb * M.arz[f];
+    }
+    const double volr = 1.0 / M.vol[c];
+    g[c] = gx * volr;
+    g[M.nT + c] = gy * volr;
+    g[2 * (size_t)M.nT + c] = gz * volr;
+  }
+}
+
+// su,sv,sw -= p_b S_b over boundary faces (nablap.f90:176-186)
+__global__ void k_gp_final(MeshView M, const double* __restrict__ p, double* __restrict__ su, double* __restrict__ sv,
+                           double* __restrict__ sw) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
+    double sx = su[c], sy = sv[c], sz = sw[c];
+    bool any = false;
+    for (int q = M.cf_ptr[c]; q < M.cf_ptr[c + 1]; ++q) {
+      const int f = M.cf_face[q];
+      if (f < M.nI) continue;
+      const double pb = p[M.nC + (f - M.nI)];
+      sx = sx - pb * M.arx[f]; sy = sy - pb * M.ary[f]; sz = sz - pb * M.arz[f];
+      any = true;
+    }
+    if (any) { su[c] = sx; sv[c] = sy; sw[c] = sz; }
+  }
+}
+
+// ------------------------------------------------------------- momentum
+struct MomParams {
+  double gds, viscos;
+  int scheme;
+  double vis_sym;  // vis(inp) with inp = numCells+1 after the cell loop (velocity.f90:379)
+};
+
+// sngrad (variant 1), gradients.f90:1720-1779
+__device__ __forceinline__ void sngrad(const MeshView& M, int i, int ijp, int ijn, double arx, double ary, double arz,
+                                       double lambda, const double* Phi, Fld dPhidxi, double& dfixi, double& dfiyi,
+                                       double& dfizi, double& dfixii, double& dfiyii, double& dfizii) {
+  const double fxn = lambda, fxp = 1.0 - lambda;
+  const double xpn = M.xc[ijn] - M.xc[ijp], ypn = M.yc[ijn] - M.yc[ijp], zpn = M.zc[ijn] - M.zc[ijp];
+  const double vole = xpn * arx + ypn * ary + zpn * arz;
+  dfixi = dPhidxi.x(ijp) * fxp + dPhidxi.x(ijn) * fxn;
+  dfiyi = dPhidxi.y(ijp) * fxp + dPhidxi.y(ijn) * fxn;
+  dfizi = dPhidxi.z(ijp) * fxp + dPhidxi.z(ijn) * fxn;
+  dfixii = dfixi + arx / vole * (Phi[ijn] - Phi[ijp] - dfixi * xpn - dfiyi * ypn - dfizi * zpn);
+  dfiyii = dfiyi + ary / vole * (Phi[ijn] - Phi[ijp] - dfixi * xpn - dfiyi * ypn - dfizi * zpn);
+  dfizii = dfizi + arz / vole * (Phi[ijn] - Phi[ijp] - dfixi * xpn - dfiyi * ypn - dfizi * zpn);
+  dfixi = dfixi * (arx - M.Df[i] * xpn);
+  dfiyi = dfiyi * (ary - M.Df[i] * ypn);
+  dfizi = dfizi * (arz - M.Df[i] * zpn);
+}
+
+// facefluxuvw, velocity.f90:754-878: a(k_ij)=can, a(k_ji)=cap; sources to scratch
+__global__ void k_mom_face(MeshView M, Dev D, MomParams P) {
+  const int nT = M.nT;
+  const Fld gu{D.gu, nT}, gv{D.gv, nT}, gw{D.gw, nT};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M.nI; i += gridDim.x * blockDim.x) {
+    const int ijp = M.owner[i], ijn = M.neighbour[i];
+    const double xf = M.xf[i], yf = M.yf[i], zf = M.zf[i];
+    const double arx = M.arx[i], ary = M.ary[i], arz = M.arz[i];
+    const double flomass = D.flmass[i], lambda = M.facint[i], gam = P.gds;
+    const double fxn = lambda, fxp = 1.0 - lambda;
+    const double game = D.vis[ijp] + (D.vis[ijn] - D.vis[ijp]) * lambda;
+    const double de = game * M.Df[i];
+    const double ce = fmin(flomass, 0.0), cp = fmax(flomass, 0.0);
+    const double can = -de + ce;
+    const double cap = -de - cp;
+    double duxi, duyi, duzi, duxii, duyii, duzii, dvxi, dvyi, dvzi, dvxii, dvyii, dvzii, dwxi, dwyi, dwzi, dwxii,
+        dwyii, dwzii;
+    sngrad(M, i, ijp, ijn, arx, ary, arz, lambda, D.u, gu, duxi, duyi, duzi, duxii, duyii, duzii);
+    sngrad(M, i, ijp, ijn, arx, ary, arz, lambda, D.v, gv, dvxi, dvyi, dvzi, dvxii, dvyii, dvzii);
+    sngrad(M, i, ijp, ijn, arx, ary, arz, lambda, D.w, gw, dwxi, dwyi, dwzi, dwxii, dwyii, dwzii);
+    double fdue = game * (duxii * arx + dvxii * ary + dwxii * arz);
+    double fdve = game * (duyii * arx + dvyii * ary + dwyii * arz);
+    double fdwe = game * (duzii * arx + dvzii * ary + dwzii * arz);
+    const double fdui = game * (duxi + duyi + duzi);
+    const double fdvi = game * (dvxi + dvyi + dvzi);
+    const double fdwi = game * (dwxi + dwyi + dwzi);
+    fdue = fdue + fdui;
+    fdve = fdve + fdvi;
+    fdwe = fdwe + fdwi;
+    const double fuuds = cp * D.u[ijp] + ce * D.u[ijn];
+    const double fvuds = cp * D.v[ijp] + ce * D.v[ijn];
+    const double fwuds = cp * D.w[ijp] + ce * D.w[ijn];
+    double ue, ve, we;
+    if (flomass >= 0.0) {
+      ue = face_value(M, ijp, ijn, xf, yf, zf, fxp, D.u, gu, P.scheme);
+      ve = face_value(M, ijp, ijn, xf, yf, zf, fxp, D.v, gv, P.scheme);
+      we = face_value(M, ijp, ijn, xf, yf, zf, fxp, D.w, gw, P.scheme);
+    } else {
+      ue = face_value(M, ijn, ijp, xf, yf, zf, fxn, D.u, gu, P.scheme);
+      ve = face_value(M, ijn, ijp, xf, yf, zf, fxn, D.v, gv, P.scheme);
+      we = face_value(M, ijn, ijp, xf, yf, zf, fxn, D.w, gw, P.scheme);
+    }
+    const double fuhigh = flomass * ue, fvhigh = flomass * ve, fwhigh = flomass * we;
+    D.a[M.ijk[i]] = can;
+    D.a[M.jik[i]] = cap;
+    D.fscr[i] = -(gam * (fuhigh - fuuds)) + fdue;
+    D.fscr[M.nI + i] = -(gam * (fvhigh - fvuds)) + fdve;
+    D.fscr[2 * (size_t)M.nI + i] = -(gam * (fwhigh - fwuds)) + fdwe;
+  }
+}
+
+// facefluxuvw_bnd, velocity.f90:882-1034
+__device__ void facefluxuvw_bnd(const MeshView& M, const Dev& D, int ijp, int ijb, int f, double& cb, double& sup,
+                                double& svp, double& swp) {
+  const int nT = M.nT;
+  const double xf = M.xf[f], yf = M.yf[f], zf = M.zf[f], arx = M.arx[f], ary = M.ary[f], arz = M.arz[f];
+  const double flomass = D.flmass[f];
+  const double xpn = xf - M.xc[ijp], ypn = yf - M.yc[ijp], zpn = zf - M.zc[ijp];
+  const double vole = xpn * arx + ypn * ary + zpn * arz;
+  const double Dfi = (arx * arx + ary * ary + arz * arz) / vole;
+  const double game = D.vis[ijb];
+  const double de = game * Dfi;
+  cb = -de + fmin(flomass, 0.0);  // 'can' of the reference, returned as cb
+  double comp[3][6];
+  const double* flds[3] = {D.u, D.v, D.w};
+  const double* grads[3] = {D.gu, D.gv, D.gw};
+  for (int q = 0; q < 3; ++q) {
+    const double* F = flds[q];
+    const Fld g{grads[q], nT};
+    double dxi = g.x(ijp), dyi = g.y(ijp), dzi = g.z(ijp);
+    const double dxii = dxi + arx / vole * (F[ijb] - F[ijp] - dxi * xpn - dyi * ypn - dzi * zpn);
+    const double dyii = dyi + ary / vole * (F[ijb] - F[ijp] - dxi * xpn - dyi * ypn - dzi * zpn);
+    const double dzii = dzi + arz / vole * (F[ijb] - F[ijp] - dxi * xpn - dyi * ypn - dzi * zpn);
+    dxi = dxi * (arx - Dfi * xpn);
+    dyi = dyi * (ary - Dfi * ypn);
+    dzi = dzi * (arz - Dfi * zpn);
+    comp[q][0] = dxi; comp[q][1] = dyi; comp[q][2] = dzi;
+    comp[q][3] = dxii; comp[q][4] = dyii; comp[q][5] = dzii;
+  }
+  const double fdue = game * (comp[0][3] * arx + comp[1][3] * ary + comp[2][3] * arz);
+  const double fdve = game * (comp[0][4] * arx + comp[1][4] * ary + comp[2][4] * arz);
+  const double fdwe = game * (comp[0][5] * arx + comp[1][5] * ary + comp[2][5] * arz);
+  const double fdui = game * (comp[0][0] + comp[0][1] + comp[0][2]);
+  const double fdvi = game * (comp[1][0] + comp[1][1] + comp[1][2]);
+  const double fdwi = game * (comp[2][0] + comp[2][1] + comp[2][2]);
+  sup = fdue + fdui;
+  svp = fdve + fdvi;
+  swp = fdwe + fdwi;
+}
+
+// sources and diagonal contributions per cell: inner-face sources in face
+// order (velocity.f90:306-313), then the boundary conditions (:326-562)
+__global__ void k_mom_cell(MeshView M, Dev D, MomParams P) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
+    double su = D.su[c], sv = D.sv[c], sw = D.sw[c];
+    double spu = 0.0, spv = 0.0, sp = 0.0;
+    for (int q = M.cf_ptr[c]; q < M.cf_ptr[c + 1]; ++q) {
+      const int f = M.cf_face[q];
+      if (f < M.nI) {
+        const double sup = D.fscr[f], svp = D.fscr[M.nI + f], swp = D.fscr[2 * (size_t)M.nI + f];
+        if (M.owner[f] == c) { su = su + sup; sv = sv + svp; sw = sw + swp; }
+        else { su = su - sup; sv = sv - svp; sw = sw - swp; }
+        continue;
+      }
+      const int bi = f - M.nI, ijb = M.nC + bi, ijp = c;
+      const int t = D.ptype[M.bpatch[bi]];
+      if (t == FC_BC_INLET || t == FC_BC_OUTLET || t == FC_BC_PRESSURE) {
+        double cb, sup, svp, swp;
+        facefluxuvw_bnd(M, D, ijp, ijb, f, cb, sup, svp, swp);
+        spu = spu - cb; spv = spv - cb; sp = sp - cb;
+        su = su - cb * D.u[ijb] + sup;
+        sv = sv - cb * D.v[ijb] + svp;
+        sw = sw - cb * D.w[ijb] + swp;
+      } else if (t == FC_BC_SYMMETRY) {
+        const double are = sqrt(M.arx[f] * M.arx[f] + M.ary[f] * M.ary[f] + M.arz[f] * M.arz[f]);
+        const double arer = 1.0 / are;
+        const double nxf = M.arx[f] * arer, nyf = M.ary[f] * arer, nzf = M.arz[f] * arer;
+        const double dpb = (M.xf[f] - M.xc[ijp]) * nxf + (M.yf[f] - M.yc[ijp]) * nyf + (M.zf[f] - M.zc[ijp]) * nzf;
+        const double cf = 2 * P.vis_sym * are / dpb;
+        su = su - cf * nxf * (nyf * D.v[ijp] + nzf * D.w[ijp]);
+        sv = sv - cf * nyf * (nxf * D.u[ijp] + nzf * D.w[ijp]);
+        sw = sw - cf * nzf * (nxf * D.u[ijp] + nyf * D.v[ijp]);
+        spu = spu + cf * (nxf * nxf);
+        spv = spv + cf * (nyf * nyf);
+        sp = sp + cf * (nzf * nzf);
+      } else if (t == FC_BC_WALL) {
+        const double viss = fmax(P.viscos, D.visw[M.bwall[bi]]);
+        const double are = sqrt(M.arx[f] * M.arx[f] + M.ary[f] * M.ary[f] + M.arz[f] * M.arz[f]);
+        const double arer = 1.0 / are;
+        const double nxf = M.arx[f] * arer, nyf = M.ary[f] * arer, nzf = M.arz[f] * arer;
+        const double dpb = (M.xf[f] - M.xc[ijp]) * nxf + (M.yf[f] - M.yc[ijp]) * nyf + (M.zf[f] - M.zc[ijp]) * nzf;
+        const double vsol = viss * are / dpb;
+        const double upb = D.u[ijp] - D.u[ijb], vpb = D.v[ijp] - D.v[ijb], wpb = D.w[ijp] - D.w[ijb];
+        spu = spu + vsol * (1. - nxf * nxf);
+        spv = spv + vsol * (1. - nyf * nyf);
+        sp = sp + vsol * (1. - nzf * nzf);
+        su = su + vsol * (D.u[ijb] * (1. - nxf * nxf) + vpb * nyf * nxf + wpb * nzf * nxf);
+        sv = sv + vsol * (upb * nxf * nyf + D.v[ijb] * (1. - nyf * nyf) + wpb * nzf * nyf);
+        sw = sw + vsol * (upb * nxf * nzf + vpb * nyf * nzf + D.w[ijb] * (1. - nzf * nzf));
+      }
+    }
+    D.su[c] = su; D.sv[c] = sv; D.sw[c] = sw;
+    D.spu[c] = spu; D.spv[c] = spv; D.sp[c] = sp;
+  }
+}
+
+// main diagonal = sp - sum(off-diagonal row), apx = 1/(a_P + small),
+// under-relaxation (velocity.f90:611-635, :667-690, :722-745).  The U pass
+// subtracts the diagonal slot as found (the previous matrix's value); V and
+// W clear it first.
+__global__ void k_mom_diag(int n, const int* __restrict__ ia, const int* __restrict__ diag, double* __restrict__ a,
+                           const double* __restrict__ spx, double* __restrict__ apx, const double* __restrict__ src,
+                           double* __restrict__ su, const double* __restrict__ fld, double urf, int clear_diag) {
+  const double urfr = 1.0 / urf, urfm = 1.0 - urf;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int kd = diag[i];
+    const double ad0 = clear_diag ? 0.0 : a[kd];
+    double s = 0.0;
+    for (int k = ia[i]; k < ia[i + 1]; ++k) s = s + (k == kd ? ad0 : a[k]);
+    const double off = s - ad0;
+    double ad = spx[i] - off;
+    apx[i] = 1. / (ad + SMALL);
+    ad = ad * urfr;
+    a[kd] = ad;
+    su[i] = src[i] + urfm * ad * fld[i];
+  }
+}
+
+// ------------------------------------------------------------- pressure
+// facefluxmass2, faceflux_mass.f90:175-249 (dPdxi weights as written there)
+__global__ void k_p_face(MeshView M, Dev D) {
+  const Fld gp{D.gp, M.nT};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M.nI; i += gridDim.x * blockDim.x) {
+    const int ijp = M.owner[i], ijn = M.neighbour[i];
+    const double lambda = M.facint[i], fxn = lambda, fxp = 1.0 - lambda;
+    const double xpn = M.xc[ijn] - M.xc[ijp], ypn = M.yc[ijn] - M.yc[ijp], zpn = M.zc[ijn] - M.zc[ijp];
+    const double dene = D.den[ijp] * fxp + D.den[ijn] * fxn;
+    const double Kj = M.vol[ijp] * D.apu[ijp] * fxp + M.vol[ijn] * D.apu[ijn] * fxn;
+    const double cap = -(dene * Kj * M.Df[i]);
+    const double ui = D.u[ijp] + (D.u[ijn] - D.u[ijp]) * lambda;
+    const double vi = D.v[ijp] + (D.v[ijn] - D.v[ijp]) * lambda;
+    const double wi = D.w[ijp] + (D.w[ijn] - D.w[ijp]) * lambda;
+    const double dpxi = (gp.x(ijn) * fxp + gp.x(ijp) * fxn) * xpn;
+    const double dpyi = (gp.y(ijn) * fxp + gp.y(ijp) * fxn) * ypn;
+    const double dpzi = (gp.z(ijn) * fxp + gp.z(ijp) * fxn) * zpn;
+    D.flmass[i] = dene * (ui * M.arx[i] + vi * M.ary[i] + wi * M.arz[i]) +
+                  cap * (D.p[ijn] - D.p[ijp] - dpxi - dpyi - dpzi);
+    D.a[M.ijk[i]] = cap;
+    D.a[M.jik[i]] = cap;
+  }
+}
+
+// diagonal -sum(cap) and source -/+flmass in face order (calcp_simple.f90:104-117),
+// then inlet/outlet mass fluxes (:131-151)
+__global__ void k_p_cell(MeshView M, Dev D) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
+    double ad = 0.0, s = 0.0;
+    for (int q = M.cf_ptr[c]; q < M.cf_ptr[c + 1]; ++q) {
+      const int f = M.cf_face[q];
+      if (f < M.nI) {
+        ad = ad - D.a[M.ijk[f]];
+        if (M.owner[f] == c) s = s - D.flmass[f];
+        else s = s + D.flmass[f];
+      } else {
+        const int t = D.ptype[M.bpatch[f - M.nI]];
+        if (t == FC_BC_INLET || t == FC_BC_OUTLET) s = s - D.flmass[f];
+      }
+    }
+    D.a[M.diag[c]] = ad;
+    D.su[c] = s;
+  }
+}
+
+// adjustMassFlow, faceflux_mass.f90:833-916: one thread, outlet faces in order
+__global__ void k_adjust_mass_flow(MeshView M, Dev D, double flomas) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  double flowo = 0.0;
+  for (int bi = 0; bi < M.nB; ++bi) {
+    if (D.ptype[M.bpatch[bi]] != FC_BC_OUTLET) continue;
+    const int f = M.nI + bi, p = M.owner[f], b = M.nC + bi;
+    D.u[b] = D.u[p]; D.v[b] = D.v[p]; D.w[b] = D.w[p];
+    D.flmass[f] = D.den[p] * (D.u[b] * M.arx[f] + D.v[b] * M.ary[f] + D.w[b] * M.arz[f]);
+    flowo = flowo + D.flmass[f];
+  }
+  const double fac = flomas / (flowo + SMALL);
+  for (int bi = 0; bi < M.nB; ++bi) {
+    if (D.ptype[M.bpatch[bi]] != FC_BC_OUTLET) continue;
+    const int f = M.nI + bi, b = M.nC + bi;
+    D.flmass[f] = D.flmass[f] * fac;
+    D.u[b] = D.u[b] * fac; D.v[b] = D.v[b] * fac; D.w[b] = D.w[b] * fac;
+  }
+}
+
+// flmass += a(k_ij) (pp_N - pp_P)  (calcp_simple.f90:331-341)
+__global__ void k_flux_correct(MeshView M, Dev D) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M.nI; i += gridDim.x * blockDim.x)
+    D.flmass[i] = D.flmass[i] + D.a[M.ijk[i]] * (D.pp[M.neighbour[i]] - D.pp[M.owner[i]]);
+}
+
+// u += su*apu, ..., p += urfP (pp - pp(pRefCell))  (calcp_simple.f90:406-419)
+__global__ void k_correct_vel_p(int nC, Dev D, double urfP, int pref, int have_pref) {
+  const double ppref = have_pref ? D.pp[pref] : 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nC; i += gridDim.x * blockDim.x) {
+    D.u[i] = D.u[i] + D.su[i] * D.apu[i];
+    D.v[i] = D.v[i] + D.sv[i] * D.apv[i];
+    D.w[i] = D.w[i] + D.sw[i] * D.apw[i];
+    D.p[i] = D.p[i] + urfP * (D.pp[i] - ppref);
+  }
+}
+
+// fluxmc2, faceflux_mass.f90:650-696 (non-orthogonal corrector)
+__global__ void k_fluxmc2_face(MeshView M, Dev D) {
+  const Fld gp{D.gp, M.nT};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M.nI; i += gridDim.x * blockDim.x) {
+    const int ijp = M.owner[i], ijn = M.neighbour[i];
+    const double sx = M.arx[i], sy = M.ary[i], sz = M.arz[i];
+    const double xpn = M.xc[ijn] - M.xc[ijp], ypn = M.yc[ijn] - M.yc[ijp], zpn = M.zc[ijn] - M.zc[ijp];
+    const double s2 = sx * sx + sy * sy + sz * sz;
+    const double dn = xpn * sx + ypn * sy + zpn * sz;
+    const double rapr = -(0.5 * (D.apu[ijp] * D.den[ijp] + D.apu[ijn] * D.den[ijn]));
+    const double dpx = 0.5 * (gp.x(ijn) + gp.x(ijp));
+    const double dpy = 0.5 * (gp.y(ijn) + gp.y(ijp));
+    const double dpz = 0.5 * (gp.z(ijn) + gp.z(ijp));
+    const double fmc = rapr * ((dn * sx - xpn * s2) * dpx + (dn * sy - ypn * s2) * dpy + (dn * sz - zpn * s2) * dpz);
+    D.flmass[i] = D.flmass[i] + fmc;
+    D.fscr[i] = fmc;
+  }
+}
+
+__global__ void k_fluxmc2_cell(MeshView M, Dev D) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int q = M.cf_ptr[c]; q < M.cf_ptr[c + 1]; ++q) {
+      const int f = M.cf_face[q];
+      if (f >= M.nI) break;
+      if (M.owner[f] == c) s = s - D.fscr[f];
+      else s = s + D.fscr[f];
+    }
+    D.su[c] = s;
+  }
+}
+
+// continuityErrors, continuityErrors.f90:1-77 (flmass indexed by the owner
+// cell as written at :26-27): per-block partials of vol*|su*apu|, vol, su
+__global__ void k_conterr(MeshView M, Dev D, double* __restrict__ part) {
+  __shared__ double sm[3][8];
+  double w = 0.0, vs = 0.0, gs = 0.0;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int q = M.cf_ptr[c]; q < M.cf_ptr[c + 1]; ++q) {
+      const int f = M.cf_face[q];
+      if (f < M.nI) {
+        const int ijp = M.owner[f];
+        if (ijp == c) s = s - D.flmass[ijp];
+        else s = s + D.flmass[ijp];
+      } else {
+        const int t = D.ptype[M.bpatch[f - M.nI]];
+        if (t == FC_BC_INLET || t == FC_BC_OUTLET) s = s - D.flmass[f];
+      }
+    }
+    w += M.vol[c] * fabs(s * D.apu[c]);
+    vs += M.vol[c];
+    gs += s;
+    D.su[c] = 0.0;
+  }
+  double v3[3] = {w, vs, gs};
+  for (int j = 0; j < 3; ++j) {
+    double t = v3[j];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31) == 0) sm[j][threadIdx.x >> 5] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double t = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sm[threadIdx.x][k];
+    part[threadIdx.x * gridDim.x + blockIdx.x] = t;
+  }
+}
+
+__global__ void k_conterr_final(const double* __restrict__ part, int nb, double* __restrict__ out) {
+  if (threadIdx.x < 3) {
+    double t = 0.0;
+    for (int b = 0; b < nb; ++b) t += part[threadIdx.x * nb + b];
+    out[threadIdx.x] = t;
+  }
+}
+
+// inner-face mass flux from the face-interpolated velocity, init.f90:167-176
+__global__ void k_init_flmass(MeshView M, Dev D) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M.nI; i += gridDim.x * blockDim.x) {
+    const int ijp = M.owner[i], ijn = M.neighbour[i];
+    const double fxn = M.facint[i], fxp = 1.0 - M.facint[i];
+    const double ui = D.u[ijp] * fxp + D.u[ijn] * fxn;
+    const double vi = D.v[ijp] * fxp + D.v[ijn] * fxn;
+    const double wi = D.w[ijp] * fxp + D.w[ijn] * fxn;
+    D.flmass[i] = D.den[ijp] * (M.arx[i] * ui + M.ary[i] * vi + M.arz[i] * wi);
+  }
+}
+
+}  // namespace
+
+// ====================================================================== host
+
+struct SimpleState {
+  fc_simple_params prm;
+  bool have_prm = false;
+  DVec<int> ptype;
+  int ptype_gen = -1;  // mesh generation the patch types were uploaded for
+  DVec<double> part, out;
+  double cumulativeContErr = 0.0;
+  double resor[5] = {0, 0, 0, 0, 0};
+};
+
+static SimpleState& sstate(fc_ctx* ctx) {
+  if (!ctx->simple) ctx->simple = new SimpleState();
+  return *ctx->simple;
+}
+
+void fc_simple_release(fc_ctx* ctx) {
+  delete ctx->simple;
+  ctx->simple = nullptr;
+}
+
+static inline int gridn(int n) { return std::max(1, std::min(65535, (n + 255) / 256)); }
+
+static int make_dev(fc_ctx* ctx, Dev& D) {
+  FieldStore& F = ctx_fields(ctx);
+  SimpleState& S = sstate(ctx);
+  const MeshDev& m = ctx->mesh;
+  if (S.ptype_gen != ctx->mesh_gen) {
+    FC_CUDA_TRY(ctx, S.ptype.alloc(std::max(1, m.numBoundaries)));
+    S.ptype_gen = ctx->mesh_gen;
+    if (m.numBoundaries)
+      FC_CUDA_TRY(ctx, cudaMemcpy(S.ptype.p, m.h_bctype.data(), m.numBoundaries * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  for (int b = 0; b < m.numBoundaries; ++b)
+    if (m.h_bctype[b] == FC_BC_PERIODIC || m.h_bctype[b] == FC_BC_PRESSURE)
+      return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "periodic and pressure boundaries are not supported on this path");
+  D.u = F.u.p; D.v = F.v.p; D.w = F.w.p; D.p = F.p.p; D.pp = F.pp.p; D.vis = F.vis.p; D.den = F.den.p;
+  D.flmass = F.flmass.p; D.visw = F.visw.p;
+  D.su = F.su.p; D.sv = F.sv.p; D.sw = F.sw.p; D.spu = F.spu.p; D.spv = F.spv.p; D.sp = F.sp.p;
+  D.apu = F.apu.p; D.apv = F.apv.p; D.apw = F.apw.p;
+  D.gu = F.gu.p; D.gv = F.gv.p; D.gw = F.gw.p; D.gp = F.gp.p;
+  D.a = ctx->sys_mesh->a.p;
+  D.fscr = F.fscratch.p;
+  D.ptype = S.ptype.p;
+  return FC_OK;
+}
+
+// gradp_and_sources(p), nablap.f90:19-208, p = "p" or "pp"
+static int gradp_and_sources(fc_ctx* ctx, const Dev& D, double* p, int pscheme) {
+  MeshView M = mesh_view(ctx);
+  const int gc = gridn(M.nC), gb = gridn(M.nB);
+  const Fld gp{D.gp, M.nT};
+  k_gp_inner<<<gc, 256, 0, ctx->stream>>>(M, p, gp, D.apu, pscheme == 2 ? 2 : 0, D.su, D.sv, D.sw);
+  for (int stage = 1; stage <= 2; ++stage) {
+    if (M.nB) k_bpres<<<gb, 256, 0, ctx->stream>>>(M, D.ptype, p, gp, stage);
+    if (stage == 2 && pscheme == 1) k_gp_inner<<<gc, 256, 0, ctx->stream>>>(M, p, gp, D.apu, 1, D.su, D.sv, D.sw);
+    k_gp_grad<<<gc, 256, 0, ctx->stream>>>(M, p, D.su, D.sv, D.sw, D.gp);
+    ctx->kernel_launches += 2 + (stage == 2 && pscheme == 1);
+  }
+  k_gp_final<<<gc, 256, 0, ctx->stream>>>(M, p, D.su, D.sv, D.sw);
+  ctx->kernel_launches += 2;
+  FC_CUDA_TRY(ctx, cudaGetLastError());
+  return FC_OK;
+}
+
+static int update_velocity_at_boundary(fc_ctx* ctx, const Dev& D) {
+  MeshView M = mesh_view(ctx);
+  if (!M.nB) return FC_OK;
+  k_update_vel_bnd<<<gridn(M.nB), 256, 0, ctx->stream>>>(M, D);
+  ctx->kernel_launches++;
+  return FC_OK;
+}
+
+extern "C" int fc_simple_set_params(fc_ctx* ctx, const fc_simple_params* prm) {
+  if (!ctx || !prm) return FC_ERR_BAD_INPUT;
+  if (prm->urfU[0] <= 0 || prm->urfU[1] <= 0 || prm->urfU[2] <= 0 || prm->npcor < 1)
+    return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_simple_set_params: bad under-relaxation or npcor");
+  SimpleState& S = sstate(ctx);
+  S.prm = *prm;
+  S.prm.lSolverU[sizeof(S.prm.lSolverU) - 1] = 0;
+  S.prm.lSolverP[sizeof(S.prm.lSolverP) - 1] = 0;
+  S.have_prm = true;
+  return FC_OK;
+}
+
+extern "C" int fc_gradp_and_sources(fc_ctx* ctx, const char* field) {
+  if (!ctx || !field) return FC_ERR_BAD_INPUT;
+  if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
+  Dev D;
+  int st = make_dev(ctx, D);
+  if (st) return st;
+  std::string f(field);
+  double* p = f == "pp" ? D.pp : f == "p" ? D.p : nullptr;
+  if (!p) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "field must be 'p' or 'pp'");
+  int ps = sstate(ctx).have_prm ? sstate(ctx).prm.pscheme : 0;
+  return gradp_and_sources(ctx, D, p, ps);
+}
+
+extern "C" int fc_init_flmass(fc_ctx* ctx) {
+  if (!ctx) return FC_ERR_BAD_INPUT;
+  if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
+  Dev D;
+  int st = make_dev(ctx, D);
+  if (st) return st;
+  MeshView M = mesh_view(ctx);
+  if (M.nI) k_init_flmass<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D);
+  ctx->kernel_launches++;
+  FC_CUDA_TRY(ctx, cudaGetLastError());
+  return FC_OK;
+}
+
+extern "C" int fc_update_velocity_at_boundary(fc_ctx* ctx) {
+  if (!ctx || !ctx->has_mesh) return FC_ERR_STATE;
+  Dev D;
+  int st = make_dev(ctx, D);
+  if (st) return st;
+  return update_velocity_at_boundary(ctx, D);
+}
+
+static int solve_into(fc_ctx* ctx, const char* solver, double* x, const double* b, double* resor_out, int itr,
+                      double tol_abs, double tol_rel, const char* chvar) {
+  fc_solve_info info;
+  int st = solve_global(ctx, solver, x, b, resor_out, itr, tol_abs, tol_rel, chvar, &info);
+  return st;
+}
+
+// calcuvw, velocity.f90:50-750 (steady SIMPLE; no buoyancy, MHD, transient
+// or periodic terms).  resor[0..2] receive the normalised initial residuals.
+extern "C" int fc_calcuvw(fc_ctx* ctx, double* resor) {
+  if (!ctx) return FC_ERR_BAD_INPUT;
+  if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
+  SimpleState& S = sstate(ctx);
+  if (!S.have_prm) return fc_fail_msg(ctx, FC_ERR_STATE, "fc_simple_set_params not called");
+  Dev D;
+  int st = make_dev(ctx, D);
+  if (st) return st;
+  const fc_simple_params& P = S.prm;
+  MeshView M = mesh_view(ctx);
+  CsrSystem* sys = ctx->sys_mesh;
+  update_velocity_at_boundary(ctx, D);
+  if ((st = fv_grad(ctx, P.gradScheme, D.u, D.gu))) return st;
+  if ((st = fv_grad(ctx, P.gradScheme, D.v, D.gv))) return st;
+  if ((st = fv_grad(ctx, P.gradScheme, D.w, D.gw))) return st;
+  if ((st = gradp_and_sources(ctx, D, D.p, P.pscheme))) return st;
+  MomParams mp;
+  mp.gds = P.gdsU;
+  mp.viscos = P.viscos;
+  mp.scheme = P.cSchemeU;
+  mp.vis_sym = 0.0;
+  if (M.nB > 0) FC_CUDA_TRY(ctx, cudaMemcpyAsync(&mp.vis_sym, D.vis + M.nC, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (M.nI) k_mom_face<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D, mp);
+  k_mom_cell<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D, mp);
+  ctx->kernel_launches += 2;
+  FC_CUDA_TRY(ctx, cudaGetLastError());
+  double r[3] = {0, 0, 0};
+  // U
+  k_mom_diag<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, sys->ia.p, sys->diag.p, D.a, D.spu, D.apu, D.su, D.su, D.u,
+                                                   P.urfU[0], 0);
+  ctx->kernel_launches++;
+  st = solve_into(ctx, P.lSolverU, D.u, D.su, &r[0], P.maxiterU, P.tolAbsU, P.tolRelU, "U");
+  if (st < 0) return st;
+  // V
+  k_mom_diag<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, sys->ia.p, sys->diag.p, D.a, D.spv, D.apv, D.sv, D.su, D.v,
+                                                   P.urfU[1], 1);
+  ctx->kernel_launches++;
+  st = solve_into(ctx, P.lSolverU, D.v, D.su, &r[1], P.maxiterU, P.tolAbsU, P.tolRelU, "V");
+  if (st < 0) return st;
+  // W
+  k_mom_diag<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, sys->ia.p, sys->diag.p, D.a, D.sp, D.apw, D.sw, D.su, D.w,
+                                                   P.urfU[2], 1);
+  ctx->kernel_launches++;
+  st = solve_into(ctx, P.lSolverU, D.w, D.su, &r[2], P.maxiterU, P.tolAbsU, P.tolRelU, "W");
+  if (st < 0) return st;
+  for (int k = 0; k < 3; ++k) S.resor[k + 1] = r[k];
+  if (resor) for (int k = 0; k < 3; ++k) resor[k] = r[k];
+  return FC_OK;
+}
+
+// calcp_simple, calcp_simple.f90:1-470 (incompressible; no periodic or
+// pressure boundaries).  *resor4 receives resor(4) as continuityErrors sets it.
+extern "C" int fc_calcp_simple(fc_ctx* ctx, double* resor4) {
+  if (!ctx) return FC_ERR_BAD_INPUT;
+  if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
+  SimpleState& S = sstate(ctx);
+  if (!S.have_prm) return fc_fail_msg(ctx, FC_ERR_STATE, "fc_simple_set_params not called");
+  Dev D;
+  int st = make_dev(ctx, D);
+  if (st) return st;
+  const fc_simple_params& P = S.prm;
+  MeshView M = mesh_view(ctx);
+  if (M.nI) k_p_face<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D);
+  bool outlets = false;
+  for (int b = 0; b < ctx->mesh.numBoundaries; ++b) outlets |= ctx->mesh.h_bctype[b] == FC_BC_OUTLET;
+  if (outlets) k_adjust_mass_flow<<<1, 32, 0, ctx->stream>>>(M, D, P.flomas);
+  k_p_cell<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D);
+  ctx->kernel_launches += 2 + outlets;
+  FC_CUDA_TRY(ctx, cudaGetLastError());
+  double r4 = 0;
+  for (int ipcorr = 1; ipcorr <= P.npcor; ++ipcorr) {
+    st = solve_into(ctx, P.lSolverP, D.pp, D.su, &r4, P.maxiterP, P.tolAbsP, P.tolRelP, "p");
+    if (st < 0) return st;
+    if (M.nI) k_flux_correct<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D);
+    // ppref = pp(pRefCell) before gradp_and_sources(pp), which only touches
+    // boundary values of pp
+    if ((st = gradp_and_sources(ctx, D, D.pp, P.pscheme))) return st;
+    const int pref = std::max(0, std::min(M.nC - 1, P.pRefCell - 1));
+    k_correct_vel_p<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, D, P.urfP, pref, 1);
+    ctx->kernel_launches += 2;
+    update_velocity_at_boundary(ctx, D);
+    if (ipcorr != P.npcor) {
+      if (M.nI) k_fluxmc2_face<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D);
+      k_fluxmc2_cell<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D);
+      ctx->kernel_launches += 2;
+    }
+  }
+  // continuityErrors
+  const int nb = std::min(1024, gridn(M.nC));
+  FC_CUDA_TRY(ctx, S.part.alloc((size_t)3 * nb));
+  FC_CUDA_TRY(ctx, S.out.alloc(3));
+  k_conterr<<<nb, 256, 0, ctx->stream>>>(M, D, S.part.p);
+  k_conterr_final<<<1, 32, 0, ctx->stream>>>(S.part.p, nb, S.out.p);
+  ctx->kernel_launches += 2;
+  double h[3];
+  FC_CUDA_TRY(ctx, cudaMemcpyAsync(h, S.out.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  const double wavg = h[0] / h[1];
+  S.cumulativeContErr += h[2];
+  S.resor[4] = wavg;
+  if (resor4) *resor4 = wavg;
+  if (ctx->verbosity)
+    std::printf("  continuity errors : avg local = %10.3E, global = %10.3E, cumulative = %10.3E\n", wavg, h[2],
+                S.cumulativeContErr);
+  return FC_OK;
+}
+
+// one outer iteration of main.f90:150-267 (calcuvw + calcp_simple)
+extern "C" int fc_simple_iteration(fc_ctx* ctx, double* resor) {
+  double r[4];
+  int st = fc_calcuvw(ctx, r);
+  if (st < 0) return st;
+  st = fc_calcp_simple(ctx, &r[3]);
+  if (st < 0) return st;
+  if (resor) for (int k = 0; k < 4; ++k) resor[k] = r[k];
+  // divergence check of main.f90:202-207
+  const double source = std::max(r[0], std::max(r[1], r[2]));
+  if (!(source <= (double)1e+30f)) return fc_fail_msg(ctx, FC_ERR_NAN, "SIMPLE iterations diverge");
+  return FC_OK;
+}

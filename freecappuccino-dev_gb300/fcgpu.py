@@ -99,6 +99,13 @@ def lib():
         "fc_grad": (i, [vp, i, vp, vp]),
         "fc_laplacian": (i, [vp, vp, vp, C.c_ulonglong]),
         "fc_solve_field": (i, [vp, cp, cp, cp, vp, i, d, d, cp, C.POINTER(SolveInfo)]),
+        "fc_simple_set_params": (i, [vp, vp]),
+        "fc_init_flmass": (i, [vp]),
+        "fc_update_velocity_at_boundary": (i, [vp]),
+        "fc_gradp_and_sources": (i, [vp, cp]),
+        "fc_calcuvw": (i, [vp, vp]),
+        "fc_calcp_simple": (i, [vp, vp]),
+        "fc_simple_iteration": (i, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -140,6 +147,36 @@ def _i32(x):
     if hasattr(x, "data_ptr") or isinstance(x, int):
         return x
     return np.ascontiguousarray(x, dtype=np.int32)
+
+
+class SimpleParams(C.Structure):
+    """fc_simple_params: namelist parameters of the SIMPLE path."""
+    _fields_ = [("densit", C.c_double), ("viscos", C.c_double), ("urfU", C.c_double * 3), ("gdsU", C.c_double),
+                ("urfP", C.c_double), ("cSchemeU", C.c_int), ("gradScheme", C.c_int), ("pscheme", C.c_int),
+                ("maxiterU", C.c_int), ("maxiterP", C.c_int), ("npcor", C.c_int), ("pRefCell", C.c_int),
+                ("tolAbsU", C.c_double), ("tolRelU", C.c_double), ("tolAbsP", C.c_double), ("tolRelP", C.c_double),
+                ("lSolverU", C.c_char * 16), ("lSolverP", C.c_char * 16), ("flomas", C.c_double)]
+
+    @classmethod
+    def cavity(cls, **kw):
+        """Settings of examples/cavity/input.nml (urfU 0.8, urfP 0.3, central
+        scheme, gds 1, BiCGStab U / ICCG p, maxiter 5 / 20, tolRel 0.01 / 0.025)."""
+        p = cls()
+        p.densit, p.viscos = kw.get("densit", 1.0), kw.get("viscos", 0.01)
+        for i in range(3):
+            p.urfU[i] = kw.get("urfU", 0.8)
+        p.gdsU, p.urfP = kw.get("gdsU", 1.0), kw.get("urfP", 0.3)
+        p.cSchemeU = kw.get("scheme", 1)
+        p.gradScheme = kw.get("grad", 0)
+        p.pscheme = kw.get("pscheme", 0)
+        p.maxiterU, p.maxiterP = kw.get("maxiterU", 5), kw.get("maxiterP", 20)
+        p.npcor, p.pRefCell = kw.get("npcor", 1), kw.get("pRefCell", 1)
+        p.tolAbsU, p.tolRelU = kw.get("tolAbsU", 1e-15), kw.get("tolRelU", 0.01)
+        p.tolAbsP, p.tolRelP = kw.get("tolAbsP", 1e-15), kw.get("tolRelP", 0.025)
+        p.lSolverU = kw.get("solverU", "bicgstab").encode()
+        p.lSolverP = kw.get("solverP", "iccg").encode()
+        p.flomas = kw.get("flomas", 0.0)
+        return p
 
 
 class Mesh:
@@ -407,3 +444,29 @@ class Context:
                                    int(itr_max), float(tol_abs), float(tol_rel), chvar.encode(), C.byref(info))
         self._check(st, "fc_solve_field")
         return float(r0[0]), info, st
+
+    # ------------------------------------------------------------ SIMPLE
+    def simple_params(self, prm):
+        self._prm = prm
+        self._check(self.L.fc_simple_set_params(self.h, C.byref(prm)), "fc_simple_set_params")
+
+    def init_flmass(self):
+        self._check(self.L.fc_init_flmass(self.h), "fc_init_flmass")
+
+    def gradp_and_sources(self, field="p"):
+        self._check(self.L.fc_gradp_and_sources(self.h, field.encode()), "fc_gradp_and_sources")
+
+    def calcuvw(self):
+        r = np.zeros(3)
+        self._check(self.L.fc_calcuvw(self.h, _ptr(r)), "fc_calcuvw")
+        return r
+
+    def calcp_simple(self):
+        r = np.zeros(1)
+        self._check(self.L.fc_calcp_simple(self.h, _ptr(r)), "fc_calcp_simple")
+        return float(r[0])
+
+    def simple_iteration(self):
+        r = np.zeros(4)
+        self._check(self.L.fc_simple_iteration(self.h, _ptr(r)), "fc_simple_iteration")
+        return r

@@ -200,6 +200,60 @@ int fc_laplacian(fc_ctx* ctx, const double* mu, const double* phi, unsigned long
 int fc_solve_field(fc_ctx* ctx, const char* solver, const char* x_field, const char* rhs_field, double* res0,
                    int itr_max, double tol_abs, double tol_rel, const char* chvar, fc_solve_info* info);
 
+/* ======================================================================== */
+/* SIMPLE path (velocity.f90 calcuvw, calcp_simple.f90, nablap.f90)          */
+/* ======================================================================== */
+/* convection schemes of face_value (interpolation.f90:28-113, :489-650) */
+#define FC_SCHEME_CDS                     0   /* 'cds'          */
+#define FC_SCHEME_CENTRAL                 1   /* 'central'      */
+#define FC_SCHEME_LINEAR_UPWIND           2   /* 'linearUpwind' */
+#define FC_SCHEME_KAPPA                   3   /* 'kappa'        */
+#define FC_SCHEME_MUSCL                  10
+#define FC_SCHEME_UMIST                  11
+#define FC_SCHEME_KOREN                  12
+#define FC_SCHEME_SMART                  13
+#define FC_SCHEME_AVLSMART               14   /* 'avl-smart' */
+#define FC_SCHEME_CHARM                  15
+#define FC_SCHEME_VANLEER                16
+#define FC_SCHEME_OSPRE                  17
+#define FC_SCHEME_MINMOD                 18
+#define FC_SCHEME_BOUNDED_LINEAR_UPWIND  19   /* 'boundedLinearUpwind'   */
+#define FC_SCHEME_BOUNDED_LINEAR_UPWIND02 20  /* 'boundedLinearUpwind02' */
+#define FC_SCHEME_BOUNDED_CENTRAL        21   /* 'boundedCentral'        */
+#define FC_SCHEME_FROMM                  22
+#define FC_SCHEME_CUI                    23
+#define FC_SCHEME_QUICK                  24
+#define FC_SCHEME_SPL13                  25
+
+/* The namelist parameters of the SIMPLE path (read_input.f90; defaults in
+ * velocity.f90:24-33 and pressure.f90:28-33). */
+typedef struct {
+  double densit, viscos;      /* density, molecular viscosity */
+  double urfU[3], gdsU, urfP; /* under-relaxation, deferred-correction blend */
+  int cSchemeU;               /* FC_SCHEME_* for the momentum convection */
+  int gradScheme;             /* FC_GRAD_* */
+  int pscheme;                /* pressure interpolation: 0 'linear', 1 'central', 2 'weighted' */
+  int maxiterU, maxiterP, npcor, pRefCell;
+  double tolAbsU, tolRelU, tolAbsP, tolRelP;
+  char lSolverU[16], lSolverP[16];  /* csrsolve names */
+  double flomas;              /* inlet mass flow (init.f90:179-195) */
+} fc_simple_params;
+
+int fc_simple_set_params(fc_ctx* ctx, const fc_simple_params* prm);
+/* inner-face mass fluxes from the face-interpolated velocity (init.f90:167-176) */
+int fc_init_flmass(fc_ctx* ctx);
+int fc_update_velocity_at_boundary(fc_ctx* ctx);
+/* gradp_and_sources(p) (nablap.f90:19-208) on field "p" or "pp": su,sv,sw and dPdxi */
+int fc_gradp_and_sources(fc_ctx* ctx, const char* field);
+/* calcuvw (velocity.f90:50-750): momentum assembly and the three solves;
+ * resor[3] receives the normalised initial residuals of U, V, W. */
+int fc_calcuvw(fc_ctx* ctx, double* resor);
+/* calcp_simple (calcp_simple.f90:1-470); *resor4 = resor(4) of continuityErrors. */
+int fc_calcp_simple(fc_ctx* ctx, double* resor4);
+/* one outer SIMPLE iteration (main.f90:159-165); resor[4] as the reference
+ * logs them; FC_ERR_NAN when max(resor(1:3)) > 1e30 (main.f90:202-207). */
+int fc_simple_iteration(fc_ctx* ctx, double* resor);
+
 #ifdef __cplusplus
 }
 #endif

@@ -272,6 +272,7 @@ def run_gpu(args, rank, world, dist):
     x_fp64 = ctx.field_get("pp")[:nC].copy()
     mixed_err = float(np.abs(x_mixed - x_fp64).max() / np.abs(x_fp64).max())
 
+    sweep = ctx.sweep_stats(0)
     peak, peak_kind = measured_peak()
     bytes_launch = iccg_bytes_per_iteration(nC, nnz) * iters
     avg_launch_ms = float(np.mean(solve_ms))
@@ -286,7 +287,9 @@ def run_gpu(args, rank, world, dist):
             "config": {"workload": f"{n}^3 perturbed-hex pressure Poisson, ICCG (DIC) FP64 to 1e-10 rel. L1",
                        "cells": nC, "nnz": nnz, "iterations_per_solve": iters,
                        "parallelism": "replicas" if world > 1 else "single GPU",
-                       "l2": "inputs larger than L2 (matrix + vectors ~0.3 GB)"},
+                       "l2": "inputs larger than L2 (matrix + vectors ~0.3 GB)",
+                       "sweep_tiles": int(sweep["tiles"]), "sweep_levels": int(sweep["levels"]),
+                       "sweep_est_us": round(sweep["est_sweep_us"], 1)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "k_iccg<double> (whole solve, one persistent launch)",

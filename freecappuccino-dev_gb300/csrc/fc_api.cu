@@ -38,7 +38,8 @@ extern "C" int fc_init(int device, fc_ctx** out) {
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
   if (!coop) { delete c; return FC_ERR_UNSUPPORTED; }
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
+      cudaEventCreate(&c->sev0) != cudaSuccess || cudaEventCreate(&c->sev1) != cudaSuccess) {
     delete c;
     return FC_ERR_CUDA;
   }
@@ -62,6 +63,8 @@ extern "C" void fc_finalize(fc_ctx* ctx) {
   fc_simple_release(ctx);
   cudaEventDestroy(ctx->ev0);
   cudaEventDestroy(ctx->ev1);
+  cudaEventDestroy(ctx->sev0);
+  cudaEventDestroy(ctx->sev1);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -104,8 +107,26 @@ static int ext_system(fc_ctx* ctx, int n, int nnz, const int* ia, const int* ja,
   }
   delete ctx->sys_ext;
   ctx->sys_ext = nullptr;
+  // a pattern equal to the mesh's CSR gets the cell centroids for its sweep tiling
+  const double* xyz = nullptr;
+  if (ctx->has_mesh && ctx->sys_mesh && n == ctx->sys_mesh->n && nnz == ctx->sys_mesh->nnz) {
+    std::vector<int> hia(n + 1), hja(nnz), hdg(n);
+    auto get = [&](const int* src, int* dst, size_t cnt) {
+      if (is_device_ptr(src)) return cudaMemcpy(dst, src, cnt * sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess;
+      std::memcpy(dst, src, cnt * sizeof(int));
+      return true;
+    };
+    if (get(ia, hia.data(), n + 1) && get(ja, hja.data(), nnz) && get(diag, hdg.data(), n)) {
+      const CsrSystem* ms = ctx->sys_mesh;
+      bool same = true;
+      for (int i = 0; i <= n && same; ++i) same = hia[i] == ms->h_ia[i] + 1;
+      for (int k = 0; k < nnz && same; ++k) same = hja[k] == ms->h_ja[k] + 1;
+      for (int i = 0; i < n && same; ++i) same = hdg[i] == ms->h_diag[i] + 1;
+      if (same) xyz = ctx->mesh.h_xyz.data();
+    }
+  }
   s = new CsrSystem();
-  int st = sys_set_pattern(ctx, s, n, nnz, ia, ja, diag);
+  int st = sys_set_pattern(ctx, s, n, nnz, ia, ja, diag, xyz);
   if (st) { delete s; return st; }
   s->key_ia = ia; s->key_ja = ja; s->key_diag = diag;
   ctx->sys_ext = s;
@@ -288,4 +309,17 @@ int solve_global(fc_ctx* ctx, const char* solver, double* x, const double* b, do
   if (res0 && !r.early) *res0 = r.resor;
   if (ctx->verbosity) print_report(sv, chvar, r);
   return r.status;
+}
+
+// Tiled sweep schedule of the mesh system (which = 0) or of the cached
+// external pattern (which = 1): out[0..7] = tiles, levels, widest tile, ring
+// depth, estimated forward sweep microseconds, ring-served entries,
+// cross-tile entries, global same-tile entries.
+extern "C" int fc_sweep_stats(fc_ctx* ctx, int which, double* out) {
+  if (!ctx || !out) return FC_ERR_BAD_INPUT;
+  CsrSystem* s = which ? ctx->sys_ext : ctx->sys_mesh;
+  if (!s) return fc_fail_msg(ctx, FC_ERR_STATE, "no such system");
+  out[0] = s->sf.ntiles; out[1] = s->sf.nlev; out[2] = s->sf.max_slots; out[3] = s->sf.R;
+  out[4] = s->est_sweep_us; out[5] = (double)s->sf.ring; out[6] = (double)s->sf.cross; out[7] = (double)s->sf.global_same;
+  return FC_OK;
 }

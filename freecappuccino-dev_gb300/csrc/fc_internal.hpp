@@ -55,6 +55,13 @@ struct GridCtl {
 #define FC_NPART 4
 enum { FC_OUT_RES0 = 0, FC_OUT_RESL, FC_OUT_FACTOR, FC_OUT_RESOR, FC_OUT_ITR, FC_OUT_EARLY, FC_OUT_BAD, FC_OUT_N = 16 };
 
+// device copy of a tiled sweep schedule (fc_schedule.hpp)
+struct DevSweep {
+  int ntiles = 0, nlev = 0, R = 1, max_slots = 0;
+  DVec<int> tile_step_ptr, step_level, tile_slots, step_row_ptr, rows, kbne;
+  long long cross = 0, ring = 0, global_same = 0;
+};
+
 struct LevelSchedule {
   int nlev = 0;
   int max_width = 0;
@@ -70,9 +77,12 @@ struct CsrSystem {
   DVec<double> a;
   DVec<float> a32;
   LevelSchedule lf, lb;              // forward (lower) and backward (upper) level sets
+  DevSweep sf, sb;                   // tiled pipeline schedules of the two sweeps
+  DVec<int> code;                    // per entry: ring index or global row (fc_schedule.hpp)
+  double est_sweep_us = 0.0;         // critical-path estimate of the forward sweep
   // workspace
   DVec<double> x, b, r, r0, p, u, z, v, d, w;
-  DVec<float> fr, fr0, fp, fu, fz, fv, fd, fx;
+  DVec<float> fr, fr0, fp, fu, fz, fv, fd, fx, fy, fw;
   DVec<double> part, out;
   DVec<unsigned> bar;
   DVec<int> status;
@@ -101,6 +111,7 @@ struct MeshDev {
   DVec<double> facint, Df;                 // numInnerFaces
   DVec<int> ijk, jik;                      // face -> CSR slot (0-based)
   std::vector<int> h_owner, h_neighbour;
+  std::vector<double> h_xyz;               // cell centroids x..., y..., z... (sweep tiling)
 };
 
 struct FieldStore;
@@ -110,7 +121,8 @@ struct fc_ctx {
   int device = 0;
   int num_sms = 0;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;    // the caller's pair (fc_event_record)
+  cudaEvent_t sev0 = nullptr, sev1 = nullptr;  // solve timing (fc_solve_info.ms)
   std::string last_error;
   int verbosity = 0;   // 1: print the reference's solver report lines
   int precision = 0;   // FC_PREC_*
@@ -124,13 +136,17 @@ struct fc_ctx {
   FieldStore* fields = nullptr;
   SimpleState* simple = nullptr;
   long long kernel_launches = 0;
+  int tracing = 0, trace_blocks = 0, trace_cap = 0;
+  DVec<unsigned long long> trace;
 };
 
 int fc_fail(fc_ctx* ctx, int code, const char* what, cudaError_t e = cudaSuccess);
 int fc_fail_msg(fc_ctx* ctx, int code, const std::string& msg);
 
 // pattern analysis (host) + upload
-int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, const int* ja1, const int* diag1);
+// xyz: optional row coordinates (3*n, x then y then z) used to cut the sweep tiles
+int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, const int* ja1, const int* diag1,
+                    const double* xyz = nullptr);
 int sys_upload_values(fc_ctx* ctx, CsrSystem* s, const double* a, bool a_on_device);
 int sys_alloc_work(fc_ctx* ctx, CsrSystem* s);
 

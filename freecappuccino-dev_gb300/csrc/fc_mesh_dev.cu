@@ -130,7 +130,7 @@ static void free_mesh_dev(MeshDev& m) {
   DVec<int>* iv[] = {&m.nnodes, &m.nodes, &m.owner, &m.neighbour, &m.bface_patch, &m.bface_wall,
                      &m.cf_ptr, &m.cf_face, &m.ijk, &m.jik};
   for (auto* v : iv) v->release();
-  m.h_owner.clear(); m.h_neighbour.clear();
+  m.h_owner.clear(); m.h_neighbour.clear(); m.h_xyz.clear();
 }
 
 void fc_release_mesh(fc_ctx* ctx) {
@@ -275,7 +275,11 @@ extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
   for (auto& v : ia1) ++v;
   for (auto& v : ja1) ++v;
   for (auto& v : dg1) ++v;
-  int st = sys_set_pattern(ctx, s, nC, nnz, ia1.data(), ja1.data(), dg1.data());
+  m.h_xyz.resize((size_t)3 * nC);
+  FC_CUDA_TRY(ctx, cudaMemcpy(m.h_xyz.data(), m.xc.p, nC * sizeof(double), cudaMemcpyDeviceToHost));
+  FC_CUDA_TRY(ctx, cudaMemcpy(m.h_xyz.data() + nC, m.yc.p, nC * sizeof(double), cudaMemcpyDeviceToHost));
+  FC_CUDA_TRY(ctx, cudaMemcpy(m.h_xyz.data() + 2 * (size_t)nC, m.zc.p, nC * sizeof(double), cudaMemcpyDeviceToHost));
+  int st = sys_set_pattern(ctx, s, nC, nnz, ia1.data(), ja1.data(), dg1.data(), m.h_xyz.data());
   if (st) { delete s; return st; }
   FC_CUDA_TRY(ctx, cudaMemset(s->a.p, 0, (size_t)nnz * sizeof(double)));
   ctx->sys_mesh = s;

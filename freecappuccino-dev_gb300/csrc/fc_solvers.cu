@@ -18,8 +18,11 @@
 
 #include "fc_internal.hpp"
 #include "fc_krylov.cuh"
+#include "fc_schedule.hpp"
 
 using namespace fcdev;
+
+extern __shared__ __align__(16) unsigned char fc_smem[];
 
 namespace {
 
@@ -41,6 +44,52 @@ struct KArgs {
   double tol_abs;
   double tol_rel;
   int skip_setup;
+  unsigned long long* trace;  // traced instantiation only: phase cycles and step stamps
+  int trace_cap;              // step stamps kept per tile and sweep
+};
+
+// phases of the ICCG kernel for the optional cycle trace
+enum { TR_SETUP = 0, TR_FWD, TR_MID, TR_BWD, TR_DOT, TR_PUPD, TR_SPMV, TR_UPD, FC_TRACE_N = 8 };
+
+// Cycle tracer of the traced ICCG instantiation: per block SM cycles per
+// phase (thread 0's clock), and for the first two sweeps after the DIC setup
+// (the forward and backward sweep of iteration 1) a stamp (clock64,
+// globaltimer) at the start of every step of the tile and after its last.
+// trace layout: [blocks][FC_TRACE_N] phase cycles, then
+// [2 sweeps][blocks][tl_cap][2] step stamps.
+struct Tracer {
+  unsigned long long* out;
+  int tl_cap, nsweep;
+  unsigned long long acc[FC_TRACE_N];
+  long long t;
+  __device__ Tracer(unsigned long long* o, int cap) : out(o), tl_cap(cap), nsweep(0) {
+    for (int k = 0; k < FC_TRACE_N; ++k) acc[k] = 0;
+    t = clock64();
+  }
+  __device__ __forceinline__ void mark(int phase) {
+    const long long now = clock64();
+    acc[phase] += (unsigned long long)(now - t);
+    t = now;
+  }
+  __device__ __forceinline__ void sweep() { ++nsweep; }
+  __device__ __forceinline__ void step(int k) {
+    if (threadIdx.x != 0 || nsweep > 2 || k >= tl_cap) return;
+    unsigned long long gt;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(gt));
+    unsigned long long* q = out + (size_t)gridDim.x * FC_TRACE_N +
+                            (((size_t)(nsweep - 1) * gridDim.x + blockIdx.x) * tl_cap + k) * 2;
+    q[0] = (unsigned long long)clock64();
+    q[1] = gt;
+  }
+  __device__ void flush() {
+    if (threadIdx.x == 0)
+      for (int k = 0; k < FC_TRACE_N; ++k) out[(size_t)blockIdx.x * FC_TRACE_N + k] = acc[k];
+  }
+};
+
+struct NoTracer : NoTrace {
+  __device__ NoTracer(unsigned long long*, int) {}
+  __device__ void flush() {}
 };
 
 template <class T>
@@ -73,30 +122,36 @@ __device__ bool residual_l1(const KArgs<T>& A, int& ph, double& l1out) {
 
 // ------------------------------------------------------------------ ICCG
 // iccg, linear_solvers.f90:364-545
-template <class T>
-__global__ void __launch_bounds__(FC_BLOCK) k_iccg(KArgs<T> A) {
+template <class T, bool TRACE = false>
+__global__ void __launch_bounds__(FC_BLOCK, 1) k_iccg(KArgs<T> A) {
   const CsrView<T>& S = A.S;
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, G = gridDim.x * blockDim.x, n = S.n;
   int ph = 0;
-  T *x = A.x, *r = A.r, *p = A.p, *z = A.z, *d = A.d;
-  for (int i = gt; i < n; i += G) { p[i] = T(0); z[i] = T(0); }
+  SweepCtx X = sweep_ctx(S, fc_smem);
+  T *x = A.x, *r = A.r, *p = A.p, *z = A.z, *d = A.d, *yf = A.u;
+  const T SENT = Sentinel<T>::value();
+  for (int i = gt; i < n; i += G) { p[i] = T(0); z[i] = T(0); yf[i] = SENT; }
+  typename std::conditional<TRACE, Tracer, NoTracer>::type tr(A.trace, A.trace_cap);
   double res0;
   if (!residual_l1(A, ph, res0)) return;
   if (res0 < A.tol_abs) { write_out(A, res0, res0, 0.0, 0.0, 0, 1); return; }
   if (!A.skip_setup)
-    if (!precond_setup<T, false>(A.C, S, d)) return;
+    if (!precond_setup<T, false>(A.C, S, X, d)) return;
+  tr.mark(TR_SETUP);
   double s0 = FC_S0, resl = 0.0, factor = 0.0, resor = 0.0;
   int itr_used = 0;
   for (int l = 1; l <= A.itr_max; ++l) {
     double rz[1] = {0.0};
     auto pre = [&](int i) { return ldcg(r + i); };
     auto post = [&](int i, T zi) { rz[0] += (double)ldcg(r + i) * (double)zi; };
-    if (!precond_apply(A.C, S, d, z, pre, post, false)) return;
+    if (!precond_apply(A.C, S, X, d, yf, z, pre, post, false, &tr)) return;
     if (!grid_reduce<1>(A.C, ph, rz)) return;
+    tr.mark(TR_DOT);
     const double sk = rz[0];
     const T bet = (T)(sk / s0);
     for (int i = gt; i < n; i += G) p[i] = ldcg(z + i) + bet * ldcg(p + i);
     if (!grid_sync(A.C)) return;
+    tr.mark(TR_PUPD);
     double pap[1] = {0.0};
     for (int i = gt; i < n; i += G) {
       T zi = row_dot(S, p, i);
@@ -104,6 +159,7 @@ __global__ void __launch_bounds__(FC_BLOCK) k_iccg(KArgs<T> A) {
       pap[0] += (double)ldcg(p + i) * (double)zi;
     }
     if (!grid_reduce<1>(A.C, ph, pap)) return;
+    tr.mark(TR_SPMV);
     const T alf = (T)(sk / pap[0]);
     double red[2] = {0.0, 0.0};
     for (int i = gt; i < n; i += G) {
@@ -111,10 +167,12 @@ __global__ void __launch_bounds__(FC_BLOCK) k_iccg(KArgs<T> A) {
       x[i] = xi;
       T ri = ldcg(r + i) - alf * ldcg(z + i);
       r[i] = ri;
+      yf[i] = SENT;
       red[0] += fabs((double)ri);
       if (l == 1) red[1] += fabs((double)__ldg(S.a + __ldg(S.dg + i)) * (double)xi);
     }
     if (!grid_reduce<2>(A.C, ph, red)) return;
+    tr.mark(TR_UPD);
     resl = red[0];
     s0 = sk;
     ++itr_used;
@@ -123,6 +181,7 @@ __global__ void __launch_bounds__(FC_BLOCK) k_iccg(KArgs<T> A) {
     if (!(rsm == rsm)) { if (gt == 0) atomicCAS(A.C.status, 0, FC_ERR_NAN); break; }
     if (rsm < A.tol_rel || resl < A.tol_abs) break;
   }
+  tr.flush();
   write_out(A, res0, resl, factor, resor, itr_used, 0);
 }
 
@@ -131,20 +190,22 @@ __global__ void __launch_bounds__(FC_BLOCK) k_iccg(KArgs<T> A) {
 // first forward sweep, and the fi/res updates into the second one (each row
 // is updated by the thread that owns it in the sweep).
 template <class T>
-__global__ void __launch_bounds__(FC_BLOCK) k_bicgstab(KArgs<T> A) {
+__global__ void __launch_bounds__(FC_BLOCK, 1) k_bicgstab(KArgs<T> A) {
   const CsrView<T>& S = A.S;
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, G = gridDim.x * blockDim.x, n = S.n;
   int ph = 0;
-  T *x = A.x, *r = A.r, *r0 = A.r0, *p = A.p, *u = A.u, *z = A.z, *v = A.v, *d = A.d;
+  SweepCtx X = sweep_ctx(S, fc_smem);
+  T *x = A.x, *r = A.r, *r0 = A.r0, *p = A.p, *u = A.u, *z = A.z, *v = A.v, *d = A.d, *yf = A.w;
+  const T SENT = Sentinel<T>::value();
   double res0;
   if (!residual_l1(A, ph, res0)) return;
   if (res0 < A.tol_abs) { write_out(A, res0, res0, 0.0, 0.0, 0, 1); return; }
   if (!A.skip_setup)
-    if (!precond_setup<T, true>(A.C, S, d)) return;
+    if (!precond_setup<T, true>(A.C, S, X, d)) return;
   double bb[1] = {0.0};
   for (int i = gt; i < n; i += G) {
     T ri = ldcg(r + i);
-    r0[i] = ri; p[i] = T(0); u[i] = T(0); z[i] = T(0); v[i] = T(0);
+    r0[i] = ri; p[i] = T(0); u[i] = T(0); z[i] = T(0); v[i] = T(0); yf[i] = SENT;
     bb[0] += (double)ri * (double)ri;
   }
   if (!grid_reduce<1>(A.C, ph, bb)) return;
@@ -162,11 +223,12 @@ __global__ void __launch_bounds__(FC_BLOCK) k_bicgstab(KArgs<T> A) {
       return pi;
     };
     auto nopost = [&](int, T) {};
-    if (!precond_apply(A.C, S, d, z, pre1, nopost, true)) return;
+    if (!precond_apply(A.C, S, X, d, yf, z, pre1, nopost, true)) return;
     double ur[1] = {0.0};
     for (int i = gt; i < n; i += G) {
       T ui = row_dot(S, z, i);
       u[i] = ui;
+      yf[i] = SENT;
       ur[0] += (double)ui * (double)ldcg(r0 + i);
     }
     if (!grid_reduce<1>(A.C, ph, ur)) return;
@@ -178,11 +240,12 @@ __global__ void __launch_bounds__(FC_BLOCK) k_bicgstab(KArgs<T> A) {
       r[i] = ri;
       return ri;
     };
-    if (!precond_apply(A.C, S, d, z, pre2, nopost, true)) return;
+    if (!precond_apply(A.C, S, X, d, yf, z, pre2, nopost, true)) return;
     double vr[2] = {0.0, 0.0};
     for (int i = gt; i < n; i += G) {
       T vi = row_dot(S, z, i);
       v[i] = vi;
+      yf[i] = SENT;
       vr[0] += (double)vi * (double)ldcg(r + i);
       vr[1] += (double)vi * (double)vi;
     }
@@ -214,7 +277,7 @@ __global__ void __launch_bounds__(FC_BLOCK) k_bicgstab(KArgs<T> A) {
 // ------------------------------------------------------------------ DPCG
 // dpcg, linear_solvers.f90:206-359
 template <class T>
-__global__ void __launch_bounds__(FC_BLOCK) k_dpcg(KArgs<T> A) {
+__global__ void __launch_bounds__(FC_BLOCK, 1) k_dpcg(KArgs<T> A) {
   const CsrView<T>& S = A.S;
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, G = gridDim.x * blockDim.x, n = S.n;
   int ph = 0;
@@ -271,36 +334,38 @@ __global__ void __launch_bounds__(FC_BLOCK) k_dpcg(KArgs<T> A) {
 // GaussSeidel, linear_solvers.f90:96-201: in-place sweep as a forward
 // level-scheduled sweep; entries left of the diagonal read this sweep's
 // values (xb), the others the previous sweep's (xa).
-__global__ void __launch_bounds__(FC_BLOCK) k_gauss_seidel(KArgs<double> A) {
+__global__ void __launch_bounds__(FC_BLOCK, 1) k_gauss_seidel(KArgs<double> A) {
   const CsrView<double>& S = A.S;
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, G = gridDim.x * blockDim.x, n = S.n;
   int ph = 0;
+  SweepCtx X = sweep_ctx(S, fc_smem);
+  double* ring = (double*)X.ring;
   double* xa = A.x;
   double* xb = A.w;
   double res0 = 0.0, resl = 0.0, factor = 0.0, resor = 0.0;
   int itr_used = 0, early = 0;
   for (int l = 1; l <= A.itr_max; ++l) {
     double red[2] = {0.0, 0.0};
-    for (int lev = 0; lev < S.nlf; ++lev) {
-      const int b = __ldg(S.lfp + lev), e = __ldg(S.lfp + lev + 1);
-      for (int idx = b + gt; idx < e; idx += G) {
-        const int i = __ldg(S.lfr + idx);
-        const int k0 = __ldg(S.ia + i), k1 = __ldg(S.ia + i + 1);
-        double s = ldcg(A.b + i);
-        for (int k = k0; k < k1; ++k) {
-          const int j = __ldg(S.ja + k);
-          const double xj = (j < i) ? ldcg(xb + j) : ldcg(xa + j);
-          s = __dsub_rn(s, __dmul_rn(__ldg(S.a + k), xj));
-        }
-        const double aii = __ldg(S.a + __ldg(S.dg + i));
-        const double xi = __dadd_rn(ldcg(xa + i), __ddiv_rn(s, __dadd_rn(aii, FC_SMALL)));
-        xb[i] = xi;
-        red[0] += fabs(s);
-        red[1] += fabs(aii * xi);
+    for (int i = gt; i < n; i += G) xb[i] = Sentinel<double>::value();
+    if (!grid_sync(A.C)) return;
+    auto gpre = [&](RowIn<double>& r) { r.q = ldcg(A.b + r.i); };
+    auto rowf = [&](const RowIn<double>& r) {
+      const int i = r.i;
+      const int kd = r.kb + row_entries(r, S.ia, S.dg, true), k1 = __ldg(S.ia + i + 1);
+      double s = r.q;
+      for (int k = r.kb; k < k1; ++k) {
+        const double xj = k < kd ? entry_value(r, k - r.kb, S.code, (const double*)ring, (const double*)xb,
+                                               X.abort_flag, A.C)
+                                 : ldcg(xa + __ldg(S.ja + k));
+        s = __dsub_rn(s, __dmul_rn(__ldg(S.a + k), xj));
       }
-      if (lev + 1 < S.nlf)
-        if (!grid_sync(A.C)) return;
-    }
+      const double aii = __ldg(S.a + kd);
+      const double xi = __dadd_rn(ldcg(xa + i), __ddiv_rn(s, __dadd_rn(aii, FC_SMALL)));
+      red[0] += fabs(s);
+      red[1] += fabs(aii * xi);
+      return xi;
+    };
+    if (!tile_sweep(A.C, S.F, S.a, S.code, (const double*)xb, ring, X.abort_flag, xb, gpre, rowf)) return;
     if (!grid_reduce<2>(A.C, ph, red)) return;
     double* t = xa; xa = xb; xb = t;
     if (l == 1) {
@@ -321,18 +386,22 @@ __global__ void __launch_bounds__(FC_BLOCK) k_gauss_seidel(KArgs<double> A) {
 
 // preconditioner only: d (DIC or DILU) and optionally z = M^-1 q
 template <class T, bool DILU>
-__global__ void __launch_bounds__(FC_BLOCK) k_precond(KArgs<T> A, int apply) {
+__global__ void __launch_bounds__(FC_BLOCK, 1) k_precond(KArgs<T> A, int apply) {
+  SweepCtx X = sweep_ctx(A.S, fc_smem);
   if (!A.skip_setup)
-    if (!precond_setup<T, DILU>(A.C, A.S, A.d)) return;
+    if (!precond_setup<T, DILU>(A.C, A.S, X, A.d)) return;
   if (!apply) return;
   const T* q = A.b;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.S.n; i += gridDim.x * blockDim.x)
+    A.u[i] = Sentinel<T>::value();
+  if (!grid_sync(A.C)) return;
   auto pre = [&](int i) { return ldcg(q + i); };
   auto nopost = [&](int, T) {};
-  precond_apply(A.C, A.S, A.d, A.z, pre, nopost, false);
+  precond_apply(A.C, A.S, X, A.d, A.u, A.z, pre, nopost, false);
 }
 
 // r = b - A x in FP64 with L1 norm (refinement step of the mixed solve)
-__global__ void __launch_bounds__(FC_BLOCK) k_residual64(KArgs<double> A) {
+__global__ void __launch_bounds__(FC_BLOCK, 1) k_residual64(KArgs<double> A) {
   int ph = 0;
   double l1;
   if (!residual_l1(A, ph, l1)) return;
@@ -373,8 +442,8 @@ CsrSystem::~CsrSystem() {
 }
 
 static void build_levels(int n, const std::vector<int>& ia, const std::vector<int>& ja, const std::vector<int>& dg,
-                         bool lower, LevelSchedule& L) {
-  std::vector<int> lev(n, 0);
+                         bool lower, LevelSchedule& L, std::vector<int>& lev) {
+  lev.assign(n, 0);
   int nlev = 0;
   if (lower) {
     for (int i = 0; i < n; ++i) {
@@ -404,8 +473,33 @@ static void build_levels(int n, const std::vector<int>& ia, const std::vector<in
   for (int i = 0; i < n; ++i) L.h_rows[pos[lev[i]]++] = i;  // ascending row order inside a level
 }
 
-int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, const int* ja1, const int* diag1) {
+static int upload_sweep(fc_ctx* ctx, const SweepSchedule& S, DevSweep& D) {
+  D.ntiles = S.ntiles; D.nlev = S.nlev; D.R = S.R; D.max_slots = S.max_slots;
+  D.cross = S.cross_tile_entries; D.ring = S.ring_entries; D.global_same = S.global_same_tile_entries;
+  auto put = [&](DVec<int>& d, const std::vector<int>& h) -> int {
+    FC_CUDA_TRY(ctx, d.alloc(std::max<size_t>(1, h.size())));
+    if (!h.empty()) FC_CUDA_TRY(ctx, cudaMemcpy(d.p, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
+    return FC_OK;
+  };
+  int st;
+  if ((st = put(D.tile_step_ptr, S.tile_step_ptr)) || (st = put(D.step_level, S.step_level)) ||
+      (st = put(D.tile_slots, S.tile_slots)) || (st = put(D.step_row_ptr, S.step_row_ptr)) ||
+      (st = put(D.rows, S.rows)) || (st = put(D.kbne, S.kbne)))
+    return st;
+  return FC_OK;
+}
+
+// step cost and cross-tile latency used to compare tile counts (measured on
+// GB300: a step of ~100 FP64 rows takes a few tenths of a microsecond, a flag
+// published by one SM is seen by another about a microsecond later)
+#define FC_SWEEP_TAU0_US 0.08
+#define FC_SWEEP_ROW_US 0.002
+#define FC_SWEEP_HOP_US 1.0
+
+int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, const int* ja1, const int* diag1,
+                    const double* xyz) {
   if (n <= 0 || nnz < n) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "csr pattern: n <= 0 or nnz < n");
+  if (nnz >= (1 << 27)) return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "csr pattern: nnz >= 2^27");
   std::vector<int> ia(n + 1), ja(nnz), dg(n);
   // the caller's arrays may live on the host or the device
   auto fetch = [&](const int* src, int* dst, size_t cnt) -> int {
@@ -449,8 +543,34 @@ int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, c
   s->n = n;
   s->nnz = nnz;
   s->tslot_oob = oob;
-  build_levels(n, ia, ja, dg, true, s->lf);
-  build_levels(n, ia, ja, dg, false, s->lb);
+  std::vector<int> levf, levb;
+  build_levels(n, ia, ja, dg, true, s->lf, levf);
+  build_levels(n, ia, ja, dg, false, s->lb, levb);
+  // tiled pipeline schedules: at most one tile per SM; the tile count is
+  // chosen among a few candidates by the critical-path estimate
+  std::vector<int> code(nnz, 0);
+  SweepSchedule SF, SB;
+  const int sms = std::max(1, ctx->num_sms);
+  int tiles = sms;
+  {
+    double best = 1e300;
+    const int cand[4] = {sms, (3 * sms) / 4, sms / 2, sms / 4};
+    std::vector<int> scratch(nnz, 0);
+    for (int ci = 0; ci < 4; ++ci) {
+      if (cand[ci] < 1 || (ci > 0 && cand[ci] == cand[ci - 1])) continue;
+      SweepSchedule trial;
+      build_sweep_schedule(n, ia.data(), ja.data(), dg.data(), levf, s->lf.nlev, true, cand[ci], xyz, trial, scratch);
+      const double est = estimate_sweep_us(trial, FC_SWEEP_TAU0_US, FC_SWEEP_ROW_US, FC_SWEEP_HOP_US);
+      if (est < best) { best = est; tiles = cand[ci]; }
+    }
+    s->est_sweep_us = best;
+  }
+  build_sweep_schedule(n, ia.data(), ja.data(), dg.data(), levf, s->lf.nlev, true, tiles, xyz, SF, code);
+  build_sweep_schedule(n, ia.data(), ja.data(), dg.data(), levb, s->lb.nlev, false, tiles, xyz, SB, code);
+  int st2;
+  if ((st2 = upload_sweep(ctx, SF, s->sf)) || (st2 = upload_sweep(ctx, SB, s->sb))) return st2;
+  FC_CUDA_TRY(ctx, s->code.alloc(nnz));
+  FC_CUDA_TRY(ctx, cudaMemcpy(s->code.p, code.data(), nnz * sizeof(int), cudaMemcpyHostToDevice));
   FC_CUDA_TRY(ctx, s->ia.alloc(n + 1));
   FC_CUDA_TRY(ctx, s->ja.alloc(nnz));
   FC_CUDA_TRY(ctx, s->diag.alloc(n));
@@ -492,7 +612,7 @@ int sys_alloc_work(fc_ctx* ctx, CsrSystem* s) {
 static int alloc_work32(fc_ctx* ctx, CsrSystem* s) {
   const int n = s->n;
   FC_CUDA_TRY(ctx, s->a32.alloc(s->nnz));
-  DVec<float>* v32[] = {&s->fr, &s->fr0, &s->fp, &s->fu, &s->fz, &s->fv, &s->fd, &s->fx};
+  DVec<float>* v32[] = {&s->fr, &s->fr0, &s->fp, &s->fu, &s->fz, &s->fv, &s->fd, &s->fx, &s->fy, &s->fw};
   for (auto* v : v32) FC_CUDA_TRY(ctx, v->alloc(n));
   return FC_OK;
 }
@@ -503,11 +623,22 @@ int sys_upload_values(fc_ctx* ctx, CsrSystem* s, const double* a, bool a_on_devi
   return FC_OK;
 }
 
+static TileSched tsched_of(DevSweep& D) {
+  TileSched t;
+  t.ntiles = D.ntiles; t.nlev = D.nlev; t.R = D.R; t.max_slots = D.max_slots;
+  t.tile_step_ptr = D.tile_step_ptr.p; t.step_level = D.step_level.p; t.tile_slots = D.tile_slots.p;
+  t.step_row_ptr = D.step_row_ptr.p; t.rows = D.rows.p; t.kbne = D.kbne.p;
+  return t;
+}
+
 template <class T>
 static CsrView<T> view_of(CsrSystem* s, const T* a) {
   CsrView<T> v;
   v.n = s->n;
   v.ia = s->ia.p; v.ja = s->ja.p; v.dg = s->diag.p; v.ts = s->tslot.p; v.a = a;
+  v.code = s->code.p;
+  v.F = tsched_of(s->sf);
+  v.B = tsched_of(s->sb);
   v.lfp = s->lf.ptr.p; v.lfr = s->lf.rows.p; v.nlf = s->lf.nlev;
   v.lbp = s->lb.ptr.p; v.lbr = s->lb.rows.p; v.nlb = s->lb.nlev;
   return v;
@@ -526,12 +657,20 @@ static int coop_blocks(fc_ctx* ctx, const void* fn, int n, int per_sm_cap) {
 
 template <class T>
 static int launch_coop(fc_ctx* ctx, CsrSystem* s, const void* fn, KArgs<T>& A, void** extra, int nextra) {
-  int blocks = coop_blocks(ctx, fn, s->n, 2);
+  // one block per tile of the sweep schedules (every tile must be resident)
+  const size_t smem = sweep_smem_bytes<T>(s->sf.R, s->sf.max_slots, s->sb.R, s->sb.max_slots);
+  if (smem > 48 * 1024)
+    FC_CUDA_TRY(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int nb = 0;
+  FC_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, FC_BLOCK, smem));
+  const int blocks = std::max(1, std::max(s->sf.ntiles, s->sb.ntiles));
+  if (nb * ctx->num_sms < blocks)
+    return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "sweep schedule needs more resident blocks than the GPU holds");
   FC_CUDA_TRY(ctx, cudaMemsetAsync(s->bar.p, 0, 2 * sizeof(unsigned), ctx->stream));
   FC_CUDA_TRY(ctx, cudaMemsetAsync(s->status.p, 0, sizeof(int), ctx->stream));
   void* args[4] = {&A, nullptr, nullptr, nullptr};
   for (int i = 0; i < nextra; ++i) args[1 + i] = extra[i];
-  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(FC_BLOCK), args, 0, ctx->stream);
+  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(FC_BLOCK), args, smem, ctx->stream);
   if (e != cudaSuccess) return fc_fail(ctx, FC_ERR_CUDA, "cooperative launch", e);
   ctx->kernel_launches++;
   return FC_OK;
@@ -545,6 +684,8 @@ static KArgs<T> make_args(CsrSystem* s, const T* a, T* x, const T* b, T* r, T* r
   A.C.bar = s->bar.p; A.C.part = s->part.p; A.C.status = s->status.p; A.C.out = s->out.p;
   A.x = x; A.b = b; A.r = r; A.r0 = r0; A.p = p; A.u = u; A.z = z; A.v = v; A.d = d; A.w = w;
   A.itr_max = itr_max; A.tol_abs = tol_abs; A.tol_rel = tol_rel; A.skip_setup = 0;
+  A.trace = nullptr;
+  A.trace_cap = 0;
   return A;
 }
 
@@ -566,9 +707,22 @@ static int solve_fp64(fc_ctx* ctx, CsrSystem* s, const std::string& solver, cons
                       const double* b, int itr_max, double tol_abs, double tol_rel, SolveResult* res) {
   KArgs<double> A = make_args<double>(s, a, x, b, s->r.p, s->r0.p, s->p.p, s->u.p, s->z.p, s->v.p, s->d.p,
                                       s->w.p, itr_max, tol_abs, tol_rel);
+  const bool traced = ctx->tracing && solver == "iccg";
+  if (traced) {
+    const int nb = std::max(1, max(s->sf.ntiles, s->sb.ntiles));
+    const int cap = max(s->sf.nlev, s->sb.nlev) + 1;
+    FC_CUDA_TRY(ctx, ctx->trace.alloc((size_t)nb * FC_TRACE_N + (size_t)2 * nb * cap * 2));
+    FC_CUDA_TRY(ctx, cudaMemsetAsync(ctx->trace.p, 0, ctx->trace.bytes(), ctx->stream));
+    A.trace = ctx->trace.p;
+    A.trace_cap = cap;
+    ctx->trace_blocks = nb;
+    ctx->trace_cap = cap;
+  }
   FC_CUDA_TRY(ctx, cudaMemsetAsync(s->out.p, 0, FC_OUT_N * sizeof(double), ctx->stream));
   int st;
-  if (solver == "iccg") st = launch_coop(ctx, s, (const void*)k_iccg<double>, A, nullptr, 0);
+  if (solver == "iccg")
+    st = launch_coop(ctx, s, traced ? (const void*)k_iccg<double, true> : (const void*)k_iccg<double>, A, nullptr,
+                     0);
   else if (solver == "bicgstab") {
     if (s->tslot_oob) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "bicgstab: pattern is not structurally symmetric");
     st = launch_coop(ctx, s, (const void*)k_bicgstab<double>, A, nullptr, 0);
@@ -627,16 +781,12 @@ static int solve_mixed(fc_ctx* ctx, CsrSystem* s, const std::string& solver, con
     k_to_float<<<eb, 256, 0, ctx->stream>>>(s->r.p, s->fr0.p, n);
     k_zero_float<<<eb, 256, 0, ctx->stream>>>(s->fx.p, n);
     ctx->kernel_launches += 2;
-    KArgs<float> F = make_args<float>(s, s->a32.p, s->fx.p, s->fr0.p, s->fr.p, s->fv.p /*r0*/, s->fp.p, s->fu.p,
-                                      s->fz.p, s->fv.p, s->fd.p, nullptr, std::min(inner_itmax, itr_max - total_itr),
+    KArgs<float> F = make_args<float>(s, s->a32.p, s->fx.p, s->fr0.p, s->fr.p, s->fy.p /*r0*/, s->fp.p, s->fu.p,
+                                      s->fz.p, s->fv.p, s->fd.p, s->fw.p, std::min(inner_itmax, itr_max - total_itr),
                                       0.0, inner_tol);
     F.skip_setup = outer > 0 ? 1 : 0;
     const void* fn = solver == "iccg" ? (const void*)k_iccg<float>
                      : solver == "bicgstab" ? (const void*)k_bicgstab<float> : (const void*)k_dpcg<float>;
-    if (solver == "bicgstab") {
-      // bicgstab needs r0 distinct from v: use the x scratch of the FP64 side
-      F.r0 = reinterpret_cast<float*>(s->w.p);
-    }
     if ((st = launch_coop(ctx, s, fn, F, nullptr, 0))) return st;
     FC_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_out, s->out.p, FC_OUT_N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     FC_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_status, s->status.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -661,7 +811,7 @@ int sys_solve(fc_ctx* ctx, CsrSystem* s, const char* solver_c, const double* a, 
   if (!a) a = s->a.p;
   std::string solver(solver_c ? solver_c : "");
   *res = SolveResult();
-  FC_CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+  FC_CUDA_TRY(ctx, cudaEventRecord(ctx->sev0, ctx->stream));
   int st;
   if (solver == "pmgmres") {
     st = gmres_solve(ctx, s, a, x, b, itr_max, 4, tol_abs, tol_rel, res);
@@ -671,10 +821,10 @@ int sys_solve(fc_ctx* ctx, CsrSystem* s, const char* solver_c, const double* a, 
     st = solve_fp64(ctx, s, solver, a, x, b, itr_max, tol_abs, tol_rel, res);
   }
   if (st) return st;
-  FC_CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
-  FC_CUDA_TRY(ctx, cudaEventSynchronize(ctx->ev1));
+  FC_CUDA_TRY(ctx, cudaEventRecord(ctx->sev1, ctx->stream));
+  FC_CUDA_TRY(ctx, cudaEventSynchronize(ctx->sev1));
   float ms = 0;
-  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  cudaEventElapsedTime(&ms, ctx->sev0, ctx->sev1);
   res->ms = ms;
   if (res->status == FC_ERR_TIMEOUT) return fc_fail_msg(ctx, FC_ERR_TIMEOUT, "solver grid barrier timed out");
   if (res->status < 0) return fc_fail_msg(ctx, res->status, "solver reported an error (NaN/Inf or breakdown)");
@@ -698,5 +848,41 @@ int sys_precond(fc_ctx* ctx, CsrSystem* s, int dilu, const double* q, double* z_
     FC_CUDA_TRY(ctx, cudaMemcpyAsync(z_out, s->z.p, s->n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   if (*s->h_status) return fc_fail_msg(ctx, *s->h_status, "preconditioner kernel failed");
+  return FC_OK;
+}
+
+// Trace of the last FP64 ICCG solve run with fc_set_tracing on.
+// out[0..FC_TRACE_N) = cycles summed over the blocks that ran, per phase;
+// out[FC_TRACE_N] = those blocks; out[FC_TRACE_N+1] = blocks of the launch
+// (B); out[FC_TRACE_N+2] = stamps per tile and sweep (K); with timeline
+// non-null it receives the stamps as [2][B][K][2] (clock64, globaltimer).
+extern "C" int fc_trace_get(fc_ctx* ctx, double* out, unsigned long long* timeline) {
+  if (!ctx || !out) return FC_ERR_BAD_INPUT;
+  if (!ctx->trace.p) return fc_fail_msg(ctx, FC_ERR_STATE, "no trace recorded");
+  FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  const int nb = ctx->trace_blocks, cap = ctx->trace_cap;
+  std::vector<unsigned long long> h(ctx->trace.n);
+  FC_CUDA_TRY(ctx, cudaMemcpy(h.data(), ctx->trace.p, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  int used = 0;
+  for (int k = 0; k < FC_TRACE_N; ++k) out[k] = 0.0;
+  for (int b = 0; b < nb; ++b) {
+    bool any = false;
+    for (int k = 0; k < FC_TRACE_N; ++k) {
+      out[k] += (double)h[(size_t)b * FC_TRACE_N + k];
+      any |= h[(size_t)b * FC_TRACE_N + k] != 0;
+    }
+    used += any;
+  }
+  out[FC_TRACE_N] = used;
+  out[FC_TRACE_N + 1] = nb;
+  out[FC_TRACE_N + 2] = cap;
+  if (timeline)
+    std::copy(h.begin() + (size_t)nb * FC_TRACE_N, h.end(), timeline);
+  return FC_OK;
+}
+
+extern "C" int fc_set_tracing(fc_ctx* ctx, int on) {
+  if (!ctx) return FC_ERR_BAD_INPUT;
+  ctx->tracing = on;
   return FC_OK;
 }

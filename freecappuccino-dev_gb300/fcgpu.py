@@ -100,6 +100,9 @@ def lib():
         "fc_laplacian": (i, [vp, vp, vp, C.c_ulonglong]),
         "fc_solve_field": (i, [vp, cp, cp, cp, vp, i, d, d, cp, C.POINTER(SolveInfo)]),
         "fc_simple_set_params": (i, [vp, vp]),
+        "fc_sweep_stats": (i, [vp, i, vp]),
+        "fc_set_tracing": (i, [vp, i]),
+        "fc_trace_get": (i, [vp, vp, vp]),
         "fc_init_flmass": (i, [vp]),
         "fc_update_velocity_at_boundary": (i, [vp]),
         "fc_gradp_and_sources": (i, [vp, cp]),
@@ -444,6 +447,31 @@ class Context:
                                    int(itr_max), float(tol_abs), float(tol_rel), chvar.encode(), C.byref(info))
         self._check(st, "fc_solve_field")
         return float(r0[0]), info, st
+
+    def sweep_stats(self, which=0):
+        out = np.zeros(8)
+        self._check(self.L.fc_sweep_stats(self.h, which, _ptr(out)), "fc_sweep_stats")
+        keys = ("tiles", "levels", "max_slots", "ring_depth", "est_sweep_us", "ring_entries", "cross_tile_entries",
+                "global_same_tile_entries")
+        return dict(zip(keys, [float(v) for v in out]))
+
+    def set_tracing(self, on=True):
+        self._check(self.L.fc_set_tracing(self.h, int(on)), "fc_set_tracing")
+
+    def trace(self, timeline=False):
+        """Phase cycles of the last traced ICCG solve: (dict phase -> cycles
+        summed over blocks, blocks); with timeline=True also the step stamps
+        as a uint64 array [sweep(fwd, bwd)][tile][step][clock64, globaltimer]."""
+        out = np.zeros(11)
+        self._check(self.L.fc_trace_get(self.h, _ptr(out), None), "fc_trace_get")
+        keys = ("setup", "fwd_sweep", "sweep_barrier", "bwd_sweep", "dot", "p_update", "spmv", "xr_update")
+        res = (dict(zip(keys, out[:8].tolist())), int(out[8]))
+        if not timeline:
+            return res
+        nb, cap = int(out[9]), int(out[10])
+        tl = np.zeros((2, nb, cap, 2), dtype=np.uint64)
+        self._check(self.L.fc_trace_get(self.h, _ptr(out), _ptr(tl)), "fc_trace_get")
+        return res + (tl,)
 
     # ------------------------------------------------------------ SIMPLE
     def simple_params(self, prm):

@@ -1,0 +1,350 @@
+// Tiled pipeline schedule of a sparse triangular sweep: chains, tiles, steps,
+// shared-memory ring codes and cross-tile waits (see fc_schedule.hpp).
+#include "fc_schedule.hpp"
+
+#include <algorithm>
+#include <deque>
+#include <numeric>
+#include <utility>
+
+namespace {
+
+struct Deps {
+  const int *ia, *ja, *dg;
+  bool fwd;
+  int begin(int i) const { return fwd ? ia[i] : dg[i] + 1; }
+  int end(int i) const { return fwd ? dg[i] : ia[i + 1]; }
+};
+
+}  // namespace
+
+// recursive coordinate bisection of items (chains) weighted by rows into
+// nparts parts; split along the axis of largest extent at the weighted median
+static void rcb(std::vector<int>& items, const std::vector<double>& cx, const std::vector<double>& cy,
+                const std::vector<double>& cz, const std::vector<int>& w, int nparts, int first_part,
+                std::vector<int>& part_of) {
+  if (nparts <= 1 || items.size() <= 1) {
+    for (int c : items) part_of[c] = first_part;
+    return;
+  }
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int c : items) {
+    const double p[3] = {cx[c], cy[c], cz[c]};
+    for (int a = 0; a < 3; ++a) { lo[a] = std::min(lo[a], p[a]); hi[a] = std::max(hi[a], p[a]); }
+  }
+  int ax = 0;
+  for (int a = 1; a < 3; ++a)
+    if (hi[a] - lo[a] > hi[ax] - lo[ax]) ax = a;
+  const std::vector<double>& key = ax == 0 ? cx : ax == 1 ? cy : cz;
+  std::stable_sort(items.begin(), items.end(), [&](int a, int b) { return key[a] < key[b]; });
+  const int nl = nparts / 2;
+  long long tot = 0;
+  for (int c : items) tot += w[c];
+  const long long want = tot * nl / nparts;
+  // cut at the widest coordinate gap among the positions whose left weight is
+  // within half a part of the balanced cut, so that grid lines sharing a
+  // coordinate stay on one side and the tile boundaries follow the mesh
+  const long long tol = std::max<long long>(1, tot / nparts / 2);
+  size_t cut = 0, best_near = 1;
+  double best_gap = -1.0;
+  long long acc = 0, best_dist = -1;
+  for (size_t q = 1; q < items.size(); ++q) {
+    acc += w[items[q - 1]];
+    const long long dist = acc > want ? acc - want : want - acc;
+    if (best_dist < 0 || dist < best_dist) { best_dist = dist; best_near = q; }
+    if (dist <= tol) {
+      const double gap = key[items[q]] - key[items[q - 1]];
+      if (gap > best_gap) { best_gap = gap; cut = q; }
+    }
+  }
+  if (cut == 0) cut = best_near;
+  cut = std::max<size_t>(1, std::min(cut, items.size() - 1));
+  std::vector<int> left(items.begin(), items.begin() + cut), right(items.begin() + cut, items.end());
+  rcb(left, cx, cy, cz, w, nl, first_part, part_of);
+  rcb(right, cx, cy, cz, w, nparts - nl, first_part + nl, part_of);
+}
+
+void build_sweep_schedule(int n, const int* ia, const int* ja, const int* dg, const std::vector<int>& lev, int nlev,
+                          bool forward, int ntiles_target, const double* xyz, SweepSchedule& S,
+                          std::vector<int>& code) {
+  S = SweepSchedule();
+  S.n = n;
+  S.nlev = nlev;
+  const Deps D{ia, ja, dg, forward};
+  // ---- 1. chains: a row continues the chain of its latest dependency
+  std::vector<int> chain_of(n, -1), has_succ(n, 0);
+  std::vector<int> chain_first;  // first row (in sweep order) of each chain
+  std::vector<int> chain_rows;   // rows per chain
+  for (int t = 0; t < n; ++t) {
+    const int i = forward ? t : n - 1 - t;
+    int best = -1;
+    for (int k = D.begin(i); k < D.end(i); ++k) {
+      const int j = ja[k];
+      if (has_succ[j]) continue;
+      if (best < 0 || lev[j] > lev[best] || (lev[j] == lev[best] && (forward ? j > best : j < best))) best = j;
+    }
+    if (best >= 0) {
+      has_succ[best] = 1;
+      chain_of[i] = chain_of[best];
+      chain_rows[chain_of[i]]++;
+    } else {
+      chain_of[i] = (int)chain_first.size();
+      chain_first.push_back(i);
+      chain_rows.push_back(1);
+    }
+  }
+  const int nch = (int)chain_first.size();
+  // ---- 2. chain graph (undirected adjacency through dependencies)
+  std::vector<std::pair<int, int>> edges;
+  edges.reserve((size_t)n * 2);
+  for (int i = 0; i < n; ++i)
+    for (int k = D.begin(i); k < D.end(i); ++k) {
+      const int a = chain_of[i], b = chain_of[ja[k]];
+      if (a != b) { edges.push_back({a, b}); edges.push_back({b, a}); }
+    }
+  std::sort(edges.begin(), edges.end());
+  edges.erase(std::unique(edges.begin(), edges.end()), edges.end());
+  std::vector<int> adj_ptr(nch + 1, 0), adj;
+  for (auto& e : edges) adj_ptr[e.first + 1]++;
+  for (int c = 0; c < nch; ++c) adj_ptr[c + 1] += adj_ptr[c];
+  adj.resize(edges.size());
+  for (size_t q = 0; q < edges.size(); ++q) adj[q] = edges[q].second;  // sorted by (first, second)
+  // ---- 3. tiles: grow regions over the chain graph in breadth-first order
+  const int T = std::max(1, std::min(ntiles_target, nch));
+  const long long target = (n + T - 1) / T;
+  std::vector<int> tile_of_chain(nch, -1);
+  std::vector<long long> tile_rows;
+  if (xyz) {
+    std::vector<double> cx(nch, 0.0), cy(nch, 0.0), cz(nch, 0.0);
+    for (int i = 0; i < n; ++i) {
+      const int c = chain_of[i];
+      cx[c] += xyz[i]; cy[c] += xyz[n + i]; cz[c] += xyz[2 * (size_t)n + i];
+    }
+    for (int c = 0; c < nch; ++c) { cx[c] /= chain_rows[c]; cy[c] /= chain_rows[c]; cz[c] /= chain_rows[c]; }
+    std::vector<int> items(nch);
+    std::iota(items.begin(), items.end(), 0);
+    rcb(items, cx, cy, cz, chain_rows, T, 0, tile_of_chain);
+    // drop empty parts
+    std::vector<int> used(T, 0);
+    for (int c = 0; c < nch; ++c) used[tile_of_chain[c]] = 1;
+    std::vector<int> nid(T, -1);
+    int m = 0;
+    for (int t = 0; t < T; ++t)
+      if (used[t]) nid[t] = m++;
+    for (int c = 0; c < nch; ++c) tile_of_chain[c] = nid[tile_of_chain[c]];
+    tile_rows.assign(m, 0);
+    for (int c = 0; c < nch; ++c) tile_rows[tile_of_chain[c]] += chain_rows[c];
+  } else {
+    std::deque<int> q;
+    int next_seed = 0;
+    while (true) {
+      while (next_seed < nch && tile_of_chain[next_seed] >= 0) ++next_seed;
+      if (next_seed >= nch) break;
+      const int t = (int)tile_rows.size();
+      tile_rows.push_back(0);
+      q.clear();
+      q.push_back(next_seed);
+      tile_of_chain[next_seed] = t;
+      while (!q.empty() && tile_rows[t] < target) {
+        const int c = q.front();
+        q.pop_front();
+        if (tile_of_chain[c] != t) continue;
+        tile_rows[t] += chain_rows[c];
+        for (int e = adj_ptr[c]; e < adj_ptr[c + 1] && tile_rows[t] < target; ++e) {
+          const int d = adj[e];
+          if (tile_of_chain[d] < 0) { tile_of_chain[d] = t; q.push_back(d); }
+        }
+      }
+      // chains queued but not consumed go back to the pool
+      for (int c : q)
+        if (tile_of_chain[c] == t) tile_of_chain[c] = -1;
+    }
+  }
+  // every chain now has a tile; merge the smallest tiles until at most T remain
+  int ntiles = (int)tile_rows.size();
+  if (ntiles > T) {
+    std::vector<int> remap(ntiles);
+    std::iota(remap.begin(), remap.end(), 0);
+    auto find = [&](int x) { while (remap[x] != x) x = remap[x] = remap[remap[x]]; return x; };
+    // tile adjacency through chain edges
+    std::vector<std::pair<int, int>> tedges;
+    for (int c = 0; c < nch; ++c)
+      for (int e = adj_ptr[c]; e < adj_ptr[c + 1]; ++e) {
+        int a = tile_of_chain[c], b = tile_of_chain[adj[e]];
+        if (a != b) tedges.push_back({a, b});
+      }
+    std::sort(tedges.begin(), tedges.end());
+    tedges.erase(std::unique(tedges.begin(), tedges.end()), tedges.end());
+    int alive = ntiles;
+    while (alive > T) {
+      int small = -1;
+      for (int t = 0; t < ntiles; ++t)
+        if (find(t) == t && (small < 0 || tile_rows[t] < tile_rows[small])) small = t;
+      int best = -1;
+      for (auto& e : tedges) {
+        if (find(e.first) != small) continue;
+        int o = find(e.second);
+        if (o != small && (best < 0 || tile_rows[o] < tile_rows[best])) best = o;
+      }
+      if (best < 0)  // isolated: merge into the smallest other tile
+        for (int t = 0; t < ntiles; ++t)
+          if (find(t) == t && t != small && (best < 0 || tile_rows[t] < tile_rows[best])) best = t;
+      remap[small] = best;
+      tile_rows[best] += tile_rows[small];
+      --alive;
+    }
+    std::vector<int> newid(ntiles, -1);
+    int m = 0;
+    for (int t = 0; t < ntiles; ++t)
+      if (find(t) == t) newid[t] = m++;
+    for (int c = 0; c < nch; ++c) tile_of_chain[c] = newid[find(tile_of_chain[c])];
+    ntiles = m;
+  }
+  S.ntiles = ntiles;
+  // ---- 4. per tile: steps (distinct levels) and slots (chains sharing a slot
+  //         when their level ranges do not overlap)
+  std::vector<int> chain_lo(nch, 1 << 30), chain_hi(nch, -1);
+  for (int i = 0; i < n; ++i) {
+    const int c = chain_of[i];
+    chain_lo[c] = std::min(chain_lo[c], lev[i]);
+    chain_hi[c] = std::max(chain_hi[c], lev[i]);
+  }
+  std::vector<std::vector<int>> tile_chains(ntiles);
+  for (int c = 0; c < nch; ++c) tile_chains[tile_of_chain[c]].push_back(c);
+  std::vector<int> slot_of_chain(nch, 0);
+  std::vector<std::vector<int>> tile_levels(ntiles);
+  std::vector<int> row_tile(n), row_step(n), row_slot(n);
+  {
+    for (int t = 0; t < ntiles; ++t) {
+      auto& ch = tile_chains[t];
+      std::sort(ch.begin(), ch.end(), [&](int a, int b) {
+        return chain_lo[a] != chain_lo[b] ? chain_lo[a] < chain_lo[b] : a < b;
+      });
+      std::vector<int> slot_free;  // level after which the slot is free
+      for (int c : ch) {
+        int s = -1;
+        for (size_t q = 0; q < slot_free.size(); ++q)
+          if (slot_free[q] < chain_lo[c] && (s < 0 || slot_free[q] > slot_free[s])) s = (int)q;
+        if (s < 0) { s = (int)slot_free.size(); slot_free.push_back(-1); }
+        slot_free[s] = chain_hi[c];
+        slot_of_chain[c] = s;
+      }
+      S.tile_slots.push_back(std::max(1, (int)slot_free.size()));
+      S.max_slots = std::max(S.max_slots, S.tile_slots.back());
+    }
+    for (int i = 0; i < n; ++i) {
+      const int t = tile_of_chain[chain_of[i]];
+      tile_levels[t].push_back(lev[i]);
+    }
+    for (int t = 0; t < ntiles; ++t) {
+      auto& L = tile_levels[t];
+      std::sort(L.begin(), L.end());
+      L.erase(std::unique(L.begin(), L.end()), L.end());
+    }
+  }
+  S.R = std::max(1, std::min(4, (int)((160 * 1024) / (8LL * std::max(1, S.max_slots)))));
+  S.tile_step_ptr.assign(ntiles + 1, 0);
+  for (int t = 0; t < ntiles; ++t) S.tile_step_ptr[t + 1] = S.tile_step_ptr[t] + (int)tile_levels[t].size();
+  const int nsteps = S.tile_step_ptr[ntiles];
+  S.step_level.resize(nsteps);
+  S.step_row_ptr.assign(nsteps + 1, 0);
+  for (int t = 0; t < ntiles; ++t)
+    for (size_t s = 0; s < tile_levels[t].size(); ++s) {
+      const int gs = S.tile_step_ptr[t] + (int)s;
+      S.step_level[gs] = tile_levels[t][s];
+      S.step_row_ptr[gs + 1] = S.step_row_ptr[gs] + S.tile_slots[t];
+    }
+  S.rows.assign(S.step_row_ptr[nsteps], -1);
+  // place every row (per tile level -> step lookup by binary search)
+  for (int i = 0; i < n; ++i) {
+    const int t = tile_of_chain[chain_of[i]];
+    const auto& L = tile_levels[t];
+    const int s = (int)(std::lower_bound(L.begin(), L.end(), lev[i]) - L.begin());
+    const int slot = slot_of_chain[chain_of[i]];
+    row_tile[i] = t;
+    row_step[i] = s;
+    row_slot[i] = slot;
+    S.rows[S.step_row_ptr[S.tile_step_ptr[t] + s] + slot] = i;
+  }
+  S.kbne.assign(S.rows.size(), 0);
+  for (size_t q = 0; q < S.rows.size(); ++q) {
+    const int i = S.rows[q];
+    if (i < 0) continue;
+    const int kb = D.begin(i), ne = D.end(i) - kb;
+    S.kbne[q] = (kb << 4) | std::min(ne, 15);
+  }
+  // ---- 5. entry codes and waits
+  std::vector<std::vector<std::pair<int, int>>> waits(nsteps);
+  for (int i = 0; i < n; ++i) {
+    const int t = row_tile[i], s = row_step[i];
+    const int gs = S.tile_step_ptr[t] + s;
+    for (int k = D.begin(i); k < D.end(i); ++k) {
+      const int j = ja[k];
+      if (row_tile[j] == t && s - row_step[j] < S.R) {
+        code[k] = (row_step[j] % S.R) * S.tile_slots[t] + row_slot[j];
+        S.ring_entries++;
+      } else {
+        code[k] = -j - 2;
+        if (row_tile[j] != t) {
+          waits[gs].push_back({row_tile[j], lev[j] + 1});
+          S.cross_tile_entries++;
+        } else {
+          S.global_same_tile_entries++;
+        }
+      }
+    }
+  }
+  S.wait_ptr.assign(nsteps + 1, 0);
+  for (int gs = 0; gs < nsteps; ++gs) {
+    auto& w = waits[gs];
+    std::sort(w.begin(), w.end());
+    // keep the largest requirement per producer tile
+    std::vector<std::pair<int, int>> m;
+    for (auto& p : w) {
+      if (!m.empty() && m.back().first == p.first) m.back().second = std::max(m.back().second, p.second);
+      else m.push_back(p);
+    }
+    for (auto& p : m) { S.wait_tile.push_back(p.first); S.wait_level.push_back(p.second); }
+    S.wait_ptr[gs + 1] = (int)S.wait_tile.size();
+  }
+}
+
+// Critical-path estimate of a sweep: every step of a tile costs
+// tau0 + per_row * (rows in the step); a step starts when the tile's previous
+// step is done and, for each producer it waits on, hop microseconds after the
+// producer published the needed progress.  Returns microseconds.
+double estimate_sweep_us(const SweepSchedule& S, double tau0, double per_row, double hop) {
+  std::vector<std::vector<double>> pub(S.ntiles);
+  std::vector<int> cur(S.ntiles, 0);
+  // steps of all tiles in level order (a valid processing order)
+  std::vector<std::pair<int, int>> order;  // (level, global step)
+  for (int t = 0; t < S.ntiles; ++t)
+    for (int gs = S.tile_step_ptr[t]; gs < S.tile_step_ptr[t + 1]; ++gs) order.push_back({S.step_level[gs], gs});
+  std::sort(order.begin(), order.end());
+  std::vector<int> tile_of_step(S.step_level.size());
+  for (int t = 0; t < S.ntiles; ++t)
+    for (int gs = S.tile_step_ptr[t]; gs < S.tile_step_ptr[t + 1]; ++gs) tile_of_step[gs] = t;
+  double tmax = 0.0;
+  for (auto& o : order) {
+    const int gs = o.second, t = tile_of_step[gs];
+    double st = pub[t].empty() ? 0.0 : pub[t].back();
+    for (int w = S.wait_ptr[gs]; w < S.wait_ptr[gs + 1]; ++w) {
+      const int q = S.wait_tile[w], need = S.wait_level[w];
+      const int q0 = S.tile_step_ptr[q];
+      // first published step of q whose next level reaches need
+      int lo = 0, hi = (int)pub[q].size() - 1, found = -1;
+      while (lo <= hi) {
+        const int mid = (lo + hi) / 2;
+        const int nxt = (q0 + mid + 1 < S.tile_step_ptr[q + 1]) ? S.step_level[q0 + mid + 1] : S.nlev;
+        if (nxt >= need) { found = mid; hi = mid - 1; } else lo = mid + 1;
+      }
+      if (found >= 0) st = std::max(st, pub[q][found] + hop);
+    }
+    int rowsn = 0;
+    for (int sl = 0; sl < S.tile_slots[t]; ++sl) rowsn += S.rows[S.step_row_ptr[gs] + sl] >= 0;
+    const double end = st + tau0 + per_row * rowsn;
+    pub[t].push_back(end);
+    tmax = std::max(tmax, end);
+  }
+  return tmax;
+}

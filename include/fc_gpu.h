@@ -154,6 +154,22 @@ int fc_precond_apply(fc_ctx* ctx, const char* kind, int n, int nnz, const int* i
 /* y = A x (ax_cr, linear_solvers.f90:1173) or y = A^T x (atx_cr, :1079). */
 int fc_spmv(fc_ctx* ctx, int n, int nnz, const int* ia, const int* ja, const double* a, const int* diag,
             const double* x, double* y, int transpose);
+/* Statistics of the tiled sweep schedule of the mesh system (which=0) or of
+ * the cached fc_csrsolve pattern (which=1): out[8] = tiles, levels, widest
+ * tile, ring depth, estimated forward-sweep us, ring-served entries,
+ * cross-tile entries, same-tile global entries. */
+int fc_sweep_stats(fc_ctx* ctx, int which, double* out);
+/* Tracing of the FP64 ICCG kernel (no counterpart in the reference): with
+ * on != 0 the solves run a traced instantiation that records per block the
+ * SM cycles of each phase and, for the forward and backward sweep of the
+ * first iteration, a (clock64, globaltimer) stamp at the start of every step
+ * of every tile.  fc_trace_get: out[11] = cycles summed over the blocks for
+ * setup, forward sweep, sweep barrier, backward sweep, dot product, p update,
+ * SpMV, x/r update; then the blocks that ran, the blocks of the launch (B)
+ * and the stamps per tile (K); timeline (optional, 2*B*K*2 entries)
+ * receives the stamps as [sweep][tile][step][clock, globaltimer]. */
+int fc_set_tracing(fc_ctx* ctx, int on);
+int fc_trace_get(fc_ctx* ctx, double* out, unsigned long long* timeline);
 /* ILU(0) factors of ilu_cr (linear_solvers.f90:1267-1385) in the CSR slots. */
 int fc_ilu0(fc_ctx* ctx, int n, int nnz, const int* ia, const int* ja, const double* a, const int* diag,
             double* l_out);

@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "fc_internal.hpp"
@@ -885,4 +886,118 @@ extern "C" int fc_set_tracing(fc_ctx* ctx, int on) {
   if (!ctx) return FC_ERR_BAD_INPUT;
   ctx->tracing = on;
   return FC_OK;
+}
+
+// ------------------------------------------------ DPCG without allocation
+// fc_dpcg_noalloc: the Jacobi-PCG kernel (k_dpcg, dpcg of
+// linear_solvers.f90:206-359) run on a fixed scratch area in static device
+// memory instead of a CsrSystem workspace, so the call allocates nothing
+// (no cudaMalloc/cudaFree, no event or stream creation, no host heap).
+//
+// Scratch (one per device, this translation unit): r, p, z (FC_NOALLOC_MAX_N
+// doubles each), the grid reduction partials (two sets of FC_NPART per
+// block), and the control block (barrier counters, status, results), which
+// is cleared before every launch.  The first call on a device resolves the
+// scratch address with cudaGetSymbolAddress while that device is current.
+namespace {
+constexpr int NA_MAX_BLOCKS = 1024;
+constexpr size_t NA_VEC = (size_t)FC_NOALLOC_MAX_N * sizeof(double);
+constexpr size_t NA_PART = (size_t)2 * FC_NPART * NA_MAX_BLOCKS * sizeof(double);
+constexpr size_t NA_OUT = (size_t)FC_OUT_N * sizeof(double);
+constexpr size_t NA_CTL = 256;  // bar[2] + status, padded
+constexpr size_t NA_BYTES = 3 * NA_VEC + NA_PART + NA_OUT + NA_CTL;
+static_assert(NA_VEC % 256 == 0 && NA_PART % 256 == 0, "scratch sections stay 256-byte aligned");
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+namespace {
+constexpr int NA_MAX_DEVICES = 64;
+std::mutex g_na_mutex;
+unsigned char* g_na_base[NA_MAX_DEVICES] = {};
+
+int na_fail(char* errmsg, int errlen, int code, const char* msg) {
+  if (errmsg && errlen > 0) std::snprintf(errmsg, (size_t)errlen, "fc_dpcg_noalloc: %s", msg);
+  return code;
+}
+}  // namespace
+
+extern "C" int fc_dpcg_noalloc(void* stream, int n, int nnz, const int* ia, const int* ja, const double* a,
+                               const int* diag, double* x, const double* b, int itr_max, double tol_abs,
+                               double tol_rel, fc_solve_info* info, char* errmsg, int errlen) {
+  if (errmsg && errlen > 0) errmsg[0] = '\0';
+  if (n <= 0 || nnz < n || !ia || !ja || !a || !diag || !x || !b || itr_max < 0)
+    return na_fail(errmsg, errlen, FC_ERR_BAD_INPUT, "bad arguments (n > 0, nnz >= n, non-null device arrays)");
+  if (n > FC_NOALLOC_MAX_N)
+    return na_fail(errmsg, errlen, FC_ERR_BAD_INPUT, "n exceeds FC_NOALLOC_MAX_N (1048576 rows)");
+  for (const void* ptr : {(const void*)ia, (const void*)ja, (const void*)a, (const void*)diag, (const void*)x,
+                          (const void*)b})
+    if (!is_device_ptr(ptr)) return na_fail(errmsg, errlen, FC_ERR_BAD_INPUT, "arrays must be device memory");
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES)
+    return na_fail(errmsg, errlen, FC_ERR_CUDA, "no current CUDA device");
+  unsigned char* base;
+  {
+    std::lock_guard<std::mutex> lock(g_na_mutex);
+    if (!g_na_base[dev]) {
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p) return na_fail(errmsg, errlen, FC_ERR_CUDA, "cudaGetSymbolAddress of the scratch failed");
+      g_na_base[dev] = (unsigned char*)p;
+    }
+    base = g_na_base[dev];
+  }
+  int sms = 0, coop = 0, occ = 0;
+  const void* fn = (const void*)k_dpcg<double>;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, FC_BLOCK, 0) != cudaSuccess || occ < 1)
+    return na_fail(errmsg, errlen, FC_ERR_UNSUPPORTED, "cooperative launch not available");
+  const int blocks = std::min(NA_MAX_BLOCKS, sms * occ);
+
+  double* r = (double*)base;
+  double* p = (double*)(base + NA_VEC);
+  double* z = (double*)(base + 2 * NA_VEC);
+  double* part = (double*)(base + 3 * NA_VEC);
+  unsigned char* zero_from = base + 3 * NA_VEC + NA_PART;  // out, then bar/status
+  double* out = (double*)zero_from;
+  unsigned* bar = (unsigned*)(zero_from + NA_OUT);
+  int* status = (int*)(zero_from + NA_OUT + 2 * sizeof(unsigned));
+
+  KArgs<double> A;
+  std::memset(&A, 0, sizeof(A));
+  A.S.n = n;
+  A.S.ia = ia; A.S.ja = ja; A.S.dg = diag; A.S.a = a;
+  A.C.bar = bar; A.C.part = part; A.C.status = status; A.C.out = out;
+  A.x = x; A.b = b; A.r = r; A.p = p; A.z = z;
+  A.itr_max = itr_max; A.tol_abs = tol_abs; A.tol_rel = tol_rel;
+
+  cudaStream_t st = (cudaStream_t)stream;
+  if (cudaMemsetAsync(zero_from, 0, NA_OUT + NA_CTL, st) != cudaSuccess)
+    return na_fail(errmsg, errlen, FC_ERR_CUDA, "clearing the control block failed");
+  void* args[1] = {&A};
+  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(FC_BLOCK), args, 0, st);
+  if (e != cudaSuccess) return na_fail(errmsg, errlen, FC_ERR_CUDA, "cooperative launch failed");
+  double h_out[FC_OUT_N];
+  int h_status = 0;
+  if (cudaMemcpyAsync(h_out, out, sizeof(h_out), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(&h_status, status, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return na_fail(errmsg, errlen, FC_ERR_CUDA, "reading the results failed");
+  fc_solve_info I;
+  std::memset(&I, 0, sizeof(I));
+  I.res0_l1 = h_out[FC_OUT_RES0];
+  I.resl = h_out[FC_OUT_RESL];
+  I.factor = h_out[FC_OUT_FACTOR];
+  I.resor = h_out[FC_OUT_RESOR];
+  I.itr_used = (int)h_out[FC_OUT_ITR];
+  I.early_exit = (int)h_out[FC_OUT_EARLY];
+  I.status = h_status;
+  if (I.status == 0 && !I.early_exit && I.itr_used >= itr_max && itr_max > 0 &&
+      !(I.resl / (I.res0_l1 + FC_SMALL) < tol_rel || I.resl < tol_abs))
+    I.status = FC_WARN_MAXITER;
+  if (info) *info = I;
+  if (h_status == FC_ERR_TIMEOUT) return na_fail(errmsg, errlen, FC_ERR_TIMEOUT, "grid barrier timed out");
+  if (h_status < 0) return na_fail(errmsg, errlen, h_status, "solver reported an error (NaN/Inf or breakdown)");
+  return I.status;
 }

@@ -30,6 +30,7 @@ FC_ERR_ZERO_PIVOT = -8
 BC = {"wall": 1, "inlet": 2, "outlet": 3, "symmetry": 4, "pressure": 5, "empty": 6, "periodic": 7}
 FC_PREC_FP64 = 0
 FC_PREC_MIXED = 1
+FC_NOALLOC_MAX_N = 1 << 20  # rows of fc_dpcg_noalloc's static scratch
 GRAD = {"gauss": 0, "lstsq": 1, "lstsq_dm": 2}
 NOMAX = 6
 
@@ -89,6 +90,7 @@ def lib():
         "fc_precond_apply": (i, [vp, cp, i, i, vp, vp, vp, vp, vp, vp]),
         "fc_spmv": (i, [vp, i, i, vp, vp, vp, vp, vp, vp, i]),
         "fc_ilu0": (i, [vp, i, i, vp, vp, vp, vp, vp]),
+        "fc_dpcg_noalloc": (i, [vp, i, i, vp, vp, vp, vp, vp, vp, i, d, d, C.POINTER(SolveInfo), vp, i]),
         "fc_set_mesh": (i, [vp, vp]),
         "fc_get_geometry": (i, [vp, cp, vp]),
         "fc_get_csr_pattern": (i, [vp, vp, vp, vp, vp, vp, vp, vp]),
@@ -329,6 +331,19 @@ class Context:
                                 0, C.byref(info))
         self._check(st, "fc_csrsolve")
         return float(r0[0]), info, st
+
+    def dpcg_noalloc(self, n, nnz, ia, ja, a, diag, x, b, itr_max, tol_abs, tol_rel, stream=None):
+        """fc_dpcg_noalloc on device arrays (0-based ia/ja/diag; x updated in
+        place); stream defaults to this context's stream.  Returns (status,
+        info); raises on an error status with the call's own message."""
+        info = SolveInfo()
+        err = C.create_string_buffer(256)
+        st = self.L.fc_dpcg_noalloc(stream if stream is not None else self.L.fc_stream(self.h), int(n), int(nnz),
+                                    _ptr(ia), _ptr(ja), _ptr(a), _ptr(diag), _ptr(x), _ptr(b), int(itr_max),
+                                    float(tol_abs), float(tol_rel), C.byref(info), C.cast(err, C.c_void_p), 256)
+        if st < 0:
+            raise FcError(st, err.value.decode())
+        return st, info
 
     def pattern_forget(self):
         self.L.fc_csr_pattern_forget(self.h)

@@ -174,6 +174,28 @@ int fc_trace_get(fc_ctx* ctx, double* out, unsigned long long* timeline);
 int fc_ilu0(fc_ctx* ctx, int n, int nnz, const int* ia, const int* ja, const double* a, const int* diag,
             double* l_out);
 
+/* Jacobi-PCG (dpcg, linear_solvers.f90:206-359) that allocates nothing.  No
+ * counterpart in the reference: it is for callers that may not allocate
+ * device memory during a solve (cudaMalloc/cudaFree synchronise the device,
+ * and a caller whose pool allocator owns the free memory cannot take more).
+ * Its work vectors live in a fixed scratch area in static device memory of
+ * the library (3 * FC_NOALLOC_MAX_N doubles + a small control block, one per
+ * device); n > FC_NOALLOC_MAX_N is rejected with FC_ERR_BAD_INPUT.
+ *  - ia(n+1), ja(nnz), diag(n) 0-based, a, x (in/out), b: DEVICE memory;
+ *    stream: a cudaStream_t (NULL = legacy default stream).
+ *  - the first call on each device looks up the scratch address
+ *    (cudaGetSymbolAddress with that device current): make that first call
+ *    before any stream capture.
+ *  - calls that overlap in time on the same device (other threads, other
+ *    streams) race on the one scratch area: serialise them.
+ *  - blocks until the solve has finished; info->ms is not measured (0).
+ *  - errmsg (may be NULL) receives a one-line reason on failure.
+ * Returns FC_OK, FC_WARN_MAXITER or an error, as fc_csrsolve. */
+#define FC_NOALLOC_MAX_N (1 << 20)
+int fc_dpcg_noalloc(void* stream, int n, int nnz, const int* ia, const int* ja, const double* a,
+                    const int* diag, double* x, const double* b, int itr_max, double tol_abs, double tol_rel,
+                    fc_solve_info* info, char* errmsg, int errlen);
+
 /* ======================================================================== */
 /* Mesh, fields and finite-volume operators on the device                   */
 /* ======================================================================== */

@@ -73,3 +73,20 @@ def test_mesh_rejects_bad_input(fc):
     bad["owner"][0] = 999
     with pytest.raises(fc.FcError):
         fc.Mesh.from_arrays(bad)
+
+
+def test_noalloc_size_limit_is_host_side(fc):
+    """fc_dpcg_noalloc rejects n > FC_NOALLOC_MAX_N before touching the
+    device (the arrays here are host dummies and are never read)."""
+    import ctypes as C
+    L = fc.lib()
+    dummy_i = np.zeros(4, dtype=np.int32)
+    dummy_d = np.zeros(4)
+    err = C.create_string_buffer(256)
+    info = fc.SolveInfo()
+    n = fc.FC_NOALLOC_MAX_N + 1
+    p = lambda arr: arr.ctypes.data_as(C.c_void_p)  # noqa: E731
+    st = L.fc_dpcg_noalloc(None, n, n, p(dummy_i), p(dummy_i), p(dummy_d), p(dummy_i), p(dummy_d), p(dummy_d),
+                           10, 0.0, 1e-8, C.byref(info), C.cast(err, C.c_void_p), 256)
+    assert st == fc.FC_ERR_BAD_INPUT
+    assert b"FC_NOALLOC_MAX_N" in err.value

@@ -311,15 +311,18 @@ int solve_global(fc_ctx* ctx, const char* solver, double* x, const double* b, do
   return r.status;
 }
 
-// Tiled sweep schedule of the mesh system (which = 0) or of the cached
-// external pattern (which = 1): out[0..7] = tiles, levels, widest tile, ring
-// depth, estimated forward sweep microseconds, ring-served entries,
-// cross-tile entries, global same-tile entries.
+// Ordered sweep structure of the mesh system (which = 0) or of the cached
+// external pattern (which = 1): out[0..9] = tiles, levels, widest step of a
+// tile, ring depth, estimated forward sweep microseconds, ring-served
+// entries, pushed entries, cross-tile entries (both triangles), stage depth,
+// most steps of a tile.
 extern "C" int fc_sweep_stats(fc_ctx* ctx, int which, double* out) {
   if (!ctx || !out) return FC_ERR_BAD_INPUT;
   CsrSystem* s = which ? ctx->sys_ext : ctx->sys_mesh;
   if (!s) return fc_fail_msg(ctx, FC_ERR_STATE, "no such system");
-  out[0] = s->sf.ntiles; out[1] = s->sf.nlev; out[2] = s->sf.max_slots; out[3] = s->sf.R;
-  out[4] = s->est_sweep_us; out[5] = (double)s->sf.ring; out[6] = (double)s->sf.cross; out[7] = (double)s->sf.global_same;
+  const DevOrdered& D = s->ord;
+  out[0] = D.ntiles; out[1] = D.nlev; out[2] = D.maxW; out[3] = D.R;
+  out[4] = s->est_sweep_us; out[5] = (double)D.ring_entries; out[6] = (double)D.pushed_entries;
+  out[7] = (double)D.cross_tile_entries; out[8] = D.K; out[9] = D.max_tile_steps;
   return FC_OK;
 }

@@ -55,11 +55,22 @@ struct GridCtl {
 #define FC_NPART 4
 enum { FC_OUT_RES0 = 0, FC_OUT_RESL, FC_OUT_FACTOR, FC_OUT_RESOR, FC_OUT_ITR, FC_OUT_EARLY, FC_OUT_BAD, FC_OUT_N = 16 };
 
-// device copy of a tiled sweep schedule (fc_schedule.hpp)
-struct DevSweep {
-  int ntiles = 0, nlev = 0, R = 1, max_slots = 0;
-  DVec<int> tile_step_ptr, step_level, tile_slots, step_row_ptr, rows, kbne;
-  long long cross = 0, ring = 0, global_same = 0;
+// device copy of a schedule-ordered sweep structure (fc_schedule.hpp)
+struct DevOrdered {
+  int n = 0, nE = 0, ntiles = 0, nsteps = 0, nlev = 0, R = 4, K = 1, maxW = 0, max_tile_steps = 0;
+  int xmax = 4, pmax = 4;            // largest exchange / push block of a step
+  int novf[2] = {0, 0}, nxv[2] = {0, 0};
+  DVec<int> tile_step_ptr, step_ptr, tile_W, perm;
+  DVec<int> srec[2], xv_ptr[2], push_ptr[2], push[2], slot[2], ucol;
+  DVec<int> ovf_ptr[2], ovf_code[2], ovf_col[2], ovf_slot[2];
+  DVec<int> lo_tslot, lo_ovf_tslot, dslot, p_ptr, p_col, p_slot;
+  long long ring_entries = 0, pushed_entries = 0, cross_tile_entries = 0;
+};
+
+// per-solve values of an ordered system in one precision (fc_sweep.cuh OrdVals)
+template <class T>
+struct OrdStore {
+  DVec<T> vrec0, vrec1, sx, aovf0, aovf1, tovf, adiag, ap, xv0, xv1, xo, bo;
 };
 
 struct LevelSchedule {
@@ -76,9 +87,10 @@ struct CsrSystem {
   bool tslot_oob = false;            // some DILU search ran past its row (non-symmetric pattern)
   DVec<double> a;
   DVec<float> a32;
-  LevelSchedule lf, lb;              // forward (lower) and backward (upper) level sets
-  DevSweep sf, sb;                   // tiled pipeline schedules of the two sweeps
-  DVec<int> code;                    // per entry: ring index or global row (fc_schedule.hpp)
+  LevelSchedule lf, lb;              // forward (lower) and backward (upper) level sets (ILU(0))
+  DevOrdered ord;                    // schedule-ordered sweep structure (DIC/DILU/Gauss-Seidel)
+  OrdStore<double> o64;
+  OrdStore<float> o32;
   double est_sweep_us = 0.0;         // critical-path estimate of the forward sweep
   // workspace
   DVec<double> x, b, r, r0, p, u, z, v, d, w;

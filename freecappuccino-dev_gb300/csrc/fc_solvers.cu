@@ -20,6 +20,7 @@
 #include "fc_internal.hpp"
 #include "fc_krylov.cuh"
 #include "fc_schedule.hpp"
+#include "fc_sweep.cuh"
 
 using namespace fcdev;
 
@@ -29,11 +30,16 @@ namespace {
 
 template <class T>
 struct KArgs {
-  CsrView<T> S;
+  CsrView<T> S;      // original numbering: values a (the caller's), pattern
+  OrdView O;         // schedule-ordered structure (iccg, bicgstab, gauss-seidel, precond)
+  OrdVals<T> V;      // per-solve values in the new numbering
+  int nnz;
   GridCtl C;
-  T* x;
-  const T* b;
-  T* r;
+  T* x;              // caller's solution (original numbering, in/out)
+  const T* b;        // caller's right-hand side (original numbering)
+  T* xo;             // x and b in the new numbering
+  T* bo;
+  T* r;              // work vectors (new numbering for the ordered kernels)
   T* r0;
   T* p;
   T* u;
@@ -106,7 +112,8 @@ __device__ void write_out(const KArgs<T>& A, double res0, double resl, double fa
   }
 }
 
-// r = b - A x over all rows; returns L1(r) (identical in every block)
+// r = b - A x over all rows in the original numbering (DPCG, refinement);
+// returns L1(r) (identical in every block)
 template <class T>
 __device__ bool residual_l1(const KArgs<T>& A, int& ph, double& l1out) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, G = gridDim.x * blockDim.x;
@@ -121,31 +128,83 @@ __device__ bool residual_l1(const KArgs<T>& A, int& ph, double& l1out) {
   return true;
 }
 
+// First phase of the ordered kernels: matrix values into the new numbering,
+// exchange arrays to the sentinel, b (and x) gathered; ends with a barrier.
+template <class T>
+__device__ bool ord_prologue(const KArgs<T>& A, bool dilu, bool with_x) {
+  ord_gather_values(A.O, A.V, A.S.a, A.nnz, dilu);
+  ord_gather_vec(A.O, A.b, A.bo);
+  if (with_x) ord_gather_vec(A.O, (const T*)A.x, A.xo);
+  return grid_sync(A.C);
+}
+
+// r = b - A x in the new numbering; returns L1(r) (identical in every block)
+template <class T>
+__device__ bool ord_residual_l1(const KArgs<T>& A, int& ph, double& l1out) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, G = gridDim.x * blockDim.x;
+  double s[1] = {0.0};
+  for (int q = gt; q < A.O.n; q += G) {
+    T rq = ord_row_residual(A.O, (const T*)A.V.ap, A.xo, ldcg(A.bo + q), q);
+    A.r[q] = rq;
+    s[0] += fabs((double)rq);
+  }
+  if (!grid_reduce<1>(A.C, ph, s)) return false;
+  l1out = s[0];
+  return true;
+}
+
+// z = M^-1 q with the DIC/DILU factors d: forward sweep into yf, barrier,
+// backward sweep into z (linear_solvers.f90:458-475); dot (optional) gets
+// sum e_i z_i of the rows this thread finished.  No barrier at the end.
+template <class T, class TracerT>
+__device__ __forceinline__ bool precond_apply(const KArgs<T>& A, OsCtx& X, const T* q, T* yf, T* z, const T* e, double* dot,
+                              TracerT* tr) {
+  const OsIO<T> f{q, nullptr, yf};
+  if (!osweep<T, OS_FWD>(A.C, A.O, A.V, f, X, nullptr, tr)) return false;
+  tr->mark(TR_FWD);
+  if (!grid_sync(A.C)) return false;
+  tr->mark(TR_MID);
+  const OsIO<T> g{yf, e, z};
+  if (dot) {
+    if (!osweep<T, OS_BWD_DOT>(A.C, A.O, A.V, g, X, dot, tr)) return false;
+  } else {
+    if (!osweep<T, OS_BWD>(A.C, A.O, A.V, g, X, nullptr, tr)) return false;
+  }
+  tr->mark(TR_BWD);
+  return true;
+}
+
+// DIC (DILU) factors d_i, inverted as in the reference
+// (linear_solvers.f90:439-445, :613-624); ends with a barrier
+template <class T, bool DILU>
+__device__ __forceinline__ bool precond_setup(const KArgs<T>& A, OsCtx& X) {
+  const OsIO<T> io{nullptr, nullptr, A.d};
+  if (!osweep<T, DILU ? OS_SETUP_DILU : OS_SETUP_DIC>(A.C, A.O, A.V, io, X, nullptr)) return false;
+  return grid_sync(A.C);
+}
+
 // ------------------------------------------------------------------ ICCG
-// iccg, linear_solvers.f90:364-545
+// iccg, linear_solvers.f90:364-545, in the schedule-ordered numbering
 template <class T, bool TRACE = false>
-__global__ void __launch_bounds__(FC_BLOCK, 1) k_iccg(KArgs<T> A) {
-  const CsrView<T>& S = A.S;
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x, G = gridDim.x * blockDim.x, n = S.n;
+__global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_iccg(KArgs<T> A) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, G = gridDim.x * blockDim.x, n = A.O.n;
   int ph = 0;
-  SweepCtx X = sweep_ctx(S, fc_smem);
-  T *x = A.x, *r = A.r, *p = A.p, *z = A.z, *d = A.d, *yf = A.u;
-  const T SENT = Sentinel<T>::value();
-  for (int i = gt; i < n; i += G) { p[i] = T(0); z[i] = T(0); yf[i] = SENT; }
+  OsCtx X = osweep_ctx<T>(A.O, fc_smem);
+  T *x = A.xo, *r = A.r, *p = A.p, *z = A.z, *yf = A.u;
   typename std::conditional<TRACE, Tracer, NoTracer>::type tr(A.trace, A.trace_cap);
+  for (int i = gt; i < n; i += G) p[i] = T(0);
+  if (!ord_prologue(A, false, true)) return;
   double res0;
-  if (!residual_l1(A, ph, res0)) return;
+  if (!ord_residual_l1(A, ph, res0)) return;
   if (res0 < A.tol_abs) { write_out(A, res0, res0, 0.0, 0.0, 0, 1); return; }
   if (!A.skip_setup)
-    if (!precond_setup<T, false>(A.C, S, X, d)) return;
+    if (!precond_setup<T, false>(A, X)) return;
   tr.mark(TR_SETUP);
   double s0 = FC_S0, resl = 0.0, factor = 0.0, resor = 0.0;
   int itr_used = 0;
   for (int l = 1; l <= A.itr_max; ++l) {
     double rz[1] = {0.0};
-    auto pre = [&](int i) { return ldcg(r + i); };
-    auto post = [&](int i, T zi) { rz[0] += (double)ldcg(r + i) * (double)zi; };
-    if (!precond_apply(A.C, S, X, d, yf, z, pre, post, false, &tr)) return;
+    if (!precond_apply(A, X, (const T*)r, yf, z, (const T*)r, rz, &tr)) return;
     if (!grid_reduce<1>(A.C, ph, rz)) return;
     tr.mark(TR_DOT);
     const double sk = rz[0];
@@ -155,7 +214,7 @@ __global__ void __launch_bounds__(FC_BLOCK, 1) k_iccg(KArgs<T> A) {
     tr.mark(TR_PUPD);
     double pap[1] = {0.0};
     for (int i = gt; i < n; i += G) {
-      T zi = row_dot(S, p, i);
+      T zi = ord_row_dot(A.O, (const T*)A.V.ap, p, i);
       z[i] = zi;
       pap[0] += (double)ldcg(p + i) * (double)zi;
     }
@@ -168,9 +227,8 @@ __global__ void __launch_bounds__(FC_BLOCK, 1) k_iccg(KArgs<T> A) {
       x[i] = xi;
       T ri = ldcg(r + i) - alf * ldcg(z + i);
       r[i] = ri;
-      yf[i] = SENT;
       red[0] += fabs((double)ri);
-      if (l == 1) red[1] += fabs((double)__ldg(S.a + __ldg(S.dg + i)) * (double)xi);
+      if (l == 1) red[1] += fabs((double)ldcg(A.V.adiag + i) * (double)xi);
     }
     if (!grid_reduce<2>(A.C, ph, red)) return;
     tr.mark(TR_UPD);
@@ -182,31 +240,30 @@ __global__ void __launch_bounds__(FC_BLOCK, 1) k_iccg(KArgs<T> A) {
     if (!(rsm == rsm)) { if (gt == 0) atomicCAS(A.C.status, 0, FC_ERR_NAN); break; }
     if (rsm < A.tol_rel || resl < A.tol_abs) break;
   }
+  ord_scatter_vec(A.O, (const T*)x, A.x);
   tr.flush();
   write_out(A, res0, resl, factor, resor, itr_used, 0);
 }
 
 // ------------------------------------------------------------- BiCGStab
-// bicgstab, linear_solvers.f90:548-786.  The pk update is fused into the
-// first forward sweep, and the fi/res updates into the second one (each row
-// is updated by the thread that owns it in the sweep).
+// bicgstab, linear_solvers.f90:548-786, in the schedule-ordered numbering
 template <class T>
-__global__ void __launch_bounds__(FC_BLOCK, 1) k_bicgstab(KArgs<T> A) {
-  const CsrView<T>& S = A.S;
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x, G = gridDim.x * blockDim.x, n = S.n;
+__global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_bicgstab(KArgs<T> A) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, G = gridDim.x * blockDim.x, n = A.O.n;
   int ph = 0;
-  SweepCtx X = sweep_ctx(S, fc_smem);
-  T *x = A.x, *r = A.r, *r0 = A.r0, *p = A.p, *u = A.u, *z = A.z, *v = A.v, *d = A.d, *yf = A.w;
-  const T SENT = Sentinel<T>::value();
+  OsCtx X = osweep_ctx<T>(A.O, fc_smem);
+  T *x = A.xo, *r = A.r, *r0 = A.r0, *p = A.p, *u = A.u, *z = A.z, *v = A.v, *yf = A.w;
+  NoTracer tr(nullptr, 0);
+  if (!ord_prologue(A, true, true)) return;
   double res0;
-  if (!residual_l1(A, ph, res0)) return;
+  if (!ord_residual_l1(A, ph, res0)) return;
   if (res0 < A.tol_abs) { write_out(A, res0, res0, 0.0, 0.0, 0, 1); return; }
   if (!A.skip_setup)
-    if (!precond_setup<T, true>(A.C, S, X, d)) return;
+    if (!precond_setup<T, true>(A, X)) return;
   double bb[1] = {0.0};
   for (int i = gt; i < n; i += G) {
     T ri = ldcg(r + i);
-    r0[i] = ri; p[i] = T(0); u[i] = T(0); z[i] = T(0); v[i] = T(0); yf[i] = SENT;
+    r0[i] = ri; p[i] = T(0); u[i] = T(0); z[i] = T(0); v[i] = T(0);
     bb[0] += (double)ri * (double)ri;
   }
   if (!grid_reduce<1>(A.C, ph, bb)) return;
@@ -218,35 +275,30 @@ __global__ void __launch_bounds__(FC_BLOCK, 1) k_bicgstab(KArgs<T> A) {
     const double om = bet * gam / (alf * beto + FC_SMALL);
     beto = bet;
     const T omT = (T)om, alfT = (T)alf;
-    auto pre1 = [&](int i) {
-      T pi = ldcg(r + i) + omT * (ldcg(p + i) - alfT * ldcg(u + i));
-      p[i] = pi;
-      return pi;
-    };
-    auto nopost = [&](int, T) {};
-    if (!precond_apply(A.C, S, X, d, yf, z, pre1, nopost, true)) return;
+    for (int i = gt; i < n; i += G) p[i] = ldcg(r + i) + omT * (ldcg(p + i) - alfT * ldcg(u + i));
+    if (!grid_sync(A.C)) return;
+    if (!precond_apply(A, X, (const T*)p, yf, z, (const T*)nullptr, nullptr, &tr)) return;
+    if (!grid_sync(A.C)) return;
     double ur[1] = {0.0};
     for (int i = gt; i < n; i += G) {
-      T ui = row_dot(S, z, i);
+      T ui = ord_row_dot(A.O, (const T*)A.V.ap, z, i);
       u[i] = ui;
-      yf[i] = SENT;
       ur[0] += (double)ui * (double)ldcg(r0 + i);
     }
     if (!grid_reduce<1>(A.C, ph, ur)) return;
     gam = bet / ur[0];
     const T gamT = (T)gam;
-    auto pre2 = [&](int i) {
+    for (int i = gt; i < n; i += G) {
       x[i] = ldcg(x + i) + gamT * ldcg(z + i);
-      T ri = ldcg(r + i) - gamT * ldcg(u + i);
-      r[i] = ri;
-      return ri;
-    };
-    if (!precond_apply(A.C, S, X, d, yf, z, pre2, nopost, true)) return;
+      r[i] = ldcg(r + i) - gamT * ldcg(u + i);
+    }
+    if (!grid_sync(A.C)) return;
+    if (!precond_apply(A, X, (const T*)r, yf, z, (const T*)nullptr, nullptr, &tr)) return;
+    if (!grid_sync(A.C)) return;
     double vr[2] = {0.0, 0.0};
     for (int i = gt; i < n; i += G) {
-      T vi = row_dot(S, z, i);
+      T vi = ord_row_dot(A.O, (const T*)A.V.ap, z, i);
       v[i] = vi;
-      yf[i] = SENT;
       vr[0] += (double)vi * (double)ldcg(r + i);
       vr[1] += (double)vi * (double)vi;
     }
@@ -261,7 +313,7 @@ __global__ void __launch_bounds__(FC_BLOCK, 1) k_bicgstab(KArgs<T> A) {
       r[i] = ri;
       red[0] += fabs((double)ri);
       red[1] += (double)ri * (double)ldcg(r0 + i);
-      if (l == 1) red[2] += fabs((double)__ldg(S.a + __ldg(S.dg + i)) * (double)xi);
+      if (l == 1) red[2] += fabs((double)ldcg(A.V.adiag + i) * (double)xi);
     }
     if (!grid_reduce<3>(A.C, ph, red)) return;
     resl = red[0];
@@ -272,6 +324,7 @@ __global__ void __launch_bounds__(FC_BLOCK, 1) k_bicgstab(KArgs<T> A) {
     if (!(rsm == rsm)) { if (gt == 0) atomicCAS(A.C.status, 0, FC_ERR_NAN); break; }
     if (rsm < A.tol_rel || resl < A.tol_abs) break;
   }
+  ord_scatter_vec(A.O, (const T*)x, A.x);
   write_out(A, res0, resl, factor, resor, itr_used, 0);
 }
 
@@ -332,41 +385,22 @@ __global__ void __launch_bounds__(FC_BLOCK, 1) k_dpcg(KArgs<T> A) {
 }
 
 // ---------------------------------------------------------- Gauss-Seidel
-// GaussSeidel, linear_solvers.f90:96-201: in-place sweep as a forward
-// level-scheduled sweep; entries left of the diagonal read this sweep's
-// values (xb), the others the previous sweep's (xa).
-__global__ void __launch_bounds__(FC_BLOCK, 1) k_gauss_seidel(KArgs<double> A) {
-  const CsrView<double>& S = A.S;
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x, G = gridDim.x * blockDim.x, n = S.n;
+// GaussSeidel, linear_solvers.f90:96-201: the in-place sweep as an ordered
+// forward sweep; entries left of the diagonal take this sweep's values
+// (xb), the diagonal and the entries right of it the previous sweep's (xa).
+__global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_gauss_seidel(KArgs<double> A) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   int ph = 0;
-  SweepCtx X = sweep_ctx(S, fc_smem);
-  double* ring = (double*)X.ring;
-  double* xa = A.x;
+  OsCtx X = osweep_ctx<double>(A.O, fc_smem);
+  if (!ord_prologue(A, false, true)) return;
+  double* xa = A.xo;
   double* xb = A.w;
   double res0 = 0.0, resl = 0.0, factor = 0.0, resor = 0.0;
   int itr_used = 0, early = 0;
   for (int l = 1; l <= A.itr_max; ++l) {
     double red[2] = {0.0, 0.0};
-    for (int i = gt; i < n; i += G) xb[i] = Sentinel<double>::value();
-    if (!grid_sync(A.C)) return;
-    auto gpre = [&](RowIn<double>& r) { r.q = ldcg(A.b + r.i); };
-    auto rowf = [&](const RowIn<double>& r) {
-      const int i = r.i;
-      const int kd = r.kb + row_entries(r, S.ia, S.dg, true), k1 = __ldg(S.ia + i + 1);
-      double s = r.q;
-      for (int k = r.kb; k < k1; ++k) {
-        const double xj = k < kd ? entry_value(r, k - r.kb, S.code, (const double*)ring, (const double*)xb,
-                                               X.abort_flag, A.C)
-                                 : ldcg(xa + __ldg(S.ja + k));
-        s = __dsub_rn(s, __dmul_rn(__ldg(S.a + k), xj));
-      }
-      const double aii = __ldg(S.a + kd);
-      const double xi = __dadd_rn(ldcg(xa + i), __ddiv_rn(s, __dadd_rn(aii, FC_SMALL)));
-      red[0] += fabs(s);
-      red[1] += fabs(aii * xi);
-      return xi;
-    };
-    if (!tile_sweep(A.C, S.F, S.a, S.code, (const double*)xb, ring, X.abort_flag, xb, gpre, rowf)) return;
+    const OsIO<double> io{A.bo, xa, xb};
+    if (!osweep<double, OS_GS>(A.C, A.O, A.V, io, X, red)) return;
     if (!grid_reduce<2>(A.C, ph, red)) return;
     double* t = xa; xa = xb; xb = t;
     if (l == 1) {
@@ -380,25 +414,23 @@ __global__ void __launch_bounds__(FC_BLOCK, 1) k_gauss_seidel(KArgs<double> A) {
     if (!(rsm == rsm)) { if (gt == 0) atomicCAS(A.C.status, 0, FC_ERR_NAN); break; }
     if (rsm < A.tol_rel || resl < A.tol_abs) break;
   }
-  if (xa != A.x)
-    for (int i = gt; i < n; i += G) A.x[i] = ldcg(xa + i);
+  ord_scatter_vec(A.O, (const double*)xa, A.x);
   write_out(A, res0, resl, factor, resor, itr_used, early);
 }
 
-// preconditioner only: d (DIC or DILU) and optionally z = M^-1 q
+// preconditioner only: d (DIC or DILU) and optionally z = M^-1 q, q = A.b;
+// results in the original numbering: d into A.v, z into A.z
 template <class T, bool DILU>
-__global__ void __launch_bounds__(FC_BLOCK, 1) k_precond(KArgs<T> A, int apply) {
-  SweepCtx X = sweep_ctx(A.S, fc_smem);
-  if (!A.skip_setup)
-    if (!precond_setup<T, DILU>(A.C, A.S, X, A.d)) return;
+__global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_precond(KArgs<T> A, int apply) {
+  OsCtx X = osweep_ctx<T>(A.O, fc_smem);
+  NoTracer tr(nullptr, 0);
+  if (!ord_prologue(A, DILU, false)) return;
+  if (!precond_setup<T, DILU>(A, X)) return;
+  ord_scatter_vec(A.O, (const T*)A.d, A.v);
   if (!apply) return;
-  const T* q = A.b;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.S.n; i += gridDim.x * blockDim.x)
-    A.u[i] = Sentinel<T>::value();
+  if (!precond_apply(A, X, (const T*)A.bo, A.u, A.w, (const T*)nullptr, nullptr, &tr)) return;
   if (!grid_sync(A.C)) return;
-  auto pre = [&](int i) { return ldcg(q + i); };
-  auto nopost = [&](int, T) {};
-  precond_apply(A.C, A.S, X, A.d, A.u, A.z, pre, nopost, false);
+  ord_scatter_vec(A.O, (const T*)A.w, A.z);
 }
 
 // r = b - A x in FP64 with L1 norm (refinement step of the mixed solve)
@@ -428,6 +460,14 @@ __global__ void k_add_float(double* __restrict__ x, const float* __restrict__ dx
 }  // namespace
 
 // ======================================================================== host
+// Critical-path model of a sweep schedule used to pick the tile count:
+// per step cost, per row cost and the delay of a value pushed to another
+// tile (its transfer plus the stage lead of the consumer), microseconds.
+#define FC_SWEEP_TAU0_US 0.15
+#define FC_SWEEP_ROW_US 0.001
+#define FC_SWEEP_HOP_US 1.5
+#define FC_RING 4                    // ring depth (steps) of the ordered sweeps
+#define FC_SWEEP_SMEM (200 * 1024)   // dynamic shared memory budget of a sweep kernel
 
 bool is_device_ptr(const void* p) {
   if (!p) return false;
@@ -474,28 +514,68 @@ static void build_levels(int n, const std::vector<int>& ia, const std::vector<in
   for (int i = 0; i < n; ++i) L.h_rows[pos[lev[i]]++] = i;  // ascending row order inside a level
 }
 
-static int upload_sweep(fc_ctx* ctx, const SweepSchedule& S, DevSweep& D) {
-  D.ntiles = S.ntiles; D.nlev = S.nlev; D.R = S.R; D.max_slots = S.max_slots;
-  D.cross = S.cross_tile_entries; D.ring = S.ring_entries; D.global_same = S.global_same_tile_entries;
-  auto put = [&](DVec<int>& d, const std::vector<int>& h) -> int {
-    FC_CUDA_TRY(ctx, d.alloc(std::max<size_t>(1, h.size())));
-    if (!h.empty()) FC_CUDA_TRY(ctx, cudaMemcpy(d.p, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
-    return FC_OK;
-  };
-  int st;
-  if ((st = put(D.tile_step_ptr, S.tile_step_ptr)) || (st = put(D.step_level, S.step_level)) ||
-      (st = put(D.tile_slots, S.tile_slots)) || (st = put(D.step_row_ptr, S.step_row_ptr)) ||
-      (st = put(D.rows, S.rows)) || (st = put(D.kbne, S.kbne)))
-    return st;
-  return FC_OK;
+template <class V>
+static cudaError_t upload_vec(DVec<int>& d, const V& h) {
+  cudaError_t e = d.alloc(std::max<size_t>(1, h.size()));
+  if (e != cudaSuccess) return e;
+  if (h.empty()) return cudaMemset(d.p, 0, sizeof(int));
+  return cudaMemcpy(d.p, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice);
 }
 
-// step cost and cross-tile latency used to compare tile counts (measured on
-// GB300: a step of ~100 FP64 rows takes a few tenths of a microsecond, a flag
-// published by one SM is seen by another about a microsecond later)
-#define FC_SWEEP_TAU0_US 0.08
-#define FC_SWEEP_ROW_US 0.002
-#define FC_SWEEP_HOP_US 1.0
+// stage depth K of the ordered sweeps: as deep as the shared memory allows
+static int ordered_stages(const DevOrdered& D) {
+  for (int K = FC_MAX_STAGES; K > 1; --K)
+    if (osweep_smem_bytes<double>(D.R, K, D.maxW, D.max_tile_steps, D.xmax, D.pmax) <= FC_SWEEP_SMEM) return K;
+  return 1;
+}
+
+static int upload_ordered(fc_ctx* ctx, const OrderedSweep& O, DevOrdered& D) {
+  D.n = O.n; D.nE = O.nE; D.ntiles = O.ntiles; D.nsteps = O.nsteps; D.nlev = O.nlev; D.R = O.R; D.maxW = O.maxW;
+  D.max_tile_steps = O.max_tile_steps;
+  D.xmax = D.pmax = 4;
+  for (int d = 0; d < 2; ++d)
+    for (int gs = 0; gs < O.nsteps; ++gs) {
+      D.xmax = std::max(D.xmax, O.dir[d].xv_ptr[gs + 1] - O.dir[d].xv_ptr[gs]);
+      D.pmax = std::max(D.pmax, O.dir[d].push_ptr[gs + 1] - O.dir[d].push_ptr[gs]);
+    }
+  D.K = ordered_stages(D);
+  if (osweep_smem_bytes<double>(D.R, D.K, D.maxW, D.max_tile_steps, D.xmax, D.pmax) > FC_SWEEP_SMEM)
+    return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "sweep tiles too wide for shared memory");
+  D.ring_entries = D.pushed_entries = D.cross_tile_entries = 0;
+  FC_CUDA_TRY(ctx, upload_vec(D.tile_step_ptr, O.tile_step_ptr));
+  FC_CUDA_TRY(ctx, upload_vec(D.step_ptr, O.step_ptr));
+  FC_CUDA_TRY(ctx, upload_vec(D.tile_W, O.tile_W));
+  FC_CUDA_TRY(ctx, upload_vec(D.perm, O.perm));
+  for (int d = 0; d < 2; ++d) {
+    const OrderedDir& H = O.dir[d];
+    D.novf[d] = H.ovf_ptr.empty() ? 0 : H.ovf_ptr.back();
+    D.nxv[d] = H.xv_ptr.back();
+    D.ring_entries += H.ring_entries;
+    D.pushed_entries += H.pushed_entries;
+    D.cross_tile_entries += H.cross_tile_entries;
+    FC_CUDA_TRY(ctx, upload_vec(D.srec[d], H.srec));
+    FC_CUDA_TRY(ctx, upload_vec(D.xv_ptr[d], H.xv_ptr));
+    FC_CUDA_TRY(ctx, upload_vec(D.push_ptr[d], H.push_ptr));
+    FC_CUDA_TRY(ctx, upload_vec(D.push[d], H.push));
+    FC_CUDA_TRY(ctx, upload_vec(D.slot[d], H.slot));
+    FC_CUDA_TRY(ctx, upload_vec(D.ovf_ptr[d], H.ovf_ptr));
+    FC_CUDA_TRY(ctx, upload_vec(D.ovf_code[d], H.ovf_code));
+    FC_CUDA_TRY(ctx, upload_vec(D.ovf_col[d], H.ovf_col));
+    FC_CUDA_TRY(ctx, upload_vec(D.ovf_slot[d], H.ovf_slot));
+  }
+  // columns of the upper entries, 4 per row (Gauss-Seidel)
+  std::vector<int> ucol((size_t)4 * O.nE, 0);
+  for (int q = 0; q < O.n; ++q)
+    for (int e = 0; e < FC_ELL; ++e) ucol[4 * (size_t)q + e] = O.dir[1].col[(size_t)e * O.nE + q];
+  FC_CUDA_TRY(ctx, upload_vec(D.ucol, ucol));
+  FC_CUDA_TRY(ctx, upload_vec(D.lo_tslot, O.lo_tslot));
+  FC_CUDA_TRY(ctx, upload_vec(D.lo_ovf_tslot, O.lo_ovf_tslot));
+  FC_CUDA_TRY(ctx, upload_vec(D.dslot, O.dslot));
+  FC_CUDA_TRY(ctx, upload_vec(D.p_ptr, O.p_ptr));
+  FC_CUDA_TRY(ctx, upload_vec(D.p_col, O.p_col));
+  FC_CUDA_TRY(ctx, upload_vec(D.p_slot, O.p_slot));
+  return FC_OK;
+}
 
 int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, const int* ja1, const int* diag1,
                     const double* xyz) {
@@ -547,31 +627,32 @@ int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, c
   std::vector<int> levf, levb;
   build_levels(n, ia, ja, dg, true, s->lf, levf);
   build_levels(n, ia, ja, dg, false, s->lb, levb);
-  // tiled pipeline schedules: at most one tile per SM; the tile count is
+  // schedule-ordered sweeps: at most one tile per SM; the tile count is
   // chosen among a few candidates by the critical-path estimate
-  std::vector<int> code(nnz, 0);
-  SweepSchedule SF, SB;
   const int sms = std::max(1, ctx->num_sms);
   int tiles = sms;
   {
+    std::vector<int> levs;
+    const int nls = symmetric_levels(n, ia.data(), ja.data(), dg.data(), levs);
     double best = 1e300;
     const int cand[4] = {sms, (3 * sms) / 4, sms / 2, sms / 4};
     std::vector<int> scratch(nnz, 0);
     for (int ci = 0; ci < 4; ++ci) {
       if (cand[ci] < 1 || (ci > 0 && cand[ci] == cand[ci - 1])) continue;
       SweepSchedule trial;
-      build_sweep_schedule(n, ia.data(), ja.data(), dg.data(), levf, s->lf.nlev, true, cand[ci], xyz, trial, scratch);
+      build_sweep_schedule(n, ia.data(), ja.data(), dg.data(), levs, nls, true, cand[ci], xyz, trial, scratch);
       const double est = estimate_sweep_us(trial, FC_SWEEP_TAU0_US, FC_SWEEP_ROW_US, FC_SWEEP_HOP_US);
       if (est < best) { best = est; tiles = cand[ci]; }
     }
     s->est_sweep_us = best;
   }
-  build_sweep_schedule(n, ia.data(), ja.data(), dg.data(), levf, s->lf.nlev, true, tiles, xyz, SF, code);
-  build_sweep_schedule(n, ia.data(), ja.data(), dg.data(), levb, s->lb.nlev, false, tiles, xyz, SB, code);
-  int st2;
-  if ((st2 = upload_sweep(ctx, SF, s->sf)) || (st2 = upload_sweep(ctx, SB, s->sb))) return st2;
-  FC_CUDA_TRY(ctx, s->code.alloc(nnz));
-  FC_CUDA_TRY(ctx, cudaMemcpy(s->code.p, code.data(), nnz * sizeof(int), cudaMemcpyHostToDevice));
+  OrderedSweep O;
+  SweepSchedule S;
+  std::string err;
+  if (!build_ordered_sweep(n, ia.data(), ja.data(), dg.data(), ts.data(), tiles, xyz, FC_RING, O, S, err))
+    return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, err);
+  int st2 = upload_ordered(ctx, O, s->ord);
+  if (st2) return st2;
   FC_CUDA_TRY(ctx, s->ia.alloc(n + 1));
   FC_CUDA_TRY(ctx, s->ja.alloc(nnz));
   FC_CUDA_TRY(ctx, s->diag.alloc(n));
@@ -594,8 +675,31 @@ int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, c
   return sys_alloc_work(ctx, s);
 }
 
+template <class T>
+static int alloc_ordered(fc_ctx* ctx, CsrSystem* s, OrdStore<T>& V) {
+  const DevOrdered& D = s->ord;
+  const size_t nE = D.nE, rec = (size_t)Rec<T>::V * nE;
+  FC_CUDA_TRY(ctx, V.vrec0.alloc(rec));
+  FC_CUDA_TRY(ctx, V.vrec1.alloc(rec));
+  FC_CUDA_TRY(ctx, V.sx.alloc(rec));
+  FC_CUDA_TRY(ctx, V.aovf0.alloc(std::max(1, D.novf[0])));
+  FC_CUDA_TRY(ctx, V.aovf1.alloc(std::max(1, D.novf[1])));
+  FC_CUDA_TRY(ctx, V.tovf.alloc(std::max(1, D.novf[0])));
+  FC_CUDA_TRY(ctx, V.xv0.alloc(std::max(4, D.nxv[0])));
+  FC_CUDA_TRY(ctx, V.xv1.alloc(std::max(4, D.nxv[1])));
+  FC_CUDA_TRY(ctx, V.adiag.alloc(nE));
+  FC_CUDA_TRY(ctx, V.ap.alloc(s->nnz));
+  FC_CUDA_TRY(ctx, V.xo.alloc(nE));
+  FC_CUDA_TRY(ctx, V.bo.alloc(nE));
+  // padding rows of the record arrays are read by the staging and never used
+  FC_CUDA_TRY(ctx, cudaMemset(V.vrec0.p, 0, V.vrec0.bytes()));
+  FC_CUDA_TRY(ctx, cudaMemset(V.vrec1.p, 0, V.vrec1.bytes()));
+  FC_CUDA_TRY(ctx, cudaMemset(V.sx.p, 0, V.sx.bytes()));
+  return FC_OK;
+}
+
 int sys_alloc_work(fc_ctx* ctx, CsrSystem* s) {
-  const int n = s->n;
+  const int n = s->ord.nE;  // padded: the sweeps stage whole 16-byte windows
   FC_CUDA_TRY(ctx, s->a.alloc(s->nnz));
   DVec<double>* v64[] = {&s->x, &s->b, &s->r, &s->r0, &s->p, &s->u, &s->z, &s->v, &s->d, &s->w};
   for (auto* v : v64) FC_CUDA_TRY(ctx, v->alloc(n));
@@ -607,15 +711,15 @@ int sys_alloc_work(fc_ctx* ctx, CsrSystem* s) {
   FC_CUDA_TRY(ctx, cudaMemset(s->bar.p, 0, 2 * sizeof(unsigned)));
   if (!s->h_out) FC_CUDA_TRY(ctx, cudaMallocHost(&s->h_out, FC_OUT_N * sizeof(double)));
   if (!s->h_status) FC_CUDA_TRY(ctx, cudaMallocHost(&s->h_status, sizeof(int)));
-  return FC_OK;
+  return alloc_ordered(ctx, s, s->o64);
 }
 
 static int alloc_work32(fc_ctx* ctx, CsrSystem* s) {
-  const int n = s->n;
+  const int n = s->ord.nE;
   FC_CUDA_TRY(ctx, s->a32.alloc(s->nnz));
   DVec<float>* v32[] = {&s->fr, &s->fr0, &s->fp, &s->fu, &s->fz, &s->fv, &s->fd, &s->fx, &s->fy, &s->fw};
   for (auto* v : v32) FC_CUDA_TRY(ctx, v->alloc(n));
-  return FC_OK;
+  return alloc_ordered(ctx, s, s->o32);
 }
 
 int sys_upload_values(fc_ctx* ctx, CsrSystem* s, const double* a, bool a_on_device) {
@@ -624,66 +728,82 @@ int sys_upload_values(fc_ctx* ctx, CsrSystem* s, const double* a, bool a_on_devi
   return FC_OK;
 }
 
-static TileSched tsched_of(DevSweep& D) {
-  TileSched t;
-  t.ntiles = D.ntiles; t.nlev = D.nlev; t.R = D.R; t.max_slots = D.max_slots;
-  t.tile_step_ptr = D.tile_step_ptr.p; t.step_level = D.step_level.p; t.tile_slots = D.tile_slots.p;
-  t.step_row_ptr = D.step_row_ptr.p; t.rows = D.rows.p; t.kbne = D.kbne.p;
-  return t;
-}
-
 template <class T>
 static CsrView<T> view_of(CsrSystem* s, const T* a) {
   CsrView<T> v;
   v.n = s->n;
   v.ia = s->ia.p; v.ja = s->ja.p; v.dg = s->diag.p; v.ts = s->tslot.p; v.a = a;
-  v.code = s->code.p;
-  v.F = tsched_of(s->sf);
-  v.B = tsched_of(s->sb);
   v.lfp = s->lf.ptr.p; v.lfr = s->lf.rows.p; v.nlf = s->lf.nlev;
   v.lbp = s->lb.ptr.p; v.lbr = s->lb.rows.p; v.nlb = s->lb.nlev;
   return v;
 }
 
-// grid size of a cooperative launch: co-resident blocks, capped so the
-// barrier stays cheap, and no more than the rows need
-static int coop_blocks(fc_ctx* ctx, const void* fn, int n, int per_sm_cap) {
-  int nb = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, FC_BLOCK, 0);
-  nb = std::max(1, std::min(nb, per_sm_cap));
-  int blocks = nb * ctx->num_sms;
-  int need = (n + FC_BLOCK - 1) / FC_BLOCK;
-  return std::max(1, std::min(blocks, need));
+static OrdView ord_view_of(CsrSystem* s) {
+  DevOrdered& D = s->ord;
+  OrdView O;
+  O.n = D.n; O.nE = D.nE; O.ntiles = D.ntiles; O.R = D.R; O.K = D.K; O.novf0 = D.novf[0]; O.novf1 = D.novf[1];
+  O.nsteps = D.nsteps; O.maxW = D.maxW; O.xmax = D.xmax; O.pmax = D.pmax;
+  O.tile_step_ptr = D.tile_step_ptr.p; O.step_ptr = D.step_ptr.p; O.tile_W = D.tile_W.p; O.perm = D.perm.p;
+  for (int d = 0; d < 2; ++d) {
+    O.srec[d] = (const int4*)D.srec[d].p; O.xv_ptr[d] = D.xv_ptr[d].p; O.push_ptr[d] = D.push_ptr[d].p;
+    O.push[d] = D.push[d].p; O.slot[d] = D.slot[d].p;
+    O.ovf_ptr[d] = D.ovf_ptr[d].p; O.ovf_code[d] = D.ovf_code[d].p; O.ovf_col[d] = D.ovf_col[d].p;
+    O.ovf_slot[d] = D.ovf_slot[d].p;
+  }
+  O.ucol = (const int4*)D.ucol.p;
+  O.lo_tslot = D.lo_tslot.p; O.lo_ovf_tslot = D.lo_ovf_tslot.p; O.dslot = D.dslot.p;
+  O.p_ptr = D.p_ptr.p; O.p_col = D.p_col.p; O.p_slot = D.p_slot.p;
+  return O;
 }
 
 template <class T>
-static int launch_coop(fc_ctx* ctx, CsrSystem* s, const void* fn, KArgs<T>& A, void** extra, int nextra) {
-  // one block per tile of the sweep schedules (every tile must be resident)
-  const size_t smem = sweep_smem_bytes<T>(s->sf.R, s->sf.max_slots, s->sb.R, s->sb.max_slots);
+static OrdVals<T> vals_of(OrdStore<T>& S) {
+  OrdVals<T> V;
+  V.vrec[0] = S.vrec0.p; V.vrec[1] = S.vrec1.p; V.sx = S.sx.p; V.aovf[0] = S.aovf0.p; V.aovf[1] = S.aovf1.p;
+  V.tovf = S.tovf.p; V.adiag = S.adiag.p; V.ap = S.ap.p; V.xv[0] = S.xv0.p; V.xv[1] = S.xv1.p;
+  return V;
+}
+
+// Cooperative launch of a persistent solver kernel: one block per SM (the
+// ordered sweeps need one resident block per tile, tiles <= SMs).
+template <class T>
+static int launch_coop(fc_ctx* ctx, CsrSystem* s, const void* fn, KArgs<T>& A, void** extra, int nextra,
+                       int block = FC_SWEEP_BLOCK) {
+  const DevOrdered& D = s->ord;
+  const size_t smem = osweep_smem_bytes<T>(D.R, D.K, D.maxW, D.max_tile_steps, D.xmax, D.pmax);
   if (smem > 48 * 1024)
     FC_CUDA_TRY(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int nb = 0;
-  FC_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, FC_BLOCK, smem));
-  const int blocks = std::max(1, std::max(s->sf.ntiles, s->sb.ntiles));
-  if (nb * ctx->num_sms < blocks)
+  FC_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, block, smem));
+  const int blocks = std::max(1, ctx->num_sms);
+  if (nb < 1 || D.ntiles > blocks)
     return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "sweep schedule needs more resident blocks than the GPU holds");
   FC_CUDA_TRY(ctx, cudaMemsetAsync(s->bar.p, 0, 2 * sizeof(unsigned), ctx->stream));
   FC_CUDA_TRY(ctx, cudaMemsetAsync(s->status.p, 0, sizeof(int), ctx->stream));
   void* args[4] = {&A, nullptr, nullptr, nullptr};
   for (int i = 0; i < nextra; ++i) args[1 + i] = extra[i];
-  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(FC_BLOCK), args, smem, ctx->stream);
+  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(block), args, smem, ctx->stream);
   if (e != cudaSuccess) return fc_fail(ctx, FC_ERR_CUDA, "cooperative launch", e);
   ctx->kernel_launches++;
   return FC_OK;
 }
+
+template <class T> static OrdStore<T>& store_of(CsrSystem* s);
+template <> OrdStore<double>& store_of<double>(CsrSystem* s) { return s->o64; }
+template <> OrdStore<float>& store_of<float>(CsrSystem* s) { return s->o32; }
 
 template <class T>
 static KArgs<T> make_args(CsrSystem* s, const T* a, T* x, const T* b, T* r, T* r0, T* p, T* u, T* z, T* v, T* d,
                           T* w, int itr_max, double tol_abs, double tol_rel) {
   KArgs<T> A;
   A.S = view_of<T>(s, a);
+  A.O = ord_view_of(s);
+  OrdStore<T>& st = store_of<T>(s);
+  A.V = vals_of<T>(st);
+  A.nnz = s->nnz;
   A.C.bar = s->bar.p; A.C.part = s->part.p; A.C.status = s->status.p; A.C.out = s->out.p;
-  A.x = x; A.b = b; A.r = r; A.r0 = r0; A.p = p; A.u = u; A.z = z; A.v = v; A.d = d; A.w = w;
+  A.x = x; A.b = b; A.xo = st.xo.p; A.bo = st.bo.p;
+  A.r = r; A.r0 = r0; A.p = p; A.u = u; A.z = z; A.v = v; A.d = d; A.w = w;
   A.itr_max = itr_max; A.tol_abs = tol_abs; A.tol_rel = tol_rel; A.skip_setup = 0;
   A.trace = nullptr;
   A.trace_cap = 0;
@@ -710,8 +830,8 @@ static int solve_fp64(fc_ctx* ctx, CsrSystem* s, const std::string& solver, cons
                                       s->w.p, itr_max, tol_abs, tol_rel);
   const bool traced = ctx->tracing && solver == "iccg";
   if (traced) {
-    const int nb = std::max(1, max(s->sf.ntiles, s->sb.ntiles));
-    const int cap = max(s->sf.nlev, s->sb.nlev) + 1;
+    const int nb = std::max(1, ctx->num_sms);
+    const int cap = s->ord.max_tile_steps + 1;
     FC_CUDA_TRY(ctx, ctx->trace.alloc((size_t)nb * FC_TRACE_N + (size_t)2 * nb * cap * 2));
     FC_CUDA_TRY(ctx, cudaMemsetAsync(ctx->trace.p, 0, ctx->trace.bytes(), ctx->stream));
     A.trace = ctx->trace.p;
@@ -727,7 +847,7 @@ static int solve_fp64(fc_ctx* ctx, CsrSystem* s, const std::string& solver, cons
   else if (solver == "bicgstab") {
     if (s->tslot_oob) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "bicgstab: pattern is not structurally symmetric");
     st = launch_coop(ctx, s, (const void*)k_bicgstab<double>, A, nullptr, 0);
-  } else if (solver == "dpcg") st = launch_coop(ctx, s, (const void*)k_dpcg<double>, A, nullptr, 0);
+  } else if (solver == "dpcg") st = launch_coop(ctx, s, (const void*)k_dpcg<double>, A, nullptr, 0, FC_BLOCK);
   else if (solver == "gauss-seidel") st = launch_coop(ctx, s, (const void*)k_gauss_seidel, A, nullptr, 0);
   else return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "unknown solver '" + solver + "'");
   if (st) return st;
@@ -759,7 +879,7 @@ static int solve_mixed(fc_ctx* ctx, CsrSystem* s, const std::string& solver, con
   bool first = true;
   const int max_outer = 64;
   for (;;) {
-    if ((st = launch_coop(ctx, s, (const void*)k_residual64, R, nullptr, 0))) return st;
+    if ((st = launch_coop(ctx, s, (const void*)k_residual64, R, nullptr, 0, FC_BLOCK))) return st;
     FC_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_out, s->out.p, FC_OUT_N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     FC_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_status, s->status.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -788,7 +908,7 @@ static int solve_mixed(fc_ctx* ctx, CsrSystem* s, const std::string& solver, con
     F.skip_setup = outer > 0 ? 1 : 0;
     const void* fn = solver == "iccg" ? (const void*)k_iccg<float>
                      : solver == "bicgstab" ? (const void*)k_bicgstab<float> : (const void*)k_dpcg<float>;
-    if ((st = launch_coop(ctx, s, fn, F, nullptr, 0))) return st;
+    if ((st = launch_coop(ctx, s, fn, F, nullptr, 0, solver == "dpcg" ? FC_BLOCK : FC_SWEEP_BLOCK))) return st;
     FC_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_out, s->out.p, FC_OUT_N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     FC_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_status, s->status.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -844,7 +964,7 @@ int sys_precond(fc_ctx* ctx, CsrSystem* s, int dilu, const double* q, double* z_
                 : launch_coop(ctx, s, (const void*)k_precond<double, false>, A, extra, 1);
   if (st) return st;
   FC_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_status, s->status.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  if (d_out) FC_CUDA_TRY(ctx, cudaMemcpyAsync(d_out, s->d.p, s->n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (d_out) FC_CUDA_TRY(ctx, cudaMemcpyAsync(d_out, s->v.p, s->n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   if (z_out && apply)
     FC_CUDA_TRY(ctx, cudaMemcpyAsync(z_out, s->z.p, s->n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));

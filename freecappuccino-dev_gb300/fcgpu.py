@@ -464,10 +464,10 @@ class Context:
         return float(r0[0]), info, st
 
     def sweep_stats(self, which=0):
-        out = np.zeros(8)
+        out = np.zeros(10)
         self._check(self.L.fc_sweep_stats(self.h, which, _ptr(out)), "fc_sweep_stats")
-        keys = ("tiles", "levels", "max_slots", "ring_depth", "est_sweep_us", "ring_entries", "cross_tile_entries",
-                "global_same_tile_entries")
+        keys = ("tiles", "levels", "max_width", "ring_depth", "est_sweep_us", "ring_entries", "pushed_entries",
+                "cross_tile_entries", "stages", "max_tile_steps")
         return dict(zip(keys, [float(v) for v in out]))
 
     def set_tracing(self, on=True):

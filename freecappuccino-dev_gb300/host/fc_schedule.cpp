@@ -348,3 +348,176 @@ double estimate_sweep_us(const SweepSchedule& S, double tau0, double per_row, do
   }
   return tmax;
 }
+
+// ---------------------------------------------------------------------------
+int symmetric_levels(int n, const int* ia, const int* ja, const int* dg, std::vector<int>& lev) {
+  lev.assign(n, 0);
+  for (int i = 0; i < n; ++i) {
+    int l = lev[i];
+    for (int k = ia[i]; k < dg[i]; ++k) l = std::max(l, lev[ja[k]] + 1);
+    lev[i] = l;
+    for (int k = dg[i] + 1; k < ia[i + 1]; ++k) lev[ja[k]] = std::max(lev[ja[k]], l + 1);
+  }
+  int nlev = 0;
+  for (int i = 0; i < n; ++i) nlev = std::max(nlev, lev[i] + 1);
+  return nlev;
+}
+
+bool build_ordered_sweep(int n, const int* ia, const int* ja, const int* dg, const int* ts, int ntiles,
+                         const double* xyz, int R, OrderedSweep& O, SweepSchedule& S, std::string& err) {
+  O = OrderedSweep();
+  O.n = n;
+  O.R = std::max(2, R);
+  std::vector<int> lev;
+  const int nlev = symmetric_levels(n, ia, ja, dg, lev);
+  O.nlev = nlev;
+  std::vector<int> code_tmp((size_t)ia[n], 0);
+  build_sweep_schedule(n, ia, ja, dg, lev, nlev, true, ntiles, xyz, S, code_tmp);
+  // ---- new numbering: tile, step, slot order, empty slots dropped
+  const int T = S.ntiles;
+  O.ntiles = T;
+  O.nsteps = S.tile_step_ptr[T];
+  O.tile_step_ptr = S.tile_step_ptr;
+  O.step_ptr.assign(O.nsteps + 1, 0);
+  O.tile_W.assign(T, 1);
+  O.perm.reserve(n);
+  O.iperm.assign(n, -1);
+  std::vector<int> row_tile(n), row_ls(n), row_pos(n);
+  for (int t = 0; t < T; ++t) {
+    O.max_tile_steps = std::max(O.max_tile_steps, S.tile_step_ptr[t + 1] - S.tile_step_ptr[t]);
+    for (int gs = S.tile_step_ptr[t]; gs < S.tile_step_ptr[t + 1]; ++gs) {
+      O.step_ptr[gs] = (int)O.perm.size();
+      int pos = 0;
+      for (int q = S.step_row_ptr[gs]; q < S.step_row_ptr[gs + 1]; ++q) {
+        const int i = S.rows[q];
+        if (i < 0) continue;
+        O.iperm[i] = (int)O.perm.size();
+        O.perm.push_back(i);
+        row_tile[i] = t;
+        row_ls[i] = gs - S.tile_step_ptr[t];
+        row_pos[i] = pos++;
+      }
+      O.tile_W[t] = std::max(O.tile_W[t], pos);
+    }
+  }
+  O.step_ptr[O.nsteps] = (int)O.perm.size();
+  if ((int)O.perm.size() != n) { err = "ordered sweep: schedule does not cover every row once"; return false; }
+  for (int t = 0; t < T; ++t) O.maxW = std::max(O.maxW, O.tile_W[t]);
+  const int nE = (n + 3) & ~3;
+  O.nE = nE;
+  const size_t E = (size_t)FC_ELL * nE;
+  // ---- per triangle: entries, codes, exchange and push blocks
+  std::vector<int> row_step(n);  // global step of every new row
+  for (int gs = 0; gs < O.nsteps; ++gs)
+    for (int q = O.step_ptr[gs]; q < O.step_ptr[gs + 1]; ++q) row_step[q] = gs;
+  for (int dirn = 0; dirn < 2; ++dirn) {
+    OrderedDir& D = O.dir[dirn];
+    D.ne.assign(nE, 0);
+    D.slot.assign(E, -1);
+    D.col.assign(E, 0);
+    D.srec.assign((size_t)4 * nE, 0);
+    D.ovf_ptr.assign(n + 1, 0);
+    for (int q = 0; q < n; ++q) {
+      const int i = O.perm[q];
+      const int k0 = dirn == 0 ? ia[i] : dg[i] + 1, k1 = dirn == 0 ? dg[i] : ia[i + 1];
+      D.ne[q] = k1 - k0;
+      D.ovf_ptr[q + 1] = D.ovf_ptr[q] + std::max(0, k1 - k0 - FC_ELL);
+    }
+    const int novf = D.ovf_ptr[n];
+    D.ovf_slot.assign(novf, -1);
+    D.ovf_code.assign(novf, 0);
+    D.ovf_col.assign(novf, 0);
+    std::vector<int> nx(n, 0);                  // exchange slots of each consumer row
+    std::vector<std::vector<std::pair<int, int>>> cons(n);  // producer -> (consumer row, its m-th slot)
+    for (int q = 0; q < n; ++q) {
+      const int i = O.perm[q], t = row_tile[i];
+      const int nst = S.tile_step_ptr[t + 1] - S.tile_step_ptr[t];
+      const int W = O.tile_W[t];
+      const int my = dirn == 0 ? row_ls[i] : nst - 1 - row_ls[i];
+      const int k0 = dirn == 0 ? ia[i] : dg[i] + 1;
+      int codes[FC_ELL] = {0, 0, 0, 0};
+      for (int e = 0; e < D.ne[q]; ++e) {
+        const int k = k0 + e, j = ja[k], qj = O.iperm[j];
+        int c;
+        if (row_tile[j] == t) {
+          const int pj = dirn == 0 ? row_ls[j] : nst - 1 - row_ls[j];
+          if (pj >= my) { err = "ordered sweep: dependency not before its consumer in the tile"; return false; }
+          if (my - pj <= O.R - 1) c = (pj % O.R) * W + row_pos[j];
+          else c = -1;
+        } else {
+          c = -1;
+          D.cross_tile_entries++;
+        }
+        if (c > 65534) { err = "ordered sweep: ring index does not fit 16 bits"; return false; }
+        if (c < 0) { cons[qj].push_back({q, nx[q]++}); D.pushed_entries++; } else D.ring_entries++;
+        if (e < FC_ELL) {
+          D.slot[(size_t)e * nE + q] = k;
+          D.col[(size_t)e * nE + q] = qj;
+          codes[e] = c + 1;
+        } else {
+          const int o = D.ovf_ptr[q] + e - FC_ELL;
+          D.ovf_slot[o] = k;
+          D.ovf_code[o] = c;
+          D.ovf_col[o] = qj;
+        }
+      }
+      D.srec[4 * (size_t)q + 2] = codes[0] | (codes[1] << 16);
+      D.srec[4 * (size_t)q + 3] = codes[2] | (codes[3] << 16);
+    }
+    // exchange blocks (consumer side) and push blocks (producer side), one
+    // per step, each starting on a multiple of 4 elements
+    D.xv_ptr.assign(O.nsteps + 1, 0);
+    D.push_ptr.assign(O.nsteps + 1, 0);
+    std::vector<int> xoff(n, 0), poff(n, 0);
+    for (int gs = 0; gs < O.nsteps; ++gs) {
+      int xs = 0, ps = 0;
+      for (int q = O.step_ptr[gs]; q < O.step_ptr[gs + 1]; ++q) {
+        xoff[q] = xs;
+        poff[q] = ps;
+        xs += nx[q];
+        ps += (int)cons[q].size();
+      }
+      if (xs > 65535 || ps > (1 << 30)) { err = "ordered sweep: exchange block of a step too large"; return false; }
+      D.xv_ptr[gs + 1] = D.xv_ptr[gs] + ((xs + 3) & ~3);
+      D.push_ptr[gs + 1] = D.push_ptr[gs] + ((ps + 3) & ~3);
+    }
+    D.push.assign(D.push_ptr[O.nsteps], 0);
+    for (int q = 0; q < n; ++q) {
+      const int np = (int)cons[q].size();
+      if (nx[q] > 255 || np > 255) { err = "ordered sweep: more than 255 exchanged entries in a row"; return false; }
+      D.srec[4 * (size_t)q] = D.ne[q] | (np << 8) | (xoff[q] << 16);
+      D.srec[4 * (size_t)q + 1] = poff[q];
+      for (int m = 0; m < np; ++m) {
+        const int qc = cons[q][m].first, mc = cons[q][m].second;
+        D.push[D.push_ptr[row_step[q]] + poff[q] + m] = D.xv_ptr[row_step[qc]] + xoff[qc] + mc;
+      }
+    }
+  }
+  // ---- DILU transpose slots of the lower entries, diagonal slots, matrix
+  O.lo_tslot.assign(E, 0);
+  O.lo_ovf_tslot.assign(O.dir[0].ovf_ptr[n], 0);
+  O.dslot.assign(nE, 0);
+  O.p_ptr.assign(n + 1, 0);
+  for (int q = 0; q < n; ++q) {
+    const int i = O.perm[q];
+    O.dslot[q] = dg[i];
+    O.p_ptr[q + 1] = O.p_ptr[q] + (ia[i + 1] - ia[i]);
+    for (int e = 0; e < O.dir[0].ne[q]; ++e) {
+      const int k = ia[i] + e;
+      const int tsk = ts ? ts[k] : k;
+      if (e < FC_ELL) O.lo_tslot[(size_t)e * nE + q] = tsk;
+      else O.lo_ovf_tslot[O.dir[0].ovf_ptr[q] + e - FC_ELL] = tsk;
+    }
+  }
+  O.p_col.resize(ia[n]);
+  O.p_slot.resize(ia[n]);
+  for (int q = 0; q < n; ++q) {
+    const int i = O.perm[q];
+    int o = O.p_ptr[q];
+    for (int k = ia[i]; k < ia[i + 1]; ++k, ++o) {
+      O.p_col[o] = O.iperm[ja[k]];
+      O.p_slot[o] = k;
+    }
+  }
+  return true;
+}

@@ -10,6 +10,7 @@
 // in the last R steps are read from a shared-memory ring, everything else
 // from global memory after the producing tile has published enough progress.
 #pragma once
+#include <string>
 #include <vector>
 
 struct SweepSchedule {
@@ -47,3 +48,70 @@ void build_sweep_schedule(int n, const int* ia, const int* ja, const int* dg, co
 // Critical-path estimate (microseconds) of a schedule: per step tau0 +
 // per_row * rows, cross-tile waits delayed by hop after publication.
 double estimate_sweep_us(const SweepSchedule& S, double tau0, double per_row, double hop);
+
+// ---------------------------------------------------------------------------
+// Schedule-ordered sweep structure.
+//
+// The rows are renumbered in schedule order: tile by tile, step by step, so
+// that every step of every tile is a contiguous range of new row indices and
+// a thread block walks consecutive memory.  The forward sweep runs the steps
+// of a tile in order, the backward sweep runs them in reverse; this is valid
+// for both triangles because the levels are taken over the symmetrised
+// pattern (row i waits for every j < i with a_ij != 0 or a_ji != 0).
+//
+// Per new row and per triangle the first FC_ELL entries (in the row's CSR
+// order) are stored column-major (entry e of row q at e*nE + q, nE = n
+// rounded up to a multiple of 4 so that every column starts 16-byte
+// aligned), the rest in an overflow list.  A dependency produced in the same tile within the last
+// R-1 steps is read from the block's shared-memory ring (code >= 0: ring
+// index (local step % R) * W + position); every other dependency is pushed:
+// its producer stores the value into the consumer's own slot of an exchange
+// array xv.  The slots of a step's rows form one contiguous block of xv (in
+// row order, entries in CSR order), so the consumer fetches all values the
+// step needs with one copy; the producer's targets likewise form one block
+// per producing step.
+#define FC_ELL 4
+
+struct OrderedDir {
+  std::vector<int> ne;        // [nE] entries of this triangle in the row
+  std::vector<int> slot;      // [FC_ELL*nE] original CSR slot, -1 past ne (coefficient gather)
+  std::vector<int> col;       // [FC_ELL*nE] new index of the entry's column
+  // [4*nE] packed row record, one 16-byte load per row:
+  //   [0] ne | np << 8 | xoff << 16   (np: pushes of the row's value; xoff:
+  //       first exchange slot of the row in its step's exchange block)
+  //   [1] poff: first push target of the row in its step's push block
+  //   [2], [3] codes of entries 0..3, 16 bits each, stored as code + 1
+  //       (0: the value arrives through the exchange block)
+  std::vector<int> srec;
+  std::vector<int> xv_ptr;    // [nsteps+1] exchange block of each step (multiples of 4)
+  std::vector<int> push_ptr;  // [nsteps+1] push block of each step (multiples of 4)
+  std::vector<int> push;      // absolute exchange positions the values are pushed to
+  std::vector<int> ovf_ptr;   // [n+1] entries e >= FC_ELL
+  std::vector<int> ovf_slot, ovf_code, ovf_col;
+  long long ring_entries = 0, pushed_entries = 0, cross_tile_entries = 0;
+};
+
+struct OrderedSweep {
+  int n = 0, nE = 0, ntiles = 0, nsteps = 0, nlev = 0, R = 4, maxW = 0, max_tile_steps = 0;
+  std::vector<int> perm, iperm;    // new -> old, old -> new
+  std::vector<int> tile_step_ptr;  // [ntiles+1]
+  std::vector<int> step_ptr;       // [nsteps+1] first new row of each step
+  std::vector<int> tile_W;         // widest step of each tile (ring / staging width)
+  OrderedDir dir[2];               // 0: left of the diagonal (forward), 1: right (backward)
+  std::vector<int> lo_tslot;       // [FC_ELL*nE] transpose slot of each lower entry (DILU)
+  std::vector<int> lo_ovf_tslot;
+  std::vector<int> dslot;          // [nE] original diagonal slot (0 in the padding)
+  std::vector<int> p_ptr, p_col, p_slot;  // the matrix in new numbering, entries in original order
+};
+
+// levels over the symmetrised lower triangle: lev(i) = 1 + max lev(j) over
+// j < i with a_ij != 0 or a_ji != 0; returns the number of levels
+int symmetric_levels(int n, const int* ia, const int* ja, const int* dg, std::vector<int>& lev);
+
+// ia, ja, dg 0-based; ts (optional) the transpose slot of every entry;
+// ntiles the tile target; xyz (optional) row coordinates for the tiling; R
+// the ring depth.  S receives the underlying tiled schedule (for the
+// critical-path estimate).  Returns false with a message if a consistency
+// check fails.
+bool build_ordered_sweep(int n, const int* ia, const int* ja, const int* dg, const int* ts, int ntiles,
+                         const double* xyz, int R, OrderedSweep& O, SweepSchedule& S, std::string& err);

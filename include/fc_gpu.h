@@ -154,10 +154,11 @@ int fc_precond_apply(fc_ctx* ctx, const char* kind, int n, int nnz, const int* i
 /* y = A x (ax_cr, linear_solvers.f90:1173) or y = A^T x (atx_cr, :1079). */
 int fc_spmv(fc_ctx* ctx, int n, int nnz, const int* ia, const int* ja, const double* a, const int* diag,
             const double* x, double* y, int transpose);
-/* Statistics of the tiled sweep schedule of the mesh system (which=0) or of
- * the cached fc_csrsolve pattern (which=1): out[8] = tiles, levels, widest
- * tile, ring depth, estimated forward-sweep us, ring-served entries,
- * cross-tile entries, same-tile global entries. */
+/* Statistics of the schedule-ordered sweep structure of the mesh system
+ * (which=0) or of the cached fc_csrsolve pattern (which=1): out[10] = tiles,
+ * levels, widest step of a tile, ring depth, estimated forward-sweep us,
+ * ring-served entries, pushed entries, cross-tile entries (both triangles),
+ * stage depth, most steps of a tile. */
 int fc_sweep_stats(fc_ctx* ctx, int which, double* out);
 /* Tracing of the FP64 ICCG kernel (no counterpart in the reference): with
  * on != 0 the solves run a traced instantiation that records per block the

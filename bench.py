@@ -33,6 +33,10 @@ PKG = os.path.join(ROOT, "freecappuccino-dev_gb300")
 METRIC = "SIMPLE iters/s & p-solve time to 1e-8 resid, mixed vs FP64 GPU; HBM GB/s"
 PERTURB, MESH_SEED, RHS_SEED = 0.15, 42, 43
 TOL_REL, ITR_MAX = 1e-10, 20000
+# ICCG iterations of a full solve to TOL_REL, from complete runs of the oracle
+# (the same counts as the GPU solver's): the CPU arms time a bounded sample of
+# iterations and scale it to a full solve
+ITERS_PER_SOLVE = {32: 95, 64: 182, 128: 358}
 
 
 def load_fc():
@@ -160,8 +164,6 @@ def run_reference(args, rank, world):
     oc.set("su", b)
     oc.laplacian(np.ones(m.numCells), np.zeros(m.numTotal), 0b1)
     ia, ja, a, dg = oc.get_int("ia"), oc.get_int("ja"), oc.get("a"), oc.get_int("diag")
-    # iterations of a full solve, from a short FP64 run's convergence rate is
-    # not known in advance: estimate from the problem size of previous runs
     iters = args.ref_iters
     per = []
     for k in range(args.warmup + args.steps):
@@ -314,7 +316,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=128, help="cells per side of the cube")
-    ap.add_argument("--ref-sample", type=int, default=40, help="ICCG iterations per CPU sample")
+    ap.add_argument("--ref-sample", type=int, default=120, help="ICCG iterations per CPU sample")
     ap.add_argument("--ref-iters", type=int, default=0, help="iterations of a full solve for the reference arm")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
@@ -326,7 +328,7 @@ def main():
         dist.init_process_group("gloo")
     if args.impl == "reference":
         if not args.ref_iters:
-            args.ref_iters = {128: 560}.get(args.n, int(4.4 * args.n))
+            args.ref_iters = ITERS_PER_SOLVE.get(args.n, int(2.8 * args.n))
         run_reference(args, rank, world)
     else:
         run_gpu(args, rank, world, dist)

@@ -522,9 +522,10 @@ static cudaError_t upload_vec(DVec<int>& d, const V& h) {
   return cudaMemcpy(d.p, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice);
 }
 
-// stage depth K of the ordered sweeps: as deep as the shared memory allows
+// stage depth K of the ordered sweeps: the largest power of two the shared
+// memory allows (the sweep indexes its buffers with k & (K-1))
 static int ordered_stages(const DevOrdered& D) {
-  for (int K = FC_MAX_STAGES; K > 1; --K)
+  for (int K = FC_MAX_STAGES; K > 1; K >>= 1)
     if (osweep_smem_bytes<double>(D.R, K, D.maxW, D.max_tile_steps, D.xmax, D.pmax) <= FC_SWEEP_SMEM) return K;
   return 1;
 }

@@ -299,7 +299,7 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
       bool ok = true;
       for (int k = 0; k < ns && ok; ++k) {
         if (*((volatile int*)X.abort_flag)) break;
-        const int b = k % K;
+        const int b = k & (K - 1);
         // a timeout here only records the status: the compute warps then run
         // out of their own bounded wait and raise the abort flag themselves,
         // so that they all see it after the same named barrier
@@ -341,43 +341,61 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
     }
   } else {
     // ------------------------------------------------------------ compute
+    const int kmask = K - 1;  // K and R are powers of two
     for (int k = 0; k < ns; ++k) {
       if (tr) tr->step(k);
-      const int b = k % K;
-      if (!mbar_wait(X.full + b, (X.parity >> b) & 1u)) {
+      const int b = k & kmask;
+      const int ls = step_of(k);
+      const int base = sp[ls], cnt = sp[ls + 1] - base, woff = base - (base & ~3);
+      // only warps with rows in this step read the buffer, so only they wait
+      // for it (an mbarrier poll by every warp would serialise on its word)
+      if ((int)(threadIdx.x & ~31u) < cnt && !mbar_wait(X.full + b, (X.parity >> b) & 1u)) {
         atomicCAS(C.status, 0, FC_ERR_TIMEOUT);
         *((volatile int*)X.abort_flag) = 1;
       }
-      const int ls = step_of(k);
-      const int base = sp[ls], cnt = sp[ls + 1] - base, woff = base - (base & ~3);
       const int xbase = xp[ls];
       const unsigned char* B = X.stage + (size_t)b * L.bytes;
       const int4* S4 = (const int4*)(B + L.oS);
       const T* VRc = (const T*)(B + L.oV);
       const T* XS = (const T*)(B + L.oXV);
       const int* PS = (const int*)(B + L.oP);
+      T* ring_out = ring + (k & (R - 1)) * W;
       for (int sl = threadIdx.x; sl < cnt; sl += nct) {
         const int q = base + sl;
         const int4 sr = S4[sl];
         const int ne = sr.x & 255, np = (sr.x >> 8) & 255, xoff = (int)((unsigned)sr.x >> 16), poff = sr.y;
         const T* vr = VRc + sl * VR;
-        // dependency values of entries 0..3: ring, or the exchange block
+        // dependency values of entries 0..3 without branches: entries past
+        // ne have code 0 and coefficient 0 and read exchange slot xoff (in
+        // bounds of the staged block or the padding), so they contribute an
+        // exact zero; ring (code > 0) or exchange block (code 0) by select
+        const unsigned cw[2] = {(unsigned)sr.z, (unsigned)sr.w};
         T dv[FC_ELL];
+        unsigned xmask = 0;  // entries that come through the exchange block
         int m = 0;
 #pragma unroll
         for (int e = 0; e < FC_ELL; ++e) {
-          dv[e] = T(0);
-          const int c = (int)(((unsigned)(e < 2 ? sr.z : sr.w) >> (16 * (e & 1))) & 0xFFFFu) - 1;
-          if (e < ne) {
-            if (c >= 0) dv[e] = ring[c];
-            else {
-              T v = XS[xoff + m];
-              if (Sentinel<T>::is(v)) v = xv_wait<T>(C, xv + xbase + xoff + m, X.abort_flag);
-              xv[xbase + xoff + m] = Sentinel<T>::value();
+          const int c1 = (int)((cw[e >> 1] >> (16 * (e & 1))) & 0xFFFFu);  // code + 1
+          const bool ex = c1 == 0 && e < ne;
+          const T rv = ring[c1 > 0 ? c1 - 1 : 0];
+          const T xv_ = XS[xoff + m];
+          dv[e] = c1 > 0 ? rv : (ex ? xv_ : T(0));
+          xmask |= (ex ? 1u : 0u) << e;
+          m += ex ? 1 : 0;
+        }
+        if (xmask) {
+          // exchanged values: poll the slot if the staged copy was taken
+          // before the producer's store, and put the sentinel back
+          int mm = 0;
+#pragma unroll
+          for (int e = 0; e < FC_ELL; ++e)
+            if ((xmask >> e) & 1u) {
+              T v = dv[e];
+              if (Sentinel<T>::is(v)) v = xv_wait<T>(C, xv + xbase + xoff + mm, X.abort_flag);
+              xv[xbase + xoff + mm] = Sentinel<T>::value();
               dv[e] = v;
-              ++m;
+              ++mm;
             }
-          }
         }
         // overflow entry e >= FC_ELL: its value and coefficient
         auto dep_ovf = [&](int e, T& a) -> T {
@@ -394,6 +412,7 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
         T val;
         if (kSetup) {
           // d_i = a_ii - sum a_k^2 d_j (DIC) or a_k d_j a_(j,i) (DILU), then 1/d_i
+          // (the recurrence is exact, so entries past ne are skipped)
           const T* sx = (const T*)(B + L.oX2) + sl * VR;
           T di = sx[0];
 #pragma unroll
@@ -449,13 +468,16 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
         } else {
           // forward: y_i = (q_i - sum a y_j) d_i;
           // backward: z_i = (y_i / (d_i + small) - sum a z_j) d_i, the division
-          // taken as a product with 1/(d_i + small) from the setup
+          // taken as a product with 1/(d_i + small) from the setup.  Entries
+          // 0..2 unconditionally (padding adds exactly zero), entry 3 when
+          // present.
           const T di = vr[4];
           T acc = ((const T*)(B + L.oQ))[woff + sl];
           if (dirn) acc = acc * vr[5];
-#pragma unroll
-          for (int e = 0; e < FC_ELL; ++e)
-            if (e < ne) acc = fma(-vr[e], dv[e], acc);
+          acc = fma(-vr[0], dv[0], acc);
+          acc = fma(-vr[1], dv[1], acc);
+          acc = fma(-vr[2], dv[2], acc);
+          if (ne > 3) acc = fma(-vr[3], dv[3], acc);
           for (int e = FC_ELL; e < ne; ++e) {
             T a;
             const T v = dep_ovf(e, a);
@@ -465,7 +487,7 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
           if (MODE == OS_BWD_DOT) red[0] += (double)((const T*)(B + L.oE))[woff + sl] * (double)val;
         }
         io.out[q] = val;
-        ring[(k % R) * W + sl] = val;
+        ring_out[sl] = val;
         for (int mm = 0; mm < np; ++mm) st_relaxed<T>(xv + PS[poff + mm], val);
       }
       bar_compute(nct);

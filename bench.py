@@ -188,6 +188,95 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+LID_PATCH = 3  # ymax patch of the box generator (xmin, xmax, ymin, ymax, zmin, zmax)
+
+
+def cavity_fields(m, nT, nC):
+    """Initial fields of the lid-driven cavity: lid u = 1 on the y = 1 wall."""
+    a = m.arrays()
+    u = np.zeros(nT)
+    st = a["startFace"][LID_PATCH] - m.numInnerFaces
+    u[nC + st:nC + st + a["nfaces"][LID_PATCH]] = 1.0
+    nwal = int(sum(nf for t, nf in zip(a["bctype"], a["nfaces"]) if t == 1))
+    return a, u, nwal
+
+
+def simple_block(fc, args, dev, with_cpu):
+    """C1: SIMPLE iterations per second on the n^3 lid-driven cavity (unit
+    cube, uniform hexes, nu = 0.01, central differencing with deferred
+    correction, Gauss gradients, BiCGStab(DILU) for U, ICCG(DIC) for p, the
+    settings of examples/cavity/input.nml), FP64 and mixed precision, plus the
+    oracle's SIMPLE iteration on one core."""
+    n = args.simple_n
+    m = fc.Mesh.box(n, n, n)
+    nC, nT = m.numCells, m.numTotal
+    a, u, nwal = cavity_fields(m, nT, nC)
+    ctx = fc.Context(dev)
+    ctx.set_mesh(m)
+    prm = fc.SimpleParams.cavity()
+
+    def reset():
+        zero = np.zeros(nT)
+        for k, v in dict(u=u, v=zero, w=zero, p=zero, pp=zero, den=np.ones(nT), vis=np.full(nT, 0.01)).items():
+            ctx.field_set(k, v)
+        ctx.field_set("visw", np.full(max(nwal, 1), 0.01))
+        for k in ("flmass", "a", "dUdxi", "dVdxi", "dWdxi", "dPdxi"):
+            ctx.field_fill(k, 0.0)
+        ctx.simple_params(prm)
+        ctx.init_flmass()
+
+    out = {"workload": f"{n}^3 lid-driven cavity, Re=100, SIMPLE (central/DC, Gauss, BiCGStab U, ICCG p)",
+           "cells": nC, "unit": "SIMPLE iters/s"}
+    for mode, key in ((fc.FC_PREC_FP64, "value"), (fc.FC_PREC_MIXED, "mixed")):
+        ctx.set_precision(mode, 1e-4, 0) if mode else ctx.set_precision(mode)
+        reset()
+        for _ in range(args.simple_skip):
+            ctx.simple_iteration()
+        ctx.sync()
+        ctx.event(0)
+        for _ in range(args.simple_iters):
+            res = ctx.simple_iteration()
+        ctx.event(1)
+        ms = ctx.elapsed_ms() / args.simple_iters
+        out[key] = 1e3 / ms
+        out[key + "_ms_per_iteration"] = ms
+        out[key + "_resor"] = [float(v) for v in res]
+    out["iterations_timed"] = f"{args.simple_iters} after {args.simple_skip} untimed"
+    ctx.set_precision(fc.FC_PREC_FP64)
+    ctx.close()
+    if with_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_lib
+        oc = oracle_lib.Case(a, fast=True)
+        zero = np.zeros(nT)
+        for k, v in dict(u=u, v=zero, w=zero, p=zero, pp=zero, den=np.ones(nT), vis=np.full(nT, 0.01)).items():
+            oc.set(k, v)
+        if nwal:
+            oc.set("visw", np.full(nwal, 0.01))
+        for k in ("flmass", "a"):
+            oc.set(k, np.zeros(oc._len(k)))
+        for k in ("dUdxi", "dVdxi", "dWdxi", "dPdxi"):
+            oc.set(k, np.zeros(3 * nT))
+        for name in ("viscos", "densit", "urfP", "gdsU", "cSchemeU", "pscheme", "maxiterU", "maxiterP", "npcor",
+                     "pRefCell", "tolAbsU", "tolRelU", "tolAbsP", "tolRelP", "gradScheme"):
+            oc.param(name, getattr(prm, name))
+        for i in range(3):
+            oc.param(f"urfU{i + 1}", prm.urfU[i])
+        oc.solver("U", prm.lSolverU.decode())
+        oc.solver("P", prm.lSolverP.decode())
+        oc.L.orc_init_flmass(oc.h)
+        for _ in range(args.simple_skip):
+            oc.simple_iteration()
+        t0 = time.perf_counter()
+        for _ in range(args.simple_cpu_iters):
+            oc.simple_iteration()
+        dt = (time.perf_counter() - t0) / args.simple_cpu_iters
+        out["cpu_baseline"] = {"value": 1.0 / dt, "unit": "SIMPLE iters/s", "cores": 1, "kind": "port",
+                               "sample": f"{args.simple_cpu_iters} SIMPLE iterations of the same cavity after "
+                                         f"{args.simple_skip} untimed (C++ restatement, -O3, one thread)"}
+    return out
+
+
 def run_gpu(args, rank, world, dist):
     fc = load_fc()
     dev = int(os.environ.get("LOCAL_RANK", "0"))
@@ -306,6 +395,8 @@ def run_gpu(args, rank, world, dist):
     ctx.close()
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(ia, ja, a_host, dg, b, iters, args.ref_sample)
+    if args.simple_n > 0:
+        line["simple"] = simple_block(fc, args, dev, not args.no_cpu)
     print(json.dumps(line), flush=True)
 
 
@@ -319,6 +410,10 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=120, help="ICCG iterations per CPU sample")
     ap.add_argument("--ref-iters", type=int, default=0, help="iterations of a full solve for the reference arm")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--simple-n", type=int, default=64, help="cells per side of the SIMPLE cavity (0: skip)")
+    ap.add_argument("--simple-iters", type=int, default=20, help="timed SIMPLE iterations")
+    ap.add_argument("--simple-skip", type=int, default=10, help="untimed SIMPLE iterations before them")
+    ap.add_argument("--simple-cpu-iters", type=int, default=3, help="oracle SIMPLE iterations timed")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

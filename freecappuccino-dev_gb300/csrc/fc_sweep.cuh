@@ -256,15 +256,6 @@ __device__ __noinline__ T xv_wait(const GridCtl& C, const T* p, int* abort_flag)
   return v;
 }
 
-template <class T>
-__device__ __forceinline__ void st_relaxed(T* p, T v);
-template <> __device__ __forceinline__ void st_relaxed<double>(double* p, double v) {
-  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(__double_as_longlong(v)) : "memory");
-}
-template <> __device__ __forceinline__ void st_relaxed<float>(float* p, float v) {
-  asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(__float_as_int(v)) : "memory");
-}
-
 // One ordered sweep of tile blockIdx.x.  dirn 0: forward over the lower
 // triangle, 1: backward over the upper one.  red (MODE OS_BWD_DOT: red[0] +=
 // e*value; OS_GS: red[0] += |residual|, red[1] += |a_ii x_i|) accumulates
@@ -285,7 +276,9 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
   const int ns = __ldg(O.tile_step_ptr + t + 1) - __ldg(O.tile_step_ptr + t);
   const StageLayout& L = X.L;
   const int K = O.K, R = O.R, W = L.W;
-  const int nct = (int)blockDim.x - 32;  // compute threads
+  const int nct = (int)blockDim.x - 32;  // threads before the staging warp
+  // compute threads of this tile: whole warps covering its widest step
+  const int ncg = min(nct, (W + 31) & ~31);
   T* ring = (T*)X.ring;
   T* xv = V.xv[dirn];
   const int* sp = X.sp;
@@ -339,8 +332,11 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
         X.used |= 1u << b;
       }
     }
-  } else {
+  } else if ((int)threadIdx.x < ncg) {
     // ------------------------------------------------------------ compute
+    // Only the ceil(W/32) warps that a step of this tile can occupy take
+    // part; the others skip the sweep, so they add no shared-memory traffic
+    // and no barrier arrivals to the steps.
     const int kmask = K - 1;  // K and R are powers of two
     for (int k = 0; k < ns; ++k) {
       if (tr) tr->step(k);
@@ -360,7 +356,7 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
       const T* XS = (const T*)(B + L.oXV);
       const int* PS = (const int*)(B + L.oP);
       T* ring_out = ring + (k & (R - 1)) * W;
-      for (int sl = threadIdx.x; sl < cnt; sl += nct) {
+      for (int sl = threadIdx.x; sl < cnt; sl += ncg) {
         const int q = base + sl;
         const int4 sr = S4[sl];
         const int ne = sr.x & 255, np = (sr.x >> 8) & 255, xoff = (int)((unsigned)sr.x >> 16), poff = sr.y;
@@ -488,9 +484,11 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
         }
         io.out[q] = val;
         ring_out[sl] = val;
-        for (int mm = 0; mm < np; ++mm) st_relaxed<T>(xv + PS[poff + mm], val);
+        // plain stores: an aligned 8-byte (4-byte) store is single-copy
+        // atomic, so a consumer polling the slot sees the sentinel or the value
+        for (int mm = 0; mm < np; ++mm) xv[PS[poff + mm]] = val;
       }
-      bar_compute(nct);
+      bar_compute(ncg);
       if (threadIdx.x == 0) mbar_arrive(X.empty + b);
       X.parity ^= 1u << b;
       X.used |= 1u << b;

@@ -117,6 +117,8 @@ struct MeshDev {
   DVec<int> owner, neighbour;              // 0-based cells
   DVec<int> bface_patch;                   // patch index of every boundary face
   DVec<int> bface_wall;                    // running wall-face counter (iWall-1) or -1
+  DVec<int> wall_face;                     // face index of every wall face, in wall-counter order
+  DVec<double> srdw;                       // |S| / normal distance per wall face (nwal)
   DVec<int> cf_ptr, cf_face;               // cell -> faces (ascending face index)
   DVec<double> arx, ary, arz, xf, yf, zf;  // numFaces
   DVec<double> xc, yc, zc, vol;            // numCells

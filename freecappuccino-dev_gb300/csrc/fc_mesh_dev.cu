@@ -121,14 +121,31 @@ __global__ void k_inner_geom(int nI, const int* __restrict__ owner, const int* _
   }
 }
 
+// dnw and srdw of the wall faces, geometry.f90:728-748
+__global__ void k_wall_geom(int nwal, const int* __restrict__ wall_face, const int* __restrict__ owner,
+                            const double* __restrict__ arx, const double* __restrict__ ary,
+                            const double* __restrict__ arz, const double* __restrict__ xf,
+                            const double* __restrict__ yf, const double* __restrict__ zf,
+                            const double* __restrict__ xc, const double* __restrict__ yc,
+                            const double* __restrict__ zc, double* srdw) {
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nwal; w += gridDim.x * blockDim.x) {
+    const int f = wall_face[w], p = owner[f];
+    const double ax = arx[f], ay = ary[f], az = arz[f];
+    const double are = __dsqrt_rn(DA(DA(DM(ax, ax), DM(ay, ay)), DM(az, az)));
+    const double nxf = DD(ax, are), nyf = DD(ay, are), nzf = DD(az, are);
+    const double dnw = DA(DA(DM(DS(xf[f], xc[p]), nxf), DM(DS(yf[f], yc[p]), nyf)), DM(DS(zf[f], zc[p]), nzf));
+    srdw[w] = DD(are, dnw);
+  }
+}
+
 }  // namespace
 
 static void free_mesh_dev(MeshDev& m) {
   DVec<double>* dv[] = {&m.x, &m.y, &m.z, &m.arx, &m.ary, &m.arz, &m.xf, &m.yf, &m.zf,
-                        &m.xc, &m.yc, &m.zc, &m.vol, &m.facint, &m.Df};
+                        &m.xc, &m.yc, &m.zc, &m.vol, &m.facint, &m.Df, &m.srdw};
   for (auto* v : dv) v->release();
   DVec<int>* iv[] = {&m.nnodes, &m.nodes, &m.owner, &m.neighbour, &m.bface_patch, &m.bface_wall,
-                     &m.cf_ptr, &m.cf_face, &m.ijk, &m.jik};
+                     &m.cf_ptr, &m.cf_face, &m.ijk, &m.jik, &m.wall_face};
   for (auto* v : iv) v->release();
   m.h_owner.clear(); m.h_neighbour.clear(); m.h_xyz.clear();
 }
@@ -189,14 +206,14 @@ extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
     }
   }
   // boundary face -> patch, wall counter
-  std::vector<int> bpatch(nB, -1), bwall(nB, -1);
+  std::vector<int> bpatch(nB, -1), bwall(nB, -1), wall_face;
   int iwall = 0;
   m.nwal = m.nsym = 0;
   for (int b = 0; b < m.numBoundaries; ++b) {
     for (int i = 0; i < hm->nfaces[b]; ++i) {
       int f = hm->startFace[b] + i - nI;
       bpatch[f] = b;
-      if (hm->bctype[b] == FC_BC_WALL) bwall[f] = iwall++;
+      if (hm->bctype[b] == FC_BC_WALL) { bwall[f] = iwall++; wall_face.push_back(nI + f); }
     }
     if (hm->bctype[b] == FC_BC_WALL) m.nwal += hm->nfaces[b];
     if (hm->bctype[b] == FC_BC_SYMMETRY) m.nsym += hm->nfaces[b];
@@ -249,6 +266,7 @@ extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
   UP(m.cf_face, cf_face.data(), cf_face.size());
   UP(m.bface_patch, bpatch.data(), nB);
   UP(m.bface_wall, bwall.data(), nB);
+  UP(m.wall_face, wall_face.data(), wall_face.size());
   UP(m.ijk, ijk.data(), nI);
   UP(m.jik, jik.data(), nI);
   DVec<double>* fv[] = {&m.arx, &m.ary, &m.arz, &m.xf, &m.yf, &m.zf};
@@ -267,6 +285,12 @@ extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
     k_inner_geom<<<grid(nI), TB, 0, ctx->stream>>>(nI, m.owner.p, m.neighbour.p, m.arx.p, m.ary.p, m.arz.p, m.xf.p,
                                                     m.yf.p, m.zf.p, m.xc.p, m.yc.p, m.zc.p, m.facint.p, m.Df.p);
   ctx->kernel_launches += 3;
+  FC_CUDA_TRY(ctx, m.srdw.alloc(m.nwal));
+  if (m.nwal > 0) {
+    k_wall_geom<<<grid(m.nwal), TB, 0, ctx->stream>>>(m.nwal, m.wall_face.p, m.owner.p, m.arx.p, m.ary.p, m.arz.p,
+                                                      m.xf.p, m.yf.p, m.zf.p, m.xc.p, m.yc.p, m.zc.p, m.srdw.p);
+    ctx->kernel_launches++;
+  }
   FC_CUDA_TRY(ctx, cudaGetLastError());
   FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   // the global matrix system of the mesh (module globals ia, ja, a, diag)
@@ -299,6 +323,7 @@ extern "C" int fc_get_geometry(fc_ctx* ctx, const char* name, double* out) {
   else if (n == "xf") v = &m.xf; else if (n == "yf") v = &m.yf; else if (n == "zf") v = &m.zf;
   else if (n == "xc") v = &m.xc; else if (n == "yc") v = &m.yc; else if (n == "zc") v = &m.zc;
   else if (n == "vol") v = &m.vol; else if (n == "facint") v = &m.facint; else if (n == "Df") v = &m.Df;
+  else if (n == "srdw") v = &m.srdw;
   else return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "unknown geometry array '" + n + "'");
   FC_CUDA_TRY(ctx, cudaMemcpy(out, v->p, v->bytes(), cudaMemcpyDeviceToHost));
   return FC_OK;

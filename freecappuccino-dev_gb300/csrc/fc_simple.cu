@@ -2,8 +2,10 @@
 // (Pressure/nablap.f90, bpres.f90), momentum assembly (Velocity/velocity.f90
 // calcuvw, facefluxuvw, facefluxuvw_bnd, updateVelocityAtBoundary), the SIMPLE
 // pressure correction (Pressure/calcp_simple.f90 with fluxes/faceflux_mass.f90
-// facefluxmass2, fluxmc2, adjustMassFlow and continuityErrors.f90) and the
-// mass-flux initialisation of init.f90.
+// facefluxmass2, fluxmc2, adjustMassFlow and continuityErrors.f90), the
+// mass-flux initialisation of init.f90 and the temperature equation
+// (ScalarEqns/temperature.f90 with fluxes/scalar_fluxes.f90 facefluxsc and
+// boundary/updateBoundary.f90).
 //
 // This translation unit is compiled with --fmad=false: the expressions below
 // are written in the reference's evaluation order and evaluate exactly as the
@@ -99,9 +101,9 @@ __device__ double face_value(const MeshView& M, int ijp, int ijn, double xf, dou
 }
 
 struct Dev {  // per-call device pointers of the fields
-  double *u, *v, *w, *p, *pp, *vis, *den, *flmass, *visw;
+  double *u, *v, *w, *p, *pp, *vis, *den, *flmass, *visw, *t;
   double *su, *sv, *sw, *spu, *spv, *sp, *apu, *apv, *apw;
-  double *gu, *gv, *gw, *gp;
+  double *gu, *gv, *gw, *gp, *gt;
   double* a;
   double* fscr;
   const int* ptype;  // FC_BC_* per patch
@@ -559,6 +561,146 @@ __global__ void k_init_flmass(MeshView M, Dev D) {
   }
 }
 
+
+// ------------------------------------------------------------ temperature
+struct ScParams {
+  double viscos, prl, prtr, sigt, pranl, gam;
+  int scheme;
+  const int* pkind;   // per patch: SC_* below
+  const int* pwall;   // per patch: iWall before its first face (isothermal walls)
+  const int* pstart;  // per patch: boundary index of its first face
+};
+enum { SC_NONE = 0, SC_FLOW = 1, SC_ISOTHERMAL = 2, SC_ADIABATIC = 3 };
+
+// facefluxsc (inner face), scalar_fluxes.f90:32-141, with the diffusion
+// coefficient of temperature.f90:122: a(k_ij)=can, a(k_ji)=cap, suadd to scratch
+__global__ void k_sc_face(MeshView M, Dev D, ScParams P) {
+  const Fld g{D.gt, M.nT};
+  const double* fi = D.t;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M.nI; i += gridDim.x * blockDim.x) {
+    const int ijp = M.owner[i], ijn = M.neighbour[i];
+    const double lambda = M.facint[i];
+    const double dcoef =
+        P.viscos * P.prl + ((D.vis[ijp] + (D.vis[ijn] - D.vis[ijp]) * lambda) - P.viscos) * P.prtr;
+    const double arx = M.arx[i], ary = M.ary[i], arz = M.arz[i], fm = D.flmass[i];
+    const double fxn = lambda, fxp = 1.0 - lambda;
+    const double xpn = M.xc[ijn] - M.xc[ijp], ypn = M.yc[ijn] - M.yc[ijp], zpn = M.zc[ijn] - M.zc[ijp];
+    const double Df = M.Df[i];
+    const double de = dcoef * Df;
+    const double ce = fmin(fm, 0.0), cp = fmax(fm, 0.0);
+    const double can = -de + ce;
+    const double cap = -de - cp;
+    double dfixi = g.x(ijp) * fxp + g.x(ijn) * fxn;
+    double dfiyi = g.y(ijp) * fxp + g.y(ijn) * fxn;
+    double dfizi = g.z(ijp) * fxp + g.z(ijn) * fxn;
+    dfixi = dfixi * (arx - Df * xpn);
+    dfiyi = dfiyi * (ary - Df * ypn);
+    dfizi = dfizi * (arz - Df * zpn);
+    const double fdfie = dcoef * (dfixi + dfiyi + dfizi);
+    double fii;
+    if (fm >= 0.0) fii = face_value(M, ijp, ijn, M.xf[i], M.yf[i], M.zf[i], fxp, fi, g, P.scheme);
+    else fii = face_value(M, ijn, ijp, M.xf[i], M.yf[i], M.zf[i], fxn, fi, g, P.scheme);
+    double fcfie = fm * fii;
+    const double fcfii = ce * fi[ijn] + cp * fi[ijp];
+    fcfie = P.gam * (fcfie - fcfii);
+    D.a[M.ijk[i]] = can;
+    D.a[M.jik[i]] = cap;
+    D.fscr[i] = -fcfie + fdfie;
+  }
+}
+
+// per cell in face order: the main-diagonal accumulation a(diag) -= can/cap
+// and su +/- suadd of the inner faces (temperature.f90:137-155), then the
+// boundary conditions of :166-225 (facefluxsc_boundary, scalar_fluxes.f90:256-337)
+__global__ void k_sc_cell(MeshView M, Dev D, ScParams P) {
+  const Fld g{D.gt, M.nT};
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
+    double ad = 0.0, su = 0.0, sp = 0.0;
+    for (int q = M.cf_ptr[c]; q < M.cf_ptr[c + 1]; ++q) {
+      const int f = M.cf_face[q];
+      if (f < M.nI) {
+        if (M.owner[f] == c) { ad = ad - D.a[M.ijk[f]]; su = su + D.fscr[f]; }
+        else { ad = ad - D.a[M.jik[f]]; su = su - D.fscr[f]; }
+        continue;
+      }
+      const int bi = f - M.nI, ijb = M.nC + bi, ijp = c, b = M.bpatch[bi];
+      const int kind = P.pkind[b];
+      if (kind == SC_FLOW) {
+        const double dcoef = P.viscos * P.prl + (D.vis[ijp] - P.viscos) / P.sigt;
+        const double arx = M.arx[f], ary = M.ary[f], arz = M.arz[f], fm = D.flmass[f];
+        const double xpn = M.xf[f] - M.xc[ijp], ypn = M.yf[f] - M.yc[ijp], zpn = M.zf[f] - M.zc[ijp];
+        const double Dfi = (arx * arx + ary * ary + arz * arz) / (xpn * arx + ypn * ary + zpn * arz);
+        const double de = dcoef * Dfi;
+        const double can = -de + fmin(fm, 0.0);
+        double dfixi = g.x(ijp), dfiyi = g.y(ijp), dfizi = g.z(ijp);
+        dfixi = dfixi * (arx - Dfi * xpn);
+        dfiyi = dfiyi * (ary - Dfi * ypn);
+        dfizi = dfizi * (arz - Dfi * zpn);
+        const double suadd = dcoef * (dfixi + dfiyi + dfizi);
+        sp = sp - can;
+        su = su - can * D.t[ijb] + suadd;
+      } else if (kind == SC_ISOTHERMAL) {
+        const int iwall = P.pwall[b] + (bi - P.pstart[b]);
+        double dcoef = P.viscos / P.pranl + (D.vis[ijp] - P.viscos) / P.sigt;
+        dcoef = dcoef * M.srdw[iwall];
+        sp = sp + dcoef;
+        su = su + dcoef * D.t[ijb];
+      } else if (kind == SC_ADIABATIC) {
+        D.t[ijb] = D.t[ijp];
+      }
+    }
+    D.a[M.diag[c]] = ad;
+    D.su[c] = su;
+    D.sp[c] = sp;
+  }
+}
+
+// updateBoundary(T), updateBoundary.f90 (no periodic pairs): outlet,
+// symmetry, pressure and empty faces take the owner's value
+__global__ void k_update_boundary(MeshView M, const int* __restrict__ ptype, double* __restrict__ phi) {
+  for (int bi = blockIdx.x * blockDim.x + threadIdx.x; bi < M.nB; bi += gridDim.x * blockDim.x) {
+    const int t = ptype[M.bpatch[bi]];
+    if (t == FC_BC_OUTLET || t == FC_BC_SYMMETRY || t == FC_BC_PRESSURE || t == FC_BC_EMPTY)
+      phi[M.nC + bi] = phi[M.owner[M.nI + bi]];
+  }
+}
+
+// min and max of phi(1:n) per block (temperature.f90:375-376)
+__global__ void k_minmax(int n, const double* __restrict__ phi, double* __restrict__ part) {
+  __shared__ double smin[32], smax[32];
+  double lo = INFINITY, hi = -INFINITY;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    lo = fmin(lo, phi[i]);
+    hi = fmax(hi, phi[i]);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if ((threadIdx.x & 31) == 0) { smin[threadIdx.x >> 5] = lo; smax[threadIdx.x >> 5] = hi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) { lo = fmin(lo, smin[w]); hi = fmax(hi, smax[w]); }
+    part[blockIdx.x] = lo;
+    part[gridDim.x + blockIdx.x] = hi;
+  }
+}
+
+// T = max(T, small) on the cells when min(T) < 0 (temperature.f90:381);
+// every block folds the per-block minima itself
+__global__ void k_clip_small(int n, double* __restrict__ phi, const double* __restrict__ part, int nb) {
+  __shared__ double s_lo;
+  if (threadIdx.x == 0) {
+    double lo = INFINITY;
+    for (int b = 0; b < nb; ++b) lo = fmin(lo, part[b]);
+    s_lo = lo;
+  }
+  __syncthreads();
+  if (!(s_lo < 0.0)) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    phi[i] = fmax(phi[i], SMALL);
+}
+
 }  // namespace
 
 // ====================================================================== host
@@ -570,7 +712,13 @@ struct SimpleState {
   int ptype_gen = -1;  // mesh generation the patch types were uploaded for
   DVec<double> part, out;
   double cumulativeContErr = 0.0;
-  double resor[5] = {0, 0, 0, 0, 0};
+  double resor[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  // temperature equation
+  fc_temperature_params tprm;
+  bool have_tprm = false;
+  int tprm_gen = -1;      // mesh generation the patch tables belong to
+  DVec<int> tpatch;       // [kind | iWall start | first boundary index] x numBoundaries
+  DVec<double> tpart;     // per-block min/max of T
 };
 
 static SimpleState& sstate(fc_ctx* ctx) {
@@ -585,7 +733,7 @@ void fc_simple_release(fc_ctx* ctx) {
 
 static inline int gridn(int n) { return std::max(1, std::min(65535, (n + 255) / 256)); }
 
-static int make_dev(fc_ctx* ctx, Dev& D) {
+static int make_dev(fc_ctx* ctx, Dev& D, bool allow_pressure = false) {
   FieldStore& F = ctx_fields(ctx);
   SimpleState& S = sstate(ctx);
   const MeshDev& m = ctx->mesh;
@@ -595,14 +743,18 @@ static int make_dev(fc_ctx* ctx, Dev& D) {
     if (m.numBoundaries)
       FC_CUDA_TRY(ctx, cudaMemcpy(S.ptype.p, m.h_bctype.data(), m.numBoundaries * sizeof(int), cudaMemcpyHostToDevice));
   }
-  for (int b = 0; b < m.numBoundaries; ++b)
-    if (m.h_bctype[b] == FC_BC_PERIODIC || m.h_bctype[b] == FC_BC_PRESSURE)
-      return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "periodic and pressure boundaries are not supported on this path");
+  for (int b = 0; b < m.numBoundaries; ++b) {
+    if (m.h_bctype[b] == FC_BC_PERIODIC)
+      return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "periodic boundaries are not supported on this path");
+    if (m.h_bctype[b] == FC_BC_PRESSURE && !allow_pressure)
+      return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "pressure boundaries are not supported on this path");
+  }
   D.u = F.u.p; D.v = F.v.p; D.w = F.w.p; D.p = F.p.p; D.pp = F.pp.p; D.vis = F.vis.p; D.den = F.den.p;
   D.flmass = F.flmass.p; D.visw = F.visw.p;
   D.su = F.su.p; D.sv = F.sv.p; D.sw = F.sw.p; D.spu = F.spu.p; D.spv = F.spv.p; D.sp = F.sp.p;
   D.apu = F.apu.p; D.apv = F.apv.p; D.apw = F.apw.p;
   D.gu = F.gu.p; D.gv = F.gv.p; D.gw = F.gw.p; D.gp = F.gp.p;
+  D.t = F.t.p; D.gt = F.gt.p;
   D.a = ctx->sys_mesh->a.p;
   D.fscr = F.fscratch.p;
   D.ptype = S.ptype.p;
@@ -809,5 +961,108 @@ extern "C" int fc_simple_iteration(fc_ctx* ctx, double* resor) {
   // divergence check of main.f90:202-207
   const double source = std::max(r[0], std::max(r[1], r[2]));
   if (!(source <= (double)1e+30f)) return fc_fail_msg(ctx, FC_ERR_NAN, "SIMPLE iterations diverge");
+  return FC_OK;
+}
+
+// ------------------------------------------------------------ temperature
+
+extern "C" int fc_temperature_set_params(fc_ctx* ctx, const fc_temperature_params* prm, const double* bc_dfraction) {
+  if (!ctx || !prm) return FC_ERR_BAD_INPUT;
+  if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
+  if (!(prm->urfT > 0) || !(prm->pranl > 0) || !(prm->sigt > 0) || prm->maxiterT < 0)
+    return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_temperature_set_params: urfT, pranl and sigt must be > 0");
+  if (prm->gradScheme < FC_GRAD_GAUSS || prm->gradScheme > FC_GRAD_LSQ_DM)
+    return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_temperature_set_params: unknown gradient scheme");
+  SimpleState& S = sstate(ctx);
+  const MeshDev& m = ctx->mesh;
+  const int nb = m.numBoundaries;
+  // patch tables: the wall counter of temperature.f90:203,236 advances on
+  // isothermal walls only, so each isothermal patch starts at the number of
+  // isothermal wall faces before it
+  std::vector<int> tab((size_t)3 * std::max(1, nb), 0);
+  int iwall = 0;
+  for (int b = 0; b < nb; ++b) {
+    const int t = m.h_bctype[b];
+    const double fr = bc_dfraction ? bc_dfraction[b] : 0.0;
+    int kind = 0;
+    if (t == FC_BC_INLET || t == FC_BC_OUTLET || t == FC_BC_PRESSURE) kind = 1;
+    else if (t == FC_BC_WALL && fr == 1.0) kind = 2;
+    else if (t == FC_BC_WALL && fr == 0.0) kind = 3;
+    tab[b] = kind;
+    tab[nb + b] = iwall;
+    tab[2 * nb + b] = m.h_startFace[b] - m.numInnerFaces;
+    if (kind == 2) iwall += m.h_nfaces[b];
+  }
+  FC_CUDA_TRY(ctx, S.tpatch.alloc(tab.size()));
+  FC_CUDA_TRY(ctx, cudaMemcpy(S.tpatch.p, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice));
+  S.tprm = *prm;
+  S.tprm.lSolverT[sizeof(S.tprm.lSolverT) - 1] = 0;
+  S.have_tprm = true;
+  S.tprm_gen = ctx->mesh_gen;
+  return FC_OK;
+}
+
+// calculate_temperature, temperature.f90:35-385 (steady; no turbulent heat
+// flux, Crank-Nicolson or periodic terms)
+extern "C" int fc_calculate_temperature(fc_ctx* ctx, int solve, double* resor7) {
+  if (!ctx) return FC_ERR_BAD_INPUT;
+  if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
+  SimpleState& S = sstate(ctx);
+  if (!S.have_tprm || S.tprm_gen != ctx->mesh_gen)
+    return fc_fail_msg(ctx, FC_ERR_STATE, "fc_temperature_set_params not called for this mesh");
+  Dev D;
+  int st = make_dev(ctx, D, true);
+  if (st) return st;
+  const fc_temperature_params& P = S.tprm;
+  MeshView M = mesh_view(ctx);
+  CsrSystem* sys = ctx->sys_mesh;
+  FieldStore& F = ctx_fields(ctx);
+  if ((st = fv_grad(ctx, P.gradScheme, D.t, D.gt))) return st;
+  ScParams sp;
+  sp.viscos = P.viscos;
+  sp.prl = 1.0 / P.pranl;
+  sp.prtr = 1. / P.sigt;
+  sp.sigt = P.sigt;
+  sp.pranl = P.pranl;
+  sp.gam = P.gdsT;
+  sp.scheme = P.cSchemeT;
+  const int nb = ctx->mesh.numBoundaries;
+  sp.pkind = S.tpatch.p;
+  sp.pwall = S.tpatch.p + nb;
+  sp.pstart = S.tpatch.p + 2 * nb;
+  FC_CUDA_TRY(ctx, cudaMemsetAsync(D.a, 0, (size_t)sys->nnz * sizeof(double), ctx->stream));
+  if (M.nI) k_sc_face<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D, sp);
+  k_sc_cell<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D, sp);
+  // main diagonal and under-relaxation (:354-365); the apx output of the
+  // shared kernel goes to scratch
+  k_mom_diag<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, sys->ia.p, sys->diag.p, D.a, D.sp, F.cscratch.p, D.su, D.su,
+                                                   D.t, P.urfT, 0);
+  ctx->kernel_launches += 2 + (M.nI > 0);
+  FC_CUDA_TRY(ctx, cudaGetLastError());
+  if (!solve) return FC_OK;
+  double r7 = 0.0;
+  st = solve_into(ctx, P.lSolverT, D.t, D.su, &r7, P.maxiterT, P.tolAbsT, P.tolRelT, "Temp");
+  if (st < 0) return st;
+  if (M.nB) {
+    k_update_boundary<<<gridn(M.nB), 256, 0, ctx->stream>>>(M, D.ptype, D.t);
+    ctx->kernel_launches++;
+  }
+  const int nbk = std::min(ctx->num_sms > 0 ? 2 * ctx->num_sms : 256, gridn(M.nC));
+  FC_CUDA_TRY(ctx, S.tpart.alloc((size_t)2 * nbk));
+  k_minmax<<<nbk, 256, 0, ctx->stream>>>(M.nC, D.t, S.tpart.p);
+  k_clip_small<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, D.t, S.tpart.p, nbk);
+  ctx->kernel_launches += 2;
+  FC_CUDA_TRY(ctx, cudaGetLastError());
+  if (ctx->verbosity) {
+    std::vector<double> h((size_t)2 * nbk);
+    FC_CUDA_TRY(ctx, cudaMemcpyAsync(h.data(), S.tpart.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+    FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    double lo = h[0], hi = h[nbk];
+    for (int b = 1; b < nbk; ++b) { lo = std::min(lo, h[b]); hi = std::max(hi, h[nbk + b]); }
+    std::printf("  %11.4E <= Temperature <= %11.4E\n", lo, hi);
+  }
+  S.resor[7] = r7;
+  if (resor7) *resor7 = r7;
   return FC_OK;
 }

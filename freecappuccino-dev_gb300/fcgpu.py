@@ -111,6 +111,8 @@ def lib():
         "fc_calcuvw": (i, [vp, vp]),
         "fc_calcp_simple": (i, [vp, vp]),
         "fc_simple_iteration": (i, [vp, vp]),
+        "fc_temperature_set_params": (i, [vp, vp, vp]),
+        "fc_calculate_temperature": (i, [vp, i, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -181,6 +183,28 @@ class SimpleParams(C.Structure):
         p.lSolverU = kw.get("solverU", "bicgstab").encode()
         p.lSolverP = kw.get("solverP", "iccg").encode()
         p.flomas = kw.get("flomas", 0.0)
+        return p
+
+
+class TemperatureParams(C.Structure):
+    """fc_temperature_params: namelist parameters of calculate_temperature."""
+    _fields_ = [("viscos", C.c_double), ("pranl", C.c_double), ("sigt", C.c_double), ("urfT", C.c_double),
+                ("gdsT", C.c_double), ("cSchemeT", C.c_int), ("gradScheme", C.c_int), ("maxiterT", C.c_int),
+                ("tolAbsT", C.c_double), ("tolRelT", C.c_double), ("lSolverT", C.c_char * 16)]
+
+    @classmethod
+    def defaults(cls, **kw):
+        """The reference's defaults (temperature.f90:14-25): urfT 0.9, gdsT 1,
+        linearUpwind, BiCGStab with maxiter 10, tolAbs 1e-13, tolRel 0.02,
+        sigt 1; pranl 0.7 (air) and viscos 0.01 unless given."""
+        p = cls()
+        p.viscos, p.pranl, p.sigt = kw.get("viscos", 0.01), kw.get("pranl", 0.7), kw.get("sigt", 1.0)
+        p.urfT, p.gdsT = kw.get("urfT", 0.9), kw.get("gdsT", 1.0)
+        p.cSchemeT = kw.get("scheme", 2)
+        p.gradScheme = kw.get("grad", 0)
+        p.maxiterT = kw.get("maxiterT", 10)
+        p.tolAbsT, p.tolRelT = kw.get("tolAbsT", 1e-13), kw.get("tolRelT", 0.02)
+        p.lSolverT = kw.get("solver", "bicgstab").encode()
         return p
 
 
@@ -513,3 +537,18 @@ class Context:
         r = np.zeros(4)
         self._check(self.L.fc_simple_iteration(self.h, _ptr(r)), "fc_simple_iteration")
         return r
+
+    # ------------------------------------------------------- temperature
+    def temperature_params(self, prm, bc_dfraction=None):
+        """prm: TemperatureParams; bc_dfraction: bcDFraction(7,:) per patch
+        (1 isothermal wall, 0 adiabatic wall) or None for all 0."""
+        self._tprm = prm
+        fr = None if bc_dfraction is None else _f64(bc_dfraction)
+        self._check(self.L.fc_temperature_set_params(self.h, C.byref(prm), _ptr(fr) if fr is not None else None),
+                    "fc_temperature_set_params")
+
+    def calculate_temperature(self, solve=True):
+        """One calculate_temperature; returns resor(7)."""
+        r = np.zeros(1)
+        self._check(self.L.fc_calculate_temperature(self.h, int(bool(solve)), _ptr(r)), "fc_calculate_temperature")
+        return float(r[0])

@@ -293,6 +293,42 @@ int fc_calcp_simple(fc_ctx* ctx, double* resor4);
  * logs them; FC_ERR_NAN when max(resor(1:3)) > 1e30 (main.f90:202-207). */
 int fc_simple_iteration(fc_ctx* ctx, double* resor);
 
+/* ---------------------------------------------------------------------------
+ * Scalar transport: the temperature equation (ScalarEqns/temperature.f90).
+ * --------------------------------------------------------------------------- */
+
+/* The namelist parameters of calculate_temperature (temperature.f90:14-25,
+ * parameters.f90:30; read_input.f90:86-88,152).  viscos and gradScheme are
+ * the global ones the reference shares with the momentum equations. */
+typedef struct {
+  double viscos;              /* molecular viscosity */
+  double pranl;               /* Prandtl number of the fluid */
+  double sigt;                /* turbulent Prandtl number (1.0 by default) */
+  double urfT, gdsT;          /* under-relaxation (0.9), deferred-correction blend (1.0) */
+  int cSchemeT;               /* FC_SCHEME_* (linearUpwind by default) */
+  int gradScheme;             /* FC_GRAD_* */
+  int maxiterT;               /* csrsolve itr_max (10) */
+  double tolAbsT, tolRelT;    /* csrsolve tolerances (1e-13, 0.02) */
+  char lSolverT[16];          /* csrsolve name ('bicgstab') */
+} fc_temperature_params;
+
+/* Sets the parameters and bcDFraction(7,1:numBoundaries) of the mesh's
+ * patches: 1.0 marks an isothermal wall (Dirichlet on T), 0.0 an adiabatic
+ * one; other values leave a wall without a temperature condition, as in the
+ * reference.  bc_dfraction may be NULL (all 0, geometry.f90:226).  Replaces
+ * the namelist read and the bcDFraction setup of field_initialization.f90. */
+int fc_temperature_set_params(fc_ctx* ctx, const fc_temperature_params* prm, const double* bc_dfraction);
+/* calculate_temperature (temperature.f90:35-385) for the steady case without
+ * turbulent heat fluxes: grad(T), the facefluxsc assembly of the matrix and
+ * sources (scalar_fluxes.f90:32-141, :256-337), the boundary conditions,
+ * under-relaxation, csrsolve(lSolverT, T, su, resor(7), ...), updateBoundary(T)
+ * and the clip to small when min(T) < 0.  With solve == 0 the call stops after
+ * the under-relaxation and leaves the system in the mesh's matrix and "su".
+ * *resor7 (may be NULL) receives resor(7).  Fields: "t", "dTdxi", "vis",
+ * "flmass"; a 'wallQFlux' patch type does not exist in the reference's mesh
+ * setup (srdw covers 'wall' patches only) and is not accepted. */
+int fc_calculate_temperature(fc_ctx* ctx, int solve, double* resor7);
+
 #ifdef __cplusplus
 }
 #endif

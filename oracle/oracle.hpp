@@ -64,6 +64,14 @@ struct Case {
   std::string lSolverU = "bicgstab", lSolverP = "iccg";
   double resor[13] = {0};
   double cumulativeContErr = 0.0;
+  // temperature transport (ScalarEqns/temperature.f90:15-25, parameters.f90:30)
+  std::vector<double> T, dTdxi;        // numTotal+1, 3*(numTotal+1)
+  std::vector<double> bcDFracT;        // bcDFraction(7,ib), 1-based per boundary
+  double pranl = 0.7, sigt = 1.0, urfT = 0.9, gdsT = 1.0;
+  int cSchemeT = 2;                    // interpolation scheme id (linearUpwind)
+  int maxiterT = 10;
+  double tolAbsT = 1e-13, tolRelT = 0.02;
+  std::string lSolverT = "bicgstab";
   double flomas = 0.0;
   int verbose = 0;
 };
@@ -123,6 +131,10 @@ void updateVelocityAtBoundary(Case& c);
 void init_flmass(Case& c);
 int calcuvw(Case& c);
 int calcp_simple(Case& c);
+// calculate_temperature (ScalarEqns/temperature.f90:35-385), steady, no
+// turbulence: assemble (a, su), solve, update boundaries, clip.  With
+// solve == false only the assembly (through the under-relaxation) is done.
+int calculate_temperature(Case& c, bool solve);
 void continuityErrors(Case& c);
 double face_value(Case& c, int ijp, int ijn, double xf, double yf, double zf, double lambda,
                   const std::vector<double>& u, std::vector<double>& dUdxi, int scheme);

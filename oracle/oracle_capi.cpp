@@ -48,6 +48,8 @@ std::vector<double>* dbl_array(Case& c, const std::string& n, int& len, int& off
   if (n == "pp") { len = c.numTotal; return &c.pp; }
   if (n == "vis") { len = c.numTotal; return &c.vis; }
   if (n == "den") { len = c.numTotal; return &c.den; }
+  if (n == "t") { len = c.numTotal; return &c.T; }
+  if (n == "dTdxi") { len = 3 * c.numTotal; offset = 3; return &c.dTdxi; }
   if (n == "flmass") { len = c.numFaces; return &c.flmass; }
   if (n == "visw") { len = c.nwal; return &c.visw; }
   if (n == "d") { len = c.numCells; return &c.d; }
@@ -152,6 +154,14 @@ int orc_case_set_param(void* h, const char* name, double val) {
   else if (n == "tolAbsP") c.tolAbsP = val;
   else if (n == "tolRelP") c.tolRelP = val;
   else if (n == "flomas") c.flomas = val;
+  else if (n == "pranl") c.pranl = val;
+  else if (n == "sigt") c.sigt = val;
+  else if (n == "urfT") c.urfT = val;
+  else if (n == "gdsT") c.gdsT = val;
+  else if (n == "cSchemeT") c.cSchemeT = (int)val;
+  else if (n == "maxiterT") c.maxiterT = (int)val;
+  else if (n == "tolAbsT") c.tolAbsT = val;
+  else if (n == "tolRelT") c.tolRelT = val;
   else return -1;
   return 0;
 }
@@ -160,7 +170,16 @@ int orc_case_set_solver(void* h, const char* which, const char* solver) {
   Case& c = *(Case*)h;
   if (std::string(which) == "U") c.lSolverU = solver;
   else if (std::string(which) == "P") c.lSolverP = solver;
+  else if (std::string(which) == "T") c.lSolverT = solver;
   else return -1;
+  return 0;
+}
+
+// bcDFraction(7, ib) of the temperature equation, ib 1-based
+int orc_case_set_bcdfrac_t(void* h, int ib, double val) {
+  Case& c = *(Case*)h;
+  if (ib < 1 || ib > c.numBoundaries) return -1;
+  c.bcDFracT[ib] = val;
   return 0;
 }
 
@@ -210,6 +229,7 @@ int orc_init_flmass(void* h) { init_flmass(*(Case*)h); return 0; }
 int orc_update_velocity_at_boundary(void* h) { updateVelocityAtBoundary(*(Case*)h); return 0; }
 int orc_calcuvw(void* h) { return calcuvw(*(Case*)h); }
 int orc_calcp_simple(void* h) { return calcp_simple(*(Case*)h); }
+int orc_calculate_temperature(void* h, int solve) { return calculate_temperature(*(Case*)h, solve != 0); }
 
 // one SIMPLE outer iteration (main.f90:159-165); resor4 gets resor(1..4);
 // elapsed_s gets the wall time of the iteration

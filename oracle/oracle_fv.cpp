@@ -754,4 +754,134 @@ int calcp_simple(Case& c) {
   return worst;
 }
 
+// ------------------------------------------------------ scalar transport
+// facefluxsc (inner face), scalar_fluxes.f90:32-141
+static void facefluxsc(Case& c, int i, int ijp, int ijn, double xf, double yf, double zf, double arx, double ary,
+                       double arz, double fm, double lambda, double gam, int scheme, const std::vector<double>& fi,
+                       std::vector<double>& dfidxi, double dcoef, double& cap, double& can, double& suadd) {
+  double fxn = lambda, fxp = 1.0 - lambda;
+  double xpn = c.xc[ijn] - c.xc[ijp], ypn = c.yc[ijn] - c.yc[ijp], zpn = c.zc[ijn] - c.zc[ijp];
+  double de = dcoef * c.Df[i];
+  double ce = std::min(fm, 0.0), cp = std::max(fm, 0.0);
+  can = -de + ce;
+  cap = -de - cp;
+  double dfixi = G(dfidxi, 1, ijp) * fxp + G(dfidxi, 1, ijn) * fxn;
+  double dfiyi = G(dfidxi, 2, ijp) * fxp + G(dfidxi, 2, ijn) * fxn;
+  double dfizi = G(dfidxi, 3, ijp) * fxp + G(dfidxi, 3, ijn) * fxn;
+  dfixi = dfixi * (arx - c.Df[i] * xpn);
+  dfiyi = dfiyi * (ary - c.Df[i] * ypn);
+  dfizi = dfizi * (arz - c.Df[i] * zpn);
+  double fdfie = dcoef * (dfixi + dfiyi + dfizi);
+  double fii;
+  if (fm >= 0.0) fii = face_value(c, ijp, ijn, xf, yf, zf, fxp, fi, dfidxi, scheme);
+  else fii = face_value(c, ijn, ijp, xf, yf, zf, fxn, fi, dfidxi, scheme);
+  double fcfie = fm * fii;
+  double fcfii = ce * fi[ijn] + cp * fi[ijp];
+  fcfie = gam * (fcfie - fcfii);
+  suadd = -fcfie + fdfie;
+}
+
+// facefluxsc_boundary, scalar_fluxes.f90:256-337
+static void facefluxsc_bnd(Case& c, int ijp, double xf, double yf, double zf, double arx, double ary, double arz,
+                           double fm, std::vector<double>& dfidxi, double dcoef, double& cap, double& can,
+                           double& suadd) {
+  double xpn = xf - c.xc[ijp], ypn = yf - c.yc[ijp], zpn = zf - c.zc[ijp];
+  double Dfi = (arx * arx + ary * ary + arz * arz) / (xpn * arx + ypn * ary + zpn * arz);
+  double de = dcoef * Dfi;
+  double ce = std::min(fm, 0.0), cp = std::max(fm, 0.0);
+  can = -de + ce;
+  cap = -de - cp;
+  double dfixi = G(dfidxi, 1, ijp), dfiyi = G(dfidxi, 2, ijp), dfizi = G(dfidxi, 3, ijp);
+  dfixi = dfixi * (arx - Dfi * xpn);
+  dfiyi = dfiyi * (ary - Dfi * ypn);
+  dfizi = dfizi * (arz - Dfi * zpn);
+  suadd = dcoef * (dfixi + dfiyi + dfizi);
+}
+
+// calculate_temperature, temperature.f90:35-385, steady and laminar-or-given
+// vis (no transient, turbulent heat-flux, Crank-Nicolson or periodic terms).
+// Isothermal walls are bcDFracT == 1, adiabatic walls bcDFracT == 0; the wall
+// counter iWall advances only on isothermal walls (:203), so srdw is indexed
+// as the reference indexes it.  Adiabatic walls copy T(ijp) to T(ijb) during
+// the assembly (:214-225).
+int calculate_temperature(Case& c, bool solve) {
+  const int nC = c.numCells;
+  const double gam = c.gdsT;
+  const double prl = 1.0 / c.pranl;
+  const double prtr = 1. / c.sigt;
+  grad(c, c.T, c.dTdxi);
+  std::fill(c.a.begin(), c.a.end(), 0.0);
+  std::fill(c.su.begin(), c.su.end(), 0.0);
+  std::fill(c.sp.begin(), c.sp.end(), 0.0);
+  for (int i = 1; i <= c.numInnerFaces; ++i) {
+    int ijp = c.owner[i], ijn = c.neighbour[i];
+    double dcoef = c.viscos * prl + ((c.vis[ijp] + (c.vis[ijn] - c.vis[ijp]) * c.facint[i]) - c.viscos) * prtr;
+    double cap, can, suadd;
+    facefluxsc(c, i, ijp, ijn, c.xf[i], c.yf[i], c.zf[i], c.arx[i], c.ary[i], c.arz[i], c.flmass[i], c.facint[i],
+               gam, c.cSchemeT, c.T, c.dTdxi, dcoef, cap, can, suadd);
+    c.a[c.ijk[i]] = can;
+    c.a[c.jik[i]] = cap;
+    c.a[c.diag[ijp]] = c.a[c.diag[ijp]] - can;
+    c.a[c.diag[ijn]] = c.a[c.diag[ijn]] - cap;
+    c.su[ijp] = c.su[ijp] + suadd;
+    c.su[ijn] = c.su[ijn] - suadd;
+  }
+  int iWall = 0;
+  for (int ib = 1; ib <= c.numBoundaries; ++ib) {
+    int t = c.bctype[ib];
+    if (t == BC_INLET || t == BC_OUTLET || t == BC_PRESSURE) {
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
+        double dcoef = c.viscos * prl + (c.vis[ijp] - c.viscos) / c.sigt;
+        double cap, can, suadd;
+        facefluxsc_bnd(c, ijp, c.xf[iface], c.yf[iface], c.zf[iface], c.arx[iface], c.ary[iface], c.arz[iface],
+                       c.flmass[iface], c.dTdxi, dcoef, cap, can, suadd);
+        c.sp[ijp] = c.sp[ijp] - can;
+        c.su[ijp] = c.su[ijp] - can * c.T[ijb] + suadd;
+      }
+    } else if (t == BC_WALL && c.bcDFracT[ib] == 1.0) {
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
+        ++iWall;
+        double dcoef = c.viscos / c.pranl + (c.vis[ijp] - c.viscos) / c.sigt;
+        dcoef = dcoef * c.srdw[iWall];
+        c.sp[ijp] = c.sp[ijp] + dcoef;
+        c.su[ijp] = c.su[ijp] + dcoef * c.T[ijb];
+        (void)iface;
+      }
+    } else if (t == BC_WALL && c.bcDFracT[ib] == 0.0) {
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
+        c.T[ijb] = c.T[ijp];
+      }
+    }
+  }
+  const double urfr = 1.0 / c.urfT, urfm = 1.0 - c.urfT;
+  for (int inp = 1; inp <= nC; ++inp) {
+    double s = 0.0;
+    for (int k = c.ia[inp]; k <= c.ia[inp + 1] - 1; ++k) s += c.a[k];
+    double off = s - c.a[c.diag[inp]];
+    c.a[c.diag[inp]] = c.sp[inp] - off;
+    c.a[c.diag[inp]] = c.a[c.diag[inp]] * urfr;
+    c.su[inp] = c.su[inp] + urfm * c.a[c.diag[inp]] * c.T[inp];
+  }
+  if (!solve) return 0;
+  SolveInfo si;
+  int st = csrsolve(c, c.lSolverT, c.T, c.su, c.resor[7], c.maxiterT, c.tolAbsT, c.tolRelT, si);
+  // updateBoundary, updateBoundary.f90 (no periodic pairs)
+  for (int ib = 1; ib <= c.numBoundaries; ++ib) {
+    int t = c.bctype[ib];
+    if (t != BC_OUTLET && t != BC_SYMMETRY && t != BC_PRESSURE && t != BC_EMPTY) continue;
+    for (int i = 1; i <= c.nfaces[ib]; ++i) {
+      int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
+      c.T[ijb] = c.T[ijp];
+    }
+  }
+  double fimin = c.T[1];
+  for (int i = 2; i <= nC; ++i) fimin = std::min(fimin, c.T[i]);
+  if (fimin < 0.0)
+    for (int i = 1; i <= nC; ++i) c.T[i] = std::max(c.T[i], kSmall);
+  return st;
+}
+
 }  // namespace orc

@@ -48,6 +48,8 @@ def lib(fast=False):
     for f in ("orc_init_flmass", "orc_update_velocity_at_boundary", "orc_calcuvw", "orc_calcp_simple"):
         getattr(L, f).argtypes = [C.c_void_p]
     L.orc_simple_iteration.argtypes = [C.c_void_p, dp, dp]
+    L.orc_case_set_bcdfrac_t.argtypes = [C.c_void_p, C.c_int, C.c_double]
+    L.orc_calculate_temperature.argtypes = [C.c_void_p, C.c_int]
     L.orc_solve.argtypes = [C.c_char_p, C.c_int, C.c_int, ip, ip, dp, ip, dp, dp, dp, C.c_int, C.c_double,
                             C.c_double, dp]
     L.orc_dic_setup.argtypes = [C.c_int, ip, ip, dp, ip, dp, C.c_int]
@@ -92,7 +94,7 @@ class Case:
     def _len(self, name):
         faces = ("arx", "ary", "arz", "xf", "yf", "zf", "flmass")
         cells = ("xc", "yc", "zc", "vol", "su", "sv", "sw", "spu", "spv", "sp", "apu", "apv", "apw", "d")
-        total = ("u", "v", "w", "p", "pp", "vis", "den")
+        total = ("u", "v", "w", "p", "pp", "vis", "den", "t")
         if name in faces:
             return self.numFaces
         if name in cells:
@@ -101,7 +103,7 @@ class Case:
             return self.numTotal
         if name in ("facint", "Df", "ijk", "jik", "neighbour"):
             return self.numInnerFaces
-        if name in ("dUdxi", "dVdxi", "dWdxi", "dPdxi"):
+        if name in ("dUdxi", "dVdxi", "dWdxi", "dPdxi", "dTdxi"):
             return 3 * self.numTotal
         if name == "Dmat":
             return 9 * self.numCells
@@ -153,6 +155,13 @@ class Case:
 
     def laplacian(self, mu, phi, mask=(1 << 64) - 1):
         self.L.orc_laplacian(self.h, _f64(mu), _f64(phi), mask)
+
+    def set_bcdfrac_t(self, ib, value):
+        """bcDFraction(7, ib) of the temperature equation (ib 1-based)."""
+        assert self.L.orc_case_set_bcdfrac_t(self.h, int(ib), float(value)) == 0
+
+    def calculate_temperature(self, solve=True):
+        return self.L.orc_calculate_temperature(self.h, 1 if solve else 0)
 
     def simple_iteration(self):
         r = np.zeros(4)

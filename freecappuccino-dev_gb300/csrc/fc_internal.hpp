@@ -81,6 +81,9 @@ struct LevelSchedule {
 };
 
 // A square CSR system on the device plus everything the solvers need.
+struct DevColoured;                  // multicolour layout of the mixed-precision inner solve (fc_mc.cu)
+void mc_release(DevColoured* m);
+
 struct CsrSystem {
   int n = 0, nnz = 0;
   DVec<int> ia, ja, diag, tslot;     // 0-based; tslot = transpose slot (DILU search)
@@ -92,6 +95,7 @@ struct CsrSystem {
   OrdStore<double> o64;
   OrdStore<float> o32;
   double est_sweep_us = 0.0;         // critical-path estimate of the forward sweep
+  DevColoured* mc = nullptr;         // built on the first FC_PREC_MIXED_COLOURED solve
   // workspace
   DVec<double> x, b, r, r0, p, u, z, v, d, w;
   DVec<float> fr, fr0, fp, fu, fz, fv, fd, fx, fy, fw;
@@ -175,6 +179,12 @@ struct SolveResult {
 
 // solve on a system; a (nnz values, NULL = s->a), x and b are device
 // vectors (x in/out).  solver: gauss-seidel|dpcg|iccg|bicgstab|pmgmres
+// FP32 inner solve of FC_PREC_MIXED_COLOURED on the multicolour layout of s
+// (fc_mc.cu): A e = r64 from e = 0, x64 += e; *itr_out iterations, *status_out
+// a device status (0 or FC_ERR_*)
+int mc_inner_solve(fc_ctx* ctx, CsrSystem* s, const double* a, const double* r64, double* x64, double tol, int itmax,
+                   bool setup, int* itr_out, int* status_out);
+int mc_colours(fc_ctx* ctx, CsrSystem* s, int* ncol);
 int sys_solve(fc_ctx* ctx, CsrSystem* s, const char* solver, const double* a, double* x, const double* b,
               int itr_max, double tol_abs, double tol_rel, SolveResult* res);
 int sys_precond(fc_ctx* ctx, CsrSystem* s, int dilu, const double* q, double* z_out, double* d_out, int apply);

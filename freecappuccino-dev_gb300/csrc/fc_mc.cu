@@ -1,0 +1,611 @@
+// FP32 inner solve of the mixed-precision path on a multicolour ordering.
+//
+// The FP64 path keeps the reference's natural-order DIC, whose triangular
+// sweeps are a long chain of dependent levels: on this GPU the sweep is bound
+// by the latency of each level, not by bytes, so running it in FP32 saves
+// little.  The inner solve of FC_PREC_MIXED_COLOURED instead colours the rows
+// (host/fc_colour.cpp), factors A by DILU in the coloured order (DIC for a
+// symmetric matrix) and applies the factors one colour at a time: every pass
+// is a data-parallel ELLPACK sweep, bound by HBM bandwidth.  The
+// preconditioner is weaker than the natural-order one (more iterations), but
+// each iteration is a handful of bandwidth-bound passes.  The refinement loop
+// around it (fc_solvers.cu) is unchanged: FP64 residual, the reference's
+// stopping test, FP64 accumulation of the corrections.
+//
+// The inner PCG runs in Eisenstat's form (S. C. Eisenstat, "Efficient
+// implementation of a class of preconditioned conjugate gradient methods",
+// SIAM J. Sci. Stat. Comput. 2 (1981) 1-4).  With the factor
+// M = (D+L) D^-1 (D+U) and A = (D+L) + (D+U) + (A_d - 2D), the operator
+// B = (D+L)^-1 A (D+U)^-1 applied to p is t + (D+L)^-1 (p + (A_d - 2D) t) with
+// t = (D+U)^-1 p: one backward and one forward sweep, no separate SpMV.  CG on
+// B (symmetric for symmetric A) with the diagonal D as preconditioner has the
+// iterates of DIC-PCG on A, mapped by x = (D+U)^-1 y and r~ = (D+L)^-1 r, so
+// an iteration reads the matrix once instead of twice.  The inner stopping test
+// is the relative reduction of the D-norm of r~; the refinement loop checks
+// the true residual.
+//
+// The inner solve is one CUDA graph per system: a prologue (the forward sweep
+// on the right-hand side, the first direction), a device-side while loop
+// whose body is one kernel per pass, and the final backward sweep x =
+// (D+U)^-1 y.  Every kernel runs at full occupancy with one thread per row;
+// the scalars of the iteration are finalised in device memory by the last
+// block of each reduction, in a fixed order, and the block that decides to
+// stop clears the loop's condition.  Dot products are summed in FP32 within
+// a warp and in FP64 across warps and blocks.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+
+#include "fc_colour.hpp"
+#include "fc_internal.hpp"
+
+#define MCG_BLOCK 512
+#define MC_UNROLL 8   // widest block whose loads are issued all at once (hex rows: 6, tets: 4)
+
+// per-colour table in device memory, MC_T entries per field: first row of
+// every colour (ncol + 1 values, multiples of 32), first entries of the lower
+// and upper blocks, widths of the lower and upper blocks
+#define MC_T (FC_MC_MAXCOL + 1)
+enum { MC_CR = 0, MC_CEL = MC_T, MC_CEU = 2 * MC_T, MC_CWL = 3 * MC_T, MC_CWU = 4 * MC_T, MC_TAB = 5 * MC_T };
+
+// scalars of one inner solve, in device memory
+struct McScal {
+  double res0, resl, rz, rzacc, pq, tol;
+  float alpha, beta;
+  int it, itmax, done, status;
+  double rz0;
+};
+
+struct DevColoured {
+  int n = 0, nP = 0, ncol = 0, maxblocks = 1;
+  std::vector<int> crow;
+  DVec<int> tab, perm, col, src, tsrc, dslot;
+  DVec<float> mval, adiag, invd, dvec, kdiag, x, r, p, q, y, t, w;
+  DVec<double> dset, part;
+  DVec<unsigned> cnt;
+  DVec<McScal> sc;
+  McScal* h_sc = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  ~DevColoured() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (h_sc) cudaFreeHost(h_sc);
+  }
+};
+
+void mc_release(DevColoured* m) { delete m; }
+
+namespace {
+
+struct McDev {
+  int nP, ncol, c0end;
+  const int* __restrict__ tab;
+  const int* __restrict__ col;
+  const int* __restrict__ src;
+  const int* __restrict__ tsrc;
+  const int* __restrict__ dslot;
+  const double* __restrict__ a;
+  float *mval, *adiag, *invd, *dvec, *kdiag;
+  double* dset;
+  float *x, *r, *p, *q, *y, *t, *w;
+  McScal* sc;
+  double* part;     // 2 * blocks of the widest launch
+  unsigned* cnt;    // arrival counter of the last-block reductions
+  cudaGraphConditionalHandle h;
+};
+
+__device__ __forceinline__ double mcg_warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ float mcg_warp_sumf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum NV values over the grid of the running kernel.  A thread's terms and
+// the warp tree are summed in FP32 (FP64 arithmetic is scarce on this part:
+// per-row FP64 accumulation cost more than the bandwidth of the pass); the
+// 16 warp sums of a block and the block partials are summed in FP64.  Each
+// block writes its fixed-order sum; the last block to arrive sums the
+// partials in block order, so the totals do not depend on arrival order.
+// Returns true in every thread of that last block, with the totals in tot.
+template <int NV>
+__device__ __forceinline__ bool mcg_reduce(const McDev& D, float (&v)[NV], double (&tot)[NV]) {
+  __shared__ double sm[NV][MCG_BLOCK / 32];
+  __shared__ double s_tot[NV];
+  __shared__ int s_last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    const float w = mcg_warp_sumf(v[j]);
+    if (lane == 0) sm[j][wid] = (double)w;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      double t = 0.0;
+      for (int w = 0; w < MCG_BLOCK / 32; ++w) t += sm[j][w];
+      D.part[j * gridDim.x + blockIdx.x] = t;
+    }
+    __threadfence();
+    s_last = atomicAdd(D.cnt, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return false;
+  __threadfence();
+  // every thread of the last block sums a strided share of the partials
+  // (independent loads in flight), then a fixed tree over the block
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    double t = 0.0;
+#pragma unroll 4
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += MCG_BLOCK) t += __ldcg(D.part + j * gridDim.x + b);
+    t = mcg_warp_sum(t);
+    if (lane == 0) sm[j][wid] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      double t = 0.0;
+      for (int w = 0; w < MCG_BLOCK / 32; ++w) t += sm[j][w];
+      s_tot[j] = t;
+    }
+    *D.cnt = 0;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < NV; ++j) tot[j] = s_tot[j];
+  return true;
+}
+
+// The scalars a kernel needs, read once per block by thread 0 and broadcast
+// through shared memory: every thread reading them from memory would send
+// one request per warp to the same L2 line, which serialises on one slice.
+struct McBcast {
+  int done;
+  float alpha, beta;
+};
+__device__ __forceinline__ McBcast mcg_scalars(const McDev& D) {
+  __shared__ McBcast s;
+  if (threadIdx.x == 0) {
+    s.done = __ldcg(&D.sc->done);
+    s.alpha = __ldcg(&D.sc->alpha);
+    s.beta = __ldcg(&D.sc->beta);
+  }
+  __syncthreads();
+  return s;
+}
+
+// stop the loop: called by the one thread that decided it
+__device__ __forceinline__ void mcg_stop(const McDev& D, int status) {
+  if (status) D.sc->status = status;
+  D.sc->done = 1;
+  cudaGraphSetConditional(D.h, 0);
+}
+
+// One row, entry k of a block at e + k * stride, all k < w (padding entries
+// hold value 0 and point at the row itself): acc + sum of mval * v[col].
+// Blocks up to MC_UNROLL wide (every hex and tet row) issue all index and
+// value loads before the gathers, so that they are in flight together; w is
+// the same for the whole colour, so no load waits on a per-row count.
+__device__ __forceinline__ float ell_sum(const McDev& D, int e, int stride, int w, const float* v, float acc) {
+  if (w <= MC_UNROLL) {
+    int c[MC_UNROLL];
+    float m[MC_UNROLL];
+#pragma unroll
+    for (int k = 0; k < MC_UNROLL; ++k)
+      if (k < w) {
+        c[k] = __ldg(D.col + e + k * stride);
+        m[k] = __ldcg(D.mval + e + k * stride);
+      }
+#pragma unroll
+    for (int k = 0; k < MC_UNROLL; ++k)
+      if (k < w) acc = fmaf(m[k], __ldcg(v + c[k]), acc);
+    return acc;
+  }
+  for (int k = 0; k < w; ++k) acc = fmaf(__ldcg(D.mval + e + k * stride), __ldcg(v + __ldg(D.col + e + k * stride)), acc);
+  return acc;
+}
+
+// r (coloured, FP32) <- r64 (original order); x, p <- 0; scalars reset
+__global__ void k_mc_gather(McDev D, const int* __restrict__ perm, const double* __restrict__ r64, double tol,
+                            int itmax) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < D.nP; i += gridDim.x * blockDim.x) {
+    const int o = perm[i];
+    D.r[i] = o >= 0 ? (float)r64[o] : 0.0f;
+    D.x[i] = 0.0f;
+    D.p[i] = 0.0f;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    McScal s;
+    s.res0 = s.resl = s.rz = s.rzacc = s.pq = s.rz0 = 0.0;
+    s.tol = tol;
+    s.alpha = s.beta = 0.0f;
+    s.it = 0; s.itmax = itmax; s.done = 0; s.status = 0;
+    *D.sc = s;
+  }
+}
+
+// x64 (original order) += x (coloured)
+__global__ void k_mc_scatter_add(int nP, const int* __restrict__ perm, const float* __restrict__ x, double* x64) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nP; i += gridDim.x * blockDim.x) {
+    const int o = perm[i];
+    if (o >= 0) x64[o] += (double)x[i];
+  }
+}
+
+// values and the coloured DILU diagonal of colour c (colours in order):
+// d_i = a_ii - sum over lower entries of a_ij a_ji / d_j, in FP64; FP32 copies
+// of d, 1/(d + small) and a_ii - 2 d
+__global__ void __launch_bounds__(MCG_BLOCK) k_mcg_setup(McDev D, int c) {
+  const int r0 = __ldg(D.tab + MC_CR + c), r1 = __ldg(D.tab + MC_CR + c + 1), stride = r1 - r0;
+  const int cel = __ldg(D.tab + MC_CEL + c), ceu = __ldg(D.tab + MC_CEU + c);
+  const int cwl = __ldg(D.tab + MC_CWL + c), cwu = __ldg(D.tab + MC_CWU + c);
+  const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= r1) return;
+  const int ds = __ldg(D.dslot + i);
+  const double aii = ds >= 0 ? __ldg(D.a + ds) : 1.0;
+  double d = aii;
+  for (int k = 0; k < cwl; ++k) {
+    const int e = cel + (i - r0) + k * stride;
+    const int sl = __ldg(D.src + e);
+    if (sl < 0) continue;
+    const double v = __ldg(D.a + sl);
+    D.mval[e] = (float)v;
+    const int ts = __ldg(D.tsrc + e);
+    const double t = ts >= 0 ? __ldg(D.a + ts) : 0.0;
+    d -= v * t / __ldcg(D.dset + __ldg(D.col + e));
+  }
+  for (int k = 0; k < cwu; ++k) {
+    const int e = ceu + (i - r0) + k * stride;
+    const int sl = __ldg(D.src + e);
+    if (sl >= 0) D.mval[e] = (float)__ldg(D.a + sl);
+  }
+  D.dset[i] = d;
+  D.dvec[i] = (float)d;
+  D.invd[i] = (float)(1.0 / (d + FC_SMALL));
+  D.kdiag[i] = (float)(aii - 2.0 * d);
+  D.adiag[i] = ds >= 0 ? (float)aii : 0.0f;
+}
+
+// colour c of (D+L) r~ = b, in place on r (lower colours already hold r~)
+__global__ void __launch_bounds__(MCG_BLOCK) k_e_fwdb(McDev D, int c) {
+  const int r0 = __ldg(D.tab + MC_CR + c), r1 = __ldg(D.tab + MC_CR + c + 1);
+  const int cel = __ldg(D.tab + MC_CEL + c), cwl = __ldg(D.tab + MC_CWL + c);
+  const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= r1) return;
+  D.r[i] = (__ldcg(D.r + i) - ell_sum(D, cel + (i - r0), r1 - r0, cwl, D.r, 0.0f)) * __ldcg(D.invd + i);
+}
+
+// z = D r~, p = z, t = p / d on the last colour; r~.z starts the iteration
+__global__ void __launch_bounds__(MCG_BLOCK) k_e_start(McDev D) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int clast = __ldg(D.tab + MC_CR + D.ncol - 1);
+  float v[1] = {0.0f};
+  if (i < D.nP) {
+    const float ri = __ldcg(D.r + i), zi = __ldcg(D.dvec + i) * ri;
+    D.y[i] = zi;
+    D.p[i] = zi;
+    if (i >= clast) D.t[i] = zi * __ldcg(D.invd + i);
+    v[0] = ri * zi;
+  }
+  double tot[1];
+  if (!mcg_reduce<1>(D, v, tot) || threadIdx.x != 0) return;
+  McScal* S = D.sc;
+  S->rz = S->rz0 = S->res0 = S->resl = tot[0];
+  if (!(tot[0] == tot[0]) || isinf(tot[0])) mcg_stop(D, FC_ERR_NAN);
+  else if (tot[0] == 0.0 || S->itmax <= 0) mcg_stop(D, 0);
+}
+
+// backward colour c (1 <= c <= C-2) of (D+U) t = p
+__global__ void __launch_bounds__(MCG_BLOCK) k_e_bwd(McDev D, int c) {
+  if (mcg_scalars(D).done) return;
+  const int r0 = __ldg(D.tab + MC_CR + c), r1 = __ldg(D.tab + MC_CR + c + 1);
+  const int ceu = __ldg(D.tab + MC_CEU + c), cwu = __ldg(D.tab + MC_CWU + c);
+  const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= r1) return;
+  D.t[i] = (__ldcg(D.p + i) - ell_sum(D, ceu + (i - r0), r1 - r0, cwu, D.t, 0.0f)) * __ldcg(D.invd + i);
+}
+
+// colour 0: the last backward colour t = (p - U t) / d and the first forward
+// colour w = (p + K t) / d (no lower entries), q = t + w, p.q
+__global__ void __launch_bounds__(MCG_BLOCK) k_e_bf0(McDev D) {
+  if (mcg_scalars(D).done) return;
+  const int r1 = __ldg(D.tab + MC_CR + 1);
+  const int ceu = __ldg(D.tab + MC_CEU), cwu = __ldg(D.tab + MC_CWU);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float v[1] = {0.0f};
+  if (i < r1) {
+    const float pi = __ldcg(D.p + i), di = __ldcg(D.invd + i), ki = __ldcg(D.kdiag + i);
+    const float ti = (pi - ell_sum(D, ceu + i, r1, cwu, D.t, 0.0f)) * di;
+    const float wi = fmaf(ki, ti, pi) * di;
+    const float qi = ti + wi;
+    D.w[i] = wi;
+    D.q[i] = qi;
+    v[0] = pi * qi;
+  }
+  double tot[1];
+  if (!mcg_reduce<1>(D, v, tot) || threadIdx.x != 0) return;
+  McScal* S = D.sc;
+  S->pq = tot[0];
+  if (D.ncol == 1) {
+    const double alpha = S->rz / tot[0];
+    if (!(alpha == alpha) || isinf(alpha)) mcg_stop(D, FC_ERR_BREAKDOWN);
+    else S->alpha = (float)alpha;
+  }
+}
+
+// forward colour c >= 1: w = (p + K t - L w) / d, q = t + w, p.q; the last
+// colour closes p.q and sets alpha
+__global__ void __launch_bounds__(MCG_BLOCK) k_e_fwd(McDev D, int c) {
+  if (mcg_scalars(D).done) return;
+  const int r0 = __ldg(D.tab + MC_CR + c), r1 = __ldg(D.tab + MC_CR + c + 1);
+  const int cel = __ldg(D.tab + MC_CEL + c), cwl = __ldg(D.tab + MC_CWL + c);
+  const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+  float v[1] = {0.0f};
+  if (i < r1) {
+    const float pi = __ldcg(D.p + i), di = __ldcg(D.invd + i), ki = __ldcg(D.kdiag + i), ti = __ldcg(D.t + i);
+    const float wi = (fmaf(ki, ti, pi) - ell_sum(D, cel + (i - r0), r1 - r0, cwl, D.w, 0.0f)) * di;
+    const float qi = ti + wi;
+    D.w[i] = wi;
+    D.q[i] = qi;
+    v[0] = pi * qi;
+  }
+  double tot[1];
+  if (!mcg_reduce<1>(D, v, tot) || threadIdx.x != 0) return;
+  McScal* S = D.sc;
+  S->pq += tot[0];
+  if (c == D.ncol - 1) {
+    const double alpha = S->rz / S->pq;
+    if (!(alpha == alpha) || isinf(alpha)) mcg_stop(D, FC_ERR_BREAKDOWN);
+    else S->alpha = (float)alpha;
+  }
+}
+
+// y += alpha p, r~ -= alpha q, z = D r~, r~.z; the stopping test on the
+// D-norm of r~ (relative to the start) or the iteration limit; beta
+__global__ void __launch_bounds__(MCG_BLOCK) k_e_upd(McDev D) {
+  const McBcast sc = mcg_scalars(D);
+  if (sc.done) return;
+  const int i4 = blockIdx.x * blockDim.x + threadIdx.x;
+  const float alpha = sc.alpha;
+  float v[1] = {0.0f};
+  if (i4 < (D.nP >> 2)) {
+    const float4 x4 = __ldcg((const float4*)D.x + i4), p4 = __ldcg((const float4*)D.p + i4);
+    const float4 q4 = __ldcg((const float4*)D.q + i4), r4 = __ldcg((const float4*)D.r + i4);
+    const float4 d4 = __ldcg((const float4*)D.dvec + i4);
+    const float4 rn = make_float4(fmaf(-alpha, q4.x, r4.x), fmaf(-alpha, q4.y, r4.y), fmaf(-alpha, q4.z, r4.z),
+                                  fmaf(-alpha, q4.w, r4.w));
+    const float4 zn = make_float4(d4.x * rn.x, d4.y * rn.y, d4.z * rn.z, d4.w * rn.w);
+    ((float4*)D.x)[i4] = make_float4(fmaf(alpha, p4.x, x4.x), fmaf(alpha, p4.y, x4.y), fmaf(alpha, p4.z, x4.z),
+                                     fmaf(alpha, p4.w, x4.w));
+    ((float4*)D.r)[i4] = rn;
+    ((float4*)D.y)[i4] = zn;
+    v[0] = (rn.x * zn.x + rn.y * zn.y) + (rn.z * zn.z + rn.w * zn.w);
+  }
+  double tot[1];
+  if (!mcg_reduce<1>(D, v, tot) || threadIdx.x != 0) return;
+  McScal* S = D.sc;
+  S->it += 1;
+  S->resl = tot[0];
+  if (!(tot[0] == tot[0]) || isinf(tot[0])) { mcg_stop(D, FC_ERR_NAN); return; }
+  // r~.z keeps the sign of A (negative for the reference's pressure matrix)
+  if (fabs(tot[0]) <= S->tol * S->tol * fabs(S->rz0) || S->it >= S->itmax) { mcg_stop(D, 0); return; }
+  S->beta = (float)(tot[0] / S->rz);
+  S->rz = tot[0];
+}
+
+// p = z + beta p; t = p / d on the last colour (the first backward colour)
+__global__ void __launch_bounds__(MCG_BLOCK) k_e_pupd(McDev D) {
+  const McBcast sc = mcg_scalars(D);
+  if (sc.done) return;
+  const int i4 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i4 >= (D.nP >> 2)) return;
+  const float beta = sc.beta;
+  const float4 z4 = __ldcg((const float4*)D.y + i4), p4 = __ldcg((const float4*)D.p + i4);
+  const float4 pn = make_float4(fmaf(beta, p4.x, z4.x), fmaf(beta, p4.y, z4.y), fmaf(beta, p4.z, z4.z),
+                                fmaf(beta, p4.w, z4.w));
+  ((float4*)D.p)[i4] = pn;
+  if (4 * i4 >= __ldg(D.tab + MC_CR + D.ncol - 1)) {  // colour boundaries are multiples of 32 rows
+    const float4 d4 = __ldcg((const float4*)D.invd + i4);
+    ((float4*)D.t)[i4] = make_float4(pn.x * d4.x, pn.y * d4.y, pn.z * d4.z, pn.w * d4.w);
+  }
+}
+
+// colour c of x = (D+U)^-1 y, in place on x (higher colours already hold x)
+__global__ void __launch_bounds__(MCG_BLOCK) k_e_xb(McDev D, int c) {
+  const int r0 = __ldg(D.tab + MC_CR + c), r1 = __ldg(D.tab + MC_CR + c + 1);
+  const int ceu = __ldg(D.tab + MC_CEU + c), cwu = __ldg(D.tab + MC_CWU + c);
+  const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= r1) return;
+  D.x[i] = (__ldcg(D.x + i) - ell_sum(D, ceu + (i - r0), r1 - r0, cwu, D.x, 0.0f)) * __ldcg(D.invd + i);
+}
+
+}  // namespace
+
+static McDev mc_dev(DevColoured& m, const double* a) {
+  McDev D;
+  D.nP = m.nP; D.ncol = m.ncol; D.c0end = m.crow[1];
+  D.tab = m.tab.p; D.col = m.col.p; D.src = m.src.p; D.tsrc = m.tsrc.p; D.dslot = m.dslot.p; D.a = a;
+  D.mval = m.mval.p; D.adiag = m.adiag.p; D.invd = m.invd.p; D.dvec = m.dvec.p; D.kdiag = m.kdiag.p;
+  D.dset = m.dset.p;
+  D.x = m.x.p; D.r = m.r.p; D.p = m.p.p; D.q = m.q.p; D.y = m.y.p; D.t = m.t.p; D.w = m.w.p;
+  D.sc = m.sc.p; D.part = m.part.p; D.cnt = m.cnt.p;
+  D.h = 0;
+  return D;
+}
+
+static inline unsigned mc_blocks(int rows) { return (unsigned)std::max(1, (rows + MCG_BLOCK - 1) / MCG_BLOCK); }
+
+// The inner PCG graph: prologue (init, first preconditioner application) and
+// a while node whose body is one iteration.  The kernels' arguments are fixed
+// (the system's own buffers); tolerance and iteration limit are read from the
+// scalar block, which k_mc_gather resets before every launch.
+static int mc_build_graph(fc_ctx* ctx, DevColoured& m) {
+  cudaGraph_t g = nullptr;
+  FC_CUDA_TRY(ctx, cudaGraphCreate(&g, 0));
+  m.graph = g;
+  cudaGraphConditionalHandle h;
+  FC_CUDA_TRY(ctx, cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+  McDev D = mc_dev(m, nullptr);
+  D.h = h;
+  const int C = m.ncol;
+  // kernel nodes copy their arguments at creation, so the locals below may go
+  int cs[FC_MC_MAXCOL];
+  for (int c = 0; c < C; ++c) cs[c] = c;
+  auto add = [&](cudaGraph_t gr, cudaGraphNode_t& prev, bool have_prev, const void* fn, unsigned blocks,
+                 void** args) -> int {
+    cudaKernelNodeParams kp = {};
+    kp.func = const_cast<void*>(fn);
+    kp.gridDim = dim3(blocks);
+    kp.blockDim = dim3(MCG_BLOCK);
+    kp.sharedMemBytes = 0;
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    cudaGraphNode_t n;
+    FC_CUDA_TRY(ctx, cudaGraphAddKernelNode(&n, gr, have_prev ? &prev : nullptr, have_prev ? 1 : 0, &kp));
+    prev = n;
+    return FC_OK;
+  };
+  auto blocks_of = [&](int c) { return mc_blocks(m.crow[c + 1] - m.crow[c]); };
+  int st;
+  cudaGraphNode_t prev = nullptr;
+  void* a1[1] = {&D};
+  // prologue: (D+L) r~ = b colour by colour, then z, p, t and r~.z
+  for (int c = 0; c < C; ++c) {
+    void* args[2] = {&D, &cs[c]};
+    if ((st = add(g, prev, c > 0, (const void*)k_e_fwdb, blocks_of(c), args))) return st;
+  }
+  if ((st = add(g, prev, true, (const void*)k_e_start, mc_blocks(m.nP), a1))) return st;
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t loop;
+  FC_CUDA_TRY(ctx, cudaGraphAddNode(&loop, g, &prev, nullptr, 1, &cp));
+  // body: backward colours C-2..1, colour 0 (backward + forward), forward
+  // colours 1..C-1, the x/r update with the stopping test, the new direction
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  cudaGraphNode_t bp = nullptr;
+  bool have = false;
+  for (int c = C - 2; c >= 1; --c) {
+    void* args[2] = {&D, &cs[c]};
+    if ((st = add(body, bp, have, (const void*)k_e_bwd, blocks_of(c), args))) return st;
+    have = true;
+  }
+  if ((st = add(body, bp, have, (const void*)k_e_bf0, blocks_of(0), a1))) return st;
+  for (int c = 1; c < C; ++c) {
+    void* args[2] = {&D, &cs[c]};
+    if ((st = add(body, bp, true, (const void*)k_e_fwd, blocks_of(c), args))) return st;
+  }
+  if ((st = add(body, bp, true, (const void*)k_e_upd, mc_blocks(m.nP / 4), a1))) return st;
+  if ((st = add(body, bp, true, (const void*)k_e_pupd, mc_blocks(m.nP / 4), a1))) return st;
+  // after the loop: x = (D+U)^-1 y, colours C-1..0
+  prev = loop;
+  for (int c = C - 1; c >= 0; --c) {
+    void* args[2] = {&D, &cs[c]};
+    if ((st = add(g, prev, true, (const void*)k_e_xb, blocks_of(c), args))) return st;
+  }
+  FC_CUDA_TRY(ctx, cudaGraphInstantiate(&m.exec, g, 0));
+  return FC_OK;
+}
+
+static int mc_prepare(fc_ctx* ctx, CsrSystem* s) {
+  if (s->mc) return FC_OK;
+  ColouredLayout L;
+  std::string why;
+  if (!build_coloured(s->n, s->h_ia.data(), s->h_ja.data(), s->h_diag.data(), L, &why))
+    return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "multicolour layout: " + why);
+  DevColoured* m = new DevColoured();
+  m->n = L.n; m->nP = L.nP; m->ncol = L.ncol;
+  m->crow.resize(L.ncol + 1);
+  for (int c = 0; c <= L.ncol; ++c) m->crow[c] = L.cslice[c] * FC_MC_SLICE;
+  std::vector<int> tab(MC_TAB, 0);
+  for (int c = 0; c <= FC_MC_MAXCOL; ++c) tab[MC_CR + c] = c <= L.ncol ? m->crow[c] : L.nP;
+  for (int c = 0; c < L.ncol; ++c) {
+    tab[MC_CEL + c] = (int)L.cel[c];
+    tab[MC_CEU + c] = (int)L.ceu[c];
+    tab[MC_CWL + c] = L.cwl[c];
+    tab[MC_CWU + c] = L.cwu[c];
+  }
+  auto up = [&](DVec<int>& d, const std::vector<int>& h) -> int {
+    FC_CUDA_TRY(ctx, d.alloc(std::max<size_t>(1, h.size())));
+    if (!h.empty()) FC_CUDA_TRY(ctx, cudaMemcpy(d.p, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
+    return FC_OK;
+  };
+  int st = 0;
+  if ((st = up(m->tab, tab)) || (st = up(m->perm, L.perm)) || (st = up(m->col, L.col)) || (st = up(m->src, L.src)) ||
+      (st = up(m->tsrc, L.tsrc)) || (st = up(m->dslot, L.dslot))) {
+    delete m;
+    return st;
+  }
+  const size_t nP = std::max(1, L.nP), ne = std::max<size_t>(1, (size_t)L.nent);
+  m->maxblocks = (int)mc_blocks(L.nP);
+  DVec<float>* fv[] = {&m->adiag, &m->invd, &m->dvec, &m->kdiag, &m->x, &m->r, &m->p, &m->q, &m->y, &m->t, &m->w};
+  bool ok = true;
+  for (auto* v : fv) ok = ok && v->alloc(nP) == cudaSuccess;
+  ok = ok && m->mval.alloc(ne) == cudaSuccess && m->dset.alloc(nP) == cudaSuccess &&
+       m->part.alloc((size_t)2 * m->maxblocks) == cudaSuccess && m->cnt.alloc(1) == cudaSuccess &&
+       m->sc.alloc(1) == cudaSuccess && cudaMallocHost(&m->h_sc, sizeof(McScal)) == cudaSuccess;
+  if (!ok) {
+    delete m;
+    return fc_fail_msg(ctx, FC_ERR_NOMEM, "multicolour buffers");
+  }
+  // padding entries keep the value 0 (the setup writes real entries only)
+  FC_CUDA_TRY(ctx, cudaMemset(m->mval.p, 0, ne * sizeof(float)));
+  FC_CUDA_TRY(ctx, cudaMemset(m->cnt.p, 0, sizeof(unsigned)));
+  if ((st = mc_build_graph(ctx, *m))) {
+    delete m;
+    return st;
+  }
+  s->mc = m;
+  return FC_OK;
+}
+
+int mc_colours(fc_ctx* ctx, CsrSystem* s, int* ncol) {
+  int st = mc_prepare(ctx, s);
+  if (st) return st;
+  *ncol = s->mc->ncol;
+  return FC_OK;
+}
+
+// One FP32 inner solve A e = r64 from e = 0 to the relative L1 reduction
+// tol, at most itmax iterations; x64 += e.  setup: refresh the FP32 values and
+// the DILU diagonal from a (the first inner solve of a refinement loop).
+int mc_inner_solve(fc_ctx* ctx, CsrSystem* s, const double* a, const double* r64, double* x64, double tol, int itmax,
+                   bool setup, int* itr_out, int* status_out) {
+  int st = mc_prepare(ctx, s);
+  if (st) return st;
+  DevColoured& m = *s->mc;
+  McDev D = mc_dev(m, a);
+  const unsigned eb = std::min(8192u, mc_blocks(m.nP));
+  k_mc_gather<<<eb, MCG_BLOCK, 0, ctx->stream>>>(D, m.perm.p, r64, tol, itmax);
+  ctx->kernel_launches++;
+  if (setup) {
+    for (int c = 0; c < m.ncol; ++c) {
+      k_mcg_setup<<<mc_blocks(m.crow[c + 1] - m.crow[c]), MCG_BLOCK, 0, ctx->stream>>>(D, c);
+      ctx->kernel_launches++;
+    }
+  }
+  FC_CUDA_TRY(ctx, cudaGetLastError());
+  FC_CUDA_TRY(ctx, cudaGraphLaunch(m.exec, ctx->stream));
+  k_mc_scatter_add<<<eb, MCG_BLOCK, 0, ctx->stream>>>(m.nP, m.perm.p, m.x.p, x64);
+  FC_CUDA_TRY(ctx, cudaMemcpyAsync(m.h_sc, m.sc.p, sizeof(McScal), cudaMemcpyDeviceToHost, ctx->stream));
+  FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  // graph kernels: prologue C + 1, per iteration 2 C (the last one may stop
+  // early), the final backward sweep C
+  ctx->kernel_launches += 2LL * m.ncol + 1 + (long long)m.h_sc->it * 2 * m.ncol;
+  *itr_out = m.h_sc->it;
+  *status_out = m.h_sc->status;
+  return FC_OK;
+}

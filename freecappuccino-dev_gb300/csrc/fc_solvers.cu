@@ -478,6 +478,7 @@ bool is_device_ptr(const void* p) {
 }
 
 CsrSystem::~CsrSystem() {
+  mc_release(mc);
   if (h_out) cudaFreeHost(h_out);
   if (h_status) cudaFreeHost(h_status);
 }
@@ -582,6 +583,8 @@ int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, c
                     const double* xyz) {
   if (n <= 0 || nnz < n) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "csr pattern: n <= 0 or nnz < n");
   if (nnz >= (1 << 27)) return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "csr pattern: nnz >= 2^27");
+  mc_release(s->mc);  // the multicolour layout belongs to the previous pattern
+  s->mc = nullptr;
   std::vector<int> ia(n + 1), ja(nnz), dg(n);
   // the caller's arrays may live on the host or the device
   auto fetch = [&](const int* src, int* dst, size_t cnt) -> int {
@@ -865,12 +868,17 @@ static int solve_mixed(fc_ctx* ctx, CsrSystem* s, const std::string& solver, con
     return solve_fp64(ctx, s, solver, a, x, b, itr_max, tol_abs, tol_rel, res);
   if (solver == "bicgstab" && s->tslot_oob)
     return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "bicgstab: pattern is not structurally symmetric");
+  // FC_PREC_MIXED_COLOURED: the ICCG inner solve runs on the multicolour
+  // ordering (fc_mc.cu); the other solvers keep the ordered FP32 kernels
+  const bool coloured = ctx->precision == FC_PREC_MIXED_COLOURED && solver == "iccg";
   int st = alloc_work32(ctx, s);
   if (st) return st;
   const int n = s->n;
   const int eb = std::min(4096, (n + 255) / 256);
-  k_to_float<<<std::min(8192, (s->nnz + 255) / 256), 256, 0, ctx->stream>>>(a, s->a32.p, s->nnz);
-  ctx->kernel_launches++;
+  if (!coloured) {
+    k_to_float<<<std::min(8192, (s->nnz + 255) / 256), 256, 0, ctx->stream>>>(a, s->a32.p, s->nnz);
+    ctx->kernel_launches++;
+  }
   KArgs<double> R = make_args<double>(s, a, x, b, s->r.p, s->r0.p, s->p.p, s->u.p, s->z.p, s->v.p, s->d.p,
                                       s->w.p, 0, tol_abs, tol_rel);
   const double inner_tol = ctx->inner_tol > 0 ? ctx->inner_tol : 1e-4;
@@ -899,6 +907,20 @@ static int solve_mixed(fc_ctx* ctx, CsrSystem* s, const std::string& solver, con
       if (rsm < tol_rel || resl < tol_abs) break;
     }
     if (outer >= max_outer || total_itr >= itr_max) { res->status = FC_WARN_MAXITER; break; }
+    if (coloured) {
+      // the last refinement step only needs the reduction that is left to
+      // the stopping test (with a factor 4 of margin)
+      const double left = 0.25 * tol_rel * (res0 + FC_SMALL) / resl;
+      const double tol_k = std::min(1e-1, std::max(inner_tol, left));
+      int itr = 0, stat = 0;
+      st = mc_inner_solve(ctx, s, a, s->r.p, x, tol_k, std::min(inner_itmax, itr_max - total_itr), outer == 0,
+                          &itr, &stat);
+      if (st) return st;
+      if (stat) { res->status = stat; return FC_OK; }
+      total_itr += itr;
+      ++outer;
+      continue;
+    }
     // inner FP32 solve of A dx = r from dx = 0
     k_to_float<<<eb, 256, 0, ctx->stream>>>(s->r.p, s->fr0.p, n);
     k_zero_float<<<eb, 256, 0, ctx->stream>>>(s->fx.p, n);
@@ -937,7 +959,7 @@ int sys_solve(fc_ctx* ctx, CsrSystem* s, const char* solver_c, const double* a, 
   int st;
   if (solver == "pmgmres") {
     st = gmres_solve(ctx, s, a, x, b, itr_max, 4, tol_abs, tol_rel, res);
-  } else if (ctx->precision == 1) {
+  } else if (ctx->precision != FC_PREC_FP64) {
     st = solve_mixed(ctx, s, solver, a, x, b, itr_max, tol_abs, tol_rel, res);
   } else {
     st = solve_fp64(ctx, s, solver, a, x, b, itr_max, tol_abs, tol_rel, res);

@@ -30,6 +30,7 @@ FC_ERR_ZERO_PIVOT = -8
 BC = {"wall": 1, "inlet": 2, "outlet": 3, "symmetry": 4, "pressure": 5, "empty": 6, "periodic": 7}
 FC_PREC_FP64 = 0
 FC_PREC_MIXED = 1
+FC_PREC_MIXED_COLOURED = 2
 FC_NOALLOC_MAX_N = 1 << 20  # rows of fc_dpcg_noalloc's static scratch
 GRAD = {"gauss": 0, "lstsq": 1, "lstsq_dm": 2}
 NOMAX = 6

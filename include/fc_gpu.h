@@ -96,13 +96,19 @@ typedef struct fc_ctx fc_ctx;
 
 #define FC_PREC_FP64   0   /* everything in FP64, as the reference */
 #define FC_PREC_MIXED  1   /* FP32 matrix/preconditioner/Krylov vectors inside FP64 iterative refinement */
+/* as FC_PREC_MIXED, but the ICCG inner solve runs on a multicolour ordering of
+ * the rows: its DIC factor is built and applied one colour at a time
+ * (bandwidth-bound passes instead of the natural order's long chain of
+ * levels).  The preconditioner differs from the reference's, the stopping
+ * test and the FP64 refinement do not; other solvers behave as FC_PREC_MIXED. */
+#define FC_PREC_MIXED_COLOURED 2
 
 int fc_init(int device, fc_ctx** out);
 void fc_finalize(fc_ctx* ctx);
 const char* fc_last_error(const fc_ctx* ctx);
 /* level 1: print the reference's solver report line after every solve */
 int fc_set_verbosity(fc_ctx* ctx, int level);
-/* FC_PREC_MIXED: inner FP32 solves to the relative tolerance inner_tol
+/* FC_PREC_MIXED(_COLOURED): inner FP32 solves to the relative tolerance inner_tol
  * (<=0: 1e-4), at most inner_itmax iterations each (<=0: itr_max); the
  * refinement loop stops on the reference's criterion in FP64. */
 int fc_set_precision(fc_ctx* ctx, int mode, double inner_tol, int inner_itmax);

@@ -145,6 +145,35 @@ def test_mixed_precision_reaches_fp64_tolerance(ctx, oracle):
     assert np.abs(x - xo).max() <= 1e-7 * np.abs(xo).max()
 
 
+@pytest.mark.parametrize("case", ["hex", "tet"])
+def test_mixed_coloured_reaches_fp64_tolerance(ctx, oracle, fc, case):
+    """FC_PREC_MIXED_COLOURED: the FP32 inner ICCG runs on the multicolour
+    ordering (2 colours on hexes, more on tets); the FP64 refinement still
+    stops on the reference's criterion, so the answer is the FP64 one."""
+    if case == "hex":
+        m, a, oc = mesh_case("hexm", 14, 12, 10)
+    else:
+        m, a, oc = mesh_case("tetm", 7, 6, 5, tets=True)
+    ia, ja, av, dg, b = laplacian_system(oc, mask=0b1)
+    xo, _, _, _ = oracle.solve("iccg", ia, ja, av, dg, np.zeros(len(dg)), b, 5000, 0.0, 1e-10)
+    ctx.set_precision(fc.FC_PREC_MIXED_COLOURED, 1e-5, 0)
+    try:
+        x, _, info, st = ctx.csrsolve("iccg", ia, ja, av, dg, np.zeros(len(dg)), b, 5000, 0.0, 1e-10)
+        # same pattern, new values: the colour-ordered factor is rebuilt
+        av2 = av * 1.7
+        av2[dg - 1] += 0.05
+        x2, _, info2, st2 = ctx.csrsolve("iccg", ia, ja, av2, dg, np.zeros(len(dg)), b, 5000, 0.0, 1e-10)
+    finally:
+        ctx.set_precision(0)
+    assert st == 0 and info.outer_iterations >= 2
+    r = b - oracle.spmv(ia, ja, av, x)
+    assert np.abs(r).sum() / info.res0_l1 < 1e-10
+    assert np.abs(x - xo).max() <= 1e-7 * np.abs(xo).max()
+    assert st2 == 0
+    r2 = b - oracle.spmv(ia, ja, av2, x2)
+    assert np.abs(r2).sum() / info2.res0_l1 < 1e-10
+
+
 def test_failure_detection_nan_rhs(ctx, fc):
     m, a, oc = mesh_case("hex", 9, 7, 6)
     ia, ja, av, dg, b = laplacian_system(oc, mask=0b1)

@@ -38,10 +38,12 @@ L2_BYTES = 129 * 1024 * 1024  # GB300 L2
 # (the same counts as the GPU solver's): the CPU arms time a bounded sample of
 # iterations and scale it to a full solve
 ITERS_PER_SOLVE = {32: 95, 64: 182, 128: 358}
-# relative tolerance of each FP32 inner solve of the mixed-precision run: two
-# refinement steps reach 1e-10 at 64^3 and 128^3 (1e-4 needs three, and the
-# restarts cost more inner iterations than the tighter inner solves)
-MIXED_INNER_TOL = 1e-6
+# relative tolerance of each FP32 inner solve of the mixed-precision runs.
+# Multicolour inner ICCG (FC_PREC_MIXED_COLOURED): 1e-5, three refinement steps
+# to 1e-10 at 128^3 (the last one only to the reduction still missing).
+# Natural-order inner ICCG (FC_PREC_MIXED): 1e-6, two refinement steps.
+MIXED_INNER_TOL = 1e-5
+MIXED_NATURAL_INNER_TOL = 1e-6
 
 
 def load_fc():
@@ -232,8 +234,8 @@ def simple_block(fc, args, dev, with_cpu):
 
     out = {"workload": f"{n}^3 lid-driven cavity, Re=100, SIMPLE (central/DC, Gauss, BiCGStab U, ICCG p)",
            "cells": nC, "unit": "SIMPLE iters/s"}
-    for mode, key in ((fc.FC_PREC_FP64, "value"), (fc.FC_PREC_MIXED, "mixed")):
-        ctx.set_precision(mode, 1e-4, 0) if mode else ctx.set_precision(mode)
+    for mode, key in ((fc.FC_PREC_FP64, "value"), (fc.FC_PREC_MIXED_COLOURED, "mixed")):
+        ctx.set_precision(mode, MIXED_INNER_TOL, 0) if mode else ctx.set_precision(mode)
         reset()
         for _ in range(args.simple_skip):
             ctx.simple_iteration()
@@ -352,21 +354,33 @@ def run_gpu(args, rank, world, dist):
     h2d = a_h.nbytes + b_h.nbytes + x_h.nbytes
     d2h = x_h.nbytes
 
-    # mixed precision (FP32 inner, FP64 refinement) to the same criterion
-    ctx.set_precision(fc.FC_PREC_MIXED, MIXED_INNER_TOL, 0)
-    for _ in range(max(1, args.warmup)):
-        minfo = step()
-    ctx.sync()
-    ctx.event(0)
-    for _ in range(args.steps):
-        minfo = step()
-    ctx.event(1)
-    mixed_ms = ctx.elapsed_ms() / args.steps
+    # mixed precision (FP32 inner, FP64 refinement) to the same criterion:
+    # the multicolour inner ICCG, and the natural-order one for comparison
     ctx.set_precision(fc.FC_PREC_FP64)
-    x_mixed = ctx.field_get("pp")[:nC].copy()
     step()
     x_fp64 = ctx.field_get("pp")[:nC].copy()
-    mixed_err = float(np.abs(x_mixed - x_fp64).max() / np.abs(x_fp64).max())
+
+    def mixed_run(mode, inner_tol):
+        ctx.set_precision(mode, inner_tol, 0)
+        for _ in range(max(1, args.warmup)):
+            mi = step()
+        ctx.sync()
+        ctx.event(0)
+        for _ in range(args.steps):
+            mi = step()
+        ctx.event(1)
+        ms = ctx.elapsed_ms() / args.steps
+        ctx.set_precision(fc.FC_PREC_FP64)
+        err = float(np.abs(ctx.field_get("pp")[:nC] - x_fp64).max() / np.abs(x_fp64).max())
+        return {"value": 1e3 / ms, "unit": "p-solves/s", "ms_per_step": ms, "speedup_vs_fp64": ms_per_step / ms,
+                "inner_iterations": mi.itr_used, "outer_iterations": mi.outer_iterations, "inner_tol": inner_tol,
+                "max_rel_diff_vs_fp64": err}
+
+    mixed = mixed_run(fc.FC_PREC_MIXED_COLOURED, MIXED_INNER_TOL)
+    mixed["inner_solver"] = ("FP32 ICCG, multicolour DIC (%d colours) in Eisenstat form, one CUDA graph"
+                             % ctx.mixed_colours(0))
+    mixed_nat = mixed_run(fc.FC_PREC_MIXED, MIXED_NATURAL_INNER_TOL)
+    mixed_nat["inner_solver"] = "FP32 ICCG, natural-order DIC (the FP64 path's sweeps)"
 
     sweep = ctx.sweep_stats(0)
     peak, peak_kind = measured_peak()
@@ -398,9 +412,7 @@ def run_gpu(args, rank, world, dist):
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
-            "mixed": {"value": 1e3 / mixed_ms, "unit": "p-solves/s", "ms_per_step": mixed_ms,
-                      "speedup_vs_fp64": ms_per_step / mixed_ms, "inner_iterations": minfo.itr_used,
-                      "outer_iterations": minfo.outer_iterations, "max_rel_diff_vs_fp64": mixed_err}}
+            "mixed": mixed, "mixed_natural_order": mixed_nat}
     ctx.close()
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(ia, ja, a_host, dg, b, iters, args.ref_sample)

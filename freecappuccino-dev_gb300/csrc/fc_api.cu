@@ -317,6 +317,13 @@ int solve_global(fc_ctx* ctx, const char* solver, double* x, const double* b, do
 // tile, ring depth, estimated forward sweep microseconds, ring-served
 // entries, pushed entries, cross-tile entries (both triangles), stage depth,
 // most steps of a tile.
+extern "C" int fc_mixed_colours(fc_ctx* ctx, int which, int* ncol) {
+  if (!ctx || !ncol) return FC_ERR_BAD_INPUT;
+  CsrSystem* s = which ? ctx->sys_ext : ctx->sys_mesh;
+  if (!s) return fc_fail_msg(ctx, FC_ERR_STATE, "no such system");
+  return mc_colours(ctx, s, ncol);
+}
+
 extern "C" int fc_sweep_stats(fc_ctx* ctx, int which, double* out) {
   if (!ctx || !out) return FC_ERR_BAD_INPUT;
   CsrSystem* s = which ? ctx->sys_ext : ctx->sys_mesh;

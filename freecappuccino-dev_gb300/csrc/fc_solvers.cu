@@ -866,11 +866,14 @@ static int solve_mixed(fc_ctx* ctx, CsrSystem* s, const std::string& solver, con
                        const double* b, int itr_max, double tol_abs, double tol_rel, SolveResult* res) {
   if (solver != "iccg" && solver != "bicgstab" && solver != "dpcg")
     return solve_fp64(ctx, s, solver, a, x, b, itr_max, tol_abs, tol_rel, res);
+  // FC_PREC_MIXED_COLOURED mixes the ICCG solves only; the others stay FP64
+  if (ctx->precision == FC_PREC_MIXED_COLOURED && solver != "iccg")
+    return solve_fp64(ctx, s, solver, a, x, b, itr_max, tol_abs, tol_rel, res);
   if (solver == "bicgstab" && s->tslot_oob)
     return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "bicgstab: pattern is not structurally symmetric");
   // FC_PREC_MIXED_COLOURED: the ICCG inner solve runs on the multicolour
-  // ordering (fc_mc.cu); the other solvers keep the ordered FP32 kernels
-  const bool coloured = ctx->precision == FC_PREC_MIXED_COLOURED && solver == "iccg";
+  // ordering (fc_mc.cu)
+  const bool coloured = ctx->precision == FC_PREC_MIXED_COLOURED;
   int st = alloc_work32(ctx, s);
   if (st) return st;
   const int n = s->n;

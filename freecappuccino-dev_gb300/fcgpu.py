@@ -104,6 +104,7 @@ def lib():
         "fc_solve_field": (i, [vp, cp, cp, cp, vp, i, d, d, cp, C.POINTER(SolveInfo)]),
         "fc_simple_set_params": (i, [vp, vp]),
         "fc_sweep_stats": (i, [vp, i, vp]),
+        "fc_mixed_colours": (i, [vp, i, vp]),
         "fc_set_tracing": (i, [vp, i]),
         "fc_trace_get": (i, [vp, vp, vp]),
         "fc_init_flmass": (i, [vp]),
@@ -494,6 +495,12 @@ class Context:
         keys = ("tiles", "levels", "max_width", "ring_depth", "est_sweep_us", "ring_entries", "pushed_entries",
                 "cross_tile_entries", "stages", "max_tile_steps")
         return dict(zip(keys, [float(v) for v in out]))
+
+    def mixed_colours(self, which=0):
+        """Colours of the multicolour ordering of FC_PREC_MIXED_COLOURED."""
+        out = np.zeros(1, np.int32)
+        self._check(self.L.fc_mixed_colours(self.h, which, _ptr(out)), "fc_mixed_colours")
+        return int(out[0])
 
     def set_tracing(self, on=True):
         self._check(self.L.fc_set_tracing(self.h, int(on)), "fc_set_tracing")

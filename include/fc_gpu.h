@@ -96,11 +96,12 @@ typedef struct fc_ctx fc_ctx;
 
 #define FC_PREC_FP64   0   /* everything in FP64, as the reference */
 #define FC_PREC_MIXED  1   /* FP32 matrix/preconditioner/Krylov vectors inside FP64 iterative refinement */
-/* as FC_PREC_MIXED, but the ICCG inner solve runs on a multicolour ordering of
- * the rows: its DIC factor is built and applied one colour at a time
- * (bandwidth-bound passes instead of the natural order's long chain of
- * levels).  The preconditioner differs from the reference's, the stopping
- * test and the FP64 refinement do not; other solvers behave as FC_PREC_MIXED. */
+/* ICCG solves as in FC_PREC_MIXED, but the FP32 inner solve runs on a
+ * multicolour ordering of the rows: its DIC factor is built and applied one
+ * colour at a time (bandwidth-bound passes instead of the natural order's long
+ * chain of levels).  The preconditioner differs from the reference's, the
+ * stopping test and the FP64 refinement do not.  The other solvers run in
+ * FP64 as in FC_PREC_FP64. */
 #define FC_PREC_MIXED_COLOURED 2
 
 int fc_init(int device, fc_ctx** out);
@@ -166,6 +167,10 @@ int fc_spmv(fc_ctx* ctx, int n, int nnz, const int* ia, const int* ja, const dou
  * ring-served entries, pushed entries, cross-tile entries (both triangles),
  * stage depth, most steps of a tile. */
 int fc_sweep_stats(fc_ctx* ctx, int which, double* out);
+/* Colours of the multicolour ordering FC_PREC_MIXED_COLOURED uses for the
+ * same systems (which as above); builds the ordering if no solve has yet.
+ * Diagnostics only: no counterpart in the reference. */
+int fc_mixed_colours(fc_ctx* ctx, int which, int* ncol);
 /* Tracing of the FP64 ICCG kernel (no counterpart in the reference): with
  * on != 0 the solves run a traced instantiation that records per block the
  * SM cycles of each phase and, for the forward and backward sweep of the

@@ -208,14 +208,14 @@ def cavity_fields(m, nT, nC):
     return a, u, nwal
 
 
-def simple_block(fc, args, dev, with_cpu):
-    """C1: SIMPLE iterations per second on the n^3 lid-driven cavity (unit
-    cube, uniform hexes, nu = 0.01, central differencing with deferred
-    correction, Gauss gradients, BiCGStab(DILU) for U, ICCG(DIC) for p, the
-    settings of examples/cavity/input.nml), FP64 and mixed precision, plus the
-    oracle's SIMPLE iteration on one core."""
-    n = args.simple_n
-    m = fc.Mesh.box(n, n, n)
+def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None):
+    """SIMPLE iterations per second on the n^3 lid-driven cavity (unit cube,
+    nu = 0.01, central differencing with deferred correction, Gauss gradients,
+    BiCGStab(DILU) for U, ICCG(DIC) for p, the settings of
+    examples/cavity/input.nml), FP64 and mixed precision, plus the oracle's
+    SIMPLE iteration on one core.  perturb > 0 moves the interior vertices by
+    U(-perturb h, perturb h) (seed 42): the non-orthogonal mesh."""
+    m = fc.Mesh.box(n, n, n, 1.0, 1.0, 1.0, perturb=perturb, seed=MESH_SEED)
     nC, nT = m.numCells, m.numTotal
     a, u, nwal = cavity_fields(m, nT, nC)
     ctx = fc.Context(dev)
@@ -232,8 +232,9 @@ def simple_block(fc, args, dev, with_cpu):
         ctx.simple_params(prm)
         ctx.init_flmass()
 
-    out = {"workload": f"{n}^3 lid-driven cavity, Re=100, SIMPLE (central/DC, Gauss, BiCGStab U, ICCG p)",
-           "cells": nC, "unit": "SIMPLE iters/s"}
+    mesh_kind = f"perturbed hexes (+-{perturb:g} h)" if perturb > 0 else "uniform hexes"
+    out = {"workload": f"{n}^3 lid-driven cavity on {mesh_kind}, Re=100, SIMPLE (central/DC, Gauss, BiCGStab U, "
+                       f"ICCG p)", "cells": nC, "unit": "SIMPLE iters/s"}
     for mode, key in ((fc.FC_PREC_FP64, "value"), (fc.FC_PREC_MIXED_COLOURED, "mixed")):
         ctx.set_precision(mode, MIXED_INNER_TOL, 0) if mode else ctx.set_precision(mode)
         reset()
@@ -249,6 +250,9 @@ def simple_block(fc, args, dev, with_cpu):
         out[key + "_ms_per_iteration"] = ms
         out[key + "_resor"] = [float(v) for v in res]
     out["iterations_timed"] = f"{args.simple_iters} after {args.simple_skip} untimed"
+    out["mixed_note"] = ("ICCG for p with the multicolour FP32 inner solve, capped at maxiterP iterations as the "
+                         "reference caps it: it reduces the p residual less per SIMPLE iteration than the "
+                         "natural-order DIC, so the *_resor after the same iterations differ")
     ctx.set_precision(fc.FC_PREC_FP64)
     ctx.close()
     if with_cpu:
@@ -272,7 +276,8 @@ def simple_block(fc, args, dev, with_cpu):
         oc.solver("U", prm.lSolverU.decode())
         oc.solver("P", prm.lSolverP.decode())
         oc.L.orc_init_flmass(oc.h)
-        for _ in range(args.simple_skip):
+        skip = args.simple_skip if cpu_skip is None else cpu_skip
+        for _ in range(skip):
             oc.simple_iteration()
         t0 = time.perf_counter()
         for _ in range(args.simple_cpu_iters):
@@ -280,7 +285,8 @@ def simple_block(fc, args, dev, with_cpu):
         dt = (time.perf_counter() - t0) / args.simple_cpu_iters
         out["cpu_baseline"] = {"value": 1.0 / dt, "unit": "SIMPLE iters/s", "cores": 1, "kind": "port",
                                "sample": f"{args.simple_cpu_iters} SIMPLE iterations of the same cavity after "
-                                         f"{args.simple_skip} untimed (C++ restatement, -O3, one thread)"}
+                                         f"{skip} untimed (C++ restatement, -O3, one thread)"}
+        out["gpu_fp64_vs_cpu"] = out["value"] / out["cpu_baseline"]["value"]
     return out
 
 
@@ -417,7 +423,10 @@ def run_gpu(args, rank, world, dist):
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(ia, ja, a_host, dg, b, iters, args.ref_sample)
     if args.simple_n > 0:
-        line["simple"] = simple_block(fc, args, dev, not args.no_cpu)
+        line["simple"] = simple_block(fc, args, dev, not args.no_cpu, args.simple_n)
+    if args.simple_big_n > 0:
+        line["simple_perturbed"] = simple_block(fc, args, dev, not args.no_cpu, args.simple_big_n, PERTURB,
+                                                cpu_skip=args.simple_big_cpu_skip)
     print(json.dumps(line), flush=True)
 
 
@@ -432,6 +441,9 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=0, help="iterations of a full solve for the reference arm")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--simple-n", type=int, default=64, help="cells per side of the SIMPLE cavity (0: skip)")
+    ap.add_argument("--simple-big-n", type=int, default=128,
+                    help="cells per side of the SIMPLE cavity on the perturbed mesh (0: skip)")
+    ap.add_argument("--simple-big-cpu-skip", type=int, default=2, help="untimed oracle iterations there")
     ap.add_argument("--simple-iters", type=int, default=20, help="timed SIMPLE iterations")
     ap.add_argument("--simple-skip", type=int, default=10, help="untimed SIMPLE iterations before them")
     ap.add_argument("--simple-cpu-iters", type=int, default=3, help="oracle SIMPLE iterations timed")

@@ -382,7 +382,10 @@ def run_gpu(args, rank, world, dist):
                 "inner_iterations": mi.itr_used, "outer_iterations": mi.outer_iterations, "inner_tol": inner_tol,
                 "max_rel_diff_vs_fp64": err}
 
+    if args.mixed_host_loop:  # profiling: the coloured inner kernels launched from the host
+        ctx.set_tracing(True)
     mixed = mixed_run(fc.FC_PREC_MIXED_COLOURED, MIXED_INNER_TOL)
+    ctx.set_tracing(False)
     mixed["inner_solver"] = ("FP32 ICCG, multicolour DIC (%d colours) in Eisenstat form, one CUDA graph"
                              % ctx.mixed_colours(0))
     mixed_nat = mixed_run(fc.FC_PREC_MIXED, MIXED_NATURAL_INNER_TOL)
@@ -440,6 +443,8 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=120, help="ICCG iterations per CPU sample")
     ap.add_argument("--ref-iters", type=int, default=0, help="iterations of a full solve for the reference arm")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--mixed-host-loop", action="store_true",
+                    help="launch the multicolour inner kernels from the host (visible to profilers)")
     ap.add_argument("--simple-n", type=int, default=64, help="cells per side of the SIMPLE cavity (0: skip)")
     ap.add_argument("--simple-big-n", type=int, default=128,
                     help="cells per side of the SIMPLE cavity on the perturbed mesh (0: skip)")

@@ -189,7 +189,7 @@ __device__ __forceinline__ McBcast mcg_scalars(const McDev& D) {
 __device__ __forceinline__ void mcg_stop(const McDev& D, int status) {
   if (status) D.sc->status = status;
   D.sc->done = 1;
-  cudaGraphSetConditional(D.h, 0);
+  if (D.h) cudaGraphSetConditional(D.h, 0);  // 0 outside the graph (host-launched diagnostic mode)
 }
 
 // One row, entry k of a block at e + k * stride, all k < w (padding entries
@@ -598,7 +598,31 @@ int mc_inner_solve(fc_ctx* ctx, CsrSystem* s, const double* a, const double* r64
     }
   }
   FC_CUDA_TRY(ctx, cudaGetLastError());
-  FC_CUDA_TRY(ctx, cudaGraphLaunch(m.exec, ctx->stream));
+  if (!ctx->tracing) {
+    FC_CUDA_TRY(ctx, cudaGraphLaunch(m.exec, ctx->stream));
+  } else {
+    // diagnostic mode (fc_set_tracing): the same kernels launched from the
+    // host, so that profilers see every launch; the loop checks the stop
+    // flag every 32 iterations (the kernels of later iterations return at once)
+    const int C = m.ncol;
+    auto blocks_of = [&](int c) { return mc_blocks(m.crow[c + 1] - m.crow[c]); };
+    for (int c = 0; c < C; ++c) k_e_fwdb<<<blocks_of(c), MCG_BLOCK, 0, ctx->stream>>>(D, c);
+    k_e_start<<<mc_blocks(m.nP), MCG_BLOCK, 0, ctx->stream>>>(D);
+    for (int base = 0; base < std::max(itmax, 1); base += 32) {
+      for (int k = 0; k < 32; ++k) {
+        for (int c = C - 2; c >= 1; --c) k_e_bwd<<<blocks_of(c), MCG_BLOCK, 0, ctx->stream>>>(D, c);
+        k_e_bf0<<<blocks_of(0), MCG_BLOCK, 0, ctx->stream>>>(D);
+        for (int c = 1; c < C; ++c) k_e_fwd<<<blocks_of(c), MCG_BLOCK, 0, ctx->stream>>>(D, c);
+        k_e_upd<<<mc_blocks(m.nP / 4), MCG_BLOCK, 0, ctx->stream>>>(D);
+        k_e_pupd<<<mc_blocks(m.nP / 4), MCG_BLOCK, 0, ctx->stream>>>(D);
+      }
+      FC_CUDA_TRY(ctx, cudaMemcpyAsync(m.h_sc, m.sc.p, sizeof(McScal), cudaMemcpyDeviceToHost, ctx->stream));
+      FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+      if (m.h_sc->done) break;
+    }
+    for (int c = C - 1; c >= 0; --c) k_e_xb<<<blocks_of(c), MCG_BLOCK, 0, ctx->stream>>>(D, c);
+    FC_CUDA_TRY(ctx, cudaGetLastError());
+  }
   k_mc_scatter_add<<<eb, MCG_BLOCK, 0, ctx->stream>>>(m.nP, m.perm.p, m.x.p, x64);
   FC_CUDA_TRY(ctx, cudaMemcpyAsync(m.h_sc, m.sc.p, sizeof(McScal), cudaMemcpyDeviceToHost, ctx->stream));
   FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));

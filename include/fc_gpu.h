@@ -179,7 +179,10 @@ int fc_mixed_colours(fc_ctx* ctx, int which, int* ncol);
  * setup, forward sweep, sweep barrier, backward sweep, dot product, p update,
  * SpMV, x/r update; then the blocks that ran, the blocks of the launch (B)
  * and the stamps per tile (K); timeline (optional, 2*B*K*2 entries)
- * receives the stamps as [sweep][tile][step][clock, globaltimer]. */
+ * receives the stamps as [sweep][tile][step][clock, globaltimer].  With
+ * tracing on, the multicolour inner solve of FC_PREC_MIXED_COLOURED launches
+ * its kernels from the host instead of its CUDA graph, so that a profiler
+ * sees each launch. */
 int fc_set_tracing(fc_ctx* ctx, int on);
 int fc_trace_get(fc_ctx* ctx, double* out, unsigned long long* timeline);
 /* ILU(0) factors of ilu_cr (linear_solvers.f90:1267-1385) in the CSR slots. */

@@ -42,6 +42,10 @@
 #include "fc_internal.hpp"
 
 #define MCG_BLOCK 512
+// the loop-body kernels run grid-stride on at most this many waves of
+// resident blocks: the per-block reduction tail (block sum, fence, arrival
+// atomic) is then paid once per wave
+#define MC_WAVES 1
 #define MC_UNROLL 8   // widest block whose loads are issued all at once (hex rows: 6, tets: 4)
 
 // per-colour table in device memory, MC_T entries per field: first row of
@@ -59,7 +63,7 @@ struct McScal {
 };
 
 struct DevColoured {
-  int n = 0, nP = 0, ncol = 0, maxblocks = 1;
+  int n = 0, nP = 0, ncol = 0, maxblocks = 1, wave = 1;
   std::vector<int> crow;
   DVec<int> tab, perm, col, src, tsrc, dslot;
   DVec<float> mval, adiag, invd, dvec, kdiag, x, r, p, q, y, t, w;
@@ -302,6 +306,7 @@ __global__ void __launch_bounds__(MCG_BLOCK) k_e_start(McDev D) {
   if (!mcg_reduce<1>(D, v, tot) || threadIdx.x != 0) return;
   McScal* S = D.sc;
   S->rz = S->rz0 = S->res0 = S->resl = tot[0];
+  S->beta = 0.0f;
   if (!(tot[0] == tot[0]) || isinf(tot[0])) mcg_stop(D, FC_ERR_NAN);
   else if (tot[0] == 0.0 || S->itmax <= 0) mcg_stop(D, 0);
 }
@@ -311,9 +316,8 @@ __global__ void __launch_bounds__(MCG_BLOCK) k_e_bwd(McDev D, int c) {
   if (mcg_scalars(D).done) return;
   const int r0 = __ldg(D.tab + MC_CR + c), r1 = __ldg(D.tab + MC_CR + c + 1);
   const int ceu = __ldg(D.tab + MC_CEU + c), cwu = __ldg(D.tab + MC_CWU + c);
-  const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= r1) return;
-  D.t[i] = (__ldcg(D.p + i) - ell_sum(D, ceu + (i - r0), r1 - r0, cwu, D.t, 0.0f)) * __ldcg(D.invd + i);
+  for (int i = r0 + blockIdx.x * blockDim.x + threadIdx.x; i < r1; i += gridDim.x * blockDim.x)
+    D.t[i] = (__ldcg(D.p + i) - ell_sum(D, ceu + (i - r0), r1 - r0, cwu, D.t, 0.0f)) * __ldcg(D.invd + i);
 }
 
 // colour 0: the last backward colour t = (p - U t) / d and the first forward
@@ -322,16 +326,15 @@ __global__ void __launch_bounds__(MCG_BLOCK) k_e_bf0(McDev D) {
   if (mcg_scalars(D).done) return;
   const int r1 = __ldg(D.tab + MC_CR + 1);
   const int ceu = __ldg(D.tab + MC_CEU), cwu = __ldg(D.tab + MC_CWU);
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   float v[1] = {0.0f};
-  if (i < r1) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < r1; i += gridDim.x * blockDim.x) {
     const float pi = __ldcg(D.p + i), di = __ldcg(D.invd + i), ki = __ldcg(D.kdiag + i);
     const float ti = (pi - ell_sum(D, ceu + i, r1, cwu, D.t, 0.0f)) * di;
     const float wi = fmaf(ki, ti, pi) * di;
     const float qi = ti + wi;
     D.w[i] = wi;
     D.q[i] = qi;
-    v[0] = pi * qi;
+    v[0] += pi * qi;
   }
   double tot[1];
   if (!mcg_reduce<1>(D, v, tot) || threadIdx.x != 0) return;
@@ -350,15 +353,14 @@ __global__ void __launch_bounds__(MCG_BLOCK) k_e_fwd(McDev D, int c) {
   if (mcg_scalars(D).done) return;
   const int r0 = __ldg(D.tab + MC_CR + c), r1 = __ldg(D.tab + MC_CR + c + 1);
   const int cel = __ldg(D.tab + MC_CEL + c), cwl = __ldg(D.tab + MC_CWL + c);
-  const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
   float v[1] = {0.0f};
-  if (i < r1) {
+  for (int i = r0 + blockIdx.x * blockDim.x + threadIdx.x; i < r1; i += gridDim.x * blockDim.x) {
     const float pi = __ldcg(D.p + i), di = __ldcg(D.invd + i), ki = __ldcg(D.kdiag + i), ti = __ldcg(D.t + i);
     const float wi = (fmaf(ki, ti, pi) - ell_sum(D, cel + (i - r0), r1 - r0, cwl, D.w, 0.0f)) * di;
     const float qi = ti + wi;
     D.w[i] = wi;
     D.q[i] = qi;
-    v[0] = pi * qi;
+    v[0] += pi * qi;
   }
   double tot[1];
   if (!mcg_reduce<1>(D, v, tot) || threadIdx.x != 0) return;
@@ -376,10 +378,9 @@ __global__ void __launch_bounds__(MCG_BLOCK) k_e_fwd(McDev D, int c) {
 __global__ void __launch_bounds__(MCG_BLOCK) k_e_upd(McDev D) {
   const McBcast sc = mcg_scalars(D);
   if (sc.done) return;
-  const int i4 = blockIdx.x * blockDim.x + threadIdx.x;
   const float alpha = sc.alpha;
   float v[1] = {0.0f};
-  if (i4 < (D.nP >> 2)) {
+  for (int i4 = blockIdx.x * blockDim.x + threadIdx.x; i4 < (D.nP >> 2); i4 += gridDim.x * blockDim.x) {
     const float4 x4 = __ldcg((const float4*)D.x + i4), p4 = __ldcg((const float4*)D.p + i4);
     const float4 q4 = __ldcg((const float4*)D.q + i4), r4 = __ldcg((const float4*)D.r + i4);
     const float4 d4 = __ldcg((const float4*)D.dvec + i4);
@@ -390,7 +391,7 @@ __global__ void __launch_bounds__(MCG_BLOCK) k_e_upd(McDev D) {
                                      fmaf(alpha, p4.w, x4.w));
     ((float4*)D.r)[i4] = rn;
     ((float4*)D.y)[i4] = zn;
-    v[0] = (rn.x * zn.x + rn.y * zn.y) + (rn.z * zn.z + rn.w * zn.w);
+    v[0] += (rn.x * zn.x + rn.y * zn.y) + (rn.z * zn.z + rn.w * zn.w);
   }
   double tot[1];
   if (!mcg_reduce<1>(D, v, tot) || threadIdx.x != 0) return;
@@ -408,17 +409,97 @@ __global__ void __launch_bounds__(MCG_BLOCK) k_e_upd(McDev D) {
 __global__ void __launch_bounds__(MCG_BLOCK) k_e_pupd(McDev D) {
   const McBcast sc = mcg_scalars(D);
   if (sc.done) return;
-  const int i4 = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i4 >= (D.nP >> 2)) return;
   const float beta = sc.beta;
-  const float4 z4 = __ldcg((const float4*)D.y + i4), p4 = __ldcg((const float4*)D.p + i4);
-  const float4 pn = make_float4(fmaf(beta, p4.x, z4.x), fmaf(beta, p4.y, z4.y), fmaf(beta, p4.z, z4.z),
-                                fmaf(beta, p4.w, z4.w));
-  ((float4*)D.p)[i4] = pn;
-  if (4 * i4 >= __ldg(D.tab + MC_CR + D.ncol - 1)) {  // colour boundaries are multiples of 32 rows
-    const float4 d4 = __ldcg((const float4*)D.invd + i4);
-    ((float4*)D.t)[i4] = make_float4(pn.x * d4.x, pn.y * d4.y, pn.z * d4.z, pn.w * d4.w);
+  const int clast = __ldg(D.tab + MC_CR + D.ncol - 1);
+  for (int i4 = blockIdx.x * blockDim.x + threadIdx.x; i4 < (D.nP >> 2); i4 += gridDim.x * blockDim.x) {
+    const float4 z4 = __ldcg((const float4*)D.y + i4), p4 = __ldcg((const float4*)D.p + i4);
+    const float4 pn = make_float4(fmaf(beta, p4.x, z4.x), fmaf(beta, p4.y, z4.y), fmaf(beta, p4.z, z4.z),
+                                  fmaf(beta, p4.w, z4.w));
+    ((float4*)D.p)[i4] = pn;
+    if (4 * i4 >= clast) {  // colour boundaries are multiples of 32 rows
+      const float4 d4 = __ldcg((const float4*)D.invd + i4);
+      ((float4*)D.t)[i4] = make_float4(pn.x * d4.x, pn.y * d4.y, pn.z * d4.z, pn.w * d4.w);
+    }
   }
+}
+
+// Two colours (red-black): the new direction p = z + beta p is folded into
+// the two colour passes, so an iteration is three kernels.  Colour 0 updates
+// its own p and gathers t_j = (z_j + beta p_j) / d_j of its colour-1
+// neighbours, whose p the colour-1 pass has not yet replaced.
+__device__ __forceinline__ float ell_sum_t(const McDev& D, int e, int stride, int w, float beta, float acc) {
+  if (w <= MC_UNROLL) {
+    int c[MC_UNROLL];
+    float m[MC_UNROLL];
+#pragma unroll
+    for (int k = 0; k < MC_UNROLL; ++k)
+      if (k < w) {
+        c[k] = __ldg(D.col + e + k * stride);
+        m[k] = __ldcg(D.mval + e + k * stride);
+      }
+#pragma unroll
+    for (int k = 0; k < MC_UNROLL; ++k)
+      if (k < w) {
+        const float tj = fmaf(beta, __ldcg(D.p + c[k]), __ldcg(D.y + c[k])) * __ldcg(D.invd + c[k]);
+        acc = fmaf(m[k], tj, acc);
+      }
+    return acc;
+  }
+  for (int k = 0; k < w; ++k) {
+    const int cj = __ldg(D.col + e + k * stride);
+    acc = fmaf(__ldcg(D.mval + e + k * stride), fmaf(beta, __ldcg(D.p + cj), __ldcg(D.y + cj)) * __ldcg(D.invd + cj), acc);
+  }
+  return acc;
+}
+
+// colour 0 of two: p = z + beta p, t = (p - U t)/d, w = (p + K t)/d, q, p.q
+__global__ void __launch_bounds__(MCG_BLOCK) k_e2_c0(McDev D) {
+  const McBcast sc = mcg_scalars(D);
+  if (sc.done) return;
+  const int r1 = __ldg(D.tab + MC_CR + 1);
+  const int ceu = __ldg(D.tab + MC_CEU), cwu = __ldg(D.tab + MC_CWU);
+  float v[1] = {0.0f};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < r1; i += gridDim.x * blockDim.x) {
+    const float pi = fmaf(sc.beta, __ldcg(D.p + i), __ldcg(D.y + i));
+    const float di = __ldcg(D.invd + i), ki = __ldcg(D.kdiag + i);
+    const float ti = (pi - ell_sum_t(D, ceu + i, r1, cwu, sc.beta, 0.0f)) * di;
+    const float wi = fmaf(ki, ti, pi) * di;
+    const float qi = ti + wi;
+    D.p[i] = pi;
+    D.w[i] = wi;
+    D.q[i] = qi;
+    v[0] += pi * qi;
+  }
+  double tot[1];
+  if (!mcg_reduce<1>(D, v, tot) || threadIdx.x != 0) return;
+  D.sc->pq = tot[0];
+}
+
+// colour 1 of two: p = z + beta p, t = p/d, w = (p + K t - L w)/d, q, p.q, alpha
+__global__ void __launch_bounds__(MCG_BLOCK) k_e2_c1(McDev D) {
+  const McBcast sc = mcg_scalars(D);
+  if (sc.done) return;
+  const int r0 = __ldg(D.tab + MC_CR + 1), r1 = __ldg(D.tab + MC_CR + 2);
+  const int cel = __ldg(D.tab + MC_CEL + 1), cwl = __ldg(D.tab + MC_CWL + 1);
+  float v[1] = {0.0f};
+  for (int i = r0 + blockIdx.x * blockDim.x + threadIdx.x; i < r1; i += gridDim.x * blockDim.x) {
+    const float pi = fmaf(sc.beta, __ldcg(D.p + i), __ldcg(D.y + i));
+    const float di = __ldcg(D.invd + i), ki = __ldcg(D.kdiag + i);
+    const float ti = pi * di;
+    const float wi = (fmaf(ki, ti, pi) - ell_sum(D, cel + (i - r0), r1 - r0, cwl, D.w, 0.0f)) * di;
+    const float qi = ti + wi;
+    D.p[i] = pi;
+    D.w[i] = wi;
+    D.q[i] = qi;
+    v[0] += pi * qi;
+  }
+  double tot[1];
+  if (!mcg_reduce<1>(D, v, tot) || threadIdx.x != 0) return;
+  McScal* S = D.sc;
+  S->pq += tot[0];
+  const double alpha = S->rz / S->pq;
+  if (!(alpha == alpha) || isinf(alpha)) mcg_stop(D, FC_ERR_BREAKDOWN);
+  else S->alpha = (float)alpha;
 }
 
 // colour c of x = (D+U)^-1 y, in place on x (higher colours already hold x)
@@ -477,6 +558,8 @@ static int mc_build_graph(fc_ctx* ctx, DevColoured& m) {
     return FC_OK;
   };
   auto blocks_of = [&](int c) { return mc_blocks(m.crow[c + 1] - m.crow[c]); };
+  // loop-body grids: capped at MC_WAVES waves of resident blocks
+  auto body_blocks = [&](unsigned nat) { return std::min(nat, (unsigned)(MC_WAVES * m.wave)); };
   int st;
   cudaGraphNode_t prev = nullptr;
   void* a1[1] = {&D};
@@ -498,18 +581,24 @@ static int mc_build_graph(fc_ctx* ctx, DevColoured& m) {
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   cudaGraphNode_t bp = nullptr;
   bool have = false;
-  for (int c = C - 2; c >= 1; --c) {
-    void* args[2] = {&D, &cs[c]};
-    if ((st = add(body, bp, have, (const void*)k_e_bwd, blocks_of(c), args))) return st;
-    have = true;
+  if (C == 2) {  // red-black: three kernels per iteration
+    if ((st = add(body, bp, false, (const void*)k_e2_c0, body_blocks(blocks_of(0)), a1))) return st;
+    if ((st = add(body, bp, true, (const void*)k_e2_c1, body_blocks(blocks_of(1)), a1))) return st;
+    if ((st = add(body, bp, true, (const void*)k_e_upd, body_blocks(mc_blocks(m.nP / 4)), a1))) return st;
+  } else {
+    for (int c = C - 2; c >= 1; --c) {
+      void* args[2] = {&D, &cs[c]};
+      if ((st = add(body, bp, have, (const void*)k_e_bwd, body_blocks(blocks_of(c)), args))) return st;
+      have = true;
+    }
+    if ((st = add(body, bp, have, (const void*)k_e_bf0, body_blocks(blocks_of(0)), a1))) return st;
+    for (int c = 1; c < C; ++c) {
+      void* args[2] = {&D, &cs[c]};
+      if ((st = add(body, bp, true, (const void*)k_e_fwd, body_blocks(blocks_of(c)), args))) return st;
+    }
+    if ((st = add(body, bp, true, (const void*)k_e_upd, body_blocks(mc_blocks(m.nP / 4)), a1))) return st;
+    if ((st = add(body, bp, true, (const void*)k_e_pupd, body_blocks(mc_blocks(m.nP / 4)), a1))) return st;
   }
-  if ((st = add(body, bp, have, (const void*)k_e_bf0, blocks_of(0), a1))) return st;
-  for (int c = 1; c < C; ++c) {
-    void* args[2] = {&D, &cs[c]};
-    if ((st = add(body, bp, true, (const void*)k_e_fwd, blocks_of(c), args))) return st;
-  }
-  if ((st = add(body, bp, true, (const void*)k_e_upd, mc_blocks(m.nP / 4), a1))) return st;
-  if ((st = add(body, bp, true, (const void*)k_e_pupd, mc_blocks(m.nP / 4), a1))) return st;
   // after the loop: x = (D+U)^-1 y, colours C-1..0
   prev = loop;
   for (int c = C - 1; c >= 0; --c) {
@@ -564,6 +653,11 @@ static int mc_prepare(fc_ctx* ctx, CsrSystem* s) {
   // padding entries keep the value 0 (the setup writes real entries only)
   FC_CUDA_TRY(ctx, cudaMemset(m->mval.p, 0, ne * sizeof(float)));
   FC_CUDA_TRY(ctx, cudaMemset(m->cnt.p, 0, sizeof(unsigned)));
+  {
+    int nb = 0;  // resident blocks per SM of the widest body kernel
+    FC_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_e2_c0, MCG_BLOCK, 0));
+    m->wave = std::max(1, ctx->num_sms) * std::max(1, nb);
+  }
   if ((st = mc_build_graph(ctx, *m))) {
     delete m;
     return st;
@@ -610,6 +704,12 @@ int mc_inner_solve(fc_ctx* ctx, CsrSystem* s, const double* a, const double* r64
     k_e_start<<<mc_blocks(m.nP), MCG_BLOCK, 0, ctx->stream>>>(D);
     for (int base = 0; base < std::max(itmax, 1); base += 32) {
       for (int k = 0; k < 32; ++k) {
+        if (C == 2) {
+          k_e2_c0<<<blocks_of(0), MCG_BLOCK, 0, ctx->stream>>>(D);
+          k_e2_c1<<<blocks_of(1), MCG_BLOCK, 0, ctx->stream>>>(D);
+          k_e_upd<<<mc_blocks(m.nP / 4), MCG_BLOCK, 0, ctx->stream>>>(D);
+          continue;
+        }
         for (int c = C - 2; c >= 1; --c) k_e_bwd<<<blocks_of(c), MCG_BLOCK, 0, ctx->stream>>>(D, c);
         k_e_bf0<<<blocks_of(0), MCG_BLOCK, 0, ctx->stream>>>(D);
         for (int c = 1; c < C; ++c) k_e_fwd<<<blocks_of(c), MCG_BLOCK, 0, ctx->stream>>>(D, c);
@@ -626,9 +726,9 @@ int mc_inner_solve(fc_ctx* ctx, CsrSystem* s, const double* a, const double* r64
   k_mc_scatter_add<<<eb, MCG_BLOCK, 0, ctx->stream>>>(m.nP, m.perm.p, m.x.p, x64);
   FC_CUDA_TRY(ctx, cudaMemcpyAsync(m.h_sc, m.sc.p, sizeof(McScal), cudaMemcpyDeviceToHost, ctx->stream));
   FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  // graph kernels: prologue C + 1, per iteration 2 C (the last one may stop
-  // early), the final backward sweep C
-  ctx->kernel_launches += 2LL * m.ncol + 1 + (long long)m.h_sc->it * 2 * m.ncol;
+  // graph kernels: prologue C + 1, per iteration 2 C (3 for two colours; the
+  // last iteration may stop early), the final backward sweep C
+  ctx->kernel_launches += 2LL * m.ncol + 1 + (long long)m.h_sc->it * (m.ncol == 2 ? 3 : 2 * m.ncol);
   *itr_out = m.h_sc->it;
   *status_out = m.h_sc->status;
   return FC_OK;

@@ -290,6 +290,40 @@ def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None):
     return out
 
 
+def spmv_leg(fc, ctx, nC, calls):
+    """FP64 y = A x through fc_spmv (ax_cr) on device-resident arrays of the
+    same 128^3 system: the per-call CUDA-event time includes the call's host
+    work and its stream synchronisation, so it bounds the kernel time from
+    above; ncu's launch list gives the kernel alone."""
+    import torch
+    ia, ja, dg, _, _ = ctx.csr_pattern()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    tia, tja, tdg = (torch.from_numpy(np.ascontiguousarray(v, dtype=np.int32)).to(dev) for v in (ia, ja, dg))
+    ta = torch.from_numpy(ctx.field_get("a")).to(dev)
+    tx = torch.from_numpy(np.random.default_rng(RHS_SEED).standard_normal(nC)).to(dev)
+    ty = torch.zeros(nC, dtype=torch.float64, device=dev)
+
+    def call():
+        st = ctx.L.fc_spmv(ctx.h, nC, len(ja), fc._ptr(tia), fc._ptr(tja), fc._ptr(ta), fc._ptr(tdg), fc._ptr(tx),
+                           fc._ptr(ty), 0)
+        if st != 0:
+            raise RuntimeError(f"fc_spmv status {st}")
+
+    for _ in range(3):
+        call()
+    ms = []
+    for _ in range(calls):
+        ctx.event(0)
+        call()
+        ctx.event(1)
+        ms.append(ctx.elapsed_ms())
+    us = float(np.median(ms)) * 1e3
+    nbytes = 12 * len(ja) + 4 * (nC + 1) + 16 * nC
+    return {"calls": calls, "us_per_call": us, "algorithmic_bytes": nbytes,
+            "gbs_per_call": nbytes / (us * 1e-6) / 1e9,
+            "note": "per call, host work and the call's synchronisation included (upper bound on the kernel)"}
+
+
 def run_gpu(args, rank, world, dist):
     fc = load_fc()
     dev = int(os.environ.get("LOCAL_RANK", "0"))
@@ -391,6 +425,7 @@ def run_gpu(args, rank, world, dist):
     mixed_nat = mixed_run(fc.FC_PREC_MIXED, MIXED_NATURAL_INNER_TOL)
     mixed_nat["inner_solver"] = "FP32 ICCG, natural-order DIC (the FP64 path's sweeps)"
 
+    spmv = spmv_leg(fc, ctx, nC, args.spmv_calls) if args.spmv_calls > 0 else None
     sweep = ctx.sweep_stats(0)
     peak, peak_kind = measured_peak()
     bytes_launch = iccg_bytes_per_iteration(nC, nnz) * iters
@@ -422,6 +457,8 @@ def run_gpu(args, rank, world, dist):
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
             "mixed": mixed, "mixed_natural_order": mixed_nat}
+    if spmv:
+        line["spmv"] = spmv
     ctx.close()
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(ia, ja, a_host, dg, b, iters, args.ref_sample)
@@ -443,6 +480,7 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=120, help="ICCG iterations per CPU sample")
     ap.add_argument("--ref-iters", type=int, default=0, help="iterations of a full solve for the reference arm")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--spmv-calls", type=int, default=20, help="timed fc_spmv calls on device arrays (0: skip)")
     ap.add_argument("--mixed-host-loop", action="store_true",
                     help="launch the multicolour inner kernels from the host (visible to profilers)")
     ap.add_argument("--simple-n", type=int, default=64, help="cells per side of the SIMPLE cavity (0: skip)")

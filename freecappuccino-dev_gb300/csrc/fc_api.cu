@@ -261,12 +261,13 @@ extern "C" int fc_spmv(fc_ctx* ctx, int n, int nnz, const int* ia, const int* ja
   CsrSystem* s = nullptr;
   int st = ext_system(ctx, n, nnz, ia, ja, diag, &s);
   if (st) return st;
-  if ((st = sys_upload_values(ctx, s, a, is_device_ptr(a)))) return st;
-  const double* dx;
+  // device-resident values and vectors are used in place
+  const double *da, *dx;
+  if ((st = stage_in(ctx, a, s->a.p, nnz, &da))) return st;
   if ((st = stage_in(ctx, x, s->b.p, n, &dx))) return st;
   const bool ydev = is_device_ptr(y);
   double* dy = ydev ? y : s->w.p;
-  if ((st = sys_spmv(ctx, s, s->a.p, dx, dy, transpose))) return st;
+  if ((st = sys_spmv(ctx, s, da, dx, dy, transpose))) return st;
   if (!ydev) FC_CUDA_TRY(ctx, cudaMemcpyAsync(y, dy, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   return FC_OK;

@@ -700,21 +700,23 @@ int mc_inner_solve(fc_ctx* ctx, CsrSystem* s, const double* a, const double* r64
     // flag every 32 iterations (the kernels of later iterations return at once)
     const int C = m.ncol;
     auto blocks_of = [&](int c) { return mc_blocks(m.crow[c + 1] - m.crow[c]); };
+    auto body_blocks = [&](unsigned nat) { return std::min(nat, (unsigned)(MC_WAVES * m.wave)); };
     for (int c = 0; c < C; ++c) k_e_fwdb<<<blocks_of(c), MCG_BLOCK, 0, ctx->stream>>>(D, c);
     k_e_start<<<mc_blocks(m.nP), MCG_BLOCK, 0, ctx->stream>>>(D);
     for (int base = 0; base < std::max(itmax, 1); base += 32) {
       for (int k = 0; k < 32; ++k) {
+        const unsigned bv = body_blocks(mc_blocks(m.nP / 4));
         if (C == 2) {
-          k_e2_c0<<<blocks_of(0), MCG_BLOCK, 0, ctx->stream>>>(D);
-          k_e2_c1<<<blocks_of(1), MCG_BLOCK, 0, ctx->stream>>>(D);
-          k_e_upd<<<mc_blocks(m.nP / 4), MCG_BLOCK, 0, ctx->stream>>>(D);
+          k_e2_c0<<<body_blocks(blocks_of(0)), MCG_BLOCK, 0, ctx->stream>>>(D);
+          k_e2_c1<<<body_blocks(blocks_of(1)), MCG_BLOCK, 0, ctx->stream>>>(D);
+          k_e_upd<<<bv, MCG_BLOCK, 0, ctx->stream>>>(D);
           continue;
         }
-        for (int c = C - 2; c >= 1; --c) k_e_bwd<<<blocks_of(c), MCG_BLOCK, 0, ctx->stream>>>(D, c);
-        k_e_bf0<<<blocks_of(0), MCG_BLOCK, 0, ctx->stream>>>(D);
-        for (int c = 1; c < C; ++c) k_e_fwd<<<blocks_of(c), MCG_BLOCK, 0, ctx->stream>>>(D, c);
-        k_e_upd<<<mc_blocks(m.nP / 4), MCG_BLOCK, 0, ctx->stream>>>(D);
-        k_e_pupd<<<mc_blocks(m.nP / 4), MCG_BLOCK, 0, ctx->stream>>>(D);
+        for (int c = C - 2; c >= 1; --c) k_e_bwd<<<body_blocks(blocks_of(c)), MCG_BLOCK, 0, ctx->stream>>>(D, c);
+        k_e_bf0<<<body_blocks(blocks_of(0)), MCG_BLOCK, 0, ctx->stream>>>(D);
+        for (int c = 1; c < C; ++c) k_e_fwd<<<body_blocks(blocks_of(c)), MCG_BLOCK, 0, ctx->stream>>>(D, c);
+        k_e_upd<<<bv, MCG_BLOCK, 0, ctx->stream>>>(D);
+        k_e_pupd<<<bv, MCG_BLOCK, 0, ctx->stream>>>(D);
       }
       FC_CUDA_TRY(ctx, cudaMemcpyAsync(m.h_sc, m.sc.p, sizeof(McScal), cudaMemcpyDeviceToHost, ctx->stream));
       FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));

@@ -208,33 +208,40 @@ def cavity_fields(m, nT, nC):
     return a, u, nwal
 
 
-def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None):
+def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None, tets=False, viscos=0.01, scheme=1, grad=0,
+                 iters=None, cpu_iters=None, urf=(0.8, 0.3)):
     """SIMPLE iterations per second on the n^3 lid-driven cavity (unit cube,
     nu = 0.01, central differencing with deferred correction, Gauss gradients,
     BiCGStab(DILU) for U, ICCG(DIC) for p, the settings of
     examples/cavity/input.nml), FP64 and mixed precision, plus the oracle's
     SIMPLE iteration on one core.  perturb > 0 moves the interior vertices by
     U(-perturb h, perturb h) (seed 42): the non-orthogonal mesh."""
-    m = fc.Mesh.box(n, n, n, 1.0, 1.0, 1.0, perturb=perturb, seed=MESH_SEED)
+    m = fc.Mesh.box(n, n, n, 1.0, 1.0, 1.0, perturb=perturb, seed=MESH_SEED, tets=tets)
+    iters = args.simple_iters if iters is None else iters
+    cpu_iters = args.simple_cpu_iters if cpu_iters is None else cpu_iters
     nC, nT = m.numCells, m.numTotal
     a, u, nwal = cavity_fields(m, nT, nC)
     ctx = fc.Context(dev)
     ctx.set_mesh(m)
-    prm = fc.SimpleParams.cavity()
+    prm = fc.SimpleParams.cavity(viscos=viscos, scheme=scheme, grad=grad, urfU=urf[0], urfP=urf[1])
 
     def reset():
         zero = np.zeros(nT)
-        for k, v in dict(u=u, v=zero, w=zero, p=zero, pp=zero, den=np.ones(nT), vis=np.full(nT, 0.01)).items():
+        for k, v in dict(u=u, v=zero, w=zero, p=zero, pp=zero, den=np.ones(nT), vis=np.full(nT, viscos)).items():
             ctx.field_set(k, v)
-        ctx.field_set("visw", np.full(max(nwal, 1), 0.01))
+        ctx.field_set("visw", np.full(max(nwal, 1), viscos))
         for k in ("flmass", "a", "dUdxi", "dVdxi", "dWdxi", "dPdxi"):
             ctx.field_fill(k, 0.0)
         ctx.simple_params(prm)
         ctx.init_flmass()
 
     mesh_kind = f"perturbed hexes (+-{perturb:g} h)" if perturb > 0 else "uniform hexes"
-    out = {"workload": f"{n}^3 lid-driven cavity on {mesh_kind}, Re=100, SIMPLE (central/DC, Gauss, BiCGStab U, "
-                       f"ICCG p)", "cells": nC, "unit": "SIMPLE iters/s"}
+    if tets:
+        mesh_kind += " split into 6 tetrahedra each"
+    sname = {1: "central", 19: "boundedLinearUpwind"}.get(scheme, str(scheme))
+    gname = {0: "Gauss", 1: "LSQ", 2: "LSQ_DM"}[grad]
+    out = {"workload": f"{n}^3 lid-driven cavity on {mesh_kind}, Re={1.0 / viscos:g}, SIMPLE ({sname}/DC, {gname}, "
+                       f"BiCGStab U, ICCG p, urfU {urf[0]:g}, urfP {urf[1]:g})", "cells": nC, "unit": "SIMPLE iters/s"}
     for mode, key in ((fc.FC_PREC_FP64, "value"), (fc.FC_PREC_MIXED_COLOURED, "mixed")):
         ctx.set_precision(mode, MIXED_INNER_TOL, 0) if mode else ctx.set_precision(mode)
         reset()
@@ -242,14 +249,14 @@ def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None):
             ctx.simple_iteration()
         ctx.sync()
         ctx.event(0)
-        for _ in range(args.simple_iters):
+        for _ in range(iters):
             res = ctx.simple_iteration()
         ctx.event(1)
-        ms = ctx.elapsed_ms() / args.simple_iters
+        ms = ctx.elapsed_ms() / iters
         out[key] = 1e3 / ms
         out[key + "_ms_per_iteration"] = ms
         out[key + "_resor"] = [float(v) for v in res]
-    out["iterations_timed"] = f"{args.simple_iters} after {args.simple_skip} untimed"
+    out["iterations_timed"] = f"{iters} after {args.simple_skip} untimed"
     out["mixed_note"] = ("ICCG for p with the multicolour FP32 inner solve, capped at maxiterP iterations as the "
                          "reference caps it: it reduces the p residual less per SIMPLE iteration than the "
                          "natural-order DIC, so the *_resor after the same iterations differ")
@@ -260,10 +267,10 @@ def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None):
         import oracle_lib
         oc = oracle_lib.Case(a, fast=True)
         zero = np.zeros(nT)
-        for k, v in dict(u=u, v=zero, w=zero, p=zero, pp=zero, den=np.ones(nT), vis=np.full(nT, 0.01)).items():
+        for k, v in dict(u=u, v=zero, w=zero, p=zero, pp=zero, den=np.ones(nT), vis=np.full(nT, viscos)).items():
             oc.set(k, v)
         if nwal:
-            oc.set("visw", np.full(nwal, 0.01))
+            oc.set("visw", np.full(nwal, viscos))
         for k in ("flmass", "a"):
             oc.set(k, np.zeros(oc._len(k)))
         for k in ("dUdxi", "dVdxi", "dWdxi", "dPdxi"):
@@ -280,11 +287,11 @@ def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None):
         for _ in range(skip):
             oc.simple_iteration()
         t0 = time.perf_counter()
-        for _ in range(args.simple_cpu_iters):
+        for _ in range(cpu_iters):
             oc.simple_iteration()
-        dt = (time.perf_counter() - t0) / args.simple_cpu_iters
+        dt = (time.perf_counter() - t0) / cpu_iters
         out["cpu_baseline"] = {"value": 1.0 / dt, "unit": "SIMPLE iters/s", "cores": 1, "kind": "port",
-                               "sample": f"{args.simple_cpu_iters} SIMPLE iterations of the same cavity after "
+                               "sample": f"{cpu_iters} SIMPLE iterations of the same cavity after "
                                          f"{skip} untimed (C++ restatement, -O3, one thread)"}
         out["gpu_fp64_vs_cpu"] = out["value"] / out["cpu_baseline"]["value"]
     return out
@@ -464,6 +471,13 @@ def run_gpu(args, rank, world, dist):
         line["cpu_baseline"] = cpu_baseline(ia, ja, a_host, dg, b, iters, args.ref_sample)
     if args.simple_n > 0:
         line["simple"] = simple_block(fc, args, dev, not args.no_cpu, args.simple_n)
+    if args.simple_tet_n > 0:
+        # C5: 6 tets per perturbed hex, Re = 400, LSQ gradients, boundedLinearUpwind.  With the cavity
+        # input's urfU 0.8 / urfP 0.3 the SIMPLE iteration diverges on this mesh (the oracle too, at
+        # 40^3 x 6 tets); 0.6 / 0.2 converges
+        line["simple_tets"] = simple_block(fc, args, dev, not args.no_cpu, args.simple_tet_n, PERTURB, cpu_skip=0,
+                                           tets=True, viscos=1.0 / 400.0, scheme=19, grad=1,
+                                           iters=args.simple_tet_iters, cpu_iters=1, urf=(0.6, 0.2))
     if args.simple_big_n > 0:
         line["simple_perturbed"] = simple_block(fc, args, dev, not args.no_cpu, args.simple_big_n, PERTURB,
                                                 cpu_skip=args.simple_big_cpu_skip)
@@ -487,6 +501,9 @@ def main():
     ap.add_argument("--simple-big-n", type=int, default=128,
                     help="cells per side of the SIMPLE cavity on the perturbed mesh (0: skip)")
     ap.add_argument("--simple-big-cpu-skip", type=int, default=2, help="untimed oracle iterations there")
+    ap.add_argument("--simple-tet-n", type=int, default=0,
+                    help="hexes per side of the tetrahedral SIMPLE cavity, 6 tets each (0: skip; 100 = 6M cells)")
+    ap.add_argument("--simple-tet-iters", type=int, default=100, help="timed SIMPLE iterations there")
     ap.add_argument("--simple-iters", type=int, default=20, help="timed SIMPLE iterations")
     ap.add_argument("--simple-skip", type=int, default=10, help="untimed SIMPLE iterations before them")
     ap.add_argument("--simple-cpu-iters", type=int, default=3, help="oracle SIMPLE iterations timed")

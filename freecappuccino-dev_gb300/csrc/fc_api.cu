@@ -318,6 +318,12 @@ int solve_global(fc_ctx* ctx, const char* solver, double* x, const double* b, do
 // tile, ring depth, estimated forward sweep microseconds, ring-served
 // entries, pushed entries, cross-tile entries (both triangles), stage depth,
 // most steps of a tile.
+extern "C" int fc_set_sweep_cap(fc_ctx* ctx, int rows) {
+  if (!ctx || rows < 0) return FC_ERR_BAD_INPUT;
+  ctx->sweep_cap = rows;
+  return FC_OK;
+}
+
 extern "C" int fc_mixed_colours(fc_ctx* ctx, int which, int* ncol) {
   if (!ctx || !ncol) return FC_ERR_BAD_INPUT;
   CsrSystem* s = which ? ctx->sys_ext : ctx->sys_mesh;

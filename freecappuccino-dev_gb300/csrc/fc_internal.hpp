@@ -155,6 +155,7 @@ struct fc_ctx {
   SimpleState* simple = nullptr;
   long long kernel_launches = 0;
   int tracing = 0, trace_blocks = 0, trace_cap = 0;
+  int sweep_cap = 0;   // rows per sweep step cap of the next pattern analyses (0: as wide as fits)
   DVec<unsigned long long> trace;
 };
 

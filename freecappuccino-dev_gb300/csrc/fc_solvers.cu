@@ -531,15 +531,27 @@ static int ordered_stages(const DevOrdered& D) {
   return 1;
 }
 
+// largest exchange and push blocks of a step (both directions)
+static void ordered_blocks(const OrderedSweep& O, int& xmax, int& pmax) {
+  xmax = pmax = 4;
+  for (int d = 0; d < 2; ++d)
+    for (int gs = 0; gs < O.nsteps; ++gs) {
+      xmax = std::max(xmax, O.dir[d].xv_ptr[gs + 1] - O.dir[d].xv_ptr[gs]);
+      pmax = std::max(pmax, O.dir[d].push_ptr[gs + 1] - O.dir[d].push_ptr[gs]);
+    }
+}
+
+// the sweep kernel's shared memory with two stage buffers fits the budget
+static bool ordered_fits(const OrderedSweep& O) {
+  int xmax, pmax;
+  ordered_blocks(O, xmax, pmax);
+  return osweep_smem_bytes<double>(O.R, 2, O.maxW, O.max_tile_steps, xmax, pmax) <= FC_SWEEP_SMEM;
+}
+
 static int upload_ordered(fc_ctx* ctx, const OrderedSweep& O, DevOrdered& D) {
   D.n = O.n; D.nE = O.nE; D.ntiles = O.ntiles; D.nsteps = O.nsteps; D.nlev = O.nlev; D.R = O.R; D.maxW = O.maxW;
   D.max_tile_steps = O.max_tile_steps;
-  D.xmax = D.pmax = 4;
-  for (int d = 0; d < 2; ++d)
-    for (int gs = 0; gs < O.nsteps; ++gs) {
-      D.xmax = std::max(D.xmax, O.dir[d].xv_ptr[gs + 1] - O.dir[d].xv_ptr[gs]);
-      D.pmax = std::max(D.pmax, O.dir[d].push_ptr[gs + 1] - O.dir[d].push_ptr[gs]);
-    }
+  ordered_blocks(O, D.xmax, D.pmax);
   D.K = ordered_stages(D);
   if (osweep_smem_bytes<double>(D.R, D.K, D.maxW, D.max_tile_steps, D.xmax, D.pmax) > FC_SWEEP_SMEM)
     return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "sweep tiles too wide for shared memory");
@@ -653,8 +665,16 @@ int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, c
   OrderedSweep O;
   SweepSchedule S;
   std::string err;
-  if (!build_ordered_sweep(n, ia.data(), ja.data(), dg.data(), ts.data(), tiles, xyz, FC_RING, O, S, err))
-    return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, err);
+  // the widest step must fit the shared-memory staging: if it does not, wide
+  // levels are split into narrower steps (more, shorter steps) until it does
+  int wmax = ctx->sweep_cap > 0 ? ctx->sweep_cap : 0;
+  for (;;) {
+    if (!build_ordered_sweep(n, ia.data(), ja.data(), dg.data(), ts.data(), tiles, xyz, FC_RING, O, S, err, wmax))
+      return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, err);
+    if (ordered_fits(O)) break;
+    wmax = wmax ? wmax / 2 : std::max(32, O.maxW / 2);
+    if (wmax < 32) return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "sweep steps too wide for shared memory");
+  }
   int st2 = upload_ordered(ctx, O, s->ord);
   if (st2) return st2;
   FC_CUDA_TRY(ctx, s->ia.alloc(n + 1));

@@ -363,13 +363,53 @@ int symmetric_levels(int n, const int* ia, const int* ja, const int* dg, std::ve
   return nlev;
 }
 
+// Splits the rows of every (tile, level) step wider than wmax into sub-levels:
+// lev(i) becomes lev(i) * M + chunk(i), chunk = rank of the row in its step /
+// wmax, then the levels are renumbered densely.  Rows of one level do not
+// depend on each other, so every dependency still points to a lower level.
+// The tiling is recomputed from the new levels (it may move rows between
+// tiles), so the split is repeated until no step is wider than wmax (a few
+// passes).  Returns the number of levels.
+static int split_wide_levels(int n, const int* ia, const int* ja, const int* dg, int ntiles, const double* xyz,
+                             int wmax, std::vector<int>& lev, int nlev) {
+  std::vector<int> code_tmp((size_t)ia[n], 0);
+  for (int pass = 0; pass < 8; ++pass) {
+    SweepSchedule T;
+    build_sweep_schedule(n, ia, ja, dg, lev, nlev, true, ntiles, xyz, T, code_tmp);
+    std::vector<int> chunk(n, 0);
+    int maxc = 0;
+    const int nsteps = T.tile_step_ptr[T.ntiles];
+    for (int gs = 0; gs < nsteps; ++gs) {
+      int cnt = 0;
+      for (int q = T.step_row_ptr[gs]; q < T.step_row_ptr[gs + 1]; ++q) {
+        const int i = T.rows[q];
+        if (i < 0) continue;
+        chunk[i] = cnt / wmax;
+        ++cnt;
+      }
+      maxc = std::max(maxc, (cnt - 1) / wmax);
+    }
+    if (maxc == 0) break;
+    const long long M = maxc + 1;
+    std::vector<long long> key(n);
+    for (int i = 0; i < n; ++i) key[i] = (long long)lev[i] * M + chunk[i];
+    std::vector<long long> uk(key);
+    std::sort(uk.begin(), uk.end());
+    uk.erase(std::unique(uk.begin(), uk.end()), uk.end());
+    for (int i = 0; i < n; ++i) lev[i] = (int)(std::lower_bound(uk.begin(), uk.end(), key[i]) - uk.begin());
+    nlev = (int)uk.size();
+  }
+  return nlev;
+}
+
 bool build_ordered_sweep(int n, const int* ia, const int* ja, const int* dg, const int* ts, int ntiles,
-                         const double* xyz, int R, OrderedSweep& O, SweepSchedule& S, std::string& err) {
+                         const double* xyz, int R, OrderedSweep& O, SweepSchedule& S, std::string& err, int wmax) {
   O = OrderedSweep();
   O.n = n;
   O.R = std::max(2, R);
   std::vector<int> lev;
-  const int nlev = symmetric_levels(n, ia, ja, dg, lev);
+  int nlev = symmetric_levels(n, ia, ja, dg, lev);
+  if (wmax > 0) nlev = split_wide_levels(n, ia, ja, dg, ntiles, xyz, wmax, lev, nlev);
   O.nlev = nlev;
   std::vector<int> code_tmp((size_t)ia[n], 0);
   build_sweep_schedule(n, ia, ja, dg, lev, nlev, true, ntiles, xyz, S, code_tmp);

@@ -110,8 +110,10 @@ int symmetric_levels(int n, const int* ia, const int* ja, const int* dg, std::ve
 
 // ia, ja, dg 0-based; ts (optional) the transpose slot of every entry;
 // ntiles the tile target; xyz (optional) row coordinates for the tiling; R
-// the ring depth.  S receives the underlying tiled schedule (for the
-// critical-path estimate).  Returns false with a message if a consistency
-// check fails.
+// the ring depth; wmax > 0 caps the rows of a step (a wider level of a tile
+// is split into consecutive steps, whose rows are independent).  S receives
+// the underlying tiled schedule (for the critical-path estimate).  Returns
+// false with a message if a consistency check fails.
 bool build_ordered_sweep(int n, const int* ia, const int* ja, const int* dg, const int* ts, int ntiles,
-                         const double* xyz, int R, OrderedSweep& O, SweepSchedule& S, std::string& err);
+                         const double* xyz, int R, OrderedSweep& O, SweepSchedule& S, std::string& err,
+                         int wmax = 0);

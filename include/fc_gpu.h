@@ -167,6 +167,13 @@ int fc_spmv(fc_ctx* ctx, int n, int nnz, const int* ia, const int* ja, const dou
  * ring-served entries, pushed entries, cross-tile entries (both triangles),
  * stage depth, most steps of a tile. */
 int fc_sweep_stats(fc_ctx* ctx, int which, double* out);
+/* Caps the rows of a sweep step in the pattern analyses that follow (rows
+ * >= 1; 0 restores the default, as wide as shared memory allows).  A level
+ * of a tile wider than the cap is split into consecutive steps; the
+ * preconditioner is unchanged.  The analysis applies the split by itself when
+ * a mesh's widest step does not fit (e.g. 6 million tetrahedra).  Tuning and
+ * testing only: no counterpart in the reference. */
+int fc_set_sweep_cap(fc_ctx* ctx, int rows);
 /* Colours of the multicolour ordering FC_PREC_MIXED_COLOURED uses for the
  * same systems (which as above); builds the ordering if no solve has yet.
  * Diagnostics only: no counterpart in the reference. */

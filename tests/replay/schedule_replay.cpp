@@ -58,11 +58,13 @@ int main(int argc, char** argv) {
   int nx = atoi(argv[1]), ny = atoi(argv[2]), nz = atoi(argv[3]), T = atoi(argv[4]);
   bool extra = argc > 5 && atoi(argv[5]);
   int R = argc > 6 ? atoi(argv[6]) : 4, K = argc > 7 ? atoi(argv[7]) : 4;
+  const int wmax = argc > 8 ? atoi(argv[8]) : 0;  // cap on the rows of a step (wide levels split)
   std::vector<int> ia, ja, dg; std::vector<double> a, xyz;
   make_pattern(nx, ny, nz, ia, ja, dg, a, xyz, 7, extra);
   int n = nx * ny * nz, nnz = ia[n];
   OrderedSweep O; SweepSchedule S; std::string err;
-  if (!build_ordered_sweep(n, ia.data(), ja.data(), dg.data(), nullptr, T, extra ? nullptr : xyz.data(), R, O, S, err)) {
+  if (!build_ordered_sweep(n, ia.data(), ja.data(), dg.data(), nullptr, T, extra ? nullptr : xyz.data(), R, O, S, err,
+                           wmax)) {
     printf("build failed: %s\n", err.c_str()); return 1;
   }
   printf("n=%d nnz=%d tiles=%d nsteps=%d nlev=%d maxW=%d maxsteps=%d ring=%lld pushed=%lld cross=%lld ovf=%d/%d\n", n, nnz,

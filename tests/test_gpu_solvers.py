@@ -174,6 +174,30 @@ def test_mixed_coloured_reaches_fp64_tolerance(ctx, oracle, fc, case):
     assert np.abs(r2).sum() / info2.res0_l1 < 1e-10
 
 
+@pytest.mark.parametrize("solver", ["iccg", "bicgstab", "gauss-seidel"])
+def test_capped_sweep_steps_keep_the_preconditioner(ctx, oracle, fc, solver):
+    """Sweep steps capped at 3 rows (levels split into consecutive steps, the
+    path wide tetrahedral meshes take): same iterations and fields as the
+    oracle."""
+    m, a, oc = mesh_case("hexcap", 9, 8, 7)
+    ia, ja, av, dg, b = laplacian_system(oc, mask=0b1)
+    if solver == "bicgstab":
+        _, _, av, _ = nonsymmetric_values(oc)
+    itr = 40
+    xo, _, info_o, _ = oracle.solve(solver, ia, ja, av, dg, np.zeros(len(dg)), b, itr, 0.0, 1e-30)
+    ctx.set_sweep_cap(3)
+    ctx.pattern_forget()
+    try:
+        x, _, info, st = ctx.csrsolve(solver, ia, ja, av, dg, np.zeros(len(dg)), b, itr, 0.0, 1e-30,
+                                      raise_on_error=False)
+        assert ctx.sweep_stats(1)["max_width"] <= 3
+    finally:
+        ctx.set_sweep_cap(0)
+        ctx.pattern_forget()
+    assert st >= 0 and info.itr_used == int(info_o[0])
+    assert np.abs(x - xo).max() <= 1e-9 * np.abs(xo).max()
+
+
 def test_failure_detection_nan_rhs(ctx, fc):
     m, a, oc = mesh_case("hex", 9, 7, 6)
     ia, ja, av, dg, b = laplacian_system(oc, mask=0b1)

@@ -24,7 +24,7 @@ def replay(tmp_path_factory):
     return exe
 
 
-# nx ny nz tiles [random couplings] [ring depth]
+# nx ny nz tiles [random couplings] [ring depth] [stage depth] [rows per step cap]
 CASES = [
     "12 10 8 16",          # structured, coordinate tiles
     "16 16 16 152",        # more tiles than chains per tile
@@ -34,6 +34,9 @@ CASES = [
     "7 3 1 2 1",
     "5 1 1 3",             # a single chain
     "1 1 1 1",             # one row
+    "30 30 30 152 0 4 4 3",  # steps capped at 3 rows: wide levels split into consecutive steps
+    "16 16 16 4 0 4 2 5",    # few wide tiles, ring depth 4, stage depth 2, steps of at most 5 rows
+    "20 7 5 40 1 4 4 4",     # capped steps with long-range couplings and overflow entries
 ]
 
 

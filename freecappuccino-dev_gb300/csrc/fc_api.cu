@@ -50,6 +50,7 @@ extern "C" int fc_init(int device, fc_ctx** out) {
 void fc_release_mesh(fc_ctx* ctx);
 void fc_fields_release(fc_ctx* ctx);
 void fc_simple_release(fc_ctx* ctx);
+void fc_adjoint_release(fc_ctx* ctx);
 
 extern "C" void fc_finalize(fc_ctx* ctx) {
   if (!ctx) return;
@@ -61,6 +62,7 @@ extern "C" void fc_finalize(fc_ctx* ctx) {
   fc_release_mesh(ctx);
   fc_fields_release(ctx);
   fc_simple_release(ctx);
+  fc_adjoint_release(ctx);
   cudaEventDestroy(ctx->ev0);
   cudaEventDestroy(ctx->ev1);
   cudaEventDestroy(ctx->sev0);

@@ -134,6 +134,7 @@ struct MeshDev {
 
 struct FieldStore;
 struct SimpleState;
+struct AdjState;
 
 struct fc_ctx {
   int device = 0;
@@ -153,6 +154,7 @@ struct fc_ctx {
   std::vector<CsrSystem*> sys_user;
   FieldStore* fields = nullptr;
   SimpleState* simple = nullptr;
+  AdjState* adj = nullptr;         // convection-diffusion adjoint (fc_adjoint.cu)
   long long kernel_launches = 0;
   int tracing = 0, trace_blocks = 0, trace_cap = 0;
   int sweep_cap = 0;   // rows per sweep step cap of the next pattern analyses (0: as wide as fits)

@@ -116,6 +116,9 @@ def lib():
         "fc_simple_iteration": (i, [vp, vp]),
         "fc_temperature_set_params": (i, [vp, vp, vp]),
         "fc_calculate_temperature": (i, [vp, i, vp]),
+        "fc_cd_assemble": (i, [vp, vp, vp]),
+        "fc_cd_solve": (i, [vp, vp, i, d, C.POINTER(SolveInfo)]),
+        "fc_cd_adjoint": (i, [vp, vp, vp, vp, i, d, C.POINTER(SolveInfo)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -157,6 +160,28 @@ def _i32(x):
     if hasattr(x, "data_ptr") or isinstance(x, int):
         return x
     return np.ascontiguousarray(x, dtype=np.int32)
+
+
+def stream_function_fluxes(arrays, psi):
+    """Face volume fluxes of the velocity curl(psi(x, y, z) e_z) through every
+    face of a mesh given by Mesh.arrays(): by Stokes' theorem the flux through
+    a face is the circulation of psi e_z around its edges, here with psi
+    linear along each edge, in the face's node order (which orients its area
+    vector).  Every edge is shared by the faces around it with opposite
+    orientations, so the fluxes of every cell sum to zero up to rounding."""
+    x, y, z = arrays["x"], arrays["y"], arrays["z"]
+    nn = np.asarray(arrays["nnodes"])
+    nodes = np.asarray(arrays["nodes"]).reshape(-1, NOMAX) - 1
+    ps = psi(x, y, z)
+    flux = np.zeros(len(nn))
+    for k in range(NOMAX):
+        on = k < nn
+        a = nodes[:, k]
+        b = np.where(k + 1 < nn, nodes[:, (k + 1) % NOMAX], nodes[:, 0])
+        a = np.where(on, a, 0)
+        b = np.where(on, b, 0)
+        flux += np.where(on, 0.5 * (ps[a] + ps[b]) * (z[b] - z[a]), 0.0)
+    return flux
 
 
 class SimpleParams(C.Structure):
@@ -550,6 +575,28 @@ class Context:
         r = np.zeros(4)
         self._check(self.L.fc_simple_iteration(self.h, _ptr(r)), "fc_simple_iteration")
         return r
+
+    # ------------------------------------------ convection-diffusion adjoint
+    def cd_assemble(self, gamma, source):
+        self._check(self.L.fc_cd_assemble(self.h, _ptr(_f64(gamma)), _ptr(_f64(source))), "fc_cd_assemble")
+
+    def cd_solve(self, itr_max=2000, tol_rel=1e-12):
+        """Returns (phi, info)."""
+        phi = np.zeros(self.mesh.numCells)
+        info = SolveInfo()
+        st = self.L.fc_cd_solve(self.h, _ptr(phi), int(itr_max), float(tol_rel), C.byref(info))
+        self._check(st, "fc_cd_solve")
+        return phi, info
+
+    def cd_adjoint(self, dJdphi, itr_max=2000, tol_rel=1e-12):
+        """Returns (lambda, dJ/dgamma, info)."""
+        n = self.mesh.numCells
+        lam, grad = np.zeros(n), np.zeros(n)
+        info = SolveInfo()
+        st = self.L.fc_cd_adjoint(self.h, _ptr(_f64(dJdphi)), _ptr(lam), _ptr(grad), int(itr_max), float(tol_rel),
+                                  C.byref(info))
+        self._check(st, "fc_cd_adjoint")
+        return lam, grad, info
 
     # ------------------------------------------------------- temperature
     def temperature_params(self, prm, bc_dfraction=None):

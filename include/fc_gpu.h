@@ -350,6 +350,30 @@ int fc_temperature_set_params(fc_ctx* ctx, const fc_temperature_params* prm, con
  * setup (srdw covers 'wall' patches only) and is not accepted. */
 int fc_calculate_temperature(fc_ctx* ctx, int solve, double* resor7);
 
+/* ---------------------------------------------------------------------------
+ * Discrete adjoint of steady scalar convection-diffusion.  No counterpart in
+ * the reference; the operator is the implicit part of its facefluxsc
+ * (scalar_fluxes.f90:32-141, :256-337) with temperature.f90's main diagonal.
+ * --------------------------------------------------------------------------- */
+
+/* A(gamma) phi = source * vol on the current mesh: upwind convection of the
+ * face fluxes in field "flmass", diffusion gamma_f Df with gamma_f the
+ * face-interpolated cell diffusivity (facint), phi = 0 on every boundary face
+ * (coefficient gamma_P |S|^2 / (d.S)), no deferred or non-orthogonal
+ * correction.  gamma, source: numCells values, host or device.  The matrix
+ * goes to the mesh's matrix, the right-hand side to field "su". */
+int fc_cd_assemble(fc_ctx* ctx, const double* gamma, const double* source);
+/* Solves the assembled system with BiCGStab from phi = 0 to the relative
+ * tolerance (the reference's L1 test); phi (numCells, host or device, may be
+ * NULL) receives the solution, which is also kept for fc_cd_adjoint. */
+int fc_cd_solve(fc_ctx* ctx, double* phi, int itr_max, double tol_rel, fc_solve_info* info);
+/* Given dJ/dphi (numCells) for the last solution: solves A^T lambda = dJ/dphi
+ * (BiCGStab on the transposed values, same pattern) and returns
+ * dJ/dgamma_c = -lambda^T (dA/dgamma_c) phi from a reverse face loop that
+ * recomputes the face coefficients.  lambda, dJdgamma may be NULL. */
+int fc_cd_adjoint(fc_ctx* ctx, const double* dJdphi, double* lambda, double* dJdgamma, int itr_max, double tol_rel,
+                  fc_solve_info* info);
+
 #ifdef __cplusplus
 }
 #endif

@@ -136,6 +136,16 @@ int calcp_simple(Case& c);
 // solve == false only the assembly (through the under-relaxation) is done.
 int calculate_temperature(Case& c, bool solve);
 void continuityErrors(Case& c);
+// Steady convection-diffusion of a passive scalar with the implicit part of
+// facefluxsc (scalar_fluxes.f90:32-141, :256-337): upwind convection,
+// diffusion gamma_f Df with gamma_f = gamma_P (1 - facint) + gamma_N facint,
+// phi = 0 on every boundary face (sp += gamma_P |S|^2 / (d.S)), main
+// diagonal = sp - sum of the row's off-diagonals (temperature.f90:359-361).
+// a <- A, su <- source * vol.  gamma, source: 1-based, numCells.
+void cd_assemble(Case& c, const std::vector<double>& gamma, const std::vector<double>& source);
+// dJ/dgamma_c = -lambda^T (dA/dgamma_c) phi, the reverse face loop of
+// cd_assemble: out (1-based, numCells)
+void cd_gradient(Case& c, const std::vector<double>& phi, const std::vector<double>& lambda, std::vector<double>& out);
 double face_value(Case& c, int ijp, int ijn, double xf, double yf, double zf, double lambda,
                   const std::vector<double>& u, std::vector<double>& dUdxi, int scheme);
 

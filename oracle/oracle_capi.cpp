@@ -231,6 +231,22 @@ int orc_calcuvw(void* h) { return calcuvw(*(Case*)h); }
 int orc_calcp_simple(void* h) { return calcp_simple(*(Case*)h); }
 int orc_calculate_temperature(void* h, int solve) { return calculate_temperature(*(Case*)h, solve != 0); }
 
+// gamma, source: numCells (0-based memory); a <- A, su <- source * vol
+int orc_cd_assemble(void* h, const double* gamma, const double* source) {
+  Case& c = *(Case*)h;
+  cd_assemble(c, pad1(gamma, c.numCells), pad1(source, c.numCells));
+  return 0;
+}
+
+// out (numCells) = dJ/dgamma for phi, lambda (numCells)
+int orc_cd_gradient(void* h, const double* phi, const double* lambda, double* out) {
+  Case& c = *(Case*)h;
+  std::vector<double> o;
+  cd_gradient(c, pad1(phi, c.numCells), pad1(lambda, c.numCells), o);
+  std::memcpy(out, o.data() + 1, sizeof(double) * c.numCells);
+  return 0;
+}
+
 // one SIMPLE outer iteration (main.f90:159-165); resor4 gets resor(1..4);
 // elapsed_s gets the wall time of the iteration
 int orc_simple_iteration(void* h, double* resor4, double* elapsed_s) {

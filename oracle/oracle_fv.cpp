@@ -884,4 +884,60 @@ int calculate_temperature(Case& c, bool solve) {
   return st;
 }
 
+// ---------------------------------------------- convection-diffusion adjoint
+void cd_assemble(Case& c, const std::vector<double>& gamma, const std::vector<double>& source) {
+  const int nC = c.numCells;
+  std::fill(c.a.begin(), c.a.end(), 0.0);
+  std::fill(c.su.begin(), c.su.end(), 0.0);
+  std::fill(c.sp.begin(), c.sp.end(), 0.0);
+  for (int i = 1; i <= c.numInnerFaces; ++i) {
+    const int ijp = c.owner[i], ijn = c.neighbour[i];
+    const double gf = gamma[ijp] * (1.0 - c.facint[i]) + gamma[ijn] * c.facint[i];
+    const double de = gf * c.Df[i];
+    const double fm = c.flmass[i];
+    c.a[c.ijk[i]] = -de + std::min(fm, 0.0);
+    c.a[c.jik[i]] = -de - std::max(fm, 0.0);
+  }
+  for (int ib = 1; ib <= c.numBoundaries; ++ib)
+    for (int i = 1; i <= c.nfaces[ib]; ++i) {
+      const int iface = c.startFace[ib] + i, ijp = c.owner[iface];
+      const double xpn = c.xf[iface] - c.xc[ijp], ypn = c.yf[iface] - c.yc[ijp], zpn = c.zf[iface] - c.zc[ijp];
+      const double arx = c.arx[iface], ary = c.ary[iface], arz = c.arz[iface];
+      const double dfi = (arx * arx + ary * ary + arz * arz) / (xpn * arx + ypn * ary + zpn * arz);
+      c.sp[ijp] = c.sp[ijp] + gamma[ijp] * dfi;
+    }
+  for (int inp = 1; inp <= nC; ++inp) {
+    double s = 0.0;
+    for (int k = c.ia[inp]; k <= c.ia[inp + 1] - 1; ++k) s += c.a[k];
+    const double off = s - c.a[c.diag[inp]];
+    c.a[c.diag[inp]] = c.sp[inp] - off;
+    c.su[inp] = source[inp] * c.vol[inp];
+  }
+}
+
+void cd_gradient(Case& c, const std::vector<double>& phi, const std::vector<double>& lambda, std::vector<double>& out) {
+  const int nC = c.numCells;
+  out.assign(nC + 1, 0.0);
+  // face order per cell, as the device gathers it: inner faces ascending,
+  // then boundary faces ascending
+  std::vector<double> sf(c.numInnerFaces + 1);
+  for (int i = 1; i <= c.numInnerFaces; ++i) {
+    const int ijp = c.owner[i], ijn = c.neighbour[i];
+    sf[i] = (lambda[ijp] - lambda[ijn]) * (phi[ijp] - phi[ijn]) * c.Df[i];
+  }
+  for (int i = 1; i <= c.numInnerFaces; ++i) {
+    const int ijp = c.owner[i], ijn = c.neighbour[i];
+    out[ijp] = out[ijp] - sf[i] * (1.0 - c.facint[i]);
+    out[ijn] = out[ijn] - sf[i] * c.facint[i];
+  }
+  for (int ib = 1; ib <= c.numBoundaries; ++ib)
+    for (int i = 1; i <= c.nfaces[ib]; ++i) {
+      const int iface = c.startFace[ib] + i, ijp = c.owner[iface];
+      const double xpn = c.xf[iface] - c.xc[ijp], ypn = c.yf[iface] - c.yc[ijp], zpn = c.zf[iface] - c.zc[ijp];
+      const double arx = c.arx[iface], ary = c.ary[iface], arz = c.arz[iface];
+      const double dfi = (arx * arx + ary * ary + arz * arz) / (xpn * arx + ypn * ary + zpn * arz);
+      out[ijp] = out[ijp] - lambda[ijp] * phi[ijp] * dfi;
+    }
+}
+
 }  // namespace orc

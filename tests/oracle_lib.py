@@ -50,6 +50,8 @@ def lib(fast=False):
     L.orc_simple_iteration.argtypes = [C.c_void_p, dp, dp]
     L.orc_case_set_bcdfrac_t.argtypes = [C.c_void_p, C.c_int, C.c_double]
     L.orc_calculate_temperature.argtypes = [C.c_void_p, C.c_int]
+    L.orc_cd_assemble.argtypes = [C.c_void_p, dp, dp]
+    L.orc_cd_gradient.argtypes = [C.c_void_p, dp, dp, dp]
     L.orc_solve.argtypes = [C.c_char_p, C.c_int, C.c_int, ip, ip, dp, ip, dp, dp, dp, C.c_int, C.c_double,
                             C.c_double, dp]
     L.orc_dic_setup.argtypes = [C.c_int, ip, ip, dp, ip, dp, C.c_int]
@@ -162,6 +164,15 @@ class Case:
 
     def calculate_temperature(self, solve=True):
         return self.L.orc_calculate_temperature(self.h, 1 if solve else 0)
+
+    def cd_assemble(self, gamma, source):
+        """Implicit convection-diffusion operator into a, source*vol into su."""
+        self.L.orc_cd_assemble(self.h, _f64(gamma), _f64(source))
+
+    def cd_gradient(self, phi, lam):
+        out = np.zeros(self.numCells)
+        self.L.orc_cd_gradient(self.h, _f64(phi), _f64(lam), out)
+        return out
 
     def simple_iteration(self):
         r = np.zeros(4)

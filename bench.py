@@ -331,6 +331,76 @@ def spmv_leg(fc, ctx, nC, calls):
             "note": "per call, host work and the call's synchronisation included (upper bound on the kernel)"}
 
 
+def adjoint_block(fc, args, dev):
+    """C4: discrete adjoint of steady convection-diffusion on the n^3
+    perturbed hex mesh of [0, 2 pi]^3: u = 0.5 (sin x cos y, -cos x sin y, 0)
+    (face fluxes of the stream function), lognormal diffusivity (mu -4,
+    sigma 0.5, seed 46), a Gaussian source blob at (pi, pi, pi) with sigma 0.5,
+    J = volume-weighted mean of phi^2 over x > pi.  Times the forward solve and
+    the adjoint (transposed solve + reverse face loop) and checks dJ/dgamma by
+    central differences of J along fd_dirs smooth random directions
+    gamma (1 +- h v), v a product of random low-frequency sines (seed 47),
+    h = 1e-2, each side a full re-solve.  (Single-cell differences need
+    solves far below the residual at which BiCGStab as the reference writes it
+    stalls at this size; they are checked on small meshes by the tests.)"""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from cd_cases import TWO_PI, cd_inputs, cd_objective, cd_source
+    n = args.adjoint_n
+    m = fc.Mesh.box(n, n, n, TWO_PI, TWO_PI, TWO_PI, perturb=PERTURB, seed=MESH_SEED)
+    a, fm, gamma = cd_inputs(fc, m)
+    ctx = fc.Context(dev)
+    ctx.set_mesh(m)
+    ctx.field_set("flmass", fm)
+    xc, yc, zc = ctx.geometry("xc"), ctx.geometry("yc"), ctx.geometry("zc")
+    vol = ctx.geometry("vol")
+    src = cd_source(xc, yc, zc)
+    tol, itmax = 1e-6, 2000
+
+    def J_of(gm):
+        ctx.cd_assemble(gm, src)
+        phi, info = ctx.cd_solve(itmax, tol)
+        if info.status != 0:
+            raise RuntimeError(f"convection-diffusion solve status {info.status}")
+        return phi, info
+
+    for _ in range(2):  # warm-up
+        phi, finfo = J_of(gamma)
+        J, g = cd_objective(phi, vol, xc)
+        lam, grad, ainfo = ctx.cd_adjoint(g, itmax, tol)
+    ctx.sync()
+    ctx.event(0)
+    ctx.cd_assemble(gamma, src)
+    ctx.event(1)
+    asm_ms = ctx.elapsed_ms()
+    phi, finfo = J_of(gamma)
+    J, g = cd_objective(phi, vol, xc)
+    ctx.event(0)
+    lam, grad, ainfo = ctx.cd_adjoint(g, itmax, tol)
+    ctx.event(1)
+    adj_ms = ctx.elapsed_ms()
+    if ainfo.status != 0:
+        raise RuntimeError(f"adjoint solve status {ainfo.status}")
+    rng = np.random.default_rng(47)
+    h, rel = 1e-2, []
+    for _ in range(args.adjoint_fd_dirs):
+        k = rng.integers(1, 4, 3)
+        ph = rng.uniform(0.0, 2.0 * np.pi, 3)
+        v = np.sin(k[0] * xc + ph[0]) * np.sin(k[1] * yc + ph[1]) * np.sin(k[2] * zc + ph[2])
+        Jp = cd_objective(J_of(gamma * (1.0 + h * v))[0], vol, xc)[0]
+        Jm = cd_objective(J_of(gamma * (1.0 - h * v))[0], vol, xc)[0]
+        fd = (Jp - Jm) / (2.0 * h)
+        ad = float(np.dot(grad, gamma * v))
+        rel.append(abs(fd - ad) / max(abs(fd), 1e-300))
+    ctx.close()
+    return {"workload": f"{n}^3 perturbed hexes on [0,2pi]^3, steady convection-diffusion, lognormal gamma, "
+                        f"J = mean phi^2 over x > pi", "cells": m.numCells, "J": J,
+            "assemble_ms": asm_ms, "forward_solve_ms": finfo.ms, "forward_iterations": finfo.itr_used,
+            "adjoint_ms": adj_ms, "adjoint_solve_ms": ainfo.ms, "adjoint_iterations": ainfo.itr_used,
+            "solver": f"BiCGStab(DILU) FP64 to {tol:g} relative L1 (forward and transposed)",
+            "fd_directions": len(rel), "fd_step": "gamma (1 +- 1e-2 v), full re-solves",
+            "fd_max_rel_err": float(max(rel)), "fd_median_rel_err": float(np.median(rel))}
+
+
 def run_gpu(args, rank, world, dist):
     fc = load_fc()
     dev = int(os.environ.get("LOCAL_RANK", "0"))
@@ -471,6 +541,8 @@ def run_gpu(args, rank, world, dist):
         line["cpu_baseline"] = cpu_baseline(ia, ja, a_host, dg, b, iters, args.ref_sample)
     if args.simple_n > 0:
         line["simple"] = simple_block(fc, args, dev, not args.no_cpu, args.simple_n)
+    if args.adjoint_n > 0:
+        line["adjoint"] = adjoint_block(fc, args, dev)
     if args.simple_tet_n > 0:
         # C5: 6 tets per perturbed hex, Re = 400, LSQ gradients, boundedLinearUpwind.  With the cavity
         # input's urfU 0.8 / urfP 0.3 the SIMPLE iteration diverges on this mesh (the oracle too, at
@@ -504,6 +576,8 @@ def main():
     ap.add_argument("--simple-tet-n", type=int, default=0,
                     help="hexes per side of the tetrahedral SIMPLE cavity, 6 tets each (0: skip; 100 = 6M cells)")
     ap.add_argument("--simple-tet-iters", type=int, default=100, help="timed SIMPLE iterations there")
+    ap.add_argument("--adjoint-n", type=int, default=96, help="cells per side of the adjoint case (0: skip)")
+    ap.add_argument("--adjoint-fd-dirs", type=int, default=32, help="directions of the finite-difference check")
     ap.add_argument("--simple-iters", type=int, default=20, help="timed SIMPLE iterations")
     ap.add_argument("--simple-skip", type=int, default=10, help="untimed SIMPLE iterations before them")
     ap.add_argument("--simple-cpu-iters", type=int, default=3, help="oracle SIMPLE iterations timed")

@@ -158,6 +158,140 @@ def cpu_baseline(ia, ja, a, diag, b, iters_per_solve, sample_iters):
                       f"in {dt:.1f} s, scaled to the {iters_per_solve} iterations of a full solve"}
 
 
+def batch_block(fc, args, dev):
+    """C3b: independent steady convection-diffusion problems solved together.
+    count problems (default 64): n^3 perturbed hex meshes of [0, 2 pi]^3 with
+    n ~ U{20..80} (seed 44), cell Peclet number U h / gamma ~ lognormal(0, 1)
+    (seed 45), the C4 velocity field and source (tests/cd_cases.py); BiCGStab
+    (DILU) to batch_tol relative L1 per problem.  Legs, all on device-resident
+    inputs: one batched launch in FP64 (planner's model plan); the mixed
+    batched solve (FP32 inner BiCGStab, FP64 refinement) on the model plan
+    and on the autotuned plan; the same problems solved one after another (a
+    batch of one each) in FP64 and mixed; the tuned mixed batch end to end
+    from host buffers.  The CPU estimate is the oracle's BiCGStab (one core)
+    timed on the smallest problems and scaled by rows x iterations."""
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    from cd_cases import cd_batch_sizes, cd_batch_system
+    ns, pe = cd_batch_sizes(args.batch_count)
+    gen = fc.Context(dev)
+    probs = [cd_batch_system(fc, gen, int(n), float(p), MESH_SEED + k) for k, (n, p) in enumerate(zip(ns, pe))]
+    gen.close()
+    np_ = len(probs)
+    rows = np.array([len(p[2]) for p in probs])
+    td = torch.device("cuda", dev)
+    da = [torch.from_numpy(p[3]).to(td) for p in probs]
+    db = [torch.from_numpy(p[4]).to(td) for p in probs]
+    xbuf = torch.zeros(int(rows.sum()), dtype=torch.float64, device=td)
+    offs = np.concatenate([[0], np.cumsum(rows)])
+    dx = [xbuf[offs[k]:offs[k + 1]] for k in range(np_)]
+    torch.cuda.synchronize()
+    ctx = fc.Context(dev)
+    tol, itmax, reps = args.batch_tol, 4000, max(1, args.batch_reps)
+
+    def make(idx):
+        B = fc.Batch(ctx)
+        for k in idx:
+            ia, ja, dg, a, b, xyz = probs[k]
+            B.add(ia, ja, dg, xyz)
+        B.plan()
+        return B
+
+    def run(B, idx):
+        xbuf.zero_()
+        torch.cuda.synchronize()
+        _, infos, st = B.solve([da[k] for k in idx], [dx[k] for k in idx], [db[k] for k in idx], itmax, 0.0, tol,
+                               raise_on_error=False)
+        if st < 0:
+            raise RuntimeError(f"batched solve status {st}: {ctx.error()}")
+        return infos
+
+    def timed(groups):
+        infos = [None] * np_
+        for B, idx in groups:  # warm-up
+            run(B, idx)
+        ctx.sync()
+        ctx.event(0)
+        for _ in range(reps):
+            xbuf.zero_()
+            torch.cuda.synchronize()
+            for B, idx in groups:
+                _, inf, st = B.solve([da[k] for k in idx], [dx[k] for k in idx], [db[k] for k in idx], itmax, 0.0,
+                                     tol, raise_on_error=False)
+                if st < 0:
+                    raise RuntimeError(f"batched solve status {st}: {ctx.error()}")
+                for k, i in zip(idx, inf):
+                    infos[k] = i
+        ctx.event(1)
+        return ctx.elapsed_ms() / reps, infos
+
+    allidx = list(range(np_))
+    out = {"problems": np_, "cells": int(rows.sum()), "cells_per_side": [int(v) for v in ns],
+           "tol_rel": tol, "solver": "BiCGStab (DILU)"}
+    ctx.set_precision(fc.FC_PREC_FP64)
+    B = make(allidx)
+    out["tiles_model"] = [int(v) for v in B.tiles()]
+    out["fp64_batched_ms"], inf64 = timed([(B, allidx)])
+    x64 = [dx[k].cpu().numpy() for k in allidx]
+    singles = [(make([k]), [k]) for k in allidx]
+    out["fp64_sequential_ms"], _ = timed(singles)
+    it64 = np.array([i.itr_used for i in inf64])
+    out["fp64_iterations"] = {"min": int(it64.min()), "median": float(np.median(it64)), "max": int(it64.max()),
+                              "not_converged": int(sum(i.status != 0 for i in inf64))}
+    ctx.set_precision(fc.FC_PREC_MIXED, args.batch_inner_tol, 0)
+    out["inner_tol"] = args.batch_inner_tol
+    out["mixed_batched_model_ms"], _ = timed([(B, allidx)])
+    a_h = [p[3] for p in probs]
+    b_h = [p[4] for p in probs]
+    x0 = [np.zeros(len(p[2])) for p in probs]
+    tiles, tune_ms = B.tune(a_h, x0, b_h, itmax, 0.0, tol, rounds=args.batch_tune_rounds)
+    out["tiles_tuned"] = [int(v) for v in tiles]
+    launches0 = ctx.kernel_launches()
+    out["mixed_batched_tuned_ms"], infm = timed([(B, allidx)])
+    out["gpu_launches_per_batched_mixed_solve"] = (ctx.kernel_launches() - launches0) / (reps + 1)
+    xm = [dx[k].cpu().numpy() for k in allidx]
+    out["mixed_max_rel_diff_vs_fp64"] = float(max(np.abs(u - v).max() / np.abs(v).max() for u, v in zip(xm, x64)))
+    out["mixed_outer_steps_max"] = int(max(i.outer_iterations for i in infm))
+    out["mixed_not_converged"] = int(sum(i.status != 0 for i in infm))
+    out["mixed_sequential_ms"], _ = timed(singles)
+    # end to end: host buffers in, solutions back
+    ctx.sync()
+    ctx.event(0)
+    B.solve(a_h, x0, b_h, itmax, 0.0, tol)
+    ctx.event(1)
+    out["mixed_batched_e2e_ms"] = ctx.elapsed_ms()
+    out["e2e_h2d_bytes"] = int(sum(p[3].nbytes + 2 * p[4].nbytes for p in probs))
+    out["e2e_d2h_bytes"] = int(sum(p[4].nbytes for p in probs))
+    out["speedup_mixed_batched_vs_fp64_sequential"] = out["fp64_sequential_ms"] / out["mixed_batched_tuned_ms"]
+    for b_, _ in singles:
+        b_.close()
+    B.close()
+    ctx.set_precision(fc.FC_PREC_FP64)
+    ctx.close()
+    if not args.no_cpu:
+        order = np.argsort(rows)
+        done_rows_iters, t_cpu, used = 0.0, 0.0, []
+        for k in order:
+            ia, ja, dg, a, b, _ = probs[k]
+            t0 = time.perf_counter()
+            x, r0, info, st = oracle_lib.solve("bicgstab", ia, ja, a, dg, np.zeros(len(dg)), b, itmax, 0.0, tol,
+                                               fast=True)
+            t_cpu += time.perf_counter() - t0
+            done_rows_iters += len(dg) * max(1, int(info[0]))
+            used.append(int(ns[k]))
+            if t_cpu > args.batch_cpu_seconds:
+                break
+        per = t_cpu / done_rows_iters
+        est = per * float((rows * it64).sum()) * 1e3
+        out["cpu_sequential_ms_est"] = est
+        out["cpu_sample"] = (f"oracle BiCGStab (C++ restatement, -O3, one thread) on the {len(used)} smallest "
+                             f"problems (n = {used[0]}..{used[-1]}) in {t_cpu:.1f} s, scaled by rows x the FP64 "
+                             f"GPU iteration counts of all {np_} problems")
+        out["speedup_mixed_batched_vs_cpu"] = est / out["mixed_batched_tuned_ms"]
+    return out
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -209,7 +343,7 @@ def cavity_fields(m, nT, nC):
 
 
 def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None, tets=False, viscos=0.01, scheme=1, grad=0,
-                 iters=None, cpu_iters=None, urf=(0.8, 0.3)):
+                 iters=None, cpu_iters=None, urf=(0.8, 0.3), momentum_batch=False):
     """SIMPLE iterations per second on the n^3 lid-driven cavity (unit cube,
     nu = 0.01, central differencing with deferred correction, Gauss gradients,
     BiCGStab(DILU) for U, ICCG(DIC) for p, the settings of
@@ -256,6 +390,37 @@ def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None, tets=Fa
         out[key] = 1e3 / ms
         out[key + "_ms_per_iteration"] = ms
         out[key + "_resor"] = [float(v) for v in res]
+    if momentum_batch:
+        # C3a: the three momentum solves of calcuvw (shared off-diagonals, three
+        # diagonals and sources) one after another and as one batched launch,
+        # on the field developed by the untimed iterations; calcuvw = assembly +
+        # the three solves, timed alone, then whole SIMPLE iterations
+        ctx.set_precision(fc.FC_PREC_FP64)
+        reset()
+        for _ in range(args.simple_skip):
+            ctx.simple_iteration()
+        c3 = {"workload": "calcuvw on the developed field: momentum assembly + U, V, W BiCGStab(DILU) solves, "
+                          f"maxiterU {prm.maxiterU}, tolRelU {prm.tolRelU:g}"}
+        for on, key in ((False, "sequential"), (True, "batched")):
+            ctx.simple_batched_momentum(on)
+            ctx.calcuvw()  # warm-up (builds the three systems on the first batched call)
+            ctx.sync()
+            ctx.event(0)
+            for _ in range(args.momentum_calls):
+                ctx.calcuvw()
+            ctx.event(1)
+            c3[key + "_calcuvw_ms"] = ctx.elapsed_ms() / args.momentum_calls
+        ctx.event(0)
+        for _ in range(iters):
+            res = ctx.simple_iteration()
+        ctx.event(1)
+        ms = ctx.elapsed_ms() / iters
+        ctx.simple_batched_momentum(False)
+        c3["speedup_calcuvw"] = c3["sequential_calcuvw_ms"] / c3["batched_calcuvw_ms"]
+        out["momentum_batched"] = c3
+        out["value_batched_momentum"] = 1e3 / ms
+        out["value_batched_momentum_ms_per_iteration"] = ms
+        out["value_batched_momentum_resor"] = [float(v) for v in res]
     out["iterations_timed"] = f"{iters} after {args.simple_skip} untimed"
     out["mixed_note"] = ("ICCG for p with the multicolour FP32 inner solve, capped at maxiterP iterations as the "
                          "reference caps it: it reduces the p residual less per SIMPLE iteration than the "
@@ -543,6 +708,8 @@ def run_gpu(args, rank, world, dist):
         line["simple"] = simple_block(fc, args, dev, not args.no_cpu, args.simple_n)
     if args.adjoint_n > 0:
         line["adjoint"] = adjoint_block(fc, args, dev)
+    if args.batch_count > 0:
+        line["batch"] = batch_block(fc, args, dev)
     if args.simple_tet_n > 0:
         # C5: 6 tets per perturbed hex, Re = 400, LSQ gradients, boundedLinearUpwind.  With the cavity
         # input's urfU 0.8 / urfP 0.3 the SIMPLE iteration diverges on this mesh (the oracle too, at
@@ -552,7 +719,7 @@ def run_gpu(args, rank, world, dist):
                                            iters=args.simple_tet_iters, cpu_iters=1, urf=(0.6, 0.2))
     if args.simple_big_n > 0:
         line["simple_perturbed"] = simple_block(fc, args, dev, not args.no_cpu, args.simple_big_n, PERTURB,
-                                                cpu_skip=args.simple_big_cpu_skip)
+                                                cpu_skip=args.simple_big_cpu_skip, momentum_batch=True)
     print(json.dumps(line), flush=True)
 
 
@@ -578,6 +745,13 @@ def main():
     ap.add_argument("--simple-tet-iters", type=int, default=100, help="timed SIMPLE iterations there")
     ap.add_argument("--adjoint-n", type=int, default=96, help="cells per side of the adjoint case (0: skip)")
     ap.add_argument("--adjoint-fd-dirs", type=int, default=32, help="directions of the finite-difference check")
+    ap.add_argument("--momentum-calls", type=int, default=5, help="timed calcuvw calls of the C3a leg")
+    ap.add_argument("--batch-count", type=int, default=64, help="problems of the batched leg (0: skip)")
+    ap.add_argument("--batch-tol", type=float, default=1e-8, help="relative L1 tolerance there")
+    ap.add_argument("--batch-inner-tol", type=float, default=1e-4, help="FP32 inner tolerance there")
+    ap.add_argument("--batch-reps", type=int, default=2, help="timed repetitions of each batched leg")
+    ap.add_argument("--batch-tune-rounds", type=int, default=3, help="autotuner plans tried")
+    ap.add_argument("--batch-cpu-seconds", type=float, default=10.0, help="oracle time of the CPU estimate")
     ap.add_argument("--simple-iters", type=int, default=20, help="timed SIMPLE iterations")
     ap.add_argument("--simple-skip", type=int, default=10, help="untimed SIMPLE iterations before them")
     ap.add_argument("--simple-cpu-iters", type=int, default=3, help="oracle SIMPLE iterations timed")

@@ -169,6 +169,10 @@ static void print_report(const std::string& solver, const char* chvar, const Sol
   std::fflush(stdout);
 }
 
+void report_solve(fc_ctx* ctx, const char* solver, const char* chvar, const SolveResult& r) {
+  if (ctx->verbosity) print_report(solver ? solver : "", chvar, r);
+}
+
 static void fill_info(fc_solve_info* info, const SolveResult& r) {
   if (!info) return;
   info->status = r.status;

@@ -47,13 +47,19 @@ struct DVec {
 // Cross-block control block of the persistent solver kernels: a bounded
 // generation barrier, per-block partial sums and a sticky status word.
 struct GridCtl {
-  unsigned* bar;     // [0] arrival count, [1] generation
-  double* part;      // nblocks * FC_NPART partial sums
-  int* status;       // 0 or a negative FC_* code (first error sticks)
-  double* out;       // scalar results written by block 0 (FC_OUT_*)
+  unsigned* bar = nullptr;     // [0] arrival count, [1] generation
+  double* part = nullptr;      // nblocks * FC_NPART partial sums
+  int* status = nullptr;       // 0 or a negative FC_* code (first error sticks)
+  double* out = nullptr;       // scalar results written by block 0 (FC_OUT_*)
+  // the blocks the kernel runs on: [base, base + nb) of the launch grid
+  // (nb = 0: the whole grid).  A batched launch gives every problem its own
+  // group of blocks, barrier and partial sums.
+  int base = 0, nb = 0;
 };
 #define FC_NPART 4
-enum { FC_OUT_RES0 = 0, FC_OUT_RESL, FC_OUT_FACTOR, FC_OUT_RESOR, FC_OUT_ITR, FC_OUT_EARLY, FC_OUT_BAD, FC_OUT_N = 16 };
+// FC_OUT_GT: device time of a batched group (ns, written by its first block)
+enum { FC_OUT_RES0 = 0, FC_OUT_RESL, FC_OUT_FACTOR, FC_OUT_RESOR, FC_OUT_ITR, FC_OUT_EARLY, FC_OUT_BAD, FC_OUT_GT,
+       FC_OUT_N = 16 };
 
 // device copy of a schedule-ordered sweep structure (fc_schedule.hpp)
 struct DevOrdered {
@@ -166,8 +172,10 @@ int fc_fail_msg(fc_ctx* ctx, int code, const std::string& msg);
 
 // pattern analysis (host) + upload
 // xyz: optional row coordinates (3*n, x then y then z) used to cut the sweep tiles
+// tiles > 0: that many sweep tiles (at most one per SM) instead of the
+// count the critical-path estimate picks
 int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, const int* ja1, const int* diag1,
-                    const double* xyz = nullptr);
+                    const double* xyz = nullptr, int tiles = 0);
 int sys_upload_values(fc_ctx* ctx, CsrSystem* s, const double* a, bool a_on_device);
 int sys_alloc_work(fc_ctx* ctx, CsrSystem* s);
 
@@ -193,6 +201,33 @@ int sys_solve(fc_ctx* ctx, CsrSystem* s, const char* solver, const double* a, do
 int sys_precond(fc_ctx* ctx, CsrSystem* s, int dilu, const double* q, double* z_out, double* d_out, int apply);
 
 bool is_device_ptr(const void* p);
+
+// ------------------------------------------------------------ batched solves
+// One problem of a batched launch (fc_batch.cu): its system, whose sweep
+// schedule has one tile per block of the problem's group, and the device
+// arrays of this solve (a: nnz values, x in/out, b: rhs, original numbering).
+struct BatchItem {
+  CsrSystem* s = nullptr;
+  const double* a = nullptr;
+  double* x = nullptr;
+  const double* b = nullptr;
+  SolveResult res;
+  double dev_ms = 0.0;   // the group's device time, summed over the launches
+};
+struct BatchDev;         // device arrays of the batched launches (fc_solvers.cu)
+void batch_dev_release(BatchDev* d);
+// the reference's solver report line of a solve (when ctx->verbosity is set)
+void report_solve(fc_ctx* ctx, const char* solver, const char* chvar, const SolveResult& r);
+// Resident blocks of the batched BiCGStab kernel (FP64 and FP32 together).
+int batch_block_budget(fc_ctx* ctx, int* budget);
+// Solves every item: one persistent launch whose block groups are the
+// items in order (items[p].s->ord.ntiles blocks each), in FP64; in
+// FC_PREC_MIXED FP32 inner launches of the same groups inside FP64
+// refinement, each problem with its own stopping test (FC_PREC_MIXED_COLOURED
+// mixes ICCG only: these BiCGStab solves stay FP64).  Per-item results in
+// items[p].res.
+int batch_solve(fc_ctx* ctx, BatchDev*& dev, std::vector<BatchItem>& items, const char* solver, int itr_max,
+                double tol_abs, double tol_rel);
 
 // cross-file helpers (C++ linkage)
 int solve_global(fc_ctx* ctx, const char* solver, double* x, const double* b, double* res0, int itr_max,

@@ -36,7 +36,14 @@ __device__ __forceinline__ unsigned atom_add_acqrel_u32(unsigned* p, unsigned v)
 
 template <class T> __device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }
 
-// Generation barrier over all blocks of the (cooperative) grid.  Returns
+// Block index, block count and grid-stride start/step within the group of
+// blocks the kernel runs on (the launch grid unless GridCtl names a group).
+__device__ __forceinline__ int vg_bid(const GridCtl& C) { return (int)blockIdx.x - C.base; }
+__device__ __forceinline__ int vg_nb(const GridCtl& C) { return C.nb > 0 ? C.nb : (int)gridDim.x; }
+__device__ __forceinline__ int vg_gt(const GridCtl& C) { return vg_bid(C) * (int)blockDim.x + (int)threadIdx.x; }
+__device__ __forceinline__ int vg_G(const GridCtl& C) { return vg_nb(C) * (int)blockDim.x; }
+
+// Generation barrier over all blocks of the (cooperative) grid or group.  Returns
 // false if the wait ran out or another block already failed; the caller then
 // leaves the kernel.
 __device__ __forceinline__ bool grid_sync(const GridCtl& C) {
@@ -47,7 +54,7 @@ __device__ __forceinline__ bool grid_sync(const GridCtl& C) {
     __threadfence();
     unsigned gen = ld_acquire_u32(C.bar + 1);
     unsigned arrived = atom_add_acqrel_u32(C.bar, 1u);
-    if (arrived == gridDim.x - 1) {
+    if (arrived == (unsigned)vg_nb(C) - 1u) {
       atomicExch(C.bar, 0u);
       st_release_u32(C.bar + 1, gen + 1u);
     } else {
@@ -84,7 +91,8 @@ __device__ __forceinline__ bool grid_reduce(const GridCtl& C, int& ph, double (&
   __shared__ double sm[NV][FC_BLOCK / 32];
   __shared__ double tot[NV];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  double* part = C.part + (size_t)(ph & 1) * FC_NPART * gridDim.x;
+  const int nb = vg_nb(C), bid = vg_bid(C);
+  double* part = C.part + (size_t)(ph & 1) * FC_NPART * nb;
   ++ph;
 #pragma unroll
   for (int j = 0; j < NV; ++j) {
@@ -97,7 +105,7 @@ __device__ __forceinline__ bool grid_reduce(const GridCtl& C, int& ph, double (&
     for (int j = 0; j < NV; ++j) {
       double s = lane < nw ? sm[j][lane] : 0.0;
       s = warp_sum(s);
-      if (lane == 0) part[j * gridDim.x + blockIdx.x] = s;
+      if (lane == 0) part[j * nb + bid] = s;
     }
   }
   if (!grid_sync(C)) return false;
@@ -105,7 +113,7 @@ __device__ __forceinline__ bool grid_reduce(const GridCtl& C, int& ph, double (&
 #pragma unroll
     for (int j = 0; j < NV; ++j) {
       double s = 0.0;
-      for (int b = lane; b < (int)gridDim.x; b += 32) s += __ldcg(part + j * gridDim.x + b);
+      for (int b = lane; b < nb; b += 32) s += __ldcg(part + j * nb + b);
       s = warp_sum(s);
       if (lane == 0) tot[j] = s;
     }

@@ -22,6 +22,7 @@
 
 #include "fc_fields.hpp"
 #include "fc_fv.cuh"
+#include "fc_batch_plan.hpp"
 #include "fc_internal.hpp"
 
 using namespace fcfv;
@@ -719,7 +720,27 @@ struct SimpleState {
   int tprm_gen = -1;      // mesh generation the patch tables belong to
   DVec<int> tpatch;       // [kind | iWall start | first boundary index] x numBoundaries
   DVec<double> tpart;     // per-block min/max of T
+  // batched U, V, W solves (fc_simple_set_batched_momentum)
+  int batch_mom = 0;
+  struct MomBatch* mb = nullptr;
+  ~SimpleState();
 };
+
+// Three systems on the mesh pattern (one per velocity component, each with a
+// third of the resident blocks as the batch planner splits them), the V and
+// W matrix values and sources, and the batched launch's device arrays.
+struct MomBatch {
+  int gen = -1;  // mesh generation the systems were built for
+  CsrSystem* sys[3] = {nullptr, nullptr, nullptr};
+  DVec<double> av, aw, bv, bw;
+  BatchDev* dev = nullptr;
+  ~MomBatch() {
+    for (CsrSystem* s : sys) delete s;
+    batch_dev_release(dev);
+  }
+};
+
+SimpleState::~SimpleState() { delete mb; }
 
 static SimpleState& sstate(fc_ctx* ctx) {
   if (!ctx->simple) ctx->simple = new SimpleState();
@@ -833,6 +854,43 @@ extern "C" int fc_update_velocity_at_boundary(fc_ctx* ctx) {
   return update_velocity_at_boundary(ctx, D);
 }
 
+static int mom_batch_prepare(fc_ctx* ctx, SimpleState& S) {
+  if (S.mb && S.mb->gen == ctx->mesh_gen) return FC_OK;
+  delete S.mb;
+  S.mb = new MomBatch();
+  MomBatch& mb = *S.mb;
+  const CsrSystem* m = ctx->sys_mesh;
+  const int n = m->n, nnz = m->nnz;
+  std::vector<int> ia1(m->h_ia), ja1(m->h_ja), dg1(m->h_diag);
+  for (int& v : ia1) ++v;
+  for (int& v : ja1) ++v;
+  for (int& v : dg1) ++v;
+  int budget = 0;
+  batch_block_budget(ctx, &budget);
+  std::vector<BatchCost> c(3);
+  for (BatchCost& x : c) { x.rows = n; x.levels = m->ord.nlev; }
+  const std::vector<int> g = plan_batch_groups(c, budget, budget, 1024);
+  if (g.size() != 3) return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "batched momentum: fewer than 3 resident blocks");
+  for (int k = 0; k < 3; ++k) {
+    mb.sys[k] = new CsrSystem();
+    int st = sys_set_pattern(ctx, mb.sys[k], n, nnz, ia1.data(), ja1.data(), dg1.data(),
+                             ctx->mesh.h_xyz.empty() ? nullptr : ctx->mesh.h_xyz.data(), g[k]);
+    if (st) return st;
+  }
+  FC_CUDA_TRY(ctx, mb.av.alloc(nnz));
+  FC_CUDA_TRY(ctx, mb.aw.alloc(nnz));
+  FC_CUDA_TRY(ctx, mb.bv.alloc(n));
+  FC_CUDA_TRY(ctx, mb.bw.alloc(n));
+  mb.gen = ctx->mesh_gen;
+  return FC_OK;
+}
+
+extern "C" int fc_simple_set_batched_momentum(fc_ctx* ctx, int on) {
+  if (!ctx) return FC_ERR_BAD_INPUT;
+  sstate(ctx).batch_mom = on ? 1 : 0;
+  return FC_OK;
+}
+
 static int solve_into(fc_ctx* ctx, const char* solver, double* x, const double* b, double* resor_out, int itr,
                       double tol_abs, double tol_rel, const char* chvar) {
   fc_solve_info info;
@@ -870,6 +928,43 @@ extern "C" int fc_calcuvw(fc_ctx* ctx, double* resor) {
   ctx->kernel_launches += 2;
   FC_CUDA_TRY(ctx, cudaGetLastError());
   double r[3] = {0, 0, 0};
+  if (S.batch_mom && std::strcmp(P.lSolverU, "bicgstab") == 0) {
+    // the three solves in one batched launch: V and W get copies of the
+    // matrix (same off-diagonals) with their own diagonal and source
+    if ((st = mom_batch_prepare(ctx, S))) return st;
+    MomBatch& mb = *S.mb;
+    const size_t nnz = (size_t)sys->nnz;
+    k_mom_diag<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, sys->ia.p, sys->diag.p, D.a, D.spu, D.apu, D.su, D.su,
+                                                     D.u, P.urfU[0], 0);
+    FC_CUDA_TRY(ctx, cudaMemcpyAsync(mb.av.p, D.a, nnz * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    FC_CUDA_TRY(ctx, cudaMemcpyAsync(mb.aw.p, D.a, nnz * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    k_mom_diag<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, sys->ia.p, sys->diag.p, mb.av.p, D.spv, D.apv, D.sv,
+                                                     mb.bv.p, D.v, P.urfU[1], 1);
+    k_mom_diag<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, sys->ia.p, sys->diag.p, mb.aw.p, D.sp, D.apw, D.sw,
+                                                     mb.bw.p, D.w, P.urfU[2], 1);
+    ctx->kernel_launches += 3;
+    std::vector<BatchItem> it(3);
+    const double* av[3] = {D.a, mb.av.p, mb.aw.p};
+    double* xv[3] = {D.u, D.v, D.w};
+    const double* bv[3] = {D.su, mb.bv.p, mb.bw.p};
+    for (int k = 0; k < 3; ++k) { it[k].s = mb.sys[k]; it[k].a = av[k]; it[k].x = xv[k]; it[k].b = bv[k]; }
+    if ((st = batch_solve(ctx, mb.dev, it, "bicgstab", P.maxiterU, P.tolAbsU, P.tolRelU))) return st;
+    const char* nm[3] = {"U", "V", "W"};
+    for (int k = 0; k < 3; ++k) {
+      const SolveResult& rs = it[k].res;
+      if (rs.status == FC_ERR_TIMEOUT) return fc_fail_msg(ctx, FC_ERR_TIMEOUT, "solver grid barrier timed out");
+      if (rs.status < 0) return fc_fail_msg(ctx, rs.status, "solver reported an error (NaN/Inf or breakdown)");
+      if (!rs.early) r[k] = rs.resor;
+      report_solve(ctx, "bicgstab", nm[k], rs);
+    }
+    // the matrix and source arrays end as the sequential passes leave them
+    FC_CUDA_TRY(ctx, cudaMemcpyAsync(D.a, mb.aw.p, nnz * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    FC_CUDA_TRY(ctx, cudaMemcpyAsync(D.su, mb.bw.p, (size_t)M.nC * sizeof(double), cudaMemcpyDeviceToDevice,
+                                     ctx->stream));
+    for (int k = 0; k < 3; ++k) S.resor[k + 1] = r[k];
+    if (resor) for (int k = 0; k < 3; ++k) resor[k] = r[k];
+    return FC_OK;
+  }
   // U
   k_mom_diag<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, sys->ia.p, sys->diag.p, D.a, D.spu, D.apu, D.su, D.su, D.u,
                                                    P.urfU[0], 0);

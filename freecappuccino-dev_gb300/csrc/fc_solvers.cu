@@ -101,7 +101,7 @@ struct NoTracer : NoTrace {
 
 template <class T>
 __device__ void write_out(const KArgs<T>& A, double res0, double resl, double factor, double resor, int itr, int early) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (vg_bid(A.C) == 0 && threadIdx.x == 0) {
     A.C.out[FC_OUT_RES0] = res0;
     A.C.out[FC_OUT_RESL] = resl;
     A.C.out[FC_OUT_FACTOR] = factor;
@@ -116,7 +116,7 @@ __device__ void write_out(const KArgs<T>& A, double res0, double resl, double fa
 // returns L1(r) (identical in every block)
 template <class T>
 __device__ bool residual_l1(const KArgs<T>& A, int& ph, double& l1out) {
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x, G = gridDim.x * blockDim.x;
+  const int gt = vg_gt(A.C), G = vg_G(A.C);
   double s[1] = {0.0};
   for (int i = gt; i < A.S.n; i += G) {
     T ri = row_residual(A.S, A.x, ldcg(A.b + i), i);
@@ -132,16 +132,16 @@ __device__ bool residual_l1(const KArgs<T>& A, int& ph, double& l1out) {
 // exchange arrays to the sentinel, b (and x) gathered; ends with a barrier.
 template <class T>
 __device__ bool ord_prologue(const KArgs<T>& A, bool dilu, bool with_x) {
-  ord_gather_values(A.O, A.V, A.S.a, A.nnz, dilu);
-  ord_gather_vec(A.O, A.b, A.bo);
-  if (with_x) ord_gather_vec(A.O, (const T*)A.x, A.xo);
+  ord_gather_values(A.C, A.O, A.V, A.S.a, A.nnz, dilu);
+  ord_gather_vec(A.C, A.O, A.b, A.bo);
+  if (with_x) ord_gather_vec(A.C, A.O, (const T*)A.x, A.xo);
   return grid_sync(A.C);
 }
 
 // r = b - A x in the new numbering; returns L1(r) (identical in every block)
 template <class T>
 __device__ bool ord_residual_l1(const KArgs<T>& A, int& ph, double& l1out) {
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x, G = gridDim.x * blockDim.x;
+  const int gt = vg_gt(A.C), G = vg_G(A.C);
   double s[1] = {0.0};
   for (int q = gt; q < A.O.n; q += G) {
     T rq = ord_row_residual(A.O, (const T*)A.V.ap, A.xo, ldcg(A.bo + q), q);
@@ -187,9 +187,9 @@ __device__ __forceinline__ bool precond_setup(const KArgs<T>& A, OsCtx& X) {
 // iccg, linear_solvers.f90:364-545, in the schedule-ordered numbering
 template <class T, bool TRACE = false>
 __global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_iccg(KArgs<T> A) {
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x, G = gridDim.x * blockDim.x, n = A.O.n;
+  const int gt = vg_gt(A.C), G = vg_G(A.C), n = A.O.n;
   int ph = 0;
-  OsCtx X = osweep_ctx<T>(A.O, fc_smem);
+  OsCtx X = osweep_ctx<T>(A.O, fc_smem, vg_bid(A.C));
   T *x = A.xo, *r = A.r, *p = A.p, *z = A.z, *yf = A.u;
   typename std::conditional<TRACE, Tracer, NoTracer>::type tr(A.trace, A.trace_cap);
   for (int i = gt; i < n; i += G) p[i] = T(0);
@@ -240,18 +240,20 @@ __global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_iccg(KArgs<T> A) {
     if (!(rsm == rsm)) { if (gt == 0) atomicCAS(A.C.status, 0, FC_ERR_NAN); break; }
     if (rsm < A.tol_rel || resl < A.tol_abs) break;
   }
-  ord_scatter_vec(A.O, (const T*)x, A.x);
+  ord_scatter_vec(A.C, A.O, (const T*)x, A.x);
   tr.flush();
   write_out(A, res0, resl, factor, resor, itr_used, 0);
 }
 
 // ------------------------------------------------------------- BiCGStab
-// bicgstab, linear_solvers.f90:548-786, in the schedule-ordered numbering
+// bicgstab, linear_solvers.f90:548-786, in the schedule-ordered numbering.
+// Runs on the blocks A.C names (the launch grid, or one problem's group of a
+// batched launch).
 template <class T>
-__global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_bicgstab(KArgs<T> A) {
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x, G = gridDim.x * blockDim.x, n = A.O.n;
+__device__ __forceinline__ void bicgstab_body(const KArgs<T>& A) {
+  const int gt = vg_gt(A.C), G = vg_G(A.C), n = A.O.n;
   int ph = 0;
-  OsCtx X = osweep_ctx<T>(A.O, fc_smem);
+  OsCtx X = osweep_ctx<T>(A.O, fc_smem, vg_bid(A.C));
   T *x = A.xo, *r = A.r, *r0 = A.r0, *p = A.p, *u = A.u, *z = A.z, *v = A.v, *yf = A.w;
   NoTracer tr(nullptr, 0);
   if (!ord_prologue(A, true, true)) return;
@@ -324,8 +326,13 @@ __global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_bicgstab(KArgs<T> A) {
     if (!(rsm == rsm)) { if (gt == 0) atomicCAS(A.C.status, 0, FC_ERR_NAN); break; }
     if (rsm < A.tol_rel || resl < A.tol_abs) break;
   }
-  ord_scatter_vec(A.O, (const T*)x, A.x);
+  ord_scatter_vec(A.C, A.O, (const T*)x, A.x);
   write_out(A, res0, resl, factor, resor, itr_used, 0);
+}
+
+template <class T>
+__global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_bicgstab(KArgs<T> A) {
+  bicgstab_body(A);
 }
 
 // ------------------------------------------------------------------ DPCG
@@ -389,9 +396,9 @@ __global__ void __launch_bounds__(FC_BLOCK, 1) k_dpcg(KArgs<T> A) {
 // forward sweep; entries left of the diagonal take this sweep's values
 // (xb), the diagonal and the entries right of it the previous sweep's (xa).
 __global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_gauss_seidel(KArgs<double> A) {
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gt = vg_gt(A.C);
   int ph = 0;
-  OsCtx X = osweep_ctx<double>(A.O, fc_smem);
+  OsCtx X = osweep_ctx<double>(A.O, fc_smem, vg_bid(A.C));
   if (!ord_prologue(A, false, true)) return;
   double* xa = A.xo;
   double* xb = A.w;
@@ -414,7 +421,7 @@ __global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_gauss_seidel(KArgs<double
     if (!(rsm == rsm)) { if (gt == 0) atomicCAS(A.C.status, 0, FC_ERR_NAN); break; }
     if (rsm < A.tol_rel || resl < A.tol_abs) break;
   }
-  ord_scatter_vec(A.O, (const double*)xa, A.x);
+  ord_scatter_vec(A.C, A.O, (const double*)xa, A.x);
   write_out(A, res0, resl, factor, resor, itr_used, early);
 }
 
@@ -422,15 +429,15 @@ __global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_gauss_seidel(KArgs<double
 // results in the original numbering: d into A.v, z into A.z
 template <class T, bool DILU>
 __global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_precond(KArgs<T> A, int apply) {
-  OsCtx X = osweep_ctx<T>(A.O, fc_smem);
+  OsCtx X = osweep_ctx<T>(A.O, fc_smem, vg_bid(A.C));
   NoTracer tr(nullptr, 0);
   if (!ord_prologue(A, DILU, false)) return;
   if (!precond_setup<T, DILU>(A, X)) return;
-  ord_scatter_vec(A.O, (const T*)A.d, A.v);
+  ord_scatter_vec(A.C, A.O, (const T*)A.d, A.v);
   if (!apply) return;
   if (!precond_apply(A, X, (const T*)A.bo, A.u, A.w, (const T*)nullptr, nullptr, &tr)) return;
   if (!grid_sync(A.C)) return;
-  ord_scatter_vec(A.O, (const T*)A.w, A.z);
+  ord_scatter_vec(A.C, A.O, (const T*)A.w, A.z);
 }
 
 // r = b - A x in FP64 with L1 norm (refinement step of the mixed solve)
@@ -455,6 +462,101 @@ __global__ void k_zero_float(float* __restrict__ d, int n) {
 }
 __global__ void k_add_float(double* __restrict__ x, const float* __restrict__ dx, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] += (double)dx[i];
+}
+
+// ------------------------------------------------------- batched launches
+// The launch grid is split into groups of consecutive blocks; bprob[b] is
+// the problem of block b.  A group copies its problem's KArgs (whose GridCtl
+// names the group: base block, block count, its own barrier, partial sums,
+// status and out slots) into shared memory and runs the single-problem code
+// on it.  Groups never wait on each other.
+struct BatchCtl {
+  int active;      // 0: the group leaves at once
+  int skip_setup;  // inner solves after the first keep the DILU factors
+  int itr_max;
+  int add_dx;      // refinement: x += dx of the previous inner solve first
+  int conv_a;      // refinement: a32 = (float)a as well
+  int pad[3];
+};
+// FP32 work arrays of a problem in the mixed modes (original numbering)
+struct BatchMix {
+  float* fx;    // inner solution dx
+  float* fr0;   // inner right-hand side (the FP64 residual, rounded)
+  float* a32;   // FP32 matrix values
+  int nnz;
+  int pad;
+};
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+template <class T>
+__device__ __forceinline__ KArgs<T>& batch_args(const KArgs<T>* __restrict__ args, int p, unsigned char* raw) {
+  static_assert(sizeof(KArgs<T>) % 4 == 0, "KArgs is copied as 32-bit words");
+  const int* src = reinterpret_cast<const int*>(args + p);
+  int* dst = reinterpret_cast<int*>(raw);
+  for (int i = threadIdx.x; i < (int)(sizeof(KArgs<T>) / 4); i += blockDim.x) dst[i] = __ldg(src + i);
+  return *reinterpret_cast<KArgs<T>*>(raw);
+}
+
+template <class T>
+__global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1)
+    k_bicgstab_batch(const KArgs<T>* __restrict__ args, const int* __restrict__ bprob, const BatchCtl* __restrict__ ctl) {
+  __shared__ __align__(16) unsigned char raw[sizeof(KArgs<T>)];
+  const int p = __ldg(bprob + blockIdx.x);
+  if (p < 0 || !ctl[p].active) return;
+  const unsigned long long t0 = globaltimer_ns();
+  KArgs<T>& A = batch_args(args, p, raw);
+  __syncthreads();
+  if (threadIdx.x == 0) { A.skip_setup = ctl[p].skip_setup; A.itr_max = ctl[p].itr_max; }
+  __syncthreads();
+  bicgstab_body(A);
+  if (vg_bid(A.C) == 0 && threadIdx.x == 0) A.C.out[FC_OUT_GT] = (double)(globaltimer_ns() - t0);
+}
+
+// Refinement step of the mixed batched solve, per group: x += dx of the
+// previous inner solve (add_dx), a32 = a (conv_a), barrier, r = b - A x in
+// FP64 with L1(r) and sum |a_ii x_i| (the reference's normalisation), the
+// inner right-hand side fr0 = (float)r and dx = 0.  The arithmetic of
+// k_residual64, k_to_float, k_zero_float and k_add_float in one pass.
+__global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1)
+    k_refine_batch(const KArgs<double>* __restrict__ args, const int* __restrict__ bprob,
+                   const BatchCtl* __restrict__ ctl, const BatchMix* __restrict__ mix) {
+  __shared__ __align__(16) unsigned char raw[sizeof(KArgs<double>)];
+  const int p = __ldg(bprob + blockIdx.x);
+  if (p < 0 || !ctl[p].active) return;
+  const unsigned long long t0 = globaltimer_ns();
+  const KArgs<double>& A = batch_args(args, p, raw);
+  __syncthreads();
+  const BatchCtl c = ctl[p];
+  const BatchMix m = mix[p];
+  const int gt = vg_gt(A.C), G = vg_G(A.C), n = A.S.n;
+  if (c.add_dx)
+    for (int i = gt; i < n; i += G) A.x[i] = A.x[i] + (double)m.fx[i];
+  if (c.conv_a)
+    for (int k = gt; k < m.nnz; k += G) m.a32[k] = (float)__ldg(A.S.a + k);
+  if (!grid_sync(A.C)) return;
+  int ph = 0;
+  double s[1] = {0.0};
+  for (int i = gt; i < n; i += G) {
+    const double ri = row_residual(A.S, (const double*)A.x, ldcg(A.b + i), i);
+    A.r[i] = ri;
+    m.fr0[i] = (float)ri;
+    m.fx[i] = 0.0f;
+    s[0] += fabs(ri);
+  }
+  if (!grid_reduce<1>(A.C, ph, s)) return;
+  double f[1] = {0.0};
+  for (int i = gt; i < n; i += G) f[0] += fabs(__ldg(A.S.a + __ldg(A.S.dg + i)) * ldcg(A.x + i));
+  if (!grid_reduce<1>(A.C, ph, f)) return;
+  if (vg_bid(A.C) == 0 && threadIdx.x == 0) {
+    A.C.out[FC_OUT_RESL] = s[0];
+    A.C.out[FC_OUT_FACTOR] = f[0];
+    A.C.out[FC_OUT_GT] = (double)(globaltimer_ns() - t0);
+  }
 }
 
 }  // namespace
@@ -592,7 +694,7 @@ static int upload_ordered(fc_ctx* ctx, const OrderedSweep& O, DevOrdered& D) {
 }
 
 int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, const int* ja1, const int* diag1,
-                    const double* xyz) {
+                    const double* xyz, int tiles_req) {
   if (n <= 0 || nnz < n) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "csr pattern: n <= 0 or nnz < n");
   if (nnz >= (1 << 27)) return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "csr pattern: nnz >= 2^27");
   mc_release(s->mc);  // the multicolour layout belongs to the previous pattern
@@ -647,7 +749,10 @@ int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, c
   // chosen among a few candidates by the critical-path estimate
   const int sms = std::max(1, ctx->num_sms);
   int tiles = sms;
-  {
+  if (tiles_req > 0) {
+    tiles = std::min(tiles_req, sms);
+    s->est_sweep_us = 0.0;
+  } else {
     std::vector<int> levs;
     const int nls = symmetric_levels(n, ia.data(), ja.data(), dg.data(), levs);
     double best = 1e300;
@@ -998,6 +1103,263 @@ int sys_solve(fc_ctx* ctx, CsrSystem* s, const char* solver_c, const double* a, 
   if (res->status == 0 && !res->early && res->itr_used >= itr_max && itr_max > 0 &&
       !(res->resl / (res->res0 + FC_SMALL) < tol_rel || res->resl < tol_abs))
     res->status = FC_WARN_MAXITER;
+  return FC_OK;
+}
+
+// ------------------------------------------------------------- batched solves
+struct BatchDev {
+  int np = 0, nblocks = 0;
+  DVec<KArgs<double>> a64, ar;
+  DVec<KArgs<float>> af;
+  DVec<BatchMix> mix;
+  DVec<BatchCtl> ctl;
+  DVec<int> bprob;
+  DVec<double> out;       // [np][FC_OUT_N]
+  DVec<int> status;       // [np]
+  DVec<unsigned> bar;     // [np][2]
+  double* h_out = nullptr;
+  int* h_status = nullptr;
+  BatchCtl* h_ctl = nullptr;
+  ~BatchDev() {
+    if (h_out) cudaFreeHost(h_out);
+    if (h_status) cudaFreeHost(h_status);
+    if (h_ctl) cudaFreeHost(h_ctl);
+  }
+};
+
+void batch_dev_release(BatchDev* d) { delete d; }
+
+int batch_block_budget(fc_ctx* ctx, int* budget) {
+  *budget = std::max(1, ctx->num_sms);
+  return FC_OK;
+}
+
+static int batch_prepare(fc_ctx* ctx, BatchDev& B, const std::vector<BatchItem>& items) {
+  const int np = (int)items.size();
+  std::vector<int> bprob;
+  for (int p = 0; p < np; ++p)
+    for (int k = 0; k < items[p].s->ord.ntiles; ++k) bprob.push_back(p);
+  if ((int)bprob.size() > std::max(1, ctx->num_sms))
+    return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "batch: the groups need more blocks than the GPU holds resident");
+  if (B.np != np) {
+    if (B.h_out) cudaFreeHost(B.h_out);
+    if (B.h_status) cudaFreeHost(B.h_status);
+    if (B.h_ctl) cudaFreeHost(B.h_ctl);
+    B.h_out = nullptr; B.h_status = nullptr; B.h_ctl = nullptr;
+    FC_CUDA_TRY(ctx, cudaMallocHost(&B.h_out, (size_t)np * FC_OUT_N * sizeof(double)));
+    FC_CUDA_TRY(ctx, cudaMallocHost(&B.h_status, (size_t)np * sizeof(int)));
+    FC_CUDA_TRY(ctx, cudaMallocHost(&B.h_ctl, (size_t)np * sizeof(BatchCtl)));
+    FC_CUDA_TRY(ctx, B.a64.alloc(np));
+    FC_CUDA_TRY(ctx, B.ar.alloc(np));
+    FC_CUDA_TRY(ctx, B.af.alloc(np));
+    FC_CUDA_TRY(ctx, B.mix.alloc(np));
+    FC_CUDA_TRY(ctx, B.ctl.alloc(np));
+    FC_CUDA_TRY(ctx, B.out.alloc((size_t)np * FC_OUT_N));
+    FC_CUDA_TRY(ctx, B.status.alloc(np));
+    FC_CUDA_TRY(ctx, B.bar.alloc((size_t)2 * np));
+    B.np = np;
+  }
+  FC_CUDA_TRY(ctx, B.bprob.alloc(bprob.size()));
+  FC_CUDA_TRY(ctx, cudaMemcpyAsync(B.bprob.p, bprob.data(), bprob.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                   ctx->stream));
+  B.nblocks = (int)bprob.size();
+  return FC_OK;
+}
+
+// GridCtl of problem p: its group of blocks, its slots of the batch arrays
+template <class T>
+static void batch_ctl(KArgs<T>& A, BatchDev& B, int p, int base, int nb) {
+  A.C.out = B.out.p + (size_t)p * FC_OUT_N;
+  A.C.status = B.status.p + p;
+  A.C.bar = B.bar.p + 2 * p;
+  A.C.base = base;
+  A.C.nb = nb;
+}
+
+static int batch_launch(fc_ctx* ctx, BatchDev& B, const void* fn, void** args, size_t smem) {
+  if (smem > 48 * 1024)
+    FC_CUDA_TRY(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int nb = 0;
+  FC_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, FC_SWEEP_BLOCK, smem));
+  if (nb < 1 || B.nblocks > nb * std::max(1, ctx->num_sms))
+    return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "batch: the groups need more blocks than the GPU holds resident");
+  FC_CUDA_TRY(ctx, cudaMemsetAsync(B.bar.p, 0, B.bar.bytes(), ctx->stream));
+  FC_CUDA_TRY(ctx, cudaMemsetAsync(B.status.p, 0, B.status.bytes(), ctx->stream));
+  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(B.nblocks), dim3(FC_SWEEP_BLOCK), args, smem, ctx->stream);
+  if (e != cudaSuccess) return fc_fail(ctx, FC_ERR_CUDA, "batched cooperative launch", e);
+  ctx->kernel_launches++;
+  return FC_OK;
+}
+
+static int batch_fetch(fc_ctx* ctx, BatchDev& B) {
+  FC_CUDA_TRY(ctx, cudaMemcpyAsync(B.h_out, B.out.p, B.out.bytes(), cudaMemcpyDeviceToHost, ctx->stream));
+  FC_CUDA_TRY(ctx, cudaMemcpyAsync(B.h_status, B.status.p, B.status.bytes(), cudaMemcpyDeviceToHost, ctx->stream));
+  FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return FC_OK;
+}
+
+static int batch_put_ctl(fc_ctx* ctx, BatchDev& B) {
+  FC_CUDA_TRY(ctx, cudaMemcpyAsync(B.ctl.p, B.h_ctl, B.ctl.bytes(), cudaMemcpyHostToDevice, ctx->stream));
+  return FC_OK;
+}
+
+template <class T>
+static size_t batch_smem(const std::vector<BatchItem>& items) {
+  size_t m = 0;
+  for (const BatchItem& it : items) {
+    const DevOrdered& D = it.s->ord;
+    m = std::max(m, osweep_smem_bytes<T>(D.R, D.K, D.maxW, D.max_tile_steps, D.xmax, D.pmax));
+  }
+  return m;
+}
+
+int batch_solve(fc_ctx* ctx, BatchDev*& dev, std::vector<BatchItem>& items, const char* solver_c, int itr_max,
+                double tol_abs, double tol_rel) {
+  const std::string solver(solver_c ? solver_c : "");
+  if (solver != "bicgstab") return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "batch: solver must be bicgstab");
+  const int np = (int)items.size();
+  if (np == 0) return FC_OK;
+  for (BatchItem& it : items) {
+    it.res = SolveResult();
+    it.dev_ms = 0.0;
+    if (it.s->tslot_oob) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "bicgstab: pattern is not structurally symmetric");
+  }
+  if (!dev) dev = new BatchDev();
+  BatchDev& B = *dev;
+  int st = batch_prepare(ctx, B, items);
+  if (st) return st;
+  std::vector<int> base(np), nbk(np);
+  for (int p = 0, acc = 0; p < np; ++p) { base[p] = acc; nbk[p] = items[p].s->ord.ntiles; acc += nbk[p]; }
+  const bool mixed = ctx->precision == FC_PREC_MIXED;
+  FC_CUDA_TRY(ctx, cudaMemsetAsync(B.out.p, 0, B.out.bytes(), ctx->stream));
+
+  if (!mixed) {
+    std::vector<KArgs<double>> h(np);
+    for (int p = 0; p < np; ++p) {
+      CsrSystem* s = items[p].s;
+      h[p] = make_args<double>(s, items[p].a, items[p].x, items[p].b, s->r.p, s->r0.p, s->p.p, s->u.p, s->z.p, s->v.p,
+                               s->d.p, s->w.p, itr_max, tol_abs, tol_rel);
+      batch_ctl(h[p], B, p, base[p], nbk[p]);
+      B.h_ctl[p] = BatchCtl{1, 0, itr_max, 0, 0, {0, 0, 0}};
+    }
+    FC_CUDA_TRY(ctx, cudaMemcpyAsync(B.a64.p, h.data(), np * sizeof(KArgs<double>), cudaMemcpyHostToDevice, ctx->stream));
+    if ((st = batch_put_ctl(ctx, B))) return st;
+    KArgs<double>* pa = B.a64.p;
+    int* pb = B.bprob.p;
+    BatchCtl* pc = B.ctl.p;
+    void* args[3] = {&pa, &pb, &pc};
+    if ((st = batch_launch(ctx, B, (const void*)k_bicgstab_batch<double>, args, batch_smem<double>(items)))) return st;
+    if ((st = batch_fetch(ctx, B))) return st;
+    for (int p = 0; p < np; ++p) {
+      const double* o = B.h_out + (size_t)p * FC_OUT_N;
+      SolveResult& r = items[p].res;
+      r.res0 = o[FC_OUT_RES0]; r.resl = o[FC_OUT_RESL]; r.factor = o[FC_OUT_FACTOR]; r.resor = o[FC_OUT_RESOR];
+      r.itr_used = (int)o[FC_OUT_ITR]; r.early = (int)o[FC_OUT_EARLY]; r.status = B.h_status[p];
+      items[p].dev_ms = o[FC_OUT_GT] * 1e-6;
+    }
+  } else {
+    // FP32 inner solves inside FP64 refinement, the arithmetic of
+    // solve_mixed per problem; the refinement steps of all problems that
+    // still run are one launch, their inner solves the next
+    std::vector<KArgs<double>> hr(np);
+    std::vector<KArgs<float>> hf(np);
+    std::vector<BatchMix> hm(np);
+    const double inner_tol = ctx->inner_tol > 0 ? ctx->inner_tol : 1e-4;
+    const int inner_itmax = ctx->inner_itmax > 0 ? ctx->inner_itmax : std::max(itr_max, 1);
+    for (int p = 0; p < np; ++p) {
+      CsrSystem* s = items[p].s;
+      if ((st = alloc_work32(ctx, s))) return st;
+      hr[p] = make_args<double>(s, items[p].a, items[p].x, items[p].b, s->r.p, s->r0.p, s->p.p, s->u.p, s->z.p,
+                                s->v.p, s->d.p, s->w.p, 0, tol_abs, tol_rel);
+      batch_ctl(hr[p], B, p, base[p], nbk[p]);
+      hf[p] = make_args<float>(s, s->a32.p, s->fx.p, s->fr0.p, s->fr.p, s->fy.p, s->fp.p, s->fu.p, s->fz.p, s->fv.p,
+                               s->fd.p, s->fw.p, 0, 0.0, inner_tol);
+      batch_ctl(hf[p], B, p, base[p], nbk[p]);
+      hm[p] = BatchMix{s->fx.p, s->fr0.p, s->a32.p, s->nnz, 0};
+    }
+    FC_CUDA_TRY(ctx, cudaMemcpyAsync(B.ar.p, hr.data(), np * sizeof(KArgs<double>), cudaMemcpyHostToDevice, ctx->stream));
+    FC_CUDA_TRY(ctx, cudaMemcpyAsync(B.af.p, hf.data(), np * sizeof(KArgs<float>), cudaMemcpyHostToDevice, ctx->stream));
+    FC_CUDA_TRY(ctx, cudaMemcpyAsync(B.mix.p, hm.data(), np * sizeof(BatchMix), cudaMemcpyHostToDevice, ctx->stream));
+    struct PState { bool first = true, done = false, inner = false; int outer = 0, total = 0; double res0 = 0, resl = 0, factor = 0; };
+    std::vector<PState> ps(np);
+    const int max_outer = 64;
+    const size_t smemf = batch_smem<float>(items);
+    KArgs<double>* pr = B.ar.p;
+    KArgs<float>* pf = B.af.p;
+    int* pb = B.bprob.p;
+    BatchCtl* pc = B.ctl.p;
+    BatchMix* pm = B.mix.p;
+    for (;;) {
+      // refinement step of every problem that is not done
+      int nact = 0;
+      for (int p = 0; p < np; ++p) {
+        const PState& q = ps[p];
+        B.h_ctl[p] = BatchCtl{q.done ? 0 : 1, 0, 0, q.outer > 0 ? 1 : 0, q.first ? 1 : 0, {0, 0, 0}};
+        nact += q.done ? 0 : 1;
+      }
+      if (!nact) break;
+      if ((st = batch_put_ctl(ctx, B))) return st;
+      void* ra[4] = {&pr, &pb, &pc, &pm};
+      if ((st = batch_launch(ctx, B, (const void*)k_refine_batch, ra, 0))) return st;
+      if ((st = batch_fetch(ctx, B))) return st;
+      int ninner = 0;
+      for (int p = 0; p < np; ++p) {
+        PState& q = ps[p];
+        q.inner = false;
+        if (q.done) continue;
+        SolveResult& r = items[p].res;
+        const double* o = B.h_out + (size_t)p * FC_OUT_N;
+        items[p].dev_ms += o[FC_OUT_GT] * 1e-6;
+        if (B.h_status[p]) { r.status = B.h_status[p]; q.done = true; continue; }
+        q.resl = o[FC_OUT_RESL];
+        if (q.first) {
+          q.res0 = q.resl;
+          q.first = false;
+          if (q.res0 < tol_abs) { r.res0 = q.res0; r.resl = q.res0; r.early = 1; r.itr_used = 0; q.done = true; continue; }
+        } else if (q.outer == 1) {
+          q.factor = o[FC_OUT_FACTOR] + FC_SMALL;
+        }
+        bool stop = false;
+        if (!std::isfinite(q.resl)) { r.status = FC_ERR_NAN; stop = true; }
+        else if (q.outer > 0 && (q.resl / (q.res0 + FC_SMALL) < tol_rel || q.resl < tol_abs)) stop = true;
+        else if (q.outer >= max_outer || q.total >= itr_max) { r.status = FC_WARN_MAXITER; stop = true; }
+        if (stop) {
+          q.done = true;
+          r.res0 = q.res0; r.resl = q.resl; r.factor = q.factor; r.resor = q.factor > 0 ? q.res0 / q.factor : 0.0;
+          r.itr_used = q.total; r.outer = q.outer;
+          continue;
+        }
+        q.inner = true;
+        ++ninner;
+      }
+      if (!ninner) break;
+      // inner FP32 solves of A dx = r from dx = 0
+      for (int p = 0; p < np; ++p) {
+        const PState& q = ps[p];
+        B.h_ctl[p] = BatchCtl{q.inner ? 1 : 0, q.outer > 0 ? 1 : 0, std::min(inner_itmax, itr_max - q.total), 0, 0,
+                              {0, 0, 0}};
+      }
+      if ((st = batch_put_ctl(ctx, B))) return st;
+      void* fa[3] = {&pf, &pb, &pc};
+      if ((st = batch_launch(ctx, B, (const void*)k_bicgstab_batch<float>, fa, smemf))) return st;
+      if ((st = batch_fetch(ctx, B))) return st;
+      for (int p = 0; p < np; ++p) {
+        PState& q = ps[p];
+        if (!q.inner) continue;
+        const double* o = B.h_out + (size_t)p * FC_OUT_N;
+        items[p].dev_ms += o[FC_OUT_GT] * 1e-6;
+        if (B.h_status[p]) { items[p].res.status = B.h_status[p]; q.done = true; continue; }
+        q.total += (int)o[FC_OUT_ITR];
+        ++q.outer;
+      }
+    }
+  }
+  for (BatchItem& it : items) {
+    SolveResult& r = it.res;
+    if (r.status == 0 && !r.early && r.itr_used >= itr_max && itr_max > 0 &&
+        !(r.resl / (r.res0 + FC_SMALL) < tol_rel || r.resl < tol_abs))
+      r.status = FC_WARN_MAXITER;
+  }
   return FC_OK;
 }
 

@@ -179,9 +179,8 @@ struct OsCtx {
 };
 
 template <class T>
-__device__ __forceinline__ OsCtx osweep_ctx(const OrdView& O, unsigned char* smem) {
+__device__ __forceinline__ OsCtx osweep_ctx(const OrdView& O, unsigned char* smem, int t) {
   OsCtx X;
-  const int t = blockIdx.x;
   const int W = t < O.ntiles ? __ldg(O.tile_W + t) : 1;
   X.L.template init<T>(W, O.xmax, O.pmax);
   // carve with this tile's width; the host sized the area for the widest
@@ -256,7 +255,7 @@ __device__ __noinline__ T xv_wait(const GridCtl& C, const T* p, int* abort_flag)
   return v;
 }
 
-// One ordered sweep of tile blockIdx.x.  dirn 0: forward over the lower
+// One ordered sweep of tile vg_bid(C).  dirn 0: forward over the lower
 // triangle, 1: backward over the upper one.  red (MODE OS_BWD_DOT: red[0] +=
 // e*value; OS_GS: red[0] += |residual|, red[1] += |a_ii x_i|) accumulates
 // per thread.  Every thread of the block calls it; it ends with a block
@@ -271,7 +270,7 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
   constexpr bool kGS = MODE == OS_GS;
   constexpr int VR = Rec<T>::V;
   if (tr) tr->sweep();
-  const int t = blockIdx.x;
+  const int t = vg_bid(C);
   if (t >= O.ntiles) return true;
   const int ns = __ldg(O.tile_step_ptr + t + 1) - __ldg(O.tile_step_ptr + t);
   const StageLayout& L = X.L;
@@ -514,8 +513,9 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
 // (original entry slots), exchange arrays filled with the sentinel.  Grid-
 // stride; the caller ends the phase with a grid barrier.
 template <class T>
-__device__ void ord_gather_values(const OrdView& O, const OrdVals<T>& V, const T* __restrict__ a, int nnz, bool dilu) {
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x, G = gridDim.x * blockDim.x, n = O.n, nE = O.nE;
+__device__ void ord_gather_values(const GridCtl& C, const OrdView& O, const OrdVals<T>& V, const T* __restrict__ a,
+                                  int nnz, bool dilu) {
+  const int gt = vg_gt(C), G = vg_G(C), n = O.n, nE = O.nE;
   constexpr int VR = Rec<T>::V;
   const T SENT = Sentinel<T>::value();
   for (int q = gt; q < n; q += G) {
@@ -547,13 +547,13 @@ __device__ void ord_gather_values(const OrdView& O, const OrdVals<T>& V, const T
 
 // y[q] = src[perm[q]] (into the new numbering) / dst[perm[q]] = y[q]
 template <class T, class U>
-__device__ __forceinline__ void ord_gather_vec(const OrdView& O, const U* __restrict__ src, T* y) {
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < O.n; q += gridDim.x * blockDim.x)
+__device__ __forceinline__ void ord_gather_vec(const GridCtl& C, const OrdView& O, const U* __restrict__ src, T* y) {
+  for (int q = vg_gt(C); q < O.n; q += vg_G(C))
     y[q] = (T)ldcg(src + __ldg(O.perm + q));
 }
 template <class T, class U>
-__device__ __forceinline__ void ord_scatter_vec(const OrdView& O, const T* y, U* dst) {
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < O.n; q += gridDim.x * blockDim.x)
+__device__ __forceinline__ void ord_scatter_vec(const GridCtl& C, const OrdView& O, const T* y, U* dst) {
+  for (int q = vg_gt(C); q < O.n; q += vg_G(C))
     dst[__ldg(O.perm + q)] = (U)ldcg(y + q);
 }
 

@@ -119,6 +119,14 @@ def lib():
         "fc_cd_assemble": (i, [vp, vp, vp]),
         "fc_cd_solve": (i, [vp, vp, i, d, C.POINTER(SolveInfo)]),
         "fc_cd_adjoint": (i, [vp, vp, vp, vp, i, d, C.POINTER(SolveInfo)]),
+        "fc_simple_set_batched_momentum": (i, [vp, i]),
+        "fc_batch_create": (i, [vp, vp]),
+        "fc_batch_destroy": (i, [vp]),
+        "fc_batch_add": (i, [vp, i, i, vp, vp, vp, vp]),
+        "fc_batch_plan": (i, [vp, vp]),
+        "fc_batch_tiles": (i, [vp, vp]),
+        "fc_batch_solve": (i, [vp, cp, vp, vp, vp, i, d, d, C.POINTER(SolveInfo)]),
+        "fc_batch_tune": (i, [vp, cp, vp, vp, vp, i, d, d, i, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -598,6 +606,10 @@ class Context:
         self._check(st, "fc_cd_adjoint")
         return lam, grad, info
 
+    def simple_batched_momentum(self, on=True):
+        """calcuvw solves U, V, W in one batched launch (bicgstab only)."""
+        self._check(self.L.fc_simple_set_batched_momentum(self.h, int(bool(on))), "fc_simple_set_batched_momentum")
+
     # ------------------------------------------------------- temperature
     def temperature_params(self, prm, bc_dfraction=None):
         """prm: TemperatureParams; bc_dfraction: bcDFraction(7,:) per patch
@@ -612,3 +624,79 @@ class Context:
         r = np.zeros(1)
         self._check(self.L.fc_calculate_temperature(self.h, int(bool(solve)), _ptr(r)), "fc_calculate_temperature")
         return float(r[0])
+
+
+class Batch:
+    """Independent sparse systems solved in one batched launch (fc_batch_*).
+    Problems are added as 1-based CSR patterns (numpy or device arrays);
+    solve() takes per-problem lists of values, solutions and right-hand
+    sides.  numpy solutions are copied and returned, device ones updated in
+    place."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        self.L = ctx.L
+        h = C.c_void_p()
+        ctx._check(self.L.fc_batch_create(ctx.h, C.byref(h)), "fc_batch_create")
+        self.h = h
+        self.sizes = []
+
+    def close(self):
+        if self.h:
+            self.L.fc_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, ia, ja, diag, xyz=None):
+        ia, ja, diag = _i32(ia), _i32(ja), _i32(diag)
+        n, nnz = len(ia) - 1, len(ja)
+        xyz = None if xyz is None else _f64(xyz)
+        k = self.L.fc_batch_add(self.h, n, nnz, _ptr(ia), _ptr(ja), _ptr(diag), _ptr(xyz))
+        self.ctx._check(k, "fc_batch_add")
+        self.sizes.append((n, nnz))
+        return k
+
+    def plan(self, tiles=None):
+        t = None if tiles is None else np.ascontiguousarray(tiles, dtype=np.int32)
+        self.ctx._check(self.L.fc_batch_plan(self.h, _ptr(t)), "fc_batch_plan")
+        return self.tiles()
+
+    def tiles(self):
+        t = np.zeros(len(self.sizes), dtype=np.int32)
+        self.ctx._check(self.L.fc_batch_tiles(self.h, _ptr(t)), "fc_batch_tiles")
+        return t
+
+    @staticmethod
+    def _ptrs(arrays):
+        v = (C.c_void_p * len(arrays))()
+        for k, a in enumerate(arrays):
+            v[k] = _ptr(a).value
+        return v
+
+    def solve(self, a, x, rhs, itr_max, tol_abs, tol_rel, solver="bicgstab", raise_on_error=True):
+        """Returns (x list, [SolveInfo], status)."""
+        a = [_f64(v) for v in a]
+        rhs = [_f64(v) for v in rhs]
+        x = [_f64(v).copy() if isinstance(v, np.ndarray) or not hasattr(v, "data_ptr") else v for v in x]
+        infos = (SolveInfo * len(a))()
+        st = self.L.fc_batch_solve(self.h, solver.encode(), self._ptrs(a), self._ptrs(x), self._ptrs(rhs),
+                                   int(itr_max), float(tol_abs), float(tol_rel), infos)
+        if raise_on_error:
+            self.ctx._check(st, "fc_batch_solve")
+        return x, list(infos), st
+
+    def tune(self, a, x0, rhs, itr_max, tol_abs, tol_rel, rounds=3, solver="bicgstab"):
+        """Measured re-planning; returns (tiles, best ms)."""
+        a = [_f64(v) for v in a]
+        rhs = [_f64(v) for v in rhs]
+        x0 = [_f64(v) for v in x0]
+        best = np.zeros(1)
+        self.ctx._check(self.L.fc_batch_tune(self.h, solver.encode(), self._ptrs(a), self._ptrs(x0),
+                                             self._ptrs(rhs), int(itr_max), float(tol_abs), float(tol_rel),
+                                             int(rounds), _ptr(best)), "fc_batch_tune")
+        return self.tiles(), float(best[0])

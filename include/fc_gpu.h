@@ -178,6 +178,41 @@ int fc_set_sweep_cap(fc_ctx* ctx, int rows);
  * same systems (which as above); builds the ordering if no solve has yet.
  * Diagnostics only: no counterpart in the reference. */
 int fc_mixed_colours(fc_ctx* ctx, int which, int* ncol);
+
+/* ---- Batched solves of independent systems (no reference counterpart: the
+ * reference makes one csrsolve call per system, linear_solvers.f90:40-91,
+ * e.g. u, v and w in calcuvw, velocity.f90:638, :693, :748).  Every problem
+ * keeps its own pattern analysis; one persistent launch solves them all, its
+ * grid split into one group of blocks per problem, each group with its own
+ * sweep tiles (one per block), barrier, reductions and stopping test.  In
+ * FC_PREC_FP64 (and FC_PREC_MIXED_COLOURED, which mixes ICCG only) a
+ * problem's iterates are those of a single bicgstab solve on the same tiles;
+ * in FC_PREC_MIXED the inner solves are FP32 BiCGStab on the natural
+ * ordering inside FP64 refinement, per problem.
+ *   fc_batch_add:   1-based CSR pattern (host or device), optional row
+ *                   coordinates xyz (3n: x..., y..., z...) for the tiling;
+ *                   returns the problem index (>= 0) or an error.
+ *   fc_batch_plan:  tiles NULL: the tuned plan cached for these problem
+ *                   sizes, else the planner's cost model; or explicit tiles
+ *                   per problem (sum <= SMs).  Builds the sweep schedules.
+ *   fc_batch_tiles: the current plan.
+ *   fc_batch_solve: solver "bicgstab"; a[p], x[p] (in/out), rhs[p] host or
+ *                   device arrays; info[p] per problem (ms = the group's
+ *                   device time).  Returns the worst status.
+ *   fc_batch_tune:  measured solves from x0 (x0 is not modified) to refine
+ *                   the model per problem, at most `rounds` plans; keeps the
+ *                   fastest, caches it for these sizes, *best_ms its time. */
+typedef struct fc_batch fc_batch;
+int fc_batch_create(fc_ctx* ctx, fc_batch** out);
+int fc_batch_destroy(fc_batch* b);
+int fc_batch_add(fc_batch* b, int n, int nnz, const int* ia, const int* ja, const int* diag, const double* xyz);
+int fc_batch_plan(fc_batch* b, const int* tiles);
+int fc_batch_tiles(fc_batch* b, int* tiles);
+int fc_batch_solve(fc_batch* b, const char* solver, const double* const* a, double* const* x,
+                   const double* const* rhs, int itr_max, double tol_abs, double tol_rel, fc_solve_info* info);
+int fc_batch_tune(fc_batch* b, const char* solver, const double* const* a, const double* const* x0,
+                  const double* const* rhs, int itr_max, double tol_abs, double tol_rel, int rounds,
+                  double* best_ms);
 /* Tracing of the FP64 ICCG kernel (no counterpart in the reference): with
  * on != 0 the solves run a traced instantiation that records per block the
  * SM cycles of each phase and, for the forward and backward sweep of the
@@ -308,6 +343,13 @@ int fc_gradp_and_sources(fc_ctx* ctx, const char* field);
 /* calcuvw (velocity.f90:50-750): momentum assembly and the three solves;
  * resor[3] receives the normalised initial residuals of U, V, W. */
 int fc_calcuvw(fc_ctx* ctx, double* resor);
+/* on != 0: calcuvw solves U, V and W together (when lSolverU is bicgstab) in
+ * one batched launch (fc_batch_*) on three copies of the mesh pattern, each
+ * with its own diagonal and source as velocity.f90:611-748 forms them; the
+ * resulting fields, residuals and matrix state are those of the three
+ * sequential solves up to the rounding of the solvers' reductions.  Default
+ * off.  No counterpart in the reference. */
+int fc_simple_set_batched_momentum(fc_ctx* ctx, int on);
 /* calcp_simple (calcp_simple.f90:1-470); *resor4 = resor(4) of continuityErrors. */
 int fc_calcp_simple(fc_ctx* ctx, double* resor4);
 /* one outer SIMPLE iteration (main.f90:159-165); resor[4] as the reference

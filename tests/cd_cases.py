@@ -59,3 +59,29 @@ def cd_fd_perturbation(ctx, gamma, src, phi, vol, xc, c, h, itr_max=500, tol_rel
         dJ.append(float((vol[mask] * (2.0 * phi[mask] * dphi[mask] + dphi[mask] ** 2)).sum() / vt))
     ctx.cd_assemble(gamma, src)
     return (dJ[0] - dJ[1]) / (2.0 * h)
+
+
+def cd_batch_sizes(count=64, lo=20, hi=80, seed_n=44, seed_pe=45):
+    """Cells per side ~ U{lo..hi} (seed 44) and cell Peclet numbers
+    Pe_h = U h / gamma ~ lognormal(0, 1) (seed 45) of the batched
+    convection-diffusion configuration."""
+    ns = np.random.default_rng(seed_n).integers(lo, hi + 1, count)
+    pe = np.random.default_rng(seed_pe).lognormal(0.0, 1.0, count)
+    return ns, pe
+
+
+def cd_batch_system(fc, ctx, n, pe_cell, seed):
+    """One problem of the batched configuration on ctx: the n^3 perturbed hex
+    mesh of [0, 2 pi]^3 (interior vertices moved by up to 0.15 h, seed), the
+    velocity above, uniform gamma = U h / pe_cell with U = 0.5, h = 2 pi / n,
+    the Gaussian source.  Returns (ia, ja, diag, a, b, xyz): 1-based CSR
+    pattern, values, right-hand side and cell centres (x..., y..., z...)."""
+    m = fc.Mesh.box(n, n, n, TWO_PI, TWO_PI, TWO_PI, perturb=0.15, seed=seed)
+    ctx.set_mesh(m)
+    _, fm, _ = cd_inputs(fc, m)
+    ctx.field_set("flmass", fm)
+    xc, yc, zc = ctx.geometry("xc"), ctx.geometry("yc"), ctx.geometry("zc")
+    gamma = np.full(m.numCells, 0.5 * (TWO_PI / n) / pe_cell)
+    ctx.cd_assemble(gamma, cd_source(xc, yc, zc))
+    ia, ja, dg, _, _ = ctx.csr_pattern()
+    return ia, ja, dg, ctx.field_get("a"), ctx.field_get("su"), np.concatenate([xc, yc, zc])

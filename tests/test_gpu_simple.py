@@ -109,6 +109,24 @@ def test_calcp_simple_assembly_bit_exact(ctx, fc):
     assert r4 == pytest.approx(oc.scalar("resor4"), rel=1e-6)
 
 
+def test_simple_iterations_batched_momentum_track_oracle(ctx, fc):
+    """U, V, W solved in one batched launch (three block groups) follow the
+    oracle's sequential solves as closely as the sequential GPU path does."""
+    m, oc = setup_cavity(ctx, fc, "cav_itb", 10, 10, 10)
+    ctx.simple_batched_momentum(True)
+    try:
+        res_g, res_o = [], []
+        for it in range(8):
+            res_g.append(ctx.simple_iteration())
+            res_o.append(oc.simple_iteration()[1])
+    finally:
+        ctx.simple_batched_momentum(False)
+    np.testing.assert_allclose(np.array(res_g), np.array(res_o), rtol=1e-7)
+    for k in ("u", "v", "w", "p"):
+        g, o = ctx.field_get(k), oc.get(k)
+        assert np.abs(g - o).max() <= 1e-8 * np.abs(o).max(), k
+
+
 @pytest.mark.parametrize("tets", [False, True])
 def test_simple_iterations_track_oracle(ctx, fc, tets):
     n = (4, 4, 3) if tets else (10, 10, 10)

@@ -248,8 +248,11 @@ def batch_block(fc, args, dev):
     it64 = np.array([i.itr_used for i in inf64])
     out["fp64_iterations"] = {"min": int(it64.min()), "median": float(np.median(it64)), "max": int(it64.max()),
                               "not_converged": int(sum(i.status != 0 for i in inf64))}
-    ctx.set_precision(fc.FC_PREC_MIXED, args.batch_inner_tol, 0)
+    # FP32 BiCGStab as the reference writes it stalls above 1e-4 on the larger
+    # problems: without a cap an inner solve runs to the outer iteration limit
+    ctx.set_precision(fc.FC_PREC_MIXED, args.batch_inner_tol, args.batch_inner_itmax)
     out["inner_tol"] = args.batch_inner_tol
+    out["inner_itmax"] = args.batch_inner_itmax
     out["mixed_batched_model_ms"], _ = timed([(B, allidx)])
     progress(f"batch: mixed batched (model plan) {out['mixed_batched_model_ms']:.1f} ms")
     a_h = [p[3] for p in probs]
@@ -762,6 +765,7 @@ def main():
     ap.add_argument("--batch-count", type=int, default=16, help="problems of the batched leg (0: skip)")
     ap.add_argument("--batch-tol", type=float, default=1e-6, help="relative L1 tolerance there")
     ap.add_argument("--batch-inner-tol", type=float, default=1e-4, help="FP32 inner tolerance there")
+    ap.add_argument("--batch-inner-itmax", type=int, default=100, help="FP32 inner iteration cap there")
     ap.add_argument("--batch-reps", type=int, default=2, help="timed repetitions of each batched leg")
     ap.add_argument("--batch-tune-rounds", type=int, default=2, help="autotuner plans tried")
     ap.add_argument("--batch-cpu-seconds", type=float, default=10.0, help="oracle time of the CPU estimate")

@@ -77,7 +77,7 @@ def build(verbose=False, jobs=None):
             if r.returncode:
                 raise RuntimeError("compile failed: " + c[-3])
     if cmds or not os.path.exists(LIB) or _stale(LIB, objs):
-        link = [nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        link = [nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lpthread"]
         r = subprocess.run(link, capture_output=True, text=True)
         if r.returncode:
             sys.stdout.write(r.stdout + r.stderr)

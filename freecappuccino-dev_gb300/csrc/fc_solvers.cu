@@ -753,19 +753,9 @@ int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, c
     tiles = std::min(tiles_req, sms);
     s->est_sweep_us = 0.0;
   } else {
-    std::vector<int> levs;
-    const int nls = symmetric_levels(n, ia.data(), ja.data(), dg.data(), levs);
-    double best = 1e300;
-    const int cand[4] = {sms, (3 * sms) / 4, sms / 2, sms / 4};
-    std::vector<int> scratch(nnz, 0);
-    for (int ci = 0; ci < 4; ++ci) {
-      if (cand[ci] < 1 || (ci > 0 && cand[ci] == cand[ci - 1])) continue;
-      SweepSchedule trial;
-      build_sweep_schedule(n, ia.data(), ja.data(), dg.data(), levs, nls, true, cand[ci], xyz, trial, scratch);
-      const double est = estimate_sweep_us(trial, FC_SWEEP_TAU0_US, FC_SWEEP_ROW_US, FC_SWEEP_HOP_US);
-      if (est < best) { best = est; tiles = cand[ci]; }
-    }
-    s->est_sweep_us = best;
+    const std::vector<int> cand = {sms, (3 * sms) / 4, sms / 2, sms / 4};
+    tiles = pick_sweep_tiles(n, ia.data(), ja.data(), dg.data(), xyz, cand, FC_SWEEP_TAU0_US, FC_SWEEP_ROW_US,
+                             FC_SWEEP_HOP_US, &s->est_sweep_us);
   }
   OrderedSweep O;
   SweepSchedule S;

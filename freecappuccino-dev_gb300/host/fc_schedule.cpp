@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <deque>
 #include <numeric>
+#include <thread>
 #include <utility>
 
 namespace {
@@ -350,6 +351,34 @@ double estimate_sweep_us(const SweepSchedule& S, double tau0, double per_row, do
 }
 
 // ---------------------------------------------------------------------------
+int pick_sweep_tiles(int n, const int* ia, const int* ja, const int* dg, const double* xyz, const std::vector<int>& cand,
+                     double tau0, double per_row, double hop, double* best_est) {
+  std::vector<int> lev;
+  const int nls = symmetric_levels(n, ia, ja, dg, lev);
+  const int nc = (int)cand.size();
+  std::vector<double> est(nc, 1e300);
+  auto trial = [&](int c) {
+    std::vector<int> code(ia[n], 0);
+    SweepSchedule S;
+    build_sweep_schedule(n, ia, ja, dg, lev, nls, true, cand[c], xyz, S, code);
+    est[c] = estimate_sweep_us(S, tau0, per_row, hop);
+  };
+  std::vector<std::thread> th;
+  for (int c = 0; c < nc; ++c) {
+    if (cand[c] < 1) continue;
+    bool dup = false;
+    for (int d = 0; d < c; ++d) dup = dup || cand[d] == cand[c];
+    if (dup) continue;
+    th.emplace_back(trial, c);
+  }
+  for (std::thread& t : th) t.join();
+  int best = -1;
+  for (int c = 0; c < nc; ++c)
+    if (best < 0 || est[c] < est[best]) best = c;
+  if (best_est) *best_est = best >= 0 ? est[best] : 0.0;
+  return best >= 0 && est[best] < 1e300 ? cand[best] : (nc ? std::max(1, cand[0]) : 1);
+}
+
 int symmetric_levels(int n, const int* ia, const int* ja, const int* dg, std::vector<int>& lev) {
   lev.assign(n, 0);
   for (int i = 0; i < n; ++i) {

@@ -108,6 +108,13 @@ struct OrderedSweep {
 // j < i with a_ij != 0 or a_ji != 0; returns the number of levels
 int symmetric_levels(int n, const int* ia, const int* ja, const int* dg, std::vector<int>& lev);
 
+// The tile count among cand whose forward schedule has the smallest
+// critical-path estimate (the trials are built concurrently, one thread
+// each; ties go to the earlier candidate, duplicates and counts < 1 are
+// skipped).  best_est (optional) receives that estimate.
+int pick_sweep_tiles(int n, const int* ia, const int* ja, const int* dg, const double* xyz, const std::vector<int>& cand,
+                     double tau0, double per_row, double hop, double* best_est);
+
 // ia, ja, dg 0-based; ts (optional) the transpose slot of every entry;
 // ntiles the tile target; xyz (optional) row coordinates for the tiling; R
 // the ring depth; wmax > 0 caps the rows of a step (a wider level of a tile

@@ -45,3 +45,24 @@ def test_ordered_sweep_replay_matches_substitution(replay, args):
     out = subprocess.run([replay] + args.split(), capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stdout + out.stderr
     assert out.stdout.strip().endswith("OK"), out.stdout
+
+
+@pytest.fixture(scope="module")
+def pick_tiles(tmp_path_factory):
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("g++ not available")
+    exe = str(tmp_path_factory.mktemp("pick") / "pick_tiles_replay")
+    subprocess.run([gxx, "-std=c++17", "-O2", "-pthread", "-I", HOST,
+                    os.path.join(HERE, "replay", "pick_tiles_replay.cpp"), os.path.join(HOST, "fc_schedule.cpp"),
+                    "-o", exe], check=True)
+    return exe
+
+
+@pytest.mark.parametrize("case", ["40 30 20 152", "7 5 3 152", "30 30 30 16 0", "3 1 1 4", "64 64 64 152"])
+def test_concurrent_tile_choice_matches_sequential(pick_tiles, case):
+    """The pattern analysis builds its candidate tile counts concurrently
+    (pick_sweep_tiles); the choice and its estimate equal building them one
+    after another."""
+    out = subprocess.run([pick_tiles] + case.split(), capture_output=True, text=True, check=True).stdout.split()
+    assert out[0] == out[2] and out[1] == out[3], out

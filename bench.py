@@ -582,6 +582,22 @@ def adjoint_block(fc, args, dev):
             "fd_max_rel_err": float(max(rel)), "fd_median_rel_err": float(np.median(rel))}
 
 
+def max_over_ranks(dist, x):
+    """x maximised over the ranks of the process group (x itself without one)."""
+    if not dist:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0])
+
+
+def replica_throughput(world, steps, elapsed_ms):
+    """Whole-job solves per second of independent replicas: every rank solves
+    `steps` systems, elapsed_ms is the slowest rank's time."""
+    return world * steps / (elapsed_ms / 1e3)
+
+
 def run_gpu(args, rank, world, dist):
     fc = load_fc()
     dev = int(os.environ.get("LOCAL_RANK", "0"))
@@ -618,13 +634,9 @@ def run_gpu(args, rank, world, dist):
         ctx.event(1)
         elapsed = ctx.elapsed_ms()
     launches = ctx.kernel_launches() - launches0
-    if dist:
-        import torch
-        t = torch.tensor([elapsed], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t[0])
+    elapsed = max_over_ranks(dist, elapsed)
     ms_per_step = elapsed / args.steps
-    value = world * args.steps / (elapsed / 1e3)
+    value = replica_throughput(world, args.steps, elapsed)
 
     # end to end through the csrsolve drop-in with host buffers
     ia, ja, dg, _, _ = ctx.csr_pattern()
@@ -745,7 +757,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--n", type=int, default=128, help="cells per side of the cube")
+    ap.add_argument("--n", "--cells-per-side", dest="n", type=int, default=128, help="cells per side of the cube")
     ap.add_argument("--ref-sample", type=int, default=120, help="ICCG iterations per CPU sample")
     ap.add_argument("--ref-iters", type=int, default=0, help="iterations of a full solve for the reference arm")
     ap.add_argument("--no-cpu", action="store_true")

@@ -152,6 +152,7 @@ static int take(fc_ctx* ctx, const double* src, double* dst, size_t n) {
 }
 
 extern "C" int fc_cd_assemble(fc_ctx* ctx, const double* gamma, const double* source) {
+  FC_RANGE();
   if (!ctx || !gamma || !source) return FC_ERR_BAD_INPUT;
   if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
   AdjState* S;
@@ -177,6 +178,7 @@ static void info_of(const SolveResult& r, fc_solve_info* info) {
 }
 
 extern "C" int fc_cd_solve(fc_ctx* ctx, double* phi, int itr_max, double tol_rel, fc_solve_info* info) {
+  FC_RANGE();
   if (!ctx || itr_max < 0) return FC_ERR_BAD_INPUT;
   if (!ctx->has_mesh || !ctx->adj || ctx->adj->gen != ctx->mesh_gen)
     return fc_fail_msg(ctx, FC_ERR_STATE, "fc_cd_assemble not called for this mesh");
@@ -185,6 +187,7 @@ extern "C" int fc_cd_solve(fc_ctx* ctx, double* phi, int itr_max, double tol_rel
   FC_CUDA_TRY(ctx, cudaMemsetAsync(S->phi.p, 0, (size_t)sys->n * sizeof(double), ctx->stream));
   SolveResult r;
   int st = sys_solve(ctx, sys, "bicgstab", sys->a.p, S->phi.p, ctx_fields(ctx).su.p, itr_max, 0.0, tol_rel, &r);
+  if (!st) log_solve(ctx, "fc_cd_solve", "bicgstab", "phi", sys->n, r);
   info_of(r, info);
   if (st) return st;
   if (phi) FC_CUDA_TRY(ctx, cudaMemcpyAsync(phi, S->phi.p, sys->n * sizeof(double), cudaMemcpyDefault, ctx->stream));
@@ -194,6 +197,7 @@ extern "C" int fc_cd_solve(fc_ctx* ctx, double* phi, int itr_max, double tol_rel
 
 extern "C" int fc_cd_adjoint(fc_ctx* ctx, const double* dJdphi, double* lambda, double* dJdgamma, int itr_max,
                              double tol_rel, fc_solve_info* info) {
+  FC_RANGE();
   if (!ctx || !dJdphi || itr_max < 0) return FC_ERR_BAD_INPUT;
   if (!ctx->has_mesh || !ctx->adj || ctx->adj->gen != ctx->mesh_gen)
     return fc_fail_msg(ctx, FC_ERR_STATE, "fc_cd_assemble and fc_cd_solve not called for this mesh");
@@ -207,6 +211,7 @@ extern "C" int fc_cd_adjoint(fc_ctx* ctx, const double* dJdphi, double* lambda, 
   FC_CUDA_TRY(ctx, cudaMemsetAsync(S->lam.p, 0, (size_t)sys->n * sizeof(double), ctx->stream));
   SolveResult r;
   st = sys_solve(ctx, sys, "bicgstab", S->aT.p, S->lam.p, S->rhs.p, itr_max, 0.0, tol_rel, &r);
+  if (!st) log_solve(ctx, "fc_cd_adjoint", "bicgstab", "lambda", sys->n, r);
   info_of(r, info);
   if (st) return st;
   if (M.nI) k_adj_face<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, S->phi.p, S->lam.p, S->sf.p);

@@ -68,6 +68,7 @@ extern "C" void fc_finalize(fc_ctx* ctx) {
   cudaEventDestroy(ctx->sev0);
   cudaEventDestroy(ctx->sev1);
   cudaStreamDestroy(ctx->stream);
+  if (ctx->solve_log) std::fclose(ctx->solve_log);
   delete ctx;
 }
 
@@ -173,6 +174,47 @@ void report_solve(fc_ctx* ctx, const char* solver, const char* chvar, const Solv
   if (ctx->verbosity) print_report(solver ? solver : "", chvar, r);
 }
 
+// JSON number (null for NaN/Inf, which JSON cannot hold)
+static void json_num(std::string& o, const char* key, double v) {
+  char buf[64];
+  if (std::isfinite(v)) std::snprintf(buf, sizeof buf, "\"%s\": %.17g", key, v);
+  else std::snprintf(buf, sizeof buf, "\"%s\": null", key);
+  o += buf;
+}
+
+void log_solve(fc_ctx* ctx, const char* api, const char* solver, const char* chvar, int n, const SolveResult& r) {
+  if (!ctx->solve_log) return;
+  char buf[256];
+  std::snprintf(buf, sizeof buf,
+                "{\"api\": \"%s\", \"solver\": \"%s\", \"var\": \"%s\", \"n\": %d, \"precision\": %d, "
+                "\"status\": %d, \"iterations\": %d, \"outer\": %d, \"early\": %d, ",
+                api ? api : "", solver ? solver : "", chvar ? chvar : "", n, ctx->precision, r.status, r.itr_used,
+                r.outer, r.early);
+  std::string o(buf);
+  json_num(o, "res0_l1", r.res0);
+  o += ", ";
+  json_num(o, "resl", r.resl);
+  o += ", ";
+  json_num(o, "resor", r.resor);
+  o += ", ";
+  json_num(o, "factor", r.factor);
+  o += ", ";
+  json_num(o, "ms", r.ms);
+  o += "}\n";
+  std::fputs(o.c_str(), ctx->solve_log);
+  std::fflush(ctx->solve_log);
+}
+
+extern "C" int fc_set_solve_log(fc_ctx* ctx, const char* path) {
+  if (!ctx) return FC_ERR_BAD_INPUT;
+  if (ctx->solve_log) std::fclose(ctx->solve_log);
+  ctx->solve_log = nullptr;
+  if (!path || !*path) return FC_OK;
+  ctx->solve_log = std::fopen(path, "a");
+  if (!ctx->solve_log) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, std::string("fc_set_solve_log: cannot open ") + path);
+  return FC_OK;
+}
+
 static void fill_info(fc_solve_info* info, const SolveResult& r) {
   if (!info) return;
   info->status = r.status;
@@ -199,6 +241,7 @@ extern "C" int fc_csrsolve(fc_ctx* ctx, const char* solver, int n, int nnz, cons
                            const double* a, const int* diag, double* fi, const double* rhs, double* res0,
                            int itr_max, double tol_abs, double tol_rel, const char* chvar, int verbose,
                            fc_solve_info* info) {
+  FC_RANGE();
   if (!ctx || !solver || !ia || !ja || !a || !diag || !fi || !rhs || n <= 0 || nnz < n || itr_max < 0)
     return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_csrsolve: bad arguments");
   std::string sv(solver);
@@ -226,12 +269,14 @@ extern "C" int fc_csrsolve(fc_ctx* ctx, const char* solver, int n, int nnz, cons
   if (res0 && !r.early) *res0 = r.resor;
   fill_info(info, r);
   if (verbose || ctx->verbosity) print_report(sv, chvar, r);
+  log_solve(ctx, "fc_csrsolve", solver, chvar, n, r);
   return r.status;
 }
 
 // ------------------------------------------------------------- building blocks
 extern "C" int fc_precond_setup(fc_ctx* ctx, const char* kind, int n, int nnz, const int* ia, const int* ja,
                                 const double* a, const int* diag, double* d_out) {
+  FC_RANGE();
   if (!ctx || !kind || !d_out) return FC_ERR_BAD_INPUT;
   std::string k(kind);
   if (k != "dic" && k != "dilu") return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "kind must be 'dic' or 'dilu'");
@@ -245,6 +290,7 @@ extern "C" int fc_precond_setup(fc_ctx* ctx, const char* kind, int n, int nnz, c
 
 extern "C" int fc_precond_apply(fc_ctx* ctx, const char* kind, int n, int nnz, const int* ia, const int* ja,
                                 const double* a, const int* diag, const double* q, double* z_out) {
+  FC_RANGE();
   if (!ctx || !kind || !q || !z_out) return FC_ERR_BAD_INPUT;
   std::string k(kind);
   if (k != "dic" && k != "dilu") return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "kind must be 'dic' or 'dilu'");
@@ -263,6 +309,7 @@ int sys_ilu0(fc_ctx* ctx, CsrSystem* s, double* l_out);
 
 extern "C" int fc_spmv(fc_ctx* ctx, int n, int nnz, const int* ia, const int* ja, const double* a,
                            const int* diag, const double* x, double* y, int transpose) {
+  FC_RANGE();
   if (!ctx || !x || !y || !a) return FC_ERR_BAD_INPUT;
   CsrSystem* s = nullptr;
   int st = ext_system(ctx, n, nnz, ia, ja, diag, &s);
@@ -316,6 +363,7 @@ int solve_global(fc_ctx* ctx, const char* solver, double* x, const double* b, do
   if (st) return st;
   if (res0 && !r.early) *res0 = r.resor;
   if (ctx->verbosity) print_report(sv, chvar, r);
+  log_solve(ctx, "mesh system", solver, chvar, s->n, r);
   return r.status;
 }
 

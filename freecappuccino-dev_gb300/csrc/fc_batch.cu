@@ -31,6 +31,7 @@ struct fc_batch {
     CsrSystem* s = nullptr;
   };
   fc_ctx* ctx = nullptr;
+  int device = 0;        // the context's device (the batch may outlive the context)
   std::vector<Prob> probs;
   BatchDev* dev = nullptr;
   bool planned = false;
@@ -172,13 +173,14 @@ extern "C" int fc_batch_create(fc_ctx* ctx, fc_batch** out) {
   if (!ctx || !out) return FC_ERR_BAD_INPUT;
   fc_batch* b = new fc_batch();
   b->ctx = ctx;
+  b->device = ctx->device;
   *out = b;
   return FC_OK;
 }
 
 extern "C" int fc_batch_destroy(fc_batch* b) {
   if (!b) return FC_ERR_BAD_INPUT;
-  cudaSetDevice(b->ctx->device);
+  cudaSetDevice(b->device);
   delete b;
   return FC_OK;
 }
@@ -232,6 +234,7 @@ extern "C" int fc_batch_add(fc_batch* b, int n, int nnz, const int* ia, const in
 }
 
 extern "C" int fc_batch_plan(fc_batch* b, const int* tiles) {
+  FC_RANGE();
   if (!b) return FC_ERR_BAD_INPUT;
   fc_ctx* ctx = b->ctx;
   if (b->probs.empty()) return fc_fail_msg(ctx, FC_ERR_STATE, "fc_batch_plan: no problems");
@@ -261,6 +264,7 @@ extern "C" int fc_batch_tiles(fc_batch* b, int* tiles) {
 extern "C" int fc_batch_solve(fc_batch* b, const char* solver, const double* const* a, double* const* x,
                               const double* const* rhs, int itr_max, double tol_abs, double tol_rel,
                               fc_solve_info* info) {
+  FC_RANGE();
   if (!b || !solver || !a || !x || !rhs || itr_max < 0) return FC_ERR_BAD_INPUT;
   fc_ctx* ctx = b->ctx;
   cudaSetDevice(ctx->device);
@@ -269,13 +273,21 @@ extern "C" int fc_batch_solve(fc_batch* b, const char* solver, const double* con
   std::vector<BatchItem> items;
   double ms = 0;
   if ((st = run(b, solver, a, x, rhs, false, itr_max, tol_abs, tol_rel, items, &ms))) return st;
-  for (size_t p = 0; p < items.size(); ++p) fill(info ? info + p : nullptr, items[p].res, items[p].dev_ms);
+  for (size_t p = 0; p < items.size(); ++p) {
+    fill(info ? info + p : nullptr, items[p].res, items[p].dev_ms);
+    if (ctx->solve_log) {
+      SolveResult r = items[p].res;
+      r.ms = items[p].dev_ms;
+      log_solve(ctx, "fc_batch_solve", solver, ("problem " + std::to_string(p)).c_str(), b->probs[p].n, r);
+    }
+  }
   return worst_status(b, items);
 }
 
 extern "C" int fc_batch_tune(fc_batch* b, const char* solver, const double* const* a, const double* const* x0,
                              const double* const* rhs, int itr_max, double tol_abs, double tol_rel, int rounds,
                              double* best_ms) {
+  FC_RANGE();
   if (!b || !solver || !a || !x0 || !rhs || rounds < 1) return FC_ERR_BAD_INPUT;
   fc_ctx* ctx = b->ctx;
   cudaSetDevice(ctx->device);

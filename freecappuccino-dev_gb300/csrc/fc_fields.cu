@@ -89,6 +89,7 @@ void launch_soa_to_aos(cudaStream_t st, const double* s, double* a, int n) {
 // copy a field in: values (count doubles, host or device).  Gradient fields
 // take the (3,numTotal) layout.  "a" sets the global matrix values (nnz).
 extern "C" int fc_field_set(fc_ctx* ctx, const char* name, const double* values, long long count) {
+  FC_RANGE();
   if (!ctx || !name || !values) return FC_ERR_BAD_INPUT;
   if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
   std::string nm(name);
@@ -115,7 +116,8 @@ extern "C" int fc_field_set(fc_ctx* ctx, const char* name, const double* values,
   return FC_OK;
 }
 
-extern "C" int fc_field_get(fc_ctx* ctx, const char* name, double* out, long long count) {
+// copies of a field into out, enqueued on the context's stream
+static int field_get_async(fc_ctx* ctx, const char* name, double* out, long long count) {
   if (!ctx || !name || !out) return FC_ERR_BAD_INPUT;
   if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
   std::string nm(name);
@@ -138,6 +140,25 @@ extern "C" int fc_field_get(fc_ctx* ctx, const char* name, double* out, long lon
     } else {
       FC_CUDA_TRY(ctx, cudaMemcpyAsync(out, s->vec->p, s->n * sizeof(double), kind, ctx->stream));
     }
+  }
+  return FC_OK;
+}
+
+extern "C" int fc_field_get(fc_ctx* ctx, const char* name, double* out, long long count) {
+  FC_RANGE();
+  int st = field_get_async(ctx, name, out, count);
+  if (st) return st;
+  FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return FC_OK;
+}
+
+extern "C" int fc_download_fields(fc_ctx* ctx, int nfields, const char* const* names, double* const* out,
+                                  const long long* counts) {
+  FC_RANGE();
+  if (!ctx || nfields < 0 || (nfields && (!names || !out || !counts))) return FC_ERR_BAD_INPUT;
+  for (int k = 0; k < nfields; ++k) {
+    int st = field_get_async(ctx, names[k], out[k], counts[k]);
+    if (st) return st;
   }
   FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   return FC_OK;

@@ -239,6 +239,7 @@ int fv_grad(fc_ctx* ctx, int scheme, const double* phi, double* g) {
 // grad(phi, dPhidxi) of the reference (gradients.f90:106-163, no limiter)
 // phi: numTotal values, dphi: (3,numTotal); host or device memory
 extern "C" int fc_grad(fc_ctx* ctx, int scheme, const double* phi, double* dphi) {
+  FC_RANGE();
   if (!ctx || !phi || !dphi) return FC_ERR_BAD_INPUT;
   if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
   FieldStore& F = ctx_fields(ctx);
@@ -266,6 +267,7 @@ extern "C" int fc_grad(fc_ctx* ctx, int scheme, const double* phi, double* dphi)
 // su accumulated with the Dirichlet boundary terms (su is not cleared, as in
 // the reference).  mu: numCells, phi: numTotal (host or device).
 extern "C" int fc_laplacian(fc_ctx* ctx, const double* mu, const double* phi, unsigned long long dirichlet_mask) {
+  FC_RANGE();
   if (!ctx || !mu || !phi) return FC_ERR_BAD_INPUT;
   if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
   MeshView M = mesh_view(ctx);
@@ -295,6 +297,7 @@ extern "C" int fc_laplacian(fc_ctx* ctx, const double* mu, const double* phi, un
 extern "C" int fc_solve_field(fc_ctx* ctx, const char* solver, const char* x_field, const char* rhs_field,
                               double* res0, int itr_max, double tol_abs, double tol_rel, const char* chvar,
                               fc_solve_info* info) {
+  FC_RANGE();
   if (!ctx || !solver || !x_field || !rhs_field) return FC_ERR_BAD_INPUT;
   if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
   FieldSlot* xs = find_field(ctx, x_field);

@@ -2,8 +2,10 @@
 // the CSR system (pattern analysis + solver workspace) and the mesh on device.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
+#include <cstdio>
 #include <string>
 #include <vector>
 
@@ -142,6 +144,16 @@ struct FieldStore;
 struct SimpleState;
 struct AdjState;
 
+// NVTX range over a C-ABI call, named after the function (shown by Nsight
+// timelines; a no-op when no tool is attached)
+struct FcRange {
+  explicit FcRange(const char* name) { nvtxRangePushA(name); }
+  ~FcRange() { nvtxRangePop(); }
+  FcRange(const FcRange&) = delete;
+  FcRange& operator=(const FcRange&) = delete;
+};
+#define FC_RANGE() FcRange fc_range_guard_(__func__)
+
 struct fc_ctx {
   int device = 0;
   int num_sms = 0;
@@ -164,6 +176,7 @@ struct fc_ctx {
   long long kernel_launches = 0;
   int tracing = 0, trace_blocks = 0, trace_cap = 0;
   int sweep_cap = 0;   // rows per sweep step cap of the next pattern analyses (0: as wide as fits)
+  std::FILE* solve_log = nullptr;  // JSON line per solve (fc_set_solve_log)
   DVec<unsigned long long> trace;
 };
 
@@ -218,6 +231,8 @@ struct BatchDev;         // device arrays of the batched launches (fc_solvers.cu
 void batch_dev_release(BatchDev* d);
 // the reference's solver report line of a solve (when ctx->verbosity is set)
 void report_solve(fc_ctx* ctx, const char* solver, const char* chvar, const SolveResult& r);
+// one JSON line for the solve in the context's solve log, if one is open
+void log_solve(fc_ctx* ctx, const char* api, const char* solver, const char* chvar, int n, const SolveResult& r);
 // Resident blocks of the batched BiCGStab kernel (FP64 and FP32 together).
 int batch_block_budget(fc_ctx* ctx, int* budget);
 // Solves every item: one persistent launch whose block groups are the

@@ -169,6 +169,7 @@ static int up(fc_ctx* ctx, DVec<T>& d, const T* h, size_t n) {
 // one-time topology bookkeeping (cell -> face lists, CSR pattern, slot
 // maps); the geometry is computed on the device.
 extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
+  FC_RANGE();
   if (!ctx || !hm) return FC_ERR_BAD_INPUT;
   std::string why;
   if (hm->validate(&why) != FC_OK) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_set_mesh: " + why);

@@ -821,6 +821,7 @@ extern "C" int fc_simple_set_params(fc_ctx* ctx, const fc_simple_params* prm) {
 }
 
 extern "C" int fc_gradp_and_sources(fc_ctx* ctx, const char* field) {
+  FC_RANGE();
   if (!ctx || !field) return FC_ERR_BAD_INPUT;
   if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
   Dev D;
@@ -834,6 +835,7 @@ extern "C" int fc_gradp_and_sources(fc_ctx* ctx, const char* field) {
 }
 
 extern "C" int fc_init_flmass(fc_ctx* ctx) {
+  FC_RANGE();
   if (!ctx) return FC_ERR_BAD_INPUT;
   if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
   Dev D;
@@ -847,6 +849,7 @@ extern "C" int fc_init_flmass(fc_ctx* ctx) {
 }
 
 extern "C" int fc_update_velocity_at_boundary(fc_ctx* ctx) {
+  FC_RANGE();
   if (!ctx || !ctx->has_mesh) return FC_ERR_STATE;
   Dev D;
   int st = make_dev(ctx, D);
@@ -901,6 +904,7 @@ static int solve_into(fc_ctx* ctx, const char* solver, double* x, const double* 
 // calcuvw, velocity.f90:50-750 (steady SIMPLE; no buoyancy, MHD, transient
 // or periodic terms).  resor[0..2] receive the normalised initial residuals.
 extern "C" int fc_calcuvw(fc_ctx* ctx, double* resor) {
+  FC_RANGE();
   if (!ctx) return FC_ERR_BAD_INPUT;
   if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
   SimpleState& S = sstate(ctx);
@@ -956,6 +960,7 @@ extern "C" int fc_calcuvw(fc_ctx* ctx, double* resor) {
       if (rs.status < 0) return fc_fail_msg(ctx, rs.status, "solver reported an error (NaN/Inf or breakdown)");
       if (!rs.early) r[k] = rs.resor;
       report_solve(ctx, "bicgstab", nm[k], rs);
+      log_solve(ctx, "mesh system (batched)", "bicgstab", nm[k], M.nC, rs);
     }
     // the matrix and source arrays end as the sequential passes leave them
     FC_CUDA_TRY(ctx, cudaMemcpyAsync(D.a, mb.aw.p, nnz * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
@@ -991,6 +996,7 @@ extern "C" int fc_calcuvw(fc_ctx* ctx, double* resor) {
 // calcp_simple, calcp_simple.f90:1-470 (incompressible; no periodic or
 // pressure boundaries).  *resor4 receives resor(4) as continuityErrors sets it.
 extern "C" int fc_calcp_simple(fc_ctx* ctx, double* resor4) {
+  FC_RANGE();
   if (!ctx) return FC_ERR_BAD_INPUT;
   if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
   SimpleState& S = sstate(ctx);
@@ -1047,6 +1053,7 @@ extern "C" int fc_calcp_simple(fc_ctx* ctx, double* resor4) {
 
 // one outer iteration of main.f90:150-267 (calcuvw + calcp_simple)
 extern "C" int fc_simple_iteration(fc_ctx* ctx, double* resor) {
+  FC_RANGE();
   double r[4];
   int st = fc_calcuvw(ctx, r);
   if (st < 0) return st;
@@ -1100,6 +1107,7 @@ extern "C" int fc_temperature_set_params(fc_ctx* ctx, const fc_temperature_param
 // calculate_temperature, temperature.f90:35-385 (steady; no turbulent heat
 // flux, Crank-Nicolson or periodic terms)
 extern "C" int fc_calculate_temperature(fc_ctx* ctx, int solve, double* resor7) {
+  FC_RANGE();
   if (!ctx) return FC_ERR_BAD_INPUT;
   if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
   SimpleState& S = sstate(ctx);

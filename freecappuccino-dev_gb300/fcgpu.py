@@ -120,6 +120,8 @@ def lib():
         "fc_cd_solve": (i, [vp, vp, i, d, C.POINTER(SolveInfo)]),
         "fc_cd_adjoint": (i, [vp, vp, vp, vp, i, d, C.POINTER(SolveInfo)]),
         "fc_simple_set_batched_momentum": (i, [vp, i]),
+        "fc_set_solve_log": (i, [vp, cp]),
+        "fc_download_fields": (i, [vp, i, vp, vp, vp]),
         "fc_batch_create": (i, [vp, vp]),
         "fc_batch_destroy": (i, [vp]),
         "fc_batch_add": (i, [vp, i, i, vp, vp, vp, vp]),
@@ -605,6 +607,19 @@ class Context:
                                   C.byref(info))
         self._check(st, "fc_cd_adjoint")
         return lam, grad, info
+
+    def set_solve_log(self, path):
+        """JSON line per solve appended to path (None: stop)."""
+        self._check(self.L.fc_set_solve_log(self.h, path.encode() if path else None), "fc_set_solve_log")
+
+    def download_fields(self, names):
+        """{name: numpy array} of several fields, one synchronisation."""
+        outs = [np.zeros(self.field_len(nm)) for nm in names]
+        cn = (C.c_char_p * len(names))(*[nm.encode() for nm in names])
+        po = (C.c_void_p * len(names))(*[o.ctypes.data for o in outs])
+        cnt = (C.c_longlong * len(names))(*[len(o) for o in outs])
+        self._check(self.L.fc_download_fields(self.h, len(names), cn, po, cnt), "fc_download_fields")
+        return dict(zip(names, outs))
 
     def simple_batched_momentum(self, on=True):
         """calcuvw solves U, V, W in one batched launch (bicgstab only)."""

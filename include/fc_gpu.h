@@ -174,6 +174,15 @@ int fc_sweep_stats(fc_ctx* ctx, int which, double* out);
  * a mesh's widest step does not fit (e.g. 6 million tetrahedra).  Tuning and
  * testing only: no counterpart in the reference. */
 int fc_set_sweep_cap(fc_ctx* ctx, int rows);
+/* Appends one JSON line per solve to the file at path (NULL or "": stop):
+ * the entry point, solver, variable, rows, precision mode, status,
+ * iterations, refinement steps, early exit, res0 (L1), final residual,
+ * resor, factor and device ms, the numbers of the reference's report line
+ * (linear_solvers.f90:540-541) in machine-readable form.  Solves through
+ * fc_csrsolve, the mesh system (SIMPLE, temperature, fc_solve_field), the
+ * batched solves and the adjoint are logged.  No counterpart in the
+ * reference. */
+int fc_set_solve_log(fc_ctx* ctx, const char* path);
 /* Colours of the multicolour ordering FC_PREC_MIXED_COLOURED uses for the
  * same systems (which as above); builds the ordering if no solve has yet.
  * Diagnostics only: no counterpart in the reference. */
@@ -276,6 +285,12 @@ int fc_get_csr_pattern(fc_ctx* ctx, int* n, int* nnz, int* ia, int* ja, int* dia
  * global matrix).  count must equal the field length. */
 int fc_field_set(fc_ctx* ctx, const char* name, const double* values, long long count);
 int fc_field_get(fc_ctx* ctx, const char* name, double* out, long long count);
+/* Several fields at once with one stream synchronisation: the device-to-host
+ * step before a restart dump (write_restart_files,
+ * src/io/write_restart_files.f90, stays on the host; after readfiles the
+ * fields go back with fc_field_set).  counts[k] as fc_field_get's count. */
+int fc_download_fields(fc_ctx* ctx, int nfields, const char* const* names, double* const* out,
+                       const long long* counts);
 int fc_field_fill(fc_ctx* ctx, const char* name, double value);
 double* fc_field_ptr(fc_ctx* ctx, const char* name);  /* device address, NULL if unknown */
 

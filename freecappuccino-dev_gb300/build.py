@@ -22,7 +22,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-r
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + INCLUDE, "-I" + HOST, "-I" + CSRC]
 # Translation units whose FP64 expressions are written in the reference's
 # evaluation order and must not be contracted into FMAs.
-PER_FILE = {"fc_simple.cu": ["--fmad=false"], "fc_adjoint.cu": ["--fmad=false"]}
+PER_FILE = {"fc_simple.cu": ["--fmad=false"], "fc_adjoint.cu": ["--fmad=false"], "fc_limiter.cu": ["--fmad=false"]}
 
 
 def _nvcc():

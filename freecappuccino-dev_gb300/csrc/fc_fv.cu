@@ -228,6 +228,9 @@ int fv_grad(fc_ctx* ctx, int scheme, const double* phi, double* g) {
   } else {
     return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "unknown gradient scheme");
   }
+  // the limiter of grad_scalar_field (gradients.f90:141-160), cells only
+  int st = fv_limit(ctx, phi, g);
+  if (st) return st;
   if (M.nT > M.nC) {
     k_zero_bnd_grad<<<grid_for(M.nT - M.nC), 256, 0, ctx->stream>>>(g, M.nC, M.nT);
     ctx->kernel_launches++;
@@ -236,7 +239,8 @@ int fv_grad(fc_ctx* ctx, int scheme, const double* phi, double* g) {
   return FC_OK;
 }
 
-// grad(phi, dPhidxi) of the reference (gradients.f90:106-163, no limiter)
+// grad(phi, dPhidxi) of the reference (gradients.f90:106-163), with the
+// context's limiter
 // phi: numTotal values, dphi: (3,numTotal); host or device memory
 extern "C" int fc_grad(fc_ctx* ctx, int scheme, const double* phi, double* dphi) {
   FC_RANGE();

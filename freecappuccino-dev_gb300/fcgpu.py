@@ -28,6 +28,7 @@ FC_ERR_UNSUPPORTED = -7
 FC_ERR_ZERO_PIVOT = -8
 
 BC = {"wall": 1, "inlet": 2, "outlet": 3, "symmetry": 4, "pressure": 5, "empty": 6, "periodic": 7}
+FC_LIMITER_NONE, FC_LIMITER_BJ, FC_LIMITER_VENKAT, FC_LIMITER_R, FC_LIMITER_MD = 0, 1, 2, 3, 4
 FC_PREC_FP64 = 0
 FC_PREC_MIXED = 1
 FC_PREC_MIXED_COLOURED = 2
@@ -121,6 +122,7 @@ def lib():
         "fc_cd_adjoint": (i, [vp, vp, vp, vp, i, d, C.POINTER(SolveInfo)]),
         "fc_simple_set_batched_momentum": (i, [vp, i]),
         "fc_set_solve_log": (i, [vp, cp]),
+        "fc_set_gradient_limiter": (i, [vp, i]),
         "fc_download_fields": (i, [vp, i, vp, vp, vp]),
         "fc_batch_create": (i, [vp, vp]),
         "fc_batch_destroy": (i, [vp]),
@@ -607,6 +609,10 @@ class Context:
                                   C.byref(info))
         self._check(st, "fc_cd_adjoint")
         return lam, grad, info
+
+    def set_gradient_limiter(self, kind):
+        """FC_LIMITER_* for every gradient of the context (0: none)."""
+        self._check(self.L.fc_set_gradient_limiter(self.h, int(kind)), "fc_set_gradient_limiter")
 
     def set_solve_log(self, path):
         """JSON line per solve appended to path (None: stop)."""

@@ -297,9 +297,20 @@ double* fc_field_ptr(fc_ctx* ctx, const char* name);  /* device address, NULL if
 #define FC_GRAD_GAUSS   0   /* grad_gauss    gradients.f90:1607 */
 #define FC_GRAD_LSQ     1   /* grad_lsq      gradients.f90:782  */
 #define FC_GRAD_LSQ_DM  2   /* grad_lsq_dm   gradients.f90:1334 */
-/* grad(phi, dPhidxi) (gradients.f90:106-163, no limiter): phi numTotal values,
- * dphi (3,numTotal); host or device memory. */
+/* grad(phi, dPhidxi) (gradients.f90:106-163): phi numTotal values, dphi
+ * (3,numTotal); host or device memory.  The context's limiter applies. */
 int fc_grad(fc_ctx* ctx, int scheme, const double* phi, double* dphi);
+/* The namelist's `limiter` (gradients.f90:13, applied by grad_scalar_field
+ * after every gradient, :141-160): every gradient of the context (fc_grad,
+ * the velocity and temperature gradients of calcuvw and
+ * calculate_temperature) is limited by it.  The pressure gradient of
+ * gradp_and_sources is not, as in the reference. */
+#define FC_LIMITER_NONE   0  /* 'none' / 'no-limit'                       */
+#define FC_LIMITER_BJ     1  /* 'Barth-Jespersen'   gradients.f90:288-366 */
+#define FC_LIMITER_VENKAT 2  /* 'Venkatakrishnan'   gradients.f90:373-451 */
+#define FC_LIMITER_R      3  /* 'R3' (its active line is R4) :456-535     */
+#define FC_LIMITER_MD     4  /* 'multidimensional'  gradients.f90:541-656 */
+int fc_set_gradient_limiter(fc_ctx* ctx, int kind);
 /* laplacian(mu, phi) (laplacian.f90:1-105): fills the global matrix "a" and
  * accumulates the Dirichlet terms into "su" (not cleared, as there).  Bit b
  * of dirichlet_mask enables the boundary term on patch b; ~0ULL reproduces

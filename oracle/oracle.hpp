@@ -55,6 +55,7 @@ struct Case {
   std::vector<double> res, reso, pk, zk, d, uk, vk;
   // parameters of the SIMPLE path
   int gradScheme = 0;  // 0 gauss, 1 lstsq, 2 lstsq_dm
+  int limiter = 0;     // gradients.f90:13: 0 none, 1 Barth-Jespersen, 2 Venkatakrishnan, 3 'R3', 4 multidimensional
   int pscheme = 0;     // 0 linear, 1 central, 2 weighted
   double densit = 1.0, viscos = 0.01;
   double urfU[3] = {0.8, 0.8, 0.8}, gdsU = 1.0, urfP = 0.3;
@@ -120,6 +121,7 @@ void grad_lsq(Case& c, const std::vector<double>& phi, std::vector<double>& dphi
 void create_matrix_lsq_dm(Case& c);
 void grad_lsq_dm(Case& c, const std::vector<double>& phi, std::vector<double>& dphidxi);
 void grad(Case& c, const std::vector<double>& phi, std::vector<double>& dphidxi);
+void slope_limiter(Case& c, const std::vector<double>& phi, std::vector<double>& dphidxi);
 
 // operators
 void laplacian(Case& c, const std::vector<double>& mu, const std::vector<double>& phi, unsigned long long dirichlet_mask);

@@ -145,6 +145,7 @@ int orc_case_set_param(void* h, const char* name, double val) {
   else if (n == "cSchemeU") c.cSchemeU = (int)val;
   else if (n == "gradScheme") c.gradScheme = (int)val;
   else if (n == "pscheme") c.pscheme = (int)val;
+  else if (n == "limiter") c.limiter = (int)val;
   else if (n == "maxiterU") c.maxiterU = (int)val;
   else if (n == "maxiterP") c.maxiterP = (int)val;
   else if (n == "npcor") c.npcor = (int)val;
@@ -199,6 +200,7 @@ int orc_grad(void* h, int scheme, double* phi, double* dphi) {
   if (scheme == 1) { if (c.Dmat.empty() || c.gradScheme != 1) create_matrix_lsq(c); grad_lsq(c, p, g); }
   else if (scheme == 2) { if (c.Dmat.empty() || c.gradScheme != 2) create_matrix_lsq_dm(c); grad_lsq_dm(c, p, g); }
   else grad_gauss(c, p, g);
+  slope_limiter(c, p, g);
   std::memcpy(dphi, g.data() + 3, sizeof(double) * 3 * c.numTotal);
   return 0;
 }

@@ -178,11 +178,92 @@ void grad_lsq_dm(Case& c, const std::vector<double>& phi, std::vector<double>& g
   lsq_apply(c, g);
 }
 
-// grad_scalar_field without limiter, gradients.f90:106-163
+// grad_scalar_field, gradients.f90:106-163: the gradient, then the limiter
 void grad(Case& c, const std::vector<double>& phi, std::vector<double>& g) {
   if (c.gradScheme == 1) grad_lsq(c, phi, g);
   else if (c.gradScheme == 2) grad_lsq_dm(c, phi, g);
   else grad_gauss(c, phi, g);
+  slope_limiter(c, phi, g);
+}
+
+// slope_limiter_Barth_Jespersen (:288-366), _Venkatakrishnan (:373-451) and
+// _r345 (:456-535, whose active line is the R4 function): the gradient of
+// each cell scaled by the smallest limiter value over its CSR row.  phi_min
+// of those routines is computed but never used; the deltas use the global
+// extremes.  abs(delta_face) < 1.e-6 compares with a default-real literal.
+static void limiter_scale(Case& c, const std::vector<double>& phi, std::vector<double>& g) {
+  const double tiny = (double)1.e-6f;
+  double fimin = phi[1], fimax = phi[1];
+  for (int inp = 2; inp <= c.numCells; ++inp) {
+    fimin = std::min(fimin, phi[inp]);
+    fimax = std::max(fimax, phi[inp]);
+  }
+  for (int inp = 1; inp <= c.numCells; ++inp) {
+    double deltamax = fimax - phi[inp];
+    double deltamin = fimin - phi[inp];
+    double slopelimit = 1.0;
+    for (int k = c.ia[inp]; k <= c.ia[inp + 1] - 1; ++k) {
+      if (k == c.diag[inp]) continue;
+      int ijp = inp, ijn = c.ja[k];
+      double delta_face = G(g, 1, ijp) * (c.xc[ijn] - c.xc[ijp]) + G(g, 2, ijp) * (c.yc[ijn] - c.yc[ijp]) +
+                          G(g, 3, ijp) * (c.zc[ijn] - c.zc[ijp]);
+      double r;
+      if (std::fabs(delta_face) < tiny) r = 1.0;
+      else if (delta_face > 0.0) r = deltamax / delta_face;
+      else r = deltamin / delta_face;
+      double lim;
+      if (c.limiter == 1) {
+        lim = r;
+      } else if (c.limiter == 2) {
+        lim = (r * r + 2.0 * r) / (r * r + r + 2.0);
+      } else {
+        double r2 = r * r, r3 = r2 * r, r4 = r2 * r2;
+        lim = (r4 + 2 * r3 - 4 * r2 + 8 * r) / (r4 + r3 + 2 * r2 - 4 * r + 8.0);
+      }
+      slopelimit = std::min(slopelimit, lim);
+    }
+    for (int k = 1; k <= 3; ++k) G(g, k, inp) = slopelimit * G(g, k, inp);
+  }
+}
+
+// slope_limiter_multidimensional, gradients.f90:541-656
+static void limiter_multidimensional(Case& c, const std::vector<double>& phi, std::vector<double>& g) {
+  std::vector<double> phimax(c.numCells + 1), phimin(c.numCells + 1);
+  for (int inp = 1; inp <= c.numCells; ++inp) {
+    phimax[inp] = phi[c.ja[c.ia[inp]]];
+    phimin[inp] = phi[c.ja[c.ia[inp]]];
+    for (int k = c.ia[inp] + 1; k <= c.ia[inp + 1] - 1; ++k) {
+      phimax[inp] = std::max(phimax[inp], phi[c.ja[k]]);
+      phimin[inp] = std::min(phimin[inp], phi[c.ja[k]]);
+    }
+  }
+  for (int iface = 1; iface <= c.numInnerFaces; ++iface) {
+    for (int k = 1; k <= 2; ++k) {
+      int ijp = k == 1 ? c.owner[iface] : c.neighbour[iface];
+      double gx = G(g, 1, ijp), gy = G(g, 2, ijp), gz = G(g, 3, ijp);
+      double xpn = c.xf[iface] - c.xc[ijp], ypn = c.yf[iface] - c.yc[ijp], zpn = c.zf[iface] - c.zc[ijp];
+      double dpn = std::sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
+      double nx = xpn / dpn, ny = ypn / dpn, nz = zpn / dpn;
+      double gn = gx * nx + gy * ny + gz * nz;
+      double gtx = gx - gn * nx, gty = gy - gn * ny, gtz = gz - gn * nz;
+      double dPhi = gx * xpn + gy * ypn + gz * zpn;
+      double dPhimax = phimax[ijp] - phi[ijp];
+      double dPhimin = phimin[ijp] - phi[ijp];
+      if (phimax[ijp] > phi[ijp] && dPhi > dPhimax) {
+        gx = gtx + nx * dPhimax; gy = gty + ny * dPhimax; gz = gtz + nz * dPhimax;
+      }
+      if (phimin[ijp] < phi[ijp] && dPhi < dPhimin) {
+        gx = gtx + nx * dPhimin; gy = gty + ny * dPhimin; gz = gtz + nz * dPhimin;
+      }
+      G(g, 1, ijp) = gx; G(g, 2, ijp) = gy; G(g, 3, ijp) = gz;
+    }
+  }
+}
+
+// the select case on `limiter` of grad_scalar_field, gradients.f90:141-160
+void slope_limiter(Case& c, const std::vector<double>& phi, std::vector<double>& g) {
+  if (c.limiter >= 1 && c.limiter <= 3) limiter_scale(c, phi, g);
+  else if (c.limiter == 4) limiter_multidimensional(c, phi, g);
 }
 
 // ------------------------------------------------------------ interpolation

@@ -225,6 +225,9 @@ int fv_grad(fc_ctx* ctx, int scheme, const double* phi, double* g) {
     if (scheme == FC_GRAD_LSQ) k_grad_lsq<false><<<grid_for(M.nC), 256, 0, ctx->stream>>>(M, F.dmat.p, phi, g);
     else k_grad_lsq<true><<<grid_for(M.nC), 256, 0, ctx->stream>>>(M, F.dmat.p, phi, g);
     ctx->kernel_launches++;
+  } else if (scheme == FC_GRAD_NODE_GAUSS) {
+    int st0 = fv_grad_node(ctx, phi, g);
+    if (st0) return st0;
   } else {
     return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "unknown gradient scheme");
   }

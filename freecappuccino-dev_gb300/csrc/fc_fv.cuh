@@ -46,3 +46,5 @@ fcfv::MeshView mesh_view(fc_ctx* ctx);
 int fv_grad(fc_ctx* ctx, int scheme, const double* phi, double* g);
 // the context's slope limiter applied to the SoA gradient g of phi (fc_limiter.cu)
 int fv_limit(fc_ctx* ctx, const double* phi, double* g);
+// node-based Gauss gradient of phi into the SoA g (fc_nodegrad.cu)
+int fv_grad_node(fc_ctx* ctx, const double* phi, double* g);

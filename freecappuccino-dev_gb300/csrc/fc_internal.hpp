@@ -179,6 +179,11 @@ struct fc_ctx {
   std::FILE* solve_log = nullptr;  // JSON line per solve (fc_set_solve_log)
   int grad_limiter = 0;            // FC_LIMITER_* applied by every gradient (fc_set_gradient_limiter)
   DVec<double> limiter_part;       // min/max partials of the limiters
+  // node-based Gauss gradients (fc_nodegrad.cu): cell-to-node method and the
+  // per-node gather lists built for mesh generation ng_gen
+  int node_interp = 0, ng_gen = -1, ng_method = -1;
+  DVec<int> ng_ptr, ng_src;
+  DVec<double> ng_w, ng_uN;
   DVec<unsigned long long> trace;
 };
 

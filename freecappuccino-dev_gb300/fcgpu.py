@@ -28,6 +28,8 @@ FC_ERR_UNSUPPORTED = -7
 FC_ERR_ZERO_PIVOT = -8
 
 BC = {"wall": 1, "inlet": 2, "outlet": 3, "symmetry": 4, "pressure": 5, "empty": 6, "periodic": 7}
+FC_GRAD_GAUSS, FC_GRAD_LSQ, FC_GRAD_LSQ_DM, FC_GRAD_NODE_GAUSS = 0, 1, 2, 3
+FC_C2N_PSL, FC_C2N_IDS = 0, 1
 FC_LIMITER_NONE, FC_LIMITER_BJ, FC_LIMITER_VENKAT, FC_LIMITER_R, FC_LIMITER_MD = 0, 1, 2, 3, 4
 FC_PREC_FP64 = 0
 FC_PREC_MIXED = 1
@@ -123,6 +125,7 @@ def lib():
         "fc_simple_set_batched_momentum": (i, [vp, i]),
         "fc_set_solve_log": (i, [vp, cp]),
         "fc_set_gradient_limiter": (i, [vp, i]),
+        "fc_set_node_interpolation": (i, [vp, i]),
         "fc_download_fields": (i, [vp, i, vp, vp, vp]),
         "fc_batch_create": (i, [vp, vp]),
         "fc_batch_destroy": (i, [vp]),
@@ -609,6 +612,10 @@ class Context:
                                   C.byref(info))
         self._check(st, "fc_cd_adjoint")
         return lam, grad, info
+
+    def set_node_interpolation(self, method):
+        """FC_C2N_PSL (0) or FC_C2N_IDS (1) for node-based gradients."""
+        self._check(self.L.fc_set_node_interpolation(self.h, int(method)), "fc_set_node_interpolation")
 
     def set_gradient_limiter(self, kind):
         """FC_LIMITER_* for every gradient of the context (0: none)."""

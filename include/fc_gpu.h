@@ -297,6 +297,14 @@ double* fc_field_ptr(fc_ctx* ctx, const char* name);  /* device address, NULL if
 #define FC_GRAD_GAUSS   0   /* grad_gauss    gradients.f90:1607 */
 #define FC_GRAD_LSQ     1   /* grad_lsq      gradients.f90:782  */
 #define FC_GRAD_LSQ_DM  2   /* grad_lsq_dm   gradients.f90:1334 */
+#define FC_GRAD_NODE_GAUSS 3 /* grad_node_based_gauss gradients.f90:1491, node values of node_interpolation.f90 */
+/* Cell-to-node interpolation of the node-based gradient (the `c2n` of
+ * node_interpolation.f90:36): FC_C2N_PSL pseudo-Laplacian (the default,
+ * :265-631) or FC_C2N_IDS inverse distance (:88-260).  The weights are built
+ * on the first node-based gradient after a mesh or method change. */
+#define FC_C2N_PSL 0
+#define FC_C2N_IDS 1
+int fc_set_node_interpolation(fc_ctx* ctx, int method);
 /* grad(phi, dPhidxi) (gradients.f90:106-163): phi numTotal values, dphi
  * (3,numTotal); host or device memory.  The context's limiter applies. */
 int fc_grad(fc_ctx* ctx, int scheme, const double* phi, double* dphi);

@@ -56,6 +56,9 @@ struct Case {
   // parameters of the SIMPLE path
   int gradScheme = 0;  // 0 gauss, 1 lstsq, 2 lstsq_dm
   int limiter = 0;     // gradients.f90:13: 0 none, 1 Barth-Jespersen, 2 Venkatakrishnan, 3 'R3', 4 multidimensional
+  // node_interpolation.f90: c2n 0 'psl' (pseudo-Laplacian, the default), 1 'ids' (inverse distance)
+  int c2n = 0;
+  std::vector<double> wCellToNode, wFaceToNode;  // 1-based, in the module's running order
   int pscheme = 0;     // 0 linear, 1 central, 2 weighted
   double densit = 1.0, viscos = 0.01;
   double urfU[3] = {0.8, 0.8, 0.8}, gdsU = 1.0, urfP = 0.3;
@@ -122,6 +125,9 @@ void create_matrix_lsq_dm(Case& c);
 void grad_lsq_dm(Case& c, const std::vector<double>& phi, std::vector<double>& dphidxi);
 void grad(Case& c, const std::vector<double>& phi, std::vector<double>& dphidxi);
 void slope_limiter(Case& c, const std::vector<double>& phi, std::vector<double>& dphidxi);
+void set_interpolation_weights(Case& c);
+void interpolate_to_nodes(Case& c, const std::vector<double>& phiC, std::vector<double>& phiN);
+void grad_node_based_gauss(Case& c, const std::vector<double>& u, std::vector<double>& dudxi);
 
 // operators
 void laplacian(Case& c, const std::vector<double>& mu, const std::vector<double>& phi, unsigned long long dirichlet_mask);

@@ -146,6 +146,7 @@ int orc_case_set_param(void* h, const char* name, double val) {
   else if (n == "gradScheme") c.gradScheme = (int)val;
   else if (n == "pscheme") c.pscheme = (int)val;
   else if (n == "limiter") c.limiter = (int)val;
+  else if (n == "c2n") { c.c2n = (int)val; c.wCellToNode.clear(); c.wFaceToNode.clear(); }
   else if (n == "maxiterU") c.maxiterU = (int)val;
   else if (n == "maxiterP") c.maxiterP = (int)val;
   else if (n == "npcor") c.npcor = (int)val;
@@ -192,13 +193,14 @@ double orc_case_get_scalar(void* h, const char* name) {
   return 0.0;
 }
 
-// scheme: 0 gauss, 1 lstsq, 2 lstsq_dm.  phi: numTotal; dphi: 3*numTotal
+// scheme: 0 gauss, 1 lstsq, 2 lstsq_dm, 3 node-based Gauss.  phi: numTotal; dphi: 3*numTotal
 int orc_grad(void* h, int scheme, double* phi, double* dphi) {
   Case& c = *(Case*)h;
   std::vector<double> p = pad1(phi, c.numTotal);
   std::vector<double> g(3 * (size_t)(c.numTotal + 1), 0.0);
   if (scheme == 1) { if (c.Dmat.empty() || c.gradScheme != 1) create_matrix_lsq(c); grad_lsq(c, p, g); }
   else if (scheme == 2) { if (c.Dmat.empty() || c.gradScheme != 2) create_matrix_lsq_dm(c); grad_lsq_dm(c, p, g); }
+  else if (scheme == 3) grad_node_based_gauss(c, p, g);
   else grad_gauss(c, p, g);
   slope_limiter(c, p, g);
   std::memcpy(dphi, g.data() + 3, sizeof(double) * 3 * c.numTotal);

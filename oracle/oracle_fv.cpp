@@ -182,8 +182,216 @@ void grad_lsq_dm(Case& c, const std::vector<double>& phi, std::vector<double>& g
 void grad(Case& c, const std::vector<double>& phi, std::vector<double>& g) {
   if (c.gradScheme == 1) grad_lsq(c, phi, g);
   else if (c.gradScheme == 2) grad_lsq_dm(c, phi, g);
+  else if (c.gradScheme == 3) grad_node_based_gauss(c, phi, g);
   else grad_gauss(c, phi, g);
   slope_limiter(c, phi, g);
+}
+
+// --------------------------------------------------- node interpolation
+// node_interpolation.f90: cell-to-node weights in the module's running
+// order (inner faces ascending, per face node, owner then neighbour), and
+// face-to-node weights of the boundary faces.  tiny is geometry.f90:41's
+// default-real 1e-30.
+static inline int NODE(const Case& c, int k, int iface) { return c.node[(size_t)iface * 6 + (k - 1)]; }
+
+// weights_inverse_distance, node_interpolation.f90:88-260
+static void weights_inverse_distance(Case& c) {
+  std::vector<double> dsum(c.numNodes + 1, 0.0);
+  auto dist = [&](double xa, double ya, double za, int ino) {
+    double dx = xa - c.x[ino], dy = ya - c.y[ino], dz = za - c.z[ino];
+    return std::sqrt(dx * dx + dy * dy + dz * dz);
+  };
+  int cnt = 0;
+  for (int iface = 1; iface <= c.numInnerFaces; ++iface) {
+    int ijp = c.owner[iface], ijn = c.neighbour[iface];
+    for (int k = 1; k <= c.nnodes[iface]; ++k) {
+      int ino = NODE(c, k, iface);
+      dsum[ino] = dsum[ino] + 1. / dist(c.xc[ijp], c.yc[ijp], c.zc[ijp], ino);
+      dsum[ino] = dsum[ino] + 1. / dist(c.xc[ijn], c.yc[ijn], c.zc[ijn], ino);
+      cnt += 2;
+    }
+  }
+  c.wCellToNode.assign(cnt + 1, 0.0);
+  int i = 0;
+  for (int iface = 1; iface <= c.numInnerFaces; ++iface) {
+    int ijp = c.owner[iface], ijn = c.neighbour[iface];
+    for (int k = 1; k <= c.nnodes[iface]; ++k) {
+      int ino = NODE(c, k, iface);
+      double dcp = dist(c.xc[ijp], c.yc[ijp], c.zc[ijp], ino);
+      c.wCellToNode[++i] = 1. / (dcp * dsum[ino]);
+      dcp = dist(c.xc[ijn], c.yc[ijn], c.zc[ijn], ino);
+      c.wCellToNode[++i] = 1. / (dcp * dsum[ino]);
+    }
+  }
+  std::fill(dsum.begin(), dsum.end(), 0.0);
+  cnt = 0;
+  for (int iface = c.numInnerFaces + 1; iface <= c.numFaces; ++iface)
+    for (int k = 1; k <= c.nnodes[iface]; ++k) {
+      int ino = NODE(c, k, iface);
+      dsum[ino] = dsum[ino] + 1. / dist(c.xf[iface], c.yf[iface], c.zf[iface], ino);
+      ++cnt;
+    }
+  c.wFaceToNode.assign(cnt + 1, 0.0);
+  i = 0;
+  for (int iface = c.numInnerFaces + 1; iface <= c.numFaces; ++iface)
+    for (int k = 1; k <= c.nnodes[iface]; ++k) {
+      int ino = NODE(c, k, iface);
+      double dcp = dist(c.xf[iface], c.yf[iface], c.zf[iface], ino);
+      c.wFaceToNode[++i] = 1. / (dcp * dsum[ino]);
+    }
+}
+
+// pseudo-Laplacian moments of one point about a node
+struct PslMoments {
+  std::vector<double> rx, ry, rz, ixx, iyy, izz, ixy, ixz, iyz;
+  explicit PslMoments(int n)
+      : rx(n, 0.0), ry(n, 0.0), rz(n, 0.0), ixx(n, 0.0), iyy(n, 0.0), izz(n, 0.0), ixy(n, 0.0), ixz(n, 0.0),
+        iyz(n, 0.0) {}
+  void add(int ino, double dx, double dy, double dz) {
+    rx[ino] = rx[ino] + dx; ry[ino] = ry[ino] + dy; rz[ino] = rz[ino] + dz;
+    ixx[ino] = ixx[ino] + dx * dx; iyy[ino] = iyy[ino] + dy * dy; izz[ino] = izz[ino] + dz * dz;
+    ixy[ino] = ixy[ino] + dx * dy; ixz[ino] = ixz[ino] + dx * dz; iyz[ino] = iyz[ino] + dy * dz;
+  }
+  // min(|1 + lam . d|, 1) with the lambdas as node_interpolation.f90:386-407 writes them
+  double weight(int ino, double dx, double dy, double dz) const {
+    const double Ixx = ixx[ino], Iyy = iyy[ino], Izz = izz[ino], Ixy = ixy[ino], Ixz = ixz[ino], Iyz = iyz[ino];
+    const double Rx = rx[ino], Ry = ry[ino], Rz = rz[ino];
+    double D = Ixx * (Iyy * Izz - Iyz * Iyz) - Ixy * (Ixy * Izz - Ixz * Iyz) + Ixz * (Ixy * Iyz - Iyy * Ixz) + kTiny30;
+    double lamx = (-(Rx * (Ixx * Izz - Iyz * Iyz)) + Ry * (Ixy * Izz - Ixz * Iyz) - Rz * (Ixy * Iyz - Iyy * Ixz)) / D;
+    double lamy = (Rx * (Ixy * Izz - Ixz * Iyz) - Ry * (Ixx * Izz - Ixz * Ixz) + Rz * (Ixx * Iyz - Ixy * Ixz)) / D;
+    double lamz = (-(Rx * (Ixy * Iyz - Iyy * Ixz)) + Ry * (Ixx * Iyz - Ixy * Ixz) - Rz * (Ixx * Iyy - Ixy * Ixy)) / D;
+    double w = 1.0 + lamx * dx + lamy * dy + lamz * dz;
+    return std::min(std::fabs(w), 1.0);
+  }
+};
+
+// weights_pseudolaplacian, node_interpolation.f90:265-631
+static void weights_pseudolaplacian(Case& c) {
+  const int nn = c.numNodes + 1;
+  {
+    PslMoments M(nn);
+    int cnt = 0;
+    for (int iface = 1; iface <= c.numInnerFaces; ++iface) {
+      int ijp = c.owner[iface], ijn = c.neighbour[iface];
+      for (int k = 1; k <= c.nnodes[iface]; ++k) {
+        int ino = NODE(c, k, iface);
+        M.add(ino, c.xc[ijp] - c.x[ino], c.yc[ijp] - c.y[ino], c.zc[ijp] - c.z[ino]);
+        M.add(ino, c.xc[ijn] - c.x[ino], c.yc[ijn] - c.y[ino], c.zc[ijn] - c.z[ino]);
+        cnt += 2;
+      }
+    }
+    c.wCellToNode.assign(cnt + 1, 0.0);
+    int i = 0;
+    for (int iface = 1; iface <= c.numInnerFaces; ++iface) {
+      int ijp = c.owner[iface], ijn = c.neighbour[iface];
+      for (int k = 1; k <= c.nnodes[iface]; ++k) {
+        int ino = NODE(c, k, iface);
+        c.wCellToNode[++i] = M.weight(ino, c.xc[ijp] - c.x[ino], c.yc[ijp] - c.y[ino], c.zc[ijp] - c.z[ino]);
+        c.wCellToNode[++i] = M.weight(ino, c.xc[ijn] - c.x[ino], c.yc[ijn] - c.y[ino], c.zc[ijn] - c.z[ino]);
+      }
+    }
+    std::vector<double> wsum(nn, 0.0);
+    i = 0;
+    for (int iface = 1; iface <= c.numInnerFaces; ++iface)
+      for (int k = 1; k <= c.nnodes[iface]; ++k) {
+        int ino = NODE(c, k, iface);
+        ++i; wsum[ino] = wsum[ino] + c.wCellToNode[i];
+        ++i; wsum[ino] = wsum[ino] + c.wCellToNode[i];
+      }
+    i = 0;
+    for (int iface = 1; iface <= c.numInnerFaces; ++iface)
+      for (int k = 1; k <= c.nnodes[iface]; ++k) {
+        int ino = NODE(c, k, iface);
+        ++i; c.wCellToNode[i] = c.wCellToNode[i] / wsum[ino];
+        ++i; c.wCellToNode[i] = c.wCellToNode[i] / wsum[ino];
+      }
+  }
+  PslMoments M(nn);
+  int cnt = 0;
+  for (int iface = c.numInnerFaces + 1; iface <= c.numFaces; ++iface)
+    for (int k = 1; k <= c.nnodes[iface]; ++k) {
+      int ino = NODE(c, k, iface);
+      M.add(ino, c.xf[iface] - c.x[ino], c.yf[iface] - c.y[ino], c.zf[iface] - c.z[ino]);
+      ++cnt;
+    }
+  c.wFaceToNode.assign(cnt + 1, 0.0);
+  int i = 0;
+  for (int iface = c.numInnerFaces + 1; iface <= c.numFaces; ++iface)
+    for (int k = 1; k <= c.nnodes[iface]; ++k) {
+      int ino = NODE(c, k, iface);
+      c.wFaceToNode[++i] = M.weight(ino, c.xf[iface] - c.x[ino], c.yf[iface] - c.y[ino], c.zf[iface] - c.z[ino]);
+    }
+  std::vector<double> wsum(nn, 0.0);
+  i = 0;
+  for (int iface = c.numInnerFaces + 1; iface <= c.numFaces; ++iface)
+    for (int k = 1; k <= c.nnodes[iface]; ++k) {
+      int ino = NODE(c, k, iface);
+      ++i; wsum[ino] = wsum[ino] + c.wFaceToNode[i];
+    }
+  i = 0;
+  for (int iface = c.numInnerFaces + 1; iface <= c.numFaces; ++iface)
+    for (int k = 1; k <= c.nnodes[iface]; ++k) {
+      int ino = NODE(c, k, iface);
+      ++i; c.wFaceToNode[i] = c.wFaceToNode[i] / wsum[ino];
+    }
+}
+
+// set_interpolation_weights, node_interpolation.f90:46-84
+void set_interpolation_weights(Case& c) {
+  if (c.c2n == 1) weights_inverse_distance(c);
+  else weights_pseudolaplacian(c);
+}
+
+// interpolate_to_nodes, node_interpolation.f90:635-700
+void interpolate_to_nodes(Case& c, const std::vector<double>& phiC, std::vector<double>& phiN) {
+  phiN.assign(c.numNodes + 1, 0.0);
+  int i = 0;
+  for (int iface = 1; iface <= c.numInnerFaces; ++iface) {
+    int ijp = c.owner[iface], ijn = c.neighbour[iface];
+    for (int k = 1; k <= c.nnodes[iface]; ++k) {
+      int ino = NODE(c, k, iface);
+      ++i; phiN[ino] = phiN[ino] + c.wCellToNode[i] * phiC[ijp];
+      ++i; phiN[ino] = phiN[ino] + c.wCellToNode[i] * phiC[ijn];
+    }
+  }
+  for (int iface = c.numInnerFaces + 1; iface <= c.numFaces; ++iface)
+    for (int k = 1; k <= c.nnodes[iface]; ++k) phiN[NODE(c, k, iface)] = 0.;
+  i = 0;
+  for (int iface = c.numInnerFaces + 1; iface <= c.numFaces; ++iface) {
+    int ib = c.numCells + (iface - c.numInnerFaces);
+    for (int k = 1; k <= c.nnodes[iface]; ++k) {
+      int ino = NODE(c, k, iface);
+      ++i; phiN[ino] = phiN[ino] + c.wFaceToNode[i] * phiC[ib];
+    }
+  }
+}
+
+// grad_node_based_gauss, gradients.f90:1491-1602
+void grad_node_based_gauss(Case& c, const std::vector<double>& u, std::vector<double>& dudxi) {
+  if (c.wCellToNode.empty()) set_interpolation_weights(c);
+  std::vector<double> uN;
+  interpolate_to_nodes(c, u, uN);
+  std::fill(dudxi.begin(), dudxi.end(), 0.0);
+  for (int iface = 1; iface <= c.numFaces; ++iface) {
+    double fie = 0.0;
+    for (int k = 1; k <= c.nnodes[iface]; ++k) fie = fie + uN[NODE(c, k, iface)];
+    fie = fie / (double)c.nnodes[iface];
+    double dfxe = fie * c.arx[iface], dfye = fie * c.ary[iface], dfze = fie * c.arz[iface];
+    int ijp = c.owner[iface];
+    G(dudxi, 1, ijp) = G(dudxi, 1, ijp) + dfxe;
+    G(dudxi, 2, ijp) = G(dudxi, 2, ijp) + dfye;
+    G(dudxi, 3, ijp) = G(dudxi, 3, ijp) + dfze;
+    if (iface <= c.numInnerFaces) {
+      int ijn = c.neighbour[iface];
+      G(dudxi, 1, ijn) = G(dudxi, 1, ijn) - dfxe;
+      G(dudxi, 2, ijn) = G(dudxi, 2, ijn) - dfye;
+      G(dudxi, 3, ijn) = G(dudxi, 3, ijn) - dfze;
+    }
+  }
+  for (int ijp = 1; ijp <= c.numCells; ++ijp) {
+    double volr = 1. / c.vol[ijp];
+    for (int k = 1; k <= 3; ++k) G(dudxi, k, ijp) = G(dudxi, k, ijp) * volr;
+  }
 }
 
 // slope_limiter_Barth_Jespersen (:288-366), _Venkatakrishnan (:373-451) and

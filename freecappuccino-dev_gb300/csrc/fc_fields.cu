@@ -42,6 +42,10 @@ int fc_fields_alloc(fc_ctx* ctx) {
   add("apu", &F.apu, nC, 0); add("apv", &F.apv, nC, 0); add("apw", &F.apw, nC, 0);
   add("dUdxi", &F.gu, 3 * nT, 1); add("dVdxi", &F.gv, 3 * nT, 1); add("dWdxi", &F.gw, 3 * nT, 1);
   add("dPdxi", &F.gp, 3 * nT, 1); add("dTdxi", &F.gt, 3 * nT, 1);
+  add("uo", &F.uo, nT, 0); add("vo", &F.vo, nT, 0); add("wo", &F.wo, nT, 0);
+  add("uoo", &F.uoo, nT, 0); add("voo", &F.voo, nT, 0); add("woo", &F.woo, nT, 0);
+  add("uooo", &F.uooo, nT, 0); add("vooo", &F.vooo, nT, 0); add("wooo", &F.wooo, nT, 0);
+  add("rU", &F.rU, nC, 0); add("rV", &F.rV, nC, 0); add("rW", &F.rW, nC, 0);
   add("fscratch", &F.fscratch, 3 * (nF > 0 ? nF : 1), 2);
   add("cscratch", &F.cscratch, 3 * nC, 2);
   (void)nI;

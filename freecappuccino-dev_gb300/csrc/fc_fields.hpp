@@ -16,6 +16,8 @@ struct FieldStore {
   DVec<double> u, v, w, p, pp, vis, den, t, flmass, visw;
   DVec<double> su, sv, sw, spu, spv, sp, apu, apv, apw;
   DVec<double> gu, gv, gw, gp, gt;  // gradients, SoA [3][numTotal]
+  DVec<double> uo, vo, wo, uoo, voo, woo, uooo, vooo, wooo;  // old time levels (numTotal)
+  DVec<double> rU, rV, rW;          // PISO: explicit momentum terms (numCells)
   DVec<double> fscratch, cscratch, cscratch_big;
   DVec<double> dmat;                // least-squares cofactors, SoA [9][numCells]
   int dmat_scheme = 0;              // scheme the cofactors were built for (0: none)

@@ -242,6 +242,20 @@ int fv_grad(fc_ctx* ctx, int scheme, const double* phi, double* g) {
   return FC_OK;
 }
 
+// grad_gauss alone (no limiter), boundary entries zeroed: the pressure
+// gradient stages of calcp_piso (calcp_piso.f90:369-372)
+int fv_grad_gauss(fc_ctx* ctx, const double* phi, double* g) {
+  MeshView M = mesh_view(ctx);
+  k_grad_gauss<<<grid_for(M.nC), 256, 0, ctx->stream>>>(M, phi, g);
+  ctx->kernel_launches++;
+  if (M.nT > M.nC) {
+    k_zero_bnd_grad<<<grid_for(M.nT - M.nC), 256, 0, ctx->stream>>>(g, M.nC, M.nT);
+    ctx->kernel_launches++;
+  }
+  FC_CUDA_TRY(ctx, cudaGetLastError());
+  return FC_OK;
+}
+
 // grad(phi, dPhidxi) of the reference (gradients.f90:106-163), with the
 // context's limiter
 // phi: numTotal values, dphi: (3,numTotal); host or device memory

@@ -48,3 +48,5 @@ int fv_grad(fc_ctx* ctx, int scheme, const double* phi, double* g);
 int fv_limit(fc_ctx* ctx, const double* phi, double* g);
 // node-based Gauss gradient of phi into the SoA g (fc_nodegrad.cu)
 int fv_grad_node(fc_ctx* ctx, const double* phi, double* g);
+// grad_gauss without the limiter (fc_fv.cu)
+int fv_grad_gauss(fc_ctx* ctx, const double* phi, double* g);

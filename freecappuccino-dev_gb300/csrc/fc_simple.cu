@@ -105,6 +105,8 @@ struct Dev {  // per-call device pointers of the fields
   double *u, *v, *w, *p, *pp, *vis, *den, *flmass, *visw, *t;
   double *su, *sv, *sw, *spu, *spv, *sp, *apu, *apv, *apw;
   double *gu, *gv, *gw, *gp, *gt;
+  double *uo, *vo, *wo, *uoo, *voo, *woo, *uooo, *vooo, *wooo;  // old time levels
+  double *rU, *rV, *rW;  // PISO: explicit momentum terms
   double* a;
   double* fscr;
   const int* ptype;  // FC_BC_* per patch
@@ -203,6 +205,8 @@ struct MomParams {
   double gds, viscos;
   int scheme;
   double vis_sym;  // vis(inp) with inp = numCells+1 after the cell loop (velocity.f90:379)
+  int tscheme;     // FC_TIME_*: unsteady term of the cell loop (velocity.f90:226-290)
+  double timestep;
 };
 
 // sngrad (variant 1), gradients.f90:1720-1779
@@ -319,6 +323,26 @@ __global__ void k_mom_cell(MeshView M, Dev D, MomParams P) {
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
     double su = D.su[c], sv = D.sv[c], sw = D.sw[c];
     double spu = 0.0, spv = 0.0, sp = 0.0;
+    // unsteady term, velocity.f90:226-290 (before the face fluxes)
+    if (P.tscheme != FC_TIME_STEADY) {
+      const double apotime = D.den[c] * M.vol[c] / P.timestep;
+      if (P.tscheme == FC_TIME_BDF) {
+        su = su + apotime * D.uo[c];
+        sv = sv + apotime * D.vo[c];
+        sw = sw + apotime * D.wo[c];
+        spu = spu + apotime; spv = spv + apotime; sp = sp + apotime;
+      } else if (P.tscheme == FC_TIME_BDF2) {
+        su = su + apotime * (2 * D.uo[c] - 0.5 * D.uoo[c]);
+        sv = sv + apotime * (2 * D.vo[c] - 0.5 * D.voo[c]);
+        sw = sw + apotime * (2 * D.wo[c] - 0.5 * D.woo[c]);
+        spu = spu + 1.5 * apotime; spv = spv + 1.5 * apotime; sp = sp + 1.5 * apotime;
+      } else {
+        su = su + apotime * (3 * D.uo[c] - 1.5 * D.uoo[c] + 1. / 3.0 * D.uooo[c]);
+        sv = sv + apotime * (3 * D.vo[c] - 1.5 * D.voo[c] + 1. / 3.0 * D.vooo[c]);
+        sw = sw + apotime * (3 * D.wo[c] - 1.5 * D.woo[c] + 1. / 3.0 * D.wooo[c]);
+        spu = spu + 11. / 6.0 * apotime; spv = spv + 11. / 6.0 * apotime; sp = sp + 11. / 6.0 * apotime;
+      }
+    }
     for (int q = M.cf_ptr[c]; q < M.cf_ptr[c + 1]; ++q) {
       const int f = M.cf_face[q];
       if (f < M.nI) {
@@ -564,6 +588,133 @@ __global__ void k_init_flmass(MeshView M, Dev D) {
 
 
 // ------------------------------------------------------------ temperature
+// ------------------------------------------------------------------- PISO
+// su = rU - sum_nb h u_nb per cell, faces in ascending order (calcp_piso.f90:
+// 94-117: owner terms through the (P,N) slot, neighbour terms through (N,P))
+__global__ void k_piso_h(MeshView M, Dev D, const double* __restrict__ h) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
+    double su = D.rU[c], sv = D.rV[c], sw = D.rW[c];
+    for (int q = M.cf_ptr[c]; q < M.cf_ptr[c + 1]; ++q) {
+      const int f = M.cf_face[q];
+      if (f >= M.nI) break;
+      double hk;
+      int o;
+      if (M.owner[f] == c) { hk = h[M.ijk[f]]; o = M.neighbour[f]; }
+      else { hk = h[M.jik[f]]; o = M.owner[f]; }
+      su = su - hk * D.u[o];
+      sv = sv - hk * D.v[o];
+      sw = sw - hk * D.w[o];
+    }
+    D.su[c] = su; D.sv[c] = sv; D.sw[c] = sw;
+  }
+}
+
+// u = apu su (calcp_piso.f90:120-122)
+__global__ void k_piso_u(int nC, Dev D) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nC; i += gridDim.x * blockDim.x) {
+    D.u[i] = D.apu[i] * D.su[i];
+    D.v[i] = D.apv[i] * D.sv[i];
+    D.w[i] = D.apw[i] * D.sw[i];
+  }
+}
+
+// facefluxmass_piso, faceflux_mass.f90:389-559: a(k_ij) = can, a(k_ji) = cap
+__global__ void k_piso_face(MeshView M, Dev D) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M.nI; i += gridDim.x * blockDim.x) {
+    const int ijp = M.owner[i], ijn = M.neighbour[i];
+    const double lambda = M.facint[i], fxn = lambda, fxp = 1.0 - lambda;
+    const double dene = D.den[ijp] * fxp + D.den[ijn] * fxn;
+    const double Kj = M.vol[ijp] * D.apu[ijp] * fxp + M.vol[ijn] * D.apu[ijn] * fxn;
+    const double cap = -(dene * Kj * M.Df[i]);
+    const double ui = D.u[ijp] + (D.u[ijn] - D.u[ijp]) * lambda;
+    const double vi = D.v[ijp] + (D.v[ijn] - D.v[ijp]) * lambda;
+    const double wi = D.w[ijp] + (D.w[ijn] - D.w[ijp]) * lambda;
+    D.flmass[i] = dene * (ui * M.arx[i] + vi * M.ary[i] + wi * M.arz[i]);
+    D.a[M.ijk[i]] = cap;
+    D.a[M.jik[i]] = cap;
+  }
+}
+
+// per-block sums of pp over the cells (pavg, calcp_piso.f90:361)
+__global__ void k_sum_cells(const double* __restrict__ x, int nC, double* __restrict__ part) {
+  __shared__ double sm[8];
+  double s = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nC; i += gridDim.x * blockDim.x) s += x[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sm[k];
+    part[blockIdx.x] = t;
+  }
+}
+
+// the block sums into part[nb] (one thread, fixed order)
+__global__ void k_sum_final(double* __restrict__ part, int nb) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  double s = 0.0;
+  for (int b = 0; b < nb; ++b) s += part[b];
+  part[nb] = s;
+}
+
+// p = (1 - urfP) p + urfP (pp - pavg), pavg = sum(pp)/numCells (:361-363)
+__global__ void k_piso_p(int nC, Dev D, const double* __restrict__ sum, double urfP) {
+  const double pavg = *sum / (double)nC;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nC; i += gridDim.x * blockDim.x)
+    D.p[i] = (1.0 - urfP) * D.p[i] + urfP * (D.pp[i] - pavg);
+}
+
+// fluxmc, faceflux_mass.f90:564-647 (the projections xpp, xep as written)
+__global__ void k_fluxmc_face(MeshView M, Dev D) {
+  const Fld gp{D.gp, M.nT};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M.nI; i += gridDim.x * blockDim.x) {
+    const int ijp = M.owner[i], ijn = M.neighbour[i];
+    const double fxn = M.facint[i], fxp = 1.0 - M.facint[i];
+    const double xf = M.xf[i], yf = M.yf[i], zf = M.zf[i], arx = M.arx[i], ary = M.ary[i], arz = M.arz[i];
+    const double xpn = M.xc[ijn] - M.xc[ijp], ypn = M.yc[ijn] - M.yc[ijp], zpn = M.zc[ijn] - M.zc[ijp];
+    const double are = sqrt(arx * arx + ary * ary + arz * arz);
+    const double nxx = arx / are, nyy = ary / are, nzz = arz / are;
+    double xpp = xf - (xf - M.xc[ijp]) * nxx, ypp = yf - (yf - M.yc[ijp]) * nyy, zpp = zf - (zf - M.zc[ijp]) * nzz;
+    double xep = xf - (xf - M.xc[ijn]) * nxx, yep = yf - (yf - M.yc[ijn]) * nyy, zep = zf - (zf - M.zc[ijn]) * nzz;
+    xpp = xpp - M.xc[ijp]; ypp = ypp - M.yc[ijp]; zpp = zpp - M.zc[ijp];
+    xep = xep - M.xc[ijn]; yep = yep - M.yc[ijn]; zep = zep - M.zc[ijn];
+    const double rapr = -((D.apu[ijp] * D.den[ijp] * M.vol[ijp] * fxp + D.apu[ijn] * D.den[ijn] * M.vol[ijn] * fxn) *
+                          are / (xpn * nxx + ypn * nyy + zpn * nzz));
+    D.fscr[i] = rapr * ((gp.x(ijn) * xep - gp.x(ijp) * xpp) + (gp.y(ijn) * yep - gp.y(ijp) * ypp) +
+                        (gp.z(ijn) * zep - gp.z(ijp) * zpp));
+  }
+}
+
+// su -= fmcor at the owner, += at the neighbour, on top of su (:382-392)
+__global__ void k_fluxmc_cell(MeshView M, Dev D) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
+    double s = D.su[c];
+    for (int q = M.cf_ptr[c]; q < M.cf_ptr[c + 1]; ++q) {
+      const int f = M.cf_face[q];
+      if (f >= M.nI) break;
+      if (M.owner[f] == c) s = s - D.fscr[f];
+      else s = s + D.fscr[f];
+    }
+    D.su[c] = s;
+  }
+}
+
+// flmass += a(k_ij) (p_N - p_P) (:396-401)
+__global__ void k_flux_correct_p(MeshView M, Dev D) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M.nI; i += gridDim.x * blockDim.x)
+    D.flmass[i] = D.flmass[i] + D.a[M.ijk[i]] * (D.p[M.neighbour[i]] - D.p[M.owner[i]]);
+}
+
+// u += su apu (:413-415)
+__global__ void k_vel_correct(int nC, Dev D) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nC; i += gridDim.x * blockDim.x) {
+    D.u[i] = D.u[i] + D.su[i] * D.apu[i];
+    D.v[i] = D.v[i] + D.sv[i] * D.apv[i];
+    D.w[i] = D.w[i] + D.sw[i] * D.apw[i];
+  }
+}
+
 struct ScParams {
   double viscos, prl, prtr, sigt, pranl, gam;
   int scheme;
@@ -720,6 +871,9 @@ struct SimpleState {
   int tprm_gen = -1;      // mesh generation the patch tables belong to
   DVec<int> tpatch;       // [kind | iWall start | first boundary index] x numBoundaries
   DVec<double> tpart;     // per-block min/max of T
+  // transient momentum and PISO (fc_transient_set_params)
+  fc_transient_params trp = {1.0, FC_TIME_STEADY, 0, 1};
+  DVec<double> h, ppart;  // calcp_piso: h = a, pavg partials
   // batched U, V, W solves (fc_simple_set_batched_momentum)
   int batch_mom = 0;
   struct MomBatch* mb = nullptr;
@@ -776,6 +930,9 @@ static int make_dev(fc_ctx* ctx, Dev& D, bool allow_pressure = false) {
   D.apu = F.apu.p; D.apv = F.apv.p; D.apw = F.apw.p;
   D.gu = F.gu.p; D.gv = F.gv.p; D.gw = F.gw.p; D.gp = F.gp.p;
   D.t = F.t.p; D.gt = F.gt.p;
+  D.uo = F.uo.p; D.vo = F.vo.p; D.wo = F.wo.p; D.uoo = F.uoo.p; D.voo = F.voo.p; D.woo = F.woo.p;
+  D.uooo = F.uooo.p; D.vooo = F.vooo.p; D.wooo = F.wooo.p;
+  D.rU = F.rU.p; D.rV = F.rV.p; D.rW = F.rW.p;
   D.a = ctx->sys_mesh->a.p;
   D.fscr = F.fscratch.p;
   D.ptype = S.ptype.p;
@@ -925,12 +1082,21 @@ extern "C" int fc_calcuvw(fc_ctx* ctx, double* resor) {
   mp.viscos = P.viscos;
   mp.scheme = P.cSchemeU;
   mp.vis_sym = 0.0;
+  mp.tscheme = S.trp.scheme;
+  mp.timestep = S.trp.timestep;
   if (M.nB > 0) FC_CUDA_TRY(ctx, cudaMemcpyAsync(&mp.vis_sym, D.vis + M.nC, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   if (M.nI) k_mom_face<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D, mp);
   k_mom_cell<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D, mp);
   ctx->kernel_launches += 2;
   FC_CUDA_TRY(ctx, cudaGetLastError());
+  // PISO keeps the explicit convection and diffusion terms (velocity.f90:565-570)
+  if (S.trp.piso) {
+    const size_t bc = (size_t)M.nC * sizeof(double);
+    FC_CUDA_TRY(ctx, cudaMemcpyAsync(D.rU, D.su, bc, cudaMemcpyDeviceToDevice, ctx->stream));
+    FC_CUDA_TRY(ctx, cudaMemcpyAsync(D.rV, D.sv, bc, cudaMemcpyDeviceToDevice, ctx->stream));
+    FC_CUDA_TRY(ctx, cudaMemcpyAsync(D.rW, D.sw, bc, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
   double r[3] = {0, 0, 0};
   if (S.batch_mom && std::strcmp(P.lSolverU, "bicgstab") == 0) {
     // the three solves in one batched launch: V and W get copies of the
@@ -995,6 +1161,29 @@ extern "C" int fc_calcuvw(fc_ctx* ctx, double* resor) {
 
 // calcp_simple, calcp_simple.f90:1-470 (incompressible; no periodic or
 // pressure boundaries).  *resor4 receives resor(4) as continuityErrors sets it.
+// continuityErrors, continuityErrors.f90:1-77: resor(4) into *resor4
+static int continuity_errors(fc_ctx* ctx, const Dev& D, double* resor4) {
+  SimpleState& S = sstate(ctx);
+  MeshView M = mesh_view(ctx);
+  const int nb = std::min(1024, gridn(M.nC));
+  FC_CUDA_TRY(ctx, S.part.alloc((size_t)3 * nb));
+  FC_CUDA_TRY(ctx, S.out.alloc(3));
+  k_conterr<<<nb, 256, 0, ctx->stream>>>(M, D, S.part.p);
+  k_conterr_final<<<1, 32, 0, ctx->stream>>>(S.part.p, nb, S.out.p);
+  ctx->kernel_launches += 2;
+  double h[3];
+  FC_CUDA_TRY(ctx, cudaMemcpyAsync(h, S.out.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  const double wavg = h[0] / h[1];
+  S.cumulativeContErr += h[2];
+  S.resor[4] = wavg;
+  if (resor4) *resor4 = wavg;
+  if (ctx->verbosity)
+    std::printf("  continuity errors : avg local = %10.3E, global = %10.3E, cumulative = %10.3E\n", wavg, h[2],
+                S.cumulativeContErr);
+  return FC_OK;
+}
+
 extern "C" int fc_calcp_simple(fc_ctx* ctx, double* resor4) {
   FC_RANGE();
   if (!ctx) return FC_ERR_BAD_INPUT;
@@ -1031,23 +1220,122 @@ extern "C" int fc_calcp_simple(fc_ctx* ctx, double* resor4) {
       ctx->kernel_launches += 2;
     }
   }
-  // continuityErrors
-  const int nb = std::min(1024, gridn(M.nC));
-  FC_CUDA_TRY(ctx, S.part.alloc((size_t)3 * nb));
-  FC_CUDA_TRY(ctx, S.out.alloc(3));
-  k_conterr<<<nb, 256, 0, ctx->stream>>>(M, D, S.part.p);
-  k_conterr_final<<<1, 32, 0, ctx->stream>>>(S.part.p, nb, S.out.p);
-  ctx->kernel_launches += 2;
-  double h[3];
-  FC_CUDA_TRY(ctx, cudaMemcpyAsync(h, S.out.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-  FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  const double wavg = h[0] / h[1];
-  S.cumulativeContErr += h[2];
-  S.resor[4] = wavg;
+  return continuity_errors(ctx, D, resor4);
+}
+
+// transient parameters (velocity.f90 unsteady term, PISO)
+extern "C" int fc_transient_set_params(fc_ctx* ctx, const fc_transient_params* prm) {
+  if (!ctx || !prm) return FC_ERR_BAD_INPUT;
+  if (prm->scheme < FC_TIME_STEADY || prm->scheme > FC_TIME_BDF3)
+    return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_transient_set_params: unknown time scheme");
+  if (prm->scheme != FC_TIME_STEADY && !(prm->timestep > 0))
+    return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_transient_set_params: timestep must be > 0");
+  if (prm->piso && prm->ncorr < 1) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_transient_set_params: ncorr < 1");
+  if (prm->piso && (prm->scheme == FC_TIME_BDF2 || prm->scheme == FC_TIME_BDF3))
+    return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED,
+                       "PISO with bdf2/bdf3: the reference extrapolates from old mass fluxes and pressures that "
+                       "time_shift never updates");
+  sstate(ctx).trp = *prm;
+  return FC_OK;
+}
+
+// time_shift, time_shift.f90 (velocity levels)
+extern "C" int fc_time_shift(fc_ctx* ctx) {
+  FC_RANGE();
+  if (!ctx) return FC_ERR_BAD_INPUT;
+  if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
+  SimpleState& S = sstate(ctx);
+  FieldStore& F = ctx_fields(ctx);
+  const size_t b = (size_t)ctx->mesh.numTotal * sizeof(double);
+  auto cp = [&](DVec<double>& d, const DVec<double>& s) {
+    return cudaMemcpyAsync(d.p, s.p, b, cudaMemcpyDeviceToDevice, ctx->stream);
+  };
+  if (S.trp.scheme == FC_TIME_BDF3) {
+    FC_CUDA_TRY(ctx, cp(F.uooo, F.uoo)); FC_CUDA_TRY(ctx, cp(F.vooo, F.voo)); FC_CUDA_TRY(ctx, cp(F.wooo, F.woo));
+  }
+  if (S.trp.scheme == FC_TIME_BDF3 || S.trp.scheme == FC_TIME_BDF2) {
+    FC_CUDA_TRY(ctx, cp(F.uoo, F.uo)); FC_CUDA_TRY(ctx, cp(F.voo, F.vo)); FC_CUDA_TRY(ctx, cp(F.woo, F.wo));
+  }
+  FC_CUDA_TRY(ctx, cp(F.uo, F.u)); FC_CUDA_TRY(ctx, cp(F.vo, F.v)); FC_CUDA_TRY(ctx, cp(F.wo, F.w));
+  return FC_OK;
+}
+
+// calcp_piso, calcp_piso.f90:86-489 (incompressible; no periodic or pressure
+// boundaries; nipgrad = 2, parameters.f90:62)
+extern "C" int fc_calcp_piso(fc_ctx* ctx, double* resor4) {
+  FC_RANGE();
+  if (!ctx) return FC_ERR_BAD_INPUT;
+  if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
+  SimpleState& S = sstate(ctx);
+  if (!S.have_prm) return fc_fail_msg(ctx, FC_ERR_STATE, "fc_simple_set_params not called");
+  if (!S.trp.piso) return fc_fail_msg(ctx, FC_ERR_STATE, "fc_calcp_piso: PISO not enabled (fc_transient_set_params)");
+  Dev D;
+  int st = make_dev(ctx, D);
+  if (st) return st;
+  const fc_simple_params& P = S.prm;
+  MeshView M = mesh_view(ctx);
+  const size_t nnz = (size_t)ctx->sys_mesh->nnz;
+  FC_CUDA_TRY(ctx, S.h.alloc(nnz));
+  FC_CUDA_TRY(ctx, cudaMemcpyAsync(S.h.p, D.a, nnz * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  const int nbs = std::min(1024, gridn(M.nC));
+  FC_CUDA_TRY(ctx, S.ppart.alloc(nbs + 1));
+  bool outlets = false;
+  for (int b = 0; b < ctx->mesh.numBoundaries; ++b) outlets |= ctx->mesh.h_bctype[b] == FC_BC_OUTLET;
+  double r4 = 0, wavg = 0;
+  for (int icorr = 1; icorr <= S.trp.ncorr; ++icorr) {
+    k_piso_h<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D, S.h.p);
+    k_piso_u<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, D);
+    if (M.nI) k_piso_face<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D);
+    if (outlets) k_adjust_mass_flow<<<1, 32, 0, ctx->stream>>>(M, D, P.flomas);
+    k_p_cell<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D);
+    ctx->kernel_launches += 4 + outlets;
+    FC_CUDA_TRY(ctx, cudaGetLastError());
+    for (int ipcorr = 1; ipcorr <= P.npcor; ++ipcorr) {
+      st = solve_into(ctx, P.lSolverP, D.pp, D.su, &r4, P.maxiterP, P.tolAbsP, P.tolRelP, "p");
+      if (st < 0) return st;
+      k_sum_cells<<<nbs, 256, 0, ctx->stream>>>(D.pp, M.nC, S.ppart.p);
+      k_sum_final<<<1, 32, 0, ctx->stream>>>(S.ppart.p, nbs);
+      k_piso_p<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, D, S.ppart.p + nbs, P.urfP);
+      ctx->kernel_launches += 3;
+      const Fld gp{D.gp, M.nT};
+      for (int stage = 1; stage <= 2; ++stage) {
+        if (M.nB) {
+          k_bpres<<<gridn(M.nB), 256, 0, ctx->stream>>>(M, D.ptype, D.p, gp, stage);
+          ctx->kernel_launches++;
+        }
+        if ((st = fv_grad_gauss(ctx, D.p, D.gp))) return st;
+      }
+      if (ipcorr != P.npcor) {
+        if (M.nI) k_fluxmc_face<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D);
+        k_fluxmc_cell<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D);
+        ctx->kernel_launches += 2;
+      } else {
+        if (M.nI) k_flux_correct_p<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D);
+        ctx->kernel_launches++;
+        if ((st = continuity_errors(ctx, D, &wavg))) return st;
+      }
+    }
+    if ((st = gradp_and_sources(ctx, D, D.p, P.pscheme))) return st;
+    k_vel_correct<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, D);
+    ctx->kernel_launches++;
+    update_velocity_at_boundary(ctx, D);
+  }
+  FC_CUDA_TRY(ctx, cudaGetLastError());
   if (resor4) *resor4 = wavg;
-  if (ctx->verbosity)
-    std::printf("  continuity errors : avg local = %10.3E, global = %10.3E, cumulative = %10.3E\n", wavg, h[2],
-                S.cumulativeContErr);
+  return FC_OK;
+}
+
+// one PISO iteration of main.f90:159-165 (calcuvw + calcp_piso)
+extern "C" int fc_piso_iteration(fc_ctx* ctx, double* resor) {
+  FC_RANGE();
+  double r[4];
+  int st = fc_calcuvw(ctx, r);
+  if (st < 0) return st;
+  st = fc_calcp_piso(ctx, &r[3]);
+  if (st < 0) return st;
+  if (resor) for (int k = 0; k < 4; ++k) resor[k] = r[k];
+  const double source = std::max(r[0], std::max(r[1], r[2]));
+  if (!(source <= (double)1e+30f)) return fc_fail_msg(ctx, FC_ERR_NAN, "PISO iterations diverge");
   return FC_OK;
 }
 

@@ -31,6 +31,7 @@ BC = {"wall": 1, "inlet": 2, "outlet": 3, "symmetry": 4, "pressure": 5, "empty":
 FC_GRAD_GAUSS, FC_GRAD_LSQ, FC_GRAD_LSQ_DM, FC_GRAD_NODE_GAUSS = 0, 1, 2, 3
 FC_C2N_PSL, FC_C2N_IDS = 0, 1
 FC_LIMITER_NONE, FC_LIMITER_BJ, FC_LIMITER_VENKAT, FC_LIMITER_R, FC_LIMITER_MD = 0, 1, 2, 3, 4
+FC_TIME_STEADY, FC_TIME_BDF, FC_TIME_BDF2, FC_TIME_BDF3 = 0, 1, 2, 3
 FC_PREC_FP64 = 0
 FC_PREC_MIXED = 1
 FC_PREC_MIXED_COLOURED = 2
@@ -126,6 +127,10 @@ def lib():
         "fc_set_solve_log": (i, [vp, cp]),
         "fc_set_gradient_limiter": (i, [vp, i]),
         "fc_set_node_interpolation": (i, [vp, i]),
+        "fc_transient_set_params": (i, [vp, vp]),
+        "fc_time_shift": (i, [vp]),
+        "fc_calcp_piso": (i, [vp, vp]),
+        "fc_piso_iteration": (i, [vp, vp]),
         "fc_download_fields": (i, [vp, i, vp, vp, vp]),
         "fc_batch_create": (i, [vp, vp]),
         "fc_batch_destroy": (i, [vp]),
@@ -227,6 +232,11 @@ class SimpleParams(C.Structure):
         p.lSolverP = kw.get("solverP", "iccg").encode()
         p.flomas = kw.get("flomas", 0.0)
         return p
+
+
+class TransientParams(C.Structure):
+    """fc_transient_params: unsteady momentum term and PISO."""
+    _fields_ = [("timestep", C.c_double), ("scheme", C.c_int), ("piso", C.c_int), ("ncorr", C.c_int)]
 
 
 class TemperatureParams(C.Structure):
@@ -475,8 +485,11 @@ class Context:
 
     def field_len(self, name):
         m = self.mesh
-        if name in ("u", "v", "w", "p", "pp", "vis", "den", "t"):
+        if name in ("u", "v", "w", "p", "pp", "vis", "den", "t", "uo", "vo", "wo", "uoo", "voo", "woo", "uooo",
+                    "vooo", "wooo"):
             return m.numTotal
+        if name in ("rU", "rV", "rW"):
+            return m.numCells
         if name == "flmass":
             return m.numFaces
         if name in ("su", "sv", "sw", "spu", "spv", "sp", "apu", "apv", "apw"):
@@ -633,6 +646,18 @@ class Context:
         cnt = (C.c_longlong * len(names))(*[len(o) for o in outs])
         self._check(self.L.fc_download_fields(self.h, len(names), cn, po, cnt), "fc_download_fields")
         return dict(zip(names, outs))
+
+    def transient_params(self, timestep, scheme, piso=0, ncorr=1):
+        prm = TransientParams(float(timestep), int(scheme), int(piso), int(ncorr))
+        self._check(self.L.fc_transient_set_params(self.h, C.byref(prm)), "fc_transient_set_params")
+
+    def time_shift(self):
+        self._check(self.L.fc_time_shift(self.h), "fc_time_shift")
+
+    def piso_iteration(self):
+        r = np.zeros(4)
+        self._check(self.L.fc_piso_iteration(self.h, _ptr(r)), "fc_piso_iteration")
+        return r
 
     def simple_batched_momentum(self, on=True):
         """calcuvw solves U, V, W in one batched launch (bicgstab only)."""

@@ -390,6 +390,36 @@ int fc_calcp_simple(fc_ctx* ctx, double* resor4);
  * logs them; FC_ERR_NAN when max(resor(1:3)) > 1e30 (main.f90:202-207). */
 int fc_simple_iteration(fc_ctx* ctx, double* resor);
 
+/* ---- Transient momentum and PISO (velocity.f90:133-290, :565-570;
+ * calcp_piso.f90:86-489; time_shift.f90; main.f90:132-165).
+ *   scheme: the unsteady term of calcuvw, FC_TIME_BDF (Euler), FC_TIME_BDF2
+ *   or FC_TIME_BDF3, on the old levels "uo", "uoo", "uooo" (and v, w);
+ *   FC_TIME_STEADY for none.  Crank-Nicolson is not supported.
+ *   piso != 0: calcuvw keeps its explicit terms in "rU", "rV", "rW" for
+ *   fc_calcp_piso; ncorr PISO correctors, npcor pressure solves per
+ *   corrector (fc_simple_params.npcor), urfP.  PISO with BDF2/BDF3 is
+ *   rejected: the reference extrapolates the mass fluxes and pressure from
+ *   old levels (velocity.f90:146-162) that its time_shift never updates.
+ *   Incompressible, without periodic or pressure boundaries, as SIMPLE.
+ * fc_time_shift: time_shift.f90 for the velocity levels.
+ * fc_calcp_piso: calcp_piso; *resor4 as continuityErrors sets resor(4).
+ * fc_piso_iteration: calcuvw + calcp_piso, resor[4], and the divergence
+ * stop of main.f90:202-207. */
+#define FC_TIME_STEADY 0
+#define FC_TIME_BDF    1
+#define FC_TIME_BDF2   2
+#define FC_TIME_BDF3   3
+typedef struct {
+  double timestep;
+  int scheme;   /* FC_TIME_* */
+  int piso;     /* 1: PISO (keep rU, rV, rW) */
+  int ncorr;    /* PISO correctors */
+} fc_transient_params;
+int fc_transient_set_params(fc_ctx* ctx, const fc_transient_params* prm);
+int fc_time_shift(fc_ctx* ctx);
+int fc_calcp_piso(fc_ctx* ctx, double* resor4);
+int fc_piso_iteration(fc_ctx* ctx, double* resor);
+
 /* ---------------------------------------------------------------------------
  * Scalar transport: the temperature equation (ScalarEqns/temperature.f90).
  * --------------------------------------------------------------------------- */

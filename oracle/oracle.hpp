@@ -58,6 +58,14 @@ struct Case {
   int limiter = 0;     // gradients.f90:13: 0 none, 1 Barth-Jespersen, 2 Venkatakrishnan, 3 'R3', 4 multidimensional
   // node_interpolation.f90: c2n 0 'psl' (pseudo-Laplacian, the default), 1 'ids' (inverse distance)
   int c2n = 0;
+  // transient momentum and PISO (velocity.f90:133-290, :565-570;
+  // calcp_piso.f90; time_shift.f90): tscheme 0 steady, 1 bdf (Euler),
+  // 2 bdf2, 3 bdf3
+  int tscheme = 0, piso = 0, ncorr = 1;
+  double timestep = 1.0;
+  std::vector<double> uo, vo, wo, uoo, voo, woo, uooo, vooo, wooo;  // numTotal+1
+  std::vector<double> rU, rV, rW;                                   // numCells+1
+  std::vector<double> h;                                            // nnz+1
   std::vector<double> wCellToNode, wFaceToNode;  // 1-based, in the module's running order
   int pscheme = 0;     // 0 linear, 1 central, 2 weighted
   double densit = 1.0, viscos = 0.01;
@@ -128,6 +136,8 @@ void slope_limiter(Case& c, const std::vector<double>& phi, std::vector<double>&
 void set_interpolation_weights(Case& c);
 void interpolate_to_nodes(Case& c, const std::vector<double>& phiC, std::vector<double>& phiN);
 void grad_node_based_gauss(Case& c, const std::vector<double>& u, std::vector<double>& dudxi);
+void time_shift(Case& c);
+int calcp_piso(Case& c);
 
 // operators
 void laplacian(Case& c, const std::vector<double>& mu, const std::vector<double>& phi, unsigned long long dirichlet_mask);

@@ -58,6 +58,18 @@ std::vector<double>* dbl_array(Case& c, const std::string& n, int& len, int& off
   if (n == "dWdxi") { len = 3 * c.numTotal; offset = 3; return &c.dWdxi; }
   if (n == "dPdxi") { len = 3 * c.numTotal; offset = 3; return &c.dPdxi; }
   if (n == "Dmat") { len = 9 * c.numCells; offset = 9; return &c.Dmat; }
+  if (n == "uo") { len = c.numTotal; return &c.uo; }
+  if (n == "vo") { len = c.numTotal; return &c.vo; }
+  if (n == "wo") { len = c.numTotal; return &c.wo; }
+  if (n == "uoo") { len = c.numTotal; return &c.uoo; }
+  if (n == "voo") { len = c.numTotal; return &c.voo; }
+  if (n == "woo") { len = c.numTotal; return &c.woo; }
+  if (n == "uooo") { len = c.numTotal; return &c.uooo; }
+  if (n == "vooo") { len = c.numTotal; return &c.vooo; }
+  if (n == "wooo") { len = c.numTotal; return &c.wooo; }
+  if (n == "rU") { len = c.numCells; return &c.rU; }
+  if (n == "rV") { len = c.numCells; return &c.rV; }
+  if (n == "rW") { len = c.numCells; return &c.rW; }
   return nullptr;
 }
 
@@ -146,6 +158,10 @@ int orc_case_set_param(void* h, const char* name, double val) {
   else if (n == "gradScheme") c.gradScheme = (int)val;
   else if (n == "pscheme") c.pscheme = (int)val;
   else if (n == "limiter") c.limiter = (int)val;
+  else if (n == "tscheme") c.tscheme = (int)val;
+  else if (n == "piso") c.piso = (int)val;
+  else if (n == "ncorr") c.ncorr = (int)val;
+  else if (n == "timestep") c.timestep = val;
   else if (n == "c2n") { c.c2n = (int)val; c.wCellToNode.clear(); c.wFaceToNode.clear(); }
   else if (n == "maxiterU") c.maxiterU = (int)val;
   else if (n == "maxiterP") c.maxiterP = (int)val;
@@ -253,6 +269,18 @@ int orc_cd_gradient(void* h, const double* phi, const double* lambda, double* ou
 
 // one SIMPLE outer iteration (main.f90:159-165); resor4 gets resor(1..4);
 // elapsed_s gets the wall time of the iteration
+int orc_time_shift(void* h) { time_shift(*(Case*)h); return 0; }
+int orc_calcp_piso(void* h) { return calcp_piso(*(Case*)h); }
+
+// calcuvw + calcp_piso (main.f90:159-165 with PISO)
+int orc_piso_iteration(void* h, double* resor4) {
+  Case& c = *(Case*)h;
+  int st = calcuvw(c);
+  int st2 = calcp_piso(c);
+  if (resor4) for (int k = 0; k < 4; ++k) resor4[k] = c.resor[k + 1];
+  return st < st2 ? st : st2;
+}
+
 int orc_simple_iteration(void* h, double* resor4, double* elapsed_s) {
   Case& c = *(Case*)h;
   auto t0 = std::chrono::steady_clock::now();

@@ -800,6 +800,34 @@ int calcuvw(Case& c) {
   grad(c, c.v, c.dVdxi);
   grad(c, c.w, c.dWdxi);
   gradp_and_sources(c, c.p);
+  // unsteady term of the cell loop, velocity.f90:226-290
+  if (c.tscheme > 0) {
+    for (int inp = 1; inp <= nC; ++inp) {
+      double apotime = c.den[inp] * c.vol[inp] / c.timestep;
+      if (c.tscheme == 1) {
+        c.su[inp] = c.su[inp] + apotime * c.uo[inp];
+        c.sv[inp] = c.sv[inp] + apotime * c.vo[inp];
+        c.sw[inp] = c.sw[inp] + apotime * c.wo[inp];
+        c.spu[inp] = c.spu[inp] + apotime;
+        c.spv[inp] = c.spv[inp] + apotime;
+        c.sp[inp] = c.sp[inp] + apotime;
+      } else if (c.tscheme == 2) {
+        c.su[inp] = c.su[inp] + apotime * (2 * c.uo[inp] - 0.5 * c.uoo[inp]);
+        c.sv[inp] = c.sv[inp] + apotime * (2 * c.vo[inp] - 0.5 * c.voo[inp]);
+        c.sw[inp] = c.sw[inp] + apotime * (2 * c.wo[inp] - 0.5 * c.woo[inp]);
+        c.spu[inp] = c.spu[inp] + 1.5 * apotime;
+        c.spv[inp] = c.spv[inp] + 1.5 * apotime;
+        c.sp[inp] = c.sp[inp] + 1.5 * apotime;
+      } else {
+        c.su[inp] = c.su[inp] + apotime * (3 * c.uo[inp] - 1.5 * c.uoo[inp] + 1. / 3.0 * c.uooo[inp]);
+        c.sv[inp] = c.sv[inp] + apotime * (3 * c.vo[inp] - 1.5 * c.voo[inp] + 1. / 3.0 * c.vooo[inp]);
+        c.sw[inp] = c.sw[inp] + apotime * (3 * c.wo[inp] - 1.5 * c.woo[inp] + 1. / 3.0 * c.wooo[inp]);
+        c.spu[inp] = c.spu[inp] + 11. / 6.0 * apotime;
+        c.spv[inp] = c.spv[inp] + 11. / 6.0 * apotime;
+        c.sp[inp] = c.sp[inp] + 11. / 6.0 * apotime;
+      }
+    }
+  }
   // inner faces :286-314
   for (int i = 1; i <= c.numInnerFaces; ++i) {
     int ijp = c.owner[i], ijn = c.neighbour[i];
@@ -861,6 +889,10 @@ int calcuvw(Case& c) {
         c.sw[ijp] = c.sw[ijp] + vsol * (upb * nxf * nzf + vpb * nyf * nzf + c.w[ijb] * (1. - nzf * nzf));
       }
     }
+  }
+  // PISO keeps the explicit convection and diffusion terms, :565-570
+  if (c.piso) {
+    for (int inp = 1; inp <= nC; ++inp) { c.rU[inp] = c.su[inp]; c.rV[inp] = c.sv[inp]; c.rW[inp] = c.sw[inp]; }
   }
   int worst = 0;
   SolveInfo si;
@@ -1040,6 +1072,131 @@ int calcp_simple(Case& c) {
     }
   }
   continuityErrors(c);
+  return worst;
+}
+
+// ---------------------------------------------------------------- PISO
+// time_shift, time_shift.f90 (velocity levels; the PISO extrapolation
+// levels of bdf2/bdf3 are not shifted there, and bdf2/bdf3 PISO is rejected)
+void time_shift(Case& c) {
+  if (c.tscheme == 3) { c.uooo = c.uoo; c.vooo = c.voo; c.wooo = c.woo; }
+  if (c.tscheme == 3 || c.tscheme == 2) { c.uoo = c.uo; c.voo = c.vo; c.woo = c.wo; }
+  c.uo = c.u; c.vo = c.v; c.wo = c.w;
+}
+
+// facefluxmass_piso, faceflux_mass.f90:389-559
+static void facefluxmass_piso(Case& c, int i, int ijp, int ijn, double arx, double ary, double arz, double lambda,
+                              double& cap, double& can, double& flmass) {
+  double fxn = lambda, fxp = 1.0 - lambda;
+  double dene = c.den[ijp] * fxp + c.den[ijn] * fxn;
+  double Kj = c.vol[ijp] * c.apu[ijp] * fxp + c.vol[ijn] * c.apu[ijn] * fxn;
+  cap = -dene * Kj * c.Df[i];
+  can = cap;
+  double ui = c.u[ijp] + (c.u[ijn] - c.u[ijp]) * lambda;
+  double vi = c.v[ijp] + (c.v[ijn] - c.v[ijp]) * lambda;
+  double wi = c.w[ijp] + (c.w[ijn] - c.w[ijp]) * lambda;
+  flmass = dene * (ui * arx + vi * ary + wi * arz);
+}
+
+// fluxmc, faceflux_mass.f90:564-647 (the projections xpp, xep as written)
+static void fluxmc(Case& c, int ijp, int ijn, double xf, double yf, double zf, double arx, double ary, double arz,
+                   double lambda, double& fmcor) {
+  double fxn = lambda, fxp = 1.0 - lambda;
+  double xpn = c.xc[ijn] - c.xc[ijp], ypn = c.yc[ijn] - c.yc[ijp], zpn = c.zc[ijn] - c.zc[ijp];
+  double are = std::sqrt(arx * arx + ary * ary + arz * arz);
+  double nxx = arx / are, nyy = ary / are, nzz = arz / are;
+  double xpp = xf - (xf - c.xc[ijp]) * nxx, ypp = yf - (yf - c.yc[ijp]) * nyy, zpp = zf - (zf - c.zc[ijp]) * nzz;
+  double xep = xf - (xf - c.xc[ijn]) * nxx, yep = yf - (yf - c.yc[ijn]) * nyy, zep = zf - (zf - c.zc[ijn]) * nzz;
+  xpp = xpp - c.xc[ijp]; ypp = ypp - c.yc[ijp]; zpp = zpp - c.zc[ijp];
+  xep = xep - c.xc[ijn]; yep = yep - c.yc[ijn]; zep = zep - c.zc[ijn];
+  double rapr = -((c.apu[ijp] * c.den[ijp] * c.vol[ijp] * fxp + c.apu[ijn] * c.den[ijn] * c.vol[ijn] * fxn) * are /
+                  (xpn * nxx + ypn * nyy + zpn * nzz));
+  fmcor = rapr * ((G(c.dPdxi, 1, ijn) * xep - G(c.dPdxi, 1, ijp) * xpp) +
+                  (G(c.dPdxi, 2, ijn) * yep - G(c.dPdxi, 2, ijp) * ypp) +
+                  (G(c.dPdxi, 3, ijn) * zep - G(c.dPdxi, 3, ijp) * zpp));
+}
+
+// calcp_piso, calcp_piso.f90:86-489, incompressible, without periodic or
+// pressure boundaries; nipgrad = 2 (parameters.f90:62)
+int calcp_piso(Case& c) {
+  const int nC = c.numCells;
+  c.h = c.a;
+  int worst = 0;
+  for (int icorr = 1; icorr <= c.ncorr; ++icorr) {
+    for (int i = 1; i <= nC; ++i) { c.su[i] = c.rU[i]; c.sv[i] = c.rV[i]; c.sw[i] = c.rW[i]; }
+    for (int i = 1; i <= c.numInnerFaces; ++i) {
+      int ijp = c.owner[i], ijn = c.neighbour[i];
+      int k = c.ijk[i];
+      c.su[ijp] = c.su[ijp] - c.h[k] * c.u[ijn];
+      c.sv[ijp] = c.sv[ijp] - c.h[k] * c.v[ijn];
+      c.sw[ijp] = c.sw[ijp] - c.h[k] * c.w[ijn];
+      k = c.jik[i];
+      c.su[ijn] = c.su[ijn] - c.h[k] * c.u[ijp];
+      c.sv[ijn] = c.sv[ijn] - c.h[k] * c.v[ijp];
+      c.sw[ijn] = c.sw[ijn] - c.h[k] * c.w[ijp];
+    }
+    for (int i = 1; i <= nC; ++i) {
+      c.u[i] = c.apu[i] * c.su[i];
+      c.v[i] = c.apv[i] * c.sv[i];
+      c.w[i] = c.apw[i] * c.sw[i];
+    }
+    std::fill(c.a.begin(), c.a.end(), 0.0);
+    std::fill(c.su.begin(), c.su.end(), 0.0);
+    for (int i = 1; i <= c.numInnerFaces; ++i) {
+      int ijp = c.owner[i], ijn = c.neighbour[i];
+      double cap, can;
+      facefluxmass_piso(c, i, ijp, ijn, c.arx[i], c.ary[i], c.arz[i], c.facint[i], cap, can, c.flmass[i]);
+      c.a[c.ijk[i]] = can;
+      c.a[c.jik[i]] = cap;
+      c.a[c.diag[ijp]] = c.a[c.diag[ijp]] - can;
+      c.a[c.diag[ijn]] = c.a[c.diag[ijn]] - cap;
+      c.su[ijp] = c.su[ijp] - c.flmass[i];
+      c.su[ijn] = c.su[ijn] + c.flmass[i];
+    }
+    adjustMassFlow(c);
+    for (int ib = 1; ib <= c.numBoundaries; ++ib) {
+      if (c.bctype[ib] != BC_INLET && c.bctype[ib] != BC_OUTLET) continue;
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int iface = c.startFace[ib] + i, ijp = c.owner[iface];
+        c.su[ijp] = c.su[ijp] - c.flmass[iface];
+      }
+    }
+    for (int ipcorr = 1; ipcorr <= c.npcor; ++ipcorr) {
+      SolveInfo si;
+      int st = csrsolve(c, c.lSolverP, c.pp, c.su, c.resor[4], c.maxiterP, c.tolAbsP, c.tolRelP, si);
+      worst = std::min(worst, st);
+      double pavg = 0.0;
+      for (int i = 1; i <= nC; ++i) pavg = pavg + c.pp[i];
+      pavg = pavg / (double)nC;
+      for (int i = 1; i <= nC; ++i) c.p[i] = (1.0 - c.urfP) * c.p[i] + c.urfP * (c.pp[i] - pavg);
+      for (int istage = 1; istage <= 2; ++istage) {
+        bpres(c, c.p, istage);
+        grad_gauss(c, c.p, c.dPdxi);
+      }
+      if (ipcorr != c.npcor) {
+        for (int i = 1; i <= c.numInnerFaces; ++i) {
+          int ijp = c.owner[i], ijn = c.neighbour[i];
+          double fmcor;
+          fluxmc(c, ijp, ijn, c.xf[i], c.yf[i], c.zf[i], c.arx[i], c.ary[i], c.arz[i], c.facint[i], fmcor);
+          c.su[ijp] = c.su[ijp] - fmcor;
+          c.su[ijn] = c.su[ijn] + fmcor;
+        }
+      } else {
+        for (int iface = 1; iface <= c.numInnerFaces; ++iface) {
+          int ijp = c.owner[iface], ijn = c.neighbour[iface];
+          c.flmass[iface] = c.flmass[iface] + c.a[c.ijk[iface]] * (c.p[ijn] - c.p[ijp]);
+        }
+        continuityErrors(c);
+      }
+    }
+    gradp_and_sources(c, c.p);
+    for (int i = 1; i <= nC; ++i) {
+      c.u[i] = c.u[i] + c.su[i] * c.apu[i];
+      c.v[i] = c.v[i] + c.sv[i] * c.apv[i];
+      c.w[i] = c.w[i] + c.sw[i] * c.apw[i];
+    }
+    updateVelocityAtBoundary(c);
+  }
   return worst;
 }
 

@@ -55,6 +55,8 @@ void setup_case(Case& c, int numNodes, int numCells, int numInnerFaces, int numB
 
   const size_t nt = c.numTotal + 1, nc = c.numCells + 1;
   c.u.assign(nt, 0.0); c.v.assign(nt, 0.0); c.w.assign(nt, 0.0);
+  for (auto* v : {&c.uo, &c.vo, &c.wo, &c.uoo, &c.voo, &c.woo, &c.uooo, &c.vooo, &c.wooo}) v->assign(nt, 0.0);
+  for (auto* v : {&c.rU, &c.rV, &c.rW}) v->assign(nc, 0.0);
   c.p.assign(nt, 0.0); c.pp.assign(nt, 0.0);
   c.vis.assign(nt, 0.0); c.den.assign(nt, 0.0);
   c.flmass.assign(c.numFaces + 1, 0.0);

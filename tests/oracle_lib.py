@@ -48,6 +48,8 @@ def lib(fast=False):
     for f in ("orc_init_flmass", "orc_update_velocity_at_boundary", "orc_calcuvw", "orc_calcp_simple"):
         getattr(L, f).argtypes = [C.c_void_p]
     L.orc_simple_iteration.argtypes = [C.c_void_p, dp, dp]
+    L.orc_time_shift.argtypes = [C.c_void_p]
+    L.orc_piso_iteration.argtypes = [C.c_void_p, dp]
     L.orc_case_set_bcdfrac_t.argtypes = [C.c_void_p, C.c_int, C.c_double]
     L.orc_calculate_temperature.argtypes = [C.c_void_p, C.c_int]
     L.orc_cd_assemble.argtypes = [C.c_void_p, dp, dp]
@@ -95,8 +97,10 @@ class Case:
 
     def _len(self, name):
         faces = ("arx", "ary", "arz", "xf", "yf", "zf", "flmass")
-        cells = ("xc", "yc", "zc", "vol", "su", "sv", "sw", "spu", "spv", "sp", "apu", "apv", "apw", "d")
-        total = ("u", "v", "w", "p", "pp", "vis", "den", "t")
+        cells = ("xc", "yc", "zc", "vol", "su", "sv", "sw", "spu", "spv", "sp", "apu", "apv", "apw", "d",
+                 "rU", "rV", "rW")
+        total = ("u", "v", "w", "p", "pp", "vis", "den", "t", "uo", "vo", "wo", "uoo", "voo", "woo", "uooo",
+                 "vooo", "wooo")
         if name in faces:
             return self.numFaces
         if name in cells:
@@ -173,6 +177,14 @@ class Case:
         out = np.zeros(self.numCells)
         self.L.orc_cd_gradient(self.h, _f64(phi), _f64(lam), out)
         return out
+
+    def time_shift(self):
+        self.L.orc_time_shift(self.h)
+
+    def piso_iteration(self):
+        r = np.zeros(4)
+        st = self.L.orc_piso_iteration(self.h, r)
+        return st, r
 
     def simple_iteration(self):
         r = np.zeros(4)

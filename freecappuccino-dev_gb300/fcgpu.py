@@ -76,6 +76,8 @@ def lib():
         "fc_mesh_from_arrays": (i, [i, i, i, i, vp, vp, vp, vp, vp, vp, vp, i, vp, vp, vp, C.POINTER(vp)]),
         "fc_mesh_read_native": (i, [cp, C.POINTER(vp)]),
         "fc_mesh_write_native": (i, [vp, cp]),
+        "fc_mesh_read_openfoam": (i, [cp, C.POINTER(vp)]),
+        "fc_mesh_write_openfoam": (i, [vp, cp]),
         "fc_mesh_info": (i, [vp, vp]),
         "fc_mesh_export": (i, [vp] + [vp] * 10),
         "fc_mesh_free": (None, [vp]),
@@ -300,6 +302,19 @@ class Mesh:
         if st != 0:
             raise FcError(st, "fc_mesh_read_native")
         return cls(h)
+
+    @classmethod
+    def read_openfoam(cls, d):
+        h = C.c_void_p()
+        st = lib().fc_mesh_read_openfoam(d.encode(), C.byref(h))
+        if st != 0:
+            raise FcError(st, "fc_mesh_read_openfoam")
+        return cls(h)
+
+    def write_openfoam(self, d):
+        st = lib().fc_mesh_write_openfoam(self.h, d.encode())
+        if st != 0:
+            raise FcError(st, "fc_mesh_write_openfoam")
 
     def write_native(self, d):
         os.makedirs(d, exist_ok=True)

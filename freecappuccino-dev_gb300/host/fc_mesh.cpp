@@ -33,6 +33,16 @@ struct SplitMix64 {
   double uniform() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
 };
 
+const char* kSideName[6] = {"xmin", "xmax", "ymin", "ymax", "zmin", "zmax"};
+
+struct V3 { double x, y, z; };
+inline V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 cross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+}  // namespace
+
+// boundary type names of the reference (bctype) <-> FC_BC_*
 const char* bc_name_of(int t) {
   switch (t) {
     case FC_BC_WALL: return "wall";
@@ -57,14 +67,6 @@ int bc_type_of(const std::string& s) {
   return 0;
 }
 
-const char* kSideName[6] = {"xmin", "xmax", "ymin", "ymax", "zmin", "zmax"};
-
-struct V3 { double x, y, z; };
-inline V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-inline V3 cross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
-inline double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-
-}  // namespace
 
 int fc_mesh::validate(std::string* why) const {
   auto fail = [&](const char* m) { if (why) *why = m; return FC_ERR_BAD_INPUT; };

@@ -5,6 +5,10 @@
 
 #include "fc_gpu.h"
 
+// the reference's boundary type names ('wall', 'inlet', ...) and FC_BC_*
+const char* bc_name_of(int t);
+int bc_type_of(const std::string& s);
+
 struct fc_mesh {
   int numNodes = 0, numCells = 0, numInnerFaces = 0, numBoundaryFaces = 0, numFaces = 0;
   std::vector<double> x, y, z;      // numNodes

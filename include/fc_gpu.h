@@ -80,6 +80,13 @@ int fc_mesh_from_arrays(int numNodes, int numCells, int numInnerFaces, int numBo
  * size of a polyMesh directory (read_mesh_native, geometry.f90:165-410). */
 int fc_mesh_read_native(const char* dir, fc_mesh** out);
 int fc_mesh_write_native(const fc_mesh* m, const char* dir);
+/* Read / write OpenFOAM-format ASCII polyMesh files (read_mesh_openfoam,
+ * geometry.f90:846-1400): points, faces, owner, neighbour with FoamFile
+ * headers and 0-based indices, sizes from the owner file's note line and
+ * confirmed by every list; boundary in the reference's one-line-per-patch
+ * format (a header line, then name type nFaces startFace). */
+int fc_mesh_read_openfoam(const char* dir, fc_mesh** out);
+int fc_mesh_write_openfoam(const fc_mesh* m, const char* dir);
 
 /* info[6] = numNodes, numCells, numInnerFaces, numBoundaryFaces, numFaces, numBoundaries */
 int fc_mesh_info(const fc_mesh* m, int* info);

@@ -90,3 +90,41 @@ def test_noalloc_size_limit_is_host_side(fc):
                            10, 0.0, 1e-8, C.byref(info), C.cast(err, C.c_void_p), 256)
     assert st == fc.FC_ERR_BAD_INPUT
     assert b"FC_NOALLOC_MAX_N" in err.value
+
+
+@pytest.mark.parametrize("tets", [False, True])
+def test_openfoam_format_roundtrip(fc, tets):
+    """fc_mesh_write_openfoam / fc_mesh_read_openfoam (read_mesh_openfoam,
+    geometry.f90:846-1400): FoamFile headers, 0-based lists, the owner
+    file's note line; the mesh comes back unchanged."""
+    m = fc.Mesh.box(3, 2, 2, 2.0, 1.0, 1.0, perturb=0.15, seed=5, tets=tets,
+                    sides=["inlet", "outlet", "wall", "wall", "symmetry", "symmetry"])
+    with tempfile.TemporaryDirectory() as d:
+        m.write_openfoam(d)
+        owner = open(os.path.join(d, "owner")).read()
+        assert "FoamFile" in owner and "nInternalFaces:" in owner
+        m2 = fc.Mesh.read_openfoam(d)
+    a, b = m.arrays(), m2.arrays()
+    for k in ("x", "y", "z", "nnodes", "nodes", "owner", "neighbour", "bctype", "nfaces", "startFace"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+
+
+def test_openfoam_reader_parses_comments_and_checks_sizes(fc):
+    """Comments and compact lists are read; a list whose own size disagrees
+    with the owner file's note is rejected, as the reference stops there."""
+    m = fc.Mesh.box(2, 2, 1, sides=["wall"] * 6)
+    with tempfile.TemporaryDirectory() as d:
+        m.write_openfoam(d)
+        p = os.path.join(d, "points")
+        txt = open(p).read()
+        head, body = txt.split("\n\n", 1)
+        n, rest = body.split("\n", 1)
+        open(p, "w").write("/* generated */\n" + head + "\n// the points\n" + n + rest)
+        m2 = fc.Mesh.read_openfoam(d)
+        np.testing.assert_array_equal(m.arrays()["x"], m2.arrays()["x"])
+        nb = os.path.join(d, "neighbour")
+        t = open(nb).read().split("\n\n", 1)
+        cnt, rest = t[1].split("\n", 1)
+        open(nb, "w").write(t[0] + "\n\n" + str(int(cnt) + 1) + "\n" + rest)
+        with pytest.raises(fc.FcError):
+            fc.Mesh.read_openfoam(d)

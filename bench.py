@@ -478,6 +478,71 @@ def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None, tets=Fa
     return out
 
 
+def piso_block(fc, args, dev, with_cpu):
+    """PISO time steps (Euler, ncorr 2, one pressure solve per corrector,
+    urf 1) of the n^3 perturbed lid-driven cavity from rest, dt = 0.1 h:
+    milliseconds per time step (time_shift + calcuvw + calcp_piso) on the
+    GPU in FP64 and the oracle's time step on one core (opt-in: --piso-n)."""
+    n = args.piso_n
+    m = fc.Mesh.box(n, n, n, 1.0, 1.0, 1.0, perturb=PERTURB, seed=MESH_SEED)
+    nC, nT = m.numCells, m.numTotal
+    a, u, nwal = cavity_fields(m, nT, nC)
+    dt = 0.1 / n
+    kw = dict(urfU=1.0, urfP=1.0, maxiterU=20, maxiterP=100, tolRelU=1e-6, tolRelP=1e-6)
+    prm = fc.SimpleParams.cavity(**kw)
+    ctx = fc.Context(dev)
+    ctx.set_mesh(m)
+    zero = np.zeros(nT)
+    for k, v in dict(u=u, v=zero, w=zero, p=zero, pp=zero, den=np.ones(nT), vis=np.full(nT, 0.01)).items():
+        ctx.field_set(k, v)
+    ctx.field_set("visw", np.full(max(nwal, 1), 0.01))
+    ctx.simple_params(prm)
+    ctx.transient_params(dt, fc.FC_TIME_BDF, 1, 2)
+    ctx.init_flmass()
+    for _ in range(2):
+        ctx.time_shift()
+        ctx.piso_iteration()
+    ctx.sync()
+    ctx.event(0)
+    for _ in range(args.piso_steps):
+        ctx.time_shift()
+        res = ctx.piso_iteration()
+    ctx.event(1)
+    ms = ctx.elapsed_ms() / args.piso_steps
+    ctx.close()
+    out = {"workload": f"{n}^3 perturbed lid-driven cavity from rest, PISO (Euler, dt {dt:g}, ncorr 2, npcor 1), "
+                       "BiCGStab U / ICCG p to 1e-6", "cells": nC, "ms_per_time_step": ms,
+           "resor_last": [float(v) for v in res], "steps_timed": f"{args.piso_steps} after 2 untimed"}
+    if with_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_lib
+        oc = oracle_lib.Case(a, fast=True)
+        for k, v in dict(u=u, v=zero, w=zero, p=zero, pp=zero, den=np.ones(nT), vis=np.full(nT, 0.01)).items():
+            oc.set(k, v)
+        if nwal:
+            oc.set("visw", np.full(nwal, 0.01))
+        for name in ("viscos", "densit", "urfP", "gdsU", "cSchemeU", "pscheme", "maxiterU", "maxiterP", "npcor",
+                     "pRefCell", "tolAbsU", "tolRelU", "tolAbsP", "tolRelP", "gradScheme"):
+            oc.param(name, getattr(prm, name))
+        for i in range(3):
+            oc.param(f"urfU{i + 1}", prm.urfU[i])
+        for k, v in dict(timestep=dt, tscheme=1, piso=1, ncorr=2).items():
+            oc.param(k, v)
+        oc.solver("U", prm.lSolverU.decode())
+        oc.solver("P", prm.lSolverP.decode())
+        oc.L.orc_init_flmass(oc.h)
+        oc.time_shift()
+        oc.piso_iteration()
+        t0 = time.perf_counter()
+        oc.time_shift()
+        oc.piso_iteration()
+        dtc = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": dtc * 1e3, "unit": "ms per time step", "cores": 1, "kind": "port",
+                               "sample": "the second time step of the same run (C++ restatement, -O3, one thread)"}
+        out["gpu_vs_cpu"] = dtc * 1e3 / ms
+    return out
+
+
 def spmv_leg(fc, ctx, nC, calls):
     """FP64 y = A x through fc_spmv (ax_cr) on device-resident arrays of the
     same 128^3 system: the per-call CUDA-event time includes the call's host
@@ -738,6 +803,8 @@ def run_gpu(args, rank, world, dist):
         line["adjoint"] = adjoint_block(fc, args, dev)
     if args.batch_count > 0:
         line["batch"] = batch_block(fc, args, dev)
+    if args.piso_n > 0:
+        line["piso"] = piso_block(fc, args, dev, not args.no_cpu)
     if args.simple_tet_n > 0:
         # C5: 6 tets per perturbed hex, Re = 400, LSQ gradients, boundedLinearUpwind.  With the cavity
         # input's urfU 0.8 / urfP 0.3 the SIMPLE iteration diverges on this mesh (the oracle too, at
@@ -774,6 +841,8 @@ def main():
     ap.add_argument("--adjoint-n", type=int, default=96, help="cells per side of the adjoint case (0: skip)")
     ap.add_argument("--adjoint-fd-dirs", type=int, default=32, help="directions of the finite-difference check")
     ap.add_argument("--momentum-calls", type=int, default=5, help="timed calcuvw calls of the C3a leg")
+    ap.add_argument("--piso-n", type=int, default=0, help="cells per side of the PISO leg (0: skip)")
+    ap.add_argument("--piso-steps", type=int, default=10, help="timed PISO time steps")
     ap.add_argument("--batch-count", type=int, default=16, help="problems of the batched leg (0: skip)")
     ap.add_argument("--batch-tol", type=float, default=1e-6, help="relative L1 tolerance there")
     ap.add_argument("--batch-inner-tol", type=float, default=1e-4, help="FP32 inner tolerance there")

@@ -1325,6 +1325,42 @@ extern "C" int fc_calcp_piso(fc_ctx* ctx, double* resor4) {
   return FC_OK;
 }
 
+// main.f90:132-267: time steps, iterations, convergence and divergence stops
+extern "C" int fc_run(fc_ctx* ctx, const fc_run_params* prm, int* steps, int* iterations, double* resor) {
+  FC_RANGE();
+  if (!ctx || !prm || prm->numstep < 0 || prm->maxit < 1) return FC_ERR_BAD_INPUT;
+  SimpleState& S = sstate(ctx);
+  const bool transient = S.trp.scheme != FC_TIME_STEADY;
+  int nsteps = 0, niters = 0, st = FC_OK;
+  double r[4] = {0, 0, 0, 0};
+  bool done = false;
+  for (int itime = 1; itime <= prm->numstep && !done; ++itime) {
+    if (transient && (st = fc_time_shift(ctx))) return st;
+    ++nsteps;
+    for (int iter = 1; iter <= prm->maxit; ++iter) {
+      if ((st = fc_calcuvw(ctx, r)) < 0) return st;
+      if ((st = S.trp.piso ? fc_calcp_piso(ctx, &r[3]) : fc_calcp_simple(ctx, &r[3])) < 0) return st;
+      if (prm->temperature) {
+        double r7 = 0;
+        if ((st = fc_calculate_temperature(ctx, 1, &r7)) < 0) return st;
+      }
+      ++niters;
+      if (steps) *steps = nsteps;
+      if (iterations) *iterations = niters;
+      if (resor) for (int k = 0; k < 4; ++k) resor[k] = r[k];
+      const double source = std::max(r[0], std::max(r[1], r[2]));
+      if (!(source <= (double)1e+30f)) return fc_fail_msg(ctx, FC_ERR_NAN, "iterations diverge");
+      if (source < prm->tolerance) {
+        if (!transient) done = true;
+        break;
+      }
+    }
+  }
+  if (steps) *steps = nsteps;
+  if (iterations) *iterations = niters;
+  return FC_OK;
+}
+
 // one PISO iteration of main.f90:159-165 (calcuvw + calcp_piso)
 extern "C" int fc_piso_iteration(fc_ctx* ctx, double* resor) {
   FC_RANGE();

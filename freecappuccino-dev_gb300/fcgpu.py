@@ -133,6 +133,7 @@ def lib():
         "fc_time_shift": (i, [vp]),
         "fc_calcp_piso": (i, [vp, vp]),
         "fc_piso_iteration": (i, [vp, vp]),
+        "fc_run": (i, [vp, vp, vp, vp, vp]),
         "fc_download_fields": (i, [vp, i, vp, vp, vp]),
         "fc_batch_create": (i, [vp, vp]),
         "fc_batch_destroy": (i, [vp]),
@@ -234,6 +235,11 @@ class SimpleParams(C.Structure):
         p.lSolverP = kw.get("solverP", "iccg").encode()
         p.flomas = kw.get("flomas", 0.0)
         return p
+
+
+class RunParams(C.Structure):
+    """fc_run_params: the outer loops of main.f90."""
+    _fields_ = [("numstep", C.c_int), ("maxit", C.c_int), ("tolerance", C.c_double), ("temperature", C.c_int)]
 
 
 class TransientParams(C.Structure):
@@ -665,6 +671,14 @@ class Context:
     def transient_params(self, timestep, scheme, piso=0, ncorr=1):
         prm = TransientParams(float(timestep), int(scheme), int(piso), int(ncorr))
         self._check(self.L.fc_transient_set_params(self.h, C.byref(prm)), "fc_transient_set_params")
+
+    def run(self, numstep, maxit, tolerance, temperature=False):
+        """main.f90's time and iteration loops; returns (steps, iterations, resor[4])."""
+        p = RunParams(int(numstep), int(maxit), float(tolerance), int(bool(temperature)))
+        steps, iters = C.c_int(0), C.c_int(0)
+        r = np.zeros(4)
+        self._check(self.L.fc_run(self.h, C.byref(p), C.byref(steps), C.byref(iters), _ptr(r)), "fc_run")
+        return steps.value, iters.value, r
 
     def time_shift(self):
         self._check(self.L.fc_time_shift(self.h), "fc_time_shift")

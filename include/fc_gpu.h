@@ -427,6 +427,22 @@ int fc_time_shift(fc_ctx* ctx);
 int fc_calcp_piso(fc_ctx* ctx, double* resor4);
 int fc_piso_iteration(fc_ctx* ctx, double* resor);
 
+/* The outer loops of main.f90:132-267: numstep time steps (time_shift first
+ * when the context is transient), in each up to maxit iterations of calcuvw
+ * + calcp_simple (or calcp_piso in PISO mode) + calculate_temperature (when
+ * temperature != 0), until max(resor(1:3)) < tolerance.  A transient run
+ * then goes on with the next time step; a steady one stops there, as
+ * converged.  Stops with FC_ERR_NAN when the iterations diverge
+ * (max(resor(1:3)) > 1e30).  *steps, *iterations: done; resor[4]: the last
+ * iteration's resor(1:4). */
+typedef struct {
+  int numstep;
+  int maxit;
+  double tolerance;
+  int temperature;
+} fc_run_params;
+int fc_run(fc_ctx* ctx, const fc_run_params* prm, int* steps, int* iterations, double* resor);
+
 /* ---------------------------------------------------------------------------
  * Scalar transport: the temperature equation (ScalarEqns/temperature.f90).
  * --------------------------------------------------------------------------- */

@@ -74,3 +74,43 @@ def test_unsupported_combinations_are_rejected(ctx, fc):
     assert e.value.code == fc.FC_ERR_UNSUPPORTED
     with pytest.raises(fc.FcError):
         ctx.transient_params(0.0, fc.FC_TIME_BDF, 0, 1)
+
+
+def oracle_run(oc, numstep, maxit, tolerance, transient, piso):
+    """main.f90:132-267 driven from Python on the oracle."""
+    steps = iters = 0
+    r = None
+    for itime in range(numstep):
+        if transient:
+            oc.time_shift()
+        steps += 1
+        done = False
+        for it in range(maxit):
+            r = oc.piso_iteration()[1] if piso else oc.simple_iteration()[1]
+            iters += 1
+            if max(r[:3]) < tolerance:
+                done = not transient
+                break
+        if done:
+            break
+    return steps, iters, r
+
+
+def test_run_loops_track_oracle(ctx, fc):
+    """fc_run: steady SIMPLE to a tolerance, then PISO time steps with up to
+    two iterations each, against the same loops on the oracle."""
+    m, oc = setup_cavity(ctx, fc, "run", 6, 6, 6, **dict(KW, urfU=0.8, urfP=0.3))
+    sg, ig, rg = ctx.run(1, 40, 1e-2)
+    so, io, ro = oracle_run(oc, 1, 40, 1e-2, False, False)
+    assert (sg, ig) == (so, io)
+    np.testing.assert_allclose(rg, ro, rtol=1e-7)
+    compare_fields(ctx, oc)
+    transient(ctx, oc, 0.01, fc.FC_TIME_BDF, 1)
+    try:
+        sg, ig, rg = ctx.run(3, 2, 1e-12)
+        so, io, ro = oracle_run(oc, 3, 2, 1e-12, True, True)
+        assert (sg, ig) == (so, io) == (3, 6)
+        np.testing.assert_allclose(rg, ro, rtol=1e-7)
+        compare_fields(ctx, oc)
+    finally:
+        steady(ctx, oc)

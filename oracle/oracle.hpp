@@ -51,6 +51,7 @@ struct Case {
   std::vector<double> u, v, w, p, pp, flmass, vis, den, visw;
   std::vector<double> dUdxi, dVdxi, dWdxi, dPdxi;  // 3*(numTotal+1)
   std::vector<double> Dmat;                        // 9*(numCells+1)  (gradients.f90:12)
+  int dmatScheme = 0;                              // gradient scheme Dmat was built for (0: none)
   // solver work vectors (linear_solvers.f90:33)
   std::vector<double> res, reso, pk, zk, d, uk, vk;
   // parameters of the SIMPLE path

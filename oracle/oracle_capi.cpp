@@ -214,8 +214,8 @@ int orc_grad(void* h, int scheme, double* phi, double* dphi) {
   Case& c = *(Case*)h;
   std::vector<double> p = pad1(phi, c.numTotal);
   std::vector<double> g(3 * (size_t)(c.numTotal + 1), 0.0);
-  if (scheme == 1) { if (c.Dmat.empty() || c.gradScheme != 1) create_matrix_lsq(c); grad_lsq(c, p, g); }
-  else if (scheme == 2) { if (c.Dmat.empty() || c.gradScheme != 2) create_matrix_lsq_dm(c); grad_lsq_dm(c, p, g); }
+  if (scheme == 1) { if (c.dmatScheme != 1) create_matrix_lsq(c); grad_lsq(c, p, g); }
+  else if (scheme == 2) { if (c.dmatScheme != 2) create_matrix_lsq_dm(c); grad_lsq_dm(c, p, g); }
   else if (scheme == 3) grad_node_based_gauss(c, p, g);
   else grad_gauss(c, p, g);
   slope_limiter(c, p, g);

@@ -67,6 +67,7 @@ static void lsq_invert(Case& c) {
 // create_matrix_lsq, gradients.f90:660-779
 void create_matrix_lsq(Case& c) {
   c.Dmat.assign(9 * (size_t)(c.numCells + 1), 0.0);
+  c.dmatScheme = 1;
   auto D = [&](int k, int i) -> double& { return c.Dmat[9 * (size_t)i + (k - 1)]; };
   for (int i = 1; i <= c.numInnerFaces; ++i) {
     int ijp = c.owner[i], ijn = c.neighbour[i];
@@ -95,6 +96,7 @@ void create_matrix_lsq(Case& c) {
 // create_matrix_lsq_dm, gradients.f90:1157-1328
 void create_matrix_lsq_dm(Case& c) {
   c.Dmat.assign(9 * (size_t)(c.numCells + 1), 0.0);
+  c.dmatScheme = 2;
   auto D = [&](int k, int i) -> double& { return c.Dmat[9 * (size_t)i + (k - 1)]; };
   for (int i = 1; i <= c.numInnerFaces; ++i) {
     int ijp = c.owner[i], ijn = c.neighbour[i];
@@ -180,6 +182,10 @@ void grad_lsq_dm(Case& c, const std::vector<double>& phi, std::vector<double>& g
 
 // grad_scalar_field, gradients.f90:106-163: the gradient, then the limiter
 void grad(Case& c, const std::vector<double>& phi, std::vector<double>& g) {
+  // the least-squares matrices of the scheme (create_matrix_lsq / _dm, built
+  // at initialisation in the reference) on first use
+  if (c.gradScheme == 1 && c.dmatScheme != 1) create_matrix_lsq(c);
+  if (c.gradScheme == 2 && c.dmatScheme != 2) create_matrix_lsq_dm(c);
   if (c.gradScheme == 1) grad_lsq(c, phi, g);
   else if (c.gradScheme == 2) grad_lsq_dm(c, phi, g);
   else if (c.gradScheme == 3) grad_node_based_gauss(c, phi, g);

@@ -134,6 +134,8 @@ def lib():
         "fc_calcp_piso": (i, [vp, vp]),
         "fc_piso_iteration": (i, [vp, vp]),
         "fc_run": (i, [vp, vp, vp, vp, vp]),
+        "fc_namelist_read": (i, [cp, vp, vp, i]),
+        "fc_apply_settings": (i, [vp, vp]),
         "fc_download_fields": (i, [vp, i, vp, vp, vp]),
         "fc_batch_create": (i, [vp, vp]),
         "fc_batch_destroy": (i, [vp]),
@@ -268,6 +270,22 @@ class TemperatureParams(C.Structure):
         p.lSolverT = kw.get("solver", "bicgstab").encode()
         return p
 
+
+class CaseSettings(C.Structure):
+    """fc_case_settings: the case namelist as the path uses it."""
+    _fields_ = [("simple", SimpleParams), ("temperature", TemperatureParams), ("transient", TransientParams),
+                ("run", RunParams), ("limiter", C.c_int), ("calcU", C.c_int), ("calcP", C.c_int),
+                ("calcT", C.c_int), ("mesh_foam", C.c_int), ("title", C.c_char * 72)]
+
+
+def read_namelist(path):
+    """fc_namelist_read: CaseSettings of a namelist file (no GPU needed)."""
+    out = CaseSettings()
+    err = C.create_string_buffer(256)
+    st = lib().fc_namelist_read(path.encode(), C.byref(out), err, 256)
+    if st != 0:
+        raise FcError(st, err.value.decode())
+    return out
 
 class Mesh:
     """Host mesh in the reference's native layout (1-based indices)."""
@@ -679,6 +697,10 @@ class Context:
         r = np.zeros(4)
         self._check(self.L.fc_run(self.h, C.byref(p), C.byref(steps), C.byref(iters), _ptr(r)), "fc_run")
         return steps.value, iters.value, r
+
+    def apply_settings(self, settings):
+        """fc_apply_settings: simple, transient, limiter and temperature settings."""
+        self._check(self.L.fc_apply_settings(self.h, C.byref(settings)), "fc_apply_settings")
 
     def time_shift(self):
         self._check(self.L.fc_time_shift(self.h), "fc_time_shift")

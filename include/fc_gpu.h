@@ -479,6 +479,30 @@ int fc_temperature_set_params(fc_ctx* ctx, const fc_temperature_params* prm, con
  * setup (srdw covers 'wall' patches only) and is not accepted. */
 int fc_calculate_temperature(fc_ctx* ctx, int solve, double* resor7);
 
+/* ---- The case namelist &input_parameters (read_input.f90:28-227) for the
+ * keys this path uses, starting from the reference's module defaults
+ * (velocity.f90:24-33, pressure.f90:28-33, temperature.f90:14-25; default-real
+ * literals such as urfU = 0.7 promoted as the reference promotes them).
+ * The gradient flags select FC_GRAD_* as grad_scalar_field does; ltransient
+ * with bdf / bdf2 / bdf3, SIMPLE / PISO, ncorr, npcor, numstep, maxit,
+ * tolerance and timestep fill the transient and loop settings.  lstsq_qr,
+ * CN, compressible and const_mflux are rejected (errmsg says which); keys
+ * of other modules are skipped.  fc_namelist_read needs no GPU.
+ * fc_apply_settings passes them to a context (simple, transient, limiter
+ * and, with calcT, temperature parameters); fc_run then runs the loops. */
+typedef struct {
+  fc_simple_params simple;
+  fc_temperature_params temperature;
+  fc_transient_params transient;
+  fc_run_params run;
+  int limiter;                /* FC_LIMITER_* */
+  int calcU, calcP, calcT;
+  int mesh_foam;              /* mesh_format 'foamMesh' (else 'nativeMesh') */
+  char title[72];
+} fc_case_settings;
+int fc_namelist_read(const char* path, fc_case_settings* out, char* errmsg, int errlen);
+int fc_apply_settings(fc_ctx* ctx, const fc_case_settings* s);
+
 /* ---------------------------------------------------------------------------
  * Discrete adjoint of steady scalar convection-diffusion.  No counterpart in
  * the reference; the operator is the implicit part of its facefluxsc

@@ -114,11 +114,11 @@ int stage(fc_batch* b, int p, const double* a, double* x, const double* rhs, Bat
   it.s = s;
   if (!a || !x || !rhs) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_batch_solve: NULL array");
   if (is_device_ptr(a)) it.a = a;
-  else { FC_CUDA_TRY(ctx, cudaMemcpyAsync(s->a.p, a, (size_t)nnz * 8, cudaMemcpyHostToDevice, ctx->stream)); it.a = s->a.p; }
+  else { FC_CUDA_TRY(ctx, cudaMemcpyAsync(s->a.p, a, (size_t)nnz * sizeof(double), cudaMemcpyHostToDevice, ctx->stream)); it.a = s->a.p; }
   if (is_device_ptr(rhs)) it.b = rhs;
-  else { FC_CUDA_TRY(ctx, cudaMemcpyAsync(s->b.p, rhs, (size_t)n * 8, cudaMemcpyHostToDevice, ctx->stream)); it.b = s->b.p; }
+  else { FC_CUDA_TRY(ctx, cudaMemcpyAsync(s->b.p, rhs, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream)); it.b = s->b.p; }
   x_host = !is_device_ptr(x);
-  if (x_host) { FC_CUDA_TRY(ctx, cudaMemcpyAsync(s->x.p, x, (size_t)n * 8, cudaMemcpyHostToDevice, ctx->stream)); it.x = s->x.p; }
+  if (x_host) { FC_CUDA_TRY(ctx, cudaMemcpyAsync(s->x.p, x, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream)); it.x = s->x.p; }
   else it.x = x;
   return FC_OK;
 }
@@ -139,7 +139,7 @@ int run(fc_batch* b, const char* solver, const double* const* a, double* const* 
       // tuning: start from the caller's x0 in the system's own vector
       CsrSystem* s = b->probs[p].s;
       const cudaMemcpyKind k = is_device_ptr(x[p]) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-      FC_CUDA_TRY(ctx, cudaMemcpyAsync(s->x.p, x[p], (size_t)b->probs[p].n * 8, k, ctx->stream));
+      FC_CUDA_TRY(ctx, cudaMemcpyAsync(s->x.p, x[p], (size_t)b->probs[p].n * sizeof(double), k, ctx->stream));
     }
     xh[p] = x_host ? 1 : 0;
   }
@@ -148,7 +148,7 @@ int run(fc_batch* b, const char* solver, const double* const* a, double* const* 
   if (!x_scratch)
     for (int p = 0; p < np; ++p)
       if (xh[p])
-        FC_CUDA_TRY(ctx, cudaMemcpyAsync(x[p], items[p].x, (size_t)b->probs[p].n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        FC_CUDA_TRY(ctx, cudaMemcpyAsync(x[p], items[p].x, (size_t)b->probs[p].n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   FC_CUDA_TRY(ctx, cudaEventRecord(ctx->sev1, ctx->stream));
   FC_CUDA_TRY(ctx, cudaEventSynchronize(ctx->sev1));
   float f = 0;

@@ -266,6 +266,11 @@ def batch_block(fc, args, dev):
     out["gpu_launches_per_batched_mixed_solve"] = (ctx.kernel_launches() - launches0) / (reps + 1)
     xm = [dx[k].cpu().numpy() for k in allidx]
     out["mixed_max_rel_diff_vs_fp64"] = float(max(np.abs(u - v).max() / np.abs(v).max() for u, v in zip(xm, x64)))
+    # per problem: FP64 iterations, mixed inner iterations and refinement steps
+    out["iterations_per_problem"] = {"fp64": [int(i.itr_used) for i in inf64],
+                                     "mixed_inner": [int(i.itr_used) for i in infm],
+                                     "mixed_outer": [int(i.outer_iterations) for i in infm],
+                                     "mixed_group_ms": [float(i.ms) for i in infm]}
     out["mixed_outer_steps_max"] = int(max(i.outer_iterations for i in infm))
     out["mixed_not_converged"] = int(sum(i.status != 0 for i in infm))
     out["mixed_sequential_ms"], _ = timed(singles)

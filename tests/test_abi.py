@@ -128,3 +128,36 @@ def test_openfoam_reader_parses_comments_and_checks_sizes(fc):
         open(nb, "w").write(t[0] + "\n\n" + str(int(cnt) + 1) + "\n" + rest)
         with pytest.raises(fc.FcError):
             fc.Mesh.read_openfoam(d)
+
+
+def test_struct_layouts_match_the_header(fc, tmp_path):
+    """The ctypes mirrors of the header's structs have the C layout: sizes
+    and field offsets from a C program compiled against include/fc_gpu.h."""
+    import ctypes as C
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if not gcc:
+        pytest.skip("gcc not available")
+    structs = {"fc_solve_info": fc.SolveInfo, "fc_simple_params": fc.SimpleParams,
+               "fc_temperature_params": fc.TemperatureParams, "fc_transient_params": fc.TransientParams,
+               "fc_run_params": fc.RunParams, "fc_case_settings": fc.CaseSettings}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "fc_gpu.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f in py._fields_:
+            lines.append(f'  printf("{cname} {f[0]} %zu\\n", offsetof({cname}, {f[0]}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([gcc, "-I", inc, str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        name, field, val = line.split()
+        got[(name, field)] = int(val)
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for f in py._fields_:
+            assert got[(cname, f[0])] == getattr(py, f[0]).offset, (cname, f[0])

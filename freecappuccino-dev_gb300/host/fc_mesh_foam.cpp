@@ -5,8 +5,9 @@
 // sizes come from the owner file's note line (nPoints, nCells, nFaces,
 // nInternalFaces), and every list's own size must confirm them, as the
 // reference checks.  Indices are 0-based in the files and 1-based in
-// fc_mesh.  `boundary` is the reference's one-line-per-patch file: a header
-// line, then `name type nFaces startFace [startFaceTwin]`.
+// fc_mesh.  `boundary` is the reference's one-line-per-patch file (a header
+// line, then `name type nFaces startFace [startFaceTwin]`) or OpenFOAM's own
+// dictionary form.
 #include <cctype>
 #include <cstdio>
 #include <cstdlib>
@@ -103,6 +104,75 @@ bool note_value(const std::string& s, const char* key, long long* v) {
   return true;
 }
 
+// OpenFOAM's dictionary-form boundary file: N ( name { type T; nFaces n;
+// startFace s; ... } ... ).  A patch's role: its type where the type names
+// one (wall, symmetryPlane / symmetry, empty, cyclic), else its name when
+// that is one of the reference's types (inlet, outlet, pressure, ...).
+bool boundary_dict(const std::string& text, fc_mesh* m) {
+  std::string s = strip_comments(text);
+  const size_t ff = s.find("FoamFile");
+  size_t pos = 0;
+  if (ff != std::string::npos) {
+    int depth = 0;
+    size_t i = s.find('{', ff);
+    for (; i < s.size(); ++i) {
+      if (s[i] == '{') ++depth;
+      else if (s[i] == '}' && --depth == 0) break;
+    }
+    pos = i + 1;
+  }
+  size_t open = s.find('(', pos);
+  if (open == std::string::npos) return false;
+  size_t i = open + 1;
+  auto skip_ws = [&]() { while (i < s.size() && std::isspace((unsigned char)s[i])) ++i; };
+  auto word = [&]() {
+    skip_ws();
+    size_t j = i;
+    while (j < s.size() && !std::isspace((unsigned char)s[j]) && s[j] != '{' && s[j] != '}' && s[j] != ';' &&
+           s[j] != '(' && s[j] != ')')
+      ++j;
+    std::string w = s.substr(i, j - i);
+    i = j;
+    return w;
+  };
+  for (;;) {
+    skip_ws();
+    if (i >= s.size()) return false;
+    if (s[i] == ')') break;
+    const std::string name = word();
+    skip_ws();
+    if (name.empty() || i >= s.size() || s[i] != '{') return false;
+    const size_t close = s.find('}', i);
+    if (close == std::string::npos) return false;
+    std::string type;
+    long long nf = -1, sf = -1;
+    std::istringstream body(s.substr(i + 1, close - i - 1));
+    std::string entry;
+    while (std::getline(body, entry, ';')) {
+      std::istringstream es(entry);
+      std::string key, val;
+      es >> key >> val;
+      if (key == "type") type = val;
+      else if (key == "nFaces") nf = std::atoll(val.c_str());
+      else if (key == "startFace") sf = std::atoll(val.c_str());
+    }
+    i = close + 1;
+    if (nf < 0 || sf < 0) return false;
+    int t = 0;
+    if (type == "wall") t = FC_BC_WALL;
+    else if (type == "symmetryPlane" || type == "symmetry") t = FC_BC_SYMMETRY;
+    else if (type == "empty") t = FC_BC_EMPTY;
+    else if (type == "cyclic") t = FC_BC_PERIODIC;
+    else t = bc_type_of(name);
+    if (!t) return false;
+    m->bcname.push_back(name);
+    m->bctype.push_back(t);
+    m->nfaces.push_back((int)nf);
+    m->startFace.push_back((int)sf);
+  }
+  return true;
+}
+
 void header(FILE* f, const char* cls, const char* object, const std::string& note) {
   std::fprintf(f, "FoamFile\n{\n    version     2.0;\n    format      ascii;\n    class       %s;\n", cls);
   if (!note.empty()) std::fprintf(f, "    note        \"%s\";\n", note.c_str());
@@ -165,9 +235,18 @@ extern "C" int fc_mesh_read_openfoam(const char* dir, fc_mesh** out) {
     if (!(fn >> m->neighbour[f])) return fail();
     m->neighbour[f] += 1;
   }
-  // boundary: a header line, then name type nFaces startFace [startFaceTwin]
-  std::ifstream bf(d + "/boundary");
-  if (!bf) return fail();
+  // boundary: OpenFOAM's dictionary form, or the reference's: a header
+  // line, then name type nFaces startFace [startFaceTwin]
+  std::string bnd_t;
+  if (!slurp(d + "/boundary", bnd_t)) return fail();
+  if (bnd_t.find("FoamFile") != std::string::npos) {
+    if (!boundary_dict(bnd_t, m)) return fail();
+    std::string why;
+    if (m->validate(&why) != FC_OK) return fail();
+    *out = m;
+    return FC_OK;
+  }
+  std::istringstream bf(bnd_t);
   std::string line;
   std::getline(bf, line);
   while (std::getline(bf, line)) {

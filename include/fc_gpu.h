@@ -84,7 +84,10 @@ int fc_mesh_write_native(const fc_mesh* m, const char* dir);
  * geometry.f90:846-1400): points, faces, owner, neighbour with FoamFile
  * headers and 0-based indices, sizes from the owner file's note line and
  * confirmed by every list; boundary in the reference's one-line-per-patch
- * format (a header line, then name type nFaces startFace). */
+ * format (a header line, then name type nFaces startFace) or in OpenFOAM's
+ * dictionary form (type wall / symmetryPlane / symmetry / empty / cyclic
+ * give the role, a generic patch takes it from its name: inlet, outlet,
+ * pressure, ...).  The writer uses the reference's format. */
 int fc_mesh_read_openfoam(const char* dir, fc_mesh** out);
 int fc_mesh_write_openfoam(const fc_mesh* m, const char* dir);
 

@@ -161,3 +161,25 @@ def test_struct_layouts_match_the_header(fc, tmp_path):
         assert got[(cname, "size")] == C.sizeof(py), cname
         for f in py._fields_:
             assert got[(cname, f[0])] == getattr(py, f[0]).offset, (cname, f[0])
+
+
+def test_openfoam_dictionary_boundary(fc):
+    """OpenFOAM's own boundary dictionary: roles from the patch type, or
+    from the name of a generic patch."""
+    m = fc.Mesh.box(3, 2, 2, sides=["inlet", "outlet", "wall", "wall", "symmetry", "symmetry"])
+    a = m.arrays()
+    with tempfile.TemporaryDirectory() as d:
+        m.write_openfoam(d)
+        kinds = {fc.BC["wall"]: "wall", fc.BC["symmetry"]: "symmetryPlane"}
+        names = ["inlet", "outlet", "bottom", "top", "front", "back"]
+        body = "".join(
+            f"    {nm}\n    {{\n        type {kinds.get(int(t), 'patch')};\n        inGroups 1(x);\n"
+            f"        nFaces {int(nf)};\n        startFace {int(sf)};\n    }}\n"
+            for nm, t, nf, sf in zip(names, a["bctype"], a["nfaces"], a["startFace"]))
+        open(os.path.join(d, "boundary"), "w").write(
+            "FoamFile\n{\n    version 2.0;\n    format ascii;\n    class polyBoundaryMesh;\n    object boundary;\n}\n"
+            f"// patches\n{len(names)}\n(\n{body})\n")
+        m2 = fc.Mesh.read_openfoam(d)
+    b = m2.arrays()
+    for k in ("bctype", "nfaces", "startFace", "owner", "neighbour"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)

@@ -3,12 +3,19 @@
 // preconditioner / matrix-vector entry points.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
 
 #include "fc_internal.hpp"
+
+static std::atomic<long long> g_device_allocs{0};
+
+void fc_count_device_alloc() { g_device_allocs.fetch_add(1, std::memory_order_relaxed); }
+
+extern "C" long long fc_device_alloc_count(void) { return g_device_allocs.load(std::memory_order_relaxed); }
 
 int fc_fail(fc_ctx* ctx, int code, const char* what, cudaError_t e) {
   if (ctx) {

@@ -22,6 +22,10 @@ constexpr double FC_S0 = static_cast<double>(1.e20f);
     if (_e != cudaSuccess) return fc_fail((ctx), FC_ERR_CUDA, #expr, _e);       \
   } while (0)
 
+// Count of the library's device allocations and frees (every device buffer
+// goes through DVec), read by fc_device_alloc_count.
+void fc_count_device_alloc();
+
 template <class T>
 struct DVec {
   T* p = nullptr;
@@ -34,12 +38,13 @@ struct DVec {
     if (count == n && p) return cudaSuccess;
     release();
     if (count == 0) return cudaSuccess;
+    fc_count_device_alloc();
     cudaError_t e = cudaMalloc(&p, count * sizeof(T));
     if (e == cudaSuccess) n = count; else p = nullptr;
     return e;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) { fc_count_device_alloc(); cudaFree(p); }
     p = nullptr;
     n = 0;
   }

@@ -1410,7 +1410,9 @@ extern "C" int fc_set_tracing(fc_ctx* ctx, int on) {
 // fc_dpcg_noalloc: the Jacobi-PCG kernel (k_dpcg, dpcg of
 // linear_solvers.f90:206-359) run on a fixed scratch area in static device
 // memory instead of a CsrSystem workspace, so the call allocates nothing
-// (no cudaMalloc/cudaFree, no event or stream creation, no host heap).
+// (no cudaMalloc/cudaFree, no event or stream creation, no host heap).  It
+// launches one block per SM as launch_coop does for fc_csrsolve("dpcg"), so
+// the grid reductions, and with them the iterates, are the same.
 //
 // Scratch (one per device, this translation unit): r, p, z (FC_NOALLOC_MAX_N
 // doubles each), the grid reduction partials (two sets of FC_NPART per
@@ -1454,6 +1456,31 @@ extern "C" int fc_dpcg_noalloc(void* stream, int n, int nnz, const int* ia, cons
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES)
     return na_fail(errmsg, errlen, FC_ERR_CUDA, "no current CUDA device");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (st) {
+    int sdev = -1;
+    if (cudaStreamGetDevice(st, &sdev) != cudaSuccess)
+      return na_fail(errmsg, errlen, FC_ERR_BAD_INPUT, "stream is not a valid CUDA stream");
+    if (sdev != dev)
+      return na_fail(errmsg, errlen, FC_ERR_BAD_INPUT,
+                     "stream belongs to another device than the current one (make its device current)");
+  }
+  for (const void* ptr : {(const void*)ia, (const void*)ja, (const void*)a, (const void*)diag, (const void*)x,
+                          (const void*)b}) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) { cudaGetLastError(); continue; }
+    if (at.type == cudaMemoryTypeDevice && at.device != dev)
+      return na_fail(errmsg, errlen, FC_ERR_BAD_INPUT, "arrays must be memory of the current device");
+  }
+  {
+    int ends[2] = {-1, -1};
+    if (cudaMemcpyAsync(ends, ia, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(ends + 1, ia + n, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return na_fail(errmsg, errlen, FC_ERR_CUDA, "reading ia[0] and ia[n] failed");
+    if (ends[0] != 0 || ends[1] != nnz)
+      return na_fail(errmsg, errlen, FC_ERR_BAD_INPUT, "ia must be 0-based with ia[0] == 0 and ia[n] == nnz");
+  }
   unsigned char* base;
   {
     std::lock_guard<std::mutex> lock(g_na_mutex);
@@ -1471,7 +1498,8 @@ extern "C" int fc_dpcg_noalloc(void* stream, int n, int nnz, const int* ia, cons
       cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, FC_BLOCK, 0) != cudaSuccess || occ < 1)
     return na_fail(errmsg, errlen, FC_ERR_UNSUPPORTED, "cooperative launch not available");
-  const int blocks = std::min(NA_MAX_BLOCKS, sms * occ);
+  // one block per SM, the grid of fc_csrsolve's launch
+  const int blocks = std::max(1, std::min(NA_MAX_BLOCKS, sms));
 
   double* r = (double*)base;
   double* p = (double*)(base + NA_VEC);
@@ -1490,7 +1518,6 @@ extern "C" int fc_dpcg_noalloc(void* stream, int n, int nnz, const int* ia, cons
   A.x = x; A.b = b; A.r = r; A.p = p; A.z = z;
   A.itr_max = itr_max; A.tol_abs = tol_abs; A.tol_rel = tol_rel;
 
-  cudaStream_t st = (cudaStream_t)stream;
   if (cudaMemsetAsync(zero_from, 0, NA_OUT + NA_CTL, st) != cudaSuccess)
     return na_fail(errmsg, errlen, FC_ERR_CUDA, "clearing the control block failed");
   void* args[1] = {&A};

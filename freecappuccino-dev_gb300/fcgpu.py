@@ -87,6 +87,7 @@ def lib():
         "fc_set_verbosity": (i, [vp, i]),
         "fc_set_precision": (i, [vp, i, d, i]),
         "fc_kernel_launches": (C.c_longlong, [vp]),
+        "fc_device_alloc_count": (C.c_longlong, []),
         "fc_stream_sync": (i, [vp]),
         "fc_stream": (vp, [vp]),
         "fc_event_record": (i, [vp, i]),
@@ -151,6 +152,11 @@ def lib():
         f.argtypes = args
     _lib = L
     return L
+
+
+def device_alloc_count():
+    """Device allocations plus frees the library has made so far."""
+    return int(lib().fc_device_alloc_count())
 
 
 def declared_symbols(header=None):

@@ -124,6 +124,9 @@ int fc_set_verbosity(fc_ctx* ctx, int level);
  * refinement loop stops on the reference's criterion in FP64. */
 int fc_set_precision(fc_ctx* ctx, int mode, double inner_tol, int inner_itmax);
 long long fc_kernel_launches(const fc_ctx* ctx);  /* kernels launched so far by this context */
+/* device allocations plus frees made by the library so far, over all
+ * contexts (a diagnostic: no reference counterpart) */
+long long fc_device_alloc_count(void);
 int fc_stream_sync(fc_ctx* ctx);
 void* fc_stream(fc_ctx* ctx);                     /* the cudaStream_t every call is ordered on */
 int fc_event_record(fc_ctx* ctx, int which);      /* which: 0 start, 1 stop (on the context stream) */
@@ -250,15 +253,19 @@ int fc_trace_get(fc_ctx* ctx, double* out, unsigned long long* timeline);
 int fc_ilu0(fc_ctx* ctx, int n, int nnz, const int* ia, const int* ja, const double* a, const int* diag,
             double* l_out);
 
-/* Jacobi-PCG (dpcg, linear_solvers.f90:206-359) that allocates nothing.  No
- * counterpart in the reference: it is for callers that may not allocate
- * device memory during a solve (cudaMalloc/cudaFree synchronise the device,
- * and a caller whose pool allocator owns the free memory cannot take more).
- * Its work vectors live in a fixed scratch area in static device memory of
- * the library (3 * FC_NOALLOC_MAX_N doubles + a small control block, one per
- * device); n > FC_NOALLOC_MAX_N is rejected with FC_ERR_BAD_INPUT.
- *  - ia(n+1), ja(nnz), diag(n) 0-based, a, x (in/out), b: DEVICE memory;
- *    stream: a cudaStream_t (NULL = legacy default stream).
+/* Jacobi-preconditioned CG solve that allocates nothing.  It has no
+ * counterpart in the reference.  It is for callers that may not allocate
+ * device memory while they solve: cudaMalloc/cudaFree synchronise the whole
+ * device and stall the caller's other streams, and a caller whose pool
+ * allocator already holds the free memory cannot get more.  Its work vectors
+ * live in a fixed scratch area in static device memory of the library
+ * (3 * FC_NOALLOC_MAX_N doubles + a small control block, one per device,
+ * held until the process exits); n > FC_NOALLOC_MAX_N is rejected with
+ * FC_ERR_BAD_INPUT.  The iteration is fc_csrsolve's "dpcg" on the same grid
+ * (one block per SM), so both give the same iterates.
+ *  - ia(n+1), ja(nnz), diag(n) 0-based with ia[0] == 0 and ia[n] == nnz;
+ *    a, x (in/out), b: DEVICE memory of the current device; stream: a
+ *    cudaStream_t of that device (NULL = legacy default stream).
  *  - the first call on each device looks up the scratch address
  *    (cudaGetSymbolAddress with that device current): make that first call
  *    before any stream capture.

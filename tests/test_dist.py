@@ -56,7 +56,7 @@ def test_reference_arm_under_torchrun_two_ranks():
     prefix of its own options.)"""
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
            "127.0.0.1", "--master-port", str(free_port()), "bench.py", "--impl", "reference", "--gpus", "2",
-           "--steps", "1", "--warmup", "0", "--cells-per-side", "10", "--ref-sample", "3"]
+           "--steps", "1", "--warmup", "0", "--cells-per-side", "10", "--ref-warmup-iters", "3"]
     env = dict(os.environ, OMP_NUM_THREADS="1")
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600, env=env)
     assert r.returncode == 0, r.stderr[-2000:]

@@ -1,0 +1,113 @@
+"""The FP32 inner BiCGStab of the mixed-precision solves against its CPU
+replay (tests/replay/bicgstab32_replay.cpp: the reference's DILU-BiCGStab,
+linear_solvers.f90:548-786, with FP32 matrix, factors and vectors and FP64
+dots, the device's precision split), on problem 11 of the batched
+convection-diffusion configuration (72^3 cells, cell Peclet 0.55):
+
+  - the iterates after k = 1..6 iterations from dx = 0, single solve
+    (fc_csrsolve in FC_PREC_MIXED with the inner solve capped at k) and
+    batched (fc_batch_solve), agree with the replay's to FP32 rounding;
+  - the first inner solve to the relative tolerance 1e-4 takes the
+    replay's iteration count, single and batched."""
+import ctypes as C
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from cd_cases import cd_batch_sizes, cd_batch_system
+from conftest import load_fcgpu
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PROBLEM = 11
+ITERATE_TOL = 1e-4     # max |x_gpu - x_replay| / max |x_replay| after k FP32 iterations
+COUNT_SLACK = 2        # iterations to 1e-4: FP32 rounding of the dot partners only
+
+
+@pytest.fixture(scope="module")
+def replay(tmp_path_factory):
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("g++ not available")
+    so = str(tmp_path_factory.mktemp("bicg32") / "libbicgstab32_replay.so")
+    subprocess.run([gxx, "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
+                    os.path.join(HERE, "replay", "bicgstab32_replay.cpp"), "-o", so], check=True)
+    L = C.CDLL(so)
+    fp = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+    ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+    dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+    L.bicgstab32.restype = C.c_int
+    L.bicgstab32.argtypes = [C.c_int, ip, ip, fp, ip, fp, fp, C.c_int, C.c_double, dp]
+
+    def run(ia, ja, a, dg, b, itr_max, tol_rel):
+        x = np.zeros(len(dg), np.float32)
+        hist = np.zeros(itr_max + 1)
+        used = L.bicgstab32(len(dg), ia.astype(np.int32), ja.astype(np.int32), a.astype(np.float32),
+                            dg.astype(np.int32), x, b.astype(np.float32), itr_max, tol_rel, hist)
+        return x.astype(np.float64), used, hist
+    return run
+
+
+@pytest.fixture(scope="module")
+def problem():
+    fc = load_fcgpu()
+    ns, pe = cd_batch_sizes(64)
+    gen = fc.Context(0)
+    try:
+        pr = cd_batch_system(fc, gen, int(ns[PROBLEM]), float(pe[PROBLEM]), 42 + PROBLEM)
+    finally:
+        gen.close()
+    return pr
+
+
+def gpu_single(fc, ctx, pr, itr_max, inner_tol, tol_rel):
+    ia, ja, dg, a, b, _ = pr
+    ctx.set_precision(fc.FC_PREC_MIXED, inner_tol, itr_max)
+    try:
+        x, _, info, st = ctx.csrsolve("bicgstab", ia, ja, a, dg, np.zeros(len(dg)), b, itr_max, 0.0, tol_rel)
+    finally:
+        ctx.set_precision(fc.FC_PREC_FP64)
+    return x, info
+
+
+def gpu_batched(fc, ctx, pr, itr_max, inner_tol, tol_rel):
+    ia, ja, dg, a, b, xyz = pr
+    ctx.set_precision(fc.FC_PREC_MIXED, inner_tol, itr_max)
+    B = fc.Batch(ctx)
+    try:
+        B.add(ia, ja, dg, xyz)
+        B.plan()
+        xs, infos, st = B.solve([a], [np.zeros(len(dg))], [b], itr_max, 0.0, tol_rel, raise_on_error=False)
+    finally:
+        B.close()
+        ctx.set_precision(fc.FC_PREC_FP64)
+    return xs[0], infos[0]
+
+
+@pytest.mark.parametrize("path", ["single", "batched"])
+def test_fp32_bicgstab_iterates_match_replay(ctx, fc, replay, problem, path):
+    ia, ja, dg, a, b, _ = problem
+    run = gpu_single if path == "single" else gpu_batched
+    for k in range(1, 7):
+        x_ref, used, _ = replay(ia, ja, a, dg, b, k, 1e-30)
+        assert used == k
+        # one refinement step whose inner solve stops after k iterations: x = dx_k
+        x, info = run(fc, ctx, problem, k, 1e-30, 1e-30)
+        assert info.itr_used == k, (path, k, info.itr_used)
+        err = np.abs(x - x_ref).max() / np.abs(x_ref).max()
+        assert err <= ITERATE_TOL, f"{path}: after {k} FP32 iterations max rel diff {err:.3e}"
+
+
+@pytest.mark.parametrize("path", ["single", "batched"])
+def test_fp32_bicgstab_inner_count_matches_replay(ctx, fc, replay, problem, path):
+    ia, ja, dg, a, b, _ = problem
+    _, used, hist = replay(ia, ja, a, dg, b, 1000, 1e-4)
+    run = gpu_single if path == "single" else gpu_batched
+    # outer tolerance 0.5: the refinement loop stops after the first inner solve
+    x, info = run(fc, ctx, problem, 1000, 1e-4, 0.5)
+    assert info.outer_iterations == 1, info.outer_iterations
+    assert abs(info.itr_used - used) <= COUNT_SLACK, f"{path}: GPU {info.itr_used} iterations, replay {used}"

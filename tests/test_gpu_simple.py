@@ -14,11 +14,11 @@ pytestmark = pytest.mark.gpu
 LID = 3  # patch index of ymax in the box generator (xmin, xmax, ymin, ymax, zmin, zmax)
 
 
-def setup_cavity(ctx, fc, key, nx, ny, nz, tets=False, sym=False, **kw):
+def setup_cavity(ctx, fc, key, nx, ny, nz, tets=False, sym=False, perturb=0.15, **kw):
     sides = ["wall"] * 6
     if sym:
         sides[4] = sides[5] = "symmetry"
-    m, a, oc = mesh_case(key, nx, ny, nz, tets=tets, sides=sides)
+    m, a, oc = mesh_case(key, nx, ny, nz, perturb=perturb, tets=tets, sides=sides)
     ctx.set_mesh(m)
     nC, nT = m.numCells, m.numTotal
     u = np.zeros(nT)

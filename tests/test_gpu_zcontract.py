@@ -1,0 +1,61 @@
+"""Parity at the sizes of the benchmark configurations, GPU against the
+oracle (the CPU restatement of the reference):
+
+  - pressure Poisson on the 128^3 perturbed hex mesh (2,097,152 cells): the
+    Laplacian coefficients bit for bit, the DIC factors
+    (linear_solvers.f90:439-445) bit for bit, and the ICCG solve to 1e-10
+    relative L1 from a zero start: the same iteration count and the field
+    within TOL_FIELD;
+  - the 64^3 lid-driven cavity (262,144 cells, Re 100, the cavity input's
+    settings) over 200 SIMPLE iterations: the residual history (resor of
+    U, V, W, p) and the final fields.
+
+The oracle's side takes about a minute on one core in all."""
+import numpy as np
+import pytest
+
+from gpu_cases import laplacian_system, mesh_case
+from test_gpu_simple import setup_cavity
+
+pytestmark = pytest.mark.gpu
+
+TOL_FIELD = 1e-8        # converged fields: max |x - x_oracle| <= TOL_FIELD * max |x_oracle|
+SIMPLE_RESOR_RTOL = 1e-6
+SIMPLE_FIELD_TOL = 1e-8
+
+
+def test_c2_128_laplacian_dic_and_iccg_match_oracle(ctx, oracle):
+    n = 128
+    m, _, oc = mesh_case("contract_c2", n, n, n)
+    ia, ja, a, dg, b = laplacian_system(oc, mask=0b1)
+    assert len(dg) == n ** 3 and len(ja) == 14_581_760
+    # the Laplacian assembled on the device, bit for bit
+    ctx.set_mesh(m)
+    ctx.laplacian(np.ones(m.numCells), np.zeros(m.numTotal), 0b1)
+    assert np.array_equal(ctx.field_get("a"), a)
+    d_gpu = ctx.precond_setup("dic", ia, ja, a, dg)
+    d_ref = oracle.dic_setup(ia, ja, a, dg)
+    assert np.array_equal(d_gpu, d_ref)
+    x, r0, info, st = ctx.csrsolve("iccg", ia, ja, a, dg, np.zeros(len(dg)), b, 20000, 0.0, 1e-10)
+    xo, r0o, info_o, st_o = oracle.solve("iccg", ia, ja, a, dg, np.zeros(len(dg)), b, 20000, 0.0, 1e-10)
+    assert st == 0 and st_o == 0
+    assert info.itr_used == int(info_o[0]), (info.itr_used, int(info_o[0]))
+    assert r0 == pytest.approx(r0o, rel=1e-12)
+    err = np.abs(x - xo).max() / np.abs(xo).max()
+    assert err <= TOL_FIELD, f"ICCG field max rel diff {err:.3e}"
+
+
+def test_c1_64_cavity_200_simple_iterations_track_oracle(ctx, fc):
+    n = 64
+    m, oc = setup_cavity(ctx, fc, "contract_c1", n, n, n, perturb=0.0)
+    res_g, res_o = [], []
+    for _ in range(200):
+        res_g.append(ctx.simple_iteration())
+        res_o.append(oc.simple_iteration()[1])
+    res_g, res_o = np.array(res_g), np.array(res_o)
+    rel = np.abs(res_g - res_o) / np.abs(res_o)
+    assert rel.max() <= SIMPLE_RESOR_RTOL, f"resor max rel diff {rel.max():.3e} at iteration {rel.max(1).argmax()}"
+    for k in ("u", "v", "w", "p"):
+        g, o = ctx.field_get(k), oc.get(k)
+        err = np.abs(g - o).max() / np.abs(o).max()
+        assert err <= SIMPLE_FIELD_TOL, f"{k}: max rel diff {err:.3e} after 200 SIMPLE iterations"

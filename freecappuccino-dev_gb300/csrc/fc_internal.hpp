@@ -71,12 +71,15 @@ enum { FC_OUT_RES0 = 0, FC_OUT_RESL, FC_OUT_FACTOR, FC_OUT_RESOR, FC_OUT_ITR, FC
 // device copy of a schedule-ordered sweep structure (fc_schedule.hpp)
 struct DevOrdered {
   int n = 0, nE = 0, ntiles = 0, nsteps = 0, nlev = 0, R = 4, K = 1, maxW = 0, max_tile_steps = 0;
+  size_t stage_area = 0;             // shared memory of the sweeps' stage buffers; K: buffers of an application
   int xmax = 4, pmax = 4;            // largest exchange / push block of a step
   int novf[2] = {0, 0}, nxv[2] = {0, 0};
   DVec<int> tile_step_ptr, step_ptr, tile_W, perm;
   DVec<int> srec[2], xv_ptr[2], push_ptr[2], push[2], slot[2], ucol;
   DVec<int> ovf_ptr[2], ovf_code[2], ovf_col[2], ovf_slot[2];
   DVec<int> lo_tslot, lo_ovf_tslot, dslot, p_ptr, p_col, p_slot;
+  DVec<int> wait_ptr[2], wait_tile[2], wait_need[2];  // producer waits of the exchange blocks
+  DVec<unsigned long long> prog;                      // progress word of every tile
   long long ring_entries = 0, pushed_entries = 0, cross_tile_entries = 0;
 };
 

@@ -132,6 +132,7 @@ __device__ bool residual_l1(const KArgs<T>& A, int& ph, double& l1out) {
 // exchange arrays to the sentinel, b (and x) gathered; ends with a barrier.
 template <class T>
 __device__ bool ord_prologue(const KArgs<T>& A, bool dilu, bool with_x) {
+  for (int t = vg_gt(A.C); t < A.O.ntiles; t += vg_G(A.C)) A.O.prog[t] = 0ull;
   ord_gather_values(A.C, A.O, A.V, A.S.a, A.nnz, dilu);
   ord_gather_vec(A.C, A.O, A.b, A.bo);
   if (with_x) ord_gather_vec(A.C, A.O, (const T*)A.x, A.xo);
@@ -625,12 +626,24 @@ static cudaError_t upload_vec(DVec<int>& d, const V& h) {
   return cudaMemcpy(d.p, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice);
 }
 
-// stage depth K of the ordered sweeps: the largest power of two the shared
-// memory allows (the sweep indexes its buffers with k & (K-1))
-static int ordered_stages(const DevOrdered& D) {
-  for (int K = FC_MAX_STAGES; K > 1; K >>= 1)
-    if (osweep_smem_bytes<double>(D.R, K, D.maxW, D.max_tile_steps, D.xmax, D.pmax) <= FC_SWEEP_SMEM) return K;
-  return 1;
+// the stage area of the ordered sweeps: the shared memory the fixed parts
+// leave (the sweep modes cut it into as many buffers as fit, at most
+// FC_MAX_STAGES); 0 when nothing is left
+static size_t ordered_stage_area(int R, int maxW, int max_tile_steps, int ntiles) {
+  const size_t fixed = osweep_fixed_bytes<double>(R, maxW, max_tile_steps, ntiles);
+  return fixed >= (size_t)FC_SWEEP_SMEM ? 0 : ((size_t)FC_SWEEP_SMEM - fixed) & ~(size_t)15;
+}
+
+// stage buffers of every sweep mode at width maxW (the widest tile); the
+// smallest over the modes is the depth the schedule is checked against
+static int ordered_min_stages(size_t area, int maxW, int xmax, int pmax) {
+  int kmin = FC_MAX_STAGES;
+  for (int m = OS_SETUP_DIC; m <= OS_GS; ++m) {
+    StageLayout L;
+    L.init_for<double>(maxW, xmax, pmax, m);
+    kmin = std::min(kmin, (size_t)L.bytes <= area ? stages_in(area, L.bytes) : 0);
+  }
+  return kmin;
 }
 
 // largest exchange and push blocks of a step (both directions)
@@ -643,20 +656,26 @@ static void ordered_blocks(const OrderedSweep& O, int& xmax, int& pmax) {
     }
 }
 
-// the sweep kernel's shared memory with two stage buffers fits the budget
+// every sweep mode gets at least two stage buffers in the shared memory
 static bool ordered_fits(const OrderedSweep& O) {
   int xmax, pmax;
   ordered_blocks(O, xmax, pmax);
-  return osweep_smem_bytes<double>(O.R, 2, O.maxW, O.max_tile_steps, xmax, pmax) <= FC_SWEEP_SMEM;
+  return ordered_min_stages(ordered_stage_area(O.R, O.maxW, O.max_tile_steps, O.ntiles), O.maxW, xmax, pmax) >= 2;
 }
 
 static int upload_ordered(fc_ctx* ctx, const OrderedSweep& O, DevOrdered& D) {
   D.n = O.n; D.nE = O.nE; D.ntiles = O.ntiles; D.nsteps = O.nsteps; D.nlev = O.nlev; D.R = O.R; D.maxW = O.maxW;
   D.max_tile_steps = O.max_tile_steps;
   ordered_blocks(O, D.xmax, D.pmax);
-  D.K = ordered_stages(D);
-  if (osweep_smem_bytes<double>(D.R, D.K, D.maxW, D.max_tile_steps, D.xmax, D.pmax) > FC_SWEEP_SMEM)
+  D.stage_area = ordered_stage_area(D.R, D.maxW, D.max_tile_steps, D.ntiles);
+  if (ordered_min_stages(D.stage_area, D.maxW, D.xmax, D.pmax) < 2)
     return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "sweep tiles too wide for shared memory");
+  {
+    // stages of the preconditioner application at the widest tile (sweep statistics)
+    StageLayout L;
+    L.init_for<double>(D.maxW, D.xmax, D.pmax, OS_FWD);
+    D.K = stages_in(D.stage_area, L.bytes);
+  }
   D.ring_entries = D.pushed_entries = D.cross_tile_entries = 0;
   FC_CUDA_TRY(ctx, upload_vec(D.tile_step_ptr, O.tile_step_ptr));
   FC_CUDA_TRY(ctx, upload_vec(D.step_ptr, O.step_ptr));
@@ -678,7 +697,12 @@ static int upload_ordered(fc_ctx* ctx, const OrderedSweep& O, DevOrdered& D) {
     FC_CUDA_TRY(ctx, upload_vec(D.ovf_code[d], H.ovf_code));
     FC_CUDA_TRY(ctx, upload_vec(D.ovf_col[d], H.ovf_col));
     FC_CUDA_TRY(ctx, upload_vec(D.ovf_slot[d], H.ovf_slot));
+    FC_CUDA_TRY(ctx, upload_vec(D.wait_ptr[d], H.wait_ptr));
+    FC_CUDA_TRY(ctx, upload_vec(D.wait_tile[d], H.wait_tile));
+    FC_CUDA_TRY(ctx, upload_vec(D.wait_need[d], H.wait_need));
   }
+  FC_CUDA_TRY(ctx, D.prog.alloc(std::max(1, O.ntiles)));
+  FC_CUDA_TRY(ctx, cudaMemset(D.prog.p, 0, D.prog.bytes()));
   // columns of the upper entries, 4 per row (Gauss-Seidel)
   std::vector<int> ucol((size_t)4 * O.nE, 0);
   for (int q = 0; q < O.n; ++q)
@@ -860,7 +884,8 @@ static CsrView<T> view_of(CsrSystem* s, const T* a) {
 static OrdView ord_view_of(CsrSystem* s) {
   DevOrdered& D = s->ord;
   OrdView O;
-  O.n = D.n; O.nE = D.nE; O.ntiles = D.ntiles; O.R = D.R; O.K = D.K; O.novf0 = D.novf[0]; O.novf1 = D.novf[1];
+  O.n = D.n; O.nE = D.nE; O.ntiles = D.ntiles; O.R = D.R; O.stage_area = (int)D.stage_area;
+  O.novf0 = D.novf[0]; O.novf1 = D.novf[1];
   O.nsteps = D.nsteps; O.maxW = D.maxW; O.xmax = D.xmax; O.pmax = D.pmax;
   O.tile_step_ptr = D.tile_step_ptr.p; O.step_ptr = D.step_ptr.p; O.tile_W = D.tile_W.p; O.perm = D.perm.p;
   for (int d = 0; d < 2; ++d) {
@@ -868,7 +893,9 @@ static OrdView ord_view_of(CsrSystem* s) {
     O.push[d] = D.push[d].p; O.slot[d] = D.slot[d].p;
     O.ovf_ptr[d] = D.ovf_ptr[d].p; O.ovf_code[d] = D.ovf_code[d].p; O.ovf_col[d] = D.ovf_col[d].p;
     O.ovf_slot[d] = D.ovf_slot[d].p;
+    O.wait_ptr[d] = D.wait_ptr[d].p; O.wait_tile[d] = D.wait_tile[d].p; O.wait_need[d] = D.wait_need[d].p;
   }
+  O.prog = D.prog.p;
   O.ucol = (const int4*)D.ucol.p;
   O.lo_tslot = D.lo_tslot.p; O.lo_ovf_tslot = D.lo_ovf_tslot.p; O.dslot = D.dslot.p;
   O.p_ptr = D.p_ptr.p; O.p_col = D.p_col.p; O.p_slot = D.p_slot.p;
@@ -889,7 +916,7 @@ template <class T>
 static int launch_coop(fc_ctx* ctx, CsrSystem* s, const void* fn, KArgs<T>& A, void** extra, int nextra,
                        int block = FC_SWEEP_BLOCK) {
   const DevOrdered& D = s->ord;
-  const size_t smem = osweep_smem_bytes<T>(D.R, D.K, D.maxW, D.max_tile_steps, D.xmax, D.pmax);
+  const size_t smem = osweep_smem_bytes<T>(D.R, D.stage_area, D.maxW, D.max_tile_steps, D.ntiles);
   if (smem > 48 * 1024)
     FC_CUDA_TRY(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int nb = 0;
@@ -1198,7 +1225,7 @@ static size_t batch_smem(const std::vector<BatchItem>& items) {
   size_t m = 0;
   for (const BatchItem& it : items) {
     const DevOrdered& D = it.s->ord;
-    m = std::max(m, osweep_smem_bytes<T>(D.R, D.K, D.maxW, D.max_tile_steps, D.xmax, D.pmax));
+    m = std::max(m, osweep_smem_bytes<T>(D.R, D.stage_area, D.maxW, D.max_tile_steps, D.ntiles));
   }
   return m;
 }

@@ -22,11 +22,18 @@
 //
 // Exchange: a value a row needs from another tile (or from more than R-1
 // steps back) is pushed by its producer into the consumer's slot of the
-// exchange array xv, whose slots start every sweep at a sentinel NaN.  The
-// staged copy is used when it already holds the value, else the slot is
-// polled (bounded) until the producer's store arrives; the consumer puts the
-// sentinel back after use.  Bulk copies read through L2, so staged data is
-// never an SM's stale L1 line.
+// exchange array xv, whose slots start every sweep at a sentinel NaN.  Every
+// tile publishes its progress (steps completed in the current sweep) in a
+// 64-bit word of global memory; a publisher thread, off the compute warps'
+// path, does the release store after each batch of completed steps.  The
+// stager issues a step's exchange-block copy only once every producer on the
+// step's wait list has published the steps the block needs, so the compute
+// warps read exchanged values from shared memory instead of paying an L2
+// round trip on every step; a consumer lags its producers by a few steps
+// and then runs at its own pace.  As a safety net the compute warps still
+// poll a slot (bounded) whose staged copy holds the sentinel, and they put
+// the sentinel back after use.  Bulk copies read through L2, so staged data
+// is never an SM's stale L1 line.
 #pragma once
 #include "fc_krylov.cuh"
 #include "fc_schedule.hpp"
@@ -58,7 +65,8 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
                "l"(src), "r"(bytes), "r"(smem_addr(mb))
                : "memory");
 }
-#define FC_MAX_STAGES 4
+#define FC_MAX_STAGES 16
+#define FC_SMEM_HDR (2 * FC_MAX_STAGES * 8)  // full and empty mbarriers at the start of the dynamic area
 #define FC_MBAR_SPIN_LIMIT (1u << 22)
 __device__ __forceinline__ void mbar_arrive(unsigned long long* mb) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(mb)) : "memory");
@@ -78,6 +86,27 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* mb, unsigned parit
 __device__ __forceinline__ void bar_compute(int nthreads) {
   asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
 }
+// progress words: release/acquire at GPU scope (tile to tile) and the
+// block-local step counter at CTA scope (compute warps to the publisher)
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ int ld_acquire_cta_s32(const int* p) {
+  int v;
+  asm volatile("ld.acquire.cta.shared::cta.s32 %0, [%1];" : "=r"(v) : "r"(smem_addr(p)) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_cta_s32(int* p, int v) {
+  asm volatile("st.release.cta.shared::cta.s32 [%0], %1;" ::"r"(smem_addr(p)), "r"(v) : "memory");
+}
+// generic-proxy writes observed by this thread (the producers' pushes,
+// acquired through their progress words) before the bulk copies it issues next
+__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
 
 // record strides (elements of T) of the per-solve row records
 template <class T> struct Rec { static constexpr int V = sizeof(T) == 8 ? 6 : 8; };
@@ -85,7 +114,8 @@ template <class T> struct Rec { static constexpr int V = sizeof(T) == 8 ? 6 : 8;
 // ------------------------------------------------------------------ views
 // device copy of an OrderedSweep (fc_schedule.hpp)
 struct OrdView {
-  int n, nE, ntiles, R, K, novf0, novf1, nsteps, maxW, xmax, pmax;
+  int n, nE, ntiles, R, novf0, novf1, nsteps, maxW, xmax, pmax;
+  int stage_area;                        // bytes of the stage area (multiple of 16)
   const int* __restrict__ tile_step_ptr;
   const int* __restrict__ step_ptr;
   const int* __restrict__ tile_W;
@@ -106,6 +136,10 @@ struct OrdView {
   const int* __restrict__ p_ptr;
   const int* __restrict__ p_col;
   const int* __restrict__ p_slot;
+  const int* __restrict__ wait_ptr[2];   // producer waits of each step's exchange block
+  const int* __restrict__ wait_tile[2];
+  const int* __restrict__ wait_need[2];
+  unsigned long long* prog;              // [ntiles] (sweep << 32) | steps completed
 };
 
 // per-solve values in the new numbering (gathered by the kernel from the
@@ -123,58 +157,89 @@ struct OrdVals {
   T* xv[2];    // exchange arrays (per-step blocks)
 };
 
+// ------------------------------------------------------------------ modes
+enum { OS_SETUP_DIC = 0, OS_SETUP_DILU, OS_FWD, OS_BWD, OS_BWD_DOT, OS_GS };
+
 // ----------------------------------------------------------- staging area
 // One stage buffer: the step's row records, coefficient records, setup
 // records (a_ii and transposes), the Gauss-Seidel upper columns and
 // coefficients, the q and e windows (rows widened to 16-byte bounds) and
-// the exchange and push blocks.
+// the exchange and push blocks.  init() lays out every area (the size the
+// host reserves per stage); init_for() only the areas one sweep mode reads,
+// so that the preconditioner applications, which need about 40% of a full
+// buffer, fit more stages into the same shared memory.
 struct StageLayout {
   int W, Wp;
   int oS, oV, oX2, oU, oV2, oQ, oE, oXV, oP, bytes;
   template <class T>
-  __host__ __device__ void init(int w, int xmax, int pmax) {
+  __host__ __device__ void init(int w, int xmax, int pmax) { init_for<T>(w, xmax, pmax, -1); }
+  template <class T>
+  __host__ __device__ void init_for(int w, int xmax, int pmax, int mode) {
+    const bool all = mode < 0;
+    const bool setup = all || mode == OS_SETUP_DIC || mode == OS_SETUP_DILU;
+    const bool gs = all || mode == OS_GS;
+    const bool kq = all || !(mode == OS_SETUP_DIC || mode == OS_SETUP_DILU);
+    const bool ke = all || mode == OS_BWD_DOT || mode == OS_GS;
     W = w;
     Wp = ((w + 3) & ~3) + 8;
     int o = 0;
-    auto take = [&](int b) { const int r = o; o += (b + 15) & ~15; return r; };
-    oS = take(16 * W);
-    oV = take((int)sizeof(T) * Rec<T>::V * W);
-    oX2 = take((int)sizeof(T) * Rec<T>::V * W);
-    oU = take(16 * W);
-    oV2 = take((int)sizeof(T) * Rec<T>::V * W);
-    oQ = take((int)sizeof(T) * Wp);
-    oE = take((int)sizeof(T) * Wp);
-    oXV = take((int)sizeof(T) * xmax);
-    oP = take(4 * pmax);
+    auto take = [&](bool used, int b) { const int r = o; if (used) o += (b + 15) & ~15; return r; };
+    oS = take(true, 16 * W);
+    oV = take(true, (int)sizeof(T) * Rec<T>::V * W);
+    oX2 = take(setup || gs, (int)sizeof(T) * Rec<T>::V * W);
+    oU = take(gs, 16 * W);
+    oV2 = take(gs, (int)sizeof(T) * Rec<T>::V * W);
+    oQ = take(kq, (int)sizeof(T) * Wp);
+    oE = take(ke, (int)sizeof(T) * Wp);
+    oXV = take(true, (int)sizeof(T) * xmax);
+    oP = take(true, 4 * pmax);
     bytes = o;
   }
 };
 
-// dynamic shared memory of an ordered-sweep kernel: 2K mbarriers, ring, K
-// stage buffers, the tile's step tables (rows, exchange and push offsets of
-// both directions) and the abort flag
+// stage buffers of one mode within a stage area of `area` bytes: the largest
+// power of two (at most FC_MAX_STAGES) whose buffers fit
+__host__ __device__ inline int stages_in(size_t area, int buffer_bytes) {
+  int K = 1;
+  while (2 * K <= FC_MAX_STAGES && (size_t)(2 * K) * (size_t)buffer_bytes <= area) K *= 2;
+  return K;
+}
+
+// dynamic shared memory of an ordered-sweep kernel: 2 FC_MAX_STAGES
+// mbarriers, ring, the stage area (cut by every sweep mode into its own
+// buffers), the tile's step tables (rows, exchange and push offsets of both
+// directions), the last progress seen of every producer tile, the abort flag
+// and the completed-steps counter
 template <class T>
-inline size_t osweep_smem_bytes(int R, int K, int maxW, int max_tile_steps, int xmax, int pmax) {
-  StageLayout L;
-  L.init<T>(maxW, xmax, pmax);
+inline size_t osweep_fixed_bytes(int R, int maxW, int max_tile_steps, int ntiles) {
   size_t ring = ((size_t)R * maxW * sizeof(T) + 15) & ~(size_t)15;
   size_t tab = ((size_t)5 * (max_tile_steps + 1) * 4 + 15) & ~(size_t)15;
-  return 64 + ring + (size_t)K * L.bytes + tab + 16;
+  size_t seen = (size_t)8 * (ntiles > 0 ? ntiles : 1);
+  return FC_SMEM_HDR + ring + tab + seen + 16;
+}
+template <class T>
+inline size_t osweep_smem_bytes(int R, size_t stage_area, int maxW, int max_tile_steps, int ntiles) {
+  return osweep_fixed_bytes<T>(R, maxW, max_tile_steps, ntiles) + stage_area;
 }
 
 struct OsCtx {
   unsigned long long* full;   // [FC_MAX_STAGES]
   unsigned long long* empty;  // [FC_MAX_STAGES]
   unsigned char* ring;
-  unsigned char* stage;
+  unsigned char* stage;       // the stage area, cut by each sweep mode into its buffers
+  size_t stage_area;
   int* sp;                    // [ns+1] first row of each local step (ascending levels)
   int* xp[2];                 // [ns+1] exchange block offsets per direction
   int* pp[2];                 // [ns+1] push block offsets per direction
+  unsigned long long* seen;   // [ntiles] last progress word read of each producer tile (stager)
   int* abort_flag;
+  int* done;                  // steps completed by this block over all its sweeps
   // stage buffer b: bit b of `parity` = parity of its next fill/completion,
   // bit b of `used` = it has been filled before (registers, no runtime-
   // indexed arrays, so the context never goes to local memory)
   unsigned parity, used;
+  unsigned seq;               // sweeps begun by this block (the high word of its progress)
+  int done_base;              // `done` at the start of the current sweep
   StageLayout L;
 };
 
@@ -186,11 +251,12 @@ __device__ __forceinline__ OsCtx osweep_ctx(const OrdView& O, unsigned char* sme
   // carve with this tile's width; the host sized the area for the widest
   X.full = (unsigned long long*)smem;
   X.empty = X.full + FC_MAX_STAGES;
-  size_t off = 64;
+  size_t off = FC_SMEM_HDR;
   X.ring = smem + off;
   off += ((size_t)O.R * W * sizeof(T) + 15) & ~(size_t)15;
   X.stage = smem + off;
-  off += (size_t)O.K * X.L.bytes;
+  X.stage_area = (size_t)O.stage_area;
+  off += X.stage_area;
   const int ns = t < O.ntiles ? __ldg(O.tile_step_ptr + t + 1) - __ldg(O.tile_step_ptr + t) : 0;
   int* tab = (int*)(smem + off);
   X.sp = tab;
@@ -199,9 +265,15 @@ __device__ __forceinline__ OsCtx osweep_ctx(const OrdView& O, unsigned char* sme
   X.pp[0] = tab + 3 * (ns + 1);
   X.pp[1] = tab + 4 * (ns + 1);
   off += ((size_t)5 * (ns + 1) * 4 + 15) & ~(size_t)15;
+  X.seen = (unsigned long long*)(smem + off);
+  off += (size_t)8 * (O.ntiles > 0 ? O.ntiles : 1);
   X.abort_flag = (int*)(smem + off);
+  X.done = X.abort_flag + 1;
   X.parity = 0;
   X.used = 0;
+  X.seq = 0;
+  X.done_base = 0;
+  for (int k = threadIdx.x; k < O.ntiles; k += blockDim.x) X.seen[k] = 0ull;
   if (t < O.ntiles) {
     const int s0 = __ldg(O.tile_step_ptr + t);
     for (int k = threadIdx.x; k <= ns; k += blockDim.x) {
@@ -214,6 +286,7 @@ __device__ __forceinline__ OsCtx osweep_ctx(const OrdView& O, unsigned char* sme
   }
   if (threadIdx.x == 0) {
     *X.abort_flag = 0;
+    *X.done = 0;
     for (int b = 0; b < FC_MAX_STAGES; ++b) {
       mbar_init(X.full + b, 1);
       mbar_init(X.empty + b, 1);
@@ -224,8 +297,6 @@ __device__ __forceinline__ OsCtx osweep_ctx(const OrdView& O, unsigned char* sme
   return X;
 }
 
-// ------------------------------------------------------------------ modes
-enum { OS_SETUP_DIC = 0, OS_SETUP_DILU, OS_FWD, OS_BWD, OS_BWD_DOT, OS_GS };
 
 // Row sources of a sweep.  q: the right-hand side (forward, backward,
 // Gauss-Seidel), e: an extra row value (the dot partner of OS_BWD_DOT, the
@@ -270,14 +341,23 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
   constexpr bool kGS = MODE == OS_GS;
   constexpr int VR = Rec<T>::V;
   if (tr) tr->sweep();
+  const unsigned seq = ++X.seq;
   const int t = vg_bid(C);
   if (t >= O.ntiles) return true;
-  const int ns = __ldg(O.tile_step_ptr + t + 1) - __ldg(O.tile_step_ptr + t);
-  const StageLayout& L = X.L;
-  const int K = O.K, R = O.R, W = L.W;
+  const int s0 = __ldg(O.tile_step_ptr + t);
+  const int ns = __ldg(O.tile_step_ptr + t + 1) - s0;
+  const int done_base = X.done_base;
+  X.done_base += ns;
+  // the areas this mode reads, as many stage buffers as the area holds
+  StageLayout L;
+  L.template init_for<T>(X.L.W, O.xmax, O.pmax, MODE);
+  const int K = stages_in(X.stage_area, L.bytes), R = O.R, W = L.W;
   const int nct = (int)blockDim.x - 32;  // threads before the staging warp
   // compute threads of this tile: whole warps covering its widest step
   const int ncg = min(nct, (W + 31) & ~31);
+  // the publisher of the tile's progress: an idle compute warp's first
+  // thread, else the second lane of the staging warp
+  const int pubt = ncg < nct ? ncg : nct + 1;
   T* ring = (T*)X.ring;
   T* xv = V.xv[dirn];
   const int* sp = X.sp;
@@ -285,10 +365,47 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
   const int* pp = X.pp[dirn];
   auto step_of = [&](int k) { return dirn ? ns - 1 - k : k; };
 
+  if ((int)threadIdx.x == pubt) {
+    // --------------------------------------------------------- publisher
+    // release the tile's completed steps of this sweep (the compute warps'
+    // value stores happen before, through their barrier and the CTA-scope
+    // release of `done`); batches whatever completed during the last store
+    const unsigned long long hi = (unsigned long long)seq << 32;
+    int pub = 0;
+    unsigned spins = 0;
+    while (pub < ns) {
+      const int d = ld_acquire_cta_s32(X.done) - done_base;
+      if (d > pub) {
+        st_release_u64(O.prog + t, hi | (unsigned)d);
+        pub = d;
+        spins = 0;
+      } else {
+        if (*((volatile int*)X.abort_flag) || ++spins > FC_SPIN_LIMIT) break;
+        __nanosleep(20);
+      }
+    }
+  }
   if ((int)threadIdx.x >= nct) {
     // ------------------------------------------------------------ stager
     if (threadIdx.x == (unsigned)nct) {
       bool ok = true;
+      // every producer on step gs's wait list has published the steps the
+      // exchange block needs (progress words of other sweeps are smaller)
+      auto producers_ready = [&](int gs) -> bool {
+        const int w0 = __ldg(O.wait_ptr[dirn] + gs), w1 = __ldg(O.wait_ptr[dirn] + gs + 1);
+        for (int w = w0; w < w1; ++w) {
+          const int P = __ldg(O.wait_tile[dirn] + w);
+          const unsigned long long target = ((unsigned long long)seq << 32) | (unsigned)__ldg(O.wait_need[dirn] + w);
+          if (X.seen[P] >= target) continue;
+          unsigned spins = 0;
+          unsigned long long v;
+          while ((v = ld_acquire_u64(O.prog + P)) < target)
+            if (++spins > FC_SPIN_LIMIT || *((volatile int*)C.status) != 0 || *((volatile int*)X.abort_flag))
+              return false;
+          X.seen[P] = v;
+        }
+        return true;
+      };
       for (int k = 0; k < ns && ok; ++k) {
         if (*((volatile int*)X.abort_flag)) break;
         const int b = k & (K - 1);
@@ -325,10 +442,21 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
         }
         if (kQ) bulk_g2s(B + L.oQ, io.q + b0, (unsigned)sizeof(T) * nw, mb);
         if (kE) bulk_g2s(B + L.oE, io.e + b0, (unsigned)sizeof(T) * nw, mb);
-        if (nx) bulk_g2s(B + L.oXV, xv + x0, (unsigned)sizeof(T) * nx, mb);
         if (np) bulk_g2s(B + L.oP, O.push[dirn] + p0, 4u * np, mb);
         X.parity ^= 1u << b;
         X.used |= 1u << b;
+        if (nx) {
+          // the exchange block last: once its producers have published
+          if (!producers_ready(s0 + ls)) {
+            // the compute warps run out of their own bounded wait on this
+            // buffer and raise the abort flag
+            atomicCAS(C.status, 0, FC_ERR_TIMEOUT);
+            ok = false;
+            break;
+          }
+          fence_proxy_async_global();
+          bulk_g2s(B + L.oXV, xv + x0, (unsigned)sizeof(T) * nx, mb);
+        }
       }
     }
   } else if ((int)threadIdx.x < ncg) {
@@ -488,7 +616,10 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
         for (int mm = 0; mm < np; ++mm) xv[PS[poff + mm]] = val;
       }
       bar_compute(ncg);
-      if (threadIdx.x == 0) mbar_arrive(X.empty + b);
+      if (threadIdx.x == 0) {
+        mbar_arrive(X.empty + b);
+        st_release_cta_s32(X.done, done_base + k + 1);
+      }
       X.parity ^= 1u << b;
       X.used |= 1u << b;
       if (*((volatile int*)X.abort_flag)) break;

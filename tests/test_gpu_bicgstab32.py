@@ -8,7 +8,9 @@ convection-diffusion configuration (72^3 cells, cell Peclet 0.55):
     (fc_csrsolve in FC_PREC_MIXED with the inner solve capped at k) and
     batched (fc_batch_solve), agree with the replay's to FP32 rounding;
   - the first inner solve to the relative tolerance 1e-4 takes the
-    replay's iteration count, single and batched."""
+    replay's iteration count, single and batched;
+  - the whole FP64 refinement to 1e-6 takes the replay's refinement steps
+    and inner iterations."""
 import ctypes as C
 import os
 import shutil
@@ -111,3 +113,52 @@ def test_fp32_bicgstab_inner_count_matches_replay(ctx, fc, replay, problem, path
     x, info = run(fc, ctx, problem, 1000, 1e-4, 0.5)
     assert info.outer_iterations == 1, info.outer_iterations
     assert abs(info.itr_used - used) <= COUNT_SLACK, f"{path}: GPU {info.itr_used} iterations, replay {used}"
+
+
+def replay_refinement(replay, pr, inner_tol, tol_rel, itr_max=4000, max_outer=64):
+    """The mixed solve's FP64 refinement around the FP32 replay: r = b - A x
+    in FP64, inner FP32 solve of A dx = (float) r from dx = 0 to inner_tol,
+    x += dx, until L1(r) / L1(r_0) < tol_rel.  Returns (inner counts, x)."""
+    import scipy.sparse as sp
+    ia, ja, dg, a, b, _ = pr
+    n = len(dg)
+    A = sp.csr_matrix((a, ja - 1, ia - 1), shape=(n, n))
+    x = np.zeros(n)
+    counts, res0 = [], None
+    for _ in range(max_outer):
+        r = b - A @ x
+        resl = np.abs(r).sum()
+        if res0 is None:
+            res0 = resl
+        elif resl / (res0 + 1e-20) < tol_rel:
+            break
+        dx, used, _ = replay(ia, ja, a, dg, r, itr_max, inner_tol)
+        counts.append(used)
+        x += dx
+    return counts, x
+
+
+@pytest.mark.parametrize("path", ["single", "batched"])
+def test_fp32_bicgstab_refinement_matches_replay(ctx, fc, replay, problem, path):
+    """The whole refinement to 1e-6 (inner solves to 1e-4): the same number
+    of refinement steps and inner iterations as the replay (the device's FP32
+    path follows its own algorithm)."""
+    counts, x_ref = replay_refinement(replay, problem, 1e-4, 1e-6)
+    ia, ja, dg, a, b, _ = problem
+    ctx.set_precision(fc.FC_PREC_MIXED, 1e-4, 0)
+    try:
+        if path == "single":
+            x, _, info, st = ctx.csrsolve("bicgstab", ia, ja, a, dg, np.zeros(len(dg)), b, 4000, 0.0, 1e-6)
+        else:
+            B = fc.Batch(ctx)
+            B.add(ia, ja, dg, problem[5])
+            B.plan()
+            xs, infos, st = B.solve([a], [np.zeros(len(dg))], [b], 4000, 0.0, 1e-6)
+            B.close()
+            x, info = xs[0], infos[0]
+    finally:
+        ctx.set_precision(fc.FC_PREC_FP64)
+    assert info.status == 0
+    assert info.outer_iterations == len(counts), (path, info.outer_iterations, counts)
+    assert abs(info.itr_used - sum(counts)) <= COUNT_SLACK * len(counts), (path, info.itr_used, counts)
+    assert np.abs(x - x_ref).max() <= 1e-5 * np.abs(x_ref).max()

@@ -53,9 +53,12 @@ def test_c1_64_cavity_200_simple_iterations_track_oracle(ctx, fc):
         res_g.append(ctx.simple_iteration())
         res_o.append(oc.simple_iteration()[1])
     res_g, res_o = np.array(res_g), np.array(res_o)
-    rel = np.abs(res_g - res_o) / np.abs(res_o)
-    assert rel.max() <= SIMPLE_RESOR_RTOL, f"resor max rel diff {rel.max():.3e} at iteration {rel.max(1).argmax()}"
-    for k in ("u", "v", "w", "p"):
-        g, o = ctx.field_get(k), oc.get(k)
-        err = np.abs(g - o).max() / np.abs(o).max()
-        assert err <= SIMPLE_FIELD_TOL, f"{k}: max rel diff {err:.3e} after 200 SIMPLE iterations"
+    # resor entries that are exactly zero on the oracle's side (W in the
+    # first iterations of this 2D-symmetric start) must be tiny on the GPU's
+    scale = np.maximum(np.abs(res_o), 1e-30)
+    rel = np.where(res_o != 0, np.abs(res_g - res_o) / scale, np.abs(res_g))
+    errs = {k: np.abs(ctx.field_get(k) - oc.get(k)).max() / np.abs(oc.get(k)).max() for k in ("u", "v", "w", "p")}
+    msg = f"resor max rel diff {rel.max():.3e} (iteration {rel.max(1).argmax()}); fields {errs}"
+    assert rel.max() <= SIMPLE_RESOR_RTOL, msg
+    for k, err in errs.items():
+        assert err <= SIMPLE_FIELD_TOL, f"{k}: " + msg

@@ -51,6 +51,10 @@ struct KArgs {
   double tol_abs;
   double tol_rel;
   int skip_setup;
+  // > 0 (FP32 inner solves of the mixed modes): stop once the L1 residual
+  // has gone stall_window iterations without falling below half of its
+  // last recorded value; the FP64 refinement around it decides convergence
+  int stall_window;
   unsigned long long* trace;  // traced instantiation only: phase cycles and step stamps
   int trace_cap;              // step stamps kept per tile and sweep
 };
@@ -273,6 +277,8 @@ __device__ __forceinline__ void bicgstab_body(const KArgs<T>& A) {
   double betn = bb[0];
   double alf = 1.0, beto = 1.0, gam = 1.0, resl = 0.0, factor = 0.0, resor = 0.0;
   int itr_used = 0;
+  double stall_ref = res0;
+  int stall_at = 0;
   for (int l = 1; l <= A.itr_max; ++l) {
     const double bet = betn;
     const double om = bet * gam / (alf * beto + FC_SMALL);
@@ -326,6 +332,10 @@ __device__ __forceinline__ void bicgstab_body(const KArgs<T>& A) {
     const double rsm = resl / (res0 + FC_SMALL);
     if (!(rsm == rsm)) { if (gt == 0) atomicCAS(A.C.status, 0, FC_ERR_NAN); break; }
     if (rsm < A.tol_rel || resl < A.tol_abs) break;
+    if (A.stall_window > 0) {
+      if (resl < 0.5 * stall_ref) { stall_ref = resl; stall_at = l; }
+      else if (l - stall_at >= A.stall_window) break;
+    }
   }
   ord_scatter_vec(A.C, A.O, (const T*)x, A.x);
   write_out(A, res0, resl, factor, resor, itr_used, 0);
@@ -570,6 +580,10 @@ __global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1)
 #define FC_SWEEP_ROW_US 0.001
 #define FC_SWEEP_HOP_US 1.5
 #define FC_RING 4                    // ring depth (steps) of the ordered sweeps
+// FP32 inner BiCGStab of the mixed modes: iterations without halving the
+// residual after which the inner solve ends (the longest such run in the
+// converging solves of the batched convection-diffusion set is 22)
+#define FC_INNER_STALL_WINDOW 32
 #define FC_SWEEP_SMEM (200 * 1024)   // dynamic shared memory budget of a sweep kernel
 
 bool is_device_ptr(const void* p) {
@@ -951,6 +965,7 @@ static KArgs<T> make_args(CsrSystem* s, const T* a, T* x, const T* b, T* r, T* r
   A.x = x; A.b = b; A.xo = st.xo.p; A.bo = st.bo.p;
   A.r = r; A.r0 = r0; A.p = p; A.u = u; A.z = z; A.v = v; A.d = d; A.w = w;
   A.itr_max = itr_max; A.tol_abs = tol_abs; A.tol_rel = tol_rel; A.skip_setup = 0;
+  A.stall_window = 0;
   A.trace = nullptr;
   A.trace_cap = 0;
   return A;
@@ -1074,6 +1089,7 @@ static int solve_mixed(fc_ctx* ctx, CsrSystem* s, const std::string& solver, con
                                       s->fz.p, s->fv.p, s->fd.p, s->fw.p, std::min(inner_itmax, itr_max - total_itr),
                                       0.0, inner_tol);
     F.skip_setup = outer > 0 ? 1 : 0;
+    if (solver == "bicgstab") F.stall_window = FC_INNER_STALL_WINDOW;
     const void* fn = solver == "iccg" ? (const void*)k_iccg<float>
                      : solver == "bicgstab" ? (const void*)k_bicgstab<float> : (const void*)k_dpcg<float>;
     if ((st = launch_coop(ctx, s, fn, F, nullptr, 0, solver == "dpcg" ? FC_BLOCK : FC_SWEEP_BLOCK))) return st;
@@ -1291,6 +1307,7 @@ int batch_solve(fc_ctx* ctx, BatchDev*& dev, std::vector<BatchItem>& items, cons
       batch_ctl(hr[p], B, p, base[p], nbk[p]);
       hf[p] = make_args<float>(s, s->a32.p, s->fx.p, s->fr0.p, s->fr.p, s->fy.p, s->fp.p, s->fu.p, s->fz.p, s->fv.p,
                                s->fd.p, s->fw.p, 0, 0.0, inner_tol);
+      hf[p].stall_window = FC_INNER_STALL_WINDOW;
       batch_ctl(hf[p], B, p, base[p], nbk[p]);
       hm[p] = BatchMix{s->fx.p, s->fr0.p, s->a32.p, s->nnz, 0};
     }

@@ -7,11 +7,14 @@
 // r -= g u); the triangular sweeps and the row products accumulate with FMA
 // in the row's entry order, as the device does.  Test infrastructure only.
 //
-// bicgstab32(n, ia, ja, a, diag, x, b, itr_max, tol_rel, hist): 1-based CSR
-// (ia(n+1), ja(nnz), diag(n)); a (FP32 values), b (FP32 right-hand side),
-// x (FP32, in: start, out: solution); stops on resl/(res0+small) < tol_rel
-// or after itr_max iterations; hist[l-1] receives resl after iteration l,
-// hist[itr_max] receives res0.  Returns the iterations used.
+// bicgstab32(n, ia, ja, a, diag, x, b, itr_max, tol_rel, stall_window,
+// hist): 1-based CSR (ia(n+1), ja(nnz), diag(n)); a (FP32 values), b (FP32
+// right-hand side), x (FP32, in: start, out: solution); stops on
+// resl/(res0+small) < tol_rel, after itr_max iterations, or (stall_window
+// > 0, the device's rule for the inner solves) once resl has gone
+// stall_window iterations without falling below half of its last recorded
+// value; hist[l-1] receives resl after iteration l, hist[itr_max] receives
+// res0.  Returns the iterations used.
 #include <cmath>
 #include <vector>
 
@@ -21,7 +24,7 @@ const float kSmallF = 1e-20f;
 }
 
 extern "C" int bicgstab32(int n, const int* ia, const int* ja, const float* a, const int* diag, float* x,
-                          const float* b, int itr_max, double tol_rel, double* hist) {
+                          const float* b, int itr_max, double tol_rel, int stall_window, double* hist) {
   auto A = [&](int k) { return a[k - 1]; };
   auto JA = [&](int k) { return ja[k - 1]; };
   std::vector<float> res(n + 1), reso(n + 1), pk(n + 1, 0.f), uk(n + 1, 0.f), zk(n + 1, 0.f), vk(n + 1, 0.f),
@@ -71,6 +74,8 @@ extern "C" int bicgstab32(int n, const int* ia, const int* ja, const float* a, c
   for (int i = 1; i <= n; ++i) { reso[i] = res[i]; betn += (double)res[i] * (double)res[i]; }
   double alf = 1.0, beto = 1.0, gam = 1.0;
   int used = 0;
+  double stall_ref = res0;
+  int stall_at = 0;
   for (int l = 1; l <= itr_max; ++l) {
     const double bet = betn;
     const double om = bet * gam / (alf * beto + kSmall);
@@ -107,6 +112,10 @@ extern "C" int bicgstab32(int n, const int* ia, const int* ja, const float* a, c
     hist[l - 1] = resl;
     used = l;
     if (resl / (res0 + kSmall) < tol_rel) break;
+    if (stall_window > 0) {
+      if (resl < 0.5 * stall_ref) { stall_ref = resl; stall_at = l; }
+      else if (l - stall_at >= stall_window) break;
+    }
   }
   return used;
 }

@@ -94,8 +94,12 @@ __global__ void k_lsq_matrix(MeshView M, double* __restrict__ D) {
 
 // grad_lsq (:782-893) and grad_lsq_dm (:1334-1486); the y row of the
 // cofactor product and the boundary weight of the dm variant (xf at the
-// boundary-face counter, :1459) are kept as the reference has them
-template <bool DM_WEIGHTED>
+// boundary-face counter, :1459) are kept as the reference has them.
+// EXACT (FC_GRAD_LSQ_EXACT / FC_GRAD_LSQ_DM_EXACT, no reference
+// counterpart): the y row of the adjugate of the symmetric normal matrix,
+// -b1 D2 + b2 D4 - b3 D8, and the dm boundary weight at the face's own
+// centre, so that the gradient of a linear field is exact
+template <bool DM_WEIGHTED, bool EXACT>
 __global__ void k_grad_lsq(MeshView M, const double* __restrict__ D, const double* __restrict__ phi,
                            double* __restrict__ g) {
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
@@ -120,7 +124,8 @@ __global__ void k_grad_lsq(MeshView M, const double* __restrict__ D, const doubl
         const double ddx = DS(M.xf[f], M.xc[p]), ddy = DS(M.yf[f], M.yc[p]), ddz = DS(M.zf[f], M.zc[p]);
         double Dx, Dy, Dz;
         if (DM_WEIGHTED) {
-          const double qx = DS(M.xf[bi], M.xc[p]), qy = DS(M.yf[bi], M.yc[p]), qz = DS(M.zf[bi], M.zc[p]);
+          const int fw = EXACT ? f : bi;
+          const double qx = DS(M.xf[fw], M.xc[p]), qy = DS(M.yf[fw], M.yc[p]), qz = DS(M.zf[fw], M.zc[p]);
           const double w = DD(delta, DA(DA(DM(qx, qx), DM(qy, qy)), DM(qz, qz)));
           Dx = DM(w, ddx); Dy = DM(w, ddy); Dz = DM(w, ddz);
         } else {
@@ -131,7 +136,8 @@ __global__ void k_grad_lsq(MeshView M, const double* __restrict__ D, const doubl
     }
     const size_t n = M.nC;
     g[c] = DA(DS(DM(b1, D[0 * n + c]), DM(b2, D[1 * n + c])), DM(b3, D[2 * n + c]));
-    g[M.nT + c] = DS(DS(DM(b1, D[3 * n + c]), DM(b2, D[4 * n + c])), DM(b3, D[5 * n + c]));
+    if (EXACT) g[M.nT + c] = DS(DS(DM(b2, D[3 * n + c]), DM(b1, D[1 * n + c])), DM(b3, D[7 * n + c]));
+    else g[M.nT + c] = DS(DS(DM(b1, D[3 * n + c]), DM(b2, D[4 * n + c])), DM(b3, D[5 * n + c]));
     g[2 * (size_t)M.nT + c] = DA(DS(DM(b1, D[6 * n + c]), DM(b2, D[7 * n + c])), DM(b3, D[8 * n + c]));
   }
 }
@@ -214,16 +220,24 @@ int fv_grad(fc_ctx* ctx, int scheme, const double* phi, double* g) {
   if (scheme == FC_GRAD_GAUSS) {
     k_grad_gauss<<<grid_for(M.nC), 256, 0, ctx->stream>>>(M, phi, g);
     ctx->kernel_launches++;
-  } else if (scheme == FC_GRAD_LSQ || scheme == FC_GRAD_LSQ_DM) {
-    if (F.dmat_scheme != scheme) {
+  } else if (scheme == FC_GRAD_LSQ || scheme == FC_GRAD_LSQ_DM || scheme == FC_GRAD_LSQ_EXACT ||
+             scheme == FC_GRAD_LSQ_DM_EXACT) {
+    // the matrix of create_matrix_lsq (LSQ, LSQ exact) or _dm (the dm variants)
+    const bool dm = scheme == FC_GRAD_LSQ_DM || scheme == FC_GRAD_LSQ_DM_EXACT;
+    const int mat = dm ? FC_GRAD_LSQ_DM : FC_GRAD_LSQ;
+    if (F.dmat_scheme != mat) {
       FC_CUDA_TRY(ctx, F.dmat.alloc((size_t)9 * M.nC));
-      if (scheme == FC_GRAD_LSQ) k_lsq_matrix<false><<<grid_for(M.nC), 256, 0, ctx->stream>>>(M, F.dmat.p);
+      if (!dm) k_lsq_matrix<false><<<grid_for(M.nC), 256, 0, ctx->stream>>>(M, F.dmat.p);
       else k_lsq_matrix<true><<<grid_for(M.nC), 256, 0, ctx->stream>>>(M, F.dmat.p);
       ctx->kernel_launches++;
-      F.dmat_scheme = scheme;
+      F.dmat_scheme = mat;
     }
-    if (scheme == FC_GRAD_LSQ) k_grad_lsq<false><<<grid_for(M.nC), 256, 0, ctx->stream>>>(M, F.dmat.p, phi, g);
-    else k_grad_lsq<true><<<grid_for(M.nC), 256, 0, ctx->stream>>>(M, F.dmat.p, phi, g);
+    if (scheme == FC_GRAD_LSQ) k_grad_lsq<false, false><<<grid_for(M.nC), 256, 0, ctx->stream>>>(M, F.dmat.p, phi, g);
+    else if (scheme == FC_GRAD_LSQ_DM)
+      k_grad_lsq<true, false><<<grid_for(M.nC), 256, 0, ctx->stream>>>(M, F.dmat.p, phi, g);
+    else if (scheme == FC_GRAD_LSQ_EXACT)
+      k_grad_lsq<false, true><<<grid_for(M.nC), 256, 0, ctx->stream>>>(M, F.dmat.p, phi, g);
+    else k_grad_lsq<true, true><<<grid_for(M.nC), 256, 0, ctx->stream>>>(M, F.dmat.p, phi, g);
     ctx->kernel_launches++;
   } else if (scheme == FC_GRAD_NODE_GAUSS) {
     int st0 = fv_grad_node(ctx, phi, g);

@@ -1397,7 +1397,7 @@ extern "C" int fc_temperature_set_params(fc_ctx* ctx, const fc_temperature_param
   if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
   if (!(prm->urfT > 0) || !(prm->pranl > 0) || !(prm->sigt > 0) || prm->maxiterT < 0)
     return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_temperature_set_params: urfT, pranl and sigt must be > 0");
-  if (prm->gradScheme < FC_GRAD_GAUSS || prm->gradScheme > FC_GRAD_NODE_GAUSS)
+  if (prm->gradScheme < FC_GRAD_GAUSS || prm->gradScheme > FC_GRAD_LSQ_DM_EXACT)
     return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_temperature_set_params: unknown gradient scheme");
   SimpleState& S = sstate(ctx);
   const MeshDev& m = ctx->mesh;

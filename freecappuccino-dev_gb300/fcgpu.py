@@ -29,6 +29,7 @@ FC_ERR_ZERO_PIVOT = -8
 
 BC = {"wall": 1, "inlet": 2, "outlet": 3, "symmetry": 4, "pressure": 5, "empty": 6, "periodic": 7}
 FC_GRAD_GAUSS, FC_GRAD_LSQ, FC_GRAD_LSQ_DM, FC_GRAD_NODE_GAUSS = 0, 1, 2, 3
+FC_GRAD_LSQ_EXACT, FC_GRAD_LSQ_DM_EXACT = 4, 5  # correct 3x3 least-squares solve (no reference counterpart)
 FC_C2N_PSL, FC_C2N_IDS = 0, 1
 FC_LIMITER_NONE, FC_LIMITER_BJ, FC_LIMITER_VENKAT, FC_LIMITER_R, FC_LIMITER_MD = 0, 1, 2, 3, 4
 FC_TIME_STEADY, FC_TIME_BDF, FC_TIME_BDF2, FC_TIME_BDF3 = 0, 1, 2, 3

@@ -315,6 +315,15 @@ double* fc_field_ptr(fc_ctx* ctx, const char* name);  /* device address, NULL if
 #define FC_GRAD_LSQ     1   /* grad_lsq      gradients.f90:782  */
 #define FC_GRAD_LSQ_DM  2   /* grad_lsq_dm   gradients.f90:1334 */
 #define FC_GRAD_NODE_GAUSS 3 /* grad_node_based_gauss gradients.f90:1491, node values of node_interpolation.f90 */
+/* Least-squares gradients with the correct 3x3 solve (no reference
+ * counterpart): grad_lsq / grad_lsq_dm compute the y component with the
+ * wrong adjugate row (b1*D4 - b2*D5 - b3*D6, gradients.f90:887,1480), and
+ * grad_lsq_dm weights boundary faces at xf(i) of the face counter
+ * (gradients.f90:1459).  The _EXACT schemes take the adjugate's y row,
+ * -b1*D2 + b2*D4 - b3*D8, and (dm) the face's own centre, so that linear
+ * fields have exact gradients.  Same matrices as FC_GRAD_LSQ / _DM. */
+#define FC_GRAD_LSQ_EXACT    4
+#define FC_GRAD_LSQ_DM_EXACT 5
 /* Cell-to-node interpolation of the node-based gradient (the `c2n` of
  * node_interpolation.f90:36): FC_C2N_PSL pseudo-Laplacian (the default,
  * :265-631) or FC_C2N_IDS inverse distance (:88-260).  The weights are built

@@ -129,9 +129,13 @@ int csrsolve(Case& c, const std::string& solver, std::vector<double>& fi, const 
 // gradients (gradients.f90)
 void grad_gauss(Case& c, const std::vector<double>& u, std::vector<double>& dudxi);
 void create_matrix_lsq(Case& c);
-void grad_lsq(Case& c, const std::vector<double>& phi, std::vector<double>& dphidxi);
+void grad_lsq(Case& c, const std::vector<double>& phi, std::vector<double>& dphidxi, bool exact = false);
 void create_matrix_lsq_dm(Case& c);
-void grad_lsq_dm(Case& c, const std::vector<double>& phi, std::vector<double>& dphidxi);
+void grad_lsq_dm(Case& c, const std::vector<double>& phi, std::vector<double>& dphidxi, bool exact = false);
+// least-squares matrix of a gradient scheme: 1 (LSQ, LSQ exact), 2 (LSQ_DM, LSQ_DM exact), 0 none
+inline int lsq_matrix_of(int scheme) { return scheme == 1 || scheme == 4 ? 1 : scheme == 2 || scheme == 5 ? 2 : 0; }
+void prepare_lsq(Case& c, int scheme);
+void grad_scheme(Case& c, int scheme, const std::vector<double>& phi, std::vector<double>& dphidxi);
 void grad(Case& c, const std::vector<double>& phi, std::vector<double>& dphidxi);
 void slope_limiter(Case& c, const std::vector<double>& phi, std::vector<double>& dphidxi);
 void set_interpolation_weights(Case& c);

@@ -214,10 +214,7 @@ int orc_grad(void* h, int scheme, double* phi, double* dphi) {
   Case& c = *(Case*)h;
   std::vector<double> p = pad1(phi, c.numTotal);
   std::vector<double> g(3 * (size_t)(c.numTotal + 1), 0.0);
-  if (scheme == 1) { if (c.dmatScheme != 1) create_matrix_lsq(c); grad_lsq(c, p, g); }
-  else if (scheme == 2) { if (c.dmatScheme != 2) create_matrix_lsq_dm(c); grad_lsq_dm(c, p, g); }
-  else if (scheme == 3) grad_node_based_gauss(c, p, g);
-  else grad_gauss(c, p, g);
+  grad_scheme(c, scheme, p, g);
   slope_limiter(c, p, g);
   std::memcpy(dphi, g.data() + 3, sizeof(double) * 3 * c.numTotal);
   return 0;
@@ -226,8 +223,8 @@ int orc_grad(void* h, int scheme, double* phi, double* dphi) {
 int orc_prepare_lsq(void* h, int scheme) {
   Case& c = *(Case*)h;
   c.gradScheme = scheme;
-  if (scheme == 1) create_matrix_lsq(c);
-  else if (scheme == 2) create_matrix_lsq_dm(c);
+  if (lsq_matrix_of(scheme) == 1) create_matrix_lsq(c);
+  else if (lsq_matrix_of(scheme) == 2) create_matrix_lsq_dm(c);
   return 0;
 }
 

@@ -126,19 +126,23 @@ void create_matrix_lsq_dm(Case& c) {
 }
 
 // cofactor apply of grad_lsq (:883-889) / grad_lsq_dm (:1476-1482),
-// including the reference's y-row (b1*D4 - b2*D5 - b3*D6)
-static void lsq_apply(Case& c, std::vector<double>& g) {
+// including the reference's y-row (b1*D4 - b2*D5 - b3*D6).  exact: the
+// y-row of the adjugate of the symmetric normal matrix instead,
+// -b1*D2 + b2*D4 - b3*D8, evaluated as (b2*D4 - b1*D2) - b3*D8 (the
+// least-squares extension lsq_exact; the other rows are the reference's)
+static void lsq_apply(Case& c, std::vector<double>& g, bool exact) {
   for (int inp = 1; inp <= c.numCells; ++inp) {
     const double* D = &c.Dmat[9 * (size_t)inp];
     double b1 = G(g, 1, inp), b2 = G(g, 2, inp), b3 = G(g, 3, inp);
     G(g, 1, inp) = b1 * D[0] - b2 * D[1] + b3 * D[2];
-    G(g, 2, inp) = b1 * D[3] - b2 * D[4] - b3 * D[5];
+    if (exact) G(g, 2, inp) = (b2 * D[3] - b1 * D[1]) - b3 * D[7];
+    else G(g, 2, inp) = b1 * D[3] - b2 * D[4] - b3 * D[5];
     G(g, 3, inp) = b1 * D[6] - b2 * D[7] + b3 * D[8];
   }
 }
 
-// grad_lsq, gradients.f90:782-893
-void grad_lsq(Case& c, const std::vector<double>& phi, std::vector<double>& g) {
+// grad_lsq, gradients.f90:782-893 (exact: the correct y-row, lsq_apply)
+void grad_lsq(Case& c, const std::vector<double>& phi, std::vector<double>& g, bool exact) {
   std::fill(g.begin(), g.end(), 0.0);
   for (int i = 1; i <= c.numInnerFaces; ++i) {
     int ijp = c.owner[i], ijn = c.neighbour[i];
@@ -155,12 +159,14 @@ void grad_lsq(Case& c, const std::vector<double>& phi, std::vector<double>& g) {
            Dz = (c.zf[iface] - c.zc[ijp]) * delta;
     G(g, 1, ijp) = G(g, 1, ijp) + Dx; G(g, 2, ijp) = G(g, 2, ijp) + Dy; G(g, 3, ijp) = G(g, 3, ijp) + Dz;
   }
-  lsq_apply(c, g);
+  lsq_apply(c, g, exact);
 }
 
 // grad_lsq_dm, gradients.f90:1334-1486 (boundary weight reads xf(i)...
-// at the boundary-face counter i, as the reference does at :1459)
-void grad_lsq_dm(Case& c, const std::vector<double>& phi, std::vector<double>& g) {
+// at the boundary-face counter i, as the reference does at :1459; exact:
+// the face's own xf(iface)..., the weight create_matrix_lsq_dm uses, and
+// the correct y-row)
+void grad_lsq_dm(Case& c, const std::vector<double>& phi, std::vector<double>& g, bool exact) {
   std::fill(g.begin(), g.end(), 0.0);
   for (int i = 1; i <= c.numInnerFaces; ++i) {
     int ijp = c.owner[i], ijn = c.neighbour[i];
@@ -172,24 +178,40 @@ void grad_lsq_dm(Case& c, const std::vector<double>& phi, std::vector<double>& g
   }
   for (int i = 1; i <= c.numBoundaryFaces; ++i) {
     int iface = c.numInnerFaces + i, ijp = c.owner[iface], ijn = c.numCells + i;
-    double ddx = c.xf[i] - c.xc[ijp], ddy = c.yf[i] - c.yc[ijp], ddz = c.zf[i] - c.zc[ijp];
+    const int iw = exact ? iface : i;
+    double ddx = c.xf[iw] - c.xc[ijp], ddy = c.yf[iw] - c.yc[ijp], ddz = c.zf[iw] - c.zc[ijp];
     double w = (phi[ijn] - phi[ijp]) / (ddx * ddx + ddy * ddy + ddz * ddz);
     double Dx = w * (c.xf[iface] - c.xc[ijp]), Dy = w * (c.yf[iface] - c.yc[ijp]), Dz = w * (c.zf[iface] - c.zc[ijp]);
     G(g, 1, ijp) = G(g, 1, ijp) + Dx; G(g, 2, ijp) = G(g, 2, ijp) + Dy; G(g, 3, ijp) = G(g, 3, ijp) + Dz;
   }
-  lsq_apply(c, g);
+  lsq_apply(c, g, exact);
+}
+
+// the least-squares matrix a gradient scheme uses (1: create_matrix_lsq,
+// 2: create_matrix_lsq_dm, 0: none), built on first use as the reference
+// builds it at initialisation
+void prepare_lsq(Case& c, int scheme) {
+  const int m = lsq_matrix_of(scheme);
+  if (m == 1 && c.dmatScheme != 1) create_matrix_lsq(c);
+  if (m == 2 && c.dmatScheme != 2) create_matrix_lsq_dm(c);
+}
+
+// one gradient scheme without the limiter: 0 Gauss, 1 LSQ, 2 LSQ_DM, 3 node
+// Gauss, 4 LSQ with the correct y-row, 5 LSQ_DM with the correct y-row and
+// boundary weight
+void grad_scheme(Case& c, int scheme, const std::vector<double>& phi, std::vector<double>& g) {
+  prepare_lsq(c, scheme);
+  if (scheme == 1 || scheme == 4) grad_lsq(c, phi, g, scheme == 4);
+  else if (scheme == 2 || scheme == 5) grad_lsq_dm(c, phi, g, scheme == 5);
+  else if (scheme == 3) grad_node_based_gauss(c, phi, g);
+  else grad_gauss(c, phi, g);
 }
 
 // grad_scalar_field, gradients.f90:106-163: the gradient, then the limiter
 void grad(Case& c, const std::vector<double>& phi, std::vector<double>& g) {
   // the least-squares matrices of the scheme (create_matrix_lsq / _dm, built
   // at initialisation in the reference) on first use
-  if (c.gradScheme == 1 && c.dmatScheme != 1) create_matrix_lsq(c);
-  if (c.gradScheme == 2 && c.dmatScheme != 2) create_matrix_lsq_dm(c);
-  if (c.gradScheme == 1) grad_lsq(c, phi, g);
-  else if (c.gradScheme == 2) grad_lsq_dm(c, phi, g);
-  else if (c.gradScheme == 3) grad_node_based_gauss(c, phi, g);
-  else grad_gauss(c, phi, g);
+  grad_scheme(c, c.gradScheme, phi, g);
   slope_limiter(c, phi, g);
 }
 

@@ -38,7 +38,7 @@ def test_csr_pattern_and_slot_maps_bit_exact(ctx, key):
 
 
 @pytest.mark.parametrize("key", ["hex", "tet"])
-@pytest.mark.parametrize("scheme", [0, 1, 2])
+@pytest.mark.parametrize("scheme", [0, 1, 2, 4, 5])
 def test_gradients_bit_exact(ctx, key, scheme):
     m, a, oc = _setup(ctx, key)
     rng = np.random.default_rng(11)
@@ -70,6 +70,24 @@ def test_linear_field_gradient_on_reference_test_mesh(ctx, fc):
     phi = np.concatenate([xc + yc + zc, (xf + yf + zf)[m.numInnerFaces:]])
     g = ctx.grad(0, phi).reshape(-1, 3)[:m.numCells]
     np.testing.assert_allclose(g, 1.0, atol=1e-12)
+
+
+@pytest.mark.parametrize("key", ["hex", "tet"])
+@pytest.mark.parametrize("scheme", [4, 5])
+def test_exact_lsq_gradient_of_linear_field(ctx, key, scheme):
+    """FC_GRAD_LSQ_EXACT / _DM_EXACT reproduce the gradient of a linear field
+    in every cell (cell values at centroids, boundary values at face
+    centres); the reference's schemes 1 and 2 miss its y component."""
+    m, a, oc = _setup(ctx, key)
+    xc, yc, zc = ctx.geometry("xc"), ctx.geometry("yc"), ctx.geometry("zc")
+    xf, yf, zf = ctx.geometry("xf"), ctx.geometry("yf"), ctx.geometry("zf")
+    lin = lambda x, y, z: 0.5 + 2.0 * x - 3.0 * y + 1.5 * z  # noqa: E731
+    nI = m.numInnerFaces
+    phi = np.concatenate([lin(xc, yc, zc), lin(xf[nI:], yf[nI:], zf[nI:])])
+    g = ctx.grad(scheme, phi).reshape(-1, 3)[:m.numCells]
+    np.testing.assert_allclose(g, np.tile([2.0, -3.0, 1.5], (m.numCells, 1)), atol=1e-9)
+    gq = ctx.grad(scheme - 3, phi).reshape(-1, 3)[:m.numCells]
+    assert np.abs(gq[:, 1] + 3.0).max() > 1e-3
 
 
 def test_poisson_solve_on_global_matrix(ctx, oracle):

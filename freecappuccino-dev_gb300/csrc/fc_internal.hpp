@@ -78,8 +78,6 @@ struct DevOrdered {
   DVec<int> srec[2], xv_ptr[2], push_ptr[2], push[2], slot[2], ucol;
   DVec<int> ovf_ptr[2], ovf_code[2], ovf_col[2], ovf_slot[2];
   DVec<int> lo_tslot, lo_ovf_tslot, dslot, p_ptr, p_col, p_slot;
-  DVec<int> wait_ptr[2], wait_tile[2], wait_need[2];  // producer waits of the exchange blocks
-  DVec<unsigned long long> prog;                      // progress word of every tile
   long long ring_entries = 0, pushed_entries = 0, cross_tile_entries = 0;
 };
 

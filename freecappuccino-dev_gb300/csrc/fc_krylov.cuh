@@ -188,6 +188,8 @@ struct NoTrace {
   __device__ __forceinline__ void mark(int) {}
   __device__ __forceinline__ void sweep() {}
   __device__ __forceinline__ void step(int) {}
+  __device__ __forceinline__ void waited(int) {}
+  __device__ __forceinline__ void staged(int) {}
 };
 
 // sum_k a_k x_j over row i (FMA accumulation, CSR order)

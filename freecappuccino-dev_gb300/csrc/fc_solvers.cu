@@ -64,10 +64,13 @@ enum { TR_SETUP = 0, TR_FWD, TR_MID, TR_BWD, TR_DOT, TR_PUPD, TR_SPMV, TR_UPD, F
 
 // Cycle tracer of the traced ICCG instantiation: per block SM cycles per
 // phase (thread 0's clock), and for the first two sweeps after the DIC setup
-// (the forward and backward sweep of iteration 1) a stamp (clock64,
-// globaltimer) at the start of every step of the tile and after its last.
+// (the forward and backward sweep of iteration 1) four stamps per step of
+// the tile: the compute warps' start of the step (clock64), the moment its
+// stage buffer had landed (clock64), the staging thread's start of the
+// step's copies (clock64) and the start of the step on the global timer
+// (ns); the stamps after the last step close the sweep.
 // trace layout: [blocks][FC_TRACE_N] phase cycles, then
-// [2 sweeps][blocks][tl_cap][2] step stamps.
+// [2 sweeps][blocks][tl_cap][4] step stamps.
 struct Tracer {
   unsigned long long* out;
   int tl_cap, nsweep;
@@ -83,14 +86,25 @@ struct Tracer {
     t = now;
   }
   __device__ __forceinline__ void sweep() { ++nsweep; }
+  __device__ __forceinline__ unsigned long long* slot(int k) {
+    return out + (size_t)gridDim.x * FC_TRACE_N + (((size_t)(nsweep - 1) * gridDim.x + blockIdx.x) * tl_cap + k) * 4;
+  }
   __device__ __forceinline__ void step(int k) {
     if (threadIdx.x != 0 || nsweep > 2 || k >= tl_cap) return;
     unsigned long long gt;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(gt));
-    unsigned long long* q = out + (size_t)gridDim.x * FC_TRACE_N +
-                            (((size_t)(nsweep - 1) * gridDim.x + blockIdx.x) * tl_cap + k) * 2;
+    unsigned long long* q = slot(k);
     q[0] = (unsigned long long)clock64();
-    q[1] = gt;
+    q[3] = gt;
+  }
+  __device__ __forceinline__ void waited(int k) {
+    if (threadIdx.x != 0 || nsweep > 2 || k >= tl_cap) return;
+    slot(k)[1] = (unsigned long long)clock64();
+  }
+  // called by the staging thread only
+  __device__ __forceinline__ void staged(int k) {
+    if (nsweep > 2 || k >= tl_cap) return;
+    slot(k)[2] = (unsigned long long)clock64();
   }
   __device__ void flush() {
     if (threadIdx.x == 0)
@@ -136,7 +150,6 @@ __device__ bool residual_l1(const KArgs<T>& A, int& ph, double& l1out) {
 // exchange arrays to the sentinel, b (and x) gathered; ends with a barrier.
 template <class T>
 __device__ bool ord_prologue(const KArgs<T>& A, bool dilu, bool with_x) {
-  for (int t = vg_gt(A.C); t < A.O.ntiles; t += vg_G(A.C)) A.O.prog[t] = 0ull;
   ord_gather_values(A.C, A.O, A.V, A.S.a, A.nnz, dilu);
   ord_gather_vec(A.C, A.O, A.b, A.bo);
   if (with_x) ord_gather_vec(A.C, A.O, (const T*)A.x, A.xo);
@@ -643,8 +656,8 @@ static cudaError_t upload_vec(DVec<int>& d, const V& h) {
 // the stage area of the ordered sweeps: the shared memory the fixed parts
 // leave (the sweep modes cut it into as many buffers as fit, at most
 // FC_MAX_STAGES); 0 when nothing is left
-static size_t ordered_stage_area(int R, int maxW, int max_tile_steps, int ntiles) {
-  const size_t fixed = osweep_fixed_bytes<double>(R, maxW, max_tile_steps, ntiles);
+static size_t ordered_stage_area(int R, int maxW, int max_tile_steps) {
+  const size_t fixed = osweep_fixed_bytes<double>(R, maxW, max_tile_steps);
   return fixed >= (size_t)FC_SWEEP_SMEM ? 0 : ((size_t)FC_SWEEP_SMEM - fixed) & ~(size_t)15;
 }
 
@@ -674,14 +687,14 @@ static void ordered_blocks(const OrderedSweep& O, int& xmax, int& pmax) {
 static bool ordered_fits(const OrderedSweep& O) {
   int xmax, pmax;
   ordered_blocks(O, xmax, pmax);
-  return ordered_min_stages(ordered_stage_area(O.R, O.maxW, O.max_tile_steps, O.ntiles), O.maxW, xmax, pmax) >= 2;
+  return ordered_min_stages(ordered_stage_area(O.R, O.maxW, O.max_tile_steps), O.maxW, xmax, pmax) >= 2;
 }
 
 static int upload_ordered(fc_ctx* ctx, const OrderedSweep& O, DevOrdered& D) {
   D.n = O.n; D.nE = O.nE; D.ntiles = O.ntiles; D.nsteps = O.nsteps; D.nlev = O.nlev; D.R = O.R; D.maxW = O.maxW;
   D.max_tile_steps = O.max_tile_steps;
   ordered_blocks(O, D.xmax, D.pmax);
-  D.stage_area = ordered_stage_area(D.R, D.maxW, D.max_tile_steps, D.ntiles);
+  D.stage_area = ordered_stage_area(D.R, D.maxW, D.max_tile_steps);
   if (ordered_min_stages(D.stage_area, D.maxW, D.xmax, D.pmax) < 2)
     return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "sweep tiles too wide for shared memory");
   {
@@ -711,12 +724,7 @@ static int upload_ordered(fc_ctx* ctx, const OrderedSweep& O, DevOrdered& D) {
     FC_CUDA_TRY(ctx, upload_vec(D.ovf_code[d], H.ovf_code));
     FC_CUDA_TRY(ctx, upload_vec(D.ovf_col[d], H.ovf_col));
     FC_CUDA_TRY(ctx, upload_vec(D.ovf_slot[d], H.ovf_slot));
-    FC_CUDA_TRY(ctx, upload_vec(D.wait_ptr[d], H.wait_ptr));
-    FC_CUDA_TRY(ctx, upload_vec(D.wait_tile[d], H.wait_tile));
-    FC_CUDA_TRY(ctx, upload_vec(D.wait_need[d], H.wait_need));
   }
-  FC_CUDA_TRY(ctx, D.prog.alloc(std::max(1, O.ntiles)));
-  FC_CUDA_TRY(ctx, cudaMemset(D.prog.p, 0, D.prog.bytes()));
   // columns of the upper entries, 4 per row (Gauss-Seidel)
   std::vector<int> ucol((size_t)4 * O.nE, 0);
   for (int q = 0; q < O.n; ++q)
@@ -907,9 +915,7 @@ static OrdView ord_view_of(CsrSystem* s) {
     O.push[d] = D.push[d].p; O.slot[d] = D.slot[d].p;
     O.ovf_ptr[d] = D.ovf_ptr[d].p; O.ovf_code[d] = D.ovf_code[d].p; O.ovf_col[d] = D.ovf_col[d].p;
     O.ovf_slot[d] = D.ovf_slot[d].p;
-    O.wait_ptr[d] = D.wait_ptr[d].p; O.wait_tile[d] = D.wait_tile[d].p; O.wait_need[d] = D.wait_need[d].p;
   }
-  O.prog = D.prog.p;
   O.ucol = (const int4*)D.ucol.p;
   O.lo_tslot = D.lo_tslot.p; O.lo_ovf_tslot = D.lo_ovf_tslot.p; O.dslot = D.dslot.p;
   O.p_ptr = D.p_ptr.p; O.p_col = D.p_col.p; O.p_slot = D.p_slot.p;
@@ -930,7 +936,7 @@ template <class T>
 static int launch_coop(fc_ctx* ctx, CsrSystem* s, const void* fn, KArgs<T>& A, void** extra, int nextra,
                        int block = FC_SWEEP_BLOCK) {
   const DevOrdered& D = s->ord;
-  const size_t smem = osweep_smem_bytes<T>(D.R, D.stage_area, D.maxW, D.max_tile_steps, D.ntiles);
+  const size_t smem = osweep_smem_bytes<T>(D.R, D.stage_area, D.maxW, D.max_tile_steps);
   if (smem > 48 * 1024)
     FC_CUDA_TRY(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int nb = 0;
@@ -993,7 +999,7 @@ static int solve_fp64(fc_ctx* ctx, CsrSystem* s, const std::string& solver, cons
   if (traced) {
     const int nb = std::max(1, ctx->num_sms);
     const int cap = s->ord.max_tile_steps + 1;
-    FC_CUDA_TRY(ctx, ctx->trace.alloc((size_t)nb * FC_TRACE_N + (size_t)2 * nb * cap * 2));
+    FC_CUDA_TRY(ctx, ctx->trace.alloc((size_t)nb * FC_TRACE_N + (size_t)2 * nb * cap * 4));
     FC_CUDA_TRY(ctx, cudaMemsetAsync(ctx->trace.p, 0, ctx->trace.bytes(), ctx->stream));
     A.trace = ctx->trace.p;
     A.trace_cap = cap;
@@ -1241,7 +1247,7 @@ static size_t batch_smem(const std::vector<BatchItem>& items) {
   size_t m = 0;
   for (const BatchItem& it : items) {
     const DevOrdered& D = it.s->ord;
-    m = std::max(m, osweep_smem_bytes<T>(D.R, D.stage_area, D.maxW, D.max_tile_steps, D.ntiles));
+    m = std::max(m, osweep_smem_bytes<T>(D.R, D.stage_area, D.maxW, D.max_tile_steps));
   }
   return m;
 }
@@ -1418,7 +1424,8 @@ int sys_precond(fc_ctx* ctx, CsrSystem* s, int dilu, const double* q, double* z_
 // out[0..FC_TRACE_N) = cycles summed over the blocks that ran, per phase;
 // out[FC_TRACE_N] = those blocks; out[FC_TRACE_N+1] = blocks of the launch
 // (B); out[FC_TRACE_N+2] = stamps per tile and sweep (K); with timeline
-// non-null it receives the stamps as [2][B][K][2] (clock64, globaltimer).
+// non-null it receives the stamps as [2][B][K][4] (step start, buffer
+// landed, staging start: clock64; step start: globaltimer).
 extern "C" int fc_trace_get(fc_ctx* ctx, double* out, unsigned long long* timeline) {
   if (!ctx || !out) return FC_ERR_BAD_INPUT;
   if (!ctx->trace.p) return fc_fail_msg(ctx, FC_ERR_STATE, "no trace recorded");

@@ -22,18 +22,11 @@
 //
 // Exchange: a value a row needs from another tile (or from more than R-1
 // steps back) is pushed by its producer into the consumer's slot of the
-// exchange array xv, whose slots start every sweep at a sentinel NaN.  Every
-// tile publishes its progress (steps completed in the current sweep) in a
-// 64-bit word of global memory; a publisher thread, off the compute warps'
-// path, does the release store after each batch of completed steps.  The
-// stager issues a step's exchange-block copy only once every producer on the
-// step's wait list has published the steps the block needs, so the compute
-// warps read exchanged values from shared memory instead of paying an L2
-// round trip on every step; a consumer lags its producers by a few steps
-// and then runs at its own pace.  As a safety net the compute warps still
-// poll a slot (bounded) whose staged copy holds the sentinel, and they put
-// the sentinel back after use.  Bulk copies read through L2, so staged data
-// is never an SM's stale L1 line.
+// exchange array xv, whose slots start every sweep at a sentinel NaN.  The
+// staged copy is used when it already holds the value, else the slot is
+// polled (bounded) until the producer's store arrives; the consumer puts the
+// sentinel back after use.  Bulk copies read through L2, so staged data is
+// never an SM's stale L1 line.
 #pragma once
 #include "fc_krylov.cuh"
 #include "fc_schedule.hpp"
@@ -86,28 +79,6 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* mb, unsigned parit
 __device__ __forceinline__ void bar_compute(int nthreads) {
   asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
 }
-// progress words: release/acquire at GPU scope (tile to tile) and the
-// block-local step counter at CTA scope (compute warps to the publisher)
-__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
-  unsigned long long v;
-  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
-  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-__device__ __forceinline__ int ld_acquire_cta_s32(const int* p) {
-  int v;
-  asm volatile("ld.acquire.cta.shared::cta.s32 %0, [%1];" : "=r"(v) : "r"(smem_addr(p)) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release_cta_s32(int* p, int v) {
-  asm volatile("st.release.cta.shared::cta.s32 [%0], %1;" ::"r"(smem_addr(p)), "r"(v) : "memory");
-}
-// generic-proxy writes observed by this thread (the producers' pushes,
-// acquired through their progress words) before the bulk copies it issues next
-__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
-
 // record strides (elements of T) of the per-solve row records
 template <class T> struct Rec { static constexpr int V = sizeof(T) == 8 ? 6 : 8; };
 
@@ -136,10 +107,6 @@ struct OrdView {
   const int* __restrict__ p_ptr;
   const int* __restrict__ p_col;
   const int* __restrict__ p_slot;
-  const int* __restrict__ wait_ptr[2];   // producer waits of each step's exchange block
-  const int* __restrict__ wait_tile[2];
-  const int* __restrict__ wait_need[2];
-  unsigned long long* prog;              // [ntiles] (sweep << 32) | steps completed
 };
 
 // per-solve values in the new numbering (gathered by the kernel from the
@@ -208,18 +175,16 @@ __host__ __device__ inline int stages_in(size_t area, int buffer_bytes) {
 // dynamic shared memory of an ordered-sweep kernel: 2 FC_MAX_STAGES
 // mbarriers, ring, the stage area (cut by every sweep mode into its own
 // buffers), the tile's step tables (rows, exchange and push offsets of both
-// directions), the last progress seen of every producer tile, the abort flag
-// and the completed-steps counter
+// directions) and the abort flag
 template <class T>
-inline size_t osweep_fixed_bytes(int R, int maxW, int max_tile_steps, int ntiles) {
+inline size_t osweep_fixed_bytes(int R, int maxW, int max_tile_steps) {
   size_t ring = ((size_t)R * maxW * sizeof(T) + 15) & ~(size_t)15;
   size_t tab = ((size_t)5 * (max_tile_steps + 1) * 4 + 15) & ~(size_t)15;
-  size_t seen = (size_t)8 * (ntiles > 0 ? ntiles : 1);
-  return FC_SMEM_HDR + ring + tab + seen + 16;
+  return FC_SMEM_HDR + ring + tab + 16;
 }
 template <class T>
-inline size_t osweep_smem_bytes(int R, size_t stage_area, int maxW, int max_tile_steps, int ntiles) {
-  return osweep_fixed_bytes<T>(R, maxW, max_tile_steps, ntiles) + stage_area;
+inline size_t osweep_smem_bytes(int R, size_t stage_area, int maxW, int max_tile_steps) {
+  return osweep_fixed_bytes<T>(R, maxW, max_tile_steps) + stage_area;
 }
 
 struct OsCtx {
@@ -231,15 +196,11 @@ struct OsCtx {
   int* sp;                    // [ns+1] first row of each local step (ascending levels)
   int* xp[2];                 // [ns+1] exchange block offsets per direction
   int* pp[2];                 // [ns+1] push block offsets per direction
-  unsigned long long* seen;   // [ntiles] last progress word read of each producer tile (stager)
   int* abort_flag;
-  int* done;                  // steps completed by this block over all its sweeps
   // stage buffer b: bit b of `parity` = parity of its next fill/completion,
   // bit b of `used` = it has been filled before (registers, no runtime-
   // indexed arrays, so the context never goes to local memory)
   unsigned parity, used;
-  unsigned seq;               // sweeps begun by this block (the high word of its progress)
-  int done_base;              // `done` at the start of the current sweep
   StageLayout L;
 };
 
@@ -265,15 +226,9 @@ __device__ __forceinline__ OsCtx osweep_ctx(const OrdView& O, unsigned char* sme
   X.pp[0] = tab + 3 * (ns + 1);
   X.pp[1] = tab + 4 * (ns + 1);
   off += ((size_t)5 * (ns + 1) * 4 + 15) & ~(size_t)15;
-  X.seen = (unsigned long long*)(smem + off);
-  off += (size_t)8 * (O.ntiles > 0 ? O.ntiles : 1);
   X.abort_flag = (int*)(smem + off);
-  X.done = X.abort_flag + 1;
   X.parity = 0;
   X.used = 0;
-  X.seq = 0;
-  X.done_base = 0;
-  for (int k = threadIdx.x; k < O.ntiles; k += blockDim.x) X.seen[k] = 0ull;
   if (t < O.ntiles) {
     const int s0 = __ldg(O.tile_step_ptr + t);
     for (int k = threadIdx.x; k <= ns; k += blockDim.x) {
@@ -286,7 +241,6 @@ __device__ __forceinline__ OsCtx osweep_ctx(const OrdView& O, unsigned char* sme
   }
   if (threadIdx.x == 0) {
     *X.abort_flag = 0;
-    *X.done = 0;
     for (int b = 0; b < FC_MAX_STAGES; ++b) {
       mbar_init(X.full + b, 1);
       mbar_init(X.empty + b, 1);
@@ -341,13 +295,9 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
   constexpr bool kGS = MODE == OS_GS;
   constexpr int VR = Rec<T>::V;
   if (tr) tr->sweep();
-  const unsigned seq = ++X.seq;
   const int t = vg_bid(C);
   if (t >= O.ntiles) return true;
-  const int s0 = __ldg(O.tile_step_ptr + t);
-  const int ns = __ldg(O.tile_step_ptr + t + 1) - s0;
-  const int done_base = X.done_base;
-  X.done_base += ns;
+  const int ns = __ldg(O.tile_step_ptr + t + 1) - __ldg(O.tile_step_ptr + t);
   // the areas this mode reads, as many stage buffers as the area holds
   StageLayout L;
   L.template init_for<T>(X.L.W, O.xmax, O.pmax, MODE);
@@ -355,9 +305,6 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
   const int nct = (int)blockDim.x - 32;  // threads before the staging warp
   // compute threads of this tile: whole warps covering its widest step
   const int ncg = min(nct, (W + 31) & ~31);
-  // the publisher of the tile's progress: an idle compute warp's first
-  // thread, else the second lane of the staging warp
-  const int pubt = ncg < nct ? ncg : nct + 1;
   T* ring = (T*)X.ring;
   T* xv = V.xv[dirn];
   const int* sp = X.sp;
@@ -365,47 +312,10 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
   const int* pp = X.pp[dirn];
   auto step_of = [&](int k) { return dirn ? ns - 1 - k : k; };
 
-  if ((int)threadIdx.x == pubt) {
-    // --------------------------------------------------------- publisher
-    // release the tile's completed steps of this sweep (the compute warps'
-    // value stores happen before, through their barrier and the CTA-scope
-    // release of `done`); batches whatever completed during the last store
-    const unsigned long long hi = (unsigned long long)seq << 32;
-    int pub = 0;
-    unsigned spins = 0;
-    while (pub < ns) {
-      const int d = ld_acquire_cta_s32(X.done) - done_base;
-      if (d > pub) {
-        st_release_u64(O.prog + t, hi | (unsigned)d);
-        pub = d;
-        spins = 0;
-      } else {
-        if (*((volatile int*)X.abort_flag) || ++spins > FC_SPIN_LIMIT) break;
-        __nanosleep(20);
-      }
-    }
-  }
   if ((int)threadIdx.x >= nct) {
     // ------------------------------------------------------------ stager
     if (threadIdx.x == (unsigned)nct) {
       bool ok = true;
-      // every producer on step gs's wait list has published the steps the
-      // exchange block needs (progress words of other sweeps are smaller)
-      auto producers_ready = [&](int gs) -> bool {
-        const int w0 = __ldg(O.wait_ptr[dirn] + gs), w1 = __ldg(O.wait_ptr[dirn] + gs + 1);
-        for (int w = w0; w < w1; ++w) {
-          const int P = __ldg(O.wait_tile[dirn] + w);
-          const unsigned long long target = ((unsigned long long)seq << 32) | (unsigned)__ldg(O.wait_need[dirn] + w);
-          if (X.seen[P] >= target) continue;
-          unsigned spins = 0;
-          unsigned long long v;
-          while ((v = ld_acquire_u64(O.prog + P)) < target)
-            if (++spins > FC_SPIN_LIMIT || *((volatile int*)C.status) != 0 || *((volatile int*)X.abort_flag))
-              return false;
-          X.seen[P] = v;
-        }
-        return true;
-      };
       for (int k = 0; k < ns && ok; ++k) {
         if (*((volatile int*)X.abort_flag)) break;
         const int b = k & (K - 1);
@@ -419,6 +329,7 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
           ok = false;
           break;
         }
+        if (tr) tr->staged(k);
         const int ls = step_of(k);
         const int base = sp[ls], cnt = sp[ls + 1] - base;
         const int b0 = base & ~3, nw = ((base + cnt + 3) & ~3) - b0;
@@ -442,21 +353,10 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
         }
         if (kQ) bulk_g2s(B + L.oQ, io.q + b0, (unsigned)sizeof(T) * nw, mb);
         if (kE) bulk_g2s(B + L.oE, io.e + b0, (unsigned)sizeof(T) * nw, mb);
+        if (nx) bulk_g2s(B + L.oXV, xv + x0, (unsigned)sizeof(T) * nx, mb);
         if (np) bulk_g2s(B + L.oP, O.push[dirn] + p0, 4u * np, mb);
         X.parity ^= 1u << b;
         X.used |= 1u << b;
-        if (nx) {
-          // the exchange block last: once its producers have published
-          if (!producers_ready(s0 + ls)) {
-            // the compute warps run out of their own bounded wait on this
-            // buffer and raise the abort flag
-            atomicCAS(C.status, 0, FC_ERR_TIMEOUT);
-            ok = false;
-            break;
-          }
-          fence_proxy_async_global();
-          bulk_g2s(B + L.oXV, xv + x0, (unsigned)sizeof(T) * nx, mb);
-        }
       }
     }
   } else if ((int)threadIdx.x < ncg) {
@@ -476,6 +376,7 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
         atomicCAS(C.status, 0, FC_ERR_TIMEOUT);
         *((volatile int*)X.abort_flag) = 1;
       }
+      if (tr) tr->waited(k);
       const int xbase = xp[ls];
       const unsigned char* B = X.stage + (size_t)b * L.bytes;
       const int4* S4 = (const int4*)(B + L.oS);
@@ -616,10 +517,7 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
         for (int mm = 0; mm < np; ++mm) xv[PS[poff + mm]] = val;
       }
       bar_compute(ncg);
-      if (threadIdx.x == 0) {
-        mbar_arrive(X.empty + b);
-        st_release_cta_s32(X.done, done_base + k + 1);
-      }
+      if (threadIdx.x == 0) mbar_arrive(X.empty + b);
       X.parity ^= 1u << b;
       X.used |= 1u << b;
       if (*((volatile int*)X.abort_flag)) break;

@@ -612,7 +612,9 @@ class Context:
     def trace(self, timeline=False):
         """Phase cycles of the last traced ICCG solve: (dict phase -> cycles
         summed over blocks, blocks); with timeline=True also the step stamps
-        as a uint64 array [sweep(fwd, bwd)][tile][step][clock64, globaltimer]."""
+        as a uint64 array [sweep(fwd, bwd)][tile][step][4]: step start,
+        stage buffer landed, staging started (clock64), step start
+        (globaltimer)."""
         out = np.zeros(11)
         self._check(self.L.fc_trace_get(self.h, _ptr(out), None), "fc_trace_get")
         keys = ("setup", "fwd_sweep", "sweep_barrier", "bwd_sweep", "dot", "p_update", "spmv", "xr_update")
@@ -620,7 +622,7 @@ class Context:
         if not timeline:
             return res
         nb, cap = int(out[9]), int(out[10])
-        tl = np.zeros((2, nb, cap, 2), dtype=np.uint64)
+        tl = np.zeros((2, nb, cap, 4), dtype=np.uint64)
         self._check(self.L.fc_trace_get(self.h, _ptr(out), _ptr(tl)), "fc_trace_get")
         return res + (tl,)
 

@@ -550,31 +550,6 @@ bool build_ordered_sweep(int n, const int* ia, const int* ja, const int* dg, con
       D.xv_ptr[gs + 1] = D.xv_ptr[gs] + ((xs + 3) & ~3);
       D.push_ptr[gs + 1] = D.push_ptr[gs] + ((ps + 3) & ~3);
     }
-    // producer waits of every step's exchange block: per producing tile the
-    // largest sweep-order step (+1) of the rows the block receives values of
-    {
-      std::vector<std::vector<std::pair<int, int>>> w(O.nsteps);
-      for (int q = 0; q < n; ++q)
-        for (const auto& cm : cons[q]) {
-          const int qc = cm.first, ip = O.perm[q], tp = row_tile[ip];
-          const int nstp = S.tile_step_ptr[tp + 1] - S.tile_step_ptr[tp];
-          const int order = dirn == 0 ? row_ls[ip] : nstp - 1 - row_ls[ip];
-          w[row_step[qc]].push_back({tp, order + 1});
-        }
-      D.wait_ptr.assign(O.nsteps + 1, 0);
-      D.wait_tile.clear();
-      D.wait_need.clear();
-      for (int gs = 0; gs < O.nsteps; ++gs) {
-        auto& v = w[gs];
-        std::sort(v.begin(), v.end());
-        for (size_t k = 0; k < v.size(); ++k) {
-          if (k + 1 < v.size() && v[k + 1].first == v[k].first) continue;  // keep the largest need per tile
-          D.wait_tile.push_back(v[k].first);
-          D.wait_need.push_back(v[k].second);
-        }
-        D.wait_ptr[gs + 1] = (int)D.wait_tile.size();
-      }
-    }
     D.push.assign(D.push_ptr[O.nsteps], 0);
     for (int q = 0; q < n; ++q) {
       const int np = (int)cons[q].size();

@@ -88,11 +88,6 @@ struct OrderedDir {
   std::vector<int> push;      // absolute exchange positions the values are pushed to
   std::vector<int> ovf_ptr;   // [n+1] entries e >= FC_ELL
   std::vector<int> ovf_slot, ovf_code, ovf_col;
-  // producers a step's exchange block waits for: for global step gs the
-  // entries [wait_ptr[gs], wait_ptr[gs+1]) give a producing tile and the
-  // number of that tile's steps (in this direction's sweep order) that must
-  // be complete before the block holds every value the step needs
-  std::vector<int> wait_ptr, wait_tile, wait_need;
   long long ring_entries = 0, pushed_entries = 0, cross_tile_entries = 0;
 };
 

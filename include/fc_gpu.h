@@ -238,12 +238,14 @@ int fc_batch_tune(fc_batch* b, const char* solver, const double* const* a, const
 /* Tracing of the FP64 ICCG kernel (no counterpart in the reference): with
  * on != 0 the solves run a traced instantiation that records per block the
  * SM cycles of each phase and, for the forward and backward sweep of the
- * first iteration, a (clock64, globaltimer) stamp at the start of every step
- * of every tile.  fc_trace_get: out[11] = cycles summed over the blocks for
- * setup, forward sweep, sweep barrier, backward sweep, dot product, p update,
- * SpMV, x/r update; then the blocks that ran, the blocks of the launch (B)
- * and the stamps per tile (K); timeline (optional, 2*B*K*2 entries)
- * receives the stamps as [sweep][tile][step][clock, globaltimer].  With
+ * first iteration, four stamps per step of every tile.  fc_trace_get:
+ * out[11] = cycles summed over the blocks for setup, forward sweep, sweep
+ * barrier, backward sweep, dot product, p update, SpMV, x/r update; then the
+ * blocks that ran, the blocks of the launch (B) and the stamps per tile (K);
+ * timeline (optional, 2*B*K*4 entries) receives the stamps as
+ * [sweep][tile][step][4]: the compute warps' start of the step, the moment
+ * its staged data had landed, the staging thread's start of its copies
+ * (clock64 of the tile's SM) and the step start on the global timer.  With
  * tracing on, the multicolour inner solve of FC_PREC_MIXED_COLOURED launches
  * its kernels from the host instead of its CUDA graph, so that a profiler
  * sees each launch. */

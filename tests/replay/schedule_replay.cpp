@@ -1,10 +1,8 @@
 // CPU replay of the schedule-ordered sweep (host/fc_schedule.hpp): builds the
 // ordered structure for a 7-point pattern (optionally with random long-range
 // and one-sided couplings), replays the forward and backward sweeps tile by
-// tile with the kernel's ring and exchange rules -- a tile runs a step as soon
-// as the producers on the step's wait list have completed the listed steps,
-// and every exchanged value must then be in place -- and checks the result
-// bit for bit against plain substitution in the original numbering, plus the
+// tile with the kernel's ring and exchange rules, and checks the result bit for
+// bit against plain substitution in the original numbering, plus the
 // exchange/push bookkeeping and the renumbered matrix.  Prints OK on success.
 #include <algorithm>
 #include <cstdio>
@@ -111,8 +109,7 @@ int main(int argc, char** argv) {
     for (size_t p = 0; p < xvn; ++p) if (pushed_cnt[p] != needed[p]) { if (bad < 5) printf("dir %d pos %zu pushed %d needed %d\n", dirn, p, pushed_cnt[p], needed[p]); bad++; }
     std::vector<double> in(n), out(n, NAN), xv(xvn, NAN);
     for (int qq = 0; qq < n; ++qq) in[qq] = dirn == 0 ? q[O.perm[qq]] : yref[O.perm[qq]];
-    std::vector<int> next(O.ntiles, 0), completed(O.ntiles, 0);
-    if ((int)D.wait_ptr.size() != O.nsteps + 1) { printf("wait_ptr size\n"); return 1; }
+    std::vector<int> next(O.ntiles, 0);
     std::vector<std::vector<double>> ring(O.ntiles);
     for (int t = 0; t < O.ntiles; ++t) ring[t].assign((size_t)R * O.tile_W[t], NAN);
     int done = 0, rounds = 0;
@@ -125,28 +122,12 @@ int main(int argc, char** argv) {
         if (next[t] >= ns) { done++; continue; }
         int k = next[t], ls = dirn ? ns - 1 - k : k, gs = O.tile_step_ptr[t] + ls;
         int base = O.step_ptr[gs], cnt = O.step_ptr[gs + 1] - base, W = O.tile_W[t];
-        // the kernel stages a step's exchange block once every producer of
-        // its wait list has completed the listed number of steps: the tile
-        // runs the step exactly then, and every exchanged value must be there
         bool ready = true;
-        for (int w = D.wait_ptr[gs]; w < D.wait_ptr[gs + 1]; ++w) {
-          const int P = D.wait_tile[w], need = D.wait_need[w];
-          if (P < 0 || P >= O.ntiles || need < 1) { printf("bad wait entry\n"); return 1; }
-          if (P == t && need > k) { printf("wait on a later step of the own tile\n"); return 1; }
-          if (completed[P] < need) ready = false;
+        for (int sl = 0; sl < cnt && ready; ++sl) {
+          int qq = base + sl; unsigned s0 = (unsigned)D.srec[4 * qq]; int ne = s0 & 255, xoff = s0 >> 16, m = 0;
+          for (int e = 0; e < ne; ++e) if (code_of(qq, e) < 0) { if (std::isnan(xv[D.xv_ptr[gs] + xoff + m])) { ready = false; break; } m++; }
         }
         if (!ready) continue;
-        for (int sl = 0; sl < cnt; ++sl) {
-          int qq = base + sl; unsigned s0 = (unsigned)D.srec[4 * qq]; int ne = s0 & 255, xoff = s0 >> 16, m = 0;
-          for (int e = 0; e < ne; ++e)
-            if (code_of(qq, e) < 0) {
-              if (std::isnan(xv[D.xv_ptr[gs] + xoff + m])) {
-                if (bad < 5) printf("dir %d tile %d step %d: wait list satisfied, exchanged value missing\n", dirn, t, k);
-                bad++;
-              }
-              m++;
-            }
-        }
         progress = true;
         std::vector<double> vals(cnt);
         for (int sl = 0; sl < cnt; ++sl) {
@@ -170,7 +151,6 @@ int main(int argc, char** argv) {
         next[t]++;
       }
       for (auto& pv : pending) xv[pv.first] = pv.second;
-      for (int t = 0; t < O.ntiles; ++t) completed[t] = next[t];
       rounds++;
       if (!progress && done < O.ntiles) { printf("DEADLOCK dir %d after %d rounds\n", dirn, rounds); return 1; }
     }

@@ -7,8 +7,15 @@ oracle (the CPU restatement of the reference):
     relative L1 from a zero start: the same iteration count and the field
     within TOL_FIELD;
   - the 64^3 lid-driven cavity (262,144 cells, Re 100, the cavity input's
-    settings) over 200 SIMPLE iterations: the residual history (resor of
-    U, V, W, p) and the final fields.
+    settings) over 200 SIMPLE iterations.  The reference's inner solves stop
+    at a relative tolerance of 0.01 / 0.025 or after 5 / 20 iterations, so
+    two correct rounding paths take different inner iteration counts now
+    and then, and their trajectories drift apart: the residual histories
+    (resor) and the fields after 200 iterations are compared with the bounds
+    that drift allows (SIMPLE_RESOR_RTOL, SIMPLE_FIELD_TOL).  The iteration
+    itself is checked tightly in lockstep: after the 200 iterations the
+    oracle takes the GPU's fields and both run one more iteration, twice
+    (LOCKSTEP_*).
 
 The oracle's side takes about a minute on one core in all."""
 import numpy as np
@@ -20,8 +27,11 @@ from test_gpu_simple import setup_cavity
 pytestmark = pytest.mark.gpu
 
 TOL_FIELD = 1e-8        # converged fields: max |x - x_oracle| <= TOL_FIELD * max |x_oracle|
-SIMPLE_RESOR_RTOL = 1e-6
-SIMPLE_FIELD_TOL = 1e-8
+SIMPLE_RESOR_RTOL = 5e-3   # drift of the residual history over 200 iterations (measured 1.3e-3)
+SIMPLE_FIELD_TOL = 1e-5    # drift of u, v, w, p after 200 iterations (measured 1.4e-6)
+LOCKSTEP_RESOR_RTOL = 1e-7
+LOCKSTEP_FIELD_TOL = 1e-8
+STATE = ("u", "v", "w", "p", "pp", "flmass")
 
 
 def test_c2_128_laplacian_dic_and_iccg_match_oracle(ctx, oracle):
@@ -45,6 +55,18 @@ def test_c2_128_laplacian_dic_and_iccg_match_oracle(ctx, oracle):
     assert err <= TOL_FIELD, f"ICCG field max rel diff {err:.3e}"
 
 
+def lockstep(ctx, oc):
+    """The oracle takes the GPU's state, both run one SIMPLE iteration:
+    (max resor rel diff, {field: max rel diff})."""
+    for k in STATE:
+        oc.set(k, ctx.field_get(k))
+    rg = np.array(ctx.simple_iteration())
+    ro = np.array(oc.simple_iteration()[1])
+    rel = np.abs(rg - ro) / np.maximum(np.abs(ro), 1e-300)
+    errs = {k: float(np.abs(ctx.field_get(k) - oc.get(k)).max() / np.abs(oc.get(k)).max()) for k in ("u", "v", "w", "p")}
+    return float(rel.max()), errs
+
+
 def test_c1_64_cavity_200_simple_iterations_track_oracle(ctx, fc):
     n = 64
     m, oc = setup_cavity(ctx, fc, "contract_c1", n, n, n, perturb=0.0)
@@ -62,3 +84,10 @@ def test_c1_64_cavity_200_simple_iterations_track_oracle(ctx, fc):
     assert rel.max() <= SIMPLE_RESOR_RTOL, msg
     for k, err in errs.items():
         assert err <= SIMPLE_FIELD_TOL, f"{k}: " + msg
+    # one more iteration from the same state, twice (the second after the
+    # first lockstep iteration has moved both sides on)
+    for _ in range(2):
+        r, e = lockstep(ctx, oc)
+        assert r <= LOCKSTEP_RESOR_RTOL, (r, e)
+        for k, err in e.items():
+            assert err <= LOCKSTEP_FIELD_TOL, (k, r, e)

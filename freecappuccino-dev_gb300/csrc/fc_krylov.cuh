@@ -190,6 +190,7 @@ struct NoTrace {
   __device__ __forceinline__ void step(int) {}
   __device__ __forceinline__ void waited(int) {}
   __device__ __forceinline__ void staged(int) {}
+  template <class V> __device__ __forceinline__ void at(int, int, V) {}
 };
 
 // sum_k a_k x_j over row i (FMA accumulation, CSR order)

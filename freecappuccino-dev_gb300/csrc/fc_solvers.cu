@@ -61,16 +61,19 @@ struct KArgs {
 
 // phases of the ICCG kernel for the optional cycle trace
 enum { TR_SETUP = 0, TR_FWD, TR_MID, TR_BWD, TR_DOT, TR_PUPD, TR_SPMV, TR_UPD, FC_TRACE_N = 8 };
+#define FC_TRACE_STAMPS 8
 
 // Cycle tracer of the traced ICCG instantiation: per block SM cycles per
 // phase (thread 0's clock), and for the first two sweeps after the DIC setup
-// (the forward and backward sweep of iteration 1) four stamps per step of
-// the tile: the compute warps' start of the step (clock64), the moment its
-// stage buffer had landed (clock64), the staging thread's start of the
-// step's copies (clock64) and the start of the step on the global timer
-// (ns); the stamps after the last step close the sweep.
-// trace layout: [blocks][FC_TRACE_N] phase cycles, then
-// [2 sweeps][blocks][tl_cap][4] step stamps.
+// (the forward and backward sweep of iteration 1) FC_TRACE_STAMPS stamps per
+// step of the tile: [0] the compute warps' start of the step (clock64), [1]
+// the moment its stage buffer had landed, [2] the staging thread's start of
+// the step's copies, [3] the start of the step on the global timer (ns),
+// and thread 0's progress through its row: [4] the next step's loads
+// issued, [5] the row's dependency values in registers, [6] its value
+// computed, [7] its stores issued; the stamps after the last step close the
+// sweep.  trace layout: [blocks][FC_TRACE_N] phase cycles, then
+// [2 sweeps][blocks][tl_cap][FC_TRACE_STAMPS] step stamps.
 struct Tracer {
   unsigned long long* out;
   int tl_cap, nsweep;
@@ -87,7 +90,16 @@ struct Tracer {
   }
   __device__ __forceinline__ void sweep() { ++nsweep; }
   __device__ __forceinline__ unsigned long long* slot(int k) {
-    return out + (size_t)gridDim.x * FC_TRACE_N + (((size_t)(nsweep - 1) * gridDim.x + blockIdx.x) * tl_cap + k) * 4;
+    return out + (size_t)gridDim.x * FC_TRACE_N +
+           (((size_t)(nsweep - 1) * gridDim.x + blockIdx.x) * tl_cap + k) * FC_TRACE_STAMPS;
+  }
+  // stamp idx of step k, taken once dep is available (thread 0)
+  template <class V>
+  __device__ __forceinline__ void at(int k, int idx, V dep) {
+    if (threadIdx.x != 0 || nsweep > 2 || k >= tl_cap) return;
+    unsigned long long c;
+    asm volatile("mov.u64 %0, %%clock64;" : "=l"(c) : "l"((unsigned long long)(long long)dep) : "memory");
+    slot(k)[idx] = c;
   }
   __device__ __forceinline__ void step(int k) {
     if (threadIdx.x != 0 || nsweep > 2 || k >= tl_cap) return;
@@ -999,7 +1011,7 @@ static int solve_fp64(fc_ctx* ctx, CsrSystem* s, const std::string& solver, cons
   if (traced) {
     const int nb = std::max(1, ctx->num_sms);
     const int cap = s->ord.max_tile_steps + 1;
-    FC_CUDA_TRY(ctx, ctx->trace.alloc((size_t)nb * FC_TRACE_N + (size_t)2 * nb * cap * 4));
+    FC_CUDA_TRY(ctx, ctx->trace.alloc((size_t)nb * FC_TRACE_N + (size_t)2 * nb * cap * FC_TRACE_STAMPS));
     FC_CUDA_TRY(ctx, cudaMemsetAsync(ctx->trace.p, 0, ctx->trace.bytes(), ctx->stream));
     A.trace = ctx->trace.p;
     A.trace_cap = cap;
@@ -1424,8 +1436,7 @@ int sys_precond(fc_ctx* ctx, CsrSystem* s, int dilu, const double* q, double* z_
 // out[0..FC_TRACE_N) = cycles summed over the blocks that ran, per phase;
 // out[FC_TRACE_N] = those blocks; out[FC_TRACE_N+1] = blocks of the launch
 // (B); out[FC_TRACE_N+2] = stamps per tile and sweep (K); with timeline
-// non-null it receives the stamps as [2][B][K][4] (step start, buffer
-// landed, staging start: clock64; step start: globaltimer).
+// non-null it receives the stamps as [2][B][K][FC_TRACE_STAMPS] (see Tracer).
 extern "C" int fc_trace_get(fc_ctx* ctx, double* out, unsigned long long* timeline) {
   if (!ctx || !out) return FC_ERR_BAD_INPUT;
   if (!ctx->trace.p) return fc_fail_msg(ctx, FC_ERR_STATE, "no trace recorded");

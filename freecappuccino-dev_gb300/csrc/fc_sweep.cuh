@@ -23,10 +23,15 @@
 // Exchange: a value a row needs from another tile (or from more than R-1
 // steps back) is pushed by its producer into the consumer's slot of the
 // exchange array xv, whose slots start every sweep at a sentinel NaN.  The
-// staged copy is used when it already holds the value, else the slot is
-// polled (bounded) until the producer's store arrives; the consumer puts the
-// sentinel back after use.  Bulk copies read through L2, so staged data is
-// never an SM's stale L1 line.
+// static data of a step is staged many steps ahead, but exchanged values
+// are not: a copy taken that early is stale, and every stale value costs
+// the consumer an L2 round trip on its critical path and, through the lag
+// it builds up, delays every tile downstream.  Instead each compute thread
+// loads the exchanged values of its row of the next step from global memory
+// while it works on the current one (relaxed loads through L2); a value
+// that still reads as the sentinel is polled (bounded) until the producer's
+// store arrives.  The consumer puts the sentinel back after use.  Bulk
+// copies read through L2, so staged data is never an SM's stale L1 line.
 #pragma once
 #include "fc_krylov.cuh"
 #include "fc_schedule.hpp"
@@ -158,7 +163,7 @@ struct StageLayout {
     oV2 = take(gs, (int)sizeof(T) * Rec<T>::V * W);
     oQ = take(kq, (int)sizeof(T) * Wp);
     oE = take(ke, (int)sizeof(T) * Wp);
-    oXV = take(true, (int)sizeof(T) * xmax);
+    oXV = take(false, (int)sizeof(T) * xmax);  // exchanged values are not staged (see the file header)
     oP = take(true, 4 * pmax);
     bytes = o;
   }
@@ -333,11 +338,11 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
         const int ls = step_of(k);
         const int base = sp[ls], cnt = sp[ls + 1] - base;
         const int b0 = base & ~3, nw = ((base + cnt + 3) & ~3) - b0;
-        const int x0 = xp[ls], nx = xp[ls + 1] - x0, p0 = pp[ls], np = pp[ls + 1] - p0;
+        const int p0 = pp[ls], np = pp[ls + 1] - p0;
         unsigned char* B = X.stage + (size_t)b * L.bytes;
         unsigned long long* mb = X.full + b;
         const unsigned vb = (unsigned)(sizeof(T) * VR) * cnt;
-        unsigned bytes = 16u * cnt + vb + (unsigned)sizeof(T) * nx + 4u * np;
+        unsigned bytes = 16u * cnt + vb + 4u * np;
         if (kSetup || kGS) bytes += vb;
         if (kGS) bytes += 16u * cnt + vb;
         if (kQ) bytes += (unsigned)sizeof(T) * nw;
@@ -353,7 +358,6 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
         }
         if (kQ) bulk_g2s(B + L.oQ, io.q + b0, (unsigned)sizeof(T) * nw, mb);
         if (kE) bulk_g2s(B + L.oE, io.e + b0, (unsigned)sizeof(T) * nw, mb);
-        if (nx) bulk_g2s(B + L.oXV, xv + x0, (unsigned)sizeof(T) * nx, mb);
         if (np) bulk_g2s(B + L.oP, O.push[dirn] + p0, 4u * np, mb);
         X.parity ^= 1u << b;
         X.used |= 1u << b;
@@ -365,6 +369,40 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
     // part; the others skip the sweep, so they add no shared-memory traffic
     // and no barrier arrivals to the steps.
     const int kmask = K - 1;  // K and R are powers of two
+    // the exchanged values of this thread's first row of step k, loaded
+    // during step k-1 (pf_ok), and whether step k's buffer was waited for then
+    T pf[FC_ELL];
+    bool pf_ok = false, pre_waited = false;
+#pragma unroll
+    for (int e = 0; e < FC_ELL; ++e) pf[e] = T(0);
+    // wait for step kk's buffer (warps with rows in it) and load the
+    // exchanged values of row threadIdx.x of that step into pf
+    auto prefetch = [&](int kk) {
+      const int lsk = step_of(kk);
+      const int bk = kk & kmask, basek = sp[lsk], cntk = sp[lsk + 1] - basek;
+      pf_ok = false;
+      pre_waited = false;
+      if ((int)(threadIdx.x & ~31u) >= cntk) return;
+      if (!mbar_wait(X.full + bk, (X.parity >> bk) & 1u)) {
+        atomicCAS(C.status, 0, FC_ERR_TIMEOUT);
+        *((volatile int*)X.abort_flag) = 1;
+      }
+      pre_waited = true;
+      if ((int)threadIdx.x >= cntk) return;
+      const int4 sr = ((const int4*)(X.stage + (size_t)bk * L.bytes + L.oS))[threadIdx.x];
+      const int ne = sr.x & 255, xoff = (int)((unsigned)sr.x >> 16);
+      const unsigned cw[2] = {(unsigned)sr.z, (unsigned)sr.w};
+      const T* src = xv + xp[lsk] + xoff;
+      int m = 0;
+#pragma unroll
+      for (int e = 0; e < FC_ELL; ++e) {
+        const bool ex = ((cw[e >> 1] >> (16 * (e & 1))) & 0xFFFFu) == 0 && e < ne;
+        pf[e] = ex ? Sentinel<T>::poll(src + m) : T(0);
+        m += ex ? 1 : 0;
+      }
+      pf_ok = true;
+    };
+    if (ns > 0) prefetch(0);
     for (int k = 0; k < ns; ++k) {
       if (tr) tr->step(k);
       const int b = k & kmask;
@@ -372,16 +410,23 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
       const int base = sp[ls], cnt = sp[ls + 1] - base, woff = base - (base & ~3);
       // only warps with rows in this step read the buffer, so only they wait
       // for it (an mbarrier poll by every warp would serialise on its word)
-      if ((int)(threadIdx.x & ~31u) < cnt && !mbar_wait(X.full + b, (X.parity >> b) & 1u)) {
+      if (!pre_waited && (int)(threadIdx.x & ~31u) < cnt && !mbar_wait(X.full + b, (X.parity >> b) & 1u)) {
         atomicCAS(C.status, 0, FC_ERR_TIMEOUT);
         *((volatile int*)X.abort_flag) = 1;
       }
       if (tr) tr->waited(k);
+      const bool have_pf = pf_ok;
+      T pfk[FC_ELL];
+#pragma unroll
+      for (int e = 0; e < FC_ELL; ++e) pfk[e] = pf[e];
+      // the next step's exchanged values are loaded while this one runs
+      if (k + 1 < ns) prefetch(k + 1);
+      else { pf_ok = false; pre_waited = false; }
+      if (tr) tr->at(k, 4, (int)pf_ok);
       const int xbase = xp[ls];
       const unsigned char* B = X.stage + (size_t)b * L.bytes;
       const int4* S4 = (const int4*)(B + L.oS);
       const T* VRc = (const T*)(B + L.oV);
-      const T* XS = (const T*)(B + L.oXV);
       const int* PS = (const int*)(B + L.oP);
       T* ring_out = ring + (k & (R - 1)) * W;
       for (int sl = threadIdx.x; sl < cnt; sl += ncg) {
@@ -390,26 +435,28 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
         const int ne = sr.x & 255, np = (sr.x >> 8) & 255, xoff = (int)((unsigned)sr.x >> 16), poff = sr.y;
         const T* vr = VRc + sl * VR;
         // dependency values of entries 0..3 without branches: entries past
-        // ne have code 0 and coefficient 0 and read exchange slot xoff (in
-        // bounds of the staged block or the padding), so they contribute an
-        // exact zero; ring (code > 0) or exchange block (code 0) by select
+        // ne have code 0 and coefficient 0, so they contribute an exact
+        // zero; ring (code > 0) or exchanged value (code 0) by select.  The
+        // thread's first row takes its exchanged values from the loads of
+        // the previous step, every other row polls them below.
         const unsigned cw[2] = {(unsigned)sr.z, (unsigned)sr.w};
+        const bool mine = have_pf && sl == (int)threadIdx.x;
         T dv[FC_ELL];
-        unsigned xmask = 0;  // entries that come through the exchange block
+        unsigned xmask = 0;  // entries that come through the exchange array
         int m = 0;
 #pragma unroll
         for (int e = 0; e < FC_ELL; ++e) {
           const int c1 = (int)((cw[e >> 1] >> (16 * (e & 1))) & 0xFFFFu);  // code + 1
           const bool ex = c1 == 0 && e < ne;
           const T rv = ring[c1 > 0 ? c1 - 1 : 0];
-          const T xv_ = XS[xoff + m];
+          const T xv_ = mine ? pfk[e] : Sentinel<T>::value();
           dv[e] = c1 > 0 ? rv : (ex ? xv_ : T(0));
           xmask |= (ex ? 1u : 0u) << e;
           m += ex ? 1 : 0;
         }
         if (xmask) {
-          // exchanged values: poll the slot if the staged copy was taken
-          // before the producer's store, and put the sentinel back
+          // exchanged values: poll the slot if the early load came before
+          // the producer's store, and put the sentinel back
           int mm = 0;
 #pragma unroll
           for (int e = 0; e < FC_ELL; ++e)
@@ -421,14 +468,14 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
               ++mm;
             }
         }
+        if (tr && sl == 0) tr->at(k, 5, __double_as_longlong((double)dv[0] + (double)dv[1] + (double)dv[2]));
         // overflow entry e >= FC_ELL: its value and coefficient
         auto dep_ovf = [&](int e, T& a) -> T {
           const int o = __ldg(O.ovf_ptr[dirn] + q) + e - FC_ELL;
           a = __ldg(V.aovf[dirn] + o);
           const int c = __ldg(O.ovf_code[dirn] + o);
           if (c >= 0) return ring[c];
-          T v = XS[xoff + m];
-          if (Sentinel<T>::is(v)) v = xv_wait<T>(C, xv + xbase + xoff + m, X.abort_flag);
+          const T v = xv_wait<T>(C, xv + xbase + xoff + m, X.abort_flag);
           xv[xbase + xoff + m] = Sentinel<T>::value();
           ++m;
           return v;
@@ -510,11 +557,13 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
           val = acc * di;
           if (MODE == OS_BWD_DOT) red[0] += (double)((const T*)(B + L.oE))[woff + sl] * (double)val;
         }
+        if (tr && sl == 0) tr->at(k, 6, __double_as_longlong((double)val));
         io.out[q] = val;
         ring_out[sl] = val;
         // plain stores: an aligned 8-byte (4-byte) store is single-copy
         // atomic, so a consumer polling the slot sees the sentinel or the value
         for (int mm = 0; mm < np; ++mm) xv[PS[poff + mm]] = val;
+        if (tr && sl == 0) tr->at(k, 7, np);
       }
       bar_compute(ncg);
       if (threadIdx.x == 0) mbar_arrive(X.empty + b);

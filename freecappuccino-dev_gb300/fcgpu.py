@@ -612,9 +612,10 @@ class Context:
     def trace(self, timeline=False):
         """Phase cycles of the last traced ICCG solve: (dict phase -> cycles
         summed over blocks, blocks); with timeline=True also the step stamps
-        as a uint64 array [sweep(fwd, bwd)][tile][step][4]: step start,
+        as a uint64 array [sweep(fwd, bwd)][tile][step][8]: step start,
         stage buffer landed, staging started (clock64), step start
-        (globaltimer)."""
+        (globaltimer), then thread 0's next-step loads issued, dependency
+        values ready, value computed, stores issued (clock64)."""
         out = np.zeros(11)
         self._check(self.L.fc_trace_get(self.h, _ptr(out), None), "fc_trace_get")
         keys = ("setup", "fwd_sweep", "sweep_barrier", "bwd_sweep", "dot", "p_update", "spmv", "xr_update")
@@ -622,7 +623,7 @@ class Context:
         if not timeline:
             return res
         nb, cap = int(out[9]), int(out[10])
-        tl = np.zeros((2, nb, cap, 4), dtype=np.uint64)
+        tl = np.zeros((2, nb, cap, 8), dtype=np.uint64)
         self._check(self.L.fc_trace_get(self.h, _ptr(out), _ptr(tl)), "fc_trace_get")
         return res + (tl,)
 

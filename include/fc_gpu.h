@@ -242,10 +242,12 @@ int fc_batch_tune(fc_batch* b, const char* solver, const double* const* a, const
  * out[11] = cycles summed over the blocks for setup, forward sweep, sweep
  * barrier, backward sweep, dot product, p update, SpMV, x/r update; then the
  * blocks that ran, the blocks of the launch (B) and the stamps per tile (K);
- * timeline (optional, 2*B*K*4 entries) receives the stamps as
- * [sweep][tile][step][4]: the compute warps' start of the step, the moment
+ * timeline (optional, 2*B*K*8 entries) receives the stamps as
+ * [sweep][tile][step][8]: the compute warps' start of the step, the moment
  * its staged data had landed, the staging thread's start of its copies
- * (clock64 of the tile's SM) and the step start on the global timer.  With
+ * (clock64 of the tile's SM), the step start on the global timer, then
+ * thread 0's next-step loads issued, its row's dependencies ready, its value
+ * computed and its stores issued (clock64).  With
  * tracing on, the multicolour inner solve of FC_PREC_MIXED_COLOURED launches
  * its kernels from the host instead of its CUDA graph, so that a profiler
  * sees each launch. */

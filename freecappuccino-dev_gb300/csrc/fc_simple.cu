@@ -439,9 +439,51 @@ __global__ void k_p_face(MeshView M, Dev D) {
   }
 }
 
+// facefluxmassPressBnd, faceflux_mass.f90:765-830, per pressure face:
+// boundary velocity, mass flux and the face's coefficient cap of the
+// pressure-correction equation (kept in bcap for k_p_cell); pp = 0 at the
+// face (calcp_simple.f90:162-183)
+__global__ void k_p_press(MeshView M, Dev D, double* __restrict__ bcap) {
+  const Fld gp{D.gp, M.nT};
+  for (int bi = blockIdx.x * blockDim.x + threadIdx.x; bi < M.nB; bi += gridDim.x * blockDim.x) {
+    if (D.ptype[M.bpatch[bi]] != FC_BC_PRESSURE) continue;
+    const int f = M.nI + bi, ijp = M.owner[f], ijb = M.nC + bi;
+    const double arx = M.arx[f], ary = M.ary[f], arz = M.arz[f];
+    const double xpn = M.xf[f] - M.xc[ijp], ypn = M.yf[f] - M.yc[ijp], zpn = M.zf[f] - M.zc[ijp];
+    const double capp = M.vol[ijp] * D.apu[ijp] / (arx * xpn + ary * ypn + arz * zpn);
+    const double dpcor = D.p[ijb] - D.p[ijp] - (gp.x(ijp) * xpn + gp.y(ijp) * ypn + gp.z(ijp) * zpn);
+    const double ub = D.u[ijp] - arx * capp * dpcor;
+    const double vb = D.v[ijp] - ary * capp * dpcor;
+    const double wb = D.w[ijp] - arz * capp * dpcor;
+    D.u[ijb] = ub; D.v[ijb] = vb; D.w[ijb] = wb;
+    D.flmass[f] = D.den[ijp] * (ub * arx + vb * ary + wb * arz);
+    bcap[bi] = -(D.den[ijp] * (arx * arx + ary * ary + arz * arz) * capp);
+    D.pp[ijb] = 0.0;
+  }
+}
+
+// facefluxmassCorrPressBnd, faceflux_mass.f90:699-762, per pressure face
+// after a pressure-correction solve (calcp_simple.f90:344-356)
+__global__ void k_p_press_corr(MeshView M, Dev D) {
+  for (int bi = blockIdx.x * blockDim.x + threadIdx.x; bi < M.nB; bi += gridDim.x * blockDim.x) {
+    if (D.ptype[M.bpatch[bi]] != FC_BC_PRESSURE) continue;
+    const int f = M.nI + bi, ijp = M.owner[f], ijb = M.nC + bi;
+    const double arx = M.arx[f], ary = M.ary[f], arz = M.arz[f];
+    const double xpn = M.xf[f] - M.xc[ijp], ypn = M.yf[f] - M.yc[ijp], zpn = M.zf[f] - M.zc[ijp];
+    const double cap = M.vol[ijp] * D.apu[ijp] / (arx * xpn + ary * ypn + arz * zpn);
+    const double dpcor = -D.pp[ijp];
+    D.u[ijb] = D.u[ijb] - arx * cap * dpcor;
+    D.v[ijb] = D.v[ijb] - ary * cap * dpcor;
+    D.w[ijb] = D.w[ijb] - arz * cap * dpcor;
+    D.flmass[f] = D.flmass[f] - D.den[ijp] * (arx * arx + ary * ary + arz * arz) * cap * dpcor;
+  }
+}
+
 // diagonal -sum(cap) and source -/+flmass in face order (calcp_simple.f90:104-117),
-// then inlet/outlet mass fluxes (:131-151)
-__global__ void k_p_cell(MeshView M, Dev D) {
+// then inlet/outlet mass fluxes and pressure faces (:131-183); a cell's
+// boundary faces follow its inner faces and come in patch order, the order
+// of the reference's loops
+__global__ void k_p_cell(MeshView M, Dev D, const double* __restrict__ bcap) {
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
     double ad = 0.0, s = 0.0;
     for (int q = M.cf_ptr[c]; q < M.cf_ptr[c + 1]; ++q) {
@@ -453,6 +495,10 @@ __global__ void k_p_cell(MeshView M, Dev D) {
       } else {
         const int t = D.ptype[M.bpatch[f - M.nI]];
         if (t == FC_BC_INLET || t == FC_BC_OUTLET) s = s - D.flmass[f];
+        else if (t == FC_BC_PRESSURE) {
+          ad = ad - bcap[f - M.nI];
+          s = s - D.flmass[f];
+        }
       }
     }
     D.a[M.diag[c]] = ad;
@@ -908,7 +954,7 @@ void fc_simple_release(fc_ctx* ctx) {
 
 static inline int gridn(int n) { return std::max(1, std::min(65535, (n + 255) / 256)); }
 
-static int make_dev(fc_ctx* ctx, Dev& D, bool allow_pressure = false) {
+static int make_dev(fc_ctx* ctx, Dev& D, bool allow_pressure = true) {
   FieldStore& F = ctx_fields(ctx);
   SimpleState& S = sstate(ctx);
   const MeshDev& m = ctx->mesh;
@@ -922,7 +968,7 @@ static int make_dev(fc_ctx* ctx, Dev& D, bool allow_pressure = false) {
     if (m.h_bctype[b] == FC_BC_PERIODIC)
       return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "periodic boundaries are not supported on this path");
     if (m.h_bctype[b] == FC_BC_PRESSURE && !allow_pressure)
-      return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "pressure boundaries are not supported on this path");
+      return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "pressure boundaries are not supported by the PISO corrector");
   }
   D.u = F.u.p; D.v = F.v.p; D.w = F.w.p; D.p = F.p.p; D.pp = F.pp.p; D.vis = F.vis.p; D.den = F.den.p;
   D.flmass = F.flmass.p; D.visw = F.visw.p;
@@ -1159,8 +1205,9 @@ extern "C" int fc_calcuvw(fc_ctx* ctx, double* resor) {
   return FC_OK;
 }
 
-// calcp_simple, calcp_simple.f90:1-470 (incompressible; no periodic or
-// pressure boundaries).  *resor4 receives resor(4) as continuityErrors sets it.
+// calcp_simple, calcp_simple.f90:1-470 (incompressible; pressure
+// boundaries, no periodic pairs).  *resor4 receives resor(4) as
+// continuityErrors sets it.
 // continuityErrors, continuityErrors.f90:1-77: resor(4) into *resor4
 static int continuity_errors(fc_ctx* ctx, const Dev& D, double* resor4) {
   SimpleState& S = sstate(ctx);
@@ -1191,27 +1238,39 @@ extern "C" int fc_calcp_simple(fc_ctx* ctx, double* resor4) {
   SimpleState& S = sstate(ctx);
   if (!S.have_prm) return fc_fail_msg(ctx, FC_ERR_STATE, "fc_simple_set_params not called");
   Dev D;
-  int st = make_dev(ctx, D);
+  int st = make_dev(ctx, D, true);
   if (st) return st;
   const fc_simple_params& P = S.prm;
   MeshView M = mesh_view(ctx);
   if (M.nI) k_p_face<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D);
-  bool outlets = false;
-  for (int b = 0; b < ctx->mesh.numBoundaries; ++b) outlets |= ctx->mesh.h_bctype[b] == FC_BC_OUTLET;
+  bool outlets = false, pressure = false;
+  for (int b = 0; b < ctx->mesh.numBoundaries; ++b) {
+    outlets |= ctx->mesh.h_bctype[b] == FC_BC_OUTLET;
+    pressure |= ctx->mesh.h_bctype[b] == FC_BC_PRESSURE;
+  }
   if (outlets) k_adjust_mass_flow<<<1, 32, 0, ctx->stream>>>(M, D, P.flomas);
-  k_p_cell<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D);
-  ctx->kernel_launches += 2 + outlets;
+  // the pressure faces' coefficients, one per boundary face, in the face
+  // scratch (free during calcp_simple)
+  double* bcap = D.fscr;
+  if (pressure) k_p_press<<<gridn(M.nB), 256, 0, ctx->stream>>>(M, D, bcap);
+  k_p_cell<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D, bcap);
+  ctx->kernel_launches += 2 + outlets + pressure;
   FC_CUDA_TRY(ctx, cudaGetLastError());
   double r4 = 0;
   for (int ipcorr = 1; ipcorr <= P.npcor; ++ipcorr) {
     st = solve_into(ctx, P.lSolverP, D.pp, D.su, &r4, P.maxiterP, P.tolAbsP, P.tolRelP, "p");
     if (st < 0) return st;
     if (M.nI) k_flux_correct<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D);
+    if (pressure) {
+      k_p_press_corr<<<gridn(M.nB), 256, 0, ctx->stream>>>(M, D);
+      ctx->kernel_launches++;
+    }
     // ppref = pp(pRefCell) before gradp_and_sources(pp), which only touches
-    // boundary values of pp
+    // boundary values of pp; with a pressure boundary the reference p' is 0
+    // (calcp_simple.f90:363-369)
     if ((st = gradp_and_sources(ctx, D, D.pp, P.pscheme))) return st;
     const int pref = std::max(0, std::min(M.nC - 1, P.pRefCell - 1));
-    k_correct_vel_p<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, D, P.urfP, pref, 1);
+    k_correct_vel_p<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, D, P.urfP, pref, pressure ? 0 : 1);
     ctx->kernel_launches += 2;
     update_velocity_at_boundary(ctx, D);
     if (ipcorr != P.npcor) {
@@ -1270,7 +1329,7 @@ extern "C" int fc_calcp_piso(fc_ctx* ctx, double* resor4) {
   if (!S.have_prm) return fc_fail_msg(ctx, FC_ERR_STATE, "fc_simple_set_params not called");
   if (!S.trp.piso) return fc_fail_msg(ctx, FC_ERR_STATE, "fc_calcp_piso: PISO not enabled (fc_transient_set_params)");
   Dev D;
-  int st = make_dev(ctx, D);
+  int st = make_dev(ctx, D, false);
   if (st) return st;
   const fc_simple_params& P = S.prm;
   MeshView M = mesh_view(ctx);
@@ -1287,7 +1346,7 @@ extern "C" int fc_calcp_piso(fc_ctx* ctx, double* resor4) {
     k_piso_u<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, D);
     if (M.nI) k_piso_face<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D);
     if (outlets) k_adjust_mass_flow<<<1, 32, 0, ctx->stream>>>(M, D, P.flomas);
-    k_p_cell<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D);
+    k_p_cell<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D, D.fscr);
     ctx->kernel_launches += 4 + outlets;
     FC_CUDA_TRY(ctx, cudaGetLastError());
     for (int ipcorr = 1; ipcorr <= P.npcor; ++ipcorr) {

@@ -1046,8 +1046,37 @@ void continuityErrors(Case& c) {
   c.resor[4] = wavg;
 }
 
-// calcp_simple, calcp_simple.f90:1-470 for incompressible SIMPLE without
-// periodic or pressure boundaries.
+// facefluxmassPressBnd, faceflux_mass.f90:765-830: mass flux and boundary
+// velocity through a pressure face, and its coefficient of the
+// pressure-correction equation
+static void facefluxmassPressBnd(Case& c, int ijp, int ijb, double xf, double yf, double zf, double arx, double ary,
+                                 double arz, double& cap, double& fluxmass) {
+  double xpn = xf - c.xc[ijp], ypn = yf - c.yc[ijp], zpn = zf - c.zc[ijp];
+  double capp = c.vol[ijp] * c.apu[ijp] / (arx * xpn + ary * ypn + arz * zpn);
+  double dpcor = c.p[ijb] - c.p[ijp] -
+                 (G(c.dPdxi, 1, ijp) * xpn + G(c.dPdxi, 2, ijp) * ypn + G(c.dPdxi, 3, ijp) * zpn);
+  c.u[ijb] = c.u[ijp] - arx * capp * dpcor;
+  c.v[ijb] = c.v[ijp] - ary * capp * dpcor;
+  c.w[ijb] = c.w[ijp] - arz * capp * dpcor;
+  fluxmass = c.den[ijp] * (c.u[ijb] * arx + c.v[ijb] * ary + c.w[ijb] * arz);
+  cap = -c.den[ijp] * (arx * arx + ary * ary + arz * arz) * capp;
+}
+
+// facefluxmassCorrPressBnd, faceflux_mass.f90:699-762: p' is zero at a
+// pressure face, so the correction is driven by -pp(ijp)
+static void facefluxmassCorrPressBnd(Case& c, int ijp, int ijb, double xf, double yf, double zf, double arx,
+                                     double ary, double arz, double& fluxmass) {
+  double xpn = xf - c.xc[ijp], ypn = yf - c.yc[ijp], zpn = zf - c.zc[ijp];
+  double cap = c.vol[ijp] * c.apu[ijp] / (arx * xpn + ary * ypn + arz * zpn);
+  double dpcor = -c.pp[ijp];
+  c.u[ijb] = c.u[ijb] - arx * cap * dpcor;
+  c.v[ijb] = c.v[ijb] - ary * cap * dpcor;
+  c.w[ijb] = c.w[ijb] - arz * cap * dpcor;
+  fluxmass = fluxmass - c.den[ijp] * (arx * arx + ary * ary + arz * arz) * cap * dpcor;
+}
+
+// calcp_simple, calcp_simple.f90:1-470 for incompressible SIMPLE, with
+// pressure boundaries (:162-183, :344-356, :363-369); no periodic pairs.
 int calcp_simple(Case& c) {
   const int nC = c.numCells;
   std::fill(c.a.begin(), c.a.end(), 0.0);
@@ -1064,11 +1093,24 @@ int calcp_simple(Case& c) {
     c.su[ijn] = c.su[ijn] + c.flmass[i];
   }
   adjustMassFlow(c);
+  bool have_pressure = false;
   for (int ib = 1; ib <= c.numBoundaries; ++ib) {
-    if (c.bctype[ib] != BC_INLET && c.bctype[ib] != BC_OUTLET) continue;
-    for (int i = 1; i <= c.nfaces[ib]; ++i) {
-      int iface = c.startFace[ib] + i, ijp = c.owner[iface];
-      c.su[ijp] = c.su[ijp] - c.flmass[iface];
+    if (c.bctype[ib] == BC_INLET || c.bctype[ib] == BC_OUTLET) {
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int iface = c.startFace[ib] + i, ijp = c.owner[iface];
+        c.su[ijp] = c.su[ijp] - c.flmass[iface];
+      }
+    } else if (c.bctype[ib] == BC_PRESSURE) {
+      have_pressure = true;
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
+        double cap;
+        facefluxmassPressBnd(c, ijp, ijb, c.xf[iface], c.yf[iface], c.zf[iface], c.arx[iface], c.ary[iface],
+                             c.arz[iface], cap, c.flmass[iface]);
+        c.a[c.diag[ijp]] = c.a[c.diag[ijp]] - cap;
+        c.su[ijp] = c.su[ijp] - c.flmass[iface];
+        c.pp[ijb] = 0.0;
+      }
     }
   }
   int worst = 0;
@@ -1080,7 +1122,16 @@ int calcp_simple(Case& c) {
       int ijp = c.owner[iface], ijn = c.neighbour[iface];
       c.flmass[iface] = c.flmass[iface] + c.a[c.ijk[iface]] * (c.pp[ijn] - c.pp[ijp]);
     }
-    double ppref = c.pp[c.pRefCell];
+    for (int ib = 1; ib <= c.numBoundaries; ++ib) {
+      if (c.bctype[ib] != BC_PRESSURE) continue;
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
+        facefluxmassCorrPressBnd(c, ijp, ijb, c.xf[iface], c.yf[iface], c.zf[iface], c.arx[iface], c.ary[iface],
+                                 c.arz[iface], c.flmass[iface]);
+      }
+    }
+    // with a pressure boundary the reference p' is zero (:363-369)
+    double ppref = have_pressure ? 0.0 : c.pp[c.pRefCell];
     gradp_and_sources(c, c.pp);
     for (int i = 1; i <= nC; ++i) c.u[i] = c.u[i] + c.su[i] * c.apu[i];
     for (int i = 1; i <= nC; ++i) c.v[i] = c.v[i] + c.sv[i] * c.apv[i];

@@ -136,7 +136,7 @@ static int adj_state(fc_ctx* ctx, AdjState*& S) {
       tm[k] = (int)(p - s->h_ja.data());
     }
   FC_CUDA_TRY(ctx, S->tmap.alloc(nnz));
-  FC_CUDA_TRY(ctx, cudaMemcpy(S->tmap.p, tm.data(), nnz * sizeof(int), cudaMemcpyHostToDevice));
+  FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, S->tmap.p, tm.data(), nnz * sizeof(int)));
   DVec<double>* nv[] = {&S->gam, &S->phi, &S->lam, &S->rhs, &S->grad};
   for (auto* v : nv) FC_CUDA_TRY(ctx, v->alloc(n));
   FC_CUDA_TRY(ctx, S->aT.alloc(nnz));

@@ -123,7 +123,7 @@ static int ext_system(fc_ctx* ctx, int n, int nnz, const int* ia, const int* ja,
   if (ctx->has_mesh && ctx->sys_mesh && n == ctx->sys_mesh->n && nnz == ctx->sys_mesh->nnz) {
     std::vector<int> hia(n + 1), hja(nnz), hdg(n);
     auto get = [&](const int* src, int* dst, size_t cnt) {
-      if (is_device_ptr(src)) return cudaMemcpy(dst, src, cnt * sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess;
+      if (is_device_ptr(src)) return fc_d2h(ctx->stream, dst, src, cnt * sizeof(int)) == cudaSuccess;
       std::memcpy(dst, src, cnt * sizeof(int));
       return true;
     };

@@ -198,7 +198,7 @@ extern "C" int fc_batch_add(fc_batch* b, int n, int nnz, const int* ia, const in
   q.dg.resize(n);
   auto fetch = [&](const void* src, void* dst, size_t bytes) -> int {
     if (is_device_ptr(src)) {
-      cudaError_t e = cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost);
+      cudaError_t e = fc_d2h(ctx->stream, dst, src, bytes);
       if (e != cudaSuccess) return fc_fail(ctx, FC_ERR_CUDA, "fc_batch_add: pattern copy", e);
     } else {
       std::memcpy(dst, src, bytes);

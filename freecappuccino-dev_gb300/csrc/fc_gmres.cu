@@ -309,9 +309,9 @@ static int build_transpose(fc_ctx* ctx, CsrSystem* s) {
   FC_CUDA_TRY(ctx, s->tptr.alloc(n + 1));
   FC_CUDA_TRY(ctx, s->tsrc.alloc(nnz));
   FC_CUDA_TRY(ctx, s->trow.alloc(nnz));
-  FC_CUDA_TRY(ctx, cudaMemcpy(s->tptr.p, ptr.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
-  FC_CUDA_TRY(ctx, cudaMemcpy(s->tsrc.p, src.data(), nnz * sizeof(int), cudaMemcpyHostToDevice));
-  FC_CUDA_TRY(ctx, cudaMemcpy(s->trow.p, row.data(), nnz * sizeof(int), cudaMemcpyHostToDevice));
+  FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, s->tptr.p, ptr.data(), (n + 1) * sizeof(int)));
+  FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, s->tsrc.p, src.data(), nnz * sizeof(int)));
+  FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, s->trow.p, row.data(), nnz * sizeof(int)));
   return FC_OK;
 }
 

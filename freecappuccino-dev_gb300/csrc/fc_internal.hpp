@@ -22,6 +22,23 @@ constexpr double FC_S0 = static_cast<double>(1.e20f);
     if (_e != cudaSuccess) return fc_fail((ctx), FC_ERR_CUDA, #expr, _e);       \
   } while (0)
 
+// Copies and fills of the library are ordered on the context's stream.  That
+// stream is created non-blocking, so work that cudaMemcpy and cudaMemset put
+// on the legacy default stream would not be ordered against the library's
+// kernels.  A pageable host source is staged before fc_h2d returns, so it may
+// be freed at once; fc_d2h waits for the copy.
+inline cudaError_t fc_h2d(cudaStream_t s, void* dst, const void* src, size_t bytes) {
+  return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) : cudaSuccess;
+}
+inline cudaError_t fc_d2h(cudaStream_t s, void* dst, const void* src, size_t bytes) {
+  if (!bytes) return cudaSuccess;
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s);
+  return e != cudaSuccess ? e : cudaStreamSynchronize(s);
+}
+inline cudaError_t fc_zero(cudaStream_t s, void* dst, size_t bytes) {
+  return bytes ? cudaMemsetAsync(dst, 0, bytes, s) : cudaSuccess;
+}
+
 // Count of the library's device allocations and frees (every device buffer
 // goes through DVec), read by fc_device_alloc_count.
 void fc_count_device_alloc();

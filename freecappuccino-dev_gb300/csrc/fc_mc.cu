@@ -629,7 +629,7 @@ static int mc_prepare(fc_ctx* ctx, CsrSystem* s) {
   }
   auto up = [&](DVec<int>& d, const std::vector<int>& h) -> int {
     FC_CUDA_TRY(ctx, d.alloc(std::max<size_t>(1, h.size())));
-    if (!h.empty()) FC_CUDA_TRY(ctx, cudaMemcpy(d.p, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
+    FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, d.p, h.data(), h.size() * sizeof(int)));
     return FC_OK;
   };
   int st = 0;
@@ -651,8 +651,8 @@ static int mc_prepare(fc_ctx* ctx, CsrSystem* s) {
     return fc_fail_msg(ctx, FC_ERR_NOMEM, "multicolour buffers");
   }
   // padding entries keep the value 0 (the setup writes real entries only)
-  FC_CUDA_TRY(ctx, cudaMemset(m->mval.p, 0, ne * sizeof(float)));
-  FC_CUDA_TRY(ctx, cudaMemset(m->cnt.p, 0, sizeof(unsigned)));
+  FC_CUDA_TRY(ctx, fc_zero(ctx->stream, m->mval.p, ne * sizeof(float)));
+  FC_CUDA_TRY(ctx, fc_zero(ctx->stream, m->cnt.p, sizeof(unsigned)));
   {
     int nb = 0;  // resident blocks per SM of the widest body kernel
     FC_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_e2_c0, MCG_BLOCK, 0));

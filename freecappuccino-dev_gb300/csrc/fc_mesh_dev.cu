@@ -159,7 +159,7 @@ void fc_release_mesh(fc_ctx* ctx) {
 template <class T>
 static int up(fc_ctx* ctx, DVec<T>& d, const T* h, size_t n) {
   FC_CUDA_TRY(ctx, d.alloc(n));
-  if (n) FC_CUDA_TRY(ctx, cudaMemcpy(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice));
+  FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, d.p, h, n * sizeof(T)));
   return FC_OK;
 }
 
@@ -301,12 +301,12 @@ extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
   for (auto& v : ja1) ++v;
   for (auto& v : dg1) ++v;
   m.h_xyz.resize((size_t)3 * nC);
-  FC_CUDA_TRY(ctx, cudaMemcpy(m.h_xyz.data(), m.xc.p, nC * sizeof(double), cudaMemcpyDeviceToHost));
-  FC_CUDA_TRY(ctx, cudaMemcpy(m.h_xyz.data() + nC, m.yc.p, nC * sizeof(double), cudaMemcpyDeviceToHost));
-  FC_CUDA_TRY(ctx, cudaMemcpy(m.h_xyz.data() + 2 * (size_t)nC, m.zc.p, nC * sizeof(double), cudaMemcpyDeviceToHost));
+  FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, m.h_xyz.data(), m.xc.p, nC * sizeof(double)));
+  FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, m.h_xyz.data() + nC, m.yc.p, nC * sizeof(double)));
+  FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, m.h_xyz.data() + 2 * (size_t)nC, m.zc.p, nC * sizeof(double)));
   int st = sys_set_pattern(ctx, s, nC, nnz, ia1.data(), ja1.data(), dg1.data(), m.h_xyz.data());
   if (st) { delete s; return st; }
-  FC_CUDA_TRY(ctx, cudaMemset(s->a.p, 0, (size_t)nnz * sizeof(double)));
+  FC_CUDA_TRY(ctx, fc_zero(ctx->stream, s->a.p, (size_t)nnz * sizeof(double)));
   ctx->sys_mesh = s;
   ctx->has_mesh = true;
   ctx->mesh_gen++;
@@ -326,7 +326,7 @@ extern "C" int fc_get_geometry(fc_ctx* ctx, const char* name, double* out) {
   else if (n == "vol") v = &m.vol; else if (n == "facint") v = &m.facint; else if (n == "Df") v = &m.Df;
   else if (n == "srdw") v = &m.srdw;
   else return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "unknown geometry array '" + n + "'");
-  FC_CUDA_TRY(ctx, cudaMemcpy(out, v->p, v->bytes(), cudaMemcpyDeviceToHost));
+  FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, out, v->p, v->bytes()));
   return FC_OK;
 }
 
@@ -347,11 +347,11 @@ extern "C" int fc_get_csr_pattern(fc_ctx* ctx, int* n_out, int* nnz_out, int* ia
   if (ijk || jik) {
     std::vector<int> t(nI);
     if (ijk) {
-      FC_CUDA_TRY(ctx, cudaMemcpy(t.data(), ctx->mesh.ijk.p, nI * sizeof(int), cudaMemcpyDeviceToHost));
+      FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, t.data(), ctx->mesh.ijk.p, nI * sizeof(int)));
       for (int f = 0; f < nI; ++f) ijk[f] = t[f] + 1;
     }
     if (jik) {
-      FC_CUDA_TRY(ctx, cudaMemcpy(t.data(), ctx->mesh.jik.p, nI * sizeof(int), cudaMemcpyDeviceToHost));
+      FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, t.data(), ctx->mesh.jik.p, nI * sizeof(int)));
       for (int f = 0; f < nI; ++f) jik[f] = t[f] + 1;
     }
   }

@@ -43,9 +43,9 @@ __global__ void k_grad_node(MeshView M, const int* __restrict__ nnodes, const in
 inline int grid_for(int n) { return std::max(1, std::min(65535, (n + 255) / 256)); }
 
 template <class T>
-cudaError_t download(std::vector<T>& h, const DVec<T>& d, size_t n) {
+cudaError_t download(cudaStream_t s, std::vector<T>& h, const DVec<T>& d, size_t n) {
   h.resize(n);
-  return n ? cudaMemcpy(h.data(), d.p, n * sizeof(T), cudaMemcpyDeviceToHost) : cudaSuccess;
+  return fc_d2h(s, h.data(), d.p, n * sizeof(T));
 }
 
 // gather lists of the current mesh and method (built on first use)
@@ -56,14 +56,14 @@ int node_interp_prepare(fc_ctx* ctx) {
   FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   std::vector<int> nnodes, nodes;
   std::vector<double> x, y, z, xf, yf, zf;
-  FC_CUDA_TRY(ctx, download(nnodes, m.nnodes, nF));
-  FC_CUDA_TRY(ctx, download(nodes, m.nodes, (size_t)nF * FC_NOMAX));
-  FC_CUDA_TRY(ctx, download(x, m.x, nN));
-  FC_CUDA_TRY(ctx, download(y, m.y, nN));
-  FC_CUDA_TRY(ctx, download(z, m.z, nN));
-  FC_CUDA_TRY(ctx, download(xf, m.xf, nF));
-  FC_CUDA_TRY(ctx, download(yf, m.yf, nF));
-  FC_CUDA_TRY(ctx, download(zf, m.zf, nF));
+  FC_CUDA_TRY(ctx, download(ctx->stream, nnodes, m.nnodes, nF));
+  FC_CUDA_TRY(ctx, download(ctx->stream, nodes, m.nodes, (size_t)nF * FC_NOMAX));
+  FC_CUDA_TRY(ctx, download(ctx->stream, x, m.x, nN));
+  FC_CUDA_TRY(ctx, download(ctx->stream, y, m.y, nN));
+  FC_CUDA_TRY(ctx, download(ctx->stream, z, m.z, nN));
+  FC_CUDA_TRY(ctx, download(ctx->stream, xf, m.xf, nF));
+  FC_CUDA_TRY(ctx, download(ctx->stream, yf, m.yf, nF));
+  FC_CUDA_TRY(ctx, download(ctx->stream, zf, m.zf, nF));
   if (m.h_xyz.size() != (size_t)3 * nC || m.h_owner.size() != (size_t)nF || m.h_neighbour.size() != (size_t)nI)
     return fc_fail_msg(ctx, FC_ERR_STATE, "node-based gradient: host mesh arrays missing");
   const double* xc = m.h_xyz.data();
@@ -75,10 +75,10 @@ int node_interp_prepare(fc_ctx* ctx) {
   FC_CUDA_TRY(ctx, ctx->ng_src.alloc(std::max<size_t>(1, ni.src.size())));
   FC_CUDA_TRY(ctx, ctx->ng_w.alloc(std::max<size_t>(1, ni.w.size())));
   FC_CUDA_TRY(ctx, ctx->ng_uN.alloc(std::max(1, nN)));
-  FC_CUDA_TRY(ctx, cudaMemcpy(ctx->ng_ptr.p, ni.ptr.data(), ni.ptr.size() * sizeof(int), cudaMemcpyHostToDevice));
+  FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, ctx->ng_ptr.p, ni.ptr.data(), ni.ptr.size() * sizeof(int)));
   if (!ni.src.empty()) {
-    FC_CUDA_TRY(ctx, cudaMemcpy(ctx->ng_src.p, ni.src.data(), ni.src.size() * sizeof(int), cudaMemcpyHostToDevice));
-    FC_CUDA_TRY(ctx, cudaMemcpy(ctx->ng_w.p, ni.w.data(), ni.w.size() * sizeof(double), cudaMemcpyHostToDevice));
+    FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, ctx->ng_src.p, ni.src.data(), ni.src.size() * sizeof(int)));
+    FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, ctx->ng_w.p, ni.w.data(), ni.w.size() * sizeof(double)));
   }
   ctx->ng_gen = ctx->mesh_gen;
   ctx->ng_method = ctx->node_interp;

@@ -962,7 +962,7 @@ static int make_dev(fc_ctx* ctx, Dev& D, bool allow_pressure = true) {
     FC_CUDA_TRY(ctx, S.ptype.alloc(std::max(1, m.numBoundaries)));
     S.ptype_gen = ctx->mesh_gen;
     if (m.numBoundaries)
-      FC_CUDA_TRY(ctx, cudaMemcpy(S.ptype.p, m.h_bctype.data(), m.numBoundaries * sizeof(int), cudaMemcpyHostToDevice));
+      FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, S.ptype.p, m.h_bctype.data(), m.numBoundaries * sizeof(int)));
   }
   for (int b = 0; b < m.numBoundaries; ++b) {
     if (m.h_bctype[b] == FC_BC_PERIODIC)
@@ -1479,7 +1479,7 @@ extern "C" int fc_temperature_set_params(fc_ctx* ctx, const fc_temperature_param
     if (kind == 2) iwall += m.h_nfaces[b];
   }
   FC_CUDA_TRY(ctx, S.tpatch.alloc(tab.size()));
-  FC_CUDA_TRY(ctx, cudaMemcpy(S.tpatch.p, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice));
+  FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, S.tpatch.p, tab.data(), tab.size() * sizeof(int)));
   S.tprm = *prm;
   S.tprm.lSolverT[sizeof(S.tprm.lSolverT) - 1] = 0;
   S.have_tprm = true;

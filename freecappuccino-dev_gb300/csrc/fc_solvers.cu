@@ -658,11 +658,11 @@ static void build_levels(int n, const std::vector<int>& ia, const std::vector<in
 }
 
 template <class V>
-static cudaError_t upload_vec(DVec<int>& d, const V& h) {
+static cudaError_t upload_vec(cudaStream_t s, DVec<int>& d, const V& h) {
   cudaError_t e = d.alloc(std::max<size_t>(1, h.size()));
   if (e != cudaSuccess) return e;
-  if (h.empty()) return cudaMemset(d.p, 0, sizeof(int));
-  return cudaMemcpy(d.p, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if (h.empty()) return fc_zero(s, d.p, sizeof(int));
+  return fc_h2d(s, d.p, h.data(), h.size() * sizeof(int));
 }
 
 // the stage area of the ordered sweeps: the shared memory the fixed parts
@@ -716,10 +716,10 @@ static int upload_ordered(fc_ctx* ctx, const OrderedSweep& O, DevOrdered& D) {
     D.K = stages_in(D.stage_area, L.bytes);
   }
   D.ring_entries = D.pushed_entries = D.cross_tile_entries = 0;
-  FC_CUDA_TRY(ctx, upload_vec(D.tile_step_ptr, O.tile_step_ptr));
-  FC_CUDA_TRY(ctx, upload_vec(D.step_ptr, O.step_ptr));
-  FC_CUDA_TRY(ctx, upload_vec(D.tile_W, O.tile_W));
-  FC_CUDA_TRY(ctx, upload_vec(D.perm, O.perm));
+  FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.tile_step_ptr, O.tile_step_ptr));
+  FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.step_ptr, O.step_ptr));
+  FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.tile_W, O.tile_W));
+  FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.perm, O.perm));
   for (int d = 0; d < 2; ++d) {
     const OrderedDir& H = O.dir[d];
     D.novf[d] = H.ovf_ptr.empty() ? 0 : H.ovf_ptr.back();
@@ -727,27 +727,27 @@ static int upload_ordered(fc_ctx* ctx, const OrderedSweep& O, DevOrdered& D) {
     D.ring_entries += H.ring_entries;
     D.pushed_entries += H.pushed_entries;
     D.cross_tile_entries += H.cross_tile_entries;
-    FC_CUDA_TRY(ctx, upload_vec(D.srec[d], H.srec));
-    FC_CUDA_TRY(ctx, upload_vec(D.xv_ptr[d], H.xv_ptr));
-    FC_CUDA_TRY(ctx, upload_vec(D.push_ptr[d], H.push_ptr));
-    FC_CUDA_TRY(ctx, upload_vec(D.push[d], H.push));
-    FC_CUDA_TRY(ctx, upload_vec(D.slot[d], H.slot));
-    FC_CUDA_TRY(ctx, upload_vec(D.ovf_ptr[d], H.ovf_ptr));
-    FC_CUDA_TRY(ctx, upload_vec(D.ovf_code[d], H.ovf_code));
-    FC_CUDA_TRY(ctx, upload_vec(D.ovf_col[d], H.ovf_col));
-    FC_CUDA_TRY(ctx, upload_vec(D.ovf_slot[d], H.ovf_slot));
+    FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.srec[d], H.srec));
+    FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.xv_ptr[d], H.xv_ptr));
+    FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.push_ptr[d], H.push_ptr));
+    FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.push[d], H.push));
+    FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.slot[d], H.slot));
+    FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.ovf_ptr[d], H.ovf_ptr));
+    FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.ovf_code[d], H.ovf_code));
+    FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.ovf_col[d], H.ovf_col));
+    FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.ovf_slot[d], H.ovf_slot));
   }
   // columns of the upper entries, 4 per row (Gauss-Seidel)
   std::vector<int> ucol((size_t)4 * O.nE, 0);
   for (int q = 0; q < O.n; ++q)
     for (int e = 0; e < FC_ELL; ++e) ucol[4 * (size_t)q + e] = O.dir[1].col[(size_t)e * O.nE + q];
-  FC_CUDA_TRY(ctx, upload_vec(D.ucol, ucol));
-  FC_CUDA_TRY(ctx, upload_vec(D.lo_tslot, O.lo_tslot));
-  FC_CUDA_TRY(ctx, upload_vec(D.lo_ovf_tslot, O.lo_ovf_tslot));
-  FC_CUDA_TRY(ctx, upload_vec(D.dslot, O.dslot));
-  FC_CUDA_TRY(ctx, upload_vec(D.p_ptr, O.p_ptr));
-  FC_CUDA_TRY(ctx, upload_vec(D.p_col, O.p_col));
-  FC_CUDA_TRY(ctx, upload_vec(D.p_slot, O.p_slot));
+  FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.ucol, ucol));
+  FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.lo_tslot, O.lo_tslot));
+  FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.lo_ovf_tslot, O.lo_ovf_tslot));
+  FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.dslot, O.dslot));
+  FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.p_ptr, O.p_ptr));
+  FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.p_col, O.p_col));
+  FC_CUDA_TRY(ctx, upload_vec(ctx->stream, D.p_slot, O.p_slot));
   return FC_OK;
 }
 
@@ -761,7 +761,7 @@ int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, c
   // the caller's arrays may live on the host or the device
   auto fetch = [&](const int* src, int* dst, size_t cnt) -> int {
     if (is_device_ptr(src)) {
-      cudaError_t e = cudaMemcpy(dst, src, cnt * sizeof(int), cudaMemcpyDeviceToHost);
+      cudaError_t e = fc_d2h(ctx->stream, dst, src, cnt * sizeof(int));
       if (e != cudaSuccess) return fc_fail(ctx, FC_ERR_CUDA, "pattern copy", e);
     } else {
       std::memcpy(dst, src, cnt * sizeof(int));
@@ -838,14 +838,14 @@ int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, c
   FC_CUDA_TRY(ctx, s->lf.rows.alloc(n));
   FC_CUDA_TRY(ctx, s->lb.ptr.alloc(s->lb.nlev + 1));
   FC_CUDA_TRY(ctx, s->lb.rows.alloc(n));
-  FC_CUDA_TRY(ctx, cudaMemcpy(s->ia.p, ia.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
-  FC_CUDA_TRY(ctx, cudaMemcpy(s->ja.p, ja.data(), nnz * sizeof(int), cudaMemcpyHostToDevice));
-  FC_CUDA_TRY(ctx, cudaMemcpy(s->diag.p, dg.data(), n * sizeof(int), cudaMemcpyHostToDevice));
-  FC_CUDA_TRY(ctx, cudaMemcpy(s->tslot.p, ts.data(), nnz * sizeof(int), cudaMemcpyHostToDevice));
-  FC_CUDA_TRY(ctx, cudaMemcpy(s->lf.ptr.p, s->lf.h_ptr.data(), (s->lf.nlev + 1) * sizeof(int), cudaMemcpyHostToDevice));
-  FC_CUDA_TRY(ctx, cudaMemcpy(s->lf.rows.p, s->lf.h_rows.data(), n * sizeof(int), cudaMemcpyHostToDevice));
-  FC_CUDA_TRY(ctx, cudaMemcpy(s->lb.ptr.p, s->lb.h_ptr.data(), (s->lb.nlev + 1) * sizeof(int), cudaMemcpyHostToDevice));
-  FC_CUDA_TRY(ctx, cudaMemcpy(s->lb.rows.p, s->lb.h_rows.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+  FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, s->ia.p, ia.data(), (n + 1) * sizeof(int)));
+  FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, s->ja.p, ja.data(), nnz * sizeof(int)));
+  FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, s->diag.p, dg.data(), n * sizeof(int)));
+  FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, s->tslot.p, ts.data(), nnz * sizeof(int)));
+  FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, s->lf.ptr.p, s->lf.h_ptr.data(), (s->lf.nlev + 1) * sizeof(int)));
+  FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, s->lf.rows.p, s->lf.h_rows.data(), n * sizeof(int)));
+  FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, s->lb.ptr.p, s->lb.h_ptr.data(), (s->lb.nlev + 1) * sizeof(int)));
+  FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, s->lb.rows.p, s->lb.h_rows.data(), n * sizeof(int)));
   s->h_ia.swap(ia);
   s->h_ja.swap(ja);
   s->h_diag.swap(dg);
@@ -869,9 +869,9 @@ static int alloc_ordered(fc_ctx* ctx, CsrSystem* s, OrdStore<T>& V) {
   FC_CUDA_TRY(ctx, V.xo.alloc(nE));
   FC_CUDA_TRY(ctx, V.bo.alloc(nE));
   // padding rows of the record arrays are read by the staging and never used
-  FC_CUDA_TRY(ctx, cudaMemset(V.vrec0.p, 0, V.vrec0.bytes()));
-  FC_CUDA_TRY(ctx, cudaMemset(V.vrec1.p, 0, V.vrec1.bytes()));
-  FC_CUDA_TRY(ctx, cudaMemset(V.sx.p, 0, V.sx.bytes()));
+  FC_CUDA_TRY(ctx, fc_zero(ctx->stream, V.vrec0.p, V.vrec0.bytes()));
+  FC_CUDA_TRY(ctx, fc_zero(ctx->stream, V.vrec1.p, V.vrec1.bytes()));
+  FC_CUDA_TRY(ctx, fc_zero(ctx->stream, V.sx.p, V.sx.bytes()));
   return FC_OK;
 }
 
@@ -885,7 +885,7 @@ int sys_alloc_work(fc_ctx* ctx, CsrSystem* s) {
   FC_CUDA_TRY(ctx, s->out.alloc(FC_OUT_N));
   FC_CUDA_TRY(ctx, s->bar.alloc(2));
   FC_CUDA_TRY(ctx, s->status.alloc(1));
-  FC_CUDA_TRY(ctx, cudaMemset(s->bar.p, 0, 2 * sizeof(unsigned)));
+  FC_CUDA_TRY(ctx, fc_zero(ctx->stream, s->bar.p, 2 * sizeof(unsigned)));
   if (!s->h_out) FC_CUDA_TRY(ctx, cudaMallocHost(&s->h_out, FC_OUT_N * sizeof(double)));
   if (!s->h_status) FC_CUDA_TRY(ctx, cudaMallocHost(&s->h_status, sizeof(int)));
   return alloc_ordered(ctx, s, s->o64);
@@ -1443,7 +1443,7 @@ extern "C" int fc_trace_get(fc_ctx* ctx, double* out, unsigned long long* timeli
   FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   const int nb = ctx->trace_blocks, cap = ctx->trace_cap;
   std::vector<unsigned long long> h(ctx->trace.n);
-  FC_CUDA_TRY(ctx, cudaMemcpy(h.data(), ctx->trace.p, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, h.data(), ctx->trace.p, h.size() * sizeof(unsigned long long)));
   int used = 0;
   for (int k = 0; k < FC_TRACE_N; ++k) out[k] = 0.0;
   for (int b = 0; b < nb; ++b) {

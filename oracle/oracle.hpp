@@ -35,6 +35,10 @@ struct Case {
   int numBoundaries = 0;
   std::vector<int> bctype, nfaces, startFace, iBndValueStart;  // 1-based per boundary
   int nwal = 0, nsym = 0;
+  // periodic pairs (geometry.f90:24, :82, :250-258): nper pairs, numPeriodic
+  // faces on the 'periodic' sides, startFaceTwin(iPer) 1-based by pair
+  int nper = 0, numPeriodic = 0;
+  std::vector<int> startFaceTwin;
   // mesh (1-based)
   std::vector<double> x, y, z;
   std::vector<int> nnodes, node;  // node[(iface)*6 + k] k=1..6 -> stored at node[iface*6 + k-1]
@@ -92,11 +96,15 @@ struct Case {
 inline double& G(std::vector<double>& g, int k, int i) { return g[3 * (size_t)i + (k - 1)]; }
 
 // mesh + geometry + CSR
+// twin: per patch, the 0-based startFace of a 'periodic' patch's twin (the
+// fifth field of its boundary-file line), ignored for other patches; NULL
+// when the mesh has no periodic patches
 void setup_case(Case& c, int numNodes, int numCells, int numInnerFaces, int numBoundaryFaces,
                 const double* x, const double* y, const double* z, const int* nnodes, const int* nodes,
                 const int* owner, const int* neighbour, int numBoundaries, const int* bctype,
-                const int* nfaces, const int* startFace);
+                const int* nfaces, const int* startFace, const int* twin = nullptr);
 void geometry(Case& c);
+void face_mapping(Case& c);
 void create_csr(Case& c);
 
 // linear solvers (linear_solvers.f90); arrays 1-based raw pointers
@@ -151,6 +159,7 @@ void laplacian(Case& c, const std::vector<double>& mu, const std::vector<double>
 void gradp_and_sources(Case& c, std::vector<double>& p);
 void bpres(Case& c, std::vector<double>& p, int istage);
 void updateVelocityAtBoundary(Case& c);
+void updateBoundary(Case& c, std::vector<double>& phi);
 void init_flmass(Case& c);
 int calcuvw(Case& c);
 int calcp_simple(Case& c);

@@ -77,8 +77,8 @@ std::vector<int>* int_array(Case& c, const std::string& n, int& len) {
   if (n == "ia") { len = c.numCells + 1; return &c.ia; }
   if (n == "ja") { len = c.nnz; return &c.ja; }
   if (n == "diag") { len = c.numCells; return &c.diag; }
-  if (n == "ijk") { len = c.numInnerFaces; return &c.ijk; }
-  if (n == "jik") { len = c.numInnerFaces; return &c.jik; }
+  if (n == "ijk") { len = c.numInnerFaces + c.numPeriodic; return &c.ijk; }
+  if (n == "jik") { len = c.numInnerFaces + c.numPeriodic; return &c.jik; }
   if (n == "owner") { len = c.numFaces; return &c.owner; }
   if (n == "neighbour") { len = c.numInnerFaces; return &c.neighbour; }
   return nullptr;
@@ -98,20 +98,20 @@ extern "C" {
 void* orc_case_new(int numNodes, int numCells, int numInnerFaces, int numBoundaryFaces, const double* x,
                    const double* y, const double* z, const int* nnodes, const int* nodes, const int* owner,
                    const int* neighbour, int numBoundaries, const int* bctype, const int* nfaces,
-                   const int* startFace) {
+                   const int* startFace, const int* twin) {
   Case* c = new Case();
   setup_case(*c, numNodes, numCells, numInnerFaces, numBoundaryFaces, x, y, z, nnodes, nodes, owner, neighbour,
-             numBoundaries, bctype, nfaces, startFace);
+             numBoundaries, bctype, nfaces, startFace, twin);
   return c;
 }
 
 void orc_case_free(void* h) { delete (Case*)h; }
 
-// out[8] = numCells, numInnerFaces, numBoundaryFaces, numFaces, numTotal, nnz, nwal, nsym
+// out[9] = numCells, numInnerFaces, numBoundaryFaces, numFaces, numTotal, nnz, nwal, nsym, numPeriodic
 int orc_case_sizes(void* h, int* out) {
   Case& c = *(Case*)h;
   out[0] = c.numCells; out[1] = c.numInnerFaces; out[2] = c.numBoundaryFaces; out[3] = c.numFaces;
-  out[4] = c.numTotal; out[5] = c.nnz; out[6] = c.nwal; out[7] = c.nsym;
+  out[4] = c.numTotal; out[5] = c.nnz; out[6] = c.nwal; out[7] = c.nsym; out[8] = c.numPeriodic;
   return 0;
 }
 

@@ -816,8 +816,54 @@ static void facefluxuvw_bnd(Case& c, int ijp, int ijb, double xf, double yf, dou
   swp = fdwe + fdwi;
 }
 
-// calcuvw, velocity.f90:50-750 for steady SIMPLE without buoyancy, MHD,
-// transient or periodic terms.  Returns the worst csrsolve status.
+// facefluxuvw_periodic, velocity.f90:1038-1179: momentum fluxes through a
+// periodic face between ijp and the twin's owner ijn, central weights 1/2,
+// the distance vector 2 (xf - xc(ijp)), the full stress tensor of the face
+// gradient, cds face values
+static void facefluxuvw_periodic(Case& c, int ijp, int ijn, double xf, double yf, double zf, double arx, double ary,
+                                 double arz, double flomass, double gam, double& cap, double& can, double& sup,
+                                 double& svp, double& swp) {
+  const double fxn = 0.5, fxp = fxn;
+  double xpn = 2 * (xf - c.xc[ijp]), ypn = 2 * (yf - c.yc[ijp]), zpn = 2 * (zf - c.zc[ijp]);
+  double dpn = std::sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
+  double are = std::sqrt(arx * arx + ary * ary + arz * arz);
+  double game = c.vis[ijp] * fxp + c.vis[ijn] * fxn;
+  double de = game * (arx * arx + ary * ary + arz * arz) / (xpn * arx + ypn * ary + zpn * arz);
+  double ce = std::min(flomass, 0.0), cp = std::max(flomass, 0.0);
+  can = -de + ce;
+  cap = -de - cp;
+  auto gi = [&](std::vector<double>& g, int k) { return G(g, k, ijp) * fxp + G(g, k, ijn) * fxn; };
+  double duxi = gi(c.dUdxi, 1), duyi = gi(c.dUdxi, 2), duzi = gi(c.dUdxi, 3);
+  double dvxi = gi(c.dVdxi, 1), dvyi = gi(c.dVdxi, 2), dvzi = gi(c.dVdxi, 3);
+  double dwxi = gi(c.dWdxi, 1), dwyi = gi(c.dWdxi, 2), dwzi = gi(c.dWdxi, 3);
+  double fdue = game * ((duxi + duxi) * arx + (duyi + dvxi) * ary + (duzi + dwxi) * arz);
+  double fdve = game * ((duyi + dvxi) * arx + (dvyi + dvyi) * ary + (dvzi + dwyi) * arz);
+  double fdwe = game * ((duzi + dwxi) * arx + (dwyi + dvzi) * ary + (dwzi + dwzi) * arz);
+  double fdui = game * are / dpn * (duxi * xpn + duyi * ypn + duzi * zpn);
+  double fdvi = game * are / dpn * (dvxi * xpn + dvyi * ypn + dvzi * zpn);
+  double fdwi = game * are / dpn * (dwxi * xpn + dwyi * ypn + dwzi * zpn);
+  double fuuds = cp * c.u[ijp] + ce * c.u[ijn];
+  double fvuds = cp * c.v[ijp] + ce * c.v[ijn];
+  double fwuds = cp * c.w[ijp] + ce * c.w[ijn];
+  double ue, ve, we;
+  if (flomass >= 0.0) {  // face_value_cds, interpolation.f90:116-157
+    ue = c.u[ijp] + (c.u[ijn] - c.u[ijp]) * fxp;
+    ve = c.v[ijp] + (c.v[ijn] - c.v[ijp]) * fxp;
+    we = c.w[ijp] + (c.w[ijn] - c.w[ijp]) * fxp;
+  } else {
+    ue = c.u[ijn] + (c.u[ijp] - c.u[ijn]) * fxn;
+    ve = c.v[ijn] + (c.v[ijp] - c.v[ijn]) * fxn;
+    we = c.w[ijn] + (c.w[ijp] - c.w[ijn]) * fxn;
+  }
+  double fuhigh = flomass * ue, fvhigh = flomass * ve, fwhigh = flomass * we;
+  sup = -gam * (fuhigh - fuuds) + fdue - fdui;
+  svp = -gam * (fvhigh - fvuds) + fdve - fdvi;
+  swp = -gam * (fwhigh - fwuds) + fdwe - fdwi;
+}
+
+// calcuvw, velocity.f90:50-750 without buoyancy or MHD terms, with the
+// unsteady terms of :226-290 and periodic pairs (:393-430).  Returns the
+// worst csrsolve status.
 int calcuvw(Case& c) {
   const int nC = c.numCells;
   std::fill(c.spu.begin(), c.spu.end(), 0.0);
@@ -868,7 +914,7 @@ int calcuvw(Case& c) {
     c.su[ijn] = c.su[ijn] - sup; c.sv[ijn] = c.sv[ijn] - svp; c.sw[ijn] = c.sw[ijn] - swp;
   }
   // boundaries :326-562
-  int iWall = 0;
+  int iWall = 0, iPer = 0, l = c.numInnerFaces;
   const int inp_stale = nC + 1;  // loop variable 'inp' after the cell loop at :183 (used at :379)
   for (int ib = 1; ib <= c.numBoundaries; ++ib) {
     int t = c.bctype[ib];
@@ -897,6 +943,20 @@ int calcuvw(Case& c) {
         c.spu[ijp] = c.spu[ijp] + cf * (nxf * nxf);
         c.spv[ijp] = c.spv[ijp] + cf * (nyf * nyf);
         c.sp[ijp] = c.sp[ijp] + cf * (nzf * nzf);
+      }
+    } else if (t == BC_PERIODIC) {  // :393-430
+      ++iPer;
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int iface = c.startFace[ib] + i, ijp = c.owner[iface];
+        int ijn = c.owner[c.startFaceTwin[iPer] + i];
+        double cap, can, sup, svp, swp;
+        facefluxuvw_periodic(c, ijp, ijn, c.xf[iface], c.yf[iface], c.zf[iface], c.arx[iface], c.ary[iface],
+                             c.arz[iface], c.flmass[iface], c.gdsU, cap, can, sup, svp, swp);
+        ++l;
+        c.a[c.ijk[l]] = can;
+        c.a[c.jik[l]] = cap;
+        c.su[ijp] = c.su[ijp] + sup; c.sv[ijp] = c.sv[ijp] + svp; c.sw[ijp] = c.sw[ijp] + swp;
+        c.su[ijn] = c.su[ijn] - sup; c.sv[ijn] = c.sv[ijn] - svp; c.sw[ijn] = c.sw[ijn] - swp;
       }
     } else if (t == BC_WALL) {
       for (int i = 1; i <= c.nfaces[ib]; ++i) {
@@ -1075,8 +1135,68 @@ static void facefluxmassCorrPressBnd(Case& c, int ijp, int ijb, double xf, doubl
   fluxmass = fluxmass - c.den[ijp] * (arx * arx + ary * ary + arz * arz) * cap * dpcor;
 }
 
+// facefluxmass2_periodic, faceflux_mass.f90:313-384: the mass flux through a
+// periodic face between ijp (owner of the face) and ijn (owner of its twin),
+// with the face's own centre standing in for the twin side (xpn = 2 (xf -
+// xc(ijp))).  Df is indexed by the face's position i within its patch, as
+// the reference writes it.
+static void facefluxmass2_periodic(Case& c, int i, int ijp, int ijn, double xf, double yf, double zf, double arx,
+                                   double ary, double arz, double lambda, double& cap, double& can,
+                                   double& fluxmass) {
+  double fxn = lambda, fxp = 1.0 - lambda;
+  double xpn = 2 * (xf - c.xc[ijp]), ypn = 2 * (yf - c.yc[ijp]), zpn = 2 * (zf - c.zc[ijp]);
+  double dene = c.den[ijp] * fxp + c.den[ijn] * fxn;
+  double Kj = c.vol[ijp] * c.apu[ijp] * fxp + c.vol[ijn] * c.apu[ijn] * fxn;
+  cap = -dene * Kj * c.Df[i];
+  can = cap;
+  Kj = (c.apu[ijp] + c.apu[ijn] + kSmall);
+  double ui = (c.u[ijp] * c.apu[ijn] + c.u[ijn] * c.apu[ijp]) / Kj;
+  double vi = (c.v[ijp] * c.apv[ijn] + c.v[ijn] * c.apv[ijp]) / Kj;
+  double wi = (c.w[ijp] * c.apw[ijn] + c.w[ijn] * c.apw[ijp]) / Kj;
+  double dpxi = (G(c.dPdxi, 1, ijn) * fxp + G(c.dPdxi, 1, ijp) * fxn) * xpn;
+  double dpyi = (G(c.dPdxi, 2, ijn) * fxp + G(c.dPdxi, 2, ijp) * fxn) * ypn;
+  double dpzi = (G(c.dPdxi, 3, ijn) * fxp + G(c.dPdxi, 3, ijp) * fxn) * zpn;
+  fluxmass = dene * (ui * arx + vi * ary + wi * arz) + cap * (c.p[ijn] - c.p[ijp] - dpxi - dpyi - dpzi);
+}
+
+// the periodic branch of the boundary loops of calcp_simple (:185-225) and
+// calcp_piso (:248-289): mass flux, both off-diagonal slots, both diagonals
+// and both sources of every pair; l runs on from numInnerFaces
+static void periodic_pressure_faces(Case& c, int ib, int& iPer, int& l) {
+  ++iPer;
+  for (int i = 1; i <= c.nfaces[ib]; ++i) {
+    int iface = c.startFace[ib] + i, ijp = c.owner[iface];
+    int iftwin = c.startFaceTwin[iPer] + i, ijn = c.owner[iftwin];
+    double cap, can;
+    facefluxmass2_periodic(c, i, ijp, ijn, c.xf[iface], c.yf[iface], c.zf[iface], c.arx[iface], c.ary[iface],
+                           c.arz[iface], 0.5, cap, can, c.flmass[iface]);
+    ++l;
+    c.a[c.ijk[l]] = cap;
+    c.a[c.jik[l]] = cap;
+    c.a[c.diag[ijp]] = c.a[c.diag[ijp]] - cap;
+    c.a[c.diag[ijn]] = c.a[c.diag[ijn]] - cap;
+    c.su[ijp] = c.su[ijp] - c.flmass[iface];
+    c.su[ijn] = c.su[ijn] + c.flmass[iface];
+  }
+}
+
+// flux correction through the periodic pairs after a pressure solve
+// (calcp_simple.f90:322-342, calcp_piso.f90:437-456, with phi = pp or p):
+// the twin face takes the same mass flux
+static void periodic_flux_correct(Case& c, int ib, int& iPer, int& l, const std::vector<double>& phi) {
+  ++iPer;
+  for (int i = 1; i <= c.nfaces[ib]; ++i) {
+    int iface = c.startFace[ib] + i, ijp = c.owner[iface];
+    int iftwin = c.startFaceTwin[iPer] + i, ijn = c.owner[iftwin];
+    ++l;
+    c.flmass[iface] = c.flmass[iface] + c.a[c.ijk[l]] * (phi[ijn] - phi[ijp]);
+    c.flmass[iftwin] = c.flmass[iface];
+  }
+}
+
 // calcp_simple, calcp_simple.f90:1-470 for incompressible SIMPLE, with
-// pressure boundaries (:162-183, :344-356, :363-369); no periodic pairs.
+// pressure boundaries (:162-183, :344-356, :363-369) and periodic pairs
+// (:185-225, :322-342).
 int calcp_simple(Case& c) {
   const int nC = c.numCells;
   std::fill(c.a.begin(), c.a.end(), 0.0);
@@ -1094,8 +1214,11 @@ int calcp_simple(Case& c) {
   }
   adjustMassFlow(c);
   bool have_pressure = false;
+  int iPer = 0, l = c.numInnerFaces;
   for (int ib = 1; ib <= c.numBoundaries; ++ib) {
-    if (c.bctype[ib] == BC_INLET || c.bctype[ib] == BC_OUTLET) {
+    if (c.bctype[ib] == BC_PERIODIC) {
+      periodic_pressure_faces(c, ib, iPer, l);
+    } else if (c.bctype[ib] == BC_INLET || c.bctype[ib] == BC_OUTLET) {
       for (int i = 1; i <= c.nfaces[ib]; ++i) {
         int iface = c.startFace[ib] + i, ijp = c.owner[iface];
         c.su[ijp] = c.su[ijp] - c.flmass[iface];
@@ -1122,7 +1245,13 @@ int calcp_simple(Case& c) {
       int ijp = c.owner[iface], ijn = c.neighbour[iface];
       c.flmass[iface] = c.flmass[iface] + c.a[c.ijk[iface]] * (c.pp[ijn] - c.pp[ijp]);
     }
+    iPer = 0;
+    l = c.numInnerFaces;
     for (int ib = 1; ib <= c.numBoundaries; ++ib) {
+      if (c.bctype[ib] == BC_PERIODIC) {
+        periodic_flux_correct(c, ib, iPer, l, c.pp);
+        continue;
+      }
       if (c.bctype[ib] != BC_PRESSURE) continue;
       for (int i = 1; i <= c.nfaces[ib]; ++i) {
         int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
@@ -1195,8 +1324,9 @@ static void fluxmc(Case& c, int ijp, int ijn, double xf, double yf, double zf, d
                   (G(c.dPdxi, 3, ijn) * zep - G(c.dPdxi, 3, ijp) * zpp));
 }
 
-// calcp_piso, calcp_piso.f90:86-489, incompressible, without periodic or
-// pressure boundaries; nipgrad = 2 (parameters.f90:62)
+// calcp_piso, calcp_piso.f90:86-489, incompressible, with periodic pairs
+// (:248-289, :437-456) and without pressure boundaries; nipgrad = 2
+// (parameters.f90:62)
 int calcp_piso(Case& c) {
   const int nC = c.numCells;
   c.h = c.a;
@@ -1233,7 +1363,12 @@ int calcp_piso(Case& c) {
       c.su[ijn] = c.su[ijn] + c.flmass[i];
     }
     adjustMassFlow(c);
+    int iPer = 0, l = c.numInnerFaces;
     for (int ib = 1; ib <= c.numBoundaries; ++ib) {
+      if (c.bctype[ib] == BC_PERIODIC) {
+        periodic_pressure_faces(c, ib, iPer, l);
+        continue;
+      }
       if (c.bctype[ib] != BC_INLET && c.bctype[ib] != BC_OUTLET) continue;
       for (int i = 1; i <= c.nfaces[ib]; ++i) {
         int iface = c.startFace[ib] + i, ijp = c.owner[iface];
@@ -1274,6 +1409,11 @@ int calcp_piso(Case& c) {
       c.v[i] = c.v[i] + c.sv[i] * c.apv[i];
       c.w[i] = c.w[i] + c.sw[i] * c.apw[i];
     }
+    // periodic pairs take the flux correction of the last p (:437-456)
+    iPer = 0;
+    l = c.numInnerFaces;
+    for (int ib = 1; ib <= c.numBoundaries; ++ib)
+      if (c.bctype[ib] == BC_PERIODIC) periodic_flux_correct(c, ib, iPer, l, c.p);
     updateVelocityAtBoundary(c);
   }
   return worst;
@@ -1306,6 +1446,62 @@ static void facefluxsc(Case& c, int i, int ijp, int ijn, double xf, double yf, d
   suadd = -fcfie + fdfie;
 }
 
+// facefluxsc_periodic, scalar_fluxes.f90:147-251: a periodic face between
+// ijp and the twin's owner ijn, central weights 1/2, the distance vector
+// 2 (xf - xc(ijp)), Df indexed by the face's position i within its patch (as
+// the reference writes it), cds face value
+static void facefluxsc_periodic(Case& c, int i, int ijp, int ijn, double xf, double yf, double zf, double arx,
+                                double ary, double arz, double fm, double gam, const std::vector<double>& fi,
+                                std::vector<double>& dfidxi, double dcoef, double& cap, double& can,
+                                double& suadd) {
+  const double fxn = 0.5, fxp = fxn;
+  double xpn = 2 * (xf - c.xc[ijp]), ypn = 2 * (yf - c.yc[ijp]), zpn = 2 * (zf - c.zc[ijp]);
+  double de = dcoef * c.Df[i];
+  double ce = std::min(fm, 0.0), cp = std::max(fm, 0.0);
+  can = -de + ce;
+  cap = -de - cp;
+  double dfixi = G(dfidxi, 1, ijp) * fxp + G(dfidxi, 1, ijn) * fxn;
+  double dfiyi = G(dfidxi, 2, ijp) * fxp + G(dfidxi, 2, ijn) * fxn;
+  double dfizi = G(dfidxi, 3, ijp) * fxp + G(dfidxi, 3, ijn) * fxn;
+  dfixi = dfixi * (arx - c.Df[i] * xpn);
+  dfiyi = dfiyi * (ary - c.Df[i] * ypn);
+  dfizi = dfizi * (arz - c.Df[i] * zpn);
+  double fdfie = dcoef * (dfixi + dfiyi + dfizi);
+  double fii;
+  if (fm >= 0.0) fii = fi[ijp] + (fi[ijn] - fi[ijp]) * fxp;  // face_value_cds, interpolation.f90:116-157
+  else fii = fi[ijn] + (fi[ijp] - fi[ijn]) * fxn;
+  double fcfie = fm * fii;
+  double fcfii = ce * fi[ijn] + cp * fi[ijp];
+  fcfie = gam * (fcfie - fcfii);
+  suadd = -fcfie + fdfie;
+}
+
+// updateBoundary, updateBoundary.f90:1-77: outlet, symmetry, pressure and
+// empty faces take the owner's value; a periodic face and its twin take the
+// mean of the pair's two cells (in patch order, so a twin patch listed after
+// its periodic patch ends with the owner's value)
+void updateBoundary(Case& c, std::vector<double>& phi) {
+  int iPer = 0;
+  for (int ib = 1; ib <= c.numBoundaries; ++ib) {
+    int t = c.bctype[ib];
+    if (t == BC_OUTLET || t == BC_SYMMETRY || t == BC_PRESSURE || t == BC_EMPTY) {
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
+        phi[ijb] = phi[ijp];
+      }
+    } else if (t == BC_PERIODIC) {
+      ++iPer;
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
+        int ijn = c.owner[c.startFaceTwin[iPer] + i];
+        phi[ijb] = 0.5 * (phi[ijp] + phi[ijn]);
+        int ijbt = c.numCells + (c.startFaceTwin[iPer] - c.numInnerFaces) + i;
+        phi[ijbt] = phi[ijb];
+      }
+    }
+  }
+}
+
 // facefluxsc_boundary, scalar_fluxes.f90:256-337
 static void facefluxsc_bnd(Case& c, int ijp, double xf, double yf, double zf, double arx, double ary, double arz,
                            double fm, std::vector<double>& dfidxi, double dcoef, double& cap, double& can,
@@ -1324,7 +1520,8 @@ static void facefluxsc_bnd(Case& c, int ijp, double xf, double yf, double zf, do
 }
 
 // calculate_temperature, temperature.f90:35-385, steady and laminar-or-given
-// vis (no transient, turbulent heat-flux, Crank-Nicolson or periodic terms).
+// vis (no transient, turbulent heat-flux or Crank-Nicolson terms), with
+// periodic pairs (:262-313).
 // Isothermal walls are bcDFracT == 1, adiabatic walls bcDFracT == 0; the wall
 // counter iWall advances only on isothermal walls (:203), so srdw is indexed
 // as the reference indexes it.  Adiabatic walls copy T(ijp) to T(ijb) during
@@ -1351,7 +1548,7 @@ int calculate_temperature(Case& c, bool solve) {
     c.su[ijp] = c.su[ijp] + suadd;
     c.su[ijn] = c.su[ijn] - suadd;
   }
-  int iWall = 0;
+  int iWall = 0, iPer = 0, l = c.numInnerFaces;
   for (int ib = 1; ib <= c.numBoundaries; ++ib) {
     int t = c.bctype[ib];
     if (t == BC_INLET || t == BC_OUTLET || t == BC_PRESSURE) {
@@ -1379,6 +1576,24 @@ int calculate_temperature(Case& c, bool solve) {
         int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
         c.T[ijb] = c.T[ijp];
       }
+    } else if (t == BC_PERIODIC) {  // temperature.f90:262-313
+      ++iPer;
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int iface = c.startFace[ib] + i, ijp = c.owner[iface];
+        int ijn = c.owner[c.startFaceTwin[iPer] + i];
+        // facint of the face's position i within its patch, as written there
+        double dcoef = c.viscos * prl + ((c.vis[ijp] + (c.vis[ijn] - c.vis[ijp]) * c.facint[i]) - c.viscos) * prtr;
+        double cap, can, suadd;
+        facefluxsc_periodic(c, i, ijp, ijn, c.xf[iface], c.yf[iface], c.zf[iface], c.arx[iface], c.ary[iface],
+                            c.arz[iface], c.flmass[iface], gam, c.T, c.dTdxi, dcoef, cap, can, suadd);
+        ++l;
+        c.a[c.ijk[l]] = can;
+        c.a[c.jik[l]] = cap;
+        c.a[c.diag[ijp]] = c.a[c.diag[ijp]] - can;
+        c.a[c.diag[ijn]] = c.a[c.diag[ijn]] - cap;
+        c.su[ijp] = c.su[ijp] + suadd;
+        c.su[ijn] = c.su[ijn] - suadd;
+      }
     }
   }
   const double urfr = 1.0 / c.urfT, urfm = 1.0 - c.urfT;
@@ -1393,15 +1608,7 @@ int calculate_temperature(Case& c, bool solve) {
   if (!solve) return 0;
   SolveInfo si;
   int st = csrsolve(c, c.lSolverT, c.T, c.su, c.resor[7], c.maxiterT, c.tolAbsT, c.tolRelT, si);
-  // updateBoundary, updateBoundary.f90 (no periodic pairs)
-  for (int ib = 1; ib <= c.numBoundaries; ++ib) {
-    int t = c.bctype[ib];
-    if (t != BC_OUTLET && t != BC_SYMMETRY && t != BC_PRESSURE && t != BC_EMPTY) continue;
-    for (int i = 1; i <= c.nfaces[ib]; ++i) {
-      int iface = c.startFace[ib] + i, ijp = c.owner[iface], ijb = c.iBndValueStart[ib] + i;
-      c.T[ijb] = c.T[ijp];
-    }
-  }
+  updateBoundary(c, c.T);
   double fimin = c.T[1];
   for (int i = 2; i <= nC; ++i) fimin = std::min(fimin, c.T[i]);
   if (fimin < 0.0)

@@ -13,7 +13,7 @@ namespace orc {
 void setup_case(Case& c, int numNodes, int numCells, int numInnerFaces, int numBoundaryFaces, const double* x,
                 const double* y, const double* z, const int* nnodes, const int* nodes, const int* owner,
                 const int* neighbour, int numBoundaries, const int* bctype, const int* nfaces,
-                const int* startFace) {
+                const int* startFace, const int* twin) {
   c.numNodes = numNodes;
   c.numCells = numCells;
   c.numInnerFaces = numInnerFaces;
@@ -26,12 +26,19 @@ void setup_case(Case& c, int numNodes, int numCells, int numInnerFaces, int numB
   c.startFace.assign(numBoundaries + 1, 0);
   c.iBndValueStart.assign(numBoundaries + 1, 0);
   c.nwal = c.nsym = 0;
+  c.nper = c.numPeriodic = 0;
+  c.startFaceTwin.assign(1, 0);
   for (int i = 1; i <= numBoundaries; ++i) {
     c.bctype[i] = bctype[i - 1];
     c.nfaces[i] = nfaces[i - 1];
     c.startFace[i] = startFace[i - 1];
     if (c.bctype[i] == BC_WALL) c.nwal += c.nfaces[i];
     else if (c.bctype[i] == BC_SYMMETRY) c.nsym += c.nfaces[i];
+    else if (c.bctype[i] == BC_PERIODIC) {  // geometry.f90:250-258
+      ++c.nper;
+      c.numPeriodic += c.nfaces[i];
+      c.startFaceTwin.push_back(twin ? twin[i - 1] : 0);
+    }
     // geometry.f90:292-294
     c.iBndValueStart[i] = numCells + (c.startFace[i] - numInnerFaces);
   }
@@ -51,6 +58,7 @@ void setup_case(Case& c, int numNodes, int numCells, int numInnerFaces, int numB
   for (int f = 1; f <= numInnerFaces; ++f) c.neighbour[f] = neighbour[f - 1];
 
   geometry(c);
+  if (c.nper > 0) face_mapping(c);  // geometry.f90:110-112
   create_csr(c);
 
   const size_t nt = c.numTotal + 1, nc = c.numCells + 1;
@@ -190,12 +198,28 @@ void geometry(Case& c) {
 // keys are compared on both components, equal keys are indistinguishable, so
 // every correct lexicographic sort yields the same arrays.
 void create_csr(Case& c) {
-  const int nC = c.numCells, nI = c.numInnerFaces;
-  c.nnz = 2 * nI + nC;  // no periodic faces on this path
+  const int nC = c.numCells, nI = c.numInnerFaces, nP = c.numPeriodic;
+  c.nnz = 2 * (nI + nP) + nC;  // sparse_matrix.f90:110
   std::vector<std::pair<int, int>> coo(c.nnz);
   for (int icell = 1; icell <= nC; ++icell) coo[icell - 1] = {icell, icell};
   for (int i = 1; i <= nI; ++i) coo[nC + i - 1] = {c.owner[i], c.neighbour[i]};
   for (int i = 1; i <= nI; ++i) coo[nC + nI + i - 1] = {c.neighbour[i], c.owner[i]};
+  // cells coupled through periodic pairs, two entries per pair (:136-165);
+  // pairs(l - nI) = (ijp, ijn) in the running order l of the face loops
+  std::vector<std::pair<int, int>> pairs;
+  {
+    int k = nC + 2 * nI, iPer = 0;
+    for (int ib = 1; ib <= c.numBoundaries; ++ib) {
+      if (c.bctype[ib] != BC_PERIODIC) continue;
+      ++iPer;
+      for (int i = 1; i <= c.nfaces[ib]; ++i) {
+        int ijp = c.owner[c.startFace[ib] + i], ijn = c.owner[c.startFaceTwin[iPer] + i];
+        coo[k++] = {ijp, ijn};
+        coo[k++] = {ijn, ijp};
+        pairs.push_back({ijp, ijn});
+      }
+    }
+  }
   std::sort(coo.begin(), coo.end());
   c.ja.assign(c.nnz + 1, 0);
   std::vector<int> iacoo(c.nnz + 1, 0);
@@ -222,12 +246,46 @@ void create_csr(Case& c) {
       if (c.ja[l] == jcell) { k = l; break; }
     return k;
   };
-  c.ijk.assign(nI + 1, 0);
-  c.jik.assign(nI + 1, 0);
+  c.ijk.assign(nI + nP + 1, 0);
+  c.jik.assign(nI + nP + 1, 0);
   for (int i = 1; i <= nI; ++i) {
     int ijp = c.owner[i], ijn = c.neighbour[i];
     c.ijk[i] = csr_to_k(ijp, ijn);
     c.jik[i] = csr_to_k(ijn, ijp);
+  }
+  for (int q = 0; q < nP; ++q) {  // :262-292
+    c.ijk[nI + 1 + q] = csr_to_k(pairs[q].first, pairs[q].second);
+    c.jik[nI + 1 + q] = csr_to_k(pairs[q].second, pairs[q].first);
+  }
+}
+
+// face_mapping, geometry.f90:1848-1997: face i of a periodic patch is paired
+// with the twin-patch face whose owner's centre is nearest (L1 distance) to
+// face i's centre; the twin faces' owners, centres and area vectors are then
+// reordered so that twin face i belongs to that pair.
+void face_mapping(Case& c) {
+  int iPer = 0;
+  for (int ib = 1; ib <= c.numBoundaries; ++ib) {
+    if (c.bctype[ib] != BC_PERIODIC) continue;
+    ++iPer;
+    const int n = c.nfaces[ib], tw = c.startFaceTwin[iPer];
+    std::vector<int> tmp(n + 1, 0), itmp(n + 1, 0);
+    for (int i = 1; i <= n; ++i) {
+      const int iface = c.startFace[ib] + i;
+      double mindist = (double)1e+30f;
+      for (int it = 1; it <= n; ++it) {
+        const int ijn = c.owner[tw + it];
+        const double dist =
+            std::fabs(c.xf[iface] - c.xc[ijn]) + std::fabs(c.yf[iface] - c.yc[ijn]) + std::fabs(c.zf[iface] - c.zc[ijn]);
+        if (dist < mindist) { mindist = dist; tmp[i] = ijn; itmp[i] = it; }
+      }
+    }
+    for (int i = 1; i <= n; ++i) c.owner[tw + i] = tmp[i];
+    std::vector<double> vtmp(n + 1);
+    for (std::vector<double>* v : {&c.xf, &c.yf, &c.zf, &c.arx, &c.ary, &c.arz}) {
+      for (int i = 1; i <= n; ++i) vtmp[i] = (*v)[tw + itmp[i]];
+      for (int i = 1; i <= n; ++i) (*v)[tw + i] = vtmp[i];
+    }
   }
 }
 

@@ -31,7 +31,7 @@ def lib(fast=False):
     dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
     ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
     L.orc_case_new.restype = C.c_void_p
-    L.orc_case_new.argtypes = [C.c_int] * 4 + [dp, dp, dp, ip, ip, ip, ip, C.c_int, ip, ip, ip]
+    L.orc_case_new.argtypes = [C.c_int] * 4 + [dp, dp, dp, ip, ip, ip, ip, C.c_int, ip, ip, ip, ip]
     L.orc_case_free.argtypes = [C.c_void_p]
     L.orc_case_sizes.argtypes = [C.c_void_p, ip]
     for f in ("orc_case_get", "orc_case_set"):
@@ -81,11 +81,12 @@ class Case:
         self.h = self.L.orc_case_new(m["numNodes"], m["numCells"], m["numInnerFaces"], m["numBoundaryFaces"],
                                      _f64(m["x"]), _f64(m["y"]), _f64(m["z"]), _i32(m["nnodes"]),
                                      _i32(m["nodes"]), _i32(m["owner"]), _i32(m["neighbour"]),
-                                     len(m["bctype"]), _i32(m["bctype"]), _i32(m["nfaces"]), _i32(m["startFace"]))
-        s = np.zeros(8, np.int32)
+                                     len(m["bctype"]), _i32(m["bctype"]), _i32(m["nfaces"]), _i32(m["startFace"]),
+                                     _i32(m.get("startFaceTwin", np.full(len(m["bctype"]), -1))))
+        s = np.zeros(9, np.int32)
         self.L.orc_case_sizes(self.h, s)
         (self.numCells, self.numInnerFaces, self.numBoundaryFaces, self.numFaces, self.numTotal, self.nnz,
-         self.nwal, self.nsym) = [int(v) for v in s]
+         self.nwal, self.nsym, self.numPeriodic) = [int(v) for v in s]
 
     def __del__(self):
         try:
@@ -107,7 +108,9 @@ class Case:
             return self.numCells
         if name in total:
             return self.numTotal
-        if name in ("facint", "Df", "ijk", "jik", "neighbour"):
+        if name in ("ijk", "jik"):
+            return self.numInnerFaces + self.numPeriodic
+        if name in ("facint", "Df", "neighbour"):
             return self.numInnerFaces
         if name in ("dUdxi", "dVdxi", "dWdxi", "dPdxi", "dTdxi"):
             return 3 * self.numTotal

@@ -51,6 +51,9 @@ def test_simple_iterations_with_pressure_outlet_track_oracle(ctx, fc, oracle):
 def test_piso_rejects_pressure_patches(ctx, fc, oracle):
     channel(oracle, dims=(6, 4, 4), ctx=ctx)
     ctx.transient_params(0.01, fc.FC_TIME_BDF, 1, 2)
-    with pytest.raises(fc.FcError) as e:
-        ctx.piso_iteration()
+    try:
+        with pytest.raises(fc.FcError) as e:
+            ctx.piso_iteration()
+    finally:
+        ctx.transient_params(1.0, fc.FC_TIME_STEADY, 0, 1)  # the shared context back to steady SIMPLE
     assert e.value.code == fc.FC_ERR_UNSUPPORTED and "PISO" in str(e.value)

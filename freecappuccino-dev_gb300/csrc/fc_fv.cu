@@ -206,6 +206,10 @@ MeshView mesh_view(fc_ctx* ctx) {
   v.arx = m.arx.p; v.ary = m.ary.p; v.arz = m.arz.p; v.xf = m.xf.p; v.yf = m.yf.p; v.zf = m.zf.p;
   v.xc = m.xc.p; v.yc = m.yc.p; v.zc = m.zc.p; v.vol = m.vol.p; v.facint = m.facint.p; v.Df = m.Df.p;
   v.ijk = m.ijk.p; v.jik = m.jik.p;
+  v.nPer = m.nPer; v.nIP = m.numInnerFaces + m.nPer;
+  v.pface = m.pface.p; v.ptwin = m.ptwin.p; v.ppos = m.ppos.p; v.pflag = m.pflag.p; v.bpair = m.bpair.p;
+  v.af_ptr = m.nPer ? m.af_ptr.p : m.cf_ptr.p;
+  v.af_ent = m.nPer ? m.af_ent.p : m.cf_face.p;
   v.diag = ctx->sys_mesh ? ctx->sys_mesh->diag.p : nullptr;
   v.ia = ctx->sys_mesh ? ctx->sys_mesh->ia.p : nullptr;
   return v;

@@ -36,6 +36,16 @@ struct MeshView {
   const double* __restrict__ Df;
   const int* __restrict__ ijk;
   const int* __restrict__ jik;
+  // periodic pairs (MeshDev): nIP = nI + nPer indexes pair q as slot-map
+  // entry nI + q
+  int nPer, nIP;
+  const int* __restrict__ pface;
+  const int* __restrict__ ptwin;
+  const int* __restrict__ ppos;
+  const int* __restrict__ pflag;
+  const int* __restrict__ bpair;
+  const int* __restrict__ af_ptr;
+  const int* __restrict__ af_ent;
   const int* __restrict__ diag;
   const int* __restrict__ ia;
 };

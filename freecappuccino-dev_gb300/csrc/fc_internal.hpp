@@ -158,9 +158,22 @@ struct MeshDev {
   DVec<double> arx, ary, arz, xf, yf, zf;  // numFaces
   DVec<double> xc, yc, zc, vol;            // numCells
   DVec<double> facint, Df;                 // numInnerFaces
-  DVec<int> ijk, jik;                      // face -> CSR slot (0-based)
+  DVec<int> ijk, jik;                      // face -> CSR slot (0-based); pairs after the inner faces
+  // periodic pairs q = 0..nPer-1 in the order of the reference's pair loops
+  // (periodic patches in order, faces in order): the periodic face, its
+  // twin face, the face's position in its patch, 1 when the twin patch
+  // comes before the periodic one; per boundary face the pair it belongs to
+  // (periodic or twin side) or -1
+  int nPer = 0;
+  DVec<int> pface, ptwin, ppos, pflag, bpair;
+  // per cell, the faces the assembly loops visit, in the reference's order:
+  // the cell -> face list without twin faces, with nF + q for a cell on the
+  // twin side of pair q placed where the periodic face's patch is visited;
+  // the cell -> face list itself when the mesh has no periodic pairs
+  DVec<int> af_ptr, af_ent;
   std::vector<int> h_owner, h_neighbour;
   std::vector<double> h_xyz;               // cell centroids x..., y..., z... (sweep tiling)
+  std::vector<double> h_face;              // face arrays during the periodic face mapping
 };
 
 struct FieldStore;

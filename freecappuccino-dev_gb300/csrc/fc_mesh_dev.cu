@@ -145,8 +145,10 @@ static void free_mesh_dev(MeshDev& m) {
                         &m.xc, &m.yc, &m.zc, &m.vol, &m.facint, &m.Df, &m.srdw};
   for (auto* v : dv) v->release();
   DVec<int>* iv[] = {&m.nnodes, &m.nodes, &m.owner, &m.neighbour, &m.bface_patch, &m.bface_wall,
-                     &m.cf_ptr, &m.cf_face, &m.ijk, &m.jik, &m.wall_face};
+                     &m.cf_ptr, &m.cf_face, &m.ijk, &m.jik, &m.wall_face, &m.pface, &m.ptwin,
+                     &m.ppos, &m.pflag, &m.bpair, &m.af_ptr, &m.af_ent};
   for (auto* v : iv) v->release();
+  m.nPer = 0;
   m.h_owner.clear(); m.h_neighbour.clear(); m.h_xyz.clear();
 }
 
@@ -172,7 +174,7 @@ extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
   FC_RANGE();
   if (!ctx || !hm) return FC_ERR_BAD_INPUT;
   std::string why;
-  if (hm->validate(&why) != FC_OK) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_set_mesh: " + why);
+  if (hm->validate(&why, true) != FC_OK) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_set_mesh: " + why);
   cudaSetDevice(ctx->device);
   fc_release_mesh(ctx);
   delete ctx->sys_mesh;
@@ -192,20 +194,22 @@ extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
   }
   for (int f = 0; f < nI; ++f) neighbour[f] = hm->neighbour[f] - 1;
   // cell -> faces, ascending face index
-  std::vector<int> cf_ptr(nC + 1, 0), cf_face;
-  for (int f = 0; f < nF; ++f) {
-    cf_ptr[owner[f] + 1]++;
-    if (f < nI) cf_ptr[neighbour[f] + 1]++;
-  }
-  for (int c = 0; c < nC; ++c) cf_ptr[c + 1] += cf_ptr[c];
-  cf_face.resize(cf_ptr[nC]);
-  {
+  std::vector<int> cf_ptr, cf_face;
+  auto cell_faces = [&]() {
+    cf_ptr.assign(nC + 1, 0);
+    for (int f = 0; f < nF; ++f) {
+      cf_ptr[owner[f] + 1]++;
+      if (f < nI) cf_ptr[neighbour[f] + 1]++;
+    }
+    for (int c = 0; c < nC; ++c) cf_ptr[c + 1] += cf_ptr[c];
+    cf_face.assign(cf_ptr[nC], 0);
     std::vector<int> pos(cf_ptr.begin(), cf_ptr.end() - 1);
     for (int f = 0; f < nF; ++f) {  // f ascending -> lists come out sorted
       cf_face[pos[owner[f]]++] = f;
       if (f < nI) cf_face[pos[neighbour[f]]++] = f;
     }
-  }
+  };
+  cell_faces();
   // boundary face -> patch, wall counter
   std::vector<int> bpatch(nB, -1), bwall(nB, -1), wall_face;
   int iwall = 0;
@@ -219,45 +223,6 @@ extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
     if (hm->bctype[b] == FC_BC_WALL) m.nwal += hm->nfaces[b];
     if (hm->bctype[b] == FC_BC_SYMMETRY) m.nsym += hm->nfaces[b];
   }
-  // CSR pattern: row i = sorted {i} U {cells sharing an inner face}; the
-  // reference sorts (row, col) pairs lexicographically, which gives exactly
-  // these rows (sparse_matrix.f90:110-202)
-  const int nnz = 2 * nI + nC;
-  std::vector<int> ia(nC + 1, 0), ja(nnz), diag(nC), ijk(nI), jik(nI);
-  for (int c = 0; c < nC; ++c) ia[c + 1] = 1 + (cf_ptr[c + 1] - cf_ptr[c]);
-  // boundary faces do not make matrix entries
-  for (int f = nI; f < nF; ++f) ia[owner[f] + 1]--;
-  for (int c = 0; c < nC; ++c) ia[c + 1] += ia[c];
-  if (ia[nC] != nnz) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_set_mesh: inconsistent face lists");
-  {
-    std::vector<int> cols;
-    for (int c = 0; c < nC; ++c) {
-      cols.clear();
-      cols.push_back(c);
-      for (int q = cf_ptr[c]; q < cf_ptr[c + 1]; ++q) {
-        int f = cf_face[q];
-        if (f >= nI) continue;
-        cols.push_back(owner[f] == c ? neighbour[f] : owner[f]);
-      }
-      std::sort(cols.begin(), cols.end());
-      for (size_t k = 0; k < cols.size(); ++k) {
-        ja[ia[c] + k] = cols[k];
-        if (cols[k] == c) diag[c] = ia[c] + (int)k;
-      }
-    }
-    // csr_to_k (utils.f90:96-147): first slot of row icell holding jcell
-    auto csr_to_k = [&](int icell, int jcell) {
-      for (int l = ia[icell]; l < ia[icell + 1]; ++l)
-        if (ja[l] == jcell) return l;
-      return -1;
-    };
-    for (int f = 0; f < nI; ++f) {
-      ijk[f] = csr_to_k(owner[f], neighbour[f]);
-      jik[f] = csr_to_k(neighbour[f], owner[f]);
-    }
-  }
-  m.h_owner = owner;
-  m.h_neighbour = neighbour;
   UP(m.x, hm->x.data(), nN); UP(m.y, hm->y.data(), nN); UP(m.z, hm->z.data(), nN);
   UP(m.nnodes, hm->nnodes.data(), nF);
   UP(m.nodes, nodes.data(), nodes.size());
@@ -268,8 +233,6 @@ extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
   UP(m.bface_patch, bpatch.data(), nB);
   UP(m.bface_wall, bwall.data(), nB);
   UP(m.wall_face, wall_face.data(), wall_face.size());
-  UP(m.ijk, ijk.data(), nI);
-  UP(m.jik, jik.data(), nI);
   DVec<double>* fv[] = {&m.arx, &m.ary, &m.arz, &m.xf, &m.yf, &m.zf};
   for (auto* v : fv) FC_CUDA_TRY(ctx, v->alloc(nF));
   DVec<double>* cv[] = {&m.xc, &m.yc, &m.zc, &m.vol};
@@ -293,6 +256,162 @@ extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
     ctx->kernel_launches++;
   }
   FC_CUDA_TRY(ctx, cudaGetLastError());
+  m.h_xyz.resize((size_t)3 * nC);
+  FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, m.h_xyz.data(), m.xc.p, nC * sizeof(double)));
+  FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, m.h_xyz.data() + nC, m.yc.p, nC * sizeof(double)));
+  FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, m.h_xyz.data() + 2 * (size_t)nC, m.zc.p, nC * sizeof(double)));
+  // periodic pairs, face_mapping (geometry.f90:1848-1997), after the
+  // geometry as there: face i of a periodic patch pairs with the twin face
+  // whose owner's centre is nearest (L1) to face i's centre, first of equals;
+  // the twin faces' owners, centres and area vectors are then reordered so
+  // that twin face i belongs to pair i
+  std::vector<int> pface, ptwin, ppos, pflag, bpair(nB, -1);
+  for (int b = 0; b < m.numBoundaries; ++b) {
+    if (hm->bctype[b] != FC_BC_PERIODIC) continue;
+    if (pface.empty()) {
+      std::vector<double> h((size_t)6 * nF);
+      for (int k = 0; k < 6; ++k) FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, h.data() + (size_t)k * nF, fv[k]->p, nF * sizeof(double)));
+      m.h_face.swap(h);
+    }
+    const double* xc = m.h_xyz.data();
+    const double *yc = xc + nC, *zc = xc + 2 * (size_t)nC;
+    const double *hxf = m.h_face.data() + 3 * (size_t)nF, *hyf = hxf + nF, *hzf = hxf + 2 * (size_t)nF;
+    const int n = hm->nfaces[b], sf = hm->startFace[b], tw = hm->twin_of(b);
+    int tp = 0;
+    while (hm->startFace[tp] != tw) ++tp;  // validated: the twin patch exists
+    std::vector<int> tmp(n), itmp(n), hit(n, 0);
+    for (int i = 0; i < n; ++i) {
+      const int f = sf + i;
+      double mindist = (double)1e+30f;
+      int best = 0;
+      for (int it = 0; it < n; ++it) {
+        const int c = owner[tw + it];
+        const double dist = std::fabs(hxf[f] - xc[c]) + std::fabs(hyf[f] - yc[c]) + std::fabs(hzf[f] - zc[c]);
+        if (dist < mindist) { mindist = dist; best = it; }
+      }
+      itmp[i] = best;
+      tmp[i] = owner[tw + best];
+      if (hit[best]++) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_set_mesh: periodic face mapping is not one to one");
+    }
+    for (int i = 0; i < n; ++i) owner[tw + i] = tmp[i];
+    for (int k = 0; k < 6; ++k) {
+      double* v = m.h_face.data() + (size_t)k * nF;
+      std::vector<double> vt(n);
+      for (int i = 0; i < n; ++i) vt[i] = v[tw + itmp[i]];
+      for (int i = 0; i < n; ++i) v[tw + i] = vt[i];
+    }
+    for (int i = 0; i < n; ++i) {
+      const int q = (int)pface.size();
+      pface.push_back(sf + i);
+      ptwin.push_back(tw + i);
+      ppos.push_back(i);
+      pflag.push_back(tp < b ? 1 : 0);
+      bpair[sf + i - nI] = q;
+      bpair[tw + i - nI] = q;
+      if (owner[sf + i] == owner[tw + i])
+        return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "fc_set_mesh: a periodic pair couples a cell with itself");
+    }
+  }
+  const int nPer = (int)pface.size();
+  m.nPer = nPer;
+  if (nPer > 0) {
+    for (int k = 0; k < 6; ++k)
+      FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, fv[k]->p, m.h_face.data() + (size_t)k * nF, nF * sizeof(double)));
+    m.h_face.clear();
+    m.h_face.shrink_to_fit();
+    FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, m.owner.p, owner.data(), nF * sizeof(int)));
+    cell_faces();  // the twin faces moved to their pairs' cells
+    FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, m.cf_ptr.p, cf_ptr.data(), cf_ptr.size() * sizeof(int)));
+    FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, m.cf_face.p, cf_face.data(), cf_face.size() * sizeof(int)));
+  }
+  // CSR pattern: row i = sorted {i} U {cells sharing an inner face} U {cells
+  // paired with i through periodic faces}; the reference sorts (row, col)
+  // pairs lexicographically, which gives exactly these rows
+  // (sparse_matrix.f90:110-202).  A cell pair coupled twice (an inner face and
+  // a periodic pair) would make a repeated column, which is rejected.
+  const int nnz = 2 * (nI + nPer) + nC;
+  std::vector<int> ia(nC + 1, 0), ja(nnz), diag(nC), ijk(nI + nPer), jik(nI + nPer);
+  {
+    std::vector<std::vector<int>> extra(nPer ? nC : 0);
+    for (int q = 0; q < nPer; ++q) {
+      const int ijp = owner[pface[q]], ijn = owner[ptwin[q]];
+      extra[ijp].push_back(ijn);
+      extra[ijn].push_back(ijp);
+    }
+    std::vector<int> cols;
+    int k0 = 0;
+    for (int c = 0; c < nC; ++c) {
+      cols.clear();
+      cols.push_back(c);
+      for (int q = cf_ptr[c]; q < cf_ptr[c + 1]; ++q) {
+        int f = cf_face[q];
+        if (f >= nI) continue;
+        cols.push_back(owner[f] == c ? neighbour[f] : owner[f]);
+      }
+      if (nPer) cols.insert(cols.end(), extra[c].begin(), extra[c].end());
+      std::sort(cols.begin(), cols.end());
+      for (size_t k = 1; k < cols.size(); ++k)
+        if (cols[k] == cols[k - 1])
+          return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "fc_set_mesh: two cells coupled twice (an inner face and a "
+                                                      "periodic pair, or two faces)");
+      ia[c] = k0;
+      for (size_t k = 0; k < cols.size(); ++k) {
+        ja[k0 + k] = cols[k];
+        if (cols[k] == c) diag[c] = k0 + (int)k;
+      }
+      k0 += (int)cols.size();
+    }
+    ia[nC] = k0;
+    if (k0 != nnz) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_set_mesh: inconsistent face lists");
+    // csr_to_k (utils.f90:96-147): first slot of row icell holding jcell
+    auto csr_to_k = [&](int icell, int jcell) {
+      for (int l = ia[icell]; l < ia[icell + 1]; ++l)
+        if (ja[l] == jcell) return l;
+      return -1;
+    };
+    for (int f = 0; f < nI; ++f) {
+      ijk[f] = csr_to_k(owner[f], neighbour[f]);
+      jik[f] = csr_to_k(neighbour[f], owner[f]);
+    }
+    for (int q = 0; q < nPer; ++q) {  // sparse_matrix.f90:262-292
+      const int ijp = owner[pface[q]], ijn = owner[ptwin[q]];
+      ijk[nI + q] = csr_to_k(ijp, ijn);
+      jik[nI + q] = csr_to_k(ijn, ijp);
+    }
+  }
+  UP(m.ijk, ijk.data(), ijk.size());
+  UP(m.jik, jik.data(), jik.size());
+  if (nPer > 0) {
+    // the assembly lists: a twin face leaves its cell's list, the pair
+    // enters the twin-side cell's list at the periodic face's place
+    std::vector<int> af_ptr(nC + 1, 0), af_ent;
+    af_ent.reserve(cf_face.size());
+    std::vector<std::vector<int>> tside(nC);
+    for (int q = 0; q < nPer; ++q) tside[owner[ptwin[q]]].push_back(q);
+    std::vector<int> row;
+    auto key = [&](int e) { return e < nF ? e : pface[e - nF]; };
+    for (int c = 0; c < nC; ++c) {
+      row.clear();
+      for (int q = cf_ptr[c]; q < cf_ptr[c + 1]; ++q) {
+        const int f = cf_face[q];
+        if (f >= nI && bpair[f - nI] >= 0 && ptwin[bpair[f - nI]] == f) continue;
+        row.push_back(f);
+      }
+      for (int q : tside[c]) row.push_back(nF + q);
+      std::stable_sort(row.begin(), row.end(), [&](int a, int b) { return key(a) < key(b); });
+      af_ent.insert(af_ent.end(), row.begin(), row.end());
+      af_ptr[c + 1] = (int)af_ent.size();
+    }
+    UP(m.af_ptr, af_ptr.data(), af_ptr.size());
+    UP(m.af_ent, af_ent.data(), af_ent.size());
+    UP(m.pface, pface.data(), nPer);
+    UP(m.ptwin, ptwin.data(), nPer);
+    UP(m.ppos, ppos.data(), nPer);
+    UP(m.pflag, pflag.data(), nPer);
+  }
+  UP(m.bpair, bpair.data(), nB);
+  m.h_owner = owner;
+  m.h_neighbour = neighbour;
   FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   // the global matrix system of the mesh (module globals ia, ja, a, diag)
   CsrSystem* s = new CsrSystem();
@@ -300,10 +419,6 @@ extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
   for (auto& v : ia1) ++v;
   for (auto& v : ja1) ++v;
   for (auto& v : dg1) ++v;
-  m.h_xyz.resize((size_t)3 * nC);
-  FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, m.h_xyz.data(), m.xc.p, nC * sizeof(double)));
-  FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, m.h_xyz.data() + nC, m.yc.p, nC * sizeof(double)));
-  FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, m.h_xyz.data() + 2 * (size_t)nC, m.zc.p, nC * sizeof(double)));
   int st = sys_set_pattern(ctx, s, nC, nnz, ia1.data(), ja1.data(), dg1.data(), m.h_xyz.data());
   if (st) { delete s; return st; }
   FC_CUDA_TRY(ctx, fc_zero(ctx->stream, s->a.p, (size_t)nnz * sizeof(double)));
@@ -331,8 +446,9 @@ extern "C" int fc_get_geometry(fc_ctx* ctx, const char* name, double* out) {
 }
 
 // CSR pattern and face -> slot maps of the mesh, 1-based as the reference
-// stores them (ia(n+1), ja(nnz), diag(n), icell_jcell_csr_index(nI),
-// jcell_icell_csr_index(nI)); any pointer may be NULL
+// stores them (ia(n+1), ja(nnz), diag(n), icell_jcell_csr_index(nI + nPer),
+// jcell_icell_csr_index(nI + nPer): the inner faces, then the periodic
+// pairs); any pointer may be NULL
 extern "C" int fc_get_csr_pattern(fc_ctx* ctx, int* n_out, int* nnz_out, int* ia, int* ja, int* diag, int* ijk,
                                   int* jik) {
   if (!ctx) return FC_ERR_BAD_INPUT;
@@ -343,7 +459,7 @@ extern "C" int fc_get_csr_pattern(fc_ctx* ctx, int* n_out, int* nnz_out, int* ia
   if (ia) for (int i = 0; i <= s->n; ++i) ia[i] = s->h_ia[i] + 1;
   if (ja) for (int k = 0; k < s->nnz; ++k) ja[k] = s->h_ja[k] + 1;
   if (diag) for (int i = 0; i < s->n; ++i) diag[i] = s->h_diag[i] + 1;
-  const int nI = ctx->mesh.numInnerFaces;
+  const int nI = ctx->mesh.numInnerFaces + ctx->mesh.nPer;
   if (ijk || jik) {
     std::vector<int> t(nI);
     if (ijk) {

@@ -88,6 +88,10 @@ int node_interp_prepare(fc_ctx* ctx) {
 }  // namespace
 
 int fv_grad_node(fc_ctx* ctx, const double* phi, double* g) {
+  // face_mapping moves a twin face's owner and centre but not its nodes; the
+  // node interpolation of such a mesh is not restated here
+  if (ctx->mesh.nPer)
+    return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "node-based gradients are not supported on meshes with periodic pairs");
   int st = node_interp_prepare(ctx);
   if (st) return st;
   MeshView M = mesh_view(ctx);

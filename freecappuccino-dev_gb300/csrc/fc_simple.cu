@@ -273,8 +273,64 @@ __global__ void k_mom_face(MeshView M, Dev D, MomParams P) {
     D.a[M.ijk[i]] = can;
     D.a[M.jik[i]] = cap;
     D.fscr[i] = -(gam * (fuhigh - fuuds)) + fdue;
-    D.fscr[M.nI + i] = -(gam * (fvhigh - fvuds)) + fdve;
-    D.fscr[2 * (size_t)M.nI + i] = -(gam * (fwhigh - fwuds)) + fdwe;
+    D.fscr[M.nIP + i] = -(gam * (fvhigh - fvuds)) + fdve;
+    D.fscr[2 * (size_t)M.nIP + i] = -(gam * (fwhigh - fwuds)) + fdwe;
+  }
+}
+
+// facefluxuvw_periodic, velocity.f90:1038-1179, per periodic pair (the
+// periodic branch of calcuvw's boundary loop, :393-430): central weights
+// 1/2, the distance vector 2 (xf - xc(ijp)), the full stress tensor of the
+// face gradient, cds face values; a(k_ij) = can, a(k_ji) = cap, sources to
+// scratch entry nI + q
+__global__ void k_mom_pair(MeshView M, Dev D, MomParams P) {
+  const int nT = M.nT;
+  const Fld gu{D.gu, nT}, gv{D.gv, nT}, gw{D.gw, nT};
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < M.nPer; q += gridDim.x * blockDim.x) {
+    const int f = M.pface[q], ijp = M.owner[f], ijn = M.owner[M.ptwin[q]];
+    const double xf = M.xf[f], yf = M.yf[f], zf = M.zf[f], arx = M.arx[f], ary = M.ary[f], arz = M.arz[f];
+    const double flomass = D.flmass[f], gam = P.gds;
+    const double fxn = 0.5, fxp = fxn;
+    const double xpn = 2 * (xf - M.xc[ijp]), ypn = 2 * (yf - M.yc[ijp]), zpn = 2 * (zf - M.zc[ijp]);
+    const double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
+    const double are = sqrt(arx * arx + ary * ary + arz * arz);
+    const double game = D.vis[ijp] * fxp + D.vis[ijn] * fxn;
+    const double de = game * (arx * arx + ary * ary + arz * arz) / (xpn * arx + ypn * ary + zpn * arz);
+    const double ce = fmin(flomass, 0.0), cp = fmax(flomass, 0.0);
+    const double can = -de + ce;
+    const double cap = -de - cp;
+    const double duxi = gu.x(ijp) * fxp + gu.x(ijn) * fxn, duyi = gu.y(ijp) * fxp + gu.y(ijn) * fxn,
+                 duzi = gu.z(ijp) * fxp + gu.z(ijn) * fxn;
+    const double dvxi = gv.x(ijp) * fxp + gv.x(ijn) * fxn, dvyi = gv.y(ijp) * fxp + gv.y(ijn) * fxn,
+                 dvzi = gv.z(ijp) * fxp + gv.z(ijn) * fxn;
+    const double dwxi = gw.x(ijp) * fxp + gw.x(ijn) * fxn, dwyi = gw.y(ijp) * fxp + gw.y(ijn) * fxn,
+                 dwzi = gw.z(ijp) * fxp + gw.z(ijn) * fxn;
+    const double fdue = game * ((duxi + duxi) * arx + (duyi + dvxi) * ary + (duzi + dwxi) * arz);
+    const double fdve = game * ((duyi + dvxi) * arx + (dvyi + dvyi) * ary + (dvzi + dwyi) * arz);
+    const double fdwe = game * ((duzi + dwxi) * arx + (dwyi + dvzi) * ary + (dwzi + dwzi) * arz);
+    const double fdui = game * are / dpn * (duxi * xpn + duyi * ypn + duzi * zpn);
+    const double fdvi = game * are / dpn * (dvxi * xpn + dvyi * ypn + dvzi * zpn);
+    const double fdwi = game * are / dpn * (dwxi * xpn + dwyi * ypn + dwzi * zpn);
+    const double fuuds = cp * D.u[ijp] + ce * D.u[ijn];
+    const double fvuds = cp * D.v[ijp] + ce * D.v[ijn];
+    const double fwuds = cp * D.w[ijp] + ce * D.w[ijn];
+    double ue, ve, we;
+    if (flomass >= 0.0) {  // face_value_cds, interpolation.f90:116-157
+      ue = D.u[ijp] + (D.u[ijn] - D.u[ijp]) * fxp;
+      ve = D.v[ijp] + (D.v[ijn] - D.v[ijp]) * fxp;
+      we = D.w[ijp] + (D.w[ijn] - D.w[ijp]) * fxp;
+    } else {
+      ue = D.u[ijn] + (D.u[ijp] - D.u[ijn]) * fxn;
+      ve = D.v[ijn] + (D.v[ijp] - D.v[ijn]) * fxn;
+      we = D.w[ijn] + (D.w[ijp] - D.w[ijn]) * fxn;
+    }
+    const double fuhigh = flomass * ue, fvhigh = flomass * ve, fwhigh = flomass * we;
+    const int l = M.nI + q;
+    D.a[M.ijk[l]] = can;
+    D.a[M.jik[l]] = cap;
+    D.fscr[l] = -gam * (fuhigh - fuuds) + fdue - fdui;
+    D.fscr[M.nIP + l] = -gam * (fvhigh - fvuds) + fdve - fdvi;
+    D.fscr[2 * (size_t)M.nIP + l] = -gam * (fwhigh - fwuds) + fdwe - fdwi;
   }
 }
 
@@ -318,7 +374,8 @@ __device__ void facefluxuvw_bnd(const MeshView& M, const Dev& D, int ijp, int ij
 }
 
 // sources and diagonal contributions per cell: inner-face sources in face
-// order (velocity.f90:306-313), then the boundary conditions (:326-562)
+// order (velocity.f90:306-313), then the boundary conditions (:326-562) in
+// patch order, the periodic pairs' sources on both of their cells (:393-430)
 __global__ void k_mom_cell(MeshView M, Dev D, MomParams P) {
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
     double su = D.su[c], sv = D.sv[c], sw = D.sw[c];
@@ -343,17 +400,21 @@ __global__ void k_mom_cell(MeshView M, Dev D, MomParams P) {
         spu = spu + 11. / 6.0 * apotime; spv = spv + 11. / 6.0 * apotime; sp = sp + 11. / 6.0 * apotime;
       }
     }
-    for (int q = M.cf_ptr[c]; q < M.cf_ptr[c + 1]; ++q) {
-      const int f = M.cf_face[q];
-      if (f < M.nI) {
-        const double sup = D.fscr[f], svp = D.fscr[M.nI + f], swp = D.fscr[2 * (size_t)M.nI + f];
-        if (M.owner[f] == c) { su = su + sup; sv = sv + svp; sw = sw + swp; }
+    for (int q = M.af_ptr[c]; q < M.af_ptr[c + 1]; ++q) {
+      const int f = M.af_ent[q];
+      if (f < M.nI || f >= M.nF) {  // inner face, or the twin side of pair f - nF
+        const int l = f < M.nI ? f : M.nI + (f - M.nF);
+        const double sup = D.fscr[l], svp = D.fscr[M.nIP + l], swp = D.fscr[2 * (size_t)M.nIP + l];
+        if (f < M.nI && M.owner[f] == c) { su = su + sup; sv = sv + svp; sw = sw + swp; }
         else { su = su - sup; sv = sv - svp; sw = sw - swp; }
         continue;
       }
       const int bi = f - M.nI, ijb = M.nC + bi, ijp = c;
       const int t = D.ptype[M.bpatch[bi]];
-      if (t == FC_BC_INLET || t == FC_BC_OUTLET || t == FC_BC_PRESSURE) {
+      if (t == FC_BC_PERIODIC) {  // the owner side of pair bpair
+        const int l = M.nI + M.bpair[bi];
+        su = su + D.fscr[l]; sv = sv + D.fscr[M.nIP + l]; sw = sw + D.fscr[2 * (size_t)M.nIP + l];
+      } else if (t == FC_BC_INLET || t == FC_BC_OUTLET || t == FC_BC_PRESSURE) {
         double cb, sup, svp, swp;
         facefluxuvw_bnd(M, D, ijp, ijb, f, cb, sup, svp, swp);
         spu = spu - cb; spv = spv - cb; sp = sp - cb;
@@ -479,22 +540,69 @@ __global__ void k_p_press_corr(MeshView M, Dev D) {
   }
 }
 
+// facefluxmass2_periodic, faceflux_mass.f90:313-384, per periodic pair (the
+// periodic branch of calcp_simple.f90:185-225 and calcp_piso.f90:248-289):
+// the pair's mass flux through its periodic face, cap in both slots.  Df is
+// indexed by the face's position within its patch, as the reference writes it.
+__global__ void k_p_pair(MeshView M, Dev D) {
+  const Fld gp{D.gp, M.nT};
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < M.nPer; q += gridDim.x * blockDim.x) {
+    const int f = M.pface[q], ijp = M.owner[f], ijn = M.owner[M.ptwin[q]];
+    const double arx = M.arx[f], ary = M.ary[f], arz = M.arz[f];
+    const double lambda = 0.5, fxn = lambda, fxp = 1.0 - lambda;
+    const double xpn = 2 * (M.xf[f] - M.xc[ijp]), ypn = 2 * (M.yf[f] - M.yc[ijp]), zpn = 2 * (M.zf[f] - M.zc[ijp]);
+    const double dene = D.den[ijp] * fxp + D.den[ijn] * fxn;
+    double Kj = M.vol[ijp] * D.apu[ijp] * fxp + M.vol[ijn] * D.apu[ijn] * fxn;
+    const double cap = -(dene * Kj * M.Df[M.ppos[q]]);
+    Kj = (D.apu[ijp] + D.apu[ijn] + SMALL);
+    const double ui = (D.u[ijp] * D.apu[ijn] + D.u[ijn] * D.apu[ijp]) / Kj;
+    const double vi = (D.v[ijp] * D.apv[ijn] + D.v[ijn] * D.apv[ijp]) / Kj;
+    const double wi = (D.w[ijp] * D.apw[ijn] + D.w[ijn] * D.apw[ijp]) / Kj;
+    const double dpxi = (gp.x(ijn) * fxp + gp.x(ijp) * fxn) * xpn;
+    const double dpyi = (gp.y(ijn) * fxp + gp.y(ijp) * fxn) * ypn;
+    const double dpzi = (gp.z(ijn) * fxp + gp.z(ijp) * fxn) * zpn;
+    D.flmass[f] = dene * (ui * arx + vi * ary + wi * arz) + cap * (D.p[ijn] - D.p[ijp] - dpxi - dpyi - dpzi);
+    const int l = M.nI + q;
+    D.a[M.ijk[l]] = cap;
+    D.a[M.jik[l]] = cap;
+  }
+}
+
+// flux correction of the periodic pairs (calcp_simple.f90:322-342 with
+// phi = pp, calcp_piso.f90:437-456 with phi = p): the twin face takes the
+// periodic face's corrected mass flux
+__global__ void k_flux_correct_pair(MeshView M, Dev D, const double* __restrict__ phi) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < M.nPer; q += gridDim.x * blockDim.x) {
+    const int f = M.pface[q], t = M.ptwin[q], ijp = M.owner[f], ijn = M.owner[t];
+    const double fm = D.flmass[f] + D.a[M.ijk[M.nI + q]] * (phi[ijn] - phi[ijp]);
+    D.flmass[f] = fm;
+    D.flmass[t] = fm;
+  }
+}
+
 // diagonal -sum(cap) and source -/+flmass in face order (calcp_simple.f90:104-117),
-// then inlet/outlet mass fluxes and pressure faces (:131-183); a cell's
-// boundary faces follow its inner faces and come in patch order, the order
-// of the reference's loops
+// then inlet/outlet mass fluxes, pressure faces and periodic pairs
+// (:131-225); a cell's boundary faces follow its inner faces and come in
+// patch order, the order of the reference's loops
 __global__ void k_p_cell(MeshView M, Dev D, const double* __restrict__ bcap) {
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
     double ad = 0.0, s = 0.0;
-    for (int q = M.cf_ptr[c]; q < M.cf_ptr[c + 1]; ++q) {
-      const int f = M.cf_face[q];
+    for (int q = M.af_ptr[c]; q < M.af_ptr[c + 1]; ++q) {
+      const int f = M.af_ent[q];
       if (f < M.nI) {
         ad = ad - D.a[M.ijk[f]];
         if (M.owner[f] == c) s = s - D.flmass[f];
         else s = s + D.flmass[f];
+      } else if (f >= M.nF) {  // the twin side of pair f - nF
+        const int pq = f - M.nF;
+        ad = ad - D.a[M.ijk[M.nI + pq]];
+        s = s + D.flmass[M.pface[pq]];
       } else {
         const int t = D.ptype[M.bpatch[f - M.nI]];
-        if (t == FC_BC_INLET || t == FC_BC_OUTLET) s = s - D.flmass[f];
+        if (t == FC_BC_PERIODIC) {
+          ad = ad - D.a[M.ijk[M.nI + M.bpair[f - M.nI]]];
+          s = s - D.flmass[f];
+        } else if (t == FC_BC_INLET || t == FC_BC_OUTLET) s = s - D.flmass[f];
         else if (t == FC_BC_PRESSURE) {
           ad = ad - bcap[f - M.nI];
           s = s - D.flmass[f];
@@ -807,6 +915,44 @@ __global__ void k_sc_face(MeshView M, Dev D, ScParams P) {
   }
 }
 
+// facefluxsc_periodic, scalar_fluxes.f90:147-251, per periodic pair (the
+// periodic branch of temperature.f90:262-313): the diffusion coefficient
+// with facint, and Df, of the face's position within its patch, as written
+// there; central weights 1/2, cds face value; a(k_ij) = can, a(k_ji) = cap,
+// suadd to scratch entry nI + q
+__global__ void k_sc_pair(MeshView M, Dev D, ScParams P) {
+  const Fld g{D.gt, M.nT};
+  const double* fi = D.t;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < M.nPer; q += gridDim.x * blockDim.x) {
+    const int f = M.pface[q], ijp = M.owner[f], ijn = M.owner[M.ptwin[q]], i = M.ppos[q];
+    const double dcoef =
+        P.viscos * P.prl + ((D.vis[ijp] + (D.vis[ijn] - D.vis[ijp]) * M.facint[i]) - P.viscos) * P.prtr;
+    const double arx = M.arx[f], ary = M.ary[f], arz = M.arz[f], fm = D.flmass[f];
+    const double fxn = 0.5, fxp = fxn;
+    const double xpn = 2 * (M.xf[f] - M.xc[ijp]), ypn = 2 * (M.yf[f] - M.yc[ijp]), zpn = 2 * (M.zf[f] - M.zc[ijp]);
+    const double Df = M.Df[i];
+    const double de = dcoef * Df;
+    const double ce = fmin(fm, 0.0), cp = fmax(fm, 0.0);
+    const double can = -de + ce;
+    const double cap = -de - cp;
+    double dfixi = g.x(ijp) * fxp + g.x(ijn) * fxn;
+    double dfiyi = g.y(ijp) * fxp + g.y(ijn) * fxn;
+    double dfizi = g.z(ijp) * fxp + g.z(ijn) * fxn;
+    dfixi = dfixi * (arx - Df * xpn);
+    dfiyi = dfiyi * (ary - Df * ypn);
+    dfizi = dfizi * (arz - Df * zpn);
+    const double fdfie = dcoef * (dfixi + dfiyi + dfizi);
+    const double fii = fm >= 0.0 ? fi[ijp] + (fi[ijn] - fi[ijp]) * fxp : fi[ijn] + (fi[ijp] - fi[ijn]) * fxn;
+    double fcfie = fm * fii;
+    const double fcfii = ce * fi[ijn] + cp * fi[ijp];
+    fcfie = P.gam * (fcfie - fcfii);
+    const int l = M.nI + q;
+    D.a[M.ijk[l]] = can;
+    D.a[M.jik[l]] = cap;
+    D.fscr[l] = -fcfie + fdfie;
+  }
+}
+
 // per cell in face order: the main-diagonal accumulation a(diag) -= can/cap
 // and su +/- suadd of the inner faces (temperature.f90:137-155), then the
 // boundary conditions of :166-225 (facefluxsc_boundary, scalar_fluxes.f90:256-337)
@@ -814,14 +960,26 @@ __global__ void k_sc_cell(MeshView M, Dev D, ScParams P) {
   const Fld g{D.gt, M.nT};
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
     double ad = 0.0, su = 0.0, sp = 0.0;
-    for (int q = M.cf_ptr[c]; q < M.cf_ptr[c + 1]; ++q) {
-      const int f = M.cf_face[q];
+    for (int q = M.af_ptr[c]; q < M.af_ptr[c + 1]; ++q) {
+      const int f = M.af_ent[q];
       if (f < M.nI) {
         if (M.owner[f] == c) { ad = ad - D.a[M.ijk[f]]; su = su + D.fscr[f]; }
         else { ad = ad - D.a[M.jik[f]]; su = su - D.fscr[f]; }
         continue;
       }
+      if (f >= M.nF) {  // the twin side of pair f - nF
+        const int l = M.nI + (f - M.nF);
+        ad = ad - D.a[M.jik[l]];
+        su = su - D.fscr[l];
+        continue;
+      }
       const int bi = f - M.nI, ijb = M.nC + bi, ijp = c, b = M.bpatch[bi];
+      if (D.ptype[b] == FC_BC_PERIODIC) {
+        const int l = M.nI + M.bpair[bi];
+        ad = ad - D.a[M.ijk[l]];
+        su = su + D.fscr[l];
+        continue;
+      }
       const int kind = P.pkind[b];
       if (kind == SC_FLOW) {
         const double dcoef = P.viscos * P.prl + (D.vis[ijp] - P.viscos) / P.sigt;
@@ -853,13 +1011,21 @@ __global__ void k_sc_cell(MeshView M, Dev D, ScParams P) {
   }
 }
 
-// updateBoundary(T), updateBoundary.f90 (no periodic pairs): outlet,
-// symmetry, pressure and empty faces take the owner's value
+// updateBoundary(T), updateBoundary.f90:1-77: outlet, symmetry, pressure
+// and empty faces take the owner's value; a periodic face and its twin the
+// mean of the pair's cells.  The reference visits the patches in order, so a
+// twin face ends with the mean when its patch comes before the periodic one,
+// else with its owner's value.
 __global__ void k_update_boundary(MeshView M, const int* __restrict__ ptype, double* __restrict__ phi) {
   for (int bi = blockIdx.x * blockDim.x + threadIdx.x; bi < M.nB; bi += gridDim.x * blockDim.x) {
     const int t = ptype[M.bpatch[bi]];
-    if (t == FC_BC_OUTLET || t == FC_BC_SYMMETRY || t == FC_BC_PRESSURE || t == FC_BC_EMPTY)
+    const int q = M.nPer ? M.bpair[bi] : -1;
+    if (t == FC_BC_PERIODIC || (q >= 0 && M.pflag[q])) {
+      const int ijp = M.owner[M.pface[q]], ijn = M.owner[M.ptwin[q]];
+      phi[M.nC + bi] = 0.5 * (phi[ijp] + phi[ijn]);
+    } else if (t == FC_BC_OUTLET || t == FC_BC_SYMMETRY || t == FC_BC_PRESSURE || t == FC_BC_EMPTY) {
       phi[M.nC + bi] = phi[M.owner[M.nI + bi]];
+    }
   }
 }
 
@@ -965,8 +1131,6 @@ static int make_dev(fc_ctx* ctx, Dev& D, bool allow_pressure = true) {
       FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, S.ptype.p, m.h_bctype.data(), m.numBoundaries * sizeof(int)));
   }
   for (int b = 0; b < m.numBoundaries; ++b) {
-    if (m.h_bctype[b] == FC_BC_PERIODIC)
-      return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "periodic boundaries are not supported on this path");
     if (m.h_bctype[b] == FC_BC_PRESSURE && !allow_pressure)
       return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "pressure boundaries are not supported by the PISO corrector");
   }
@@ -1133,6 +1297,10 @@ extern "C" int fc_calcuvw(fc_ctx* ctx, double* resor) {
   if (M.nB > 0) FC_CUDA_TRY(ctx, cudaMemcpyAsync(&mp.vis_sym, D.vis + M.nC, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   if (M.nI) k_mom_face<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D, mp);
+  if (M.nPer) {
+    k_mom_pair<<<gridn(M.nPer), 256, 0, ctx->stream>>>(M, D, mp);
+    ctx->kernel_launches++;
+  }
   k_mom_cell<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D, mp);
   ctx->kernel_launches += 2;
   FC_CUDA_TRY(ctx, cudaGetLastError());
@@ -1206,7 +1374,7 @@ extern "C" int fc_calcuvw(fc_ctx* ctx, double* resor) {
 }
 
 // calcp_simple, calcp_simple.f90:1-470 (incompressible; pressure
-// boundaries, no periodic pairs).  *resor4 receives resor(4) as
+// boundaries and periodic pairs).  *resor4 receives resor(4) as
 // continuityErrors sets it.
 // continuityErrors, continuityErrors.f90:1-77: resor(4) into *resor4
 static int continuity_errors(fc_ctx* ctx, const Dev& D, double* resor4) {
@@ -1243,6 +1411,10 @@ extern "C" int fc_calcp_simple(fc_ctx* ctx, double* resor4) {
   const fc_simple_params& P = S.prm;
   MeshView M = mesh_view(ctx);
   if (M.nI) k_p_face<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D);
+  if (M.nPer) {
+    k_p_pair<<<gridn(M.nPer), 256, 0, ctx->stream>>>(M, D);
+    ctx->kernel_launches++;
+  }
   bool outlets = false, pressure = false;
   for (int b = 0; b < ctx->mesh.numBoundaries; ++b) {
     outlets |= ctx->mesh.h_bctype[b] == FC_BC_OUTLET;
@@ -1261,6 +1433,10 @@ extern "C" int fc_calcp_simple(fc_ctx* ctx, double* resor4) {
     st = solve_into(ctx, P.lSolverP, D.pp, D.su, &r4, P.maxiterP, P.tolAbsP, P.tolRelP, "p");
     if (st < 0) return st;
     if (M.nI) k_flux_correct<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D);
+    if (M.nPer) {
+      k_flux_correct_pair<<<gridn(M.nPer), 256, 0, ctx->stream>>>(M, D, D.pp);
+      ctx->kernel_launches++;
+    }
     if (pressure) {
       k_p_press_corr<<<gridn(M.nB), 256, 0, ctx->stream>>>(M, D);
       ctx->kernel_launches++;
@@ -1319,8 +1495,8 @@ extern "C" int fc_time_shift(fc_ctx* ctx) {
   return FC_OK;
 }
 
-// calcp_piso, calcp_piso.f90:86-489 (incompressible; no periodic or pressure
-// boundaries; nipgrad = 2, parameters.f90:62)
+// calcp_piso, calcp_piso.f90:86-489 (incompressible; periodic pairs, no
+// pressure boundaries; nipgrad = 2, parameters.f90:62)
 extern "C" int fc_calcp_piso(fc_ctx* ctx, double* resor4) {
   FC_RANGE();
   if (!ctx) return FC_ERR_BAD_INPUT;
@@ -1345,6 +1521,10 @@ extern "C" int fc_calcp_piso(fc_ctx* ctx, double* resor4) {
     k_piso_h<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D, S.h.p);
     k_piso_u<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, D);
     if (M.nI) k_piso_face<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D);
+    if (M.nPer) {
+      k_p_pair<<<gridn(M.nPer), 256, 0, ctx->stream>>>(M, D);
+      ctx->kernel_launches++;
+    }
     if (outlets) k_adjust_mass_flow<<<1, 32, 0, ctx->stream>>>(M, D, P.flomas);
     k_p_cell<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D, D.fscr);
     ctx->kernel_launches += 4 + outlets;
@@ -1377,6 +1557,10 @@ extern "C" int fc_calcp_piso(fc_ctx* ctx, double* resor4) {
     if ((st = gradp_and_sources(ctx, D, D.p, P.pscheme))) return st;
     k_vel_correct<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, D);
     ctx->kernel_launches++;
+    if (M.nPer) {  // the pairs' flux correction with the last p (calcp_piso.f90:437-456)
+      k_flux_correct_pair<<<gridn(M.nPer), 256, 0, ctx->stream>>>(M, D, D.p);
+      ctx->kernel_launches++;
+    }
     update_velocity_at_boundary(ctx, D);
   }
   FC_CUDA_TRY(ctx, cudaGetLastError());
@@ -1518,6 +1702,10 @@ extern "C" int fc_calculate_temperature(fc_ctx* ctx, int solve, double* resor7) 
   sp.pstart = S.tpatch.p + 2 * nb;
   FC_CUDA_TRY(ctx, cudaMemsetAsync(D.a, 0, (size_t)sys->nnz * sizeof(double), ctx->stream));
   if (M.nI) k_sc_face<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D, sp);
+  if (M.nPer) {
+    k_sc_pair<<<gridn(M.nPer), 256, 0, ctx->stream>>>(M, D, sp);
+    ctx->kernel_launches++;
+  }
   k_sc_cell<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D, sp);
   // main diagonal and under-relaxation (:354-365); the apx output of the
   // shared kernel goes to scratch

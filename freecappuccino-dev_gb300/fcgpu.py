@@ -81,6 +81,8 @@ def lib():
         "fc_mesh_write_openfoam": (i, [vp, cp]),
         "fc_mesh_info": (i, [vp, vp]),
         "fc_mesh_export": (i, [vp] + [vp] * 10),
+        "fc_mesh_set_twin": (i, [vp, i, i]),
+        "fc_mesh_twins": (i, [vp, vp]),
         "fc_mesh_free": (None, [vp]),
         "fc_init": (i, [i, C.POINTER(vp)]),
         "fc_finalize": (None, [vp]),
@@ -324,7 +326,15 @@ class Mesh:
                                        *[_ptr(v) for v in arrs[7:]], C.byref(h))
         if st != 0:
             raise FcError(st, "fc_mesh_from_arrays")
-        return cls(h)
+        m = cls(h)
+        twin = a.get("startFaceTwin")
+        if twin is not None:
+            for b, t in enumerate(np.asarray(twin)):
+                if a["bctype"][b] == BC["periodic"]:
+                    st = lib().fc_mesh_set_twin(m.h, b, int(t))
+                    if st != 0:
+                        raise FcError(st, "fc_mesh_set_twin")
+        return m
 
     @classmethod
     def read_native(cls, d):
@@ -362,6 +372,8 @@ class Mesh:
         lib().fc_mesh_export(self.h, *[_ptr(out[k]) for k in ("x", "y", "z", "nnodes", "nodes", "owner",
                                                               "neighbour", "bctype", "nfaces", "startFace")])
         out["neighbour"] = out["neighbour"][:nI]
+        out["startFaceTwin"] = np.zeros(nB, np.int32)
+        lib().fc_mesh_twins(self.h, _ptr(out["startFaceTwin"]))
         out.update(numNodes=nN, numCells=self.numCells, numInnerFaces=nI, numBoundaryFaces=self.numBoundaryFaces)
         return out
 
@@ -518,16 +530,21 @@ class Context:
         return out
 
     def csr_pattern(self):
+        """(ia, ja, diag, ijk, jik), 1-based; the slot maps hold the inner
+        faces, then the periodic pairs."""
         m = self.mesh
-        nnz = 2 * m.numInnerFaces + m.numCells
+        n, nnz = C.c_int(0), C.c_int(0)
+        self._check(self.L.fc_get_csr_pattern(self.h, C.byref(n), C.byref(nnz), None, None, None, None, None),
+                    "fc_get_csr_pattern")
+        nl = (nnz.value - n.value) // 2  # numInnerFaces + numPeriodic
         ia = np.zeros(m.numCells + 1, np.int32)
-        ja = np.zeros(nnz, np.int32)
+        ja = np.zeros(nnz.value, np.int32)
         dg = np.zeros(m.numCells, np.int32)
-        ijk = np.zeros(max(1, m.numInnerFaces), np.int32)
-        jik = np.zeros(max(1, m.numInnerFaces), np.int32)
+        ijk = np.zeros(max(1, nl), np.int32)
+        jik = np.zeros(max(1, nl), np.int32)
         self._check(self.L.fc_get_csr_pattern(self.h, None, None, _ptr(ia), _ptr(ja), _ptr(dg), _ptr(ijk), _ptr(jik)),
                     "fc_get_csr_pattern")
-        return ia, ja, dg, ijk[:m.numInnerFaces], jik[:m.numInnerFaces]
+        return ia, ja, dg, ijk[:nl], jik[:nl]
 
     def field_len(self, name):
         m = self.mesh

@@ -68,7 +68,33 @@ int bc_type_of(const std::string& s) {
 }
 
 
-int fc_mesh::validate(std::string* why) const {
+// one line of the reference's boundary file: name type nFaces startFace, and
+// for a periodic patch the startFace of its twin (geometry.f90:234-258);
+// false on an unknown type, true (nothing added) on a line that is not a patch
+bool parse_boundary_line(const std::string& line, fc_mesh* m) {
+  std::istringstream ls(line);
+  std::string name, type;
+  int nf, sf;
+  if (!(ls >> name >> type >> nf >> sf)) return true;
+  const int t = bc_type_of(type);
+  if (!t) return false;
+  int tw = -1;
+  if (t == FC_BC_PERIODIC && !(ls >> tw)) return false;
+  m->bcname.push_back(name); m->bctype.push_back(t); m->nfaces.push_back(nf); m->startFace.push_back(sf);
+  m->startFaceTwin.push_back(tw);
+  return true;
+}
+
+void write_boundary_lines(FILE* f, const fc_mesh& m) {
+  std::fprintf(f, "#bcname bctype nFaces startFace\n");
+  for (size_t b = 0; b < m.bctype.size(); ++b) {
+    std::fprintf(f, "%s %s %d %d", m.bcname[b].c_str(), bc_name_of(m.bctype[b]), m.nfaces[b], m.startFace[b]);
+    if (m.bctype[b] == FC_BC_PERIODIC) std::fprintf(f, " %d", m.twin_of(b));
+    std::fprintf(f, "\n");
+  }
+}
+
+int fc_mesh::validate(std::string* why, bool complete) const {
   auto fail = [&](const char* m) { if (why) *why = m; return FC_ERR_BAD_INPUT; };
   if (numNodes <= 0 || numCells <= 0 || numInnerFaces < 0 || numBoundaryFaces < 0) return fail("non-positive mesh sizes");
   if (numFaces != numInnerFaces + numBoundaryFaces) return fail("numFaces != numInnerFaces + numBoundaryFaces");
@@ -90,11 +116,33 @@ int fc_mesh::validate(std::string* why) const {
   for (size_t b = 0; b < bctype.size(); ++b) {
     if (startFace[b] != expect) return fail("boundary patches must be contiguous and follow the inner faces");
     if (nfaces[b] < 0) return fail("negative patch size");
-    if (bctype[b] == FC_BC_PERIODIC) return fail("periodic patches are not supported on this path");
     if (bctype[b] < FC_BC_WALL || bctype[b] > FC_BC_PERIODIC) return fail("unknown boundary type");
     expect += nfaces[b];
   }
   if (expect != numFaces) return fail("boundary patches do not cover all boundary faces");
+  // periodic pairs: the twin is another patch of the same size typed 'empty',
+  // twin of one periodic patch only; at most three pairs (startFaceTwin(3),
+  // geometry.f90:82); the pair loops index Df and facint by the face's
+  // position within its patch, so a patch has at most numInnerFaces faces
+  int nper = 0;
+  std::vector<int> used(bctype.size(), 0);
+  for (size_t b = 0; b < bctype.size(); ++b) {
+    if (bctype[b] != FC_BC_PERIODIC) continue;
+    ++nper;
+    const int tw = twin_of(b);
+    if (tw < 0) {
+      if (complete) return fail("a periodic patch names no twin (startFaceTwin)");
+      continue;
+    }
+    size_t t = 0;
+    while (t < bctype.size() && !(startFace[t] == tw && t != b)) ++t;
+    if (t == bctype.size()) return fail("the startFaceTwin of a periodic patch is the start of no other patch");
+    if (nfaces[t] != nfaces[b]) return fail("a periodic patch and its twin differ in size");
+    if (bctype[t] != FC_BC_EMPTY) return fail("the twin of a periodic patch must be typed 'empty'");
+    if (used[t]++) return fail("a patch is the twin of two periodic patches");
+    if (nfaces[b] > numInnerFaces) return fail("a periodic patch has more faces than the mesh has inner faces");
+  }
+  if (nper > 3) return fail("more than three periodic pairs");
   return FC_OK;
 }
 
@@ -299,12 +347,16 @@ extern "C" int fc_mesh_box(int nx, int ny, int nz, double lx, double ly, double 
       }
   if (tets) box_tet(*m, nx, ny, nz); else box_hex(*m, nx, ny, nz);
   m->bctype.resize(6); m->bcname.resize(6);
+  m->startFaceTwin.assign(6, -1);
   for (int s = 0; s < 6; ++s) {
     m->bctype[s] = side_bctype ? side_bctype[s] : FC_BC_WALL;
     m->bcname[s] = kSideName[s];
   }
+  // a periodic side pairs with the opposite side, which must be 'empty'
+  for (int s = 0; s < 6; ++s)
+    if (m->bctype[s] == FC_BC_PERIODIC) m->startFaceTwin[s] = m->startFace[s ^ 1];
   std::string why;
-  if (m->validate(&why) != FC_OK) { delete m; return FC_ERR_BAD_INPUT; }
+  if (m->validate(&why, true) != FC_OK) { delete m; return FC_ERR_BAD_INPUT; }
   *out = m;
   return FC_OK;
 }
@@ -328,6 +380,7 @@ extern "C" int fc_mesh_from_arrays(int numNodes, int numCells, int numInnerFaces
   for (int b = 0; b < numBoundaries; ++b) {
     m->bctype.push_back(bctype[b]); m->nfaces.push_back(nfaces[b]); m->startFace.push_back(startFace[b]);
     m->bcname.push_back(std::string("patch") + std::to_string(b + 1));
+    m->startFaceTwin.push_back(-1);
   }
   std::string why;
   if (m->validate(&why) != FC_OK) { delete m; return FC_ERR_BAD_INPUT; }
@@ -361,9 +414,7 @@ extern "C" int fc_mesh_write_native(const fc_mesh* m, const char* dir) {
   std::fclose(f);
   f = open("boundary");
   if (!f) return FC_ERR_BAD_INPUT;
-  std::fprintf(f, "#bcname bctype nFaces startFace\n");
-  for (size_t b = 0; b < m->bctype.size(); ++b)
-    std::fprintf(f, "%s %s %d %d\n", m->bcname[b].c_str(), bc_name_of(m->bctype[b]), m->nfaces[b], m->startFace[b]);
+  write_boundary_lines(f, *m);
   std::fclose(f);
   f = open("size");
   if (!f) return FC_ERR_BAD_INPUT;
@@ -384,13 +435,7 @@ extern "C" int fc_mesh_read_native(const char* dir, fc_mesh** out) {
   std::string line;
   while (fb && std::getline(fb, line)) {
     if (line.empty() || line[0] == '#') continue;
-    std::istringstream ls(line);
-    std::string name, type;
-    int nf, sf;
-    if (!(ls >> name >> type >> nf >> sf)) continue;
-    int t = bc_type_of(type);
-    if (!t) { delete m; return FC_ERR_BAD_INPUT; }
-    m->bcname.push_back(name); m->bctype.push_back(t); m->nfaces.push_back(nf); m->startFace.push_back(sf);
+    if (!parse_boundary_line(line, m)) { delete m; return FC_ERR_BAD_INPUT; }
   }
   std::ifstream fp(d + "/points");
   m->x.resize(m->numNodes); m->y.resize(m->numNodes); m->z.resize(m->numNodes);
@@ -437,6 +482,25 @@ extern "C" int fc_mesh_export(const fc_mesh* m, double* x, double* y, double* z,
   if (bctype && nb) std::memcpy(bctype, m->bctype.data(), sizeof(int) * nb);
   if (nfaces && nb) std::memcpy(nfaces, m->nfaces.data(), sizeof(int) * nb);
   if (startFace && nb) std::memcpy(startFace, m->startFace.data(), sizeof(int) * nb);
+  return FC_OK;
+}
+
+extern "C" int fc_mesh_set_twin(fc_mesh* m, int patch, int startFaceTwin) {
+  if (!m || patch < 0 || patch >= (int)m->bctype.size() || m->bctype[patch] != FC_BC_PERIODIC) return FC_ERR_BAD_INPUT;
+  m->startFaceTwin.resize(m->bctype.size(), -1);
+  const int old = m->startFaceTwin[patch];
+  m->startFaceTwin[patch] = startFaceTwin;
+  std::string why;
+  if (m->validate(&why) != FC_OK) {
+    m->startFaceTwin[patch] = old;
+    return FC_ERR_BAD_INPUT;
+  }
+  return FC_OK;
+}
+
+extern "C" int fc_mesh_twins(const fc_mesh* m, int* startFaceTwin) {
+  if (!m || !startFaceTwin) return FC_ERR_BAD_INPUT;
+  for (size_t b = 0; b < m->bctype.size(); ++b) startFaceTwin[b] = m->twin_of(b);
   return FC_OK;
 }
 

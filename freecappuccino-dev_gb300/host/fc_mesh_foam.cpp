@@ -106,10 +106,12 @@ bool note_value(const std::string& s, const char* key, long long* v) {
 
 // OpenFOAM's dictionary-form boundary file: N ( name { type T; nFaces n;
 // startFace s; ... } ... ).  A patch's role: its type where the type names
-// one (wall, symmetryPlane / symmetry, empty, cyclic), else its name when
-// that is one of the reference's types (inlet, outlet, pressure, ...).
+// one (wall, symmetryPlane / symmetry, empty, cyclic with its
+// neighbourPatch), else its name when that is one of the reference's types
+// (inlet, outlet, pressure, ...).
 bool boundary_dict(const std::string& text, fc_mesh* m) {
   std::string s = strip_comments(text);
+  std::vector<std::string> nbr;  // neighbourPatch per patch
   const size_t ff = s.find("FoamFile");
   size_t pos = 0;
   if (ff != std::string::npos) {
@@ -144,7 +146,7 @@ bool boundary_dict(const std::string& text, fc_mesh* m) {
     if (name.empty() || i >= s.size() || s[i] != '{') return false;
     const size_t close = s.find('}', i);
     if (close == std::string::npos) return false;
-    std::string type;
+    std::string type, nbp;
     long long nf = -1, sf = -1;
     std::istringstream body(s.substr(i + 1, close - i - 1));
     std::string entry;
@@ -155,6 +157,7 @@ bool boundary_dict(const std::string& text, fc_mesh* m) {
       if (key == "type") type = val;
       else if (key == "nFaces") nf = std::atoll(val.c_str());
       else if (key == "startFace") sf = std::atoll(val.c_str());
+      else if (key == "neighbourPatch") nbp = val;
     }
     i = close + 1;
     if (nf < 0 || sf < 0) return false;
@@ -169,6 +172,20 @@ bool boundary_dict(const std::string& text, fc_mesh* m) {
     m->bctype.push_back(t);
     m->nfaces.push_back((int)nf);
     m->startFace.push_back((int)sf);
+    m->startFaceTwin.push_back(-1);
+    nbr.push_back(nbp);
+  }
+  // a cyclic pair in the reference's form: the patch listed first becomes
+  // the 'empty' twin, the second the 'periodic' patch naming it
+  for (size_t b = 0; b < m->bctype.size(); ++b) {
+    if (m->bctype[b] != FC_BC_PERIODIC) continue;
+    size_t t = 0;
+    while (t < m->bcname.size() && m->bcname[t] != nbr[b]) ++t;
+    if (t == m->bcname.size() || t == b || m->bctype[t] != FC_BC_PERIODIC || nbr[t] != m->bcname[b]) return false;
+    if (t < b) {
+      m->bctype[t] = FC_BC_EMPTY;
+      m->startFaceTwin[b] = m->startFace[t];
+    }
   }
   return true;
 }
@@ -249,18 +266,8 @@ extern "C" int fc_mesh_read_openfoam(const char* dir, fc_mesh** out) {
   std::istringstream bf(bnd_t);
   std::string line;
   std::getline(bf, line);
-  while (std::getline(bf, line)) {
-    std::istringstream ls(line);
-    std::string name, type;
-    int nfc, sf;
-    if (!(ls >> name >> type >> nfc >> sf)) continue;
-    const int t = bc_type_of(type);
-    if (!t) return fail();
-    m->bcname.push_back(name);
-    m->bctype.push_back(t);
-    m->nfaces.push_back(nfc);
-    m->startFace.push_back(sf);
-  }
+  while (std::getline(bf, line))
+    if (!parse_boundary_line(line, m)) return fail();
   std::string why;
   if (m->validate(&why) != FC_OK) return fail();
   *out = m;
@@ -308,9 +315,7 @@ extern "C" int fc_mesh_write_openfoam(const fc_mesh* m, const char* dir) {
   std::fclose(f);
   f = std::fopen((d + "/boundary").c_str(), "w");
   if (!f) return FC_ERR_BAD_INPUT;
-  std::fprintf(f, "#bcname bctype nFaces startFace\n");
-  for (size_t b = 0; b < m->bctype.size(); ++b)
-    std::fprintf(f, "%s %s %d %d\n", m->bcname[b].c_str(), bc_name_of(m->bctype[b]), m->nfaces[b], m->startFace[b]);
+  write_boundary_lines(f, *m);
   std::fclose(f);
   return FC_OK;
 }

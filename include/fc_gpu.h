@@ -46,7 +46,7 @@ extern "C" {
 #define FC_BC_SYMMETRY   4   /* 'symmetry' */
 #define FC_BC_PRESSURE   5   /* 'pressure' */
 #define FC_BC_EMPTY      6   /* 'empty'    */
-#define FC_BC_PERIODIC   7   /* 'periodic' (not supported on this path yet) */
+#define FC_BC_PERIODIC   7   /* 'periodic': paired with an 'empty' twin patch (startFaceTwin) */
 
 /* ======================================================================== */
 /* Host-side mesh (native polyMesh format of read_mesh_native,              */
@@ -59,7 +59,8 @@ typedef struct fc_mesh fc_mesh;
 /* Structured nx*ny*nz hex box on [0,lx]x[0,ly]x[0,lz].  Interior vertices are
  * moved by U(-perturb*h, +perturb*h) per axis (seeded).  tets!=0 splits every
  * hex into 6 tetrahedra.  side_bctype[6] gives the FC_BC_* type of the
- * patches xmin,xmax,ymin,ymax,zmin,zmax (NULL: all walls).  Inner faces are
+ * patches xmin,xmax,ymin,ymax,zmin,zmax (NULL: all walls); a FC_BC_PERIODIC
+ * side is paired with the opposite side, which must be FC_BC_EMPTY.  Inner faces are
  * ordered by (owner,neighbour), owner<neighbour, area vector owner->neighbour;
  * boundary faces are grouped by patch in the order above. */
 int fc_mesh_box(int nx, int ny, int nz, double lx, double ly, double lz,
@@ -75,6 +76,14 @@ int fc_mesh_from_arrays(int numNodes, int numCells, int numInnerFaces, int numBo
                         const int* owner, const int* neighbour,
                         int numBoundaries, const int* bctype, const int* nfaces,
                         const int* startFace, fc_mesh** out);
+
+/* Periodic pairs (geometry.f90:250-258): a FC_BC_PERIODIC patch names its
+ * twin by the twin's 0-based startFace (the fifth field of the patch's line
+ * in the boundary file).  The twin is another patch of the same size typed
+ * FC_BC_EMPTY; at most three pairs.  fc_mesh_set_twin sets it for a mesh
+ * built from arrays; fc_mesh_twins gives it per patch (-1: not periodic). */
+int fc_mesh_set_twin(fc_mesh* m, int patch, int startFaceTwin);
+int fc_mesh_twins(const fc_mesh* m, int* startFaceTwin);
 
 /* Read / write the native files points, faces, owner, neighbour, boundary,
  * size of a polyMesh directory (read_mesh_native, geometry.f90:165-410). */
@@ -288,15 +297,20 @@ int fc_dpcg_noalloc(void* stream, int n, int nnz, const int* ia, const int* ja, 
 /* ======================================================================== */
 /* Upload the mesh and build everything derived from it once: cell -> face
  * lists, the geometry of read_mesh_native (geometry.f90:416-665, computed on
- * the device), the CSR pattern and face -> CSR slot maps of create_CSR_matrix
- * (sparse_matrix.f90:86-296), and zeroed fields.  Replaces read_mesh +
- * create_CSR_matrix + create_fields (main.f90:105-107). */
+ * the device), the periodic face mapping (face_mapping, geometry.f90:
+ * 1848-1997: the twin faces' owners, centres and area vectors reordered to
+ * their pairs), the CSR pattern and face -> CSR slot maps of
+ * create_CSR_matrix (sparse_matrix.f90:86-296, periodic pairs included), and
+ * zeroed fields.  Replaces read_mesh + create_CSR_matrix + create_fields
+ * (main.f90:105-107).  A mesh whose periodic mapping is not one to one, or
+ * that couples two cells twice, is rejected. */
 int fc_set_mesh(fc_ctx* ctx, const fc_mesh* m);
 /* Geometry arrays by the reference's names: "arx","ary","arz","xf","yf","zf"
  * (numFaces), "xc","yc","zc","vol" (numCells), "facint","Df" (numInnerFaces). */
 int fc_get_geometry(fc_ctx* ctx, const char* name, double* out);
-/* CSR pattern (ia, ja, diag) and icell_jcell_csr_index / jcell_icell_csr_index,
- * 1-based; any output may be NULL. */
+/* CSR pattern (ia, ja, diag) and icell_jcell_csr_index / jcell_icell_csr_index
+ * (numInnerFaces + numPeriodic entries: inner faces, then the periodic pairs
+ * in patch and face order), 1-based; any output may be NULL. */
 int fc_get_csr_pattern(fc_ctx* ctx, int* n, int* nnz, int* ia, int* ja, int* diag, int* ijk, int* jik);
 
 /* Fields by the reference's variable names: "u","v","w","p","pp","vis","den","t"
@@ -404,8 +418,9 @@ int fc_init_flmass(fc_ctx* ctx);
 int fc_update_velocity_at_boundary(fc_ctx* ctx);
 /* gradp_and_sources(p) (nablap.f90:19-208) on field "p" or "pp": su,sv,sw and dPdxi */
 int fc_gradp_and_sources(fc_ctx* ctx, const char* field);
-/* calcuvw (velocity.f90:50-750): momentum assembly and the three solves;
- * resor[3] receives the normalised initial residuals of U, V, W. */
+/* calcuvw (velocity.f90:50-750): momentum assembly (periodic pairs by
+ * facefluxuvw_periodic, :1038-1179) and the three solves; resor[3] receives
+ * the normalised initial residuals of U, V, W. */
 int fc_calcuvw(fc_ctx* ctx, double* resor);
 /* on != 0: calcuvw solves U, V and W together (when lSolverU is bicgstab) in
  * one batched launch (fc_batch_*) on three copies of the mesh pattern, each
@@ -430,7 +445,8 @@ int fc_simple_iteration(fc_ctx* ctx, double* resor);
  *   corrector (fc_simple_params.npcor), urfP.  PISO with BDF2/BDF3 is
  *   rejected: the reference extrapolates the mass fluxes and pressure from
  *   old levels (velocity.f90:146-162) that its time_shift never updates.
- *   Incompressible, without periodic or pressure boundaries, as SIMPLE.
+ *   Incompressible, with periodic pairs as SIMPLE, without pressure
+ *   boundaries.
  * fc_time_shift: time_shift.f90 for the velocity levels.
  * fc_calcp_piso: calcp_piso; *resor4 as continuityErrors sets resor(4).
  * fc_piso_iteration: calcuvw + calcp_piso, resor[4], and the divergence
@@ -493,7 +509,8 @@ typedef struct {
 int fc_temperature_set_params(fc_ctx* ctx, const fc_temperature_params* prm, const double* bc_dfraction);
 /* calculate_temperature (temperature.f90:35-385) for the steady case without
  * turbulent heat fluxes: grad(T), the facefluxsc assembly of the matrix and
- * sources (scalar_fluxes.f90:32-141, :256-337), the boundary conditions,
+ * sources (scalar_fluxes.f90:32-141, :147-251 for periodic pairs, :256-337),
+ * the boundary conditions,
  * under-relaxation, csrsolve(lSolverT, T, su, resor(7), ...), updateBoundary(T)
  * and the clip to small when min(T) < 0.  With solve == 0 the call stops after
  * the under-relaxation and leaves the system in the mesh's matrix and "su".

@@ -374,6 +374,35 @@ def cavity_fields(m, nT, nC):
     return a, u, nwal
 
 
+def simple_iterations(n=128, iters=4, perturb=PERTURB, dev=0):
+    """`iters` FP64 SIMPLE iterations of the n^3 lid-driven cavity of the
+    SIMPLE leg (perturbed hexes, seed MESH_SEED): the command the kernel
+    launch lists and ncu captures of one SIMPLE iteration run, e.g.
+    python -c "import bench; bench.simple_iterations(128, 4)".  Returns the
+    last iteration's resor."""
+    fc = load_fc()
+    m = fc.Mesh.box(n, n, n, 1.0, 1.0, 1.0, perturb=perturb, seed=MESH_SEED)
+    nC, nT = m.numCells, m.numTotal
+    _, u, nwal = cavity_fields(m, nT, nC)
+    ctx = fc.Context(dev)
+    ctx.set_mesh(m)
+    zero = np.zeros(nT)
+    for k, v in dict(u=u, v=zero, w=zero, p=zero, pp=zero, den=np.ones(nT), vis=np.full(nT, 0.01)).items():
+        ctx.field_set(k, v)
+    ctx.field_set("visw", np.full(max(nwal, 1), 0.01))
+    for k in ("flmass", "a", "dUdxi", "dVdxi", "dWdxi", "dPdxi"):
+        ctx.field_fill(k, 0.0)
+    ctx.simple_params(fc.SimpleParams.cavity(viscos=0.01))
+    ctx.init_flmass()
+    r = None
+    for _ in range(iters):
+        r = ctx.simple_iteration()
+    ctx.sync()
+    print("simple_iterations", n, iters, "launches", ctx.kernel_launches(), "resor", list(r), flush=True)
+    ctx.close()
+    return r
+
+
 def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None, tets=False, viscos=0.01, scheme=1, grad=0,
                  iters=None, cpu_iters=None, urf=(0.8, 0.3), momentum_batch=False):
     """SIMPLE iterations per second on the n^3 lid-driven cavity (unit cube,
@@ -643,6 +672,16 @@ def adjoint_block(fc, args, dev):
     adj_ms = ctx.elapsed_ms()
     if ainfo.status != 0:
         raise RuntimeError(f"adjoint solve status {ainfo.status}")
+    # the reverse face loop against the oracle's cd_gradient on the same phi
+    # and lambda, at this size (one face loop on the host)
+    oracle_diff = None
+    if not args.no_cpu:
+        import oracle_lib
+        oc = oracle_lib.Case(a)
+        oc.set("flmass", fm)
+        go = oc.cd_gradient(phi, lam)
+        oracle_diff = float(np.abs(grad - go).max() / max(np.abs(go).max(), 1e-300))
+        del oc
     rng = np.random.default_rng(47)
     h, rel = 1e-2, []
     for _ in range(args.adjoint_fd_dirs):
@@ -661,7 +700,8 @@ def adjoint_block(fc, args, dev):
             "adjoint_ms": adj_ms, "adjoint_solve_ms": ainfo.ms, "adjoint_iterations": ainfo.itr_used,
             "solver": f"BiCGStab(DILU) FP64 to {tol:g} relative L1 (forward and transposed)",
             "fd_directions": len(rel), "fd_step": "gamma (1 +- 1e-2 v), full re-solves",
-            "fd_max_rel_err": float(max(rel)), "fd_median_rel_err": float(np.median(rel))}
+            "fd_max_rel_err": float(max(rel)), "fd_median_rel_err": float(np.median(rel)),
+            "oracle_gradient_max_rel_diff": oracle_diff}
 
 
 def max_over_ranks(dist, x):

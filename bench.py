@@ -816,6 +816,11 @@ def run_gpu(args, rank, world, dist):
                              % ctx.mixed_colours(0))
     mixed_nat = mixed_run(fc.FC_PREC_MIXED, MIXED_NATURAL_INNER_TOL)
     mixed_nat["inner_solver"] = "FP32 ICCG, natural-order DIC (the FP64 path's sweeps)"
+    # precision's share of the mixed speed-up: the same multicolour inner
+    # solve, refinement and stopping test in FP64
+    col64 = mixed_run(fc.FC_PREC_COLOURED_FP64, MIXED_INNER_TOL)
+    col64["inner_solver"] = "FP64 ICCG, the same multicolour DIC in Eisenstat form (diagnostic)"
+    mixed["speedup_vs_coloured_fp64"] = col64["ms_per_step"] / mixed["ms_per_step"]
 
     spmv = spmv_leg(fc, ctx, nC, args.spmv_calls) if args.spmv_calls > 0 else None
     sweep = ctx.sweep_stats(0)
@@ -846,7 +851,8 @@ def run_gpu(args, rank, world, dist):
             "solve": {"iterations_per_solve": iters, "parallelism": "replicas" if world > 1 else "single GPU",
                       "sweep_tiles": int(sweep["tiles"]), "sweep_levels": int(sweep["levels"]),
                       "sweep_est_us": round(sweep["est_sweep_us"], 1)},
-            "mixed_natural_order": mixed_nat}
+            "mixed_natural_order": mixed_nat,
+            "coloured_fp64": col64}
     if spmv:
         line["spmv"] = spmv
     ctx.close()

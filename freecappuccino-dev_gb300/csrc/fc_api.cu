@@ -88,7 +88,8 @@ extern "C" int fc_set_verbosity(fc_ctx* ctx, int level) {
 }
 
 extern "C" int fc_set_precision(fc_ctx* ctx, int mode, double inner_tol, int inner_itmax) {
-  if (!ctx || (mode != FC_PREC_FP64 && mode != FC_PREC_MIXED && mode != FC_PREC_MIXED_COLOURED))
+  if (!ctx || (mode != FC_PREC_FP64 && mode != FC_PREC_MIXED && mode != FC_PREC_MIXED_COLOURED &&
+               mode != FC_PREC_COLOURED_FP64))
     return FC_ERR_BAD_INPUT;
   ctx->precision = mode;
   ctx->inner_tol = inner_tol;

@@ -246,11 +246,11 @@ struct SolveResult {
 
 // solve on a system; a (nnz values, NULL = s->a), x and b are device
 // vectors (x in/out).  solver: gauss-seidel|dpcg|iccg|bicgstab|pmgmres
-// FP32 inner solve of FC_PREC_MIXED_COLOURED on the multicolour layout of s
-// (fc_mc.cu): A e = r64 from e = 0, x64 += e; *itr_out iterations, *status_out
-// a device status (0 or FC_ERR_*)
+// inner solve of FC_PREC_MIXED_COLOURED (FP32) or FC_PREC_COLOURED_FP64
+// (fp64) on the multicolour layout of s (fc_mc.cu): A e = r64 from e = 0,
+// x64 += e; *itr_out iterations, *status_out a device status (0 or FC_ERR_*)
 int mc_inner_solve(fc_ctx* ctx, CsrSystem* s, const double* a, const double* r64, double* x64, double tol, int itmax,
-                   bool setup, int* itr_out, int* status_out);
+                   bool setup, bool fp64, int* itr_out, int* status_out);
 int mc_colours(fc_ctx* ctx, CsrSystem* s, int* ncol);
 int sys_solve(fc_ctx* ctx, CsrSystem* s, const char* solver, const double* a, double* x, const double* b,
               int itr_max, double tol_abs, double tol_rel, SolveResult* res);

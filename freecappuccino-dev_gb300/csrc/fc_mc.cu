@@ -1,9 +1,12 @@
-// FP32 inner solve of the mixed-precision path on a multicolour ordering.
+// Inner solve of the mixed-precision path on a multicolour ordering: FP32
+// (FC_PREC_MIXED_COLOURED) and, as a diagnostic of what the precision
+// contributes, the same solve in FP64 (FC_PREC_COLOURED_FP64); the kernels
+// are templates on the value type.
 //
 // The FP64 path keeps the reference's natural-order DIC, whose triangular
 // sweeps are a long chain of dependent levels: on this GPU the sweep is bound
 // by the latency of each level, not by bytes, so running it in FP32 saves
-// little.  The inner solve of FC_PREC_MIXED_COLOURED instead colours the rows
+// little.  The coloured inner solve instead colours the rows
 // (host/fc_colour.cpp), factors A by DILU in the coloured order (DIC for a
 // symmetric matrix) and applies the factors one colour at a time: every pass
 // is a data-parallel ELLPACK sweep, bound by HBM bandwidth.  The
@@ -30,8 +33,8 @@
 // (D+U)^-1 y.  Every kernel runs at full occupancy with one thread per row;
 // the scalars of the iteration are finalised in device memory by the last
 // block of each reduction, in a fixed order, and the block that decides to
-// stop clears the loop's condition.  Dot products are summed in FP32 within
-// a warp and in FP64 across warps and blocks.
+// stop clears the loop's condition.  Dot products and norms are accumulated
+// in FP64 in both value types.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -57,34 +60,52 @@ enum { MC_CR = 0, MC_CEL = MC_T, MC_CEU = 2 * MC_T, MC_CWL = 3 * MC_T, MC_CWU = 
 // scalars of one inner solve, in device memory
 struct McScal {
   double res0, resl, rz, rzacc, pq, tol;
-  float alpha, beta;
+  double alpha, beta;
   int it, itmax, done, status;
   double rz0;
 };
 
+// the buffers of one value type: FP32 (FC_PREC_MIXED_COLOURED) or FP64
+// (FC_PREC_COLOURED_FP64) matrix values, DILU diagonal, its reciprocal and
+// a_ii - 2 d, the Krylov vectors, and the inner solve's graph
+template <class T>
+struct McBuf {
+  DVec<T> mval, adiag, invd, dvec, kdiag, x, r, p, q, y, t, w;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int wave = 1;  // resident blocks of the widest loop-body kernel on the whole GPU
+  bool ready = false;
+  ~McBuf() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+  }
+};
+
 struct DevColoured {
-  int n = 0, nP = 0, ncol = 0, maxblocks = 1, wave = 1;
+  int n = 0, nP = 0, ncol = 0, maxblocks = 1;
+  size_t nent = 1;  // ELLPACK entries of the layout
   std::vector<int> crow;
   DVec<int> tab, perm, col, src, tsrc, dslot;
-  DVec<float> mval, adiag, invd, dvec, kdiag, x, r, p, q, y, t, w;
   DVec<double> dset, part;
   DVec<unsigned> cnt;
   DVec<McScal> sc;
   McScal* h_sc = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
+  McBuf<float> f32;
+  McBuf<double> f64;
   ~DevColoured() {
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
     if (h_sc) cudaFreeHost(h_sc);
   }
 };
+
+static McBuf<float>& mc_buf(DevColoured& m, float) { return m.f32; }
+static McBuf<double>& mc_buf(DevColoured& m, double) { return m.f64; }
 
 void mc_release(DevColoured* m) { delete m; }
 
 namespace {
 
-struct McDev {
+template <class T>
+struct McDevT {
   int nP, ncol, c0end;
   const int* __restrict__ tab;
   const int* __restrict__ col;
@@ -92,9 +113,9 @@ struct McDev {
   const int* __restrict__ tsrc;
   const int* __restrict__ dslot;
   const double* __restrict__ a;
-  float *mval, *adiag, *invd, *dvec, *kdiag;
+  T *mval, *adiag, *invd, *dvec, *kdiag;
   double* dset;
-  float *x, *r, *p, *q, *y, *t, *w;
+  T *x, *r, *p, *q, *y, *t, *w;
   McScal* sc;
   double* part;     // 2 * blocks of the widest launch
   unsigned* cnt;    // arrival counter of the last-block reductions
@@ -107,29 +128,43 @@ __device__ __forceinline__ double mcg_warp_sum(double v) {
   return v;
 }
 
-__device__ __forceinline__ float mcg_warp_sumf(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
+__device__ __forceinline__ float mfma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double mfma(double a, double b, double c) { return fma(a, b, c); }
+
+// four consecutive values of a vector (16-byte aligned: the padded row count
+// is a multiple of 32)
+__device__ __forceinline__ void ld4(const float* p, int i4, float (&v)[4]) {
+  const float4 t = __ldcg((const float4*)p + i4);
+  v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+}
+__device__ __forceinline__ void ld4(const double* p, int i4, double (&v)[4]) {
+  const double2 a = __ldcg((const double2*)p + 2 * i4), b = __ldcg((const double2*)p + 2 * i4 + 1);
+  v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+__device__ __forceinline__ void st4(float* p, int i4, const float (&v)[4]) {
+  ((float4*)p)[i4] = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void st4(double* p, int i4, const double (&v)[4]) {
+  ((double2*)p)[2 * i4] = make_double2(v[0], v[1]);
+  ((double2*)p)[2 * i4 + 1] = make_double2(v[2], v[3]);
 }
 
-// Sum NV values over the grid of the running kernel.  A thread's terms and
-// the warp tree are summed in FP32 (FP64 arithmetic is scarce on this part:
-// per-row FP64 accumulation cost more than the bandwidth of the pass); the
-// 16 warp sums of a block and the block partials are summed in FP64.  Each
-// block writes its fixed-order sum; the last block to arrive sums the
-// partials in block order, so the totals do not depend on arrival order.
-// Returns true in every thread of that last block, with the totals in tot.
-template <int NV>
-__device__ __forceinline__ bool mcg_reduce(const McDev& D, float (&v)[NV], double (&tot)[NV]) {
+// Sum NV values over the grid of the running kernel, in FP64 throughout: a
+// thread's terms (products of FP32 values are exact in FP64), the warp
+// tree, the 16 warp sums of a block and the block partials.  Each block
+// writes its fixed-order sum; the last block to arrive sums the partials in
+// block order, so the totals do not depend on arrival order.  Returns true in
+// every thread of that last block, with the totals in tot.
+template <int NV, class T>
+__device__ __forceinline__ bool mcg_reduce(const McDevT<T>& D, double (&v)[NV], double (&tot)[NV]) {
   __shared__ double sm[NV][MCG_BLOCK / 32];
   __shared__ double s_tot[NV];
   __shared__ int s_last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int j = 0; j < NV; ++j) {
-    const float w = mcg_warp_sumf(v[j]);
-    if (lane == 0) sm[j][wid] = (double)w;
+    const double w = mcg_warp_sum(v[j]);
+    if (lane == 0) sm[j][wid] = w;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -176,9 +211,10 @@ __device__ __forceinline__ bool mcg_reduce(const McDev& D, float (&v)[NV], doubl
 // one request per warp to the same L2 line, which serialises on one slice.
 struct McBcast {
   int done;
-  float alpha, beta;
+  double alpha, beta;
 };
-__device__ __forceinline__ McBcast mcg_scalars(const McDev& D) {
+template <class T>
+__device__ __forceinline__ McBcast mcg_scalars(const McDevT<T>& D) {
   __shared__ McBcast s;
   if (threadIdx.x == 0) {
     s.done = __ldcg(&D.sc->done);
@@ -190,7 +226,8 @@ __device__ __forceinline__ McBcast mcg_scalars(const McDev& D) {
 }
 
 // stop the loop: called by the one thread that decided it
-__device__ __forceinline__ void mcg_stop(const McDev& D, int status) {
+template <class T>
+__device__ __forceinline__ void mcg_stop(const McDevT<T>& D, int status) {
   if (status) D.sc->status = status;
   D.sc->done = 1;
   if (D.h) cudaGraphSetConditional(D.h, 0);  // 0 outside the graph (host-launched diagnostic mode)
@@ -201,10 +238,11 @@ __device__ __forceinline__ void mcg_stop(const McDev& D, int status) {
 // Blocks up to MC_UNROLL wide (every hex and tet row) issue all index and
 // value loads before the gathers, so that they are in flight together; w is
 // the same for the whole colour, so no load waits on a per-row count.
-__device__ __forceinline__ float ell_sum(const McDev& D, int e, int stride, int w, const float* v, float acc) {
+template <class T>
+__device__ __forceinline__ T ell_sum(const McDevT<T>& D, int e, int stride, int w, const T* v, T acc) {
   if (w <= MC_UNROLL) {
     int c[MC_UNROLL];
-    float m[MC_UNROLL];
+    T m[MC_UNROLL];
 #pragma unroll
     for (int k = 0; k < MC_UNROLL; ++k)
       if (k < w) {
@@ -213,34 +251,36 @@ __device__ __forceinline__ float ell_sum(const McDev& D, int e, int stride, int 
       }
 #pragma unroll
     for (int k = 0; k < MC_UNROLL; ++k)
-      if (k < w) acc = fmaf(m[k], __ldcg(v + c[k]), acc);
+      if (k < w) acc = mfma(m[k], __ldcg(v + c[k]), acc);
     return acc;
   }
-  for (int k = 0; k < w; ++k) acc = fmaf(__ldcg(D.mval + e + k * stride), __ldcg(v + __ldg(D.col + e + k * stride)), acc);
+  for (int k = 0; k < w; ++k) acc = mfma(__ldcg(D.mval + e + k * stride), __ldcg(v + __ldg(D.col + e + k * stride)), acc);
   return acc;
 }
 
-// r (coloured, FP32) <- r64 (original order); x, p <- 0; scalars reset
-__global__ void k_mc_gather(McDev D, const int* __restrict__ perm, const double* __restrict__ r64, double tol,
+// r (coloured, value type T) <- r64 (original order); x, p <- 0; scalars reset
+template <class T>
+__global__ void k_mc_gather(McDevT<T> D, const int* __restrict__ perm, const double* __restrict__ r64, double tol,
                             int itmax) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < D.nP; i += gridDim.x * blockDim.x) {
     const int o = perm[i];
-    D.r[i] = o >= 0 ? (float)r64[o] : 0.0f;
-    D.x[i] = 0.0f;
-    D.p[i] = 0.0f;
+    D.r[i] = o >= 0 ? (T)r64[o] : T(0);
+    D.x[i] = T(0);
+    D.p[i] = T(0);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     McScal s;
     s.res0 = s.resl = s.rz = s.rzacc = s.pq = s.rz0 = 0.0;
     s.tol = tol;
-    s.alpha = s.beta = 0.0f;
+    s.alpha = s.beta = 0.0;
     s.it = 0; s.itmax = itmax; s.done = 0; s.status = 0;
     *D.sc = s;
   }
 }
 
 // x64 (original order) += x (coloured)
-__global__ void k_mc_scatter_add(int nP, const int* __restrict__ perm, const float* __restrict__ x, double* x64) {
+template <class T>
+__global__ void k_mc_scatter_add(int nP, const int* __restrict__ perm, const T* __restrict__ x, double* x64) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nP; i += gridDim.x * blockDim.x) {
     const int o = perm[i];
     if (o >= 0) x64[o] += (double)x[i];
@@ -248,9 +288,10 @@ __global__ void k_mc_scatter_add(int nP, const int* __restrict__ perm, const flo
 }
 
 // values and the coloured DILU diagonal of colour c (colours in order):
-// d_i = a_ii - sum over lower entries of a_ij a_ji / d_j, in FP64; FP32 copies
-// of d, 1/(d + small) and a_ii - 2 d
-__global__ void __launch_bounds__(MCG_BLOCK) k_mcg_setup(McDev D, int c) {
+// d_i = a_ii - sum over lower entries of a_ij a_ji / d_j, in FP64; copies in
+// T of d, 1/(d + small) and a_ii - 2 d
+template <class T>
+__global__ void __launch_bounds__(MCG_BLOCK) k_mcg_setup(McDevT<T> D, int c) {
   const int r0 = __ldg(D.tab + MC_CR + c), r1 = __ldg(D.tab + MC_CR + c + 1), stride = r1 - r0;
   const int cel = __ldg(D.tab + MC_CEL + c), ceu = __ldg(D.tab + MC_CEU + c);
   const int cwl = __ldg(D.tab + MC_CWL + c), cwu = __ldg(D.tab + MC_CWU + c);
@@ -264,7 +305,7 @@ __global__ void __launch_bounds__(MCG_BLOCK) k_mcg_setup(McDev D, int c) {
     const int sl = __ldg(D.src + e);
     if (sl < 0) continue;
     const double v = __ldg(D.a + sl);
-    D.mval[e] = (float)v;
+    D.mval[e] = (T)v;
     const int ts = __ldg(D.tsrc + e);
     const double t = ts >= 0 ? __ldg(D.a + ts) : 0.0;
     d -= v * t / __ldcg(D.dset + __ldg(D.col + e));
@@ -272,69 +313,73 @@ __global__ void __launch_bounds__(MCG_BLOCK) k_mcg_setup(McDev D, int c) {
   for (int k = 0; k < cwu; ++k) {
     const int e = ceu + (i - r0) + k * stride;
     const int sl = __ldg(D.src + e);
-    if (sl >= 0) D.mval[e] = (float)__ldg(D.a + sl);
+    if (sl >= 0) D.mval[e] = (T)__ldg(D.a + sl);
   }
   D.dset[i] = d;
-  D.dvec[i] = (float)d;
-  D.invd[i] = (float)(1.0 / (d + FC_SMALL));
-  D.kdiag[i] = (float)(aii - 2.0 * d);
-  D.adiag[i] = ds >= 0 ? (float)aii : 0.0f;
+  D.dvec[i] = (T)d;
+  D.invd[i] = (T)(1.0 / (d + FC_SMALL));
+  D.kdiag[i] = (T)(aii - 2.0 * d);
+  D.adiag[i] = ds >= 0 ? (T)aii : T(0);
 }
 
 // colour c of (D+L) r~ = b, in place on r (lower colours already hold r~)
-__global__ void __launch_bounds__(MCG_BLOCK) k_e_fwdb(McDev D, int c) {
+template <class T>
+__global__ void __launch_bounds__(MCG_BLOCK) k_e_fwdb(McDevT<T> D, int c) {
   const int r0 = __ldg(D.tab + MC_CR + c), r1 = __ldg(D.tab + MC_CR + c + 1);
   const int cel = __ldg(D.tab + MC_CEL + c), cwl = __ldg(D.tab + MC_CWL + c);
   const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= r1) return;
-  D.r[i] = (__ldcg(D.r + i) - ell_sum(D, cel + (i - r0), r1 - r0, cwl, D.r, 0.0f)) * __ldcg(D.invd + i);
+  D.r[i] = (__ldcg(D.r + i) - ell_sum(D, cel + (i - r0), r1 - r0, cwl, D.r, T(0))) * __ldcg(D.invd + i);
 }
 
 // z = D r~, p = z, t = p / d on the last colour; r~.z starts the iteration
-__global__ void __launch_bounds__(MCG_BLOCK) k_e_start(McDev D) {
+template <class T>
+__global__ void __launch_bounds__(MCG_BLOCK) k_e_start(McDevT<T> D) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int clast = __ldg(D.tab + MC_CR + D.ncol - 1);
-  float v[1] = {0.0f};
+  double v[1] = {0.0};
   if (i < D.nP) {
-    const float ri = __ldcg(D.r + i), zi = __ldcg(D.dvec + i) * ri;
+    const T ri = __ldcg(D.r + i), zi = __ldcg(D.dvec + i) * ri;
     D.y[i] = zi;
     D.p[i] = zi;
     if (i >= clast) D.t[i] = zi * __ldcg(D.invd + i);
-    v[0] = ri * zi;
+    v[0] = (double)ri * (double)zi;
   }
   double tot[1];
   if (!mcg_reduce<1>(D, v, tot) || threadIdx.x != 0) return;
   McScal* S = D.sc;
   S->rz = S->rz0 = S->res0 = S->resl = tot[0];
-  S->beta = 0.0f;
+  S->beta = 0.0;
   if (!(tot[0] == tot[0]) || isinf(tot[0])) mcg_stop(D, FC_ERR_NAN);
   else if (tot[0] == 0.0 || S->itmax <= 0) mcg_stop(D, 0);
 }
 
 // backward colour c (1 <= c <= C-2) of (D+U) t = p
-__global__ void __launch_bounds__(MCG_BLOCK) k_e_bwd(McDev D, int c) {
+template <class T>
+__global__ void __launch_bounds__(MCG_BLOCK) k_e_bwd(McDevT<T> D, int c) {
   if (mcg_scalars(D).done) return;
   const int r0 = __ldg(D.tab + MC_CR + c), r1 = __ldg(D.tab + MC_CR + c + 1);
   const int ceu = __ldg(D.tab + MC_CEU + c), cwu = __ldg(D.tab + MC_CWU + c);
   for (int i = r0 + blockIdx.x * blockDim.x + threadIdx.x; i < r1; i += gridDim.x * blockDim.x)
-    D.t[i] = (__ldcg(D.p + i) - ell_sum(D, ceu + (i - r0), r1 - r0, cwu, D.t, 0.0f)) * __ldcg(D.invd + i);
+    D.t[i] = (__ldcg(D.p + i) - ell_sum(D, ceu + (i - r0), r1 - r0, cwu, D.t, T(0))) * __ldcg(D.invd + i);
 }
 
 // colour 0: the last backward colour t = (p - U t) / d and the first forward
 // colour w = (p + K t) / d (no lower entries), q = t + w, p.q
-__global__ void __launch_bounds__(MCG_BLOCK) k_e_bf0(McDev D) {
+template <class T>
+__global__ void __launch_bounds__(MCG_BLOCK) k_e_bf0(McDevT<T> D) {
   if (mcg_scalars(D).done) return;
   const int r1 = __ldg(D.tab + MC_CR + 1);
   const int ceu = __ldg(D.tab + MC_CEU), cwu = __ldg(D.tab + MC_CWU);
-  float v[1] = {0.0f};
+  double v[1] = {0.0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < r1; i += gridDim.x * blockDim.x) {
-    const float pi = __ldcg(D.p + i), di = __ldcg(D.invd + i), ki = __ldcg(D.kdiag + i);
-    const float ti = (pi - ell_sum(D, ceu + i, r1, cwu, D.t, 0.0f)) * di;
-    const float wi = fmaf(ki, ti, pi) * di;
-    const float qi = ti + wi;
+    const T pi = __ldcg(D.p + i), di = __ldcg(D.invd + i), ki = __ldcg(D.kdiag + i);
+    const T ti = (pi - ell_sum(D, ceu + i, r1, cwu, D.t, T(0))) * di;
+    const T wi = mfma(ki, ti, pi) * di;
+    const T qi = ti + wi;
     D.w[i] = wi;
     D.q[i] = qi;
-    v[0] += pi * qi;
+    v[0] += (double)pi * (double)qi;
   }
   double tot[1];
   if (!mcg_reduce<1>(D, v, tot) || threadIdx.x != 0) return;
@@ -343,24 +388,25 @@ __global__ void __launch_bounds__(MCG_BLOCK) k_e_bf0(McDev D) {
   if (D.ncol == 1) {
     const double alpha = S->rz / tot[0];
     if (!(alpha == alpha) || isinf(alpha)) mcg_stop(D, FC_ERR_BREAKDOWN);
-    else S->alpha = (float)alpha;
+    else S->alpha = alpha;
   }
 }
 
 // forward colour c >= 1: w = (p + K t - L w) / d, q = t + w, p.q; the last
 // colour closes p.q and sets alpha
-__global__ void __launch_bounds__(MCG_BLOCK) k_e_fwd(McDev D, int c) {
+template <class T>
+__global__ void __launch_bounds__(MCG_BLOCK) k_e_fwd(McDevT<T> D, int c) {
   if (mcg_scalars(D).done) return;
   const int r0 = __ldg(D.tab + MC_CR + c), r1 = __ldg(D.tab + MC_CR + c + 1);
   const int cel = __ldg(D.tab + MC_CEL + c), cwl = __ldg(D.tab + MC_CWL + c);
-  float v[1] = {0.0f};
+  double v[1] = {0.0};
   for (int i = r0 + blockIdx.x * blockDim.x + threadIdx.x; i < r1; i += gridDim.x * blockDim.x) {
-    const float pi = __ldcg(D.p + i), di = __ldcg(D.invd + i), ki = __ldcg(D.kdiag + i), ti = __ldcg(D.t + i);
-    const float wi = (fmaf(ki, ti, pi) - ell_sum(D, cel + (i - r0), r1 - r0, cwl, D.w, 0.0f)) * di;
-    const float qi = ti + wi;
+    const T pi = __ldcg(D.p + i), di = __ldcg(D.invd + i), ki = __ldcg(D.kdiag + i), ti = __ldcg(D.t + i);
+    const T wi = (mfma(ki, ti, pi) - ell_sum(D, cel + (i - r0), r1 - r0, cwl, D.w, T(0))) * di;
+    const T qi = ti + wi;
     D.w[i] = wi;
     D.q[i] = qi;
-    v[0] += pi * qi;
+    v[0] += (double)pi * (double)qi;
   }
   double tot[1];
   if (!mcg_reduce<1>(D, v, tot) || threadIdx.x != 0) return;
@@ -369,29 +415,31 @@ __global__ void __launch_bounds__(MCG_BLOCK) k_e_fwd(McDev D, int c) {
   if (c == D.ncol - 1) {
     const double alpha = S->rz / S->pq;
     if (!(alpha == alpha) || isinf(alpha)) mcg_stop(D, FC_ERR_BREAKDOWN);
-    else S->alpha = (float)alpha;
+    else S->alpha = alpha;
   }
 }
 
 // y += alpha p, r~ -= alpha q, z = D r~, r~.z; the stopping test on the
 // D-norm of r~ (relative to the start) or the iteration limit; beta
-__global__ void __launch_bounds__(MCG_BLOCK) k_e_upd(McDev D) {
+template <class T>
+__global__ void __launch_bounds__(MCG_BLOCK) k_e_upd(McDevT<T> D) {
   const McBcast sc = mcg_scalars(D);
   if (sc.done) return;
-  const float alpha = sc.alpha;
-  float v[1] = {0.0f};
+  const T alpha = (T)sc.alpha;
+  double v[1] = {0.0};
   for (int i4 = blockIdx.x * blockDim.x + threadIdx.x; i4 < (D.nP >> 2); i4 += gridDim.x * blockDim.x) {
-    const float4 x4 = __ldcg((const float4*)D.x + i4), p4 = __ldcg((const float4*)D.p + i4);
-    const float4 q4 = __ldcg((const float4*)D.q + i4), r4 = __ldcg((const float4*)D.r + i4);
-    const float4 d4 = __ldcg((const float4*)D.dvec + i4);
-    const float4 rn = make_float4(fmaf(-alpha, q4.x, r4.x), fmaf(-alpha, q4.y, r4.y), fmaf(-alpha, q4.z, r4.z),
-                                  fmaf(-alpha, q4.w, r4.w));
-    const float4 zn = make_float4(d4.x * rn.x, d4.y * rn.y, d4.z * rn.z, d4.w * rn.w);
-    ((float4*)D.x)[i4] = make_float4(fmaf(alpha, p4.x, x4.x), fmaf(alpha, p4.y, x4.y), fmaf(alpha, p4.z, x4.z),
-                                     fmaf(alpha, p4.w, x4.w));
-    ((float4*)D.r)[i4] = rn;
-    ((float4*)D.y)[i4] = zn;
-    v[0] += (rn.x * zn.x + rn.y * zn.y) + (rn.z * zn.z + rn.w * zn.w);
+    T x4[4], p4[4], q4[4], r4[4], d4[4], zn[4];
+    ld4(D.x, i4, x4); ld4(D.p, i4, p4); ld4(D.q, i4, q4); ld4(D.r, i4, r4); ld4(D.dvec, i4, d4);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      r4[k] = mfma(-alpha, q4[k], r4[k]);
+      zn[k] = d4[k] * r4[k];
+      x4[k] = mfma(alpha, p4[k], x4[k]);
+      v[0] += (double)r4[k] * (double)zn[k];
+    }
+    st4(D.x, i4, x4);
+    st4(D.r, i4, r4);
+    st4(D.y, i4, zn);
   }
   double tot[1];
   if (!mcg_reduce<1>(D, v, tot) || threadIdx.x != 0) return;
@@ -401,24 +449,29 @@ __global__ void __launch_bounds__(MCG_BLOCK) k_e_upd(McDev D) {
   if (!(tot[0] == tot[0]) || isinf(tot[0])) { mcg_stop(D, FC_ERR_NAN); return; }
   // r~.z keeps the sign of A (negative for the reference's pressure matrix)
   if (fabs(tot[0]) <= S->tol * S->tol * fabs(S->rz0) || S->it >= S->itmax) { mcg_stop(D, 0); return; }
-  S->beta = (float)(tot[0] / S->rz);
+  S->beta = tot[0] / S->rz;
   S->rz = tot[0];
 }
 
 // p = z + beta p; t = p / d on the last colour (the first backward colour)
-__global__ void __launch_bounds__(MCG_BLOCK) k_e_pupd(McDev D) {
+template <class T>
+__global__ void __launch_bounds__(MCG_BLOCK) k_e_pupd(McDevT<T> D) {
   const McBcast sc = mcg_scalars(D);
   if (sc.done) return;
-  const float beta = sc.beta;
+  const T beta = (T)sc.beta;
   const int clast = __ldg(D.tab + MC_CR + D.ncol - 1);
   for (int i4 = blockIdx.x * blockDim.x + threadIdx.x; i4 < (D.nP >> 2); i4 += gridDim.x * blockDim.x) {
-    const float4 z4 = __ldcg((const float4*)D.y + i4), p4 = __ldcg((const float4*)D.p + i4);
-    const float4 pn = make_float4(fmaf(beta, p4.x, z4.x), fmaf(beta, p4.y, z4.y), fmaf(beta, p4.z, z4.z),
-                                  fmaf(beta, p4.w, z4.w));
-    ((float4*)D.p)[i4] = pn;
+    T z4[4], p4[4];
+    ld4(D.y, i4, z4); ld4(D.p, i4, p4);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) p4[k] = mfma(beta, p4[k], z4[k]);
+    st4(D.p, i4, p4);
     if (4 * i4 >= clast) {  // colour boundaries are multiples of 32 rows
-      const float4 d4 = __ldcg((const float4*)D.invd + i4);
-      ((float4*)D.t)[i4] = make_float4(pn.x * d4.x, pn.y * d4.y, pn.z * d4.z, pn.w * d4.w);
+      T d4[4];
+      ld4(D.invd, i4, d4);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) d4[k] = p4[k] * d4[k];
+      st4(D.t, i4, d4);
     }
   }
 }
@@ -427,10 +480,11 @@ __global__ void __launch_bounds__(MCG_BLOCK) k_e_pupd(McDev D) {
 // the two colour passes, so an iteration is three kernels.  Colour 0 updates
 // its own p and gathers t_j = (z_j + beta p_j) / d_j of its colour-1
 // neighbours, whose p the colour-1 pass has not yet replaced.
-__device__ __forceinline__ float ell_sum_t(const McDev& D, int e, int stride, int w, float beta, float acc) {
+template <class T>
+__device__ __forceinline__ T ell_sum_t(const McDevT<T>& D, int e, int stride, int w, T beta, T acc) {
   if (w <= MC_UNROLL) {
     int c[MC_UNROLL];
-    float m[MC_UNROLL];
+    T m[MC_UNROLL];
 #pragma unroll
     for (int k = 0; k < MC_UNROLL; ++k)
       if (k < w) {
@@ -440,35 +494,37 @@ __device__ __forceinline__ float ell_sum_t(const McDev& D, int e, int stride, in
 #pragma unroll
     for (int k = 0; k < MC_UNROLL; ++k)
       if (k < w) {
-        const float tj = fmaf(beta, __ldcg(D.p + c[k]), __ldcg(D.y + c[k])) * __ldcg(D.invd + c[k]);
-        acc = fmaf(m[k], tj, acc);
+        const T tj = mfma(beta, __ldcg(D.p + c[k]), __ldcg(D.y + c[k])) * __ldcg(D.invd + c[k]);
+        acc = mfma(m[k], tj, acc);
       }
     return acc;
   }
   for (int k = 0; k < w; ++k) {
     const int cj = __ldg(D.col + e + k * stride);
-    acc = fmaf(__ldcg(D.mval + e + k * stride), fmaf(beta, __ldcg(D.p + cj), __ldcg(D.y + cj)) * __ldcg(D.invd + cj), acc);
+    acc = mfma(__ldcg(D.mval + e + k * stride), mfma(beta, __ldcg(D.p + cj), __ldcg(D.y + cj)) * __ldcg(D.invd + cj), acc);
   }
   return acc;
 }
 
 // colour 0 of two: p = z + beta p, t = (p - U t)/d, w = (p + K t)/d, q, p.q
-__global__ void __launch_bounds__(MCG_BLOCK) k_e2_c0(McDev D) {
+template <class T>
+__global__ void __launch_bounds__(MCG_BLOCK) k_e2_c0(McDevT<T> D) {
   const McBcast sc = mcg_scalars(D);
   if (sc.done) return;
+  const T beta = (T)sc.beta;
   const int r1 = __ldg(D.tab + MC_CR + 1);
   const int ceu = __ldg(D.tab + MC_CEU), cwu = __ldg(D.tab + MC_CWU);
-  float v[1] = {0.0f};
+  double v[1] = {0.0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < r1; i += gridDim.x * blockDim.x) {
-    const float pi = fmaf(sc.beta, __ldcg(D.p + i), __ldcg(D.y + i));
-    const float di = __ldcg(D.invd + i), ki = __ldcg(D.kdiag + i);
-    const float ti = (pi - ell_sum_t(D, ceu + i, r1, cwu, sc.beta, 0.0f)) * di;
-    const float wi = fmaf(ki, ti, pi) * di;
-    const float qi = ti + wi;
+    const T pi = mfma(beta, __ldcg(D.p + i), __ldcg(D.y + i));
+    const T di = __ldcg(D.invd + i), ki = __ldcg(D.kdiag + i);
+    const T ti = (pi - ell_sum_t(D, ceu + i, r1, cwu, beta, T(0))) * di;
+    const T wi = mfma(ki, ti, pi) * di;
+    const T qi = ti + wi;
     D.p[i] = pi;
     D.w[i] = wi;
     D.q[i] = qi;
-    v[0] += pi * qi;
+    v[0] += (double)pi * (double)qi;
   }
   double tot[1];
   if (!mcg_reduce<1>(D, v, tot) || threadIdx.x != 0) return;
@@ -476,22 +532,24 @@ __global__ void __launch_bounds__(MCG_BLOCK) k_e2_c0(McDev D) {
 }
 
 // colour 1 of two: p = z + beta p, t = p/d, w = (p + K t - L w)/d, q, p.q, alpha
-__global__ void __launch_bounds__(MCG_BLOCK) k_e2_c1(McDev D) {
+template <class T>
+__global__ void __launch_bounds__(MCG_BLOCK) k_e2_c1(McDevT<T> D) {
   const McBcast sc = mcg_scalars(D);
   if (sc.done) return;
+  const T beta = (T)sc.beta;
   const int r0 = __ldg(D.tab + MC_CR + 1), r1 = __ldg(D.tab + MC_CR + 2);
   const int cel = __ldg(D.tab + MC_CEL + 1), cwl = __ldg(D.tab + MC_CWL + 1);
-  float v[1] = {0.0f};
+  double v[1] = {0.0};
   for (int i = r0 + blockIdx.x * blockDim.x + threadIdx.x; i < r1; i += gridDim.x * blockDim.x) {
-    const float pi = fmaf(sc.beta, __ldcg(D.p + i), __ldcg(D.y + i));
-    const float di = __ldcg(D.invd + i), ki = __ldcg(D.kdiag + i);
-    const float ti = pi * di;
-    const float wi = (fmaf(ki, ti, pi) - ell_sum(D, cel + (i - r0), r1 - r0, cwl, D.w, 0.0f)) * di;
-    const float qi = ti + wi;
+    const T pi = mfma(beta, __ldcg(D.p + i), __ldcg(D.y + i));
+    const T di = __ldcg(D.invd + i), ki = __ldcg(D.kdiag + i);
+    const T ti = pi * di;
+    const T wi = (mfma(ki, ti, pi) - ell_sum(D, cel + (i - r0), r1 - r0, cwl, D.w, T(0))) * di;
+    const T qi = ti + wi;
     D.p[i] = pi;
     D.w[i] = wi;
     D.q[i] = qi;
-    v[0] += pi * qi;
+    v[0] += (double)pi * (double)qi;
   }
   double tot[1];
   if (!mcg_reduce<1>(D, v, tot) || threadIdx.x != 0) return;
@@ -499,27 +557,29 @@ __global__ void __launch_bounds__(MCG_BLOCK) k_e2_c1(McDev D) {
   S->pq += tot[0];
   const double alpha = S->rz / S->pq;
   if (!(alpha == alpha) || isinf(alpha)) mcg_stop(D, FC_ERR_BREAKDOWN);
-  else S->alpha = (float)alpha;
+  else S->alpha = alpha;
 }
 
 // colour c of x = (D+U)^-1 y, in place on x (higher colours already hold x)
-__global__ void __launch_bounds__(MCG_BLOCK) k_e_xb(McDev D, int c) {
+template <class T>
+__global__ void __launch_bounds__(MCG_BLOCK) k_e_xb(McDevT<T> D, int c) {
   const int r0 = __ldg(D.tab + MC_CR + c), r1 = __ldg(D.tab + MC_CR + c + 1);
   const int ceu = __ldg(D.tab + MC_CEU + c), cwu = __ldg(D.tab + MC_CWU + c);
   const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= r1) return;
-  D.x[i] = (__ldcg(D.x + i) - ell_sum(D, ceu + (i - r0), r1 - r0, cwu, D.x, 0.0f)) * __ldcg(D.invd + i);
+  D.x[i] = (__ldcg(D.x + i) - ell_sum(D, ceu + (i - r0), r1 - r0, cwu, D.x, T(0))) * __ldcg(D.invd + i);
 }
 
 }  // namespace
 
-static McDev mc_dev(DevColoured& m, const double* a) {
-  McDev D;
+template <class T>
+static McDevT<T> mc_dev(DevColoured& m, McBuf<T>& b, const double* a) {
+  McDevT<T> D;
   D.nP = m.nP; D.ncol = m.ncol; D.c0end = m.crow[1];
   D.tab = m.tab.p; D.col = m.col.p; D.src = m.src.p; D.tsrc = m.tsrc.p; D.dslot = m.dslot.p; D.a = a;
-  D.mval = m.mval.p; D.adiag = m.adiag.p; D.invd = m.invd.p; D.dvec = m.dvec.p; D.kdiag = m.kdiag.p;
+  D.mval = b.mval.p; D.adiag = b.adiag.p; D.invd = b.invd.p; D.dvec = b.dvec.p; D.kdiag = b.kdiag.p;
   D.dset = m.dset.p;
-  D.x = m.x.p; D.r = m.r.p; D.p = m.p.p; D.q = m.q.p; D.y = m.y.p; D.t = m.t.p; D.w = m.w.p;
+  D.x = b.x.p; D.r = b.r.p; D.p = b.p.p; D.q = b.q.p; D.y = b.y.p; D.t = b.t.p; D.w = b.w.p;
   D.sc = m.sc.p; D.part = m.part.p; D.cnt = m.cnt.p;
   D.h = 0;
   return D;
@@ -531,13 +591,14 @@ static inline unsigned mc_blocks(int rows) { return (unsigned)std::max(1, (rows 
 // a while node whose body is one iteration.  The kernels' arguments are fixed
 // (the system's own buffers); tolerance and iteration limit are read from the
 // scalar block, which k_mc_gather resets before every launch.
-static int mc_build_graph(fc_ctx* ctx, DevColoured& m) {
+template <class T>
+static int mc_build_graph(fc_ctx* ctx, DevColoured& m, McBuf<T>& b) {
   cudaGraph_t g = nullptr;
   FC_CUDA_TRY(ctx, cudaGraphCreate(&g, 0));
-  m.graph = g;
+  b.graph = g;
   cudaGraphConditionalHandle h;
   FC_CUDA_TRY(ctx, cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
-  McDev D = mc_dev(m, nullptr);
+  McDevT<T> D = mc_dev(m, b, nullptr);
   D.h = h;
   const int C = m.ncol;
   // kernel nodes copy their arguments at creation, so the locals below may go
@@ -559,16 +620,16 @@ static int mc_build_graph(fc_ctx* ctx, DevColoured& m) {
   };
   auto blocks_of = [&](int c) { return mc_blocks(m.crow[c + 1] - m.crow[c]); };
   // loop-body grids: capped at MC_WAVES waves of resident blocks
-  auto body_blocks = [&](unsigned nat) { return std::min(nat, (unsigned)(MC_WAVES * m.wave)); };
+  auto body_blocks = [&](unsigned nat) { return std::min(nat, (unsigned)(MC_WAVES * b.wave)); };
   int st;
   cudaGraphNode_t prev = nullptr;
   void* a1[1] = {&D};
   // prologue: (D+L) r~ = b colour by colour, then z, p, t and r~.z
   for (int c = 0; c < C; ++c) {
     void* args[2] = {&D, &cs[c]};
-    if ((st = add(g, prev, c > 0, (const void*)k_e_fwdb, blocks_of(c), args))) return st;
+    if ((st = add(g, prev, c > 0, (const void*)k_e_fwdb<T>, blocks_of(c), args))) return st;
   }
-  if ((st = add(g, prev, true, (const void*)k_e_start, mc_blocks(m.nP), a1))) return st;
+  if ((st = add(g, prev, true, (const void*)k_e_start<T>, mc_blocks(m.nP), a1))) return st;
   cudaGraphNodeParams cp = {};
   cp.type = cudaGraphNodeTypeConditional;
   cp.conditional.handle = h;
@@ -582,30 +643,30 @@ static int mc_build_graph(fc_ctx* ctx, DevColoured& m) {
   cudaGraphNode_t bp = nullptr;
   bool have = false;
   if (C == 2) {  // red-black: three kernels per iteration
-    if ((st = add(body, bp, false, (const void*)k_e2_c0, body_blocks(blocks_of(0)), a1))) return st;
-    if ((st = add(body, bp, true, (const void*)k_e2_c1, body_blocks(blocks_of(1)), a1))) return st;
-    if ((st = add(body, bp, true, (const void*)k_e_upd, body_blocks(mc_blocks(m.nP / 4)), a1))) return st;
+    if ((st = add(body, bp, false, (const void*)k_e2_c0<T>, body_blocks(blocks_of(0)), a1))) return st;
+    if ((st = add(body, bp, true, (const void*)k_e2_c1<T>, body_blocks(blocks_of(1)), a1))) return st;
+    if ((st = add(body, bp, true, (const void*)k_e_upd<T>, body_blocks(mc_blocks(m.nP / 4)), a1))) return st;
   } else {
     for (int c = C - 2; c >= 1; --c) {
       void* args[2] = {&D, &cs[c]};
-      if ((st = add(body, bp, have, (const void*)k_e_bwd, body_blocks(blocks_of(c)), args))) return st;
+      if ((st = add(body, bp, have, (const void*)k_e_bwd<T>, body_blocks(blocks_of(c)), args))) return st;
       have = true;
     }
-    if ((st = add(body, bp, have, (const void*)k_e_bf0, body_blocks(blocks_of(0)), a1))) return st;
+    if ((st = add(body, bp, have, (const void*)k_e_bf0<T>, body_blocks(blocks_of(0)), a1))) return st;
     for (int c = 1; c < C; ++c) {
       void* args[2] = {&D, &cs[c]};
-      if ((st = add(body, bp, true, (const void*)k_e_fwd, body_blocks(blocks_of(c)), args))) return st;
+      if ((st = add(body, bp, true, (const void*)k_e_fwd<T>, body_blocks(blocks_of(c)), args))) return st;
     }
-    if ((st = add(body, bp, true, (const void*)k_e_upd, body_blocks(mc_blocks(m.nP / 4)), a1))) return st;
-    if ((st = add(body, bp, true, (const void*)k_e_pupd, body_blocks(mc_blocks(m.nP / 4)), a1))) return st;
+    if ((st = add(body, bp, true, (const void*)k_e_upd<T>, body_blocks(mc_blocks(m.nP / 4)), a1))) return st;
+    if ((st = add(body, bp, true, (const void*)k_e_pupd<T>, body_blocks(mc_blocks(m.nP / 4)), a1))) return st;
   }
   // after the loop: x = (D+U)^-1 y, colours C-1..0
   prev = loop;
   for (int c = C - 1; c >= 0; --c) {
     void* args[2] = {&D, &cs[c]};
-    if ((st = add(g, prev, true, (const void*)k_e_xb, blocks_of(c), args))) return st;
+    if ((st = add(g, prev, true, (const void*)k_e_xb<T>, blocks_of(c), args))) return st;
   }
-  FC_CUDA_TRY(ctx, cudaGraphInstantiate(&m.exec, g, 0));
+  FC_CUDA_TRY(ctx, cudaGraphInstantiate(&b.exec, g, 0));
   return FC_OK;
 }
 
@@ -638,31 +699,39 @@ static int mc_prepare(fc_ctx* ctx, CsrSystem* s) {
     delete m;
     return st;
   }
-  const size_t nP = std::max(1, L.nP), ne = std::max<size_t>(1, (size_t)L.nent);
+  const size_t nP = std::max(1, L.nP);
+  m->nent = std::max<size_t>(1, (size_t)L.nent);
   m->maxblocks = (int)mc_blocks(L.nP);
-  DVec<float>* fv[] = {&m->adiag, &m->invd, &m->dvec, &m->kdiag, &m->x, &m->r, &m->p, &m->q, &m->y, &m->t, &m->w};
-  bool ok = true;
-  for (auto* v : fv) ok = ok && v->alloc(nP) == cudaSuccess;
-  ok = ok && m->mval.alloc(ne) == cudaSuccess && m->dset.alloc(nP) == cudaSuccess &&
-       m->part.alloc((size_t)2 * m->maxblocks) == cudaSuccess && m->cnt.alloc(1) == cudaSuccess &&
-       m->sc.alloc(1) == cudaSuccess && cudaMallocHost(&m->h_sc, sizeof(McScal)) == cudaSuccess;
+  bool ok = m->dset.alloc(nP) == cudaSuccess && m->part.alloc((size_t)2 * m->maxblocks) == cudaSuccess &&
+            m->cnt.alloc(1) == cudaSuccess && m->sc.alloc(1) == cudaSuccess &&
+            cudaMallocHost(&m->h_sc, sizeof(McScal)) == cudaSuccess;
   if (!ok) {
     delete m;
     return fc_fail_msg(ctx, FC_ERR_NOMEM, "multicolour buffers");
   }
-  // padding entries keep the value 0 (the setup writes real entries only)
-  FC_CUDA_TRY(ctx, fc_zero(ctx->stream, m->mval.p, ne * sizeof(float)));
   FC_CUDA_TRY(ctx, fc_zero(ctx->stream, m->cnt.p, sizeof(unsigned)));
-  {
-    int nb = 0;  // resident blocks per SM of the widest body kernel
-    FC_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_e2_c0, MCG_BLOCK, 0));
-    m->wave = std::max(1, ctx->num_sms) * std::max(1, nb);
-  }
-  if ((st = mc_build_graph(ctx, *m))) {
-    delete m;
-    return st;
-  }
   s->mc = m;
+  return FC_OK;
+}
+
+// the buffers and the graph of value type T, on first use
+template <class T>
+static int mc_prepare_buf(fc_ctx* ctx, DevColoured& m, McBuf<T>& b) {
+  if (b.ready) return FC_OK;
+  const size_t nP = std::max(1, m.nP);
+  DVec<T>* fv[] = {&b.adiag, &b.invd, &b.dvec, &b.kdiag, &b.x, &b.r, &b.p, &b.q, &b.y, &b.t, &b.w};
+  bool ok = true;
+  for (auto* v : fv) ok = ok && v->alloc(nP) == cudaSuccess;
+  ok = ok && b.mval.alloc(m.nent) == cudaSuccess;
+  if (!ok) return fc_fail_msg(ctx, FC_ERR_NOMEM, "multicolour buffers");
+  // padding entries keep the value 0 (the setup writes real entries only)
+  FC_CUDA_TRY(ctx, fc_zero(ctx->stream, b.mval.p, m.nent * sizeof(T)));
+  int nb = 0;  // resident blocks per SM of the widest body kernel
+  FC_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_e2_c0<T>, MCG_BLOCK, 0));
+  b.wave = std::max(1, ctx->num_sms) * std::max(1, nb);
+  int st = mc_build_graph(ctx, m, b);
+  if (st) return st;
+  b.ready = true;
   return FC_OK;
 }
 
@@ -676,12 +745,13 @@ int mc_colours(fc_ctx* ctx, CsrSystem* s, int* ncol) {
 // One FP32 inner solve A e = r64 from e = 0 to the relative L1 reduction
 // tol, at most itmax iterations; x64 += e.  setup: refresh the FP32 values and
 // the DILU diagonal from a (the first inner solve of a refinement loop).
-int mc_inner_solve(fc_ctx* ctx, CsrSystem* s, const double* a, const double* r64, double* x64, double tol, int itmax,
-                   bool setup, int* itr_out, int* status_out) {
-  int st = mc_prepare(ctx, s);
+template <class T>
+static int mc_inner_solve_t(fc_ctx* ctx, DevColoured& m, const double* a, const double* r64, double* x64, double tol,
+                            int itmax, bool setup, int* itr_out, int* status_out) {
+  McBuf<T>& b = mc_buf(m, T(0));
+  int st = mc_prepare_buf(ctx, m, b);
   if (st) return st;
-  DevColoured& m = *s->mc;
-  McDev D = mc_dev(m, a);
+  McDevT<T> D = mc_dev(m, b, a);
   const unsigned eb = std::min(8192u, mc_blocks(m.nP));
   k_mc_gather<<<eb, MCG_BLOCK, 0, ctx->stream>>>(D, m.perm.p, r64, tol, itmax);
   ctx->kernel_launches++;
@@ -693,14 +763,14 @@ int mc_inner_solve(fc_ctx* ctx, CsrSystem* s, const double* a, const double* r64
   }
   FC_CUDA_TRY(ctx, cudaGetLastError());
   if (!ctx->tracing) {
-    FC_CUDA_TRY(ctx, cudaGraphLaunch(m.exec, ctx->stream));
+    FC_CUDA_TRY(ctx, cudaGraphLaunch(b.exec, ctx->stream));
   } else {
     // diagnostic mode (fc_set_tracing): the same kernels launched from the
     // host, so that profilers see every launch; the loop checks the stop
     // flag every 32 iterations (the kernels of later iterations return at once)
     const int C = m.ncol;
     auto blocks_of = [&](int c) { return mc_blocks(m.crow[c + 1] - m.crow[c]); };
-    auto body_blocks = [&](unsigned nat) { return std::min(nat, (unsigned)(MC_WAVES * m.wave)); };
+    auto body_blocks = [&](unsigned nat) { return std::min(nat, (unsigned)(MC_WAVES * b.wave)); };
     for (int c = 0; c < C; ++c) k_e_fwdb<<<blocks_of(c), MCG_BLOCK, 0, ctx->stream>>>(D, c);
     k_e_start<<<mc_blocks(m.nP), MCG_BLOCK, 0, ctx->stream>>>(D);
     for (int base = 0; base < std::max(itmax, 1); base += 32) {
@@ -725,7 +795,7 @@ int mc_inner_solve(fc_ctx* ctx, CsrSystem* s, const double* a, const double* r64
     for (int c = C - 1; c >= 0; --c) k_e_xb<<<blocks_of(c), MCG_BLOCK, 0, ctx->stream>>>(D, c);
     FC_CUDA_TRY(ctx, cudaGetLastError());
   }
-  k_mc_scatter_add<<<eb, MCG_BLOCK, 0, ctx->stream>>>(m.nP, m.perm.p, m.x.p, x64);
+  k_mc_scatter_add<<<eb, MCG_BLOCK, 0, ctx->stream>>>(m.nP, m.perm.p, b.x.p, x64);
   FC_CUDA_TRY(ctx, cudaMemcpyAsync(m.h_sc, m.sc.p, sizeof(McScal), cudaMemcpyDeviceToHost, ctx->stream));
   FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   // graph kernels: prologue C + 1, per iteration 2 C (3 for two colours; the
@@ -734,4 +804,12 @@ int mc_inner_solve(fc_ctx* ctx, CsrSystem* s, const double* a, const double* r64
   *itr_out = m.h_sc->it;
   *status_out = m.h_sc->status;
   return FC_OK;
+}
+
+int mc_inner_solve(fc_ctx* ctx, CsrSystem* s, const double* a, const double* r64, double* x64, double tol, int itmax,
+                   bool setup, bool fp64, int* itr_out, int* status_out) {
+  int st = mc_prepare(ctx, s);
+  if (st) return st;
+  return fp64 ? mc_inner_solve_t<double>(ctx, *s->mc, a, r64, x64, tol, itmax, setup, itr_out, status_out)
+              : mc_inner_solve_t<float>(ctx, *s->mc, a, r64, x64, tol, itmax, setup, itr_out, status_out);
 }

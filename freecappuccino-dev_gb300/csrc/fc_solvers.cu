@@ -1041,14 +1041,13 @@ static int solve_mixed(fc_ctx* ctx, CsrSystem* s, const std::string& solver, con
                        const double* b, int itr_max, double tol_abs, double tol_rel, SolveResult* res) {
   if (solver != "iccg" && solver != "bicgstab" && solver != "dpcg")
     return solve_fp64(ctx, s, solver, a, x, b, itr_max, tol_abs, tol_rel, res);
-  // FC_PREC_MIXED_COLOURED mixes the ICCG solves only; the others stay FP64
-  if (ctx->precision == FC_PREC_MIXED_COLOURED && solver != "iccg")
-    return solve_fp64(ctx, s, solver, a, x, b, itr_max, tol_abs, tol_rel, res);
+  // the coloured modes change the ICCG solves only; the others stay FP64
+  const bool coloured = ctx->precision == FC_PREC_MIXED_COLOURED || ctx->precision == FC_PREC_COLOURED_FP64;
+  if (coloured && solver != "iccg") return solve_fp64(ctx, s, solver, a, x, b, itr_max, tol_abs, tol_rel, res);
   if (solver == "bicgstab" && s->tslot_oob)
     return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "bicgstab: pattern is not structurally symmetric");
-  // FC_PREC_MIXED_COLOURED: the ICCG inner solve runs on the multicolour
-  // ordering (fc_mc.cu)
-  const bool coloured = ctx->precision == FC_PREC_MIXED_COLOURED;
+  // the coloured modes: the ICCG inner solve runs on the multicolour
+  // ordering (fc_mc.cu), in FP32 or, as a diagnostic, in FP64
   int st = alloc_work32(ctx, s);
   if (st) return st;
   const int n = s->n;
@@ -1092,7 +1091,7 @@ static int solve_mixed(fc_ctx* ctx, CsrSystem* s, const std::string& solver, con
       const double tol_k = std::min(1e-1, std::max(inner_tol, left));
       int itr = 0, stat = 0;
       st = mc_inner_solve(ctx, s, a, s->r.p, x, tol_k, std::min(inner_itmax, itr_max - total_itr), outer == 0,
-                          &itr, &stat);
+                          ctx->precision == FC_PREC_COLOURED_FP64, &itr, &stat);
       if (st) return st;
       if (stat) { res->status = stat; return FC_OK; }
       total_itr += itr;

@@ -36,6 +36,7 @@ FC_TIME_STEADY, FC_TIME_BDF, FC_TIME_BDF2, FC_TIME_BDF3 = 0, 1, 2, 3
 FC_PREC_FP64 = 0
 FC_PREC_MIXED = 1
 FC_PREC_MIXED_COLOURED = 2
+FC_PREC_COLOURED_FP64 = 3  # the coloured inner ICCG in FP64 (diagnostic)
 FC_NOALLOC_MAX_N = 1 << 20  # rows of fc_dpcg_noalloc's static scratch
 GRAD = {"gauss": 0, "lstsq": 1, "lstsq_dm": 2}
 NOMAX = 6

@@ -122,6 +122,10 @@ typedef struct fc_ctx fc_ctx;
  * stopping test and the FP64 refinement do not.  The other solvers run in
  * FP64 as in FC_PREC_FP64. */
 #define FC_PREC_MIXED_COLOURED 2
+/* A diagnostic of precision's share in FC_PREC_MIXED_COLOURED: the same
+ * multicolour preconditioner, refinement loop and stopping test, with the
+ * inner solve in FP64.  No counterpart in the reference. */
+#define FC_PREC_COLOURED_FP64 3
 
 int fc_init(int device, fc_ctx** out);
 void fc_finalize(fc_ctx* ctx);

@@ -145,18 +145,20 @@ def test_mixed_precision_reaches_fp64_tolerance(ctx, oracle):
     assert np.abs(x - xo).max() <= 1e-7 * np.abs(xo).max()
 
 
+@pytest.mark.parametrize("mode", ["mixed", "fp64"])
 @pytest.mark.parametrize("case", ["hex", "tet"])
-def test_mixed_coloured_reaches_fp64_tolerance(ctx, oracle, fc, case):
+def test_mixed_coloured_reaches_fp64_tolerance(ctx, oracle, fc, case, mode):
     """FC_PREC_MIXED_COLOURED: the FP32 inner ICCG runs on the multicolour
     ordering (2 colours on hexes, more on tets); the FP64 refinement still
-    stops on the reference's criterion, so the answer is the FP64 one."""
+    stops on the reference's criterion, so the answer is the FP64 one.
+    FC_PREC_COLOURED_FP64 runs the same inner solve in FP64."""
     if case == "hex":
         m, a, oc = mesh_case("hexm", 14, 12, 10)
     else:
         m, a, oc = mesh_case("tetm", 7, 6, 5, tets=True)
     ia, ja, av, dg, b = laplacian_system(oc, mask=0b1)
     xo, _, _, _ = oracle.solve("iccg", ia, ja, av, dg, np.zeros(len(dg)), b, 5000, 0.0, 1e-10)
-    ctx.set_precision(fc.FC_PREC_MIXED_COLOURED, 1e-5, 0)
+    ctx.set_precision(fc.FC_PREC_MIXED_COLOURED if mode == "mixed" else fc.FC_PREC_COLOURED_FP64, 1e-5, 0)
     try:
         x, _, info, st = ctx.csrsolve("iccg", ia, ja, av, dg, np.zeros(len(dg)), b, 5000, 0.0, 1e-10)
         # same pattern, new values: the colour-ordered factor is rebuilt

@@ -158,8 +158,8 @@ def progress(msg):
 
 def batch_block(fc, args, dev):
     """C3b: independent steady convection-diffusion problems solved together.
-    count problems (64 in the configuration, 16 by default here to keep the
-    default run short): n^3 perturbed hex meshes of [0, 2 pi]^3 with
+    count problems (64, the configuration's count, by default): n^3
+    perturbed hex meshes of [0, 2 pi]^3 with
     n ~ U{20..80} (seed 44), cell Peclet number U h / gamma ~ lognormal(0, 1)
     (seed 45), the C4 velocity field and source (tests/cd_cases.py); BiCGStab
     (DILU) to batch_tol relative L1 per problem.  Legs, all on device-resident
@@ -404,7 +404,7 @@ def simple_iterations(n=128, iters=4, perturb=PERTURB, dev=0):
 
 
 def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None, tets=False, viscos=0.01, scheme=1, grad=0,
-                 iters=None, cpu_iters=None, urf=(0.8, 0.3), momentum_batch=False):
+                 iters=None, cpu_iters=None, urf=(0.8, 0.3), momentum_batch=False, skip=None):
     """SIMPLE iterations per second on the n^3 lid-driven cavity (unit cube,
     nu = 0.01, central differencing with deferred correction, Gauss gradients,
     BiCGStab(DILU) for U, ICCG(DIC) for p, the settings of
@@ -413,6 +413,7 @@ def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None, tets=Fa
     U(-perturb h, perturb h) (seed 42): the non-orthogonal mesh."""
     m = fc.Mesh.box(n, n, n, 1.0, 1.0, 1.0, perturb=perturb, seed=MESH_SEED, tets=tets)
     iters = args.simple_iters if iters is None else iters
+    skip = args.simple_skip if skip is None else skip
     cpu_iters = args.simple_cpu_iters if cpu_iters is None else cpu_iters
     nC, nT = m.numCells, m.numTotal
     a, u, nwal = cavity_fields(m, nT, nC)
@@ -440,7 +441,7 @@ def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None, tets=Fa
     for mode, key in ((fc.FC_PREC_FP64, "value"), (fc.FC_PREC_MIXED_COLOURED, "mixed")):
         ctx.set_precision(mode, MIXED_INNER_TOL, 0) if mode else ctx.set_precision(mode)
         reset()
-        for _ in range(args.simple_skip):
+        for _ in range(skip):
             ctx.simple_iteration()
         ctx.sync()
         ctx.event(0)
@@ -458,7 +459,7 @@ def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None, tets=Fa
         # the three solves, timed alone, then whole SIMPLE iterations
         ctx.set_precision(fc.FC_PREC_FP64)
         reset()
-        for _ in range(args.simple_skip):
+        for _ in range(max(skip, 10)):
             ctx.simple_iteration()
         c3 = {"workload": "calcuvw on the developed field: momentum assembly + U, V, W BiCGStab(DILU) solves, "
                           f"maxiterU {prm.maxiterU}, tolRelU {prm.tolRelU:g}"}
@@ -483,7 +484,7 @@ def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None, tets=Fa
         out["value_batched_momentum"] = 1e3 / ms
         out["value_batched_momentum_ms_per_iteration"] = ms
         out["value_batched_momentum_resor"] = [float(v) for v in res]
-    out["iterations_timed"] = f"{iters} after {args.simple_skip} untimed"
+    out["iterations_timed"] = f"{iters} after {skip} untimed"
     out["mixed_note"] = ("ICCG for p with the multicolour FP32 inner solve, capped at maxiterP iterations as the "
                          "reference caps it: it reduces the p residual less per SIMPLE iteration than the "
                          "natural-order DIC, so the *_resor after the same iterations differ")
@@ -621,6 +622,62 @@ def spmv_leg(fc, ctx, nC, calls):
     return {"calls": calls, "us_per_call": us, "algorithmic_bytes": nbytes,
             "gbs_per_call": nbytes / (us * 1e-6) / 1e9,
             "note": "per call, host work and the call's synchronisation included (upper bound on the kernel)"}
+
+
+def gradient_block(fc, args, dev):
+    """Gradient kernels on the n^3 perturbed hex mesh (128^3: 2,097,152
+    cells): fc_grad on a device-resident smooth field for Gauss, LSQ,
+    LSQ_DM, their exact 3x3 forms and the node-based Gauss gradient, and
+    Gauss with each slope limiter.  Event time per call (the limiter and
+    node-gradient calls include their extra passes); minimal bytes = the
+    field and the geometry each gradient reads once plus the gradient it
+    writes, for a bandwidth figure."""
+    n = args.grad_n
+    m = fc.Mesh.box(n, n, n, 1.0, 1.0, 1.0, perturb=PERTURB, seed=MESH_SEED)
+    ctx = fc.Context(dev)
+    ctx.set_mesh(m)
+    nC, nI, nF, nT = m.numCells, m.numInnerFaces, m.numFaces, m.numTotal
+    xc, yc, zc = ctx.geometry("xc"), ctx.geometry("yc"), ctx.geometry("zc")
+    phi = np.zeros(nT)
+    phi[:nC] = np.sin(3 * xc) * np.cos(2 * yc) + zc * zc
+    ctx.field_set("u", phi)
+    pu, pg = ctx.field_ptr("u"), ctx.field_ptr("dUdxi")
+    # gauss: phi, owner/neighbour, area vectors, facint, vol in; g out
+    gauss_bytes = 8 * nT + 4 * (nF + nI) + 24 * nF + 8 * nI + 8 * nC + 24 * nT
+    lsq_bytes = 8 * nT + 4 * (nF + nI) + 24 * nF + 72 * nC + 24 * nT  # face centres or cell centres, D matrix
+
+    def timed(scheme, calls):
+        def call():
+            st = ctx.L.fc_grad(ctx.h, scheme, pu, pg)
+            if st != 0:
+                raise RuntimeError(f"fc_grad({scheme}) status {st}: {ctx.error()}")
+        for _ in range(3):
+            call()
+        ctx.sync()
+        ctx.event(0)
+        for _ in range(calls):
+            call()
+        ctx.event(1)
+        return ctx.elapsed_ms() / calls
+
+    out = {"workload": f"{n}^3 perturbed hexes (+-{PERTURB:g} h), smooth field, fc_grad on device arrays",
+           "cells": nC, "calls": args.grad_calls}
+    for name, scheme, nbytes in (("gauss", fc.FC_GRAD_GAUSS, gauss_bytes), ("lsq", fc.FC_GRAD_LSQ, lsq_bytes),
+                                 ("lsq_dm", fc.FC_GRAD_LSQ_DM, lsq_bytes),
+                                 ("lsq_exact", fc.FC_GRAD_LSQ_EXACT, lsq_bytes),
+                                 ("lsq_dm_exact", fc.FC_GRAD_LSQ_DM_EXACT, lsq_bytes),
+                                 ("node_gauss", fc.FC_GRAD_NODE_GAUSS, None)):
+        ms = timed(scheme, args.grad_calls)
+        out[name + "_ms"] = ms
+        if nbytes:
+            out[name + "_min_bytes_gbs"] = nbytes / (ms * 1e-3) / 1e9
+    for name, kind in (("barth_jespersen", fc.FC_LIMITER_BJ), ("venkatakrishnan", fc.FC_LIMITER_VENKAT),
+                       ("r3", fc.FC_LIMITER_R), ("multidimensional", fc.FC_LIMITER_MD)):
+        ctx.set_gradient_limiter(kind)
+        out["gauss_" + name + "_ms"] = timed(fc.FC_GRAD_GAUSS, args.grad_calls)
+    ctx.set_gradient_limiter(fc.FC_LIMITER_NONE)
+    ctx.close()
+    return out
 
 
 def adjoint_block(fc, args, dev):
@@ -860,6 +917,8 @@ def run_gpu(args, rank, world, dist):
         line["cpu_baseline"] = cpu_baseline(ia, ja, a_host, dg, b)
     if args.simple_n > 0:
         line["simple"] = simple_block(fc, args, dev, not args.no_cpu, args.simple_n)
+    if args.grad_n > 0:
+        line["gradients"] = gradient_block(fc, args, dev)
     if args.adjoint_n > 0:
         line["adjoint"] = adjoint_block(fc, args, dev)
     if args.batch_count > 0:
@@ -875,7 +934,8 @@ def run_gpu(args, rank, world, dist):
                                            iters=args.simple_tet_iters, cpu_iters=1, urf=(0.6, 0.2))
     if args.simple_big_n > 0:
         line["simple_perturbed"] = simple_block(fc, args, dev, not args.no_cpu, args.simple_big_n, PERTURB,
-                                                cpu_skip=args.simple_big_cpu_skip, momentum_batch=True)
+                                                cpu_skip=args.simple_big_cpu_skip, momentum_batch=True,
+                                                iters=args.simple_big_iters, skip=args.simple_big_skip)
     print(json.dumps(line), flush=True)
 
 
@@ -899,20 +959,25 @@ def main():
     ap.add_argument("--simple-tet-n", type=int, default=0,
                     help="hexes per side of the tetrahedral SIMPLE cavity, 6 tets each (0: skip; 100 = 6M cells)")
     ap.add_argument("--simple-tet-iters", type=int, default=100, help="timed SIMPLE iterations there")
+    ap.add_argument("--grad-n", type=int, default=128, help="cells per side of the gradient-kernel leg (0: skip)")
+    ap.add_argument("--grad-calls", type=int, default=20, help="timed fc_grad calls per scheme there")
     ap.add_argument("--adjoint-n", type=int, default=96, help="cells per side of the adjoint case (0: skip)")
     ap.add_argument("--adjoint-fd-dirs", type=int, default=32, help="directions of the finite-difference check")
     ap.add_argument("--momentum-calls", type=int, default=5, help="timed calcuvw calls of the C3a leg")
-    ap.add_argument("--piso-n", type=int, default=0, help="cells per side of the PISO leg (0: skip)")
+    ap.add_argument("--piso-n", type=int, default=64, help="cells per side of the PISO leg (0: skip)")
     ap.add_argument("--piso-steps", type=int, default=10, help="timed PISO time steps")
-    ap.add_argument("--batch-count", type=int, default=16, help="problems of the batched leg (0: skip)")
+    ap.add_argument("--batch-count", type=int, default=64, help="problems of the batched leg (0: skip)")
     ap.add_argument("--batch-tol", type=float, default=1e-6, help="relative L1 tolerance there")
     ap.add_argument("--batch-inner-tol", type=float, default=1e-4, help="FP32 inner tolerance there")
     ap.add_argument("--batch-inner-itmax", type=int, default=100, help="FP32 inner iteration cap there")
     ap.add_argument("--batch-reps", type=int, default=2, help="timed repetitions of each batched leg")
     ap.add_argument("--batch-tune-rounds", type=int, default=2, help="autotuner plans tried")
     ap.add_argument("--batch-cpu-seconds", type=float, default=10.0, help="oracle time of the CPU estimate")
-    ap.add_argument("--simple-iters", type=int, default=20, help="timed SIMPLE iterations")
-    ap.add_argument("--simple-skip", type=int, default=10, help="untimed SIMPLE iterations before them")
+    ap.add_argument("--simple-iters", type=int, default=200,
+                    help="timed SIMPLE iterations of the 64^3 cavity (the configuration's 200 outer iterations)")
+    ap.add_argument("--simple-skip", type=int, default=0, help="untimed SIMPLE iterations before them")
+    ap.add_argument("--simple-big-iters", type=int, default=20, help="timed SIMPLE iterations of the 128^3 leg")
+    ap.add_argument("--simple-big-skip", type=int, default=10, help="untimed SIMPLE iterations before them")
     ap.add_argument("--simple-cpu-iters", type=int, default=3, help="oracle SIMPLE iterations timed")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))

@@ -560,8 +560,11 @@ class Context:
             return m.numCells
         if name in ("dUdxi", "dVdxi", "dWdxi", "dPdxi", "dTdxi"):
             return 3 * m.numTotal
-        if name == "a":
-            return 2 * m.numInnerFaces + m.numCells
+        if name == "a":  # nnz: 2 (numInnerFaces + numPeriodic) + numCells
+            n, nnz = C.c_int(0), C.c_int(0)
+            self._check(self.L.fc_get_csr_pattern(self.h, C.byref(n), C.byref(nnz), None, None, None, None, None),
+                        "fc_get_csr_pattern")
+            return nnz.value
         if name == "visw":
             return self._nwal()
         raise KeyError(name)

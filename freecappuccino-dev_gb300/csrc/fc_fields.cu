@@ -46,6 +46,10 @@ int fc_fields_alloc(fc_ctx* ctx) {
   add("uoo", &F.uoo, nT, 0); add("voo", &F.voo, nT, 0); add("woo", &F.woo, nT, 0);
   add("uooo", &F.uooo, nT, 0); add("vooo", &F.vooo, nT, 0); add("wooo", &F.wooo, nT, 0);
   add("rU", &F.rU, nC, 0); add("rV", &F.rV, nC, 0); add("rW", &F.rW, nC, 0);
+  add("te", &F.te, nT, 0); add("ed", &F.ed, nT, 0); add("fsst", &F.fsst, nT, 0);
+  add("dTEdxi", &F.gte, 3 * nT, 1); add("dEDdxi", &F.ged, 3 * nT, 1);
+  add("gen", &F.gen, nC, 0); add("magStrain", &F.mag, nC, 0); add("walldist", &F.wd, nC, 0);
+  add("tau", &F.tau, nW, 0); add("ypl", &F.ypl, nW, 0);
   add("fscratch", &F.fscratch, 3 * (nF > 0 ? nF : 1), 2);
   add("cscratch", &F.cscratch, 3 * nC, 2);
   (void)nI;

@@ -18,6 +18,10 @@ struct FieldStore {
   DVec<double> gu, gv, gw, gp, gt;  // gradients, SoA [3][numTotal]
   DVec<double> uo, vo, wo, uoo, voo, woo, uooo, vooo, wooo;  // old time levels (numTotal)
   DVec<double> rU, rV, rW;          // PISO: explicit momentum terms (numCells)
+  // k-omega SST: k, omega, blending function F1 (numTotal), their gradients
+  // (SoA), production, strain magnitude, wall distance (numCells), wall shear
+  // stress and y+ (per wall face)
+  DVec<double> te, ed, fsst, gte, ged, gen, mag, wd, tau, ypl;
   DVec<double> fscratch, cscratch, cscratch_big;
   DVec<double> dmat;                // least-squares cofactors, SoA [9][numCells]
   int dmat_scheme = 0;              // scheme the cofactors were built for (0: none)

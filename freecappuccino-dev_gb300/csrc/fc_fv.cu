@@ -203,6 +203,7 @@ MeshView mesh_view(fc_ctx* ctx) {
   v.owner = m.owner.p; v.neighbour = m.neighbour.p; v.cf_ptr = m.cf_ptr.p; v.cf_face = m.cf_face.p;
   v.bpatch = m.bface_patch.p; v.bwall = m.bface_wall.p;
   v.srdw = m.srdw.p;
+  v.dnw = m.dnw.p;
   v.arx = m.arx.p; v.ary = m.ary.p; v.arz = m.arz.p; v.xf = m.xf.p; v.yf = m.yf.p; v.zf = m.zf.p;
   v.xc = m.xc.p; v.yc = m.yc.p; v.zc = m.zc.p; v.vol = m.vol.p; v.facint = m.facint.p; v.Df = m.Df.p;
   v.ijk = m.ijk.p; v.jik = m.jik.p;

@@ -22,6 +22,7 @@ struct MeshView {
   const int* __restrict__ bpatch;
   const int* __restrict__ bwall;
   const double* __restrict__ srdw;
+  const double* __restrict__ dnw;
   const double* __restrict__ arx;
   const double* __restrict__ ary;
   const double* __restrict__ arz;

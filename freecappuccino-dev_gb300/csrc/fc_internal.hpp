@@ -154,6 +154,7 @@ struct MeshDev {
   DVec<int> bface_wall;                    // running wall-face counter (iWall-1) or -1
   DVec<int> wall_face;                     // face index of every wall face, in wall-counter order
   DVec<double> srdw;                       // |S| / normal distance per wall face (nwal)
+  DVec<double> dnw;                        // normal distance of the owner's centre per wall face (nwal)
   DVec<int> cf_ptr, cf_face;               // cell -> faces (ascending face index)
   DVec<double> arx, ary, arz, xf, yf, zf;  // numFaces
   DVec<double> xc, yc, zc, vol;            // numCells

@@ -127,7 +127,7 @@ __global__ void k_wall_geom(int nwal, const int* __restrict__ wall_face, const i
                             const double* __restrict__ arz, const double* __restrict__ xf,
                             const double* __restrict__ yf, const double* __restrict__ zf,
                             const double* __restrict__ xc, const double* __restrict__ yc,
-                            const double* __restrict__ zc, double* srdw) {
+                            const double* __restrict__ zc, double* srdw, double* dnw_out) {
   for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nwal; w += gridDim.x * blockDim.x) {
     const int f = wall_face[w], p = owner[f];
     const double ax = arx[f], ay = ary[f], az = arz[f];
@@ -135,6 +135,7 @@ __global__ void k_wall_geom(int nwal, const int* __restrict__ wall_face, const i
     const double nxf = DD(ax, are), nyf = DD(ay, are), nzf = DD(az, are);
     const double dnw = DA(DA(DM(DS(xf[f], xc[p]), nxf), DM(DS(yf[f], yc[p]), nyf)), DM(DS(zf[f], zc[p]), nzf));
     srdw[w] = DD(are, dnw);
+    dnw_out[w] = dnw;
   }
 }
 
@@ -142,7 +143,7 @@ __global__ void k_wall_geom(int nwal, const int* __restrict__ wall_face, const i
 
 static void free_mesh_dev(MeshDev& m) {
   DVec<double>* dv[] = {&m.x, &m.y, &m.z, &m.arx, &m.ary, &m.arz, &m.xf, &m.yf, &m.zf,
-                        &m.xc, &m.yc, &m.zc, &m.vol, &m.facint, &m.Df, &m.srdw};
+                        &m.xc, &m.yc, &m.zc, &m.vol, &m.facint, &m.Df, &m.srdw, &m.dnw};
   for (auto* v : dv) v->release();
   DVec<int>* iv[] = {&m.nnodes, &m.nodes, &m.owner, &m.neighbour, &m.bface_patch, &m.bface_wall,
                      &m.cf_ptr, &m.cf_face, &m.ijk, &m.jik, &m.wall_face, &m.pface, &m.ptwin,
@@ -250,9 +251,11 @@ extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
                                                     m.yf.p, m.zf.p, m.xc.p, m.yc.p, m.zc.p, m.facint.p, m.Df.p);
   ctx->kernel_launches += 3;
   FC_CUDA_TRY(ctx, m.srdw.alloc(m.nwal));
+  FC_CUDA_TRY(ctx, m.dnw.alloc(m.nwal));
   if (m.nwal > 0) {
     k_wall_geom<<<grid(m.nwal), TB, 0, ctx->stream>>>(m.nwal, m.wall_face.p, m.owner.p, m.arx.p, m.ary.p, m.arz.p,
-                                                      m.xf.p, m.yf.p, m.zf.p, m.xc.p, m.yc.p, m.zc.p, m.srdw.p);
+                                                      m.xf.p, m.yf.p, m.zf.p, m.xc.p, m.yc.p, m.zc.p, m.srdw.p,
+                                                      m.dnw.p);
     ctx->kernel_launches++;
   }
   FC_CUDA_TRY(ctx, cudaGetLastError());
@@ -440,6 +443,7 @@ extern "C" int fc_get_geometry(fc_ctx* ctx, const char* name, double* out) {
   else if (n == "xc") v = &m.xc; else if (n == "yc") v = &m.yc; else if (n == "zc") v = &m.zc;
   else if (n == "vol") v = &m.vol; else if (n == "facint") v = &m.facint; else if (n == "Df") v = &m.Df;
   else if (n == "srdw") v = &m.srdw;
+  else if (n == "dnw") v = &m.dnw;
   else return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "unknown geometry array '" + n + "'");
   FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, out, v->p, v->bytes()));
   return FC_OK;

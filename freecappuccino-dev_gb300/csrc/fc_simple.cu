@@ -878,40 +878,95 @@ struct ScParams {
 };
 enum { SC_NONE = 0, SC_FLOW = 1, SC_ISOTHERMAL = 2, SC_ADIABATIC = 3 };
 
+// facefluxsc (inner face i), scalar_fluxes.f90:32-141, for a given diffusion
+// coefficient: the matrix coefficients and the explicit source suadd
+__device__ __forceinline__ void facefluxsc_inner(const MeshView& M, int i, int ijp, int ijn, double fm, double dcoef,
+                                                 double gam, int scheme, const double* fi, const Fld& g,
+                                                 double& cap, double& can, double& suadd) {
+  const double lambda = M.facint[i];
+  const double arx = M.arx[i], ary = M.ary[i], arz = M.arz[i];
+  const double fxn = lambda, fxp = 1.0 - lambda;
+  const double xpn = M.xc[ijn] - M.xc[ijp], ypn = M.yc[ijn] - M.yc[ijp], zpn = M.zc[ijn] - M.zc[ijp];
+  const double Df = M.Df[i];
+  const double de = dcoef * Df;
+  const double ce = fmin(fm, 0.0), cp = fmax(fm, 0.0);
+  can = -de + ce;
+  cap = -de - cp;
+  double dfixi = g.x(ijp) * fxp + g.x(ijn) * fxn;
+  double dfiyi = g.y(ijp) * fxp + g.y(ijn) * fxn;
+  double dfizi = g.z(ijp) * fxp + g.z(ijn) * fxn;
+  dfixi = dfixi * (arx - Df * xpn);
+  dfiyi = dfiyi * (ary - Df * ypn);
+  dfizi = dfizi * (arz - Df * zpn);
+  const double fdfie = dcoef * (dfixi + dfiyi + dfizi);
+  double fii;
+  if (fm >= 0.0) fii = face_value(M, ijp, ijn, M.xf[i], M.yf[i], M.zf[i], fxp, fi, g, scheme);
+  else fii = face_value(M, ijn, ijp, M.xf[i], M.yf[i], M.zf[i], fxn, fi, g, scheme);
+  double fcfie = fm * fii;
+  const double fcfii = ce * fi[ijn] + cp * fi[ijp];
+  fcfie = gam * (fcfie - fcfii);
+  suadd = -fcfie + fdfie;
+}
+
+// facefluxsc_boundary, scalar_fluxes.f90:256-337, face f of cell ijp: can
+// and suadd (cap is not used by the callers)
+__device__ __forceinline__ void facefluxsc_bnd(const MeshView& M, int f, int ijp, double fm, double dcoef,
+                                               const Fld& g, double& can, double& suadd) {
+  const double arx = M.arx[f], ary = M.ary[f], arz = M.arz[f];
+  const double xpn = M.xf[f] - M.xc[ijp], ypn = M.yf[f] - M.yc[ijp], zpn = M.zf[f] - M.zc[ijp];
+  const double Dfi = (arx * arx + ary * ary + arz * arz) / (xpn * arx + ypn * ary + zpn * arz);
+  const double de = dcoef * Dfi;
+  can = -de + fmin(fm, 0.0);
+  double dfixi = g.x(ijp), dfiyi = g.y(ijp), dfizi = g.z(ijp);
+  dfixi = dfixi * (arx - Dfi * xpn);
+  dfiyi = dfiyi * (ary - Dfi * ypn);
+  dfizi = dfizi * (arz - Dfi * zpn);
+  suadd = dcoef * (dfixi + dfiyi + dfizi);
+}
+
+// facefluxsc_periodic, scalar_fluxes.f90:147-251, pair q: central weights
+// 1/2, the distance vector 2 (xf - xc(ijp)), Df of the face's position in
+// its patch (as written there), cds face value
+__device__ __forceinline__ void facefluxsc_pair(const MeshView& M, int q, int ijp, int ijn, double fm, double dcoef,
+                                                double gam, const double* fi, const Fld& g, double& cap, double& can,
+                                                double& suadd) {
+  const int f = M.pface[q], i = M.ppos[q];
+  const double arx = M.arx[f], ary = M.ary[f], arz = M.arz[f];
+  const double fxn = 0.5, fxp = fxn;
+  const double xpn = 2 * (M.xf[f] - M.xc[ijp]), ypn = 2 * (M.yf[f] - M.yc[ijp]), zpn = 2 * (M.zf[f] - M.zc[ijp]);
+  const double Df = M.Df[i];
+  const double de = dcoef * Df;
+  const double ce = fmin(fm, 0.0), cp = fmax(fm, 0.0);
+  can = -de + ce;
+  cap = -de - cp;
+  double dfixi = g.x(ijp) * fxp + g.x(ijn) * fxn;
+  double dfiyi = g.y(ijp) * fxp + g.y(ijn) * fxn;
+  double dfizi = g.z(ijp) * fxp + g.z(ijn) * fxn;
+  dfixi = dfixi * (arx - Df * xpn);
+  dfiyi = dfiyi * (ary - Df * ypn);
+  dfizi = dfizi * (arz - Df * zpn);
+  const double fdfie = dcoef * (dfixi + dfiyi + dfizi);
+  const double fii = fm >= 0.0 ? fi[ijp] + (fi[ijn] - fi[ijp]) * fxp : fi[ijn] + (fi[ijp] - fi[ijn]) * fxn;
+  double fcfie = fm * fii;
+  const double fcfii = ce * fi[ijn] + cp * fi[ijp];
+  fcfie = gam * (fcfie - fcfii);
+  suadd = -fcfie + fdfie;
+}
+
 // facefluxsc (inner face), scalar_fluxes.f90:32-141, with the diffusion
 // coefficient of temperature.f90:122: a(k_ij)=can, a(k_ji)=cap, suadd to scratch
 __global__ void k_sc_face(MeshView M, Dev D, ScParams P) {
   const Fld g{D.gt, M.nT};
-  const double* fi = D.t;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M.nI; i += gridDim.x * blockDim.x) {
     const int ijp = M.owner[i], ijn = M.neighbour[i];
     const double lambda = M.facint[i];
     const double dcoef =
         P.viscos * P.prl + ((D.vis[ijp] + (D.vis[ijn] - D.vis[ijp]) * lambda) - P.viscos) * P.prtr;
-    const double arx = M.arx[i], ary = M.ary[i], arz = M.arz[i], fm = D.flmass[i];
-    const double fxn = lambda, fxp = 1.0 - lambda;
-    const double xpn = M.xc[ijn] - M.xc[ijp], ypn = M.yc[ijn] - M.yc[ijp], zpn = M.zc[ijn] - M.zc[ijp];
-    const double Df = M.Df[i];
-    const double de = dcoef * Df;
-    const double ce = fmin(fm, 0.0), cp = fmax(fm, 0.0);
-    const double can = -de + ce;
-    const double cap = -de - cp;
-    double dfixi = g.x(ijp) * fxp + g.x(ijn) * fxn;
-    double dfiyi = g.y(ijp) * fxp + g.y(ijn) * fxn;
-    double dfizi = g.z(ijp) * fxp + g.z(ijn) * fxn;
-    dfixi = dfixi * (arx - Df * xpn);
-    dfiyi = dfiyi * (ary - Df * ypn);
-    dfizi = dfizi * (arz - Df * zpn);
-    const double fdfie = dcoef * (dfixi + dfiyi + dfizi);
-    double fii;
-    if (fm >= 0.0) fii = face_value(M, ijp, ijn, M.xf[i], M.yf[i], M.zf[i], fxp, fi, g, P.scheme);
-    else fii = face_value(M, ijn, ijp, M.xf[i], M.yf[i], M.zf[i], fxn, fi, g, P.scheme);
-    double fcfie = fm * fii;
-    const double fcfii = ce * fi[ijn] + cp * fi[ijp];
-    fcfie = P.gam * (fcfie - fcfii);
+    double cap, can, suadd;
+    facefluxsc_inner(M, i, ijp, ijn, D.flmass[i], dcoef, P.gam, P.scheme, D.t, g, cap, can, suadd);
     D.a[M.ijk[i]] = can;
     D.a[M.jik[i]] = cap;
-    D.fscr[i] = -fcfie + fdfie;
+    D.fscr[i] = suadd;
   }
 }
 
@@ -922,34 +977,16 @@ __global__ void k_sc_face(MeshView M, Dev D, ScParams P) {
 // suadd to scratch entry nI + q
 __global__ void k_sc_pair(MeshView M, Dev D, ScParams P) {
   const Fld g{D.gt, M.nT};
-  const double* fi = D.t;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < M.nPer; q += gridDim.x * blockDim.x) {
     const int f = M.pface[q], ijp = M.owner[f], ijn = M.owner[M.ptwin[q]], i = M.ppos[q];
     const double dcoef =
         P.viscos * P.prl + ((D.vis[ijp] + (D.vis[ijn] - D.vis[ijp]) * M.facint[i]) - P.viscos) * P.prtr;
-    const double arx = M.arx[f], ary = M.ary[f], arz = M.arz[f], fm = D.flmass[f];
-    const double fxn = 0.5, fxp = fxn;
-    const double xpn = 2 * (M.xf[f] - M.xc[ijp]), ypn = 2 * (M.yf[f] - M.yc[ijp]), zpn = 2 * (M.zf[f] - M.zc[ijp]);
-    const double Df = M.Df[i];
-    const double de = dcoef * Df;
-    const double ce = fmin(fm, 0.0), cp = fmax(fm, 0.0);
-    const double can = -de + ce;
-    const double cap = -de - cp;
-    double dfixi = g.x(ijp) * fxp + g.x(ijn) * fxn;
-    double dfiyi = g.y(ijp) * fxp + g.y(ijn) * fxn;
-    double dfizi = g.z(ijp) * fxp + g.z(ijn) * fxn;
-    dfixi = dfixi * (arx - Df * xpn);
-    dfiyi = dfiyi * (ary - Df * ypn);
-    dfizi = dfizi * (arz - Df * zpn);
-    const double fdfie = dcoef * (dfixi + dfiyi + dfizi);
-    const double fii = fm >= 0.0 ? fi[ijp] + (fi[ijn] - fi[ijp]) * fxp : fi[ijn] + (fi[ijp] - fi[ijn]) * fxn;
-    double fcfie = fm * fii;
-    const double fcfii = ce * fi[ijn] + cp * fi[ijp];
-    fcfie = P.gam * (fcfie - fcfii);
+    double cap, can, suadd;
+    facefluxsc_pair(M, q, ijp, ijn, D.flmass[f], dcoef, P.gam, D.t, g, cap, can, suadd);
     const int l = M.nI + q;
     D.a[M.ijk[l]] = can;
     D.a[M.jik[l]] = cap;
-    D.fscr[l] = -fcfie + fdfie;
+    D.fscr[l] = suadd;
   }
 }
 
@@ -983,16 +1020,8 @@ __global__ void k_sc_cell(MeshView M, Dev D, ScParams P) {
       const int kind = P.pkind[b];
       if (kind == SC_FLOW) {
         const double dcoef = P.viscos * P.prl + (D.vis[ijp] - P.viscos) / P.sigt;
-        const double arx = M.arx[f], ary = M.ary[f], arz = M.arz[f], fm = D.flmass[f];
-        const double xpn = M.xf[f] - M.xc[ijp], ypn = M.yf[f] - M.yc[ijp], zpn = M.zf[f] - M.zc[ijp];
-        const double Dfi = (arx * arx + ary * ary + arz * arz) / (xpn * arx + ypn * ary + zpn * arz);
-        const double de = dcoef * Dfi;
-        const double can = -de + fmin(fm, 0.0);
-        double dfixi = g.x(ijp), dfiyi = g.y(ijp), dfizi = g.z(ijp);
-        dfixi = dfixi * (arx - Dfi * xpn);
-        dfiyi = dfiyi * (ary - Dfi * ypn);
-        dfizi = dfizi * (arz - Dfi * zpn);
-        const double suadd = dcoef * (dfixi + dfiyi + dfizi);
+        double can, suadd;
+        facefluxsc_bnd(M, f, ijp, D.flmass[f], dcoef, g, can, suadd);
         sp = sp - can;
         su = su - can * D.t[ijb] + suadd;
       } else if (kind == SC_ISOTHERMAL) {
@@ -1065,6 +1094,275 @@ __global__ void k_clip_small(int n, double* __restrict__ phi, const double* __re
     phi[i] = fmax(phi[i], SMALL);
 }
 
+
+// ---------------------------------------------------------------- k-omega SST
+// k_omega_SST.f90:21-38 and parameters.f90:15-17
+#define SST_BETTAST 0.09
+#define SST_SIGMK1 0.85
+#define SST_SIGMK2 1.0
+#define SST_SIGMOM1 0.5
+#define SST_SIGMOM2 0.856
+#define SST_BETAI1 0.075
+#define SST_BETAI2 0.0828
+#define SST_A1 0.31
+#define SST_ALPHA2 0.44
+#define SST_CAPPA 0.41
+#define SST_ELOG 8.432
+
+struct Turb {  // the model's device fields and constants of one call
+  double *te, *ed, *fsst, *gte, *ged, *gen, *mag, *wd, *tau, *ypl;
+  double viscos, densit, cmu25, alpha1;
+};
+
+// calc_strain_and_vorticity.f90:1-60: the strain magnitude sqrt(2 Sij Sij)
+__global__ void k_sst_strain(int nC, int nT, const double* __restrict__ gu, const double* __restrict__ gv,
+                             const double* __restrict__ gw, double* __restrict__ mag) {
+  const Fld u{gu, nT}, v{gv, nT}, w{gw, nT};
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nC; c += gridDim.x * blockDim.x) {
+    const double s11 = u.x(c), s12 = 0.5 * (u.y(c) + v.x(c)), s13 = 0.5 * (u.z(c) + w.x(c));
+    const double s22 = v.y(c), s23 = 0.5 * (v.z(c) + w.y(c)), s33 = w.z(c);
+    mag[c] = sqrt(2 * (s11 * s11 + s22 * s22 + s33 * s33 + 2 * (s12 * s12 + s13 * s13 + s23 * s23)));
+  }
+}
+
+// k sources, k_omega_SST.f90:159-219: the production and its limiter, the
+// production to su, the destruction beta* omega rho vol to sp
+__global__ void k_sst_src_k(MeshView M, Dev D, Turb T) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
+    double gen = fabs(D.vis[c] - T.viscos) * T.mag[c] * T.mag[c];
+    gen = fmin(gen, 0.9 * D.den[c] * T.te[c] * T.ed[c]);
+    T.gen[c] = gen;
+    const double genp = fmax(gen, 0.0), genn = fmin(gen, 0.0);
+    D.su[c] = genp * M.vol[c];
+    double sp = SST_BETTAST * T.ed[c] * D.den[c] * M.vol[c];
+    D.sp[c] = sp - genn * M.vol[c] / (T.te[c] + SMALL);
+  }
+}
+
+// omega sources, k_omega_SST.f90:300-398: the blending function F1 (fsst),
+// production alpha gen / nu_t, cross diffusion, destruction beta rho omega^2
+__global__ void k_sst_src_w(MeshView M, Dev D, Turb T) {
+  const Fld gk{T.gte, M.nT}, gw{T.ged, M.nT};
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
+    const double wldist = T.wd[c], den = D.den[c], te = T.te[c], ed = T.ed[c];
+    const double dot = gk.x(c) * gw.x(c) + gk.y(c) * gw.y(c) + gk.z(c) * gw.z(c);
+    const double domegapl = fmax(2 * SST_SIGMOM2 * den / (ed) * dot, SMALL);
+    const double ksi = fmin(fmax(sqrt(te) / (SST_BETTAST * wldist * ed + SMALL),
+                                 500.0 * T.viscos / den / (wldist * wldist * ed + SMALL)),
+                            4.0 * den * te * SST_SIGMOM2 / (domegapl * (wldist * wldist)));
+    const double ksi2 = ksi * ksi;
+    const double f1 = tanh(ksi2 * ksi2);
+    T.fsst[c] = f1;
+    const double genp = fmax(T.gen[c], 0.0), genn = fmin(T.gen[c], 0.0);
+    const double vist = (D.vis[c] - T.viscos) / T.densit;
+    const double alphasst = f1 * T.alpha1 + (1.0 - f1) * SST_ALPHA2;
+    double su = alphasst * genp * M.vol[c] / (vist + SMALL);
+    double domega = 2 * (1.0 - f1) * den * SST_SIGMOM2 / (ed + SMALL) * dot;
+    domega = fmax(domega, 0.0);
+    D.su[c] = su + domega * M.vol[c];
+    const double bettasst = f1 * SST_BETAI1 + (1.0 - f1) * SST_BETAI2;
+    const double sp = bettasst * den * ed * M.vol[c];
+    D.sp[c] = sp - alphasst * genn * M.vol[c] / (vist * ed + SMALL);
+  }
+}
+
+// the blended diffusion coefficient of cell c: sigma1 F1 + sigma2 (1 - F1)
+__device__ __forceinline__ double sst_prtr(const Turb& T, int c, int ifi) {
+  return ifi == 1 ? T.fsst[c] * SST_SIGMK1 + (1.0 - T.fsst[c]) * SST_SIGMK2
+                  : T.fsst[c] * SST_SIGMOM1 + (1.0 - T.fsst[c]) * SST_SIGMOM2;
+}
+
+// inner faces of calcsc, k_omega_SST.f90:448-488: the owner's blended sigma
+__global__ void k_sst_face(MeshView M, Dev D, Turb T, int ifi, double gam, int scheme) {
+  const double* fi = ifi == 1 ? T.te : T.ed;
+  const Fld g{ifi == 1 ? T.gte : T.ged, M.nT};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M.nI; i += gridDim.x * blockDim.x) {
+    const int ijp = M.owner[i], ijn = M.neighbour[i];
+    const double prtr = sst_prtr(T, ijp, ifi);
+    const double viste = (D.vis[ijp] + (D.vis[ijn] - D.vis[ijp]) * M.facint[i]) - T.viscos;
+    const double dcoef = T.viscos + viste * prtr;
+    double cap, can, suadd;
+    facefluxsc_inner(M, i, ijp, ijn, D.flmass[i], dcoef, gam, scheme, fi, g, cap, can, suadd);
+    D.a[M.ijk[i]] = can;
+    D.a[M.jik[i]] = cap;
+    D.fscr[i] = suadd;
+  }
+}
+
+// periodic pairs of calcsc, k_omega_SST.f90:521-560: the pair's mean sigma
+// and mean viscosity
+__global__ void k_sst_pair(MeshView M, Dev D, Turb T, int ifi, double gam) {
+  const double* fi = ifi == 1 ? T.te : T.ed;
+  const Fld g{ifi == 1 ? T.gte : T.ged, M.nT};
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < M.nPer; q += gridDim.x * blockDim.x) {
+    const int f = M.pface[q], ijp = M.owner[f], ijn = M.owner[M.ptwin[q]];
+    const double prtr = 0.5 * (sst_prtr(T, ijp, ifi) + sst_prtr(T, ijn, ifi));
+    const double viste = 0.5 * (D.vis[ijp] + D.vis[ijn]) - T.viscos;
+    const double dcoef = T.viscos + viste * prtr;
+    double cap, can, suadd;
+    facefluxsc_pair(M, q, ijp, ijn, D.flmass[f], dcoef, gam, fi, g, cap, can, suadd);
+    const int l = M.nI + q;
+    D.a[M.ijk[l]] = can;
+    D.a[M.jik[l]] = cap;
+    D.fscr[l] = suadd;
+  }
+}
+
+// per cell, in the reference's order: the face sources, then the boundary
+// conditions of k_omega_SST.f90:495-660 patch by patch (flow patches through
+// facefluxsc_boundary; walls: the wall-function production of k, omega fixed
+// in the wall cell with its matrix row cleared), then the main diagonal and
+// the under-relaxation (:712-726)
+__global__ void k_sst_cell(MeshView M, Dev D, Turb T, int ifi, double urf) {
+  double* fi = ifi == 1 ? T.te : T.ed;
+  const Fld g{ifi == 1 ? T.gte : T.ged, M.nT};
+  const double urfrs = 1.0 / urf, urfms = 1.0 - urf;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
+    double su = D.su[c], sp = D.sp[c];
+    int cleared_at = -1;  // list position of the last wall face that cleared the row
+    for (int q = M.af_ptr[c]; q < M.af_ptr[c + 1]; ++q) {
+      const int f = M.af_ent[q];
+      if (f < M.nI) {
+        if (M.owner[f] == c) su = su + D.fscr[f];
+        else su = su - D.fscr[f];
+        continue;
+      }
+      if (f >= M.nF) {  // the twin side of pair f - nF
+        su = su - D.fscr[M.nI + (f - M.nF)];
+        continue;
+      }
+      const int bi = f - M.nI, ijb = M.nC + bi;
+      const int t = D.ptype[M.bpatch[bi]];
+      if (t == FC_BC_PERIODIC) {
+        su = su + D.fscr[M.nI + M.bpair[bi]];
+      } else if (t == FC_BC_INLET || t == FC_BC_OUTLET || t == FC_BC_PRESSURE) {
+        const double viste = D.vis[ijb] - T.viscos;
+        const double dcoef = T.viscos + viste * sst_prtr(T, c, ifi);
+        double can, suadd;
+        facefluxsc_bnd(M, f, c, D.flmass[f], dcoef, g, can, suadd);
+        sp = sp - can;
+        su = su - can * fi[ijb] + suadd;
+      } else if (t == FC_BC_WALL) {
+        const int iw = M.bwall[bi];
+        const double dnw = M.dnw[iw];
+        if (ifi == 1) {
+          su = su - T.gen[c] * M.vol[c];
+          const double viss = fmax(T.viscos, D.visw[iw]);
+          const double arx = M.arx[f], ary = M.ary[f], arz = M.arz[f];
+          const double are = sqrt(arx * arx + ary * ary + arz * arz);
+          const double nxf = arx / are, nyf = ary / are, nzf = arz / are;
+          const double Vnp = D.u[c] * nxf + D.v[c] * nyf + D.w[c] * nzf;
+          double xtp = D.u[c] - Vnp * nxf, ytp = D.v[c] - Vnp * nyf, ztp = D.w[c] - Vnp * nzf;
+          const double Vtp = sqrt(xtp * xtp + ytp * ytp + ztp * ztp);
+          xtp = xtp / Vtp;
+          ytp = ytp / Vtp;
+          ztp = ztp / Vtp;
+          const double Ut2 = fabs((D.u[ijb] - D.u[c]) * xtp + (D.v[ijb] - D.v[c]) * ytp + (D.w[ijb] - D.w[c]) * ztp);
+          const double tau = viss * Ut2 / dnw;
+          T.tau[iw] = tau;
+          const double gen = fabs(tau) * T.cmu25 * sqrt(T.te[c]) / (dnw * SST_CAPPA);
+          T.gen[c] = gen;
+          su = su + gen * M.vol[c];
+        } else {
+          const double wlog = sqrt(T.te[c]) / (T.cmu25 * SST_CAPPA * dnw);
+          const double wvis = 6.0 * (T.viscos / D.den[c]) / (SST_BETAI1 * (dnw * dnw));
+          const double ed = sqrt(wvis * wvis + wlog * wlog);
+          T.ed[c] = ed;
+          su = ed;
+          sp = 1.0;
+          cleared_at = q;
+        }
+      }
+    }
+    const int kd = M.diag[c], k0 = M.ia[c], k1 = M.ia[c + 1];
+    if (cleared_at >= 0) {
+      // the row is cleared where the wall face comes; periodic pairs of
+      // later patches write their slots of this row afterwards, as there
+      int kslot[4];
+      double kval[4];
+      int nk = 0;
+      for (int q = cleared_at + 1; q < M.af_ptr[c + 1] && nk < 4; ++q) {
+        const int f = M.af_ent[q];
+        int slot = -1;
+        if (f >= M.nF) slot = M.jik[M.nI + (f - M.nF)];
+        else if (f >= M.nI && D.ptype[M.bpatch[f - M.nI]] == FC_BC_PERIODIC) slot = M.ijk[M.nI + M.bpair[f - M.nI]];
+        if (slot >= 0) { kslot[nk] = slot; kval[nk] = D.a[slot]; ++nk; }
+      }
+      for (int k = k0; k < k1; ++k) D.a[k] = 0.0;
+      for (int j = 0; j < nk; ++j) D.a[kslot[j]] = kval[j];
+    }
+    double ad = sp;
+    for (int k = k0; k < k1; ++k)
+      if (k != kd) ad = ad - D.a[k];
+    ad = ad * urfrs;
+    D.a[kd] = ad;
+    D.su[c] = su + urfms * ad * fi[c];
+    D.sp[c] = sp;
+  }
+}
+
+// modify_mu_eff, k_omega_SST.f90:800-830: the eddy viscosity with the F2
+// limiter, under-relaxed
+__global__ void k_sst_mu(MeshView M, Dev D, Turb T, double urf) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < M.nC; c += gridDim.x * blockDim.x) {
+    const double visold = D.vis[c], wldist = T.wd[c], te = T.te[c], ed = T.ed[c], den = D.den[c];
+    const double etha = fmax(2 * sqrt(te) / (SST_BETTAST * wldist * ed), (500 * T.viscos / den) / (wldist * wldist * ed));
+    const double f2 = tanh(etha * etha);
+    double vis = T.viscos + den * SST_A1 * te / (fmax(SST_A1 * ed, T.mag[c] * f2));
+    D.vis[c] = urf * vis + (1.0 - urf) * visold;
+  }
+}
+
+// the wall faces of modify_mu_eff, k_omega_SST.f90:836-955: y+, the wall
+// shear stress and the wall viscosity from the blended wall law
+__global__ void k_sst_mu_wall(MeshView M, Dev D, Turb T, int nwal, const int* __restrict__ wall_face) {
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nwal; w += gridDim.x * blockDim.x) {
+    const int f = wall_face[w], c = M.owner[f], ijb = M.nC + (f - M.nI);
+    const double dnw = M.dnw[w], den = D.den[c];
+    const double arx = M.arx[f], ary = M.ary[f], arz = M.arz[f];
+    const double are = sqrt(arx * arx + ary * ary + arz * arz);
+    const double nxf = arx / are, nyf = ary / are, nzf = arz / are;
+    const double Vnp = D.u[c] * nxf + D.v[c] * nyf + D.w[c] * nzf;
+    const double xtp = D.u[c] - Vnp * nxf, ytp = D.v[c] - Vnp * nyf, ztp = D.w[c] - Vnp * nzf;
+    const double Vtp = sqrt(xtp * xtp + ytp * ytp + ztp * ztp);
+    const double Utau = sqrt(T.viscos * Vtp / (T.densit * dnw) + T.cmu25 * T.te[c]);
+    const double ypl = den * Utau * dnw / T.viscos;
+    T.ypl[w] = ypl;
+    const double Utauvis = ypl;
+    const double Utaulog = 1.0 / SST_CAPPA * log(SST_ELOG * ypl);
+    const double uv2 = Utauvis * Utauvis, ul2 = Utaulog * Utaulog;
+    const double Upl = sqrt(sqrt(uv2 * uv2 + ul2 * ul2));
+    const double viscw = den * Utau * dnw / Upl;
+    const double r = Vtp / Upl;
+    T.tau[w] = den * (r * r);
+    const double visw = fmax(T.viscos, viscw);
+    D.visw[w] = visw;
+    D.vis[ijb] = visw;
+  }
+}
+
+// wall_distance.f90: non-wall boundary values of phi from the owners, then
+// (after the Gauss gradient) d = -|grad phi| + sqrt(|grad phi|^2 + 2 phi)
+__global__ void k_wd_bnd(MeshView M, const int* __restrict__ ptype, double* __restrict__ phi) {
+  for (int bi = blockIdx.x * blockDim.x + threadIdx.x; bi < M.nB; bi += gridDim.x * blockDim.x)
+    if (ptype[M.bpatch[bi]] != FC_BC_WALL) phi[M.nC + bi] = phi[M.owner[M.nI + bi]];
+}
+__global__ void k_wd_dist(int nC, int nT, const double* __restrict__ phi, const double* __restrict__ gphi,
+                          double* __restrict__ wd) {
+  const Fld g{gphi, nT};
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nC; c += gridDim.x * blockDim.x) {
+    const double gx = g.x(c), gy = g.y(c), gz = g.z(c);
+    wd[c] = -sqrt(gx * gx + gy * gy + gz * gz) + sqrt(gx * gx + gy * gy + gz * gz + 2 * phi[c]);
+  }
+}
+__global__ void k_wd_init(int nC, int nT, const double* __restrict__ vol, double* __restrict__ q,
+                          double* __restrict__ mu, double* __restrict__ phi) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nT; i += gridDim.x * blockDim.x) {
+    if (i < nC) { q[i] = -vol[i]; mu[i] = 1.0; }
+    phi[i] = 0.0;
+  }
+}
+
 }  // namespace
 
 // ====================================================================== host
@@ -1086,6 +1384,9 @@ struct SimpleState {
   // transient momentum and PISO (fc_transient_set_params)
   fc_transient_params trp = {1.0, FC_TIME_STEADY, 0, 1};
   DVec<double> h, ppart;  // calcp_piso: h = a, pavg partials
+  // k-omega SST (fc_turbulence_set_params)
+  fc_turbulence_params kprm;
+  bool have_kprm = false;
   // batched U, V, W solves (fc_simple_set_batched_momentum)
   int batch_mom = 0;
   struct MomBatch* mb = nullptr;
@@ -1738,5 +2039,136 @@ extern "C" int fc_calculate_temperature(fc_ctx* ctx, int solve, double* resor7) 
   }
   S.resor[7] = r7;
   if (resor7) *resor7 = r7;
+  return FC_OK;
+}
+
+// ------------------------------------------------------------ k-omega SST
+static bool turb_scalar_ok(const fc_turb_scalar& t) {
+  return t.urf > 0 && t.maxiter >= 0 && t.tolRel >= 0 && t.tolAbs >= 0;
+}
+
+extern "C" int fc_turbulence_set_params(fc_ctx* ctx, const fc_turbulence_params* prm) {
+  if (!ctx || !prm) return FC_ERR_BAD_INPUT;
+  if (!turb_scalar_ok(prm->k) || !turb_scalar_ok(prm->omega) || !(prm->urfVis > 0))
+    return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_turbulence_set_params: urf > 0, maxiter >= 0 and tolerances >= 0");
+  if (prm->gradScheme < FC_GRAD_GAUSS || prm->gradScheme > FC_GRAD_LSQ_DM_EXACT)
+    return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_turbulence_set_params: unknown gradient scheme");
+  SimpleState& S = sstate(ctx);
+  S.kprm = *prm;
+  S.kprm.k.lSolver[sizeof(S.kprm.k.lSolver) - 1] = 0;
+  S.kprm.omega.lSolver[sizeof(S.kprm.omega.lSolver) - 1] = 0;
+  S.have_kprm = true;
+  return FC_OK;
+}
+
+// wall_distance_poisson, wall_distance.f90:29-118
+extern "C" int fc_wall_distance(fc_ctx* ctx) {
+  FC_RANGE();
+  if (!ctx) return FC_ERR_BAD_INPUT;
+  if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
+  Dev D;
+  int st = make_dev(ctx, D, true);
+  if (st) return st;
+  MeshView M = mesh_view(ctx);
+  FieldStore& F = ctx_fields(ctx);
+  DVec<double> q, mu, phi, gphi;
+  FC_CUDA_TRY(ctx, q.alloc(M.nC));
+  FC_CUDA_TRY(ctx, mu.alloc(M.nC));
+  FC_CUDA_TRY(ctx, phi.alloc(M.nT));
+  FC_CUDA_TRY(ctx, gphi.alloc(3 * (size_t)M.nT));
+  k_wd_init<<<gridn(M.nT), 256, 0, ctx->stream>>>(M.nC, M.nT, M.vol, q.p, mu.p, phi.p);
+  ctx->kernel_launches++;
+  if ((st = fc_laplacian(ctx, mu.p, phi.p, ~0ULL))) return st;
+  double r = 0.0;
+  st = solve_into(ctx, "iccg", phi.p, q.p, &r, 500, (double)1e-12f, (double)1e-10f, "Wdis");
+  if (st < 0) return st;
+  if (M.nB) {
+    k_wd_bnd<<<gridn(M.nB), 256, 0, ctx->stream>>>(M, D.ptype, phi.p);
+    ctx->kernel_launches++;
+  }
+  if ((st = fv_grad_gauss(ctx, phi.p, gphi.p))) return st;
+  k_wd_dist<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, M.nT, phi.p, gphi.p, F.wd.p);
+  ctx->kernel_launches++;
+  FC_CUDA_TRY(ctx, cudaGetLastError());
+  FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // the temporaries go out of scope
+  return FC_OK;
+}
+
+// calcsc, k_omega_SST.f90:91-785, for ifi = 1 (k) or 2 (omega)
+static int sst_calcsc(fc_ctx* ctx, const Dev& D, const Turb& T, int ifi, double* resor) {
+  SimpleState& S = sstate(ctx);
+  const fc_turb_scalar& P = ifi == 1 ? S.kprm.k : S.kprm.omega;
+  MeshView M = mesh_view(ctx);
+  CsrSystem* sys = ctx->sys_mesh;
+  double* fi = ifi == 1 ? T.te : T.ed;
+  int st = fv_grad(ctx, S.kprm.gradScheme, fi, ifi == 1 ? T.gte : T.ged);
+  if (st) return st;
+  FC_CUDA_TRY(ctx, cudaMemsetAsync(D.a, 0, (size_t)sys->nnz * sizeof(double), ctx->stream));
+  if (ifi == 1) k_sst_src_k<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D, T);
+  else k_sst_src_w<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D, T);
+  if (M.nI) k_sst_face<<<gridn(M.nI), 256, 0, ctx->stream>>>(M, D, T, ifi, P.gds, P.cScheme);
+  if (M.nPer) k_sst_pair<<<gridn(M.nPer), 256, 0, ctx->stream>>>(M, D, T, ifi, P.gds);
+  k_sst_cell<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D, T, ifi, P.urf);
+  ctx->kernel_launches += 2 + (M.nI > 0) + (M.nPer > 0);
+  FC_CUDA_TRY(ctx, cudaGetLastError());
+  st = solve_into(ctx, P.lSolver, fi, D.su, resor, P.maxiter, P.tolAbs, P.tolRel, ifi == 1 ? "k" : "Omega");
+  if (st < 0) return st;
+  if (M.nB) {
+    k_update_boundary<<<gridn(M.nB), 256, 0, ctx->stream>>>(M, D.ptype, fi);
+    ctx->kernel_launches++;
+  }
+  // the clip to small when min(fi) < 0, over all numTotal values (:771-782)
+  const int nbk = std::min(ctx->num_sms > 0 ? 2 * ctx->num_sms : 256, gridn(M.nT));
+  FC_CUDA_TRY(ctx, S.tpart.alloc((size_t)2 * nbk));
+  k_minmax<<<nbk, 256, 0, ctx->stream>>>(M.nT, fi, S.tpart.p);
+  k_clip_small<<<gridn(M.nT), 256, 0, ctx->stream>>>(M.nT, fi, S.tpart.p, nbk);
+  ctx->kernel_launches += 2;
+  FC_CUDA_TRY(ctx, cudaGetLastError());
+  return FC_OK;
+}
+
+// modify_viscosity_turbulence.f90:25-45 with the k-omega SST model
+extern "C" int fc_kw_sst(fc_ctx* ctx, double* resor56) {
+  FC_RANGE();
+  if (!ctx) return FC_ERR_BAD_INPUT;
+  if (!ctx->has_mesh) return fc_fail_msg(ctx, FC_ERR_STATE, "no mesh");
+  SimpleState& S = sstate(ctx);
+  if (!S.have_prm) return fc_fail_msg(ctx, FC_ERR_STATE, "fc_simple_set_params not called");
+  if (!S.have_kprm) return fc_fail_msg(ctx, FC_ERR_STATE, "fc_turbulence_set_params not called");
+  Dev D;
+  int st = make_dev(ctx, D, true);
+  if (st) return st;
+  MeshView M = mesh_view(ctx);
+  FieldStore& F = ctx_fields(ctx);
+  Turb T;
+  T.te = F.te.p; T.ed = F.ed.p; T.fsst = F.fsst.p; T.gte = F.gte.p; T.ged = F.ged.p;
+  T.gen = F.gen.p; T.mag = F.mag.p; T.wd = F.wd.p; T.tau = F.tau.p; T.ypl = F.ypl.p;
+  T.viscos = S.prm.viscos;
+  T.densit = S.prm.densit;
+  T.cmu25 = std::sqrt(std::sqrt(0.09));
+  T.alpha1 = 5. / 9.0;
+  if ((st = fv_grad_gauss(ctx, D.u, D.gu))) return st;
+  if ((st = fv_grad_gauss(ctx, D.v, D.gv))) return st;
+  if ((st = fv_grad_gauss(ctx, D.w, D.gw))) return st;
+  k_sst_strain<<<gridn(M.nC), 256, 0, ctx->stream>>>(M.nC, M.nT, D.gu, D.gv, D.gw, T.mag);
+  ctx->kernel_launches++;
+  double r5 = 0.0, r6 = 0.0;
+  if ((st = sst_calcsc(ctx, D, T, 1, &r5))) return st;
+  if ((st = sst_calcsc(ctx, D, T, 2, &r6))) return st;
+  k_sst_mu<<<gridn(M.nC), 256, 0, ctx->stream>>>(M, D, T, S.kprm.urfVis);
+  ctx->kernel_launches++;
+  if (M.nB) {
+    k_update_boundary<<<gridn(M.nB), 256, 0, ctx->stream>>>(M, D.ptype, D.vis);
+    ctx->kernel_launches++;
+  }
+  const MeshDev& m = ctx->mesh;
+  if (m.nwal > 0) {
+    k_sst_mu_wall<<<gridn(m.nwal), 256, 0, ctx->stream>>>(M, D, T, m.nwal, m.wall_face.p);
+    ctx->kernel_launches++;
+  }
+  FC_CUDA_TRY(ctx, cudaGetLastError());
+  S.resor[5] = r5;
+  S.resor[6] = r6;
+  if (resor56) { resor56[0] = r5; resor56[1] = r6; }
   return FC_OK;
 }

@@ -126,6 +126,9 @@ def lib():
         "fc_calcp_simple": (i, [vp, vp]),
         "fc_simple_iteration": (i, [vp, vp]),
         "fc_temperature_set_params": (i, [vp, vp, vp]),
+        "fc_turbulence_set_params": (i, [vp, vp]),
+        "fc_wall_distance": (i, [vp]),
+        "fc_kw_sst": (i, [vp, vp]),
         "fc_calculate_temperature": (i, [vp, i, vp]),
         "fc_cd_assemble": (i, [vp, vp, vp]),
         "fc_cd_solve": (i, [vp, vp, i, d, C.POINTER(SolveInfo)]),
@@ -278,6 +281,37 @@ class TemperatureParams(C.Structure):
         p.maxiterT = kw.get("maxiterT", 10)
         p.tolAbsT, p.tolRelT = kw.get("tolAbsT", 1e-13), kw.get("tolRelT", 0.02)
         p.lSolverT = kw.get("solver", "bicgstab").encode()
+        return p
+
+
+class TurbScalar(C.Structure):
+    """fc_turb_scalar: settings of one turbulence scalar (TurbModelData.f90)."""
+    _fields_ = [("urf", C.c_double), ("gds", C.c_double), ("cScheme", C.c_int), ("lSolver", C.c_char * 16),
+                ("maxiter", C.c_int), ("tolAbs", C.c_double), ("tolRel", C.c_double)]
+
+    @classmethod
+    def defaults(cls, **kw):
+        """TurbModelData.f90's defaults: urf 0.7, gds 1, linearUpwind,
+        BiCGStab, maxiter 10, tolAbs 1e-10 (a default-real literal), tolRel 0.01."""
+        t = cls()
+        t.urf, t.gds = kw.get("urf", 0.7), kw.get("gds", 1.0)
+        t.cScheme = kw.get("scheme", 2)
+        t.lSolver = kw.get("solver", "bicgstab").encode()
+        t.maxiter = kw.get("maxiter", 10)
+        t.tolAbs, t.tolRel = kw.get("tolAbs", float(np.float32(1e-10))), kw.get("tolRel", 0.01)
+        return t
+
+
+class TurbulenceParams(C.Structure):
+    """fc_turbulence_params: the k-omega SST model's settings."""
+    _fields_ = [("k", TurbScalar), ("omega", TurbScalar), ("urfVis", C.c_double), ("gradScheme", C.c_int)]
+
+    @classmethod
+    def defaults(cls, k=None, omega=None, urfVis=1.0, grad=0):
+        p = cls()
+        p.k = k or TurbScalar.defaults()
+        p.omega = omega or TurbScalar.defaults()
+        p.urfVis, p.gradScheme = urfVis, grad
         return p
 
 
@@ -550,15 +584,19 @@ class Context:
     def field_len(self, name):
         m = self.mesh
         if name in ("u", "v", "w", "p", "pp", "vis", "den", "t", "uo", "vo", "wo", "uoo", "voo", "woo", "uooo",
-                    "vooo", "wooo"):
+                    "vooo", "wooo", "te", "ed", "fsst"):
             return m.numTotal
+        if name in ("gen", "magStrain", "walldist"):
+            return m.numCells
+        if name in ("tau", "ypl"):
+            return self._nwal()
         if name in ("rU", "rV", "rW"):
             return m.numCells
         if name == "flmass":
             return m.numFaces
         if name in ("su", "sv", "sw", "spu", "spv", "sp", "apu", "apv", "apw"):
             return m.numCells
-        if name in ("dUdxi", "dVdxi", "dWdxi", "dPdxi", "dTdxi"):
+        if name in ("dUdxi", "dVdxi", "dWdxi", "dPdxi", "dTdxi", "dTEdxi", "dEDdxi"):
             return 3 * m.numTotal
         if name == "a":  # nnz: 2 (numInnerFaces + numPeriodic) + numCells
             n, nnz = C.c_int(0), C.c_int(0)
@@ -753,6 +791,21 @@ class Context:
         fr = None if bc_dfraction is None else _f64(bc_dfraction)
         self._check(self.L.fc_temperature_set_params(self.h, C.byref(prm), _ptr(fr) if fr is not None else None),
                     "fc_temperature_set_params")
+
+    def turbulence_params(self, prm):
+        """prm: TurbulenceParams of the k-omega SST model."""
+        self._kprm = prm
+        self._check(self.L.fc_turbulence_set_params(self.h, C.byref(prm)), "fc_turbulence_set_params")
+
+    def wall_distance(self):
+        """wall_distance_poisson into the field "walldist"."""
+        self._check(self.L.fc_wall_distance(self.h), "fc_wall_distance")
+
+    def kw_sst(self):
+        """One modify_viscosity_turbulence with the k-omega SST model; returns resor(5:6)."""
+        r = np.zeros(2)
+        self._check(self.L.fc_kw_sst(self.h, _ptr(r)), "fc_kw_sst")
+        return r
 
     def calculate_temperature(self, solve=True):
         """One calculate_temperature; returns resor(7)."""

@@ -523,6 +523,48 @@ int fc_temperature_set_params(fc_ctx* ctx, const fc_temperature_params* prm, con
  * setup (srdw covers 'wall' patches only) and is not accepted. */
 int fc_calculate_temperature(fc_ctx* ctx, int solve, double* resor7);
 
+/* ---- Turbulence: the k-omega SST model (TurbulenceModels/k_omega_SST.f90),
+ * high-Re form (LowRe = .false.), steady, without buoyancy.  The settings of
+ * one transported scalar (TurbModelData.f90 TurbScalar): */
+typedef struct {
+  double urf, gds;       /* under-relaxation, deferred-correction factor */
+  int cScheme;           /* interpolation scheme id, as cSchemeU */
+  char lSolver[16];      /* csrsolve solver name */
+  int maxiter;
+  double tolAbs, tolRel;
+} fc_turb_scalar;
+typedef struct {
+  fc_turb_scalar k, omega;  /* TurbModel%Scalar(1) and (2) */
+  double urfVis;            /* TurbModel%urfVis, eddy-viscosity under-relaxation */
+  int gradScheme;           /* FC_GRAD_* of grad(k) and grad(omega), the case's gradient scheme */
+} fc_turbulence_params;
+/* Defaults of TurbModelData.f90: urf 0.7, gds 1, linearUpwind, bicgstab,
+ * maxiter 10, tolAbs 1e-10 (a default-real literal), tolRel 0.01; urfVis 1;
+ * Gauss gradients.  viscos and densit come from fc_simple_set_params. */
+int fc_turbulence_set_params(fc_ctx* ctx, const fc_turbulence_params* prm);
+/* wall_distance_poisson (mesh/wall_distance.f90:29-118): the field
+ * "walldist" (numCells) from lap(phi) = -1 solved by ICCG with the
+ * reference's laplacian (phi = 0 on every patch; 500 iterations, tolAbs
+ * 1e-12, tolRel 1e-10, both default-real literals), non-wall boundary values
+ * from the owners, d = -|grad phi| + sqrt(|grad phi|^2 + 2 phi).  The
+ * matrix "a" and "su" are overwritten / added to, as there. */
+int fc_wall_distance(fc_ctx* ctx);
+/* modify_viscosity_turbulence (modify_viscosity_turbulence.f90:25-45) with
+ * TurbModel%name = 'k_omega_sst': Gauss gradients of u, v, w ("dUdxi"...),
+ * the strain magnitude ("magStrain", calc_strain_and_vorticity.f90), the k
+ * and omega equations (calcsc, k_omega_SST.f90:91-785: production with its
+ * limiter, the blending function "fsst", cross diffusion, sigma-blended
+ * diffusion, inlet/outlet/pressure and periodic faces, wall functions:
+ * the wall-cell production of k and omega fixed in wall cells, csrsolve,
+ * updateBoundary, the clip to small) and the eddy viscosity "vis" with its
+ * wall values "visw", "ypl", "tau" (modify_mu_eff, :790-958).  Fields: "te"
+ * (k), "ed" (omega), "fsst" (read by the k equation before the omega
+ * equation recomputes it; the reference reads it uninitialised on the first
+ * call, zero here), "gen", "walldist" (fc_wall_distance), "u", "v", "w",
+ * "vis", "den", "flmass", "visw".  resor56 (may be NULL) receives resor(5)
+ * and resor(6). */
+int fc_kw_sst(fc_ctx* ctx, double* resor56);
+
 /* ---- The case namelist &input_parameters (read_input.f90:28-227) for the
  * keys this path uses, starting from the reference's module defaults
  * (velocity.f90:24-33, pressure.f90:28-33, temperature.f90:14-25; default-real

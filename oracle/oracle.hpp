@@ -29,6 +29,16 @@ static const double kTiny30 = (double)1e-30f;   // interpolation.f90:556 (+1e-30
 
 enum { BC_WALL = 1, BC_INLET = 2, BC_OUTLET = 3, BC_SYMMETRY = 4, BC_PRESSURE = 5, BC_EMPTY = 6, BC_PERIODIC = 7 };
 
+// settings of one turbulence scalar (TurbModelData.f90 TurbScalar; the
+// default tolAbs 1e-10 is a default-real literal)
+struct TurbScalar {
+  double urf = 0.7, gds = 1.0;
+  int cScheme = 2;  // linearUpwind
+  std::string lSolver = "bicgstab";
+  int maxiter = 10;
+  double tolAbs = (double)1e-10f, tolRel = 0.01;
+};
+
 struct Case {
   // sizes (geometry.f90:17-24)
   int numNodes = 0, numCells = 0, numInnerFaces = 0, numBoundaryFaces = 0, numFaces = 0, numTotal = 0;
@@ -91,6 +101,14 @@ struct Case {
   std::string lSolverT = "bicgstab";
   double flomas = 0.0;
   int verbose = 0;
+  // k-omega SST (k_omega_SST.f90, calc_strain_and_vorticity.f90,
+  // wall_distance.f90): te = k, ed = omega
+  std::vector<double> te, ed, fsst;         // numTotal+1
+  std::vector<double> dTEdxi, dEDdxi;       // 3*(numTotal+1)
+  std::vector<double> gen, magStrain, walldist;  // numCells+1
+  std::vector<double> tau, ypl;             // nwal+1
+  TurbScalar turbK, turbW;                  // TurbModel%Scalar(1), (2)
+  double urfVis = 1.0;                      // TurbModel%urfVis
 };
 
 inline double& G(std::vector<double>& g, int k, int i) { return g[3 * (size_t)i + (k - 1)]; }
@@ -160,6 +178,22 @@ void gradp_and_sources(Case& c, std::vector<double>& p);
 void bpres(Case& c, std::vector<double>& p, int istage);
 void updateVelocityAtBoundary(Case& c);
 void updateBoundary(Case& c, std::vector<double>& phi);
+// scalar face fluxes (scalar_fluxes.f90), shared by the temperature and the
+// turbulence equations
+void facefluxsc(Case& c, int i, int ijp, int ijn, double xf, double yf, double zf, double arx, double ary, double arz,
+                double fm, double lambda, double gam, int scheme, const std::vector<double>& fi,
+                std::vector<double>& dfidxi, double dcoef, double& cap, double& can, double& suadd);
+void facefluxsc_bnd(Case& c, int ijp, double xf, double yf, double zf, double arx, double ary, double arz, double fm,
+                    std::vector<double>& dfidxi, double dcoef, double& cap, double& can, double& suadd);
+void facefluxsc_periodic(Case& c, int i, int ijp, int ijn, double xf, double yf, double zf, double arx, double ary,
+                         double arz, double fm, double gam, const std::vector<double>& fi,
+                         std::vector<double>& dfidxi, double dcoef, double& cap, double& can, double& suadd);
+// k-omega SST (oracle_turb.cpp)
+int wall_distance_poisson(Case& c);
+void calc_strain(Case& c);
+int calcsc_sst(Case& c, int ifi);
+void modify_mu_eff_sst(Case& c);
+int modify_viscosity_k_omega_sst(Case& c);
 void init_flmass(Case& c);
 int calcuvw(Case& c);
 int calcp_simple(Case& c);

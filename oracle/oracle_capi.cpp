@@ -58,6 +58,16 @@ std::vector<double>* dbl_array(Case& c, const std::string& n, int& len, int& off
   if (n == "dWdxi") { len = 3 * c.numTotal; offset = 3; return &c.dWdxi; }
   if (n == "dPdxi") { len = 3 * c.numTotal; offset = 3; return &c.dPdxi; }
   if (n == "Dmat") { len = 9 * c.numCells; offset = 9; return &c.Dmat; }
+  if (n == "te") { len = c.numTotal; return &c.te; }
+  if (n == "ed") { len = c.numTotal; return &c.ed; }
+  if (n == "fsst") { len = c.numTotal; return &c.fsst; }
+  if (n == "dTEdxi") { len = 3 * c.numTotal; offset = 3; return &c.dTEdxi; }
+  if (n == "dEDdxi") { len = 3 * c.numTotal; offset = 3; return &c.dEDdxi; }
+  if (n == "gen") { len = c.numCells; return &c.gen; }
+  if (n == "magStrain") { len = c.numCells; return &c.magStrain; }
+  if (n == "walldist") { len = c.numCells; return &c.walldist; }
+  if (n == "tau") { len = c.nwal; return &c.tau; }
+  if (n == "ypl") { len = c.nwal; return &c.ypl; }
   if (n == "uo") { len = c.numTotal; return &c.uo; }
   if (n == "vo") { len = c.numTotal; return &c.vo; }
   if (n == "wo") { len = c.numTotal; return &c.wo; }
@@ -180,6 +190,14 @@ int orc_case_set_param(void* h, const char* name, double val) {
   else if (n == "maxiterT") c.maxiterT = (int)val;
   else if (n == "tolAbsT") c.tolAbsT = val;
   else if (n == "tolRelT") c.tolRelT = val;
+  else if (n == "urfVis") c.urfVis = val;
+  else if (n.size() > 1 && (n.back() == 'K' || n.back() == 'W') && n.compare(0, n.size() - 1, "urf") == 0)
+    (n.back() == 'K' ? c.turbK : c.turbW).urf = val;
+  else if (n == "gdsK" || n == "gdsW") (n.back() == 'K' ? c.turbK : c.turbW).gds = val;
+  else if (n == "cSchemeK" || n == "cSchemeW") (n.back() == 'K' ? c.turbK : c.turbW).cScheme = (int)val;
+  else if (n == "maxiterK" || n == "maxiterW") (n.back() == 'K' ? c.turbK : c.turbW).maxiter = (int)val;
+  else if (n == "tolAbsK" || n == "tolAbsW") (n.back() == 'K' ? c.turbK : c.turbW).tolAbs = val;
+  else if (n == "tolRelK" || n == "tolRelW") (n.back() == 'K' ? c.turbK : c.turbW).tolRel = val;
   else return -1;
   return 0;
 }
@@ -189,6 +207,8 @@ int orc_case_set_solver(void* h, const char* which, const char* solver) {
   if (std::string(which) == "U") c.lSolverU = solver;
   else if (std::string(which) == "P") c.lSolverP = solver;
   else if (std::string(which) == "T") c.lSolverT = solver;
+  else if (std::string(which) == "K") c.turbK.lSolver = solver;
+  else if (std::string(which) == "W") c.turbW.lSolver = solver;
   else return -1;
   return 0;
 }
@@ -247,6 +267,11 @@ int orc_update_velocity_at_boundary(void* h) { updateVelocityAtBoundary(*(Case*)
 int orc_calcuvw(void* h) { return calcuvw(*(Case*)h); }
 int orc_calcp_simple(void* h) { return calcp_simple(*(Case*)h); }
 int orc_calculate_temperature(void* h, int solve) { return calculate_temperature(*(Case*)h, solve != 0); }
+int orc_wall_distance(void* h) { return wall_distance_poisson(*(Case*)h); }
+int orc_calc_strain(void* h) { calc_strain(*(Case*)h); return 0; }
+int orc_calcsc_sst(void* h, int ifi) { return calcsc_sst(*(Case*)h, ifi); }
+int orc_modify_mu_eff_sst(void* h) { modify_mu_eff_sst(*(Case*)h); return 0; }
+int orc_kw_sst(void* h) { return modify_viscosity_k_omega_sst(*(Case*)h); }
 
 // gamma, source: numCells (0-based memory); a <- A, su <- source * vol
 int orc_cd_assemble(void* h, const double* gamma, const double* source) {

@@ -1421,7 +1421,7 @@ int calcp_piso(Case& c) {
 
 // ------------------------------------------------------ scalar transport
 // facefluxsc (inner face), scalar_fluxes.f90:32-141
-static void facefluxsc(Case& c, int i, int ijp, int ijn, double xf, double yf, double zf, double arx, double ary,
+void facefluxsc(Case& c, int i, int ijp, int ijn, double xf, double yf, double zf, double arx, double ary,
                        double arz, double fm, double lambda, double gam, int scheme, const std::vector<double>& fi,
                        std::vector<double>& dfidxi, double dcoef, double& cap, double& can, double& suadd) {
   double fxn = lambda, fxp = 1.0 - lambda;
@@ -1450,7 +1450,7 @@ static void facefluxsc(Case& c, int i, int ijp, int ijn, double xf, double yf, d
 // ijp and the twin's owner ijn, central weights 1/2, the distance vector
 // 2 (xf - xc(ijp)), Df indexed by the face's position i within its patch (as
 // the reference writes it), cds face value
-static void facefluxsc_periodic(Case& c, int i, int ijp, int ijn, double xf, double yf, double zf, double arx,
+void facefluxsc_periodic(Case& c, int i, int ijp, int ijn, double xf, double yf, double zf, double arx,
                                 double ary, double arz, double fm, double gam, const std::vector<double>& fi,
                                 std::vector<double>& dfidxi, double dcoef, double& cap, double& can,
                                 double& suadd) {
@@ -1503,7 +1503,7 @@ void updateBoundary(Case& c, std::vector<double>& phi) {
 }
 
 // facefluxsc_boundary, scalar_fluxes.f90:256-337
-static void facefluxsc_bnd(Case& c, int ijp, double xf, double yf, double zf, double arx, double ary, double arz,
+void facefluxsc_bnd(Case& c, int ijp, double xf, double yf, double zf, double arx, double ary, double arz,
                            double fm, std::vector<double>& dfidxi, double dcoef, double& cap, double& can,
                            double& suadd) {
   double xpn = xf - c.xc[ijp], ypn = yf - c.yc[ijp], zpn = zf - c.zc[ijp];

@@ -72,6 +72,10 @@ void setup_case(Case& c, int numNodes, int numCells, int numInnerFaces, int numB
   c.dUdxi.assign(3 * nt, 0.0); c.dVdxi.assign(3 * nt, 0.0);
   c.dWdxi.assign(3 * nt, 0.0); c.dPdxi.assign(3 * nt, 0.0);
   c.T.assign(nt, 0.0); c.dTdxi.assign(3 * nt, 0.0);
+  for (auto* v : {&c.te, &c.ed, &c.fsst}) v->assign(nt, 0.0);
+  c.dTEdxi.assign(3 * nt, 0.0); c.dEDdxi.assign(3 * nt, 0.0);
+  for (auto* v : {&c.gen, &c.magStrain, &c.walldist}) v->assign(nc, 0.0);
+  c.tau.assign(c.nwal + 1, 0.0); c.ypl.assign(c.nwal + 1, 0.0);
   c.bcDFracT.assign(numBoundaries + 1, 0.0);  // geometry.f90:226 bcDFraction = 0
   c.a.assign(c.nnz + 1, 0.0);
   c.su.assign(nc, 0.0); c.sv.assign(nc, 0.0); c.sw.assign(nc, 0.0);

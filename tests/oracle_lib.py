@@ -45,8 +45,10 @@ def lib(fast=False):
     L.orc_prepare_lsq.argtypes = [C.c_void_p, C.c_int]
     L.orc_laplacian.argtypes = [C.c_void_p, dp, dp, C.c_ulonglong]
     L.orc_gradp_and_sources.argtypes = [C.c_void_p, C.c_int]
-    for f in ("orc_init_flmass", "orc_update_velocity_at_boundary", "orc_calcuvw", "orc_calcp_simple"):
+    for f in ("orc_init_flmass", "orc_update_velocity_at_boundary", "orc_calcuvw", "orc_calcp_simple",
+              "orc_wall_distance", "orc_calc_strain", "orc_modify_mu_eff_sst", "orc_kw_sst"):
         getattr(L, f).argtypes = [C.c_void_p]
+    L.orc_calcsc_sst.argtypes = [C.c_void_p, C.c_int]
     L.orc_simple_iteration.argtypes = [C.c_void_p, dp, dp]
     L.orc_time_shift.argtypes = [C.c_void_p]
     L.orc_piso_iteration.argtypes = [C.c_void_p, dp]
@@ -99,9 +101,9 @@ class Case:
     def _len(self, name):
         faces = ("arx", "ary", "arz", "xf", "yf", "zf", "flmass")
         cells = ("xc", "yc", "zc", "vol", "su", "sv", "sw", "spu", "spv", "sp", "apu", "apv", "apw", "d",
-                 "rU", "rV", "rW")
+                 "rU", "rV", "rW", "gen", "magStrain", "walldist")
         total = ("u", "v", "w", "p", "pp", "vis", "den", "t", "uo", "vo", "wo", "uoo", "voo", "woo", "uooo",
-                 "vooo", "wooo")
+                 "vooo", "wooo", "te", "ed", "fsst")
         if name in faces:
             return self.numFaces
         if name in cells:
@@ -112,7 +114,7 @@ class Case:
             return self.numInnerFaces + self.numPeriodic
         if name in ("facint", "Df", "neighbour"):
             return self.numInnerFaces
-        if name in ("dUdxi", "dVdxi", "dWdxi", "dPdxi", "dTdxi"):
+        if name in ("dUdxi", "dVdxi", "dWdxi", "dPdxi", "dTdxi", "dTEdxi", "dEDdxi"):
             return 3 * self.numTotal
         if name == "Dmat":
             return 9 * self.numCells
@@ -122,7 +124,7 @@ class Case:
             return self.numCells + 1
         if name == "diag":
             return self.numCells
-        if name in ("dnw", "srdw", "visw"):
+        if name in ("dnw", "srdw", "visw", "tau", "ypl"):
             return self.nwal
         if name in ("dns", "srds"):
             return self.nsym
@@ -180,6 +182,13 @@ class Case:
         out = np.zeros(self.numCells)
         self.L.orc_cd_gradient(self.h, _f64(phi), _f64(lam), out)
         return out
+
+    def wall_distance(self):
+        return self.L.orc_wall_distance(self.h)
+
+    def kw_sst(self):
+        """One modify_viscosity_turbulence with the k-omega SST model."""
+        return self.L.orc_kw_sst(self.h)
 
     def time_shift(self):
         self.L.orc_time_shift(self.h)

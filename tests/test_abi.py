@@ -141,7 +141,8 @@ def test_struct_layouts_match_the_header(fc, tmp_path):
         pytest.skip("gcc not available")
     structs = {"fc_solve_info": fc.SolveInfo, "fc_simple_params": fc.SimpleParams,
                "fc_temperature_params": fc.TemperatureParams, "fc_transient_params": fc.TransientParams,
-               "fc_run_params": fc.RunParams, "fc_case_settings": fc.CaseSettings}
+               "fc_run_params": fc.RunParams, "fc_case_settings": fc.CaseSettings,
+               "fc_turb_scalar": fc.TurbScalar, "fc_turbulence_params": fc.TurbulenceParams}
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "fc_gpu.h"', "int main(void) {"]
     for cname, py in structs.items():
         lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')

@@ -445,13 +445,22 @@ def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None, tets=Fa
             ctx.simple_iteration()
         ctx.sync()
         ctx.event(0)
+        done, err = 0, None
         for _ in range(iters):
-            res = ctx.simple_iteration()
+            try:
+                res = ctx.simple_iteration()
+            except fc.FcError as e:  # a diverging run ends the timed loop
+                err = str(e)
+                break
+            done += 1
         ctx.event(1)
-        ms = ctx.elapsed_ms() / iters
+        ms = ctx.elapsed_ms() / max(done, 1)
         out[key] = 1e3 / ms
         out[key + "_ms_per_iteration"] = ms
-        out[key + "_resor"] = [float(v) for v in res]
+        out[key + "_resor"] = [float(v) for v in res] if done else None
+        if err:
+            out[key + "_stopped"] = f"after {done} of {iters} iterations: {err}"
+            progress(f"simple {n}^3 {key}: stopped after {done} iterations: {err}")
     if momentum_batch:
         # C3a: the three momentum solves of calcuvw (shared off-diagonals, three
         # diagonals and sources) one after another and as one batched launch,

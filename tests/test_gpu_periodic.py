@@ -104,8 +104,8 @@ def test_temperature_with_periodic_pairs(ctx, fc, oracle, layout):
     # mean too when its patch comes first, its owner's value when after
     pf, tf = pair_faces(a)
     nC, nI = m.numCells, m.numInnerFaces
-    assert np.array_equal(g[nC + pf - nI], o[nC + pf - nI])
-    assert np.array_equal(g[nC + tf - nI], o[nC + tf - nI])
+    for faces in (pf, tf):
+        assert np.abs(g[nC + faces - nI] - o[nC + faces - nI]).max() <= FIELD_TOL * np.abs(o).max()
     same = np.array_equal(g[nC + tf - nI], g[nC + pf - nI])
     assert same == (layout == "twin_first")
 

@@ -403,6 +403,87 @@ def simple_iterations(n=128, iters=4, perturb=PERTURB, dev=0):
     return r
 
 
+TURB_VISCOS = 1e-3  # Re 1000 cavity for the turbulence leg
+
+
+def turbulent_cavity(fc, n, dev=0):
+    """The n^3 perturbed lid-driven cavity at Re 1000 with the k-omega SST
+    model (TurbModelData.f90 defaults; k = 1e-4 and omega = 1 everywhere at
+    the start), its wall distance computed: (fc.Mesh, context, arrays)."""
+    m = fc.Mesh.box(n, n, n, 1.0, 1.0, 1.0, perturb=PERTURB, seed=MESH_SEED)
+    nC, nT = m.numCells, m.numTotal
+    a, u, nwal = cavity_fields(m, nT, nC)
+    ctx = fc.Context(dev)
+    ctx.set_mesh(m)
+    zero = np.zeros(nT)
+    for k, v in dict(u=u, v=zero, w=zero, p=zero, pp=zero, den=np.ones(nT), vis=np.full(nT, TURB_VISCOS),
+                     te=np.full(nT, 1e-4), ed=np.full(nT, 1.0)).items():
+        ctx.field_set(k, v)
+    ctx.field_set("visw", np.full(max(nwal, 1), TURB_VISCOS))
+    for k in ("flmass", "a", "dUdxi", "dVdxi", "dWdxi", "dPdxi", "fsst"):
+        ctx.field_fill(k, 0.0)
+    ctx.simple_params(fc.SimpleParams.cavity(viscos=TURB_VISCOS))
+    ctx.turbulence_params(fc.TurbulenceParams.defaults())
+    ctx.init_flmass()
+    ctx.wall_distance()
+    return m, ctx, a
+
+
+def turbulence_iterations(n=128, iters=3, dev=0):
+    """`iters` SIMPLE iterations each followed by the k-omega SST update on
+    the turbulent cavity: the command the launch lists and ncu captures of
+    the turbulence kernels run, e.g.
+    python -c "import bench; bench.turbulence_iterations(128, 3)"."""
+    fc = load_fc()
+    m, ctx, _ = turbulent_cavity(fc, n, dev)
+    for _ in range(iters):
+        ctx.simple_iteration()
+        r = ctx.kw_sst()
+    ctx.sync()
+    print("turbulence_iterations", n, iters, "resor56", list(r), flush=True)
+    ctx.close()
+
+
+def turbulence_block(fc, args, dev, with_cpu):
+    """f2: the k-omega SST update (fc_kw_sst: strain, k and omega equations
+    with BiCGStab, eddy viscosity) on the n^3 turbulent cavity after a few
+    SIMPLE + SST iterations; event time per call, and the oracle's update of
+    the same state on one core."""
+    n = args.turb_n
+    m, ctx, a = turbulent_cavity(fc, n, dev)
+    for _ in range(3):
+        ctx.simple_iteration()
+        ctx.kw_sst()
+    state = {k: ctx.field_get(k) for k in ("u", "v", "w", "p", "flmass", "vis", "te", "ed", "fsst", "visw",
+                                            "walldist")}
+    ctx.sync()
+    ctx.event(0)
+    for _ in range(args.turb_calls):
+        r = ctx.kw_sst()
+    ctx.event(1)
+    ms = ctx.elapsed_ms() / args.turb_calls
+    out = {"workload": f"{n}^3 perturbed lid-driven cavity, Re {1.0 / TURB_VISCOS:g}, k-omega SST (high-Re, wall "
+                       "functions), BiCGStab(DILU) for k and omega (maxiter 10, tolRel 0.01)",
+           "cells": m.numCells, "kw_sst_ms": ms, "kw_sst_per_s": 1e3 / ms, "resor56": [float(v) for v in r],
+           "calls": args.turb_calls}
+    ctx.close()
+    if with_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_lib
+        oc = oracle_lib.Case(a, fast=True)
+        for k, v in state.items():
+            oc.set(k, v)
+        oc.set("den", np.ones(m.numTotal))
+        oc.param("viscos", TURB_VISCOS)
+        t0 = time.perf_counter()
+        oc.kw_sst()
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 1.0 / dt, "unit": "SST updates/s", "cores": 1, "kind": "port",
+                               "sample": "one k-omega SST update of the same state (C++ restatement, -O3, one thread)"}
+        out["gpu_vs_cpu"] = out["kw_sst_per_s"] / out["cpu_baseline"]["value"]
+    return out
+
+
 def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None, tets=False, viscos=0.01, scheme=1, grad=0,
                  iters=None, cpu_iters=None, urf=(0.8, 0.3), momentum_batch=False, skip=None):
     """SIMPLE iterations per second on the n^3 lid-driven cavity (unit cube,
@@ -411,14 +492,19 @@ def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None, tets=Fa
     examples/cavity/input.nml), FP64 and mixed precision, plus the oracle's
     SIMPLE iteration on one core.  perturb > 0 moves the interior vertices by
     U(-perturb h, perturb h) (seed 42): the non-orthogonal mesh."""
+    t0 = time.perf_counter()
     m = fc.Mesh.box(n, n, n, 1.0, 1.0, 1.0, perturb=perturb, seed=MESH_SEED, tets=tets)
+    t_box = time.perf_counter() - t0
     iters = args.simple_iters if iters is None else iters
     skip = args.simple_skip if skip is None else skip
     cpu_iters = args.simple_cpu_iters if cpu_iters is None else cpu_iters
     nC, nT = m.numCells, m.numTotal
     a, u, nwal = cavity_fields(m, nT, nC)
     ctx = fc.Context(dev)
+    t0 = time.perf_counter()
     ctx.set_mesh(m)
+    ctx.sync()
+    t_set = time.perf_counter() - t0
     prm = fc.SimpleParams.cavity(viscos=viscos, scheme=scheme, grad=grad, urfU=urf[0], urfP=urf[1])
 
     def reset():
@@ -437,7 +523,8 @@ def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None, tets=Fa
     sname = {1: "central", 19: "boundedLinearUpwind"}.get(scheme, str(scheme))
     gname = {0: "Gauss", 1: "LSQ", 2: "LSQ_DM"}[grad]
     out = {"workload": f"{n}^3 lid-driven cavity on {mesh_kind}, Re={1.0 / viscos:g}, SIMPLE ({sname}/DC, {gname}, "
-                       f"BiCGStab U, ICCG p, urfU {urf[0]:g}, urfP {urf[1]:g})", "cells": nC, "unit": "SIMPLE iters/s"}
+                       f"BiCGStab U, ICCG p, urfU {urf[0]:g}, urfP {urf[1]:g})", "cells": nC, "unit": "SIMPLE iters/s",
+           "setup_s": {"mesh_box_host": round(t_box, 2), "fc_set_mesh": round(t_set, 2)}}
     for mode, key in ((fc.FC_PREC_FP64, "value"), (fc.FC_PREC_MIXED_COLOURED, "mixed")):
         ctx.set_precision(mode, MIXED_INNER_TOL, 0) if mode else ctx.set_precision(mode)
         reset()
@@ -934,6 +1021,8 @@ def run_gpu(args, rank, world, dist):
         line["batch"] = batch_block(fc, args, dev)
     if args.piso_n > 0:
         line["piso"] = piso_block(fc, args, dev, not args.no_cpu)
+    if args.turb_n > 0:
+        line["turbulence"] = turbulence_block(fc, args, dev, not args.no_cpu)
     if args.simple_tet_n > 0:
         # C5: 6 tets per perturbed hex, Re = 400, LSQ gradients, boundedLinearUpwind.  With the cavity
         # input's urfU 0.8 / urfP 0.3 the SIMPLE iteration diverges on this mesh (the oracle too, at
@@ -974,6 +1063,8 @@ def main():
     ap.add_argument("--adjoint-fd-dirs", type=int, default=32, help="directions of the finite-difference check")
     ap.add_argument("--momentum-calls", type=int, default=5, help="timed calcuvw calls of the C3a leg")
     ap.add_argument("--piso-n", type=int, default=64, help="cells per side of the PISO leg (0: skip)")
+    ap.add_argument("--turb-n", type=int, default=128, help="cells per side of the k-omega SST leg (0: skip)")
+    ap.add_argument("--turb-calls", type=int, default=5, help="timed fc_kw_sst calls there")
     ap.add_argument("--piso-steps", type=int, default=10, help="timed PISO time steps")
     ap.add_argument("--batch-count", type=int, default=64, help="problems of the batched leg (0: skip)")
     ap.add_argument("--batch-tol", type=float, default=1e-6, help="relative L1 tolerance there")

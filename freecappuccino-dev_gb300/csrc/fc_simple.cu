@@ -924,12 +924,13 @@ __device__ __forceinline__ void facefluxsc_bnd(const MeshView& M, int f, int ijp
   suadd = dcoef * (dfixi + dfiyi + dfizi);
 }
 
-// facefluxsc_periodic, scalar_fluxes.f90:147-251, pair q: central weights
-// 1/2, the distance vector 2 (xf - xc(ijp)), Df of the face's position in
-// its patch (as written there), cds face value
-__device__ __forceinline__ void facefluxsc_pair(const MeshView& M, int q, int ijp, int ijn, double fm, double dcoef,
-                                                double gam, const double* fi, const Fld& g, double& cap, double& can,
-                                                double& suadd) {
+// facefluxsc_periodic, scalar_fluxes.f90:147-251, pair q, with the pair's
+// two cell values fp (owner side) and fn (twin side): central weights 1/2,
+// the distance vector 2 (xf - xc(ijp)), Df of the face's position in its
+// patch (as written there), cds face value
+__device__ __forceinline__ void facefluxsc_pair2(const MeshView& M, int q, int ijp, int ijn, double fm, double dcoef,
+                                                 double gam, double fp, double fn, const Fld& g, double& cap,
+                                                 double& can, double& suadd) {
   const int f = M.pface[q], i = M.ppos[q];
   const double arx = M.arx[f], ary = M.ary[f], arz = M.arz[f];
   const double fxn = 0.5, fxp = fxn;
@@ -946,11 +947,18 @@ __device__ __forceinline__ void facefluxsc_pair(const MeshView& M, int q, int ij
   dfiyi = dfiyi * (ary - Df * ypn);
   dfizi = dfizi * (arz - Df * zpn);
   const double fdfie = dcoef * (dfixi + dfiyi + dfizi);
-  const double fii = fm >= 0.0 ? fi[ijp] + (fi[ijn] - fi[ijp]) * fxp : fi[ijn] + (fi[ijp] - fi[ijn]) * fxn;
+  const double fii = fm >= 0.0 ? fp + (fn - fp) * fxp : fn + (fp - fn) * fxn;
   double fcfie = fm * fii;
-  const double fcfii = ce * fi[ijn] + cp * fi[ijp];
+  const double fcfii = ce * fn + cp * fp;
   fcfie = gam * (fcfie - fcfii);
   suadd = -fcfie + fdfie;
+}
+
+// the same with the cell values read from the field fi
+__device__ __forceinline__ void facefluxsc_pair(const MeshView& M, int q, int ijp, int ijn, double fm, double dcoef,
+                                                double gam, const double* fi, const Fld& g, double& cap, double& can,
+                                                double& suadd) {
+  facefluxsc_pair2(M, q, ijp, ijn, fm, dcoef, gam, fi[ijp], fi[ijn], g, cap, can, suadd);
 }
 
 // facefluxsc (inner face), scalar_fluxes.f90:32-141, with the diffusion
@@ -1189,8 +1197,30 @@ __global__ void k_sst_face(MeshView M, Dev D, Turb T, int ifi, double gam, int s
   }
 }
 
+// omega fixed in a wall cell by its wall face w, k_omega_SST.f90:625-650
+__device__ __forceinline__ double sst_wall_omega(const MeshView& M, const Dev& D, const Turb& T, int c, int w) {
+  const double dnw = M.dnw[w];
+  const double wlog = sqrt(T.te[c]) / (T.cmu25 * SST_CAPPA * dnw);
+  const double wvis = 6.0 * (T.viscos / D.den[c]) / (SST_BETAI1 * (dnw * dnw));
+  return sqrt(wvis * wvis + wlog * wlog);
+}
+
+// omega of cell c as the boundary loop leaves it when it reaches patch pb:
+// the wall faces of earlier patches have already fixed it (the last one wins)
+__device__ double sst_omega_before(const MeshView& M, const Dev& D, const Turb& T, int c, int pb) {
+  double e = T.ed[c];
+  for (int q = M.cf_ptr[c]; q < M.cf_ptr[c + 1]; ++q) {
+    const int f = M.cf_face[q];
+    if (f < M.nI) continue;
+    const int bi = f - M.nI, b = M.bpatch[bi];
+    if (b < pb && D.ptype[b] == FC_BC_WALL) e = sst_wall_omega(M, D, T, c, M.bwall[bi]);
+  }
+  return e;
+}
+
 // periodic pairs of calcsc, k_omega_SST.f90:521-560: the pair's mean sigma
-// and mean viscosity
+// and mean viscosity.  In the omega equation the pair sees the omega values
+// that the wall patches listed before its periodic patch have fixed.
 __global__ void k_sst_pair(MeshView M, Dev D, Turb T, int ifi, double gam) {
   const double* fi = ifi == 1 ? T.te : T.ed;
   const Fld g{ifi == 1 ? T.gte : T.ged, M.nT};
@@ -1200,7 +1230,13 @@ __global__ void k_sst_pair(MeshView M, Dev D, Turb T, int ifi, double gam) {
     const double viste = 0.5 * (D.vis[ijp] + D.vis[ijn]) - T.viscos;
     const double dcoef = T.viscos + viste * prtr;
     double cap, can, suadd;
-    facefluxsc_pair(M, q, ijp, ijn, D.flmass[f], dcoef, gam, fi, g, cap, can, suadd);
+    if (ifi == 2) {
+      const int pb = M.bpatch[f - M.nI];
+      facefluxsc_pair2(M, q, ijp, ijn, D.flmass[f], dcoef, gam, sst_omega_before(M, D, T, ijp, pb),
+                       sst_omega_before(M, D, T, ijn, pb), g, cap, can, suadd);
+    } else {
+      facefluxsc_pair(M, q, ijp, ijn, D.flmass[f], dcoef, gam, fi, g, cap, can, suadd);
+    }
     const int l = M.nI + q;
     D.a[M.ijk[l]] = can;
     D.a[M.jik[l]] = cap;
@@ -1264,9 +1300,7 @@ __global__ void k_sst_cell(MeshView M, Dev D, Turb T, int ifi, double urf) {
           T.gen[c] = gen;
           su = su + gen * M.vol[c];
         } else {
-          const double wlog = sqrt(T.te[c]) / (T.cmu25 * SST_CAPPA * dnw);
-          const double wvis = 6.0 * (T.viscos / D.den[c]) / (SST_BETAI1 * (dnw * dnw));
-          const double ed = sqrt(wvis * wvis + wlog * wlog);
+          const double ed = sst_wall_omega(M, D, T, c, iw);
           T.ed[c] = ed;
           su = ed;
           sp = 1.0;

@@ -284,11 +284,11 @@ int fc_ilu0(fc_ctx* ctx, int n, int nnz, const int* ia, const int* ja, const dou
  *    a, x (in/out), b: DEVICE memory of the current device; stream: a
  *    cudaStream_t of that device (NULL = legacy default stream).
  *  - the first call on each device looks up the scratch address
- *    (cudaGetSymbolAddress with that device current): make that first call
- *    before any stream capture.
+ *    (cudaGetSymbolAddress with that device current).
  *  - calls that overlap in time on the same device (other threads, other
  *    streams) race on the one scratch area: serialise them.
- *  - blocks until the solve has finished; info->ms is not measured (0).
+ *  - blocks until the solve has finished (it synchronises the stream), so it
+ *    cannot be captured into a CUDA graph; info->ms is not measured (0).
  *  - errmsg (may be NULL) receives a one-line reason on failure.
  * Returns FC_OK, FC_WARN_MAXITER or an error, as fc_csrsolve. */
 #define FC_NOALLOC_MAX_N (1 << 20)

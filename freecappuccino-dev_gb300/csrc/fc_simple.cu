@@ -1090,11 +1090,19 @@ __global__ void k_minmax(int n, const double* __restrict__ phi, double* __restri
 // T = max(T, small) on the cells when min(T) < 0 (temperature.f90:381);
 // every block folds the per-block minima itself
 __global__ void k_clip_small(int n, double* __restrict__ phi, const double* __restrict__ part, int nb) {
+  // every block reduces the per-block minima itself, all threads sharing the
+  // loads (a single thread's serial loop over them dominated the pass)
+  __shared__ double s_w[32];
   __shared__ double s_lo;
+  double lo = INFINITY;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) lo = fmin(lo, part[b]);
+  for (int o = 16; o > 0; o >>= 1) lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+  if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = lo;
+  __syncthreads();
   if (threadIdx.x == 0) {
-    double lo = INFINITY;
-    for (int b = 0; b < nb; ++b) lo = fmin(lo, part[b]);
-    s_lo = lo;
+    double m = s_w[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmin(m, s_w[w]);
+    s_lo = m;
   }
   __syncthreads();
   if (!(s_lo < 0.0)) return;

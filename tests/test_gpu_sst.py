@@ -18,6 +18,7 @@ pytestmark = pytest.mark.gpu
 
 ASSEMBLY_RTOL = 1e-12
 FIELD_RTOL = 1e-8
+FIRST_RESOR_RTOL = 1e-4
 TURB = ("te", "ed")
 
 
@@ -70,15 +71,22 @@ def test_kw_sst_assembly_matches_oracle(ctx, fc, oracle):
 
 
 def test_kw_sst_with_simple_iterations_tracks_oracle(ctx, fc, oracle):
+    """Four SIMPLE iterations each followed by the SST update, the oracle
+    taking the GPU's state before each update (lockstep): the update's
+    residuals and fields.  The first update starts from uniform k and omega,
+    where the normalised residual resor(5) divides rounding noise by rounding
+    noise, so its residuals are compared loosely (FIRST_RESOR_RTOL)."""
     m, a, oc = setup(ctx, fc, oracle)
     ctx.wall_distance()
     oc.wall_distance()
     oc.set("walldist", ctx.field_get("walldist"))
-    for _ in range(4):
+    for it in range(4):
         ctx.simple_iteration()
-        oc.simple_iteration()
+        for k in ("u", "v", "w", "p", "flmass", "vis", "te", "ed", "fsst", "visw"):
+            oc.set(k, ctx.field_get(k))
         r = ctx.kw_sst()
         assert oc.kw_sst() >= 0
-        np.testing.assert_allclose(r, [oc.scalar("resor5"), oc.scalar("resor6")], rtol=1e-6)
-    for k in ("u", "v", "w", "p", "te", "ed", "vis"):
-        assert rel(ctx.field_get(k), oc.get(k)) <= FIELD_RTOL, k
+        np.testing.assert_allclose(r, [oc.scalar("resor5"), oc.scalar("resor6")],
+                                   rtol=FIRST_RESOR_RTOL if it == 0 else 1e-6)
+        for k in ("te", "ed", "vis", "fsst", "visw"):
+            assert rel(ctx.field_get(k), oc.get(k)) <= FIELD_RTOL, (it, k)

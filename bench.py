@@ -444,6 +444,60 @@ def turbulence_iterations(n=128, iters=3, dev=0):
     ctx.close()
 
 
+def mesh_setup(n=100, tets=True, perturb=PERTURB, dev=0):
+    """fc_set_mesh of the n^3 perturbed box (6 tetrahedra per hex when
+    `tets`): wall-clock seconds of the host mesh generation, of set_mesh and
+    of its phases (fc_get_setup_times), e.g.
+    python -c "import bench; bench.mesh_setup(100, True)" (6,000,000 cells)."""
+    fc = load_fc()
+    t0 = time.perf_counter()
+    m = fc.Mesh.box(n, n, n, 1.0, 1.0, 1.0, perturb=perturb, seed=MESH_SEED, tets=tets)
+    t_box = time.perf_counter() - t0
+    ctx = fc.Context(dev)
+    t0 = time.perf_counter()
+    ctx.set_mesh(m)
+    ctx.sync()
+    out = {"cells": m.numCells, "mesh_box_host": round(t_box, 3), "fc_set_mesh": round(time.perf_counter() - t0, 3),
+           "phases": {k: round(v, 3) for k, v in ctx.setup_times().items()}}
+    ctx.close()
+    print(json.dumps(out), flush=True)
+    return out
+
+
+def temperature_iterations(n=128, iters=3, dev=0):
+    """`iters` SIMPLE iterations each followed by calculate_temperature on the
+    n^3 perturbed cavity with the hot lid (isothermal lid at T = 1, the other
+    walls adiabatic, temperature.f90's defaults): the command the profiles of
+    the temperature kernels run, e.g.
+    python -c "import bench; bench.temperature_iterations(128, 3)"."""
+    fc = load_fc()
+    m = fc.Mesh.box(n, n, n, 1.0, 1.0, 1.0, perturb=PERTURB, seed=MESH_SEED)
+    nC, nT = m.numCells, m.numTotal
+    a, u, nwal = cavity_fields(m, nT, nC)
+    ctx = fc.Context(dev)
+    ctx.set_mesh(m)
+    zero = np.zeros(nT)
+    t = np.zeros(nT)
+    st = a["startFace"][LID_PATCH] - m.numInnerFaces
+    t[nC + st:nC + st + a["nfaces"][LID_PATCH]] = 1.0
+    for k, v in dict(u=u, v=zero, w=zero, p=zero, pp=zero, den=np.ones(nT), vis=np.full(nT, 0.01), t=t).items():
+        ctx.field_set(k, v)
+    ctx.field_set("visw", np.full(max(nwal, 1), 0.01))
+    for k in ("flmass", "a", "dUdxi", "dVdxi", "dWdxi", "dPdxi", "dTdxi"):
+        ctx.field_fill(k, 0.0)
+    ctx.simple_params(fc.SimpleParams.cavity(viscos=0.01))
+    bcdf = np.zeros(len(a["bctype"]))
+    bcdf[LID_PATCH] = 1.0
+    ctx.temperature_params(fc.TemperatureParams.defaults(), bcdf)
+    ctx.init_flmass()
+    for _ in range(iters):
+        ctx.simple_iteration()
+        r7 = ctx.calculate_temperature()
+    ctx.sync()
+    print("temperature_iterations", n, iters, "resor7", r7, flush=True)
+    ctx.close()
+
+
 def turbulence_block(fc, args, dev, with_cpu):
     """f2: the k-omega SST update (fc_kw_sst: strain, k and omega equations
     with BiCGStab, eddy viscosity) on the n^3 turbulent cavity after a few
@@ -524,7 +578,8 @@ def simple_block(fc, args, dev, with_cpu, n, perturb=0.0, cpu_skip=None, tets=Fa
     gname = {0: "Gauss", 1: "LSQ", 2: "LSQ_DM"}[grad]
     out = {"workload": f"{n}^3 lid-driven cavity on {mesh_kind}, Re={1.0 / viscos:g}, SIMPLE ({sname}/DC, {gname}, "
                        f"BiCGStab U, ICCG p, urfU {urf[0]:g}, urfP {urf[1]:g})", "cells": nC, "unit": "SIMPLE iters/s",
-           "setup_s": {"mesh_box_host": round(t_box, 2), "fc_set_mesh": round(t_set, 2)}}
+           "setup_s": {"mesh_box_host": round(t_box, 2), "fc_set_mesh": round(t_set, 2),
+                       "fc_set_mesh_phases": {k: round(v, 3) for k, v in ctx.setup_times().items()}}}
     for mode, key in ((fc.FC_PREC_FP64, "value"), (fc.FC_PREC_MIXED_COLOURED, "mixed")):
         ctx.set_precision(mode, MIXED_INNER_TOL, 0) if mode else ctx.set_precision(mode)
         reset()

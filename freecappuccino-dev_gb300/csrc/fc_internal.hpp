@@ -126,6 +126,7 @@ struct CsrSystem {
   OrdStore<double> o64;
   OrdStore<float> o32;
   double est_sweep_us = 0.0;         // critical-path estimate of the forward sweep
+  double t_tiling = 0.0, t_schedule = 0.0;  // seconds of the tile-count choice and of the ordered sweep build
   DevColoured* mc = nullptr;         // built on the first FC_PREC_MIXED_COLOURED solve
   // workspace
   DVec<double> x, b, r, r0, p, u, z, v, d, w;
@@ -204,6 +205,7 @@ struct fc_ctx {
   MeshDev mesh;
   bool has_mesh = false;
   int mesh_gen = 0;    // incremented by every fc_set_mesh
+  double setup_s[FC_SETUP_PHASES] = {};  // phase times of the last fc_set_mesh
   CsrSystem* sys_ext = nullptr;    // pattern cache of fc_csrsolve
   CsrSystem* sys_mesh = nullptr;   // global matrix of the mesh (sparse_matrix module)
   std::vector<CsrSystem*> sys_user;

@@ -42,15 +42,35 @@ __global__ void k_minmax_part(const double* __restrict__ phi, int nC, double* __
   }
 }
 
-__global__ void k_minmax_final(const double* __restrict__ part, int nb, double* __restrict__ mm) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// the block minima and maxima folded by one block, every thread sharing the
+// loads (one thread's serial loop over them took ten times the pass itself)
+constexpr int kMinMaxFinalThreads = 256;
+
+__global__ void __launch_bounds__(kMinMaxFinalThreads) k_minmax_final(const double* __restrict__ part, int nb,
+                                                                       double* __restrict__ mm) {
+  __shared__ double smin[kMinMaxFinalThreads / 32], smax[kMinMaxFinalThreads / 32];
   double lo = part[0], hi = part[1];
-  for (int b = 1; b < nb; ++b) {
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
     lo = fclim::dmin(lo, part[2 * b]);
     hi = fclim::dmax(hi, part[2 * b + 1]);
   }
-  mm[0] = lo;
-  mm[1] = hi;
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fclim::dmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fclim::dmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    smin[threadIdx.x >> 5] = lo;
+    smax[threadIdx.x >> 5] = hi;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      lo = fclim::dmin(lo, smin[w]);
+      hi = fclim::dmax(hi, smax[w]);
+    }
+    mm[0] = lo;
+    mm[1] = hi;
+  }
 }
 
 template <int KIND>
@@ -101,7 +121,7 @@ int fv_limit(fc_ctx* ctx, const double* phi, double* g) {
     FC_CUDA_TRY(ctx, part.alloc((size_t)2 * kMinMaxBlocks + 2));
     double* mm = part.p + 2 * kMinMaxBlocks;
     k_minmax_part<<<nb, 256, 0, ctx->stream>>>(phi, M.nC, part.p);
-    k_minmax_final<<<1, 32, 0, ctx->stream>>>(part.p, nb, mm);
+    k_minmax_final<<<1, kMinMaxFinalThreads, 0, ctx->stream>>>(part.p, nb, mm);
     if (kind == FC_LIMITER_BJ) k_limit_scale<FC_LIMITER_BJ><<<gb, 256, 0, ctx->stream>>>(M, ja, phi, mm, g);
     else if (kind == FC_LIMITER_VENKAT) k_limit_scale<FC_LIMITER_VENKAT><<<gb, 256, 0, ctx->stream>>>(M, ja, phi, mm, g);
     else k_limit_scale<FC_LIMITER_R><<<gb, 256, 0, ctx->stream>>>(M, ja, phi, mm, g);

@@ -5,12 +5,14 @@
 //
 // Deterministic by construction: every cell accumulates its faces in
 // ascending face index (the order of the reference's face loops) through a
-// cell -> face list, so no atomics are used and the sums are those of the
-// reference.  The geometry uses non-contracted FP64 arithmetic and matches
-// the reference bit for bit.
+// cell -> face list, so the geometry sums are those of the reference; the
+// geometry uses non-contracted FP64 arithmetic and matches the reference bit
+// for bit.  The CSR rows are filled with atomics in arrival order and then
+// sorted, which gives the same pattern whatever the order.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -139,6 +141,156 @@ __global__ void k_wall_geom(int nwal, const int* __restrict__ wall_face, const i
   }
 }
 
+// ------------------------------------------------------------ CSR pattern
+// create_CSR_matrix (sparse_matrix.f90:86-296) on the device.  The links of
+// the pattern are e = 0..nI-1, the inner faces (owner, neighbour), then
+// e = nI..nI+nPer-1, the periodic pairs (owner of the periodic face, owner
+// of its twin).  Row i of the pattern is {i} and the cell at the other end of
+// every link of i, in ascending column order: the rows the reference gets by
+// sorting the (row, column) pairs (sparse_matrix.f90:110-202).
+__device__ __forceinline__ void link_cells(int e, int nI, const int* __restrict__ owner,
+                                           const int* __restrict__ neighbour, const int* __restrict__ pface,
+                                           const int* __restrict__ ptwin, int& i, int& j) {
+  if (e < nI) {
+    i = owner[e];
+    j = neighbour[e];
+  } else {
+    i = owner[pface[e - nI]];
+    j = owner[ptwin[e - nI]];
+  }
+}
+
+// off-diagonal entries per row
+__global__ void k_csr_count(int nL, int nI, const int* __restrict__ owner, const int* __restrict__ neighbour,
+                            const int* __restrict__ pface, const int* __restrict__ ptwin, int* cnt) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nL; e += gridDim.x * blockDim.x) {
+    int i, j;
+    link_cells(e, nI, owner, neighbour, pface, ptwin, i, j);
+    atomicAdd(&cnt[i], 1);
+    atomicAdd(&cnt[j], 1);
+  }
+}
+
+// exclusive scan of the row lengths cnt[c] + 1 (c < n) and 0 (c = n) into
+// ia[0..n], in three passes: block scans with block totals, a scan of the
+// totals, the totals added back
+constexpr int SCAN_TB = 1024;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int* s_w, int& total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_w[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int w = lane < (int)(blockDim.x >> 5) ? s_w[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    s_w[lane] = w;  // inclusive warp totals
+  }
+  __syncthreads();
+  total = s_w[(blockDim.x >> 5) - 1];
+  const int r = x - v + (wid > 0 ? s_w[wid - 1] : 0);
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(SCAN_TB) k_csr_scan_rows(int n, const int* __restrict__ cnt, int* ia, int* bsum) {
+  __shared__ int s_w[32];
+  const int c = blockIdx.x * SCAN_TB + threadIdx.x;
+  const int v = c < n ? cnt[c] + 1 : 0;
+  int total;
+  const int r = block_exclusive_scan(v, s_w, total);
+  if (c <= n) ia[c] = r;
+  if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
+
+// one block: the block totals scanned in place (exclusive), in chunks
+__global__ void __launch_bounds__(SCAN_TB) k_csr_scan_totals(int nb, int* bsum) {
+  __shared__ int s_w[32];
+  int carry = 0;
+  for (int base = 0; base < nb; base += SCAN_TB) {
+    const int b = base + threadIdx.x;
+    const int v = b < nb ? bsum[b] : 0;
+    int total;
+    const int r = block_exclusive_scan(v, s_w, total);
+    if (b < nb) bsum[b] = carry + r;
+    carry += total;
+  }
+}
+
+__global__ void __launch_bounds__(SCAN_TB) k_csr_scan_add(int n, const int* __restrict__ bsum, int* ia) {
+  const int c = blockIdx.x * SCAN_TB + threadIdx.x;
+  if (c <= n) ia[c] += bsum[blockIdx.x];
+}
+
+// the diagonal first in every row, the other ends of the links after it in
+// arrival order (sorted next)
+__global__ void k_csr_fill(int nC, int nL, int nI, const int* __restrict__ owner, const int* __restrict__ neighbour,
+                           const int* __restrict__ pface, const int* __restrict__ ptwin, const int* __restrict__ ia,
+                           int* pos, int* ja) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nC; c += stride) ja[ia[c]] = c;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nL; e += stride) {
+    int i, j;
+    link_cells(e, nI, owner, neighbour, pface, ptwin, i, j);
+    ja[ia[i] + 1 + atomicAdd(&pos[i], 1)] = j;
+    ja[ia[j] + 1 + atomicAdd(&pos[j], 1)] = i;
+  }
+}
+
+// every row sorted (insertion sort: rows hold a cell's neighbours); a column
+// repeated in a row (two cells coupled twice) sets bit 0 of *flag; diag[c]
+// is the slot of column c in row c
+__global__ void k_csr_sort(int nC, const int* __restrict__ ia, int* ja, int* diag, int* flag) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nC; c += gridDim.x * blockDim.x) {
+    const int b = ia[c], e = ia[c + 1];
+    for (int k = b + 1; k < e; ++k) {
+      const int v = ja[k];
+      int l = k - 1;
+      while (l >= b && ja[l] > v) {
+        ja[l + 1] = ja[l];
+        --l;
+      }
+      ja[l + 1] = v;
+    }
+    int d = -1;
+    for (int k = b; k < e; ++k) {
+      if (k > b && ja[k] == ja[k - 1]) atomicOr(flag, 1);
+      if (ja[k] == c) d = k;
+    }
+    diag[c] = d;
+  }
+}
+
+// face -> slot maps, csr_to_k (utils.f90:96-147): the first slot of row i
+// holding column j, for (owner, neighbour) and (neighbour, owner) of every
+// link (sparse_matrix.f90:205-292)
+__device__ __forceinline__ int csr_slot(const int* __restrict__ ia, const int* __restrict__ ja, int i, int j) {
+  int lo = ia[i], hi = ia[i + 1] - 1;  // columns strictly increasing
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (ja[mid] < j) lo = mid + 1; else hi = mid;
+  }
+  return ja[lo] == j ? lo : -1;
+}
+
+__global__ void k_csr_slots(int nL, int nI, const int* __restrict__ owner, const int* __restrict__ neighbour,
+                            const int* __restrict__ pface, const int* __restrict__ ptwin, const int* __restrict__ ia,
+                            const int* __restrict__ ja, int* ijk, int* jik) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nL; e += gridDim.x * blockDim.x) {
+    int i, j;
+    link_cells(e, nI, owner, neighbour, pface, ptwin, i, j);
+    ijk[e] = csr_slot(ia, ja, i, j);
+    jik[e] = csr_slot(ia, ja, j, i);
+  }
+}
+
 }  // namespace
 
 static void free_mesh_dev(MeshDev& m) {
@@ -168,12 +320,32 @@ static int up(fc_ctx* ctx, DVec<T>& d, const T* h, size_t n) {
 
 #define UP(dst, src, cnt) do { int _s = up(ctx, dst, src, cnt); if (_s) return _s; } while (0)
 
+// wall-clock time of the set-up phases: lap() waits for the stream, adds the
+// time since the previous lap to the phase and starts the next one
+struct PhaseClock {
+  fc_ctx* ctx;
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  explicit PhaseClock(fc_ctx* c) : ctx(c) {
+    for (double& v : ctx->setup_s) v = 0.0;
+  }
+  int lap(int phase) {
+    FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    const auto now = std::chrono::steady_clock::now();
+    ctx->setup_s[phase] += std::chrono::duration<double>(now - t).count();
+    t = now;
+    return FC_OK;
+  }
+};
+#define FC_TRY(call) do { int _s = (call); if (_s) return _s; } while (0)
+
 // Build everything the path needs from the host mesh.  Host work is the
-// one-time topology bookkeeping (cell -> face lists, CSR pattern, slot
-// maps); the geometry is computed on the device.
+// one-time topology bookkeeping (cell -> face lists, the periodic face
+// mapping) and the sweep schedule of the global matrix; the geometry, the
+// CSR pattern and its slot maps are computed on the device.
 extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
   FC_RANGE();
   if (!ctx || !hm) return FC_ERR_BAD_INPUT;
+  PhaseClock clk(ctx);
   std::string why;
   if (hm->validate(&why, true) != FC_OK) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_set_mesh: " + why);
   cudaSetDevice(ctx->device);
@@ -240,6 +412,7 @@ extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
   for (auto* v : cv) FC_CUDA_TRY(ctx, v->alloc(nC));
   FC_CUDA_TRY(ctx, m.facint.alloc(nI));
   FC_CUDA_TRY(ctx, m.Df.alloc(nI));
+  FC_TRY(clk.lap(FC_SETUP_TOPOLOGY));
   const int TB = 256;
   auto grid = [&](int n) { return std::max(1, std::min(65535, (n + TB - 1) / TB)); };
   k_face_geom<<<grid(nF), TB, 0, ctx->stream>>>(nF, m.nnodes.p, m.nodes.p, m.x.p, m.y.p, m.z.p, m.arx.p, m.ary.p,
@@ -259,6 +432,7 @@ extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
     ctx->kernel_launches++;
   }
   FC_CUDA_TRY(ctx, cudaGetLastError());
+  FC_TRY(clk.lap(FC_SETUP_GEOMETRY));
   m.h_xyz.resize((size_t)3 * nC);
   FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, m.h_xyz.data(), m.xc.p, nC * sizeof(double)));
   FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, m.h_xyz.data() + nC, m.yc.p, nC * sizeof(double)));
@@ -327,63 +501,57 @@ extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
     FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, m.cf_ptr.p, cf_ptr.data(), cf_ptr.size() * sizeof(int)));
     FC_CUDA_TRY(ctx, fc_h2d(ctx->stream, m.cf_face.p, cf_face.data(), cf_face.size() * sizeof(int)));
   }
-  // CSR pattern: row i = sorted {i} U {cells sharing an inner face} U {cells
-  // paired with i through periodic faces}; the reference sorts (row, col)
-  // pairs lexicographically, which gives exactly these rows
-  // (sparse_matrix.f90:110-202).  A cell pair coupled twice (an inner face and
-  // a periodic pair) would make a repeated column, which is rejected.
-  const int nnz = 2 * (nI + nPer) + nC;
-  std::vector<int> ia(nC + 1, 0), ja(nnz), diag(nC), ijk(nI + nPer), jik(nI + nPer);
-  {
-    std::vector<std::vector<int>> extra(nPer ? nC : 0);
-    for (int q = 0; q < nPer; ++q) {
-      const int ijp = owner[pface[q]], ijn = owner[ptwin[q]];
-      extra[ijp].push_back(ijn);
-      extra[ijn].push_back(ijp);
-    }
-    std::vector<int> cols;
-    int k0 = 0;
-    for (int c = 0; c < nC; ++c) {
-      cols.clear();
-      cols.push_back(c);
-      for (int q = cf_ptr[c]; q < cf_ptr[c + 1]; ++q) {
-        int f = cf_face[q];
-        if (f >= nI) continue;
-        cols.push_back(owner[f] == c ? neighbour[f] : owner[f]);
-      }
-      if (nPer) cols.insert(cols.end(), extra[c].begin(), extra[c].end());
-      std::sort(cols.begin(), cols.end());
-      for (size_t k = 1; k < cols.size(); ++k)
-        if (cols[k] == cols[k - 1])
-          return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "fc_set_mesh: two cells coupled twice (an inner face and a "
-                                                      "periodic pair, or two faces)");
-      ia[c] = k0;
-      for (size_t k = 0; k < cols.size(); ++k) {
-        ja[k0 + k] = cols[k];
-        if (cols[k] == c) diag[c] = k0 + (int)k;
-      }
-      k0 += (int)cols.size();
-    }
-    ia[nC] = k0;
-    if (k0 != nnz) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_set_mesh: inconsistent face lists");
-    // csr_to_k (utils.f90:96-147): first slot of row icell holding jcell
-    auto csr_to_k = [&](int icell, int jcell) {
-      for (int l = ia[icell]; l < ia[icell + 1]; ++l)
-        if (ja[l] == jcell) return l;
-      return -1;
-    };
-    for (int f = 0; f < nI; ++f) {
-      ijk[f] = csr_to_k(owner[f], neighbour[f]);
-      jik[f] = csr_to_k(neighbour[f], owner[f]);
-    }
-    for (int q = 0; q < nPer; ++q) {  // sparse_matrix.f90:262-292
-      const int ijp = owner[pface[q]], ijn = owner[ptwin[q]];
-      ijk[nI + q] = csr_to_k(ijp, ijn);
-      jik[nI + q] = csr_to_k(ijn, ijp);
-    }
+  if (nPer > 0) {
+    UP(m.pface, pface.data(), nPer);
+    UP(m.ptwin, ptwin.data(), nPer);
   }
-  UP(m.ijk, ijk.data(), ijk.size());
-  UP(m.jik, jik.data(), jik.size());
+  FC_TRY(clk.lap(FC_SETUP_PERIODIC));
+  // CSR pattern and slot maps on the device (the kernels above); a cell
+  // pair coupled twice (an inner face and a periodic pair, or two faces)
+  // would make a repeated column, which is rejected
+  const int nL = nI + nPer;
+  if (2LL * nL + nC >= (1LL << 31)) return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "fc_set_mesh: nnz >= 2^31");
+  const int nnz = 2 * nL + nC;
+  const int nb = (nC + 1 + SCAN_TB - 1) / SCAN_TB;
+  std::vector<int> ia(nC + 1), ja(nnz), diag(nC);
+  {
+    DVec<int> cnt, bsum, d_ia, d_ja, d_dg, flag;
+    FC_CUDA_TRY(ctx, cnt.alloc(nC));
+    FC_CUDA_TRY(ctx, bsum.alloc(nb));
+    FC_CUDA_TRY(ctx, d_ia.alloc(nC + 1));
+    FC_CUDA_TRY(ctx, d_ja.alloc(nnz));
+    FC_CUDA_TRY(ctx, d_dg.alloc(nC));
+    FC_CUDA_TRY(ctx, flag.alloc(1));
+    FC_CUDA_TRY(ctx, m.ijk.alloc(std::max(1, nL)));
+    FC_CUDA_TRY(ctx, m.jik.alloc(std::max(1, nL)));
+    FC_CUDA_TRY(ctx, fc_zero(ctx->stream, cnt.p, cnt.bytes()));
+    FC_CUDA_TRY(ctx, fc_zero(ctx->stream, flag.p, flag.bytes()));
+    const int* pf = nPer ? m.pface.p : nullptr;
+    const int* pt = nPer ? m.ptwin.p : nullptr;
+    if (nL > 0) k_csr_count<<<grid(nL), TB, 0, ctx->stream>>>(nL, nI, m.owner.p, m.neighbour.p, pf, pt, cnt.p);
+    k_csr_scan_rows<<<nb, SCAN_TB, 0, ctx->stream>>>(nC, cnt.p, d_ia.p, bsum.p);
+    k_csr_scan_totals<<<1, SCAN_TB, 0, ctx->stream>>>(nb, bsum.p);
+    k_csr_scan_add<<<nb, SCAN_TB, 0, ctx->stream>>>(nC, bsum.p, d_ia.p);
+    FC_CUDA_TRY(ctx, fc_zero(ctx->stream, cnt.p, cnt.bytes()));
+    k_csr_fill<<<grid(std::max(nC, nL)), TB, 0, ctx->stream>>>(nC, nL, nI, m.owner.p, m.neighbour.p, pf, pt, d_ia.p,
+                                                               cnt.p, d_ja.p);
+    k_csr_sort<<<grid(nC), TB, 0, ctx->stream>>>(nC, d_ia.p, d_ja.p, d_dg.p, flag.p);
+    if (nL > 0)
+      k_csr_slots<<<grid(nL), TB, 0, ctx->stream>>>(nL, nI, m.owner.p, m.neighbour.p, pf, pt, d_ia.p, d_ja.p,
+                                                    m.ijk.p, m.jik.p);
+    ctx->kernel_launches += 6 + 2 * (nL > 0);
+    FC_CUDA_TRY(ctx, cudaGetLastError());
+    int hflag = 0;
+    FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, &hflag, flag.p, sizeof(int)));
+    if (hflag)
+      return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "fc_set_mesh: two cells coupled twice (an inner face and a "
+                                                  "periodic pair, or two faces)");
+    FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, ia.data(), d_ia.p, ia.size() * sizeof(int)));
+    FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, ja.data(), d_ja.p, ja.size() * sizeof(int)));
+    FC_CUDA_TRY(ctx, fc_d2h(ctx->stream, diag.data(), d_dg.p, diag.size() * sizeof(int)));
+  }
+  if (ia[nC] != nnz) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "fc_set_mesh: inconsistent face lists");
+  FC_TRY(clk.lap(FC_SETUP_CSR));
   if (nPer > 0) {
     // the assembly lists: a twin face leaves its cell's list, the pair
     // enters the twin-side cell's list at the periodic face's place
@@ -407,15 +575,13 @@ extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
     }
     UP(m.af_ptr, af_ptr.data(), af_ptr.size());
     UP(m.af_ent, af_ent.data(), af_ent.size());
-    UP(m.pface, pface.data(), nPer);
-    UP(m.ptwin, ptwin.data(), nPer);
     UP(m.ppos, ppos.data(), nPer);
     UP(m.pflag, pflag.data(), nPer);
   }
   UP(m.bpair, bpair.data(), nB);
   m.h_owner = owner;
   m.h_neighbour = neighbour;
-  FC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  FC_TRY(clk.lap(FC_SETUP_PERIODIC));
   // the global matrix system of the mesh (module globals ia, ja, a, diag)
   CsrSystem* s = new CsrSystem();
   std::vector<int> ia1(ia), ja1(ja), dg1(diag);
@@ -428,7 +594,18 @@ extern "C" int fc_set_mesh(fc_ctx* ctx, const fc_mesh* hm) {
   ctx->sys_mesh = s;
   ctx->has_mesh = true;
   ctx->mesh_gen++;
-  return fc_fields_alloc(ctx);
+  FC_TRY(clk.lap(FC_SETUP_ANALYSIS));
+  ctx->setup_s[FC_SETUP_TILING] = s->t_tiling;
+  ctx->setup_s[FC_SETUP_SCHEDULE] = s->t_schedule;
+  ctx->setup_s[FC_SETUP_ANALYSIS] = std::max(0.0, ctx->setup_s[FC_SETUP_ANALYSIS] - s->t_tiling - s->t_schedule);
+  FC_TRY(fc_fields_alloc(ctx));
+  return clk.lap(FC_SETUP_FIELDS);
+}
+
+extern "C" int fc_get_setup_times(fc_ctx* ctx, double* seconds) {
+  if (!ctx || !seconds) return FC_ERR_BAD_INPUT;
+  for (int k = 0; k < FC_SETUP_PHASES; ++k) seconds[k] = ctx->setup_s[k];
+  return FC_OK;
 }
 
 // geometry arrays back to the host (FC_GEO_* selects; length by kind)

@@ -720,12 +720,17 @@ __global__ void k_conterr(MeshView M, Dev D, double* __restrict__ part) {
   }
 }
 
+// warp j sums the block partials of quantity j in a fixed order (lane l
+// takes blocks l, l+32, ..., then a shuffle tree), so the sum is the same
+// on every run; one thread per quantity looping over the partials took a
+// thousand dependent loads
 __global__ void k_conterr_final(const double* __restrict__ part, int nb, double* __restrict__ out) {
-  if (threadIdx.x < 3) {
-    double t = 0.0;
-    for (int b = 0; b < nb; ++b) t += part[threadIdx.x * nb + b];
-    out[threadIdx.x] = t;
-  }
+  const int j = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (j >= 3) return;
+  double t = 0.0;
+  for (int b = lane; b < nb; b += 32) t += part[j * nb + b];
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if (lane == 0) out[j] = t;
 }
 
 // inner-face mass flux from the face-interpolated velocity, init.f90:167-176
@@ -805,11 +810,13 @@ __global__ void k_sum_cells(const double* __restrict__ x, int nC, double* __rest
 }
 
 // the block sums into part[nb] (one thread, fixed order)
+// the block partials summed by one warp in a fixed order (as k_conterr_final)
 __global__ void k_sum_final(double* __restrict__ part, int nb) {
-  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
   double s = 0.0;
-  for (int b = 0; b < nb; ++b) s += part[b];
-  part[nb] = s;
+  for (int b = threadIdx.x; b < nb; b += 32) s += part[b];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (threadIdx.x == 0) part[nb] = s;
 }
 
 // p = (1 - urfP) p + urfP (pp - pavg), pavg = sum(pp)/numCells (:361-363)
@@ -1727,7 +1734,7 @@ static int continuity_errors(fc_ctx* ctx, const Dev& D, double* resor4) {
   FC_CUDA_TRY(ctx, S.part.alloc((size_t)3 * nb));
   FC_CUDA_TRY(ctx, S.out.alloc(3));
   k_conterr<<<nb, 256, 0, ctx->stream>>>(M, D, S.part.p);
-  k_conterr_final<<<1, 32, 0, ctx->stream>>>(S.part.p, nb, S.out.p);
+  k_conterr_final<<<1, 96, 0, ctx->stream>>>(S.part.p, nb, S.out.p);
   ctx->kernel_launches += 2;
   double h[3];
   FC_CUDA_TRY(ctx, cudaMemcpyAsync(h, S.out.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -807,6 +808,10 @@ int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, c
   // chosen among a few candidates by the critical-path estimate
   const int sms = std::max(1, ctx->num_sms);
   int tiles = sms;
+  auto t0 = std::chrono::steady_clock::now();
+  auto since = [](std::chrono::steady_clock::time_point a) {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
+  };
   if (tiles_req > 0) {
     tiles = std::min(tiles_req, sms);
     s->est_sweep_us = 0.0;
@@ -815,6 +820,8 @@ int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, c
     tiles = pick_sweep_tiles(n, ia.data(), ja.data(), dg.data(), xyz, cand, FC_SWEEP_TAU0_US, FC_SWEEP_ROW_US,
                              FC_SWEEP_HOP_US, &s->est_sweep_us);
   }
+  s->t_tiling = since(t0);
+  t0 = std::chrono::steady_clock::now();
   OrderedSweep O;
   SweepSchedule S;
   std::string err;
@@ -828,6 +835,7 @@ int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, c
     wmax = wmax ? wmax / 2 : std::max(32, O.maxW / 2);
     if (wmax < 32) return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "sweep steps too wide for shared memory");
   }
+  s->t_schedule = since(t0);
   int st2 = upload_ordered(ctx, O, s->ord);
   if (st2) return st2;
   FC_CUDA_TRY(ctx, s->ia.alloc(n + 1));

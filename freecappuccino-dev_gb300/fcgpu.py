@@ -106,6 +106,7 @@ def lib():
         "fc_set_mesh": (i, [vp, vp]),
         "fc_get_geometry": (i, [vp, cp, vp]),
         "fc_get_csr_pattern": (i, [vp, vp, vp, vp, vp, vp, vp, vp]),
+        "fc_get_setup_times": (i, [vp, vp]),
         "fc_field_set": (i, [vp, cp, vp, C.c_longlong]),
         "fc_field_get": (i, [vp, cp, vp, C.c_longlong]),
         "fc_field_fill": (i, [vp, cp, d]),
@@ -580,6 +581,14 @@ class Context:
         self._check(self.L.fc_get_csr_pattern(self.h, None, None, _ptr(ia), _ptr(ja), _ptr(dg), _ptr(ijk), _ptr(jik)),
                     "fc_get_csr_pattern")
         return ia, ja, dg, ijk[:nl], jik[:nl]
+
+    SETUP_PHASES = ("topology", "geometry", "periodic", "csr", "tiling", "schedule", "analysis", "fields")
+
+    def setup_times(self):
+        """Seconds of the phases of the last set_mesh (fc_get_setup_times)."""
+        t = np.zeros(len(self.SETUP_PHASES))
+        self._check(self.L.fc_get_setup_times(self.h, _ptr(t)), "fc_get_setup_times")
+        return dict(zip(self.SETUP_PHASES, t.tolist()))
 
     def field_len(self, name):
         m = self.mesh

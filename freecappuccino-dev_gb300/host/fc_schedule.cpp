@@ -4,7 +4,9 @@
 
 #include <algorithm>
 #include <deque>
+#include <limits>
 #include <numeric>
+#include <set>
 #include <thread>
 #include <utility>
 
@@ -20,10 +22,12 @@ struct Deps {
 }  // namespace
 
 // recursive coordinate bisection of items (chains) weighted by rows into
-// nparts parts; split along the axis of largest extent at the weighted median
+// nparts parts; split along the axis of largest extent at the weighted
+// median.  The two halves of the first levels are cut concurrently (they
+// write disjoint entries of part_of).
 static void rcb(std::vector<int>& items, const std::vector<double>& cx, const std::vector<double>& cy,
                 const std::vector<double>& cz, const std::vector<int>& w, int nparts, int first_part,
-                std::vector<int>& part_of) {
+                std::vector<int>& part_of, int depth = 0) {
   if (nparts <= 1 || items.size() <= 1) {
     for (int c : items) part_of[c] = first_part;
     return;
@@ -37,7 +41,12 @@ static void rcb(std::vector<int>& items, const std::vector<double>& cx, const st
   for (int a = 1; a < 3; ++a)
     if (hi[a] - lo[a] > hi[ax] - lo[ax]) ax = a;
   const std::vector<double>& key = ax == 0 ? cx : ax == 1 ? cy : cz;
-  std::stable_sort(items.begin(), items.end(), [&](int a, int b) { return key[a] < key[b]; });
+  // stable sort by the coordinate, on (key, item) pairs kept together
+  std::vector<std::pair<double, int>> kv(items.size());
+  for (size_t q = 0; q < items.size(); ++q) kv[q] = {key[items[q]], items[q]};
+  std::stable_sort(kv.begin(), kv.end(),
+                   [](const std::pair<double, int>& a, const std::pair<double, int>& b) { return a.first < b.first; });
+  for (size_t q = 0; q < kv.size(); ++q) items[q] = kv[q].second;
   const int nl = nparts / 2;
   long long tot = 0;
   for (int c : items) tot += w[c];
@@ -54,15 +63,40 @@ static void rcb(std::vector<int>& items, const std::vector<double>& cx, const st
     const long long dist = acc > want ? acc - want : want - acc;
     if (best_dist < 0 || dist < best_dist) { best_dist = dist; best_near = q; }
     if (dist <= tol) {
-      const double gap = key[items[q]] - key[items[q - 1]];
+      const double gap = kv[q].first - kv[q - 1].first;
       if (gap > best_gap) { best_gap = gap; cut = q; }
     }
   }
   if (cut == 0) cut = best_near;
   cut = std::max<size_t>(1, std::min(cut, items.size() - 1));
   std::vector<int> left(items.begin(), items.begin() + cut), right(items.begin() + cut, items.end());
-  rcb(left, cx, cy, cz, w, nl, first_part, part_of);
-  rcb(right, cx, cy, cz, w, nparts - nl, first_part + nl, part_of);
+  kv.clear();
+  kv.shrink_to_fit();
+  if (depth < 3 && items.size() > 4096) {
+    std::thread th([&]() { rcb(left, cx, cy, cz, w, nl, first_part, part_of, depth + 1); });
+    rcb(right, cx, cy, cz, w, nparts - nl, first_part + nl, part_of, depth + 1);
+    th.join();
+  } else {
+    rcb(left, cx, cy, cz, w, nl, first_part, part_of, depth + 1);
+    rcb(right, cx, cy, cz, w, nparts - nl, first_part + nl, part_of, depth + 1);
+  }
+}
+
+// runs body(lo, hi) over [0, n) in contiguous chunks on up to
+// hardware_concurrency threads
+template <class F>
+static void parallel_chunks(int n, F body) {
+  const int nt = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), std::max(1, n / 4)));
+  if (nt <= 1) {
+    body(0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int k = 0; k < nt; ++k) {
+    const int lo = (int)((long long)n * k / nt), hi = (int)((long long)n * (k + 1) / nt);
+    th.emplace_back([&body, lo, hi]() { body(lo, hi); });
+  }
+  for (std::thread& t : th) t.join();
 }
 
 void build_sweep_schedule(int n, const int* ia, const int* ja, const int* dg, const std::vector<int>& lev, int nlev,
@@ -95,21 +129,26 @@ void build_sweep_schedule(int n, const int* ia, const int* ja, const int* dg, co
     }
   }
   const int nch = (int)chain_first.size();
-  // ---- 2. chain graph (undirected adjacency through dependencies)
-  std::vector<std::pair<int, int>> edges;
-  edges.reserve((size_t)n * 2);
-  for (int i = 0; i < n; ++i)
-    for (int k = D.begin(i); k < D.end(i); ++k) {
-      const int a = chain_of[i], b = chain_of[ja[k]];
-      if (a != b) { edges.push_back({a, b}); edges.push_back({b, a}); }
-    }
-  std::sort(edges.begin(), edges.end());
-  edges.erase(std::unique(edges.begin(), edges.end()), edges.end());
-  std::vector<int> adj_ptr(nch + 1, 0), adj;
-  for (auto& e : edges) adj_ptr[e.first + 1]++;
-  for (int c = 0; c < nch; ++c) adj_ptr[c + 1] += adj_ptr[c];
-  adj.resize(edges.size());
-  for (size_t q = 0; q < edges.size(); ++q) adj[q] = edges[q].second;  // sorted by (first, second)
+  // ---- 2. chain graph (undirected adjacency through dependencies), built
+  //         only where the tiles are grown or merged over it: the coordinate
+  //         bisection gives at most the target count by itself
+  std::vector<int> adj_ptr, adj;
+  auto chain_graph = [&]() {
+    std::vector<std::pair<int, int>> edges;
+    edges.reserve((size_t)n * 2);
+    for (int i = 0; i < n; ++i)
+      for (int k = D.begin(i); k < D.end(i); ++k) {
+        const int a = chain_of[i], b = chain_of[ja[k]];
+        if (a != b) { edges.push_back({a, b}); edges.push_back({b, a}); }
+      }
+    std::sort(edges.begin(), edges.end());
+    edges.erase(std::unique(edges.begin(), edges.end()), edges.end());
+    adj_ptr.assign(nch + 1, 0);
+    for (auto& e : edges) adj_ptr[e.first + 1]++;
+    for (int c = 0; c < nch; ++c) adj_ptr[c + 1] += adj_ptr[c];
+    adj.resize(edges.size());
+    for (size_t q = 0; q < edges.size(); ++q) adj[q] = edges[q].second;  // sorted by (first, second)
+  };
   // ---- 3. tiles: grow regions over the chain graph in breadth-first order
   const int T = std::max(1, std::min(ntiles_target, nch));
   const long long target = (n + T - 1) / T;
@@ -136,6 +175,7 @@ void build_sweep_schedule(int n, const int* ia, const int* ja, const int* dg, co
     tile_rows.assign(m, 0);
     for (int c = 0; c < nch; ++c) tile_rows[tile_of_chain[c]] += chain_rows[c];
   } else {
+    chain_graph();
     std::deque<int> q;
     int next_seed = 0;
     while (true) {
@@ -164,6 +204,7 @@ void build_sweep_schedule(int n, const int* ia, const int* ja, const int* dg, co
   // every chain now has a tile; merge the smallest tiles until at most T remain
   int ntiles = (int)tile_rows.size();
   if (ntiles > T) {
+    if (adj_ptr.empty()) chain_graph();
     std::vector<int> remap(ntiles);
     std::iota(remap.begin(), remap.end(), 0);
     auto find = [&](int x) { while (remap[x] != x) x = remap[x] = remap[remap[x]]; return x; };
@@ -213,30 +254,56 @@ void build_sweep_schedule(int n, const int* ia, const int* ja, const int* dg, co
   std::vector<std::vector<int>> tile_chains(ntiles);
   for (int c = 0; c < nch; ++c) tile_chains[tile_of_chain[c]].push_back(c);
   std::vector<int> slot_of_chain(nch, 0);
-  std::vector<std::vector<int>> tile_levels(ntiles);
   std::vector<int> row_tile(n), row_step(n), row_slot(n);
-  {
-    for (int t = 0; t < ntiles; ++t) {
+  // slots, tile by tile (concurrently): the chains in order of their first
+  // level each take the free slot (its last chain ended before that level)
+  // that was freed last, the lowest such slot on ties, else a new slot; the
+  // free slots are kept ordered by (level after which free, -slot)
+  S.tile_slots.assign(ntiles, 1);
+  parallel_chunks(ntiles, [&](int t0, int t1) {
+    for (int t = t0; t < t1; ++t) {
       auto& ch = tile_chains[t];
       std::sort(ch.begin(), ch.end(), [&](int a, int b) {
         return chain_lo[a] != chain_lo[b] ? chain_lo[a] < chain_lo[b] : a < b;
       });
-      std::vector<int> slot_free;  // level after which the slot is free
+      std::set<std::pair<int, int>> slot_free;
+      int nslots = 0;
       for (int c : ch) {
-        int s = -1;
-        for (size_t q = 0; q < slot_free.size(); ++q)
-          if (slot_free[q] < chain_lo[c] && (s < 0 || slot_free[q] > slot_free[s])) s = (int)q;
-        if (s < 0) { s = (int)slot_free.size(); slot_free.push_back(-1); }
-        slot_free[s] = chain_hi[c];
-        slot_of_chain[c] = s;
+        auto it = slot_free.lower_bound({chain_lo[c], std::numeric_limits<int>::min()});
+        int sl;
+        if (it != slot_free.begin()) {
+          --it;
+          sl = -it->second;
+          slot_free.erase(it);
+        } else {
+          sl = nslots++;
+        }
+        slot_free.insert({chain_hi[c], -sl});
+        slot_of_chain[c] = sl;
       }
-      S.tile_slots.push_back(std::max(1, (int)slot_free.size()));
-      S.max_slots = std::max(S.max_slots, S.tile_slots.back());
+      S.tile_slots[t] = std::max(1, nslots);
     }
-    for (int i = 0; i < n; ++i) {
-      const int t = tile_of_chain[chain_of[i]];
-      tile_levels[t].push_back(lev[i]);
+  });
+  for (int t = 0; t < ntiles; ++t) S.max_slots = std::max(S.max_slots, S.tile_slots[t]);
+  // the distinct levels of every tile, ascending: marked in a (tile, level)
+  // table that then maps a row's level to its step, or sorted per tile when
+  // that table would be large
+  std::vector<std::vector<int>> tile_levels(ntiles);
+  const size_t tab_cells = (size_t)ntiles * (size_t)std::max(1, nlev);
+  std::vector<int> step_tab;
+  if (tab_cells <= ((size_t)1 << 24)) {
+    step_tab.assign(tab_cells, -1);
+    for (int i = 0; i < n; ++i) step_tab[(size_t)tile_of_chain[chain_of[i]] * nlev + lev[i]] = -2;
+    for (int t = 0; t < ntiles; ++t) {
+      int* tab = step_tab.data() + (size_t)t * nlev;
+      for (int l = 0; l < nlev; ++l)
+        if (tab[l] == -2) {
+          tab[l] = (int)tile_levels[t].size();
+          tile_levels[t].push_back(l);
+        }
     }
+  } else {
+    for (int i = 0; i < n; ++i) tile_levels[tile_of_chain[chain_of[i]]].push_back(lev[i]);
     for (int t = 0; t < ntiles; ++t) {
       auto& L = tile_levels[t];
       std::sort(L.begin(), L.end());
@@ -256,11 +323,16 @@ void build_sweep_schedule(int n, const int* ia, const int* ja, const int* dg, co
       S.step_row_ptr[gs + 1] = S.step_row_ptr[gs] + S.tile_slots[t];
     }
   S.rows.assign(S.step_row_ptr[nsteps], -1);
-  // place every row (per tile level -> step lookup by binary search)
+  // place every row (its tile's level -> step from the table, else by binary search)
   for (int i = 0; i < n; ++i) {
     const int t = tile_of_chain[chain_of[i]];
-    const auto& L = tile_levels[t];
-    const int s = (int)(std::lower_bound(L.begin(), L.end(), lev[i]) - L.begin());
+    int s;
+    if (!step_tab.empty()) {
+      s = step_tab[(size_t)t * nlev + lev[i]];
+    } else {
+      const auto& L = tile_levels[t];
+      s = (int)(std::lower_bound(L.begin(), L.end(), lev[i]) - L.begin());
+    }
     const int slot = slot_of_chain[chain_of[i]];
     row_tile[i] = t;
     row_step[i] = s;
@@ -420,13 +492,23 @@ static int split_wide_levels(int n, const int* ia, const int* ja, const int* dg,
     }
     if (maxc == 0) break;
     const long long M = maxc + 1;
-    std::vector<long long> key(n);
-    for (int i = 0; i < n; ++i) key[i] = (long long)lev[i] * M + chunk[i];
-    std::vector<long long> uk(key);
-    std::sort(uk.begin(), uk.end());
-    uk.erase(std::unique(uk.begin(), uk.end()), uk.end());
-    for (int i = 0; i < n; ++i) lev[i] = (int)(std::lower_bound(uk.begin(), uk.end(), key[i]) - uk.begin());
-    nlev = (int)uk.size();
+    if ((long long)nlev * M <= (1LL << 26)) {
+      // dense ranks of the keys lev * M + chunk through a table of all keys
+      std::vector<int> rank((size_t)nlev * M, 0);
+      for (int i = 0; i < n; ++i) rank[(size_t)lev[i] * M + chunk[i]] = 1;
+      int r = 0;
+      for (int& v : rank) v = v ? r++ : -1;
+      for (int i = 0; i < n; ++i) lev[i] = rank[(size_t)lev[i] * M + chunk[i]];
+      nlev = r;
+    } else {
+      std::vector<long long> key(n);
+      for (int i = 0; i < n; ++i) key[i] = (long long)lev[i] * M + chunk[i];
+      std::vector<long long> uk(key);
+      std::sort(uk.begin(), uk.end());
+      uk.erase(std::unique(uk.begin(), uk.end()), uk.end());
+      for (int i = 0; i < n; ++i) lev[i] = (int)(std::lower_bound(uk.begin(), uk.end(), key[i]) - uk.begin());
+      nlev = (int)uk.size();
+    }
   }
   return nlev;
 }
@@ -451,7 +533,11 @@ bool build_ordered_sweep(int n, const int* ia, const int* ja, const int* dg, con
   O.tile_W.assign(T, 1);
   O.perm.reserve(n);
   O.iperm.assign(n, -1);
-  std::vector<int> row_tile(n), row_ls(n), row_pos(n);
+  // per old row: new index, tile, step within the tile, position in the
+  // step, kept together so that a dependency costs one cache line
+  struct RowInfo { int q, tile, ls, pos; };
+  std::vector<RowInfo> rinfo(n);
+  std::vector<int> row_tile(n), row_ls(n);
   for (int t = 0; t < T; ++t) {
     O.max_tile_steps = std::max(O.max_tile_steps, S.tile_step_ptr[t + 1] - S.tile_step_ptr[t]);
     for (int gs = S.tile_step_ptr[t]; gs < S.tile_step_ptr[t + 1]; ++gs) {
@@ -464,7 +550,7 @@ bool build_ordered_sweep(int n, const int* ia, const int* ja, const int* dg, con
         O.perm.push_back(i);
         row_tile[i] = t;
         row_ls[i] = gs - S.tile_step_ptr[t];
-        row_pos[i] = pos++;
+        rinfo[i] = {O.iperm[i], t, row_ls[i], pos++};
       }
       O.tile_W[t] = std::max(O.tile_W[t], pos);
     }
@@ -479,7 +565,8 @@ bool build_ordered_sweep(int n, const int* ia, const int* ja, const int* dg, con
   std::vector<int> row_step(n);  // global step of every new row
   for (int gs = 0; gs < O.nsteps; ++gs)
     for (int q = O.step_ptr[gs]; q < O.step_ptr[gs + 1]; ++q) row_step[q] = gs;
-  for (int dirn = 0; dirn < 2; ++dirn) {
+  // the two triangles are independent: built concurrently
+  auto build_dir = [&](int dirn, std::string& derr) -> bool {
     OrderedDir& D = O.dir[dirn];
     D.ne.assign(nE, 0);
     D.slot.assign(E, -1);
@@ -496,8 +583,11 @@ bool build_ordered_sweep(int n, const int* ia, const int* ja, const int* dg, con
     D.ovf_slot.assign(novf, -1);
     D.ovf_code.assign(novf, 0);
     D.ovf_col.assign(novf, 0);
-    std::vector<int> nx(n, 0);                  // exchange slots of each consumer row
-    std::vector<std::vector<std::pair<int, int>>> cons(n);  // producer -> (consumer row, its m-th slot)
+    std::vector<int> nx(n, 0);  // exchange slots of each consumer row
+    // pushes in the order they arise (consumer row ascending, entries in CSR
+    // order): producer row, consumer row, the consumer's slot number; grouped
+    // by producer below (a counting sort keeps that order within a producer)
+    std::vector<int> push_src, push_dst, push_m;
     for (int q = 0; q < n; ++q) {
       const int i = O.perm[q], t = row_tile[i];
       const int nst = S.tile_step_ptr[t + 1] - S.tile_step_ptr[t];
@@ -506,19 +596,28 @@ bool build_ordered_sweep(int n, const int* ia, const int* ja, const int* dg, con
       const int k0 = dirn == 0 ? ia[i] : dg[i] + 1;
       int codes[FC_ELL] = {0, 0, 0, 0};
       for (int e = 0; e < D.ne[q]; ++e) {
-        const int k = k0 + e, j = ja[k], qj = O.iperm[j];
+        const int k = k0 + e, j = ja[k];
+        const RowInfo rj = rinfo[j];
+        const int qj = rj.q;
         int c;
-        if (row_tile[j] == t) {
-          const int pj = dirn == 0 ? row_ls[j] : nst - 1 - row_ls[j];
-          if (pj >= my) { err = "ordered sweep: dependency not before its consumer in the tile"; return false; }
-          if (my - pj <= O.R - 1) c = (pj % O.R) * W + row_pos[j];
+        if (rj.tile == t) {
+          const int pj = dirn == 0 ? rj.ls : nst - 1 - rj.ls;
+          if (pj >= my) { derr = "ordered sweep: dependency not before its consumer in the tile"; return false; }
+          if (my - pj <= O.R - 1) c = (pj % O.R) * W + rj.pos;
           else c = -1;
         } else {
           c = -1;
           D.cross_tile_entries++;
         }
-        if (c > 65534) { err = "ordered sweep: ring index does not fit 16 bits"; return false; }
-        if (c < 0) { cons[qj].push_back({q, nx[q]++}); D.pushed_entries++; } else D.ring_entries++;
+        if (c > 65534) { derr = "ordered sweep: ring index does not fit 16 bits"; return false; }
+        if (c < 0) {
+          push_src.push_back(qj);
+          push_dst.push_back(q);
+          push_m.push_back(nx[q]++);
+          D.pushed_entries++;
+        } else {
+          D.ring_entries++;
+        }
         if (e < FC_ELL) {
           D.slot[(size_t)e * nE + q] = k;
           D.col[(size_t)e * nE + q] = qj;
@@ -533,6 +632,20 @@ bool build_ordered_sweep(int n, const int* ia, const int* ja, const int* dg, con
       D.srec[4 * (size_t)q + 2] = codes[0] | (codes[1] << 16);
       D.srec[4 * (size_t)q + 3] = codes[2] | (codes[3] << 16);
     }
+    std::vector<int> cons_ptr(n + 1, 0), cons_q(push_src.size()), cons_m(push_src.size());
+    for (int qj : push_src) cons_ptr[qj + 1]++;
+    for (int q = 0; q < n; ++q) cons_ptr[q + 1] += cons_ptr[q];
+    {
+      std::vector<int> fill(cons_ptr.begin(), cons_ptr.end() - 1);
+      for (size_t u = 0; u < push_src.size(); ++u) {
+        const int o = fill[push_src[u]]++;
+        cons_q[o] = push_dst[u];
+        cons_m[o] = push_m[u];
+      }
+    }
+    std::vector<int>().swap(push_src);
+    std::vector<int>().swap(push_dst);
+    std::vector<int>().swap(push_m);
     // exchange blocks (consumer side) and push blocks (producer side), one
     // per step, each starting on a multiple of 4 elements
     D.xv_ptr.assign(O.nsteps + 1, 0);
@@ -544,24 +657,32 @@ bool build_ordered_sweep(int n, const int* ia, const int* ja, const int* dg, con
         xoff[q] = xs;
         poff[q] = ps;
         xs += nx[q];
-        ps += (int)cons[q].size();
+        ps += cons_ptr[q + 1] - cons_ptr[q];
       }
-      if (xs > 65535 || ps > (1 << 30)) { err = "ordered sweep: exchange block of a step too large"; return false; }
+      if (xs > 65535 || ps > (1 << 30)) { derr = "ordered sweep: exchange block of a step too large"; return false; }
       D.xv_ptr[gs + 1] = D.xv_ptr[gs] + ((xs + 3) & ~3);
       D.push_ptr[gs + 1] = D.push_ptr[gs] + ((ps + 3) & ~3);
     }
     D.push.assign(D.push_ptr[O.nsteps], 0);
     for (int q = 0; q < n; ++q) {
-      const int np = (int)cons[q].size();
-      if (nx[q] > 255 || np > 255) { err = "ordered sweep: more than 255 exchanged entries in a row"; return false; }
+      const int np = cons_ptr[q + 1] - cons_ptr[q];
+      if (nx[q] > 255 || np > 255) { derr = "ordered sweep: more than 255 exchanged entries in a row"; return false; }
       D.srec[4 * (size_t)q] = D.ne[q] | (np << 8) | (xoff[q] << 16);
       D.srec[4 * (size_t)q + 1] = poff[q];
       for (int m = 0; m < np; ++m) {
-        const int qc = cons[q][m].first, mc = cons[q][m].second;
+        const int qc = cons_q[cons_ptr[q] + m], mc = cons_m[cons_ptr[q] + m];
         D.push[D.push_ptr[row_step[q]] + poff[q] + m] = D.xv_ptr[row_step[qc]] + xoff[qc] + mc;
       }
     }
-  }
+    return true;
+  };
+  std::string err1;
+  bool ok1 = true;
+  std::thread th1([&]() { ok1 = build_dir(1, err1); });
+  const bool ok0 = build_dir(0, err);
+  th1.join();
+  if (!ok0) return false;
+  if (!ok1) { err = err1; return false; }
   // ---- DILU transpose slots of the lower entries, diagonal slots, matrix
   O.lo_tslot.assign(E, 0);
   O.lo_ovf_tslot.assign(O.dir[0].ovf_ptr[n], 0);

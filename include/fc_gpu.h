@@ -316,6 +316,25 @@ int fc_get_geometry(fc_ctx* ctx, const char* name, double* out);
  * (numInnerFaces + numPeriodic entries: inner faces, then the periodic pairs
  * in patch and face order), 1-based; any output may be NULL. */
 int fc_get_csr_pattern(fc_ctx* ctx, int* n, int* nnz, int* ia, int* ja, int* diag, int* ijk, int* jik);
+/* Wall-clock seconds of the phases of the last fc_set_mesh, in this order:
+ * FC_SETUP_TOPOLOGY (host checks, cell -> face lists, topology upload),
+ * FC_SETUP_GEOMETRY (device geometry), FC_SETUP_PERIODIC (face mapping),
+ * FC_SETUP_CSR (device CSR pattern and slot maps, with their download),
+ * FC_SETUP_TILING (the sweep tile count: trial schedules of the candidate
+ * counts), FC_SETUP_SCHEDULE (the schedule-ordered sweep structure, with
+ * every step-width cap tried), FC_SETUP_ANALYSIS (the rest of the pattern
+ * analysis: checks, transpose slots, level sets, uploads), FC_SETUP_FIELDS
+ * (field allocation).  seconds holds FC_SETUP_PHASES values. */
+#define FC_SETUP_TOPOLOGY 0
+#define FC_SETUP_GEOMETRY 1
+#define FC_SETUP_PERIODIC 2
+#define FC_SETUP_CSR 3
+#define FC_SETUP_TILING 4
+#define FC_SETUP_SCHEDULE 5
+#define FC_SETUP_ANALYSIS 6
+#define FC_SETUP_FIELDS 7
+#define FC_SETUP_PHASES 8
+int fc_get_setup_times(fc_ctx* ctx, double* seconds);
 
 /* Fields by the reference's variable names: "u","v","w","p","pp","vis","den","t"
  * (numTotal), "flmass" (numFaces), "visw" (number of wall faces), "su","sv",

@@ -184,3 +184,13 @@ def test_openfoam_dictionary_boundary(fc):
     b = m2.arrays()
     for k in ("bctype", "nfaces", "startFace", "owner", "neighbour"):
         np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+
+
+def test_setup_phase_names_match_the_header(fc):
+    """Context.setup_times() names the values of fc_get_setup_times in the
+    order of the header's FC_SETUP_* indices."""
+    import re
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "fc_gpu.h")
+    idx = {m.group(1).lower(): int(m.group(2)) for m in re.finditer(r"#define FC_SETUP_(\w+) (\d+)", open(inc).read())}
+    assert idx.pop("phases") == len(fc.Context.SETUP_PHASES)
+    assert {name: k for k, name in enumerate(fc.Context.SETUP_PHASES)} == idx

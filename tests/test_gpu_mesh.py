@@ -37,6 +37,31 @@ def test_csr_pattern_and_slot_maps_bit_exact(ctx, key):
         assert np.array_equal(v, oc.get_int(name)), name
 
 
+@pytest.mark.parametrize("key,dims", [("csr_hex", dict(nx=40, ny=30, nz=20)),
+                                      ("csr_tet", dict(nx=14, ny=12, nz=10, tets=True))])
+def test_csr_pattern_across_scan_blocks(ctx, key, dims):
+    """24,000 hexes and 10,080 tetrahedra: the row-length scan of the device
+    CSR build spans many blocks of 1024 rows."""
+    kw = dict(dims)
+    m, a, oc = mesh_case(key, kw.pop("nx"), kw.pop("ny"), kw.pop("nz"), **kw)
+    ctx.set_mesh(m)
+    ia, ja, dg, ijk, jik = ctx.csr_pattern()
+    for name, v in (("ia", ia), ("ja", ja), ("diag", dg), ("ijk", ijk), ("jik", jik)):
+        assert np.array_equal(v, oc.get_int(name)), name
+    t = ctx.setup_times()
+    assert set(t) == set(ctx.SETUP_PHASES) and min(t.values()) >= 0.0
+    assert t["csr"] > 0.0 and t["tiling"] > 0.0 and t["schedule"] > 0.0
+
+
+def test_cells_coupled_twice_are_rejected(ctx, fc):
+    """Two cells across x, periodic in x: the inner face and the periodic
+    pair couple the same two cells, which would repeat a CSR column."""
+    from periodic_cases import SIDES
+    m = fc.Mesh.box(2, 3, 3, 1.0, 1.0, 1.0, perturb=0.0, sides=SIDES)
+    with pytest.raises(fc.FcError, match="coupled twice"):
+        ctx.set_mesh(m)
+
+
 @pytest.mark.parametrize("key", ["hex", "tet"])
 @pytest.mark.parametrize("scheme", [0, 1, 2, 4, 5])
 def test_gradients_bit_exact(ctx, key, scheme):

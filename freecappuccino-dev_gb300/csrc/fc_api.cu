@@ -386,6 +386,12 @@ extern "C" int fc_set_sweep_cap(fc_ctx* ctx, int rows) {
   return FC_OK;
 }
 
+extern "C" int fc_set_sweep_tiles(fc_ctx* ctx, int tiles) {
+  if (!ctx || tiles < 0) return FC_ERR_BAD_INPUT;
+  ctx->sweep_tiles = tiles;
+  return FC_OK;
+}
+
 extern "C" int fc_mixed_colours(fc_ctx* ctx, int which, int* ncol) {
   if (!ctx || !ncol) return FC_ERR_BAD_INPUT;
   CsrSystem* s = which ? ctx->sys_ext : ctx->sys_mesh;

@@ -215,6 +215,7 @@ struct fc_ctx {
   long long kernel_launches = 0;
   int tracing = 0, trace_blocks = 0, trace_cap = 0;
   int sweep_cap = 0;   // rows per sweep step cap of the next pattern analyses (0: as wide as fits)
+  int sweep_tiles = 0; // tile count of the next pattern analyses (0: the estimate's choice)
   std::FILE* solve_log = nullptr;  // JSON line per solve (fc_set_solve_log)
   int grad_limiter = 0;            // FC_LIMITER_* applied by every gradient (fc_set_gradient_limiter)
   DVec<double> limiter_part;       // min/max partials of the limiters

@@ -812,6 +812,7 @@ int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, c
   auto since = [](std::chrono::steady_clock::time_point a) {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
   };
+  if (tiles_req <= 0 && ctx->sweep_tiles > 0) tiles_req = ctx->sweep_tiles;
   if (tiles_req > 0) {
     tiles = std::min(tiles_req, sms);
     s->est_sweep_us = 0.0;

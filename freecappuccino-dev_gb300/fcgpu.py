@@ -118,6 +118,7 @@ def lib():
         "fc_sweep_stats": (i, [vp, i, vp]),
         "fc_mixed_colours": (i, [vp, i, vp]),
         "fc_set_sweep_cap": (i, [vp, i]),
+        "fc_set_sweep_tiles": (i, [vp, i]),
         "fc_set_tracing": (i, [vp, i]),
         "fc_trace_get": (i, [vp, vp, vp]),
         "fc_init_flmass": (i, [vp]),
@@ -663,6 +664,10 @@ class Context:
         keys = ("tiles", "levels", "max_width", "ring_depth", "est_sweep_us", "ring_entries", "pushed_entries",
                 "cross_tile_entries", "stages", "max_tile_steps")
         return dict(zip(keys, [float(v) for v in out]))
+
+    def set_sweep_tiles(self, tiles):
+        """Tile count of the pattern analyses that follow (0: the default)."""
+        self._check(self.L.fc_set_sweep_tiles(self.h, int(tiles)), "fc_set_sweep_tiles")
 
     def set_sweep_cap(self, rows):
         """Rows per sweep step cap of the next pattern analyses (0: default)."""

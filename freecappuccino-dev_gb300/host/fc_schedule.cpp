@@ -101,7 +101,7 @@ static void parallel_chunks(int n, F body) {
 
 void build_sweep_schedule(int n, const int* ia, const int* ja, const int* dg, const std::vector<int>& lev, int nlev,
                           bool forward, int ntiles_target, const double* xyz, SweepSchedule& S,
-                          std::vector<int>& code) {
+                          std::vector<int>& code, bool with_waits) {
   S = SweepSchedule();
   S.n = n;
   S.nlev = nlev;
@@ -339,13 +339,7 @@ void build_sweep_schedule(int n, const int* ia, const int* ja, const int* dg, co
     row_slot[i] = slot;
     S.rows[S.step_row_ptr[S.tile_step_ptr[t] + s] + slot] = i;
   }
-  S.kbne.assign(S.rows.size(), 0);
-  for (size_t q = 0; q < S.rows.size(); ++q) {
-    const int i = S.rows[q];
-    if (i < 0) continue;
-    const int kb = D.begin(i), ne = D.end(i) - kb;
-    S.kbne[q] = (kb << 4) | std::min(ne, 15);
-  }
+  if (!with_waits) return;
   // ---- 5. entry codes and waits
   std::vector<std::vector<std::pair<int, int>>> waits(nsteps);
   for (int i = 0; i < n; ++i) {
@@ -473,10 +467,10 @@ int symmetric_levels(int n, const int* ia, const int* ja, const int* dg, std::ve
 // passes).  Returns the number of levels.
 static int split_wide_levels(int n, const int* ia, const int* ja, const int* dg, int ntiles, const double* xyz,
                              int wmax, std::vector<int>& lev, int nlev) {
-  std::vector<int> code_tmp((size_t)ia[n], 0);
+  std::vector<int> code_tmp;  // not written by a layout-only build
   for (int pass = 0; pass < 8; ++pass) {
     SweepSchedule T;
-    build_sweep_schedule(n, ia, ja, dg, lev, nlev, true, ntiles, xyz, T, code_tmp);
+    build_sweep_schedule(n, ia, ja, dg, lev, nlev, true, ntiles, xyz, T, code_tmp, false);
     std::vector<int> chunk(n, 0);
     int maxc = 0;
     const int nsteps = T.tile_step_ptr[T.ntiles];

@@ -24,7 +24,6 @@ struct SweepSchedule {
   std::vector<int> tile_slots;     // rows per step (padded width) of each tile
   std::vector<int> step_row_ptr;   // offset of each global step's padded row list
   std::vector<int> rows;           // padded row ids, -1 = empty slot
-  std::vector<int> kbne;           // per padded slot: first swept CSR entry << 4 | min(entries, 15)
   std::vector<int> wait_ptr;       // per global step: waits [ptr[s], ptr[s+1])
   std::vector<int> wait_tile;      // producer tile of a wait
   std::vector<int> wait_level;     // producer must have published progress >= this level
@@ -41,9 +40,12 @@ struct SweepSchedule {
 // tiles be cut by recursive coordinate bisection of the chain centroids:
 // dependencies along the mesh then run one way between tiles, so tiles
 // pipeline instead of waiting on each other at every level.  Without
-// coordinates the tiles are grown over the chain graph.
+// coordinates the tiles are grown over the chain graph.  with_waits false
+// stops after the layout (tiles, steps, rows): code, the waits and the entry
+// counts are left empty.
 void build_sweep_schedule(int n, const int* ia, const int* ja, const int* dg, const std::vector<int>& lev, int nlev,
-                          bool forward, int ntiles, const double* xyz, SweepSchedule& S, std::vector<int>& code);
+                          bool forward, int ntiles, const double* xyz, SweepSchedule& S, std::vector<int>& code,
+                          bool with_waits = true);
 
 // Critical-path estimate (microseconds) of a schedule: per step tau0 +
 // per_row * rows, cross-tile waits delayed by hop after publication.

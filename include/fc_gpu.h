@@ -200,6 +200,12 @@ int fc_sweep_stats(fc_ctx* ctx, int which, double* out);
  * a mesh's widest step does not fit (e.g. 6 million tetrahedra).  Tuning and
  * testing only: no counterpart in the reference. */
 int fc_set_sweep_cap(fc_ctx* ctx, int rows);
+/* Sets the tile count (thread blocks of the ordered sweeps, at most one per
+ * SM) of the pattern analyses that follow; 0 restores the default, the
+ * candidate count with the smallest critical-path estimate.  The
+ * preconditioner and the iterates do not depend on it.  Tuning and testing
+ * only: no counterpart in the reference. */
+int fc_set_sweep_tiles(fc_ctx* ctx, int tiles);
 /* Appends one JSON line per solve to the file at path (NULL or "": stop):
  * the entry point, solver, variable, rows, precision mode, status,
  * iterations, refinement steps, early exit, res0 (L1), final residual,

@@ -156,6 +156,9 @@ def progress(msg):
     print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
 
 
+BATCH_TOL, BATCH_INNER_TOL, BATCH_INNER_ITMAX = 1e-6, 1e-4, 100  # C3b: BiCGStab to 1e-6; FP32 inner settings
+
+
 def batch_block(fc, args, dev):
     """C3b: independent steady convection-diffusion problems solved together.
     count problems (64, the configuration's count, by default): n^3
@@ -374,25 +377,29 @@ def cavity_fields(m, nT, nC):
     return a, u, nwal
 
 
-def simple_iterations(n=128, iters=4, perturb=PERTURB, dev=0):
+def simple_iterations(n=128, iters=4, perturb=PERTURB, dev=0, tets=False, viscos=0.01, scheme=1, grad=0,
+                      urf=(0.8, 0.3)):
     """`iters` FP64 SIMPLE iterations of the n^3 lid-driven cavity of the
-    SIMPLE leg (perturbed hexes, seed MESH_SEED): the command the kernel
-    launch lists and ncu captures of one SIMPLE iteration run, e.g.
-    python -c "import bench; bench.simple_iterations(128, 4)".  Returns the
-    last iteration's resor."""
+    SIMPLE leg (perturbed hexes, seed MESH_SEED; `tets` splits every hex into
+    6 tetrahedra): the command the kernel launch lists and ncu captures of
+    one SIMPLE iteration run, e.g.
+    python -c "import bench; bench.simple_iterations(128, 4)", or for the
+    6M-tet cavity of the C5 leg (Re 400, boundedLinearUpwind, LSQ gradients)
+    python -c "import bench; bench.simple_iterations(100, 3, tets=True, viscos=1/400, scheme=19, grad=1, urf=(0.6, 0.2))".
+    Returns the last iteration's resor."""
     fc = load_fc()
-    m = fc.Mesh.box(n, n, n, 1.0, 1.0, 1.0, perturb=perturb, seed=MESH_SEED)
+    m = fc.Mesh.box(n, n, n, 1.0, 1.0, 1.0, perturb=perturb, seed=MESH_SEED, tets=tets)
     nC, nT = m.numCells, m.numTotal
     _, u, nwal = cavity_fields(m, nT, nC)
     ctx = fc.Context(dev)
     ctx.set_mesh(m)
     zero = np.zeros(nT)
-    for k, v in dict(u=u, v=zero, w=zero, p=zero, pp=zero, den=np.ones(nT), vis=np.full(nT, 0.01)).items():
+    for k, v in dict(u=u, v=zero, w=zero, p=zero, pp=zero, den=np.ones(nT), vis=np.full(nT, viscos)).items():
         ctx.field_set(k, v)
-    ctx.field_set("visw", np.full(max(nwal, 1), 0.01))
+    ctx.field_set("visw", np.full(max(nwal, 1), viscos))
     for k in ("flmass", "a", "dUdxi", "dVdxi", "dWdxi", "dPdxi"):
         ctx.field_fill(k, 0.0)
-    ctx.simple_params(fc.SimpleParams.cavity(viscos=0.01))
+    ctx.simple_params(fc.SimpleParams.cavity(viscos=viscos, scheme=scheme, grad=grad, urfU=urf[0], urfP=urf[1]))
     ctx.init_flmass()
     r = None
     for _ in range(iters):
@@ -441,6 +448,69 @@ def turbulence_iterations(n=128, iters=3, dev=0):
         r = ctx.kw_sst()
     ctx.sync()
     print("turbulence_iterations", n, iters, "resor56", list(r), flush=True)
+    ctx.close()
+
+
+def batch_solves(count=64, mixed=False, dev=0):
+    """One batched BiCGStab(DILU) solve of the first `count` problems of the
+    C3b set (FP64, or with `mixed` the FP32-inner / FP64-refinement solve with
+    the bench's inner settings) after one untimed solve: the command of the
+    batched kernels' launch list and ncu captures, e.g.
+    python -c "import bench; bench.batch_solves(8)"."""
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from cd_cases import cd_batch_sizes, cd_batch_system
+    fc = load_fc()
+    ns, pe = cd_batch_sizes(count)
+    gen = fc.Context(dev)
+    probs = [cd_batch_system(fc, gen, int(n), float(q), MESH_SEED + k) for k, (n, q) in enumerate(zip(ns, pe))]
+    gen.close()
+    td = torch.device("cuda", dev)
+    da = [torch.from_numpy(p[3]).to(td) for p in probs]
+    db = [torch.from_numpy(p[4]).to(td) for p in probs]
+    dx = [torch.zeros(len(p[2]), dtype=torch.float64, device=td) for p in probs]
+    ctx = fc.Context(dev)
+    if mixed:
+        ctx.set_precision(fc.FC_PREC_MIXED, BATCH_INNER_TOL, BATCH_INNER_ITMAX)
+    B = fc.Batch(ctx)
+    for ia, ja, dg, a, b, xyz in probs:
+        B.add(ia, ja, dg, xyz)
+    B.plan()
+    for _ in range(2):
+        for x in dx:
+            x.zero_()
+        _, infos, st = B.solve(da, dx, db, 4000, 0.0, BATCH_TOL, raise_on_error=False)
+    ctx.sync()
+    print("batch_solves", count, "mixed" if mixed else "fp64", "status", st,
+          "iterations", [int(i.itr_used) for i in infos], flush=True)
+    B.close()
+    ctx.close()
+
+
+def adjoint_solves(n=96, calls=2, dev=0):
+    """`calls` rounds of the C4 adjoint on the n^3 mesh: assembly
+    (fc_cd_assemble), the forward BiCGStab(DILU) solve, the objective and the
+    adjoint (transposed solve and reverse face loop): the command of the
+    adjoint kernels' launch list and ncu captures, e.g.
+    python -c "import bench; bench.adjoint_solves(96, 2)"."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from cd_cases import TWO_PI, cd_inputs, cd_objective, cd_source
+    fc = load_fc()
+    m = fc.Mesh.box(n, n, n, TWO_PI, TWO_PI, TWO_PI, perturb=PERTURB, seed=MESH_SEED)
+    _, fm, gamma = cd_inputs(fc, m)
+    ctx = fc.Context(dev)
+    ctx.set_mesh(m)
+    ctx.field_set("flmass", fm)
+    xc, yc, zc = ctx.geometry("xc"), ctx.geometry("yc"), ctx.geometry("zc")
+    vol = ctx.geometry("vol")
+    src = cd_source(xc, yc, zc)
+    for _ in range(calls):
+        ctx.cd_assemble(gamma, src)
+        phi, finfo = ctx.cd_solve(2000, 1e-6)
+        J, g = cd_objective(phi, vol, xc)
+        lam, grad, ainfo = ctx.cd_adjoint(g, 2000, 1e-6)
+    ctx.sync()
+    print("adjoint_solves", n, calls, "J", J, "iterations", finfo.itr_used, ainfo.itr_used, flush=True)
     ctx.close()
 
 
@@ -1122,9 +1192,9 @@ def main():
     ap.add_argument("--turb-calls", type=int, default=5, help="timed fc_kw_sst calls there")
     ap.add_argument("--piso-steps", type=int, default=10, help="timed PISO time steps")
     ap.add_argument("--batch-count", type=int, default=64, help="problems of the batched leg (0: skip)")
-    ap.add_argument("--batch-tol", type=float, default=1e-6, help="relative L1 tolerance there")
-    ap.add_argument("--batch-inner-tol", type=float, default=1e-4, help="FP32 inner tolerance there")
-    ap.add_argument("--batch-inner-itmax", type=int, default=100, help="FP32 inner iteration cap there")
+    ap.add_argument("--batch-tol", type=float, default=BATCH_TOL, help="relative L1 tolerance there")
+    ap.add_argument("--batch-inner-tol", type=float, default=BATCH_INNER_TOL, help="FP32 inner tolerance there")
+    ap.add_argument("--batch-inner-itmax", type=int, default=BATCH_INNER_ITMAX, help="FP32 inner iteration cap there")
     ap.add_argument("--batch-reps", type=int, default=2, help="timed repetitions of each batched leg")
     ap.add_argument("--batch-tune-rounds", type=int, default=2, help="autotuner plans tried")
     ap.add_argument("--batch-cpu-seconds", type=float, default=10.0, help="oracle time of the CPU estimate")

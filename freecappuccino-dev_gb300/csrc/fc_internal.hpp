@@ -90,6 +90,7 @@ struct DevOrdered {
   int n = 0, nE = 0, ntiles = 0, nsteps = 0, nlev = 0, R = 4, K = 1, maxW = 0, max_tile_steps = 0;
   size_t stage_area = 0;             // shared memory of the sweeps' stage buffers; K: buffers of an application
   int xmax = 4, pmax = 4;            // largest exchange / push block of a step
+  bool gs_ok = false;                // the Gauss-Seidel mode gets two stage buffers
   int novf[2] = {0, 0}, nxv[2] = {0, 0};
   DVec<int> tile_step_ptr, step_ptr, tile_W, perm;
   DVec<int> srec[2], xv_ptr[2], push_ptr[2], push[2], slot[2], ucol;
@@ -127,6 +128,7 @@ struct CsrSystem {
   OrdStore<float> o32;
   double est_sweep_us = 0.0;         // critical-path estimate of the forward sweep
   double t_tiling = 0.0, t_schedule = 0.0;  // seconds of the tile-count choice and of the ordered sweep build
+  const double* xyz_src = nullptr;   // row coordinates the tiles were cut with (the mesh's, or none)
   DevColoured* mc = nullptr;         // built on the first FC_PREC_MIXED_COLOURED solve
   // workspace
   DVec<double> x, b, r, r0, p, u, z, v, d, w;
@@ -234,8 +236,10 @@ int fc_fail_msg(fc_ctx* ctx, int code, const std::string& msg);
 // xyz: optional row coordinates (3*n, x then y then z) used to cut the sweep tiles
 // tiles > 0: that many sweep tiles (at most one per SM) instead of the
 // count the critical-path estimate picks
+// with_gs: the Gauss-Seidel sweep mode must fit the staging too (else a
+// Gauss-Seidel solve analyses the pattern again with it)
 int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, const int* ja1, const int* diag1,
-                    const double* xyz = nullptr, int tiles = 0);
+                    const double* xyz = nullptr, int tiles = 0, bool with_gs = false);
 int sys_upload_values(fc_ctx* ctx, CsrSystem* s, const double* a, bool a_on_device);
 int sys_alloc_work(fc_ctx* ctx, CsrSystem* s);
 

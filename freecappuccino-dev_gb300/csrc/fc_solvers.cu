@@ -674,11 +674,12 @@ static size_t ordered_stage_area(int R, int maxW, int max_tile_steps) {
   return fixed >= (size_t)FC_SWEEP_SMEM ? 0 : ((size_t)FC_SWEEP_SMEM - fixed) & ~(size_t)15;
 }
 
-// stage buffers of every sweep mode at width maxW (the widest tile); the
-// smallest over the modes is the depth the schedule is checked against
-static int ordered_min_stages(size_t area, int maxW, int xmax, int pmax) {
+// stage buffers of the sweep modes up to last_mode at width maxW (the widest
+// tile); the smallest over the modes is the depth the schedule is checked
+// against.  The Gauss-Seidel mode (OS_GS, the last) stages the most per row.
+static int ordered_min_stages(size_t area, int maxW, int xmax, int pmax, int last_mode = OS_GS) {
   int kmin = FC_MAX_STAGES;
-  for (int m = OS_SETUP_DIC; m <= OS_GS; ++m) {
+  for (int m = OS_SETUP_DIC; m <= last_mode; ++m) {
     StageLayout L;
     L.init_for<double>(maxW, xmax, pmax, m);
     kmin = std::min(kmin, (size_t)L.bytes <= area ? stages_in(area, L.bytes) : 0);
@@ -696,20 +697,51 @@ static void ordered_blocks(const OrderedSweep& O, int& xmax, int& pmax) {
     }
 }
 
-// every sweep mode gets at least two stage buffers in the shared memory
-static bool ordered_fits(const OrderedSweep& O) {
+// The staging a structure needs: two stage buffers for every sweep mode the
+// solves use (the factor setups, the applications, Gauss-Seidel when
+// with_gs) and FC_APPLY_STAGES for the applications, which run every
+// iteration: with fewer the staging thread cannot run far enough ahead to
+// hide its copies (measured on 6M tetrahedra: steps of 616 rows with two
+// application stages took 222 ms per SIMPLE iteration, steps of 364 rows
+// with four 179 ms, despite 2,512 levels against 4,088).
+#define FC_APPLY_STAGES 4
+static int last_mode_of(bool with_gs) { return with_gs ? OS_GS : OS_BWD_DOT; }
+static bool staging_ok(size_t area, int maxW, int xmax, int pmax, bool with_gs) {
+  if (ordered_min_stages(area, maxW, xmax, pmax, last_mode_of(with_gs)) < 2) return false;
+  for (int m = OS_FWD; m <= OS_BWD_DOT; ++m) {
+    StageLayout L;
+    L.init_for<double>(maxW, xmax, pmax, m);
+    if ((size_t)L.bytes > area || stages_in(area, L.bytes) < FC_APPLY_STAGES) return false;
+  }
+  return true;
+}
+static bool ordered_fits(const OrderedSweep& O, bool with_gs) {
   int xmax, pmax;
   ordered_blocks(O, xmax, pmax);
-  return ordered_min_stages(ordered_stage_area(O.R, O.maxW, O.max_tile_steps), O.maxW, xmax, pmax) >= 2;
+  return staging_ok(ordered_stage_area(O.R, O.maxW, O.max_tile_steps), O.maxW, xmax, pmax, with_gs);
 }
 
-static int upload_ordered(fc_ctx* ctx, const OrderedSweep& O, DevOrdered& D) {
+// The widest step (a multiple of 32 rows, at most maxW) whose staging
+// would be enough with exchange and push blocks of three entries per row, the
+// most a capped step of the meshes measured needed, and the tile step
+// tables grown in proportion to the split; 0 if none.  The first cap tried
+// when a schedule does not fit, instead of halving the width.
+static int estimated_step_cap(int R, int maxW, int max_tile_steps, bool with_gs) {
+  for (int w = maxW & ~31; w >= 32; w -= 32) {
+    const int steps = (int)std::min<long long>(1LL << 24, (long long)max_tile_steps * ((maxW + w - 1) / w));
+    if (staging_ok(ordered_stage_area(R, w, steps), w, 3 * w, 3 * w, with_gs)) return w;
+  }
+  return 0;
+}
+
+static int upload_ordered(fc_ctx* ctx, const OrderedSweep& O, DevOrdered& D, bool with_gs) {
   D.n = O.n; D.nE = O.nE; D.ntiles = O.ntiles; D.nsteps = O.nsteps; D.nlev = O.nlev; D.R = O.R; D.maxW = O.maxW;
   D.max_tile_steps = O.max_tile_steps;
   ordered_blocks(O, D.xmax, D.pmax);
   D.stage_area = ordered_stage_area(D.R, D.maxW, D.max_tile_steps);
-  if (ordered_min_stages(D.stage_area, D.maxW, D.xmax, D.pmax) < 2)
+  if (ordered_min_stages(D.stage_area, D.maxW, D.xmax, D.pmax, last_mode_of(with_gs)) < 2)
     return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "sweep tiles too wide for shared memory");
+  D.gs_ok = ordered_min_stages(D.stage_area, D.maxW, D.xmax, D.pmax, OS_GS) >= 2;
   {
     // stages of the preconditioner application at the widest tile (sweep statistics)
     StageLayout L;
@@ -753,7 +785,7 @@ static int upload_ordered(fc_ctx* ctx, const OrderedSweep& O, DevOrdered& D) {
 }
 
 int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, const int* ja1, const int* diag1,
-                    const double* xyz, int tiles_req) {
+                    const double* xyz, int tiles_req, bool with_gs) {
   if (n <= 0 || nnz < n) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "csr pattern: n <= 0 or nnz < n");
   if (nnz >= (1 << 27)) return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "csr pattern: nnz >= 2^27");
   mc_release(s->mc);  // the multicolour layout belongs to the previous pattern
@@ -826,18 +858,24 @@ int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, c
   OrderedSweep O;
   SweepSchedule S;
   std::string err;
-  // the widest step must fit the shared-memory staging: if it does not, wide
-  // levels are split into narrower steps (more, shorter steps) until it does
+  // the widest step must fit the shared-memory staging of the modes the
+  // solves use (Gauss-Seidel only when with_gs; a Gauss-Seidel solve on a
+  // structure without it analyses the pattern again): if it does not, wide
+  // levels are split into narrower steps (more, shorter steps), first at the
+  // estimated widest cap that fits, then at 7/8 of the previous cap, until
+  // it does
   int wmax = ctx->sweep_cap > 0 ? ctx->sweep_cap : 0;
   for (;;) {
     if (!build_ordered_sweep(n, ia.data(), ja.data(), dg.data(), ts.data(), tiles, xyz, FC_RING, O, S, err, wmax))
       return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, err);
-    if (ordered_fits(O)) break;
-    wmax = wmax ? wmax / 2 : std::max(32, O.maxW / 2);
+    if (ordered_fits(O, with_gs)) break;
+    const int est = wmax ? 0 : estimated_step_cap(FC_RING, O.maxW, O.max_tile_steps, with_gs);
+    wmax = est > 0 ? est : (wmax ? (wmax * 7 / 8) & ~7 : std::max(32, O.maxW / 2));
     if (wmax < 32) return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "sweep steps too wide for shared memory");
   }
   s->t_schedule = since(t0);
-  int st2 = upload_ordered(ctx, O, s->ord);
+  s->xyz_src = xyz;
+  int st2 = upload_ordered(ctx, O, s->ord, with_gs);
   if (st2) return st2;
   FC_CUDA_TRY(ctx, s->ia.alloc(n + 1));
   FC_CUDA_TRY(ctx, s->ja.alloc(nnz));
@@ -1012,8 +1050,26 @@ static int fetch_out(fc_ctx* ctx, CsrSystem* s, SolveResult* res) {
   return FC_OK;
 }
 
+// A Gauss-Seidel solve on a structure whose steps are too wide for the
+// Gauss-Seidel staging: the pattern is analysed again with that mode in the
+// fit (narrower steps), on the same tiles and row coordinates.  The matrix
+// values and work vectors of the system stay in place.
+static int sys_reanalyse_for_gs(fc_ctx* ctx, CsrSystem* s) {
+  std::vector<int> ia1(s->h_ia), ja1(s->h_ja), dg1(s->h_diag);
+  for (auto& v : ia1) ++v;
+  for (auto& v : ja1) ++v;
+  for (auto& v : dg1) ++v;
+  const double* xyz = s->xyz_src;
+  if (xyz && !(ctx->has_mesh && xyz == ctx->mesh.h_xyz.data())) xyz = nullptr;  // the mesh it came from is gone
+  return sys_set_pattern(ctx, s, s->n, s->nnz, ia1.data(), ja1.data(), dg1.data(), xyz, s->ord.ntiles, true);
+}
+
 static int solve_fp64(fc_ctx* ctx, CsrSystem* s, const std::string& solver, const double* a, double* x,
                       const double* b, int itr_max, double tol_abs, double tol_rel, SolveResult* res) {
+  if (solver == "gauss-seidel" && !s->ord.gs_ok) {
+    const int st = sys_reanalyse_for_gs(ctx, s);
+    if (st) return st;
+  }
   KArgs<double> A = make_args<double>(s, a, x, b, s->r.p, s->r0.p, s->p.p, s->u.p, s->z.p, s->v.p, s->d.p,
                                       s->w.p, itr_max, tol_abs, tol_rel);
   const bool traced = ctx->tracing && solver == "iccg";

@@ -17,6 +17,16 @@ void fc_count_device_alloc() { g_device_allocs.fetch_add(1, std::memory_order_re
 
 extern "C" long long fc_device_alloc_count(void) { return g_device_allocs.load(std::memory_order_relaxed); }
 
+static std::atomic<int> g_alloc_fill{-1};
+
+int fc_alloc_fill() { return g_alloc_fill.load(std::memory_order_relaxed); }
+
+extern "C" int fc_debug_fill_allocations(int byte) {
+  if (byte < -1 || byte > 255) return FC_ERR_BAD_INPUT;
+  g_alloc_fill.store(byte, std::memory_order_relaxed);
+  return FC_OK;
+}
+
 int fc_fail(fc_ctx* ctx, int code, const char* what, cudaError_t e) {
   if (ctx) {
     ctx->last_error = std::string(what ? what : "");

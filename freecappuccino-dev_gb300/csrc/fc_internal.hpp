@@ -42,6 +42,8 @@ inline cudaError_t fc_zero(cudaStream_t s, void* dst, size_t bytes) {
 // Count of the library's device allocations and frees (every device buffer
 // goes through DVec), read by fc_device_alloc_count.
 void fc_count_device_alloc();
+// byte every new device allocation is filled with, or -1 (fc_debug_fill_allocations)
+int fc_alloc_fill();
 
 template <class T>
 struct DVec {
@@ -57,7 +59,17 @@ struct DVec {
     if (count == 0) return cudaSuccess;
     fc_count_device_alloc();
     cudaError_t e = cudaMalloc(&p, count * sizeof(T));
-    if (e == cudaSuccess) n = count; else p = nullptr;
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    n = count;
+    const int fill = fc_alloc_fill();
+    if (fill >= 0) {
+      // synchronous: done before any stream of the library can use the buffer
+      e = cudaMemset(p, fill, count * sizeof(T));
+      if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    }
     return e;
   }
   void release() {

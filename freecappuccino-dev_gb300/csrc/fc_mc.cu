@@ -262,11 +262,17 @@ __device__ __forceinline__ T ell_sum(const McDevT<T>& D, int e, int stride, int 
 template <class T>
 __global__ void k_mc_gather(McDevT<T> D, const int* __restrict__ perm, const double* __restrict__ r64, double tol,
                             int itmax) {
+  // t, w and q start at zero too: a padding entry of an ELLPACK block (value
+  // 0, column = its own row) reads the row's t or w before the iteration has
+  // written it, and 0 times uninitialised memory may be NaN
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < D.nP; i += gridDim.x * blockDim.x) {
     const int o = perm[i];
     D.r[i] = o >= 0 ? (T)r64[o] : T(0);
     D.x[i] = T(0);
     D.p[i] = T(0);
+    D.t[i] = T(0);
+    D.w[i] = T(0);
+    D.q[i] = T(0);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     McScal s;

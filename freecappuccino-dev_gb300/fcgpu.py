@@ -92,6 +92,7 @@ def lib():
         "fc_set_precision": (i, [vp, i, d, i]),
         "fc_kernel_launches": (C.c_longlong, [vp]),
         "fc_device_alloc_count": (C.c_longlong, []),
+        "fc_debug_fill_allocations": (i, [i]),
         "fc_stream_sync": (i, [vp]),
         "fc_stream": (vp, [vp]),
         "fc_event_record": (i, [vp, i]),
@@ -166,6 +167,14 @@ def lib():
 def device_alloc_count():
     """Device allocations plus frees the library has made so far."""
     return int(lib().fc_device_alloc_count())
+
+
+def debug_fill_allocations(byte):
+    """Fill every later device allocation with `byte` (-1: off); 0xFF makes
+    uninitialised floats and doubles NaN (fc_debug_fill_allocations)."""
+    st = lib().fc_debug_fill_allocations(int(byte))
+    if st < 0:
+        raise FcError(st, "fc_debug_fill_allocations")
 
 
 def declared_symbols(header=None):

@@ -140,6 +140,12 @@ long long fc_kernel_launches(const fc_ctx* ctx);  /* kernels launched so far by 
 /* device allocations plus frees made by the library so far, over all
  * contexts (a diagnostic: no reference counterpart) */
 long long fc_device_alloc_count(void);
+/* Fills every device allocation the library makes from now on with the byte
+ * value (0..255; -1, the default, leaves new memory as the allocator gives
+ * it), over all contexts.  0xFF makes every float and double NaN, so that a
+ * read of memory nothing has written shows up in the results.  Testing only:
+ * no reference counterpart. */
+int fc_debug_fill_allocations(int byte);
 int fc_stream_sync(fc_ctx* ctx);
 void* fc_stream(fc_ctx* ctx);                     /* the cudaStream_t every call is ordered on */
 int fc_event_record(fc_ctx* ctx, int which);      /* which: 0 start, 1 stop (on the context stream) */

@@ -417,5 +417,12 @@ extern "C" int fc_sweep_stats(fc_ctx* ctx, int which, double* out) {
   out[0] = D.ntiles; out[1] = D.nlev; out[2] = D.maxW; out[3] = D.R;
   out[4] = s->est_sweep_us; out[5] = (double)D.ring_entries; out[6] = (double)D.pushed_entries;
   out[7] = (double)D.cross_tile_entries; out[8] = D.K; out[9] = D.max_tile_steps;
+  out[10] = D.Wc;
+  return FC_OK;
+}
+
+extern "C" int fc_set_sweep_stage_rows(fc_ctx* ctx, int rows) {
+  if (!ctx || rows < 0) return FC_ERR_BAD_INPUT;
+  ctx->stage_rows = rows;
   return FC_OK;
 }

@@ -103,6 +103,7 @@ struct DevOrdered {
   size_t stage_area = 0;             // shared memory of the sweeps' stage buffers; K: buffers of an application
   int xmax = 4, pmax = 4;            // largest exchange / push block of a step
   bool gs_ok = false;                // the Gauss-Seidel mode gets two stage buffers
+  int Wc = 0;                        // staged rows of a step (0: whole steps are staged)
   int novf[2] = {0, 0}, nxv[2] = {0, 0};
   DVec<int> tile_step_ptr, step_ptr, tile_W, perm;
   DVec<int> srec[2], xv_ptr[2], push_ptr[2], push[2], slot[2], ucol;
@@ -230,6 +231,7 @@ struct fc_ctx {
   int tracing = 0, trace_blocks = 0, trace_cap = 0;
   int sweep_cap = 0;   // rows per sweep step cap of the next pattern analyses (0: as wide as fits)
   int sweep_tiles = 0; // tile count of the next pattern analyses (0: the estimate's choice)
+  int stage_rows = 0;  // staged rows of a step in the next pattern analyses (0: as many as fit; tests)
   std::FILE* solve_log = nullptr;  // JSON line per solve (fc_set_solve_log)
   int grad_limiter = 0;            // FC_LIMITER_* applied by every gradient (fc_set_gradient_limiter)
   DVec<double> limiter_part;       // min/max partials of the limiters

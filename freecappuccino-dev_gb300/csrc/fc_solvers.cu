@@ -187,19 +187,19 @@ __device__ bool ord_residual_l1(const KArgs<T>& A, int& ph, double& l1out) {
 // z = M^-1 q with the DIC/DILU factors d: forward sweep into yf, barrier,
 // backward sweep into z (linear_solvers.f90:458-475); dot (optional) gets
 // sum e_i z_i of the rows this thread finished.  No barrier at the end.
-template <class T, class TracerT>
+template <class T, bool WIDE, class TracerT>
 __device__ __forceinline__ bool precond_apply(const KArgs<T>& A, OsCtx& X, const T* q, T* yf, T* z, const T* e, double* dot,
                               TracerT* tr) {
   const OsIO<T> f{q, nullptr, yf};
-  if (!osweep<T, OS_FWD>(A.C, A.O, A.V, f, X, nullptr, tr)) return false;
+  if (!osweep<T, OS_FWD, WIDE>(A.C, A.O, A.V, f, X, nullptr, tr)) return false;
   tr->mark(TR_FWD);
   if (!grid_sync(A.C)) return false;
   tr->mark(TR_MID);
   const OsIO<T> g{yf, e, z};
   if (dot) {
-    if (!osweep<T, OS_BWD_DOT>(A.C, A.O, A.V, g, X, dot, tr)) return false;
+    if (!osweep<T, OS_BWD_DOT, WIDE>(A.C, A.O, A.V, g, X, dot, tr)) return false;
   } else {
-    if (!osweep<T, OS_BWD>(A.C, A.O, A.V, g, X, nullptr, tr)) return false;
+    if (!osweep<T, OS_BWD, WIDE>(A.C, A.O, A.V, g, X, nullptr, tr)) return false;
   }
   tr->mark(TR_BWD);
   return true;
@@ -207,16 +207,16 @@ __device__ __forceinline__ bool precond_apply(const KArgs<T>& A, OsCtx& X, const
 
 // DIC (DILU) factors d_i, inverted as in the reference
 // (linear_solvers.f90:439-445, :613-624); ends with a barrier
-template <class T, bool DILU>
+template <class T, bool DILU, bool WIDE>
 __device__ __forceinline__ bool precond_setup(const KArgs<T>& A, OsCtx& X) {
   const OsIO<T> io{nullptr, nullptr, A.d};
-  if (!osweep<T, DILU ? OS_SETUP_DILU : OS_SETUP_DIC>(A.C, A.O, A.V, io, X, nullptr)) return false;
+  if (!osweep<T, DILU ? OS_SETUP_DILU : OS_SETUP_DIC, WIDE>(A.C, A.O, A.V, io, X, nullptr)) return false;
   return grid_sync(A.C);
 }
 
 // ------------------------------------------------------------------ ICCG
 // iccg, linear_solvers.f90:364-545, in the schedule-ordered numbering
-template <class T, bool TRACE = false>
+template <class T, bool TRACE = false, bool WIDE = false>
 __global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_iccg(KArgs<T> A) {
   const int gt = vg_gt(A.C), G = vg_G(A.C), n = A.O.n;
   int ph = 0;
@@ -229,13 +229,13 @@ __global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_iccg(KArgs<T> A) {
   if (!ord_residual_l1(A, ph, res0)) return;
   if (res0 < A.tol_abs) { write_out(A, res0, res0, 0.0, 0.0, 0, 1); return; }
   if (!A.skip_setup)
-    if (!precond_setup<T, false>(A, X)) return;
+    if (!precond_setup<T, false, WIDE>(A, X)) return;
   tr.mark(TR_SETUP);
   double s0 = FC_S0, resl = 0.0, factor = 0.0, resor = 0.0;
   int itr_used = 0;
   for (int l = 1; l <= A.itr_max; ++l) {
     double rz[1] = {0.0};
-    if (!precond_apply(A, X, (const T*)r, yf, z, (const T*)r, rz, &tr)) return;
+    if (!precond_apply<T, WIDE>(A, X, (const T*)r, yf, z, (const T*)r, rz, &tr)) return;
     if (!grid_reduce<1>(A.C, ph, rz)) return;
     tr.mark(TR_DOT);
     const double sk = rz[0];
@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_iccg(KArgs<T> A) {
 // bicgstab, linear_solvers.f90:548-786, in the schedule-ordered numbering.
 // Runs on the blocks A.C names (the launch grid, or one problem's group of a
 // batched launch).
-template <class T>
+template <class T, bool WIDE>
 __device__ __forceinline__ void bicgstab_body(const KArgs<T>& A) {
   const int gt = vg_gt(A.C), G = vg_G(A.C), n = A.O.n;
   int ph = 0;
@@ -292,7 +292,7 @@ __device__ __forceinline__ void bicgstab_body(const KArgs<T>& A) {
   if (!ord_residual_l1(A, ph, res0)) return;
   if (res0 < A.tol_abs) { write_out(A, res0, res0, 0.0, 0.0, 0, 1); return; }
   if (!A.skip_setup)
-    if (!precond_setup<T, true>(A, X)) return;
+    if (!precond_setup<T, true, WIDE>(A, X)) return;
   double bb[1] = {0.0};
   for (int i = gt; i < n; i += G) {
     T ri = ldcg(r + i);
@@ -312,7 +312,7 @@ __device__ __forceinline__ void bicgstab_body(const KArgs<T>& A) {
     const T omT = (T)om, alfT = (T)alf;
     for (int i = gt; i < n; i += G) p[i] = ldcg(r + i) + omT * (ldcg(p + i) - alfT * ldcg(u + i));
     if (!grid_sync(A.C)) return;
-    if (!precond_apply(A, X, (const T*)p, yf, z, (const T*)nullptr, nullptr, &tr)) return;
+    if (!precond_apply<T, WIDE>(A, X, (const T*)p, yf, z, (const T*)nullptr, nullptr, &tr)) return;
     if (!grid_sync(A.C)) return;
     double ur[1] = {0.0};
     for (int i = gt; i < n; i += G) {
@@ -328,7 +328,7 @@ __device__ __forceinline__ void bicgstab_body(const KArgs<T>& A) {
       r[i] = ldcg(r + i) - gamT * ldcg(u + i);
     }
     if (!grid_sync(A.C)) return;
-    if (!precond_apply(A, X, (const T*)r, yf, z, (const T*)nullptr, nullptr, &tr)) return;
+    if (!precond_apply<T, WIDE>(A, X, (const T*)r, yf, z, (const T*)nullptr, nullptr, &tr)) return;
     if (!grid_sync(A.C)) return;
     double vr[2] = {0.0, 0.0};
     for (int i = gt; i < n; i += G) {
@@ -367,9 +367,9 @@ __device__ __forceinline__ void bicgstab_body(const KArgs<T>& A) {
   write_out(A, res0, resl, factor, resor, itr_used, 0);
 }
 
-template <class T>
+template <class T, bool WIDE = false>
 __global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_bicgstab(KArgs<T> A) {
-  bicgstab_body(A);
+  bicgstab_body<T, WIDE>(A);
 }
 
 // ------------------------------------------------------------------ DPCG
@@ -432,6 +432,7 @@ __global__ void __launch_bounds__(FC_BLOCK, 1) k_dpcg(KArgs<T> A) {
 // GaussSeidel, linear_solvers.f90:96-201: the in-place sweep as an ordered
 // forward sweep; entries left of the diagonal take this sweep's values
 // (xb), the diagonal and the entries right of it the previous sweep's (xa).
+template <bool WIDE = false>
 __global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_gauss_seidel(KArgs<double> A) {
   const int gt = vg_gt(A.C);
   int ph = 0;
@@ -444,7 +445,7 @@ __global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_gauss_seidel(KArgs<double
   for (int l = 1; l <= A.itr_max; ++l) {
     double red[2] = {0.0, 0.0};
     const OsIO<double> io{A.bo, xa, xb};
-    if (!osweep<double, OS_GS>(A.C, A.O, A.V, io, X, red)) return;
+    if (!osweep<double, OS_GS, WIDE>(A.C, A.O, A.V, io, X, red)) return;
     if (!grid_reduce<2>(A.C, ph, red)) return;
     double* t = xa; xa = xb; xb = t;
     if (l == 1) {
@@ -464,15 +465,15 @@ __global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_gauss_seidel(KArgs<double
 
 // preconditioner only: d (DIC or DILU) and optionally z = M^-1 q, q = A.b;
 // results in the original numbering: d into A.v, z into A.z
-template <class T, bool DILU>
+template <class T, bool DILU, bool WIDE = false>
 __global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1) k_precond(KArgs<T> A, int apply) {
   OsCtx X = osweep_ctx<T>(A.O, fc_smem, vg_bid(A.C));
   NoTracer tr(nullptr, 0);
   if (!ord_prologue(A, DILU, false)) return;
-  if (!precond_setup<T, DILU>(A, X)) return;
+  if (!precond_setup<T, DILU, WIDE>(A, X)) return;
   ord_scatter_vec(A.C, A.O, (const T*)A.d, A.v);
   if (!apply) return;
-  if (!precond_apply(A, X, (const T*)A.bo, A.u, A.w, (const T*)nullptr, nullptr, &tr)) return;
+  if (!precond_apply<T, WIDE>(A, X, (const T*)A.bo, A.u, A.w, (const T*)nullptr, nullptr, &tr)) return;
   if (!grid_sync(A.C)) return;
   ord_scatter_vec(A.C, A.O, (const T*)A.w, A.z);
 }
@@ -539,7 +540,7 @@ __device__ __forceinline__ KArgs<T>& batch_args(const KArgs<T>* __restrict__ arg
   return *reinterpret_cast<KArgs<T>*>(raw);
 }
 
-template <class T>
+template <class T, bool WIDE = false>
 __global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1)
     k_bicgstab_batch(const KArgs<T>* __restrict__ args, const int* __restrict__ bprob, const BatchCtl* __restrict__ ctl) {
   __shared__ __align__(16) unsigned char raw[sizeof(KArgs<T>)];
@@ -550,7 +551,7 @@ __global__ void __launch_bounds__(FC_SWEEP_BLOCK, 1)
   __syncthreads();
   if (threadIdx.x == 0) { A.skip_setup = ctl[p].skip_setup; A.itr_max = ctl[p].itr_max; }
   __syncthreads();
-  bicgstab_body(A);
+  bicgstab_body<T, WIDE>(A);
   if (vg_bid(A.C) == 0 && threadIdx.x == 0) A.C.out[FC_OUT_GT] = (double)(globaltimer_ns() - t0);
 }
 
@@ -705,6 +706,9 @@ static void ordered_blocks(const OrderedSweep& O, int& xmax, int& pmax) {
 // application stages took 222 ms per SIMPLE iteration, steps of 364 rows
 // with four 179 ms, despite 2,512 levels against 4,088).
 #define FC_APPLY_STAGES 4
+// fewest staged rows of a step for which wide levels are kept whole (below,
+// they are split into narrower steps)
+#define FC_MIN_STAGED_ROWS 64
 static int last_mode_of(bool with_gs) { return with_gs ? OS_GS : OS_BWD_DOT; }
 static bool staging_ok(size_t area, int maxW, int xmax, int pmax, bool with_gs) {
   if (ordered_min_stages(area, maxW, xmax, pmax, last_mode_of(with_gs)) < 2) return false;
@@ -734,18 +738,45 @@ static int estimated_step_cap(int R, int maxW, int max_tile_steps, bool with_gs)
   return 0;
 }
 
-static int upload_ordered(fc_ctx* ctx, const OrderedSweep& O, DevOrdered& D, bool with_gs) {
+// largest push block of the steps of at most w rows (the blocks that are staged)
+static int staged_push_max(const OrderedSweep& O, int w) {
+  int pmax = 4;
+  for (int d = 0; d < 2; ++d)
+    for (int gs = 0; gs < O.nsteps; ++gs)
+      if (O.step_ptr[gs + 1] - O.step_ptr[gs] <= w)
+        pmax = std::max(pmax, O.dir[d].push_ptr[gs + 1] - O.dir[d].push_ptr[gs]);
+  return pmax;
+}
+
+// The rows of a step the stage buffers hold when a wider step reads its
+// further rows, and its push block, from global memory: the largest multiple
+// of 32 (below maxW) whose staging is enough, with the ring at the full
+// width; 0 if none.
+static int staged_rows_fit(const OrderedSweep& O, bool with_gs) {
+  int xmax, pmax;
+  ordered_blocks(O, xmax, pmax);
+  const size_t area = ordered_stage_area(O.R, O.maxW, O.max_tile_steps);
+  for (int w = (O.maxW - 1) & ~31; w >= 32; w -= 32)
+    if (staging_ok(area, w, xmax, staged_push_max(O, w), with_gs)) return w;
+  return 0;
+}
+
+// Wc > 0: a step stages its first Wc rows (fewer than the widest step)
+static int upload_ordered(fc_ctx* ctx, const OrderedSweep& O, DevOrdered& D, bool with_gs, int Wc) {
   D.n = O.n; D.nE = O.nE; D.ntiles = O.ntiles; D.nsteps = O.nsteps; D.nlev = O.nlev; D.R = O.R; D.maxW = O.maxW;
   D.max_tile_steps = O.max_tile_steps;
   ordered_blocks(O, D.xmax, D.pmax);
+  D.Wc = Wc > 0 && Wc < D.maxW ? Wc : 0;
+  const int Ws = D.Wc > 0 ? D.Wc : D.maxW;
+  if (D.Wc > 0) D.pmax = staged_push_max(O, D.Wc);  // the push blocks the stage buffers hold
   D.stage_area = ordered_stage_area(D.R, D.maxW, D.max_tile_steps);
-  if (ordered_min_stages(D.stage_area, D.maxW, D.xmax, D.pmax, last_mode_of(with_gs)) < 2)
+  if (ordered_min_stages(D.stage_area, Ws, D.xmax, D.pmax, last_mode_of(with_gs)) < 2)
     return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "sweep tiles too wide for shared memory");
-  D.gs_ok = ordered_min_stages(D.stage_area, D.maxW, D.xmax, D.pmax, OS_GS) >= 2;
+  D.gs_ok = ordered_min_stages(D.stage_area, Ws, D.xmax, D.pmax, OS_GS) >= 2;
   {
-    // stages of the preconditioner application at the widest tile (sweep statistics)
+    // stages of the preconditioner application (sweep statistics)
     StageLayout L;
-    L.init_for<double>(D.maxW, D.xmax, D.pmax, OS_FWD);
+    L.init_for<double>(Ws, D.xmax, D.pmax, OS_FWD);
     D.K = stages_in(D.stage_area, L.bytes);
   }
   D.ring_entries = D.pushed_entries = D.cross_tile_entries = 0;
@@ -865,17 +896,37 @@ int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, c
   // estimated widest cap that fits, then at 7/8 of the previous cap, until
   // it does
   int wmax = ctx->sweep_cap > 0 ? ctx->sweep_cap : 0;
+  int wc = 0;  // rows a step stages when its further rows stay in global memory
   for (;;) {
     if (!build_ordered_sweep(n, ia.data(), ja.data(), dg.data(), ts.data(), tiles, xyz, FC_RING, O, S, err, wmax))
       return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, err);
+    if (ctx->stage_rows > 0 && ctx->stage_rows < O.maxW) {
+      // forced (tuning, tests), where every mode the solves use still gets
+      // two stage buffers
+      int xmax, pmax;
+      ordered_blocks(O, xmax, pmax);
+      const int w = ctx->stage_rows;
+      if (ordered_min_stages(ordered_stage_area(O.R, O.maxW, O.max_tile_steps), w, xmax, staged_push_max(O, w),
+                             last_mode_of(with_gs)) >= 2) {
+        wc = w;
+        break;
+      }
+    }
     if (ordered_fits(O, with_gs)) break;
+    if (wmax == 0) {
+      // wide levels kept whole: the stage buffers hold the first rows of a
+      // step, the others are read from global memory
+      wc = staged_rows_fit(O, with_gs);
+      if (wc >= FC_MIN_STAGED_ROWS) break;
+      wc = 0;
+    }
     const int est = wmax ? 0 : estimated_step_cap(FC_RING, O.maxW, O.max_tile_steps, with_gs);
     wmax = est > 0 ? est : (wmax ? (wmax * 7 / 8) & ~7 : std::max(32, O.maxW / 2));
     if (wmax < 32) return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "sweep steps too wide for shared memory");
   }
   s->t_schedule = since(t0);
   s->xyz_src = xyz;
-  int st2 = upload_ordered(ctx, O, s->ord, with_gs);
+  int st2 = upload_ordered(ctx, O, s->ord, with_gs, wc);
   if (st2) return st2;
   FC_CUDA_TRY(ctx, s->ia.alloc(n + 1));
   FC_CUDA_TRY(ctx, s->ja.alloc(nnz));
@@ -967,7 +1018,7 @@ static OrdView ord_view_of(CsrSystem* s) {
   OrdView O;
   O.n = D.n; O.nE = D.nE; O.ntiles = D.ntiles; O.R = D.R; O.stage_area = (int)D.stage_area;
   O.novf0 = D.novf[0]; O.novf1 = D.novf[1];
-  O.nsteps = D.nsteps; O.maxW = D.maxW; O.xmax = D.xmax; O.pmax = D.pmax;
+  O.nsteps = D.nsteps; O.maxW = D.maxW; O.xmax = D.xmax; O.pmax = D.pmax; O.Wc = D.Wc;
   O.tile_step_ptr = D.tile_step_ptr.p; O.step_ptr = D.step_ptr.p; O.tile_W = D.tile_W.p; O.perm = D.perm.p;
   for (int d = 0; d < 2; ++d) {
     O.srec[d] = (const int4*)D.srec[d].p; O.xv_ptr[d] = D.xv_ptr[d].p; O.push_ptr[d] = D.push_ptr[d].p;
@@ -1073,6 +1124,7 @@ static int solve_fp64(fc_ctx* ctx, CsrSystem* s, const std::string& solver, cons
   KArgs<double> A = make_args<double>(s, a, x, b, s->r.p, s->r0.p, s->p.p, s->u.p, s->z.p, s->v.p, s->d.p,
                                       s->w.p, itr_max, tol_abs, tol_rel);
   const bool traced = ctx->tracing && solver == "iccg";
+  const bool wide = s->ord.Wc > 0;  // steps wider than the stage buffers hold
   if (traced) {
     const int nb = std::max(1, ctx->num_sms);
     const int cap = s->ord.max_tile_steps + 1;
@@ -1086,13 +1138,19 @@ static int solve_fp64(fc_ctx* ctx, CsrSystem* s, const std::string& solver, cons
   FC_CUDA_TRY(ctx, cudaMemsetAsync(s->out.p, 0, FC_OUT_N * sizeof(double), ctx->stream));
   int st;
   if (solver == "iccg")
-    st = launch_coop(ctx, s, traced ? (const void*)k_iccg<double, true> : (const void*)k_iccg<double>, A, nullptr,
+    st = launch_coop(ctx, s,
+                     traced ? (wide ? (const void*)k_iccg<double, true, true> : (const void*)k_iccg<double, true>)
+                            : wide ? (const void*)k_iccg<double, false, true> : (const void*)k_iccg<double>,
+                     A, nullptr,
                      0);
   else if (solver == "bicgstab") {
     if (s->tslot_oob) return fc_fail_msg(ctx, FC_ERR_BAD_INPUT, "bicgstab: pattern is not structurally symmetric");
-    st = launch_coop(ctx, s, (const void*)k_bicgstab<double>, A, nullptr, 0);
+    st = launch_coop(ctx, s, wide ? (const void*)k_bicgstab<double, true> : (const void*)k_bicgstab<double>, A,
+                     nullptr, 0);
   } else if (solver == "dpcg") st = launch_coop(ctx, s, (const void*)k_dpcg<double>, A, nullptr, 0, FC_BLOCK);
-  else if (solver == "gauss-seidel") st = launch_coop(ctx, s, (const void*)k_gauss_seidel, A, nullptr, 0);
+  else if (solver == "gauss-seidel")
+    st = launch_coop(ctx, s, wide ? (const void*)k_gauss_seidel<true> : (const void*)k_gauss_seidel<false>, A,
+                     nullptr, 0);
   else return fc_fail_msg(ctx, FC_ERR_UNSUPPORTED, "unknown solver '" + solver + "'");
   if (st) return st;
   return fetch_out(ctx, s, res);
@@ -1172,8 +1230,10 @@ static int solve_mixed(fc_ctx* ctx, CsrSystem* s, const std::string& solver, con
                                       0.0, inner_tol);
     F.skip_setup = outer > 0 ? 1 : 0;
     if (solver == "bicgstab") F.stall_window = FC_INNER_STALL_WINDOW;
-    const void* fn = solver == "iccg" ? (const void*)k_iccg<float>
-                     : solver == "bicgstab" ? (const void*)k_bicgstab<float> : (const void*)k_dpcg<float>;
+    const bool wide = s->ord.Wc > 0;
+    const void* fn = solver == "iccg" ? (wide ? (const void*)k_iccg<float, false, true> : (const void*)k_iccg<float>)
+                     : solver == "bicgstab" ? (wide ? (const void*)k_bicgstab<float, true> : (const void*)k_bicgstab<float>)
+                                            : (const void*)k_dpcg<float>;
     if ((st = launch_coop(ctx, s, fn, F, nullptr, 0, solver == "dpcg" ? FC_BLOCK : FC_SWEEP_BLOCK))) return st;
     FC_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_out, s->out.p, FC_OUT_N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     FC_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_status, s->status.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1328,6 +1388,13 @@ static size_t batch_smem(const std::vector<BatchItem>& items) {
   return m;
 }
 
+// some problem of the batch has steps wider than its stage buffers hold
+static bool batch_wide(const std::vector<BatchItem>& items) {
+  for (const BatchItem& it : items)
+    if (it.s->ord.Wc > 0) return true;
+  return false;
+}
+
 int batch_solve(fc_ctx* ctx, BatchDev*& dev, std::vector<BatchItem>& items, const char* solver_c, int itr_max,
                 double tol_abs, double tol_rel) {
   const std::string solver(solver_c ? solver_c : "");
@@ -1363,7 +1430,9 @@ int batch_solve(fc_ctx* ctx, BatchDev*& dev, std::vector<BatchItem>& items, cons
     int* pb = B.bprob.p;
     BatchCtl* pc = B.ctl.p;
     void* args[3] = {&pa, &pb, &pc};
-    if ((st = batch_launch(ctx, B, (const void*)k_bicgstab_batch<double>, args, batch_smem<double>(items)))) return st;
+    const void* fn64 = batch_wide(items) ? (const void*)k_bicgstab_batch<double, true>
+                                         : (const void*)k_bicgstab_batch<double>;
+    if ((st = batch_launch(ctx, B, fn64, args, batch_smem<double>(items)))) return st;
     if ((st = batch_fetch(ctx, B))) return st;
     for (int p = 0; p < np; ++p) {
       const double* o = B.h_out + (size_t)p * FC_OUT_N;
@@ -1457,7 +1526,9 @@ int batch_solve(fc_ctx* ctx, BatchDev*& dev, std::vector<BatchItem>& items, cons
       }
       if ((st = batch_put_ctl(ctx, B))) return st;
       void* fa[3] = {&pf, &pb, &pc};
-      if ((st = batch_launch(ctx, B, (const void*)k_bicgstab_batch<float>, fa, smemf))) return st;
+      const void* fn32 = batch_wide(items) ? (const void*)k_bicgstab_batch<float, true>
+                                           : (const void*)k_bicgstab_batch<float>;
+      if ((st = batch_launch(ctx, B, fn32, fa, smemf))) return st;
       if ((st = batch_fetch(ctx, B))) return st;
       for (int p = 0; p < np; ++p) {
         PState& q = ps[p];
@@ -1484,8 +1555,10 @@ int sys_precond(fc_ctx* ctx, CsrSystem* s, int dilu, const double* q, double* z_
   KArgs<double> A = make_args<double>(s, s->a.p, s->x.p, q, s->r.p, s->r0.p, s->p.p, s->u.p, s->z.p, s->v.p, s->d.p,
                                       s->w.p, 0, 0.0, 0.0);
   void* extra[1] = {&apply};
-  int st = dilu ? launch_coop(ctx, s, (const void*)k_precond<double, true>, A, extra, 1)
-                : launch_coop(ctx, s, (const void*)k_precond<double, false>, A, extra, 1);
+  const bool wide = s->ord.Wc > 0;
+  const void* fn = dilu ? (wide ? (const void*)k_precond<double, true, true> : (const void*)k_precond<double, true>)
+                        : (wide ? (const void*)k_precond<double, false, true> : (const void*)k_precond<double, false>);
+  int st = launch_coop(ctx, s, fn, A, extra, 1);
   if (st) return st;
   FC_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_status, s->status.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   if (d_out) FC_CUDA_TRY(ctx, cudaMemcpyAsync(d_out, s->v.p, s->n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));

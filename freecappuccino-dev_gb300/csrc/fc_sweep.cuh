@@ -33,6 +33,7 @@
 // store arrives.  The consumer puts the sentinel back after use.  Bulk
 // copies read through L2, so staged data is never an SM's stale L1 line.
 #pragma once
+#include <type_traits>
 #include "fc_krylov.cuh"
 #include "fc_schedule.hpp"
 
@@ -92,6 +93,10 @@ template <class T> struct Rec { static constexpr int V = sizeof(T) == 8 ? 6 : 8;
 struct OrdView {
   int n, nE, ntiles, R, novf0, novf1, nsteps, maxW, xmax, pmax;
   int stage_area;                        // bytes of the stage area (multiple of 16)
+  // rows of a step that are staged in shared memory: the rows of a wider
+  // step past the first Wc read their records from global memory, and the
+  // step's push block is read from global memory too (0: every step fits)
+  int Wc;
   const int* __restrict__ tile_step_ptr;
   const int* __restrict__ step_ptr;
   const int* __restrict__ tile_W;
@@ -285,12 +290,14 @@ __device__ __noinline__ T xv_wait(const GridCtl& C, const T* p, int* abort_flag)
   return v;
 }
 
-// One ordered sweep of tile vg_bid(C).  dirn 0: forward over the lower
+// One ordered sweep of tile vg_bid(C).  WIDE: the structure has steps wider
+// than the stage buffers hold (OrdView::Wc > 0), whose further rows read
+// their records from global memory; without it the staged path is all there is.  dirn 0: forward over the lower
 // triangle, 1: backward over the upper one.  red (MODE OS_BWD_DOT: red[0] +=
 // e*value; OS_GS: red[0] += |residual|, red[1] += |a_ii x_i|) accumulates
 // per thread.  Every thread of the block calls it; it ends with a block
 // barrier but no grid barrier, and returns false if a wait ran out.
-template <class T, int MODE, class TracerT = NoTrace>
+template <class T, int MODE, bool WIDE = false, class TracerT = NoTrace>
 __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const OrdVals<T>& V, const OsIO<T>& io, OsCtx& X,
                        double* red, TracerT* tr = nullptr) {
   constexpr int dirn = (MODE == OS_BWD || MODE == OS_BWD_DOT) ? 1 : 0;
@@ -304,9 +311,12 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
   if (t >= O.ntiles) return true;
   const int ns = __ldg(O.tile_step_ptr + t + 1) - __ldg(O.tile_step_ptr + t);
   // the areas this mode reads, as many stage buffers as the area holds
+  // W: the tile's widest step (ring stride, compute threads); Ws: the rows of
+  // a step the stage buffers hold
+  const int W = X.L.W, Ws = WIDE && O.Wc > 0 ? min(W, O.Wc) : W;
   StageLayout L;
-  L.template init_for<T>(X.L.W, O.xmax, O.pmax, MODE);
-  const int K = stages_in(X.stage_area, L.bytes), R = O.R, W = L.W;
+  L.template init_for<T>(Ws, O.xmax, O.pmax, MODE);
+  const int K = stages_in(X.stage_area, L.bytes), R = O.R;
   const int nct = (int)blockDim.x - 32;  // threads before the staging warp
   // compute threads of this tile: whole warps covering its widest step
   const int ncg = min(nct, (W + 31) & ~31);
@@ -336,9 +346,9 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
         }
         if (tr) tr->staged(k);
         const int ls = step_of(k);
-        const int base = sp[ls], cnt = sp[ls + 1] - base;
+        const int base = sp[ls], cnt = WIDE ? min(sp[ls + 1] - base, Ws) : sp[ls + 1] - base;  // the staged rows
         const int b0 = base & ~3, nw = ((base + cnt + 3) & ~3) - b0;
-        const int p0 = pp[ls], np = pp[ls + 1] - p0;
+        const int p0 = pp[ls], np = !WIDE || sp[ls + 1] - base <= Ws ? pp[ls + 1] - p0 : 0;
         unsigned char* B = X.stage + (size_t)b * L.bytes;
         unsigned long long* mb = X.full + b;
         const unsigned vb = (unsigned)(sizeof(T) * VR) * cnt;
@@ -389,7 +399,9 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
       }
       pre_waited = true;
       if ((int)threadIdx.x >= cntk) return;
-      const int4 sr = ((const int4*)(X.stage + (size_t)bk * L.bytes + L.oS))[threadIdx.x];
+      const int4 sr = !WIDE || (int)threadIdx.x < Ws
+                          ? ((const int4*)(X.stage + (size_t)bk * L.bytes + L.oS))[threadIdx.x]
+                          : __ldg(O.srec[dirn] + basek + threadIdx.x);
       const int ne = sr.x & 255, xoff = (int)((unsigned)sr.x >> 16);
       const unsigned cw[2] = {(unsigned)sr.z, (unsigned)sr.w};
       const T* src = xv + xp[lsk] + xoff;
@@ -427,13 +439,22 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
       const unsigned char* B = X.stage + (size_t)b * L.bytes;
       const int4* S4 = (const int4*)(B + L.oS);
       const T* VRc = (const T*)(B + L.oV);
-      const int* PS = (const int*)(B + L.oP);
+      // the push block: staged for a step the stage buffer holds whole, else
+      // read from global memory
+      const int* PS = !WIDE || cnt <= Ws ? (const int*)(B + L.oP) : O.push[dirn] + pp[ls];
       T* ring_out = ring + (k & (R - 1)) * W;
-      for (int sl = threadIdx.x; sl < cnt; sl += ncg) {
+      // one row of the step; STG: its records are in the stage buffer, else
+      // (the rows of a wider step past the staged ones) in global memory
+      auto row = [&](const int sl, auto stg_tag) {
+        constexpr bool STG = decltype(stg_tag)::value;
         const int q = base + sl;
-        const int4 sr = S4[sl];
+        const int4 sr = STG ? S4[sl] : __ldg(O.srec[dirn] + q);
         const int ne = sr.x & 255, np = (sr.x >> 8) & 255, xoff = (int)((unsigned)sr.x >> 16), poff = sr.y;
-        const T* vr = VRc + sl * VR;
+        T vl[VR];  // an unstaged row's coefficient record
+        if constexpr (!STG)
+#pragma unroll
+          for (int e = 0; e < VR; ++e) vl[e] = ldcg(V.vrec[dirn] + (size_t)q * VR + e);
+        const T* vr = STG ? VRc + sl * VR : vl;
         // dependency values of entries 0..3 without branches: entries past
         // ne have code 0 and coefficient 0, so they contribute an exact
         // zero; ring (code > 0) or exchanged value (code 0) by select.  The
@@ -484,7 +505,11 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
         if (kSetup) {
           // d_i = a_ii - sum a_k^2 d_j (DIC) or a_k d_j a_(j,i) (DILU), then 1/d_i
           // (the recurrence is exact, so entries past ne are skipped)
-          const T* sx = (const T*)(B + L.oX2) + sl * VR;
+          T sl_x[VR];
+          if constexpr (!STG)
+#pragma unroll
+            for (int e = 0; e < VR; ++e) sl_x[e] = ldcg(V.sx + (size_t)q * VR + e);
+          const T* sx = STG ? (const T*)(B + L.oX2) + sl * VR : sl_x;
           T di = sx[0];
 #pragma unroll
           for (int e = 0; e < FC_ELL; ++e)
@@ -508,7 +533,7 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
         } else if (kGS) {
           // s = b - sum_{k<kd} a x_new - a_ii x_old_i - sum_{k>kd} a x_old;
           // x_i = x_old_i + s / (a_ii + small)   (exact arithmetic)
-          T s = ((const T*)(B + L.oQ))[woff + sl];
+          T s = STG ? ((const T*)(B + L.oQ))[woff + sl] : ldcg(io.q + q);
 #pragma unroll
           for (int e = 0; e < FC_ELL; ++e)
             if (e < ne) s = sub_rn(s, mul_rn(vr[e], dv[e]));
@@ -517,12 +542,16 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
             const T xj = dep_ovf(e, a);
             s = sub_rn(s, mul_rn(a, xj));
           }
-          const T aii = ((const T*)(B + L.oX2))[sl * VR];
-          const T xo = ((const T*)(B + L.oE))[woff + sl];
+          const T aii = STG ? ((const T*)(B + L.oX2))[sl * VR] : ldcg(V.sx + (size_t)q * VR);
+          const T xo = STG ? ((const T*)(B + L.oE))[woff + sl] : ldcg(io.e + q);
           s = sub_rn(s, mul_rn(aii, xo));
           const int nu = __ldg(&O.srec[1][q].x) & 255;
-          const T* v2 = (const T*)(B + L.oV2) + sl * VR;
-          const int4 uc = ((const int4*)(B + L.oU))[sl];
+          T v2l[VR];
+          if constexpr (!STG)
+#pragma unroll
+            for (int e = 0; e < VR; ++e) v2l[e] = ldcg(V.vrec[1] + (size_t)q * VR + e);
+          const T* v2 = STG ? (const T*)(B + L.oV2) + sl * VR : v2l;
+          const int4 uc = STG ? ((const int4*)(B + L.oU))[sl] : __ldg(O.ucol + q);
 #pragma unroll
           for (int e = 0; e < FC_ELL; ++e)
             if (e < nu) {
@@ -543,7 +572,7 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
           // 0..2 unconditionally (padding adds exactly zero), entry 3 when
           // present.
           const T di = vr[4];
-          T acc = ((const T*)(B + L.oQ))[woff + sl];
+          T acc = STG ? ((const T*)(B + L.oQ))[woff + sl] : ldcg(io.q + q);
           if (dirn) acc = acc * vr[5];
           acc = fma(-vr[0], dv[0], acc);
           acc = fma(-vr[1], dv[1], acc);
@@ -555,7 +584,8 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
             acc = fma(-a, v, acc);
           }
           val = acc * di;
-          if (MODE == OS_BWD_DOT) red[0] += (double)((const T*)(B + L.oE))[woff + sl] * (double)val;
+          if (MODE == OS_BWD_DOT)
+            red[0] += (double)(STG ? ((const T*)(B + L.oE))[woff + sl] : ldcg(io.e + q)) * (double)val;
         }
         if (tr && sl == 0) tr->at(k, 6, __double_as_longlong((double)val));
         io.out[q] = val;
@@ -564,6 +594,14 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
         // atomic, so a consumer polling the slot sees the sentinel or the value
         for (int mm = 0; mm < np; ++mm) xv[PS[poff + mm]] = val;
         if (tr && sl == 0) tr->at(k, 7, np);
+      };
+      for (int sl = threadIdx.x; sl < cnt; sl += ncg) {
+        if constexpr (WIDE) {
+          if (sl < Ws) row(sl, std::true_type{});
+          else row(sl, std::false_type{});
+        } else {
+          row(sl, std::true_type{});
+        }
       }
       bar_compute(ncg);
       if (threadIdx.x == 0) mbar_arrive(X.empty + b);

@@ -120,6 +120,7 @@ def lib():
         "fc_mixed_colours": (i, [vp, i, vp]),
         "fc_set_sweep_cap": (i, [vp, i]),
         "fc_set_sweep_tiles": (i, [vp, i]),
+        "fc_set_sweep_stage_rows": (i, [vp, i]),
         "fc_set_tracing": (i, [vp, i]),
         "fc_trace_get": (i, [vp, vp, vp]),
         "fc_init_flmass": (i, [vp]),
@@ -668,11 +669,15 @@ class Context:
         return float(r0[0]), info, st
 
     def sweep_stats(self, which=0):
-        out = np.zeros(10)
+        out = np.zeros(11)
         self._check(self.L.fc_sweep_stats(self.h, which, _ptr(out)), "fc_sweep_stats")
         keys = ("tiles", "levels", "max_width", "ring_depth", "est_sweep_us", "ring_entries", "pushed_entries",
-                "cross_tile_entries", "stages", "max_tile_steps")
+                "cross_tile_entries", "stages", "max_tile_steps", "staged_rows")
         return dict(zip(keys, [float(v) for v in out]))
+
+    def set_sweep_stage_rows(self, rows):
+        """Rows of a step held in the stage buffers in the pattern analyses that follow (0: the default)."""
+        self._check(self.L.fc_set_sweep_stage_rows(self.h, int(rows)), "fc_set_sweep_stage_rows")
 
     def set_sweep_tiles(self, tiles):
         """Tile count of the pattern analyses that follow (0: the default)."""

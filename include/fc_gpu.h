@@ -194,10 +194,12 @@ int fc_precond_apply(fc_ctx* ctx, const char* kind, int n, int nnz, const int* i
 int fc_spmv(fc_ctx* ctx, int n, int nnz, const int* ia, const int* ja, const double* a, const int* diag,
             const double* x, double* y, int transpose);
 /* Statistics of the schedule-ordered sweep structure of the mesh system
- * (which=0) or of the cached fc_csrsolve pattern (which=1): out[10] = tiles,
+ * (which=0) or of the cached fc_csrsolve pattern (which=1): out[11] = tiles,
  * levels, widest step of a tile, ring depth, estimated forward-sweep us,
  * ring-served entries, pushed entries, cross-tile entries (both triangles),
- * stage depth, most steps of a tile. */
+ * stage depth, most steps of a tile, rows of a step held in the stage
+ * buffers (0: whole steps; the further rows of a wider step are read from
+ * global memory). */
 int fc_sweep_stats(fc_ctx* ctx, int which, double* out);
 /* Caps the rows of a sweep step in the pattern analyses that follow (rows
  * >= 1; 0 restores the default, as wide as shared memory allows).  A level
@@ -212,6 +214,12 @@ int fc_set_sweep_cap(fc_ctx* ctx, int rows);
  * preconditioner and the iterates do not depend on it.  Tuning and testing
  * only: no counterpart in the reference. */
 int fc_set_sweep_tiles(fc_ctx* ctx, int tiles);
+/* Sets the rows of a step that the stage buffers hold in the pattern
+ * analyses that follow (0 restores the default: whole steps where they fit,
+ * else as many rows as fit); the further rows of a wider step read their
+ * records from global memory.  Results do not depend on it.  Tuning and
+ * testing only: no counterpart in the reference. */
+int fc_set_sweep_stage_rows(fc_ctx* ctx, int rows);
 /* Appends one JSON line per solve to the file at path (NULL or "": stop):
  * the entry point, solver, variable, rows, precision mode, status,
  * iterations, refinement steps, early exit, res0 (L1), final residual,

@@ -875,6 +875,10 @@ int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, c
   auto since = [](std::chrono::steady_clock::time_point a) {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
   };
+  // systems whose tiles the caller plans (the batched solves) split wide
+  // levels into steps, as their tile planner assumes; the others keep them
+  // whole with staged rows (below)
+  const bool planned_tiles = tiles_req > 0;
   if (tiles_req <= 0 && ctx->sweep_tiles > 0) tiles_req = ctx->sweep_tiles;
   if (tiles_req > 0) {
     tiles = std::min(tiles_req, sms);
@@ -913,7 +917,7 @@ int sys_set_pattern(fc_ctx* ctx, CsrSystem* s, int n, int nnz, const int* ia1, c
       }
     }
     if (ordered_fits(O, with_gs)) break;
-    if (wmax == 0) {
+    if (wmax == 0 && !planned_tiles) {
       // wide levels kept whole: the stage buffers hold the first rows of a
       // step, the others are read from global memory
       wc = staged_rows_fit(O, with_gs);

@@ -202,10 +202,12 @@ int fc_spmv(fc_ctx* ctx, int n, int nnz, const int* ia, const int* ja, const dou
  * global memory). */
 int fc_sweep_stats(fc_ctx* ctx, int which, double* out);
 /* Caps the rows of a sweep step in the pattern analyses that follow (rows
- * >= 1; 0 restores the default, as wide as shared memory allows).  A level
- * of a tile wider than the cap is split into consecutive steps; the
- * preconditioner is unchanged.  The analysis applies the split by itself when
- * a mesh's widest step does not fit (e.g. 6 million tetrahedra).  Tuning and
+ * >= 1; 0 restores the default).  A level of a tile wider than the cap is
+ * split into consecutive steps; the preconditioner is unchanged.  By default
+ * a level too wide for the shared-memory staging (e.g. on 6 million
+ * tetrahedra) stays one step whose first rows are staged (see
+ * fc_set_sweep_stage_rows), and the analysis splits levels by itself only
+ * for batched systems or when too few rows would be staged.  Tuning and
  * testing only: no counterpart in the reference. */
 int fc_set_sweep_cap(fc_ctx* ctx, int rows);
 /* Sets the tile count (thread blocks of the ordered sweeps, at most one per

@@ -81,6 +81,11 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* mb, unsigned parit
   }
   return true;
 }
+// a hint to bring the line holding p into L2 (prefetch.global.L2)
+__device__ __forceinline__ void l2_prefetch(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // barrier among the first nthreads threads (the compute warps)
 __device__ __forceinline__ void bar_compute(int nthreads) {
   asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
@@ -434,6 +439,28 @@ __device__ __forceinline__ bool osweep(const GridCtl& C, const OrdView& O, const
       // the next step's exchanged values are loaded while this one runs
       if (k + 1 < ns) prefetch(k + 1);
       else { pf_ok = false; pre_waited = false; }
+      if constexpr (WIDE) {
+        // the records of this thread's unstaged rows of the next step are
+        // brought into L2 while this step runs (they are read through L2)
+        if (k + 1 < ns) {
+          const int lsn = step_of(k + 1), basen = sp[lsn], cntn = sp[lsn + 1] - basen;
+          for (int sl = threadIdx.x; sl < cntn; sl += ncg) {
+            if (sl < Ws) continue;
+            const int qn = basen + sl;
+            l2_prefetch(O.srec[dirn] + qn);
+            l2_prefetch(V.vrec[dirn] + (size_t)qn * VR);
+            l2_prefetch(V.vrec[dirn] + (size_t)qn * VR + VR - 1);
+            if (kQ) l2_prefetch(io.q + qn);
+            if (kE) l2_prefetch(io.e + qn);
+          }
+          // a wide step's push block, read from global memory, line by line
+          if (cntn > Ws) {
+            const int* pb = O.push[dirn] + pp[lsn];
+            const int npn = pp[lsn + 1] - pp[lsn];
+            for (int o = (int)threadIdx.x * 32; o < npn; o += ncg * 32) l2_prefetch(pb + o);
+          }
+        }
+      }
       if (tr) tr->at(k, 4, (int)pf_ok);
       const int xbase = xp[ls];
       const unsigned char* B = X.stage + (size_t)b * L.bytes;

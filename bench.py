@@ -488,7 +488,7 @@ def batch_solves(count=64, mixed=False, dev=0):
 
 
 def adjoint_solves(n=96, calls=2, dev=0):
-    """`calls` rounds of the C4 adjoint on the n^3 mesh: assembly
+    """`calls` passes of the C4 adjoint on the n^3 mesh: assembly
     (fc_cd_assemble), the forward BiCGStab(DILU) solve, the objective and the
     adjoint (transposed solve and reverse face loop): the command of the
     adjoint kernels' launch list and ncu captures, e.g.
